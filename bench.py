@@ -1,0 +1,355 @@
+"""Benchmark of the batched 2D pair-HMM E-step on GB300.
+
+Default workload: MixDom2 with n_dom=3, n_frag=1, n_classes=1 (17 states),
+200 pairs with ancestor lengths LogUniform(30, 600), per-pair t, forward +
+backward + expected counts -- one E-step over the batch per step (synthetic
+data, seed 0 + rank).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+metric: cell-state updates per second of the E-step, where one E-step over a
+pair counts (Lx+1)(Ly+1)*N cell-state updates (real lengths, no padding).
+`value` times the persistent batched launch with inputs resident in HBM;
+`e2e` times the public API call (pairhmm.api.estep_batch_mixdom2) from host
+sequences to host results, host<->device copies included.  L2 is flushed
+(256 MiB write) between timed steps.  Multi-GPU runs are independent
+replicas (pairs are independent; no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, 'tkf-mixdom_gb300')
+for _p in (ROOT, PKG_DIR):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+WORKLOAD = 'mixdom2_k3f1c1_200pairs_len30-600'
+PROFILE_SUMMARY = os.path.join(ROOT, 'profiles', 'estep_kernels_mixdom2_k3f1c1.md')
+SMS = 152
+FP32_LANES_PER_SM = 128
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--workload', default=WORKLOAD)
+    ap.add_argument('--no-plain', action='store_true')
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--pairs', type=int, default=0,
+                    help='use only the first P pairs (small case for ncu captures)')
+    ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return ws, rank, local
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            return json.load(f), 'measured'
+    except OSError:
+        return {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0, 'sm_max_mhz': 2070.0}, 'fallback'
+
+
+def profile_traffic():
+    """dram bytes per launch of the dominant kernel from the committed ncu summary."""
+    try:
+        for line in open(PROFILE_SUMMARY):
+            if line.startswith('traffic_bytes_per_launch_full_workload:'):
+                return float(line.split(':', 1)[1].split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', f'--id={self.gpu_id}', f'--query-gpu={self.Q}',
+                 '--format=csv,noheader,nounits', '-lms', '100'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.6)
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in out.strip().splitlines():
+            f = [v.strip() for v in line.split(',')]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith('active'):
+                    reasons.add(n)
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': mx,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def cpu_baseline(workload, seconds, threads=1):
+    """The FP64 oracle on a bounded sample of the same pairs (host cores)."""
+    from oracle import models as om, dp as odp, estep as oe
+    p = workload.params
+    done_cells = 0
+    t0 = time.perf_counter()
+    order = np.argsort(workload.cells())
+    n = 0
+    for b in order:
+        x, y, t = workload.xs[b], workload.ys[b], float(workload.ts[b])
+        pb = dict(p)
+        pb['t'] = t
+        chi, st, groups, EM, EI, ED, _ = oe.mixdom2_model(pb)
+        emit = odp.log_emission_table(st, groups, x, y, EM, EI, ED)
+        odp.forward_backward(om.safe_log(chi), st, emit)
+        done_cells += (len(x) + 1) * (len(y) + 1)
+        n += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    el = time.perf_counter() - t0
+    N = workload.n_states
+    return {'value': done_cells * N / el, 'unit': 'cell-state updates/s', 'cores': threads,
+            'kind': 'port',
+            'sample': f'{n} smallest pairs of the workload ({done_cells} cells), FP64 NumPy oracle '
+                      f'forward+backward+counts, {el:.1f} s'}
+
+
+def _ref_worker(args):
+    import numpy as _np
+    sys.path[:0] = [ROOT, PKG_DIR]
+    from oracle import models as om, dp as odp, estep as oe
+    p, x, y = args
+    chi, st, groups, EM, EI, ED, _ = oe.mixdom2_model(p)
+    emit = odp.log_emission_table(st, groups, x, y, EM, EI, ED)
+    odp.forward_backward(om.safe_log(chi), st, emit)
+    return (len(x) + 1) * (len(y) + 1)
+
+
+def run_reference(args, rank, ws):
+    """CPU arm: the reference's algorithm (FP64 restatement) on all host cores."""
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from pairhmm import synth
+    w = synth.CONFIGS[args.workload](seed=0)
+    cores = len(os.sched_getaffinity(0))
+    order = np.argsort(w.cells())
+    # bounded sample: the smallest pairs up to ~2e5 cells per step
+    sample, cells = [], 0
+    for b in order:
+        pb = dict(w.params)
+        pb['t'] = float(w.ts[b])
+        sample.append((pb, w.xs[b], w.ys[b]))
+        cells += w.cells()[b]
+        if cells > 2.0e5 * max(1, cores // 4):
+            break
+    ctx = mp.get_context('spawn')
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_ref_worker, sample[:cores])
+        t0 = time.perf_counter()
+        tot = 0
+        for _ in range(args.steps):
+            tot += sum(pool.map(_ref_worker, sample))
+        el = time.perf_counter() - t0
+    N = w.n_states
+    val = tot * N / el
+    line = {'metric': 'pair-HMM E-step cell-state updates/s', 'value': val, 'unit': 'cell-state updates/s',
+            'impl': 'reference', 'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': el / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': args.workload, 'sample_pairs': len(sample), 'sample_cells': int(cells),
+                       'note': 'reference is JAX-only (not installable here); its algorithm is run '
+                               'as the FP64 NumPy restatement in oracle/'},
+            'cpu_baseline': {'value': val, 'unit': 'cell-state updates/s', 'cores': cores, 'kind': 'port',
+                             'sample': f'{len(sample)} smallest pairs, {int(cells)} cells per step'},
+            'e2e': {'value': val, 'unit': 'cell-state updates/s', 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse_args()
+    ws, rank, local = dist_setup(args)
+    if args.impl == 'reference':
+        return run_reference(args, rank, ws)
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group('nccl', device_id=torch.device('cuda', local))
+    from pairhmm import synth, api, _lib
+    from pairhmm import models as pm
+    dev = torch.device('cuda', local)
+    w = synth.CONFIGS[args.workload](seed=rank)
+    if args.pairs:
+        w.xs, w.ys, w.ts = w.xs[:args.pairs], w.ys[:args.pairs], w.ts[:args.pairs]
+    N = w.n_states
+    cells = w.cells()
+    cell_states = float((cells * N).sum())
+    # ---- inputs resident in HBM
+    K, F, chi, csubs, EM, EI, ED = api._mixdom2_tables(w.params, w.ts, dev)
+    plan = api.get_plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)
+    batch = _lib.make_batch(w.xs, w.ys, chi, EM, EI, ED, device=dev)
+    plan.set_timing(True)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    out = None
+    for _ in range(max(3, args.warmup)):
+        out = _lib.estep(plan, batch, out=out)
+    torch.cuda.synchronize()
+    status = out['status'].cpu().numpy()
+    try:
+        gid = str(torch.cuda.get_device_properties(dev).uuid)
+        gid = gid if gid.startswith('GPU-') else f'GPU-{gid}'
+    except Exception:
+        gid = str(local)
+    sampler = ClockSampler(gid)
+    sampler.start()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_ms, fwd_ms, bwd_ms = [], [], []
+    for k in range(args.steps):
+        flush.fill_(k & 0xff)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = _lib.estep(plan, batch, out=out)
+        e1.record(stream)
+        a, b = plan.kernel_times()
+        fwd_ms.append(a)
+        bwd_ms.append(b)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    clocks = sampler.stop()
+    total_ms = float(np.sum(step_ms))
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = cell_states * ws * args.steps / (total_ms / 1e3)
+    ms_step = total_ms / args.steps
+    # ---- end to end through the public API (host sequences -> host results)
+    e2e_ms = []
+    h2d = int(sum(len(x) + len(y) for x, y in zip(w.xs, w.ys)) + 8 * len(w.ts))
+    d2h = 0
+    for k in range(0 if args.no_e2e else args.warmup + args.steps):
+        flush.fill_(k & 0xff)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = api.estep_batch_mixdom2(w.params, w.xs, w.ys, w.ts)
+        host = {kk: v.cpu().numpy() for kk, v in r.items()}
+        t1 = time.perf_counter()
+        if k >= args.warmup:
+            e2e_ms.append((t1 - t0) * 1e3)
+        d2h = int(sum(v.nbytes for v in host.values()))
+    e2e_total = float(np.sum(e2e_ms)) if e2e_ms else float('nan')
+    if ws > 1:
+        t = torch.tensor([e2e_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = cell_states * ws * args.steps / (e2e_total / 1e3)
+    # ---- plain: one launch sequence per pair (the single-pair path)
+    plain = None
+    if not args.no_plain and rank == 0:
+        subs = []
+        for b in range(len(w.xs)):
+            subs.append(_lib.make_batch([w.xs[b]], [w.ys[b]], chi[b:b + 1], EM[b:b + 1],
+                                        EI[b:b + 1], ED[b:b + 1], device=dev))
+        plan.set_timing(False)
+        for sb in subs[:3]:
+            _lib.estep(plan, sb)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for sb in subs:
+            _lib.estep(plan, sb)
+        e1.record(stream)
+        e1.synchronize()
+        pms = e0.elapsed_time(e1)
+        plain = {'value': cell_states / (pms / 1e3), 'ms_per_step': pms,
+                 'pairs_per_s': len(w.xs) / (pms / 1e3),
+                 'note': 'same pairs, one phmm_estep call (forward + backward launch) per pair'}
+    # ---- roofline of the dominant kernel
+    peaks, src = measured_peaks()
+    fwd_avg, bwd_avg = float(np.mean(fwd_ms)), float(np.mean(bwd_ms))
+    total_cells = float(cells.sum())
+    dom = 'backward_kernel' if bwd_avg >= fwd_avg else 'forward_kernel'
+    flop = (4.0 if dom == 'backward_kernel' else 2.0) * N * N * total_cells
+    dur = bwd_avg if dom == 'backward_kernel' else fwd_avg
+    achieved = flop / (dur / 1e3) / 1e12
+    fp32_peak = SMS * FP32_LANES_PER_SM * 2 * peaks.get('sm_max_mhz', 2070.0) * 1e6 / 1e12
+    roofline = {'bound': 'fp32', 'kernel': dom, 'achieved': achieved, 'peak': fp32_peak,
+                'unit': 'TFLOP/s', 'frac': achieved / fp32_peak,
+                'traffic': profile_traffic(),
+                'peak_source': f'{SMS} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 FLOP x sm_max_mhz '
+                               f'({peaks.get("sm_max_mhz")} MHz, {src} MEASURED_PEAKS.json); '
+                               'the DP has no tensor-core or HBM bound (see DESIGN.md)',
+                'flop_per_cell': (4 if dom == 'backward_kernel' else 2) * N * N,
+                'fwd_kernel_ms': fwd_avg, 'bwd_kernel_ms': bwd_avg,
+                'hbm_peak_gbs': peaks.get('hbm_gbs')}
+    if rank == 0:
+        cpu = cpu_baseline(w, args.cpu_seconds) if args.cpu_seconds > 0 else None
+        line = {
+            'metric': 'pair-HMM E-step cell-state updates/s', 'value': value,
+            'unit': 'cell-state updates/s', 'n_gpus': ws, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': ms_step, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': args.workload, 'model': 'MixDom2 n_dom=3 n_frag=1 n_classes=1',
+                       'n_states': N, 'pairs_per_gpu': len(w.xs), 'cells_per_gpu': int(total_cells),
+                       'cell_states_per_step_per_gpu': cell_states, 'pairs_per_s': len(w.xs) * ws / (ms_step / 1e3),
+                       'l2': 'flushed (256 MiB write) between timed steps', 'parallelism': f'replicas x{ws}',
+                       'status_nonzero': int((status != 0).sum())},
+            'roofline': roofline, 'cpu_baseline': cpu,
+            'e2e': {'value': e2e_value, 'unit': 'cell-state updates/s', 'h2d_bytes_per_step': h2d,
+                    'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_total / args.steps,
+                    'api': 'pairhmm.api.estep_batch_mixdom2'},
+            'plain': plain, 'gpu_launches': 2 * args.steps, 'clocks': clocks,
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,139 @@
+/*
+ * pairhmm.h -- C ABI of the GB300 (sm_103a) batched 2D pair-HMM
+ * forward / backward / E-step library.
+ *
+ * The library replaces the device side of the reference's 2D pair-HMM
+ * dynamic programme (evoldoers/tkf-mixdom, python/tkfmixdom/jax/dp/hmm.py)
+ * for batches of sequence pairs.  Every entry point is stream-ordered, takes
+ * plain pointers and sizes, and returns 0 on success or a negative PHMM_E_*
+ * code (message via phmm_last_error).
+ *
+ * Conventions shared with the reference:
+ *   - state types: 0 = S (start), 1 = M, 2 = I, 3 = D, 4 = E
+ *     (core/params.py:21); state index 0 is the start state
+ *     (dp/hmm.py:1212, 1236) and the End column is the first E-typed state
+ *     (dp/hmm.py:17-23);
+ *   - residues are 0..19 plus the wildcard 20 whose emission factor is 1
+ *     (dp/hmm.py:646-648);
+ *   - transitions are given in linear probability space (the exponential of
+ *     the reference's log_trans; NEG_INF entries become 0);
+ *   - per-emission-group tables: M[g][a][b] = P(emit x=a, y=b), I[g][b],
+ *     D[g][a] (linear, 21 x 21 / 21 entries including the wildcard row and
+ *     column), one group per MixDom (domain, fragment) location, one group
+ *     for TKF91/TKF92 (dp/hmm.py:628-851 build these as log tables).
+ */
+#ifndef PAIRHMM_H_
+#define PAIRHMM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHMM_OK 0
+#define PHMM_E_ARG -1      /* bad argument / unsupported model shape */
+#define PHMM_E_CUDA -2     /* CUDA runtime error (allocation, launch) */
+#define PHMM_E_KERNEL -3   /* a kernel reported a failure in status[] */
+
+/* per-pair status bits written by the kernels */
+#define PHMM_ST_TIMEOUT 1      /* a bounded inter-CTA wait gave up */
+#define PHMM_ST_ZERO_LL 2      /* likelihood underflowed to 0 or is not finite */
+#define PHMM_ST_BAD_RESIDUE 4  /* residue > 20 (clamped to the wildcard) */
+#define PHMM_ST_SCALE_CLAMP 8  /* a posterior scale exponent was clamped */
+
+/* Model description: the state space of one pair HMM.  Replaces the
+ * (log_trans.shape, state_types) pair of dp/hmm.py:1775/1834 plus the
+ * state -> emission-group map of dp/hmm.py:719-729 (MixDom2) /
+ * dp/hmm.py:820-823 (MixDom1). */
+typedef struct phmm_model_desc {
+    int32_t n_states;            /* N */
+    const int8_t *state_types;   /* host [N] */
+    const int32_t *state_group;  /* host [N]; group of each M/I/D state, ignored otherwise */
+    int32_t n_groups;            /* G */
+} phmm_model_desc;
+
+/* A batch of pairs.  Device pointers unless noted.  Replaces the bucketed
+ * (xs_pad, ys_pad, Lx_real, Ly_real, log_chis, sub stacks) arguments of the
+ * reference's jit(vmap(forward_backward_2d)) callers
+ * (train/tkf92_svi_bw.py:263-334, train_pfam.py:1674-1741); no padding is
+ * needed: every pair runs at its real lengths. */
+typedef struct phmm_batch {
+    int32_t n_pairs;
+    const int32_t *Lx_host;      /* host [P] ancestor lengths */
+    const int32_t *Ly_host;      /* host [P] descendant lengths */
+    const uint8_t *residues;     /* device: concatenated residues */
+    const int64_t *x_off_host;   /* host [P] offset of x_p in residues */
+    const int64_t *y_off_host;   /* host [P] offset of y_p in residues */
+    const float *chi;            /* device [P or 1][N][N] transition matrix */
+    int32_t chi_per_pair;        /* 1: one matrix per pair, 0: shared */
+    const float *emit_M;         /* device [P or 1][G][21][21] */
+    const float *emit_I;         /* device [P or 1][G][21] */
+    const float *emit_D;         /* device [P or 1][G][21] */
+    int32_t emit_per_pair;       /* 1: tables per pair, 0: shared */
+} phmm_batch;
+
+typedef struct phmm_plan phmm_plan;
+
+/* Create a plan for one state space.  Scratch memory is allocated lazily
+ * by the first batch that needs it and reused afterwards. */
+int phmm_plan_create(const phmm_model_desc *model, phmm_plan **out);
+void phmm_plan_destroy(phmm_plan *plan);
+
+/* Forward pass only: ll_out[p] = log P(x_p, y_p) (float64).
+ * Replaces forward_2d (dp/hmm.py:1775-1801) and
+ * forward_backward_2d(..., forward_only=True) (dp/hmm.py:1834-1914);
+ * stream is a cudaStream_t. */
+int phmm_forward(phmm_plan *plan, const phmm_batch *batch,
+                 double *ll_out, int32_t *status_out, void *stream);
+
+/* Full E-step: log-likelihood, expected transition counts and the
+ * per-group character-indexed expected emission counts.
+ *   ll_out    [P]           float64
+ *   n_trans   [P][N][N]     float64, reference state order
+ *                           (forward_backward_2d's expected_trans,
+ *                           dp/hmm.py:1940-1971)
+ *   cnt_M     [P][G][21][21] sum of M-type posteriors by (x_i, y_j)
+ *   cnt_I     [P][G][21]     sum of I-type posteriors by y_j
+ *   cnt_D     [P][G][21]     sum of D-type posteriors by x_i
+ * The per-class counts of train/likelihood.py:279-344 and the VJP counts of
+ * train/vjp.py:513-625 follow from cnt_* in a small float64 epilogue.
+ * Replaces forward_backward_2d (dp/hmm.py:1834-1973) as called by
+ * e_step / e_step_mixdom2 (train/likelihood.py:49-373). */
+int phmm_estep(phmm_plan *plan, const phmm_batch *batch,
+               double *ll_out, double *n_trans, double *cnt_M, double *cnt_I,
+               double *cnt_D, int32_t *status_out, void *stream);
+
+/* E-step that also writes full lattice tables (optional, nullable):
+ *   log_F, log_B [sum_p (Lx+1)(Ly+1)][N] float64 log forward / backward
+ *   post         [sum_p (Lx+1)(Ly+1)][N] float64 posteriors
+ * pair p's block starts at cell offset sum_{q<p} (Lx_q+1)(Ly_q+1), row-major
+ * (i, j).  For API parity with forward_2d / backward_2d /
+ * forward_backward_2d (dp/hmm.py:1775-1973); not a fast path. */
+int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch,
+                      double *ll_out, double *n_trans, double *cnt_M,
+                      double *cnt_I, double *cnt_D, int32_t *status_out,
+                      double *log_F, double *log_B, double *post, void *stream);
+
+/* Per-kernel CUDA-event timing on the launching stream (diagnostics and
+ * benchmarking; no counterpart in the reference, which has no kernels).
+ * phmm_kernel_times waits for the last call's events and returns the forward
+ * and backward kernel durations in milliseconds (backward 0 after
+ * phmm_forward). */
+int phmm_set_timing(phmm_plan *plan, int enable);
+int phmm_kernel_times(phmm_plan *plan, float *fwd_ms, float *bwd_ms);
+
+/* Number of kernel launches issued by the last call on this plan. */
+int phmm_last_launch_count(const phmm_plan *plan);
+
+/* Last error message (thread-local); returns its length. */
+int phmm_last_error(char *buf, size_t len);
+
+/* ABI version of this library. */
+int phmm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PAIRHMM_H_ */

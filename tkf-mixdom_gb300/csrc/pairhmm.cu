@@ -1,0 +1,1165 @@
+// pairhmm.cu -- batched 2D pair-HMM forward / backward / E-step for GB300
+// (sm_103a), behind the C ABI declared in include/pairhmm.h.
+//
+// Algorithm (the reference's, evoldoers/tkf-mixdom python/tkfmixdom/jax/
+// dp/hmm.py:1120-1973): forward F[i,j,k] = e[i,j,k] sum_s F[pred_k(i,j),s]
+// chi[s,k], backward B[i,j,s] = sum_k chi[s,k] e[succ_k] B[succ_k,k], expected
+// transitions n[s,k] = sum_cells F chi e B / P, evaluated here in float32
+// probability space instead of float64 log space.
+//
+// GB300 design:
+//  * Work unit = a STRIPE of 32 lattice rows of one pair (all columns).  A
+//    CTA sweeps its stripe along anti-diagonals: at step t lane r of every
+//    warp owns cell (i0 + r, t - r); warp w owns the 4-state "quad" w of the
+//    cell's state vector.  Two __syncthreads per step, no global traffic on
+//    the critical path except the halo row.
+//  * Stripes of one pair are PIPELINED across CTAs: stripe s+1 consumes the
+//    bottom row of stripe s through a global edge buffer, in chunks of 32
+//    columns published with release/acquire progress counters.  A persistent
+//    grid pops (pair, stripe) items from an atomic queue ordered
+//    longest-pair-first, so long pairs spread over many SMs and short pairs
+//    fill the gaps.  A stripe only ever waits for a stripe popped before it,
+//    so progress needs no co-residency guarantee; every wait is bounded.
+//  * Scaling: each cell's state vector is renormalised by an exact power of
+//    two (its own exponent, int32), so the DP has no underflow and the only
+//    rounding is that of the float32 multiply-adds.
+//  * The E-step backward kernel fuses: the backward recursion, posteriors,
+//    per-group character-indexed emission counts (float64 shared-memory
+//    bins) and the transition-count outer products (float32 per-thread
+//    accumulators with Kahan compensation, float64 at the flush).  The
+//    forward pass of an E-step stores the scaled forward lattice (stripe-
+//    diagonal layout, read back with cp.async one diagonal ahead).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pairhmm.h"
+
+namespace {
+
+constexpr int TH = 32;             // rows per stripe == lanes per warp
+constexpr int HC = 32;             // halo chunk width (columns)
+constexpr int MAXS = 64;           // max padded state slots (16 quads)
+constexpr int MAXQ = MAXS / 4;
+constexpr int NBIN = 441 + 21 + 21;
+constexpr int EXP_NONE = -(1 << 28);
+constexpr double LN2 = 0.69314718055994530942;
+constexpr double NEG_INF_LL = -1e30;  // reference NEG_INF (dp/hmm.py:108)
+enum { T_S = 0, T_M = 1, T_I = 2, T_D = 3, T_E = 4, T_NONE = 5 };
+
+struct PairMeta {
+    int64_t x_off, y_off;
+    int64_t lat_base;    // first cell of the pair's lattice (stripe-diagonal layout)
+    int64_t edge_base;   // first cell of the pair's edge rows
+    int64_t tab_base;    // first cell of the pair's optional row-major tables
+    int32_t Lx, Ly;
+    int32_t n_stripes;
+    int32_t stripe_base;
+};
+
+struct KParams {
+    int N, NS, NQ, G, e_idx, s_slot;
+    int kbeg[3], kend[3];               // slot ranges of the M, I, D groups
+    int16_t slot_orig[MAXS];            // original state index or -1
+    int8_t slot_type[MAXS];             // T_M/T_I/T_D dest, T_S start, T_NONE pad
+    int16_t slot_group[MAXS];
+    int8_t quad_type[MAXQ];
+    const uint8_t *res;
+    const PairMeta *meta;
+    const int2 *items;
+    int n_items;
+    int *counter;
+    const float *chi;
+    int64_t chi_stride;
+    const float *eM, *eI, *eD;
+    int64_t eM_stride, eID_stride;
+    float *lat;
+    int *lat_exp;
+    float *edge;
+    int *edge_exp;
+    int *progress;
+    double *ll;
+    int *status;
+    double *n_trans, *cntM, *cntI, *cntD;
+    double *F_log, *B_log, *post;
+    int max_ly;
+    long long spin_limit;
+};
+
+struct SmemLayout {
+    int chi, chiE, tM, tI, tD, ring, raw, mx, halo, fst, ft, ut;  // float offsets
+    int ringE, haloE, fstE;                                         // int offsets
+    int bins;                                                       // double offset
+    int ys;                                                         // byte offset
+    int bytes;
+};
+
+__host__ __device__ inline int al4(int v) { return (v + 3) & ~3; }
+
+__host__ __device__ inline SmemLayout make_layout(int NS, int NQ, int G, int max_ly, bool bwd) {
+    SmemLayout L;
+    int o = 0;
+    L.chi = o; o += NS * NS;
+    L.chiE = o; o += al4(NS);
+    L.tM = o; o += al4(G * 441);
+    L.tI = o; o += al4(G * 21);
+    L.tD = o; o += al4(G * 21);
+    L.ring = o; o += 3 * NS * TH;
+    L.raw = o; o += NS * TH;
+    L.mx = o; o += al4(NQ * TH);
+    L.halo = o; o += al4(2 * NS * (HC + 1));
+    if (bwd) {
+        L.fst = o; o += 2 * TH * NS;
+        L.ft = o; o += TH * NS;
+        L.ut = o; o += TH * NS;
+    } else {
+        L.fst = L.ft = L.ut = -1;
+    }
+    L.ringE = o; o += 3 * TH;
+    L.haloE = o; o += al4(2 * (HC + 1));
+    if (bwd) { L.fstE = o; o += 2 * TH; } else { L.fstE = -1; }
+    o = (o + 3) & ~3;
+    if (bwd) { L.bins = o / 2; o += 2 * G * NBIN; } else { L.bins = -1; }
+    int bytes = o * 4;
+    L.ys = bytes;
+    bytes += max_ly + 1;
+    L.bytes = (bytes + 15) & ~15;
+    return L;
+}
+
+// 2^e as a float, exact for e in [-149, 127]; 0 below.
+__device__ __forceinline__ float pow2f(int e) {
+    if (e >= -126) return __int_as_float((min(e, 127) + 127) << 23);
+    if (e >= -149) return __int_as_float(1 << (e + 149));
+    return 0.0f;
+}
+
+__device__ __forceinline__ int ld_acquire(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int *p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Bounded wait until *p >= need.  Returns false when the bound is hit.
+__device__ bool wait_geq(const int *p, int need, long long limit) {
+    long long it = 0;
+    while (ld_acquire(p) < need) {
+        if (++it > limit) return false;
+        __nanosleep(128);
+    }
+    return true;
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+__device__ __forceinline__ float4 f4scale(float4 a, float s) {
+    return make_float4(a.x * s, a.y * s, a.z * s, a.w * s);
+}
+__device__ __forceinline__ float f4max(float4 a) { return fmaxf(fmaxf(a.x, a.y), fmaxf(a.z, a.w)); }
+__device__ __forceinline__ float f4get(float4 a, int u) {
+    return u == 0 ? a.x : (u == 1 ? a.y : (u == 2 ? a.z : a.w));
+}
+
+// Load the per-pair model into shared memory: transitions in slot layout
+// (transposed for the backward pass), End column, emission tables, and the
+// descendant residues.  Returns nothing; ends with __syncthreads().
+__device__ void load_pair_model(const KParams &P, int p, const PairMeta &m, const SmemLayout &L,
+                                float *sm, unsigned char *smb, bool transpose) {
+    const int NS = P.NS, N = P.N, G = P.G;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const float *chi = P.chi + (int64_t)p * P.chi_stride;
+    float *chiS = sm + L.chi;
+    for (int idx = tid; idx < NS * NS; idx += nt) {
+        int s = idx / NS, k = idx % NS;
+        int os = P.slot_orig[s], ok = P.slot_orig[k];
+        int kt = P.slot_type[k];
+        float v = 0.0f;
+        if (os >= 0 && ok >= 0 && (kt == T_M || kt == T_I || kt == T_D)) v = __ldg(chi + os * N + ok);
+        if (transpose) chiS[k * NS + s] = v; else chiS[s * NS + k] = v;
+    }
+    for (int s = tid; s < NS; s += nt) {
+        int os = P.slot_orig[s];
+        sm[L.chiE + s] = (os >= 0) ? __ldg(chi + os * N + P.e_idx) : 0.0f;
+    }
+    const float *eM = P.eM + (int64_t)p * P.eM_stride;
+    const float *eI = P.eI + (int64_t)p * P.eID_stride;
+    const float *eD = P.eD + (int64_t)p * P.eID_stride;
+    for (int idx = tid; idx < G * 441; idx += nt) sm[L.tM + idx] = __ldg(eM + idx);
+    for (int idx = tid; idx < G * 21; idx += nt) {
+        sm[L.tI + idx] = __ldg(eI + idx);
+        sm[L.tD + idx] = __ldg(eD + idx);
+    }
+    unsigned char *ys = smb + L.ys;
+    for (int j = tid; j <= m.Ly; j += nt) {
+        int c = 0;
+        if (j >= 1) {
+            c = P.res[m.y_off + j - 1];
+            if (c > 20) { c = 20; atomicOr(P.status + p, PHMM_ST_BAD_RESIDUE); }
+        }
+        ys[j] = (unsigned char)c;
+    }
+    __syncthreads();
+}
+
+// Per-thread emission lookup bases of the 4 slots of quad q for row char xi.
+struct EmitBase {
+    int off[4];
+    float mask[4];
+    int type;
+};
+
+__device__ __forceinline__ EmitBase emit_base(const KParams &P, const SmemLayout &L, int q, int xi) {
+    EmitBase eb;
+    eb.type = P.quad_type[q];
+    for (int u = 0; u < 4; ++u) {
+        int k = 4 * q + u;
+        int kt = P.slot_type[k];
+        int g = P.slot_group[k];
+        bool em = (kt == T_M || kt == T_I || kt == T_D);
+        eb.mask[u] = em ? 1.0f : 0.0f;
+        if (!em) g = 0;
+        if (eb.type == T_M) eb.off[u] = L.tM + g * 441 + xi * 21;   // + y_j
+        else if (eb.type == T_I) eb.off[u] = L.tI + g * 21;          // + y_j
+        else eb.off[u] = L.tD + g * 21 + xi;                         // (no y)
+    }
+    return eb;
+}
+
+__device__ __forceinline__ float4 emit4(const float *sm, const EmitBase &eb, int yj) {
+    int add = (eb.type == T_D) ? 0 : yj;
+    return make_float4(sm[eb.off[0] + add] * eb.mask[0], sm[eb.off[1] + add] * eb.mask[1],
+                       sm[eb.off[2] + add] * eb.mask[2], sm[eb.off[3] + add] * eb.mask[3]);
+}
+
+// ---------------------------------------------------------------- forward
+__device__ void forward_stripe(const KParams &P, int p, int si, const SmemLayout &L, float *sm,
+                               unsigned char *smb, int *s_flag) {
+    const PairMeta m = P.meta[p];
+    const int NS = P.NS, NQ = P.NQ, N = P.N;
+    const int Lx = m.Lx, Ly = m.Ly;
+    const int i0 = si * TH;
+    const int nrows = min(TH, Lx + 1 - i0);
+    const int lane = threadIdx.x & 31, q = threadIdx.x >> 5;
+    const int r = lane;
+    const int i = i0 + r;
+    const bool has_below = si + 1 < m.n_stripes;
+    int *prog_above = (si > 0) ? P.progress + m.stripe_base + si - 1 : nullptr;
+    int *prog_mine = P.progress + m.stripe_base + si;
+    const float *edge_above = P.edge + (m.edge_base + (int64_t)(si - 1) * (Ly + 1)) * NS;
+    const int *edgeE_above = P.edge_exp + m.edge_base + (int64_t)(si - 1) * (Ly + 1);
+    float *edge_mine = P.edge + (m.edge_base + (int64_t)si * (Ly + 1)) * NS;
+    int *edgeE_mine = P.edge_exp + m.edge_base + (int64_t)si * (Ly + 1);
+    const int64_t latc = m.lat_base + (int64_t)si * (TH + Ly) * TH;  // this stripe's first lattice cell
+
+    load_pair_model(P, p, m, L, sm, smb, false);
+    const unsigned char *ys = smb + L.ys;
+    int xi = 0;
+    if (r < nrows && i >= 1) {
+        xi = P.res[m.x_off + i - 1];
+        if (xi > 20) { xi = 20; atomicOr(P.status + p, PHMM_ST_BAD_RESIDUE); }
+    }
+    const EmitBase eb = emit_base(P, L, q, xi);
+    const float4 *chi4 = reinterpret_cast<const float4 *>(sm + L.chi) + q;
+    float *ring = sm + L.ring;
+    int *ringE = reinterpret_cast<int *>(sm) + L.ringE;
+    float *halo = sm + L.halo;
+    int *haloE = reinterpret_cast<int *>(sm) + L.haloE;
+    float *raw = sm + L.raw;
+    float *mx = sm + L.mx;
+    const int T_last = (nrows - 1) + Ly;
+    const int qt = eb.type;
+    bool aborted = false;
+
+    for (int t = 0; t <= T_last; ++t) {
+        // ---- top halo chunk (row i0-1 from the stripe above)
+        if (si > 0 && (t % HC) == 0 && t <= Ly) {
+            const int c = t / HC;
+            const int cbeg = c * HC, cend = min(cbeg + HC, Ly + 1);
+            if (threadIdx.x == 0) *s_flag = wait_geq(prog_above, cend, P.spin_limit) ? 0 : 1;
+            __syncthreads();
+            if (*s_flag) { aborted = true; break; }
+            float *hb = halo + (c & 1) * NS * (HC + 1);
+            int *hbE = haloE + (c & 1) * (HC + 1);
+            const int ncol = cend - cbeg;
+            for (int idx = threadIdx.x; idx < ncol * NS; idx += blockDim.x) {
+                int col = idx / NS, s = idx % NS;
+                hb[s * (HC + 1) + col] = __ldcg(edge_above + (int64_t)(cbeg + col) * NS + s);
+            }
+            for (int col = threadIdx.x; col < ncol; col += blockDim.x) hbE[col] = __ldcg(edgeE_above + cbeg + col);
+            __syncthreads();
+        }
+        // ---- phase A: raw state values of this diagonal
+        const int j = t - r;
+        const bool valid = (r < nrows) && (j >= 0) && (j <= Ly);
+        int Eref = EXP_NONE;
+        if (valid) {
+            const float *pp = nullptr;
+            int pst = TH, Ep = EXP_NONE;
+            // I pred (i, j-1): diag t-1, row r
+            const bool hasI = j >= 1;
+            const bool hasD = i >= 1;
+            const bool hasM = hasD && hasI;
+            int EI_ = EXP_NONE, ED_ = EXP_NONE, EM_ = EXP_NONE;
+            const float *pI = ring + ((t + 2) % 3) * NS * TH + r;
+            const float *pD = nullptr, *pM = nullptr;
+            int stD = TH, stM = TH;
+            if (hasI) EI_ = ringE[((t + 2) % 3) * TH + r];
+            if (hasD) {
+                if (r >= 1) {
+                    pD = ring + ((t + 2) % 3) * NS * TH + (r - 1);
+                    ED_ = ringE[((t + 2) % 3) * TH + r - 1];
+                } else {
+                    pD = halo + ((j / HC) & 1) * NS * (HC + 1) + (j % HC);
+                    stD = HC + 1;
+                    ED_ = haloE[((j / HC) & 1) * (HC + 1) + (j % HC)];
+                }
+            }
+            if (hasM) {
+                if (r >= 1) {
+                    pM = ring + ((t + 1) % 3) * NS * TH + (r - 1);
+                    EM_ = ringE[((t + 1) % 3) * TH + r - 1];
+                } else {
+                    const int jm = j - 1;
+                    pM = halo + ((jm / HC) & 1) * NS * (HC + 1) + (jm % HC);
+                    stM = HC + 1;
+                    EM_ = haloE[((jm / HC) & 1) * (HC + 1) + (jm % HC)];
+                }
+            }
+            Eref = max(max(hasI ? EI_ : EXP_NONE, hasD ? ED_ : EXP_NONE), hasM ? EM_ : EXP_NONE);
+            bool have = false;
+            if (qt == T_M && hasM) { pp = pM; pst = stM; Ep = EM_; have = true; }
+            if (qt == T_I && hasI) { pp = pI; pst = TH; Ep = EI_; have = true; }
+            if (qt == T_D && hasD) { pp = pD; pst = stD; Ep = ED_; have = true; }
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (have && Ep > EXP_NONE) {
+                for (int s = 0; s < NS; s += 4) {
+                    const float v0 = pp[(s + 0) * pst], v1 = pp[(s + 1) * pst];
+                    const float v2 = pp[(s + 2) * pst], v3 = pp[(s + 3) * pst];
+                    const float4 c0 = chi4[(s + 0) * NQ], c1 = chi4[(s + 1) * NQ];
+                    const float4 c2 = chi4[(s + 2) * NQ], c3 = chi4[(s + 3) * NQ];
+                    acc.x = fmaf(v0, c0.x, acc.x); acc.y = fmaf(v0, c0.y, acc.y);
+                    acc.z = fmaf(v0, c0.z, acc.z); acc.w = fmaf(v0, c0.w, acc.w);
+                    acc.x = fmaf(v1, c1.x, acc.x); acc.y = fmaf(v1, c1.y, acc.y);
+                    acc.z = fmaf(v1, c1.z, acc.z); acc.w = fmaf(v1, c1.w, acc.w);
+                    acc.x = fmaf(v2, c2.x, acc.x); acc.y = fmaf(v2, c2.y, acc.y);
+                    acc.z = fmaf(v2, c2.z, acc.z); acc.w = fmaf(v2, c2.w, acc.w);
+                    acc.x = fmaf(v3, c3.x, acc.x); acc.y = fmaf(v3, c3.y, acc.y);
+                    acc.z = fmaf(v3, c3.z, acc.z); acc.w = fmaf(v3, c3.w, acc.w);
+                }
+                const float4 e = emit4(sm, eb, ys[j]);
+                const float sc = pow2f(Ep - Eref);
+                acc = make_float4(acc.x * e.x * sc, acc.y * e.y * sc, acc.z * e.z * sc, acc.w * e.w * sc);
+            }
+            float *rw = raw + (4 * q) * TH + r;
+            rw[0] = acc.x; rw[TH] = acc.y; rw[2 * TH] = acc.z; rw[3 * TH] = acc.w;
+            mx[q * TH + r] = f4max(acc);
+        }
+        __syncthreads();
+        // ---- phase B: per-cell power-of-two renormalisation
+        if (valid) {
+            float mval = 0.0f;
+            for (int qq = 0; qq < NQ; ++qq) mval = fmaxf(mval, mx[qq * TH + r]);
+            const float *rw = raw + (4 * q) * TH + r;
+            float4 v = make_float4(rw[0], rw[TH], rw[2 * TH], rw[3 * TH]);
+            int Ecell = EXP_NONE;
+            if (mval > 0.0f) {
+                int e;
+                frexpf(mval, &e);
+                v = make_float4(ldexpf(v.x, -e), ldexpf(v.y, -e), ldexpf(v.z, -e), ldexpf(v.w, -e));
+                Ecell = Eref + e;
+            } else {
+                v = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            if (i == 0 && j == 0) {  // origin: F[0,0,start] = 1 (dp/hmm.py:1212)
+                v = make_float4(0.f, 0.f, 0.f, 0.f);
+                const int ss = P.s_slot;
+                if (ss / 4 == q) {
+                    if (ss % 4 == 0) v.x = 1.f; else if (ss % 4 == 1) v.y = 1.f;
+                    else if (ss % 4 == 2) v.z = 1.f; else v.w = 1.f;
+                }
+                Ecell = 0;
+            }
+            float *rg = ring + (t % 3) * NS * TH + (4 * q) * TH + r;
+            rg[0] = v.x; rg[TH] = v.y; rg[2 * TH] = v.z; rg[3 * TH] = v.w;
+            if (q == 0) ringE[(t % 3) * TH + r] = Ecell;
+            if (has_below && r == TH - 1) {
+                reinterpret_cast<float4 *>(edge_mine + (int64_t)j * NS)[q] = v;
+                if (q == 0) edgeE_mine[j] = Ecell;
+            }
+            if (P.lat) {
+                const int64_t cell = latc + (int64_t)t * TH + r;
+                reinterpret_cast<float4 *>(P.lat + cell * NS)[q] = v;
+                if (q == 0) P.lat_exp[cell] = Ecell;
+            }
+            if (P.F_log) {
+                const int64_t cell = m.tab_base + (int64_t)i * (Ly + 1) + j;
+                for (int u = 0; u < 4; ++u) {
+                    const int os = P.slot_orig[4 * q + u];
+                    if (os < 0) continue;
+                    const float x = f4get(v, u);
+                    P.F_log[cell * N + os] = (x > 0.f && Ecell > EXP_NONE)
+                        ? log((double)x) + (double)Ecell * LN2 : NEG_INF_LL;
+                }
+            }
+        }
+        __syncthreads();
+        // ---- publish bottom-row progress for the stripe below
+        if (has_below && threadIdx.x == 0) {
+            const int jb = t - (TH - 1);
+            if (jb >= 0 && jb <= Ly && (((jb + 1) % HC) == 0 || jb == Ly)) {
+                __threadfence();
+                st_release(prog_mine, jb + 1);
+            }
+        }
+    }
+    if (aborted) {
+        if (threadIdx.x == 0) {
+            atomicOr(P.status + p, PHMM_ST_TIMEOUT);
+            if (has_below) { __threadfence(); st_release(prog_mine, Ly + 1); }
+            if (si + 1 == m.n_stripes) P.ll[p] = NEG_INF_LL;
+        }
+        __syncthreads();
+        return;
+    }
+    // ---- log-likelihood at the terminal cell (dp/hmm.py:1913)
+    if (si + 1 == m.n_stripes && q == 0) {
+        const int rT = Lx - i0;
+        const float *cellv = ring + (T_last % 3) * NS * TH + rT;
+        double acc = 0.0;
+        for (int s = lane; s < NS; s += 32) acc += (double)cellv[s * TH] * (double)sm[L.chiE + s];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            const int E = ringE[(T_last % 3) * TH + rT];
+            double ll = NEG_INF_LL;
+            if (acc > 0.0 && isfinite(acc) && E > EXP_NONE) ll = log(acc) + (double)E * LN2;
+            else atomicOr(P.status + p, PHMM_ST_ZERO_LL);
+            P.ll[p] = ll;
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(512) forward_kernel(const KParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_item;
+    __shared__ int s_flag;
+    float *sm = reinterpret_cast<float *>(smem_raw);
+    const SmemLayout L = make_layout(P.NS, P.NQ, P.G, P.max_ly, false);
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(P.counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= P.n_items) break;
+        const int2 w = P.items[it];
+        forward_stripe(P, w.x, w.y, L, sm, smem_raw, &s_flag);
+    }
+}
+
+// ---------------------------------------------------------------- backward + counts
+__device__ void backward_stripe(const KParams &P, int p, int si, const SmemLayout &L, float *sm,
+                                unsigned char *smb, int *s_flag) {
+    const PairMeta m = P.meta[p];
+    const int NS = P.NS, NQ = P.NQ, N = P.N, G = P.G;
+    const int Lx = m.Lx, Ly = m.Ly;
+    const int i0 = si * TH;
+    const int nrows = min(TH, Lx + 1 - i0);
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int lane = tid & 31, q = tid >> 5;
+    const int r = lane;
+    const int i = i0 + r;
+    const bool has_below = si + 1 < m.n_stripes;
+    const bool has_above = si > 0;
+    int *prog_below = has_below ? P.progress + m.stripe_base + si + 1 : nullptr;
+    int *prog_mine = P.progress + m.stripe_base + si;
+    const float *edge_below = P.edge + (m.edge_base + (int64_t)(si + 1) * (Ly + 1)) * NS;
+    const int *edgeE_below = P.edge_exp + m.edge_base + (int64_t)(si + 1) * (Ly + 1);
+    float *edge_mine = P.edge + (m.edge_base + (int64_t)si * (Ly + 1)) * NS;
+    int *edgeE_mine = P.edge_exp + m.edge_base + (int64_t)si * (Ly + 1);
+    const int64_t latc = m.lat_base + (int64_t)si * (TH + Ly) * TH;
+
+    const double llv = P.ll[p];
+    if (!(llv > -1e29)) {  // forward failed: no counts for this pair
+        __syncthreads();
+        if (tid == 0 && has_above) { __threadfence(); st_release(prog_mine, Ly + 1); }
+        return;
+    }
+    const double lam = llv / LN2;
+    const double Epd = floor(lam);
+    const int Ep = (int)Epd;
+    const float rfrac = (float)exp2(-(lam - Epd));
+
+    load_pair_model(P, p, m, L, sm, smb, true);
+    double *bins = reinterpret_cast<double *>(sm) + L.bins;
+    for (int idx = tid; idx < G * NBIN; idx += nt) bins[idx] = 0.0;
+    const unsigned char *ys = smb + L.ys;
+    int xi = 0;
+    if (r < nrows && i >= 1) xi = min((int)P.res[m.x_off + i - 1], 20);
+    const EmitBase eb = emit_base(P, L, q, xi);
+    const int qt = eb.type;
+    float *ring = sm + L.ring;
+    int *ringE = reinterpret_cast<int *>(sm) + L.ringE;
+    float *halo = sm + L.halo;
+    int *haloE = reinterpret_cast<int *>(sm) + L.haloE;
+    float *raw = sm + L.raw;
+    float *mx = sm + L.mx;
+    float *fst = sm + L.fst;
+    int *fstE = reinterpret_cast<int *>(sm) + L.fstE;
+    float4 *ft4 = reinterpret_cast<float4 *>(sm + L.ft);
+    float4 *ut4 = reinterpret_cast<float4 *>(sm + L.ut);
+    const float4 *chiB4 = reinterpret_cast<const float4 *>(sm + L.chi) + q;  // chiB[k][4q..]
+
+    // count-phase role: (source quad sq, dest quad kq, row group rg)
+    const int npairs = NQ * NQ;
+    const int RG = nt / npairs;
+    const int cp = tid % npairs, rg = tid / npairs;
+    const int sq = cp / NQ, kq = cp % NQ;
+    const bool counter_role = rg < RG && P.quad_type[kq] != T_NONE;
+    float csum[16], ccomp[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) { csum[u] = 0.f; ccomp[u] = 0.f; }
+
+    const int T_last = (nrows - 1) + Ly;
+    // lattice prefetch (cp.async): diagonal t goes to buffer t & 1
+    auto prefetch = [&](int t) {
+        if (t >= 0) {
+            const float *src = P.lat + (latc + (int64_t)t * TH) * NS;
+            float *dst = fst + (t & 1) * TH * NS;
+            for (int idx = tid; idx < TH * NS / 4; idx += nt) cp_async16(dst + 4 * idx, src + 4 * idx);
+            const int *srcE = P.lat_exp + latc + (int64_t)t * TH;
+            int *dstE = fstE + (t & 1) * TH;
+            for (int idx = tid; idx < TH / 4; idx += nt) cp_async16(dstE + 4 * idx, srcE + 4 * idx);
+        }
+        cp_commit();
+    };
+    prefetch(T_last);
+    bool aborted = false;
+
+    for (int t = T_last; t >= 0; --t) {
+        prefetch(t - 1);
+        // ---- bottom halo chunk (row i0+TH from the stripe below)
+        const int jb = t - (nrows - 1);
+        if (has_below && jb >= 0 && jb <= Ly && (jb == Ly || (jb % HC) == HC - 1)) {
+            const int c = jb / HC;
+            const int cbeg = c * HC, cend = min(cbeg + HC, Ly + 1);
+            if (tid == 0) *s_flag = wait_geq(prog_below, Ly + 1 - cbeg, P.spin_limit) ? 0 : 1;
+            __syncthreads();
+            if (*s_flag) { aborted = true; break; }
+            float *hb = halo + (c & 1) * NS * (HC + 1);
+            int *hbE = haloE + (c & 1) * (HC + 1);
+            const int ncol = cend - cbeg;
+            for (int idx = tid; idx < ncol * NS; idx += nt) {
+                int col = idx / NS, s = idx % NS;
+                hb[s * (HC + 1) + col] = __ldcg(edge_below + (int64_t)(cbeg + col) * NS + s);
+            }
+            for (int col = tid; col < ncol; col += nt) hbE[col] = __ldcg(edgeE_below + cbeg + col);
+            __syncthreads();
+        }
+        // ---- phase A: raw backward values for source slots 4q..4q+3
+        const int j = t - r;
+        const bool valid = (r < nrows) && (j >= 0) && (j <= Ly);
+        const bool terminal = valid && i == Lx && j == Ly;
+        int Eref = EXP_NONE;
+        // successor pointers/exponents, kept for the count preparation
+        const float *wM = nullptr, *wI = nullptr, *wD = nullptr;
+        int sM = TH, sI = TH, sD = TH;
+        int EM_ = EXP_NONE, EI_ = EXP_NONE, ED_ = EXP_NONE;
+        if (valid) {
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (terminal) {
+                acc = reinterpret_cast<const float4 *>(sm + L.chiE)[q];
+                Eref = 0;
+            } else {
+                const bool hasI = j + 1 <= Ly;
+                const bool hasD = i + 1 <= Lx;
+                const bool hasM = hasI && hasD;
+                if (hasI) {
+                    wI = ring + ((t + 1) % 3) * NS * TH + r;
+                    EI_ = ringE[((t + 1) % 3) * TH + r];
+                }
+                if (hasD) {
+                    if (r + 1 < nrows) {
+                        wD = ring + ((t + 1) % 3) * NS * TH + r + 1;
+                        ED_ = ringE[((t + 1) % 3) * TH + r + 1];
+                    } else {
+                        wD = halo + ((j / HC) & 1) * NS * (HC + 1) + (j % HC);
+                        sD = HC + 1;
+                        ED_ = haloE[((j / HC) & 1) * (HC + 1) + (j % HC)];
+                    }
+                }
+                if (hasM) {
+                    if (r + 1 < nrows) {
+                        wM = ring + ((t + 2) % 3) * NS * TH + r + 1;
+                        EM_ = ringE[((t + 2) % 3) * TH + r + 1];
+                    } else {
+                        const int jm = j + 1;
+                        wM = halo + ((jm / HC) & 1) * NS * (HC + 1) + (jm % HC);
+                        sM = HC + 1;
+                        EM_ = haloE[((jm / HC) & 1) * (HC + 1) + (jm % HC)];
+                    }
+                }
+                Eref = max(max(EI_, ED_), EM_);
+                const float *wp[3] = {wM, wI, wD};
+                const int ws[3] = {sM, sI, sD};
+                const int we[3] = {EM_, EI_, ED_};
+                for (int ty = 0; ty < 3; ++ty) {
+                    if (wp[ty] == nullptr || we[ty] <= EXP_NONE) continue;
+                    const float *w = wp[ty];
+                    const int st = ws[ty];
+                    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+                    for (int k = P.kbeg[ty]; k < P.kend[ty]; ++k) {
+                        const float wv = w[k * st];
+                        const float4 c = chiB4[k * NQ];
+                        a.x = fmaf(wv, c.x, a.x); a.y = fmaf(wv, c.y, a.y);
+                        a.z = fmaf(wv, c.z, a.z); a.w = fmaf(wv, c.w, a.w);
+                    }
+                    const float sc = pow2f(we[ty] - Eref);
+                    acc.x = fmaf(a.x, sc, acc.x); acc.y = fmaf(a.y, sc, acc.y);
+                    acc.z = fmaf(a.z, sc, acc.z); acc.w = fmaf(a.w, sc, acc.w);
+                }
+            }
+            float *rw = raw + (4 * q) * TH + r;
+            rw[0] = acc.x; rw[TH] = acc.y; rw[2 * TH] = acc.z; rw[3 * TH] = acc.w;
+            mx[q * TH + r] = f4max(acc);
+        }
+        cp_wait1();
+        __syncthreads();
+        // ---- phase B: normalise, store w = e*b, prepare count operands
+        float4 ftv = make_float4(0.f, 0.f, 0.f, 0.f), utv = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (valid) {
+            float mval = 0.0f;
+            for (int qq = 0; qq < NQ; ++qq) mval = fmaxf(mval, mx[qq * TH + r]);
+            const float *rw = raw + (4 * q) * TH + r;
+            float4 b = make_float4(rw[0], rw[TH], rw[2 * TH], rw[3 * TH]);
+            int Eb = EXP_NONE;
+            if (mval > 0.0f) {
+                int e;
+                frexpf(mval, &e);
+                b = make_float4(ldexpf(b.x, -e), ldexpf(b.y, -e), ldexpf(b.z, -e), ldexpf(b.w, -e));
+                Eb = Eref + e;
+            } else {
+                b = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            const float4 e4 = emit4(sm, eb, ys[j]);
+            const float4 w = make_float4(b.x * e4.x, b.y * e4.y, b.z * e4.z, b.w * e4.w);
+            float *rg = ring + (t % 3) * NS * TH + (4 * q) * TH + r;
+            rg[0] = w.x; rg[TH] = w.y; rg[2 * TH] = w.z; rg[3 * TH] = w.w;
+            if (q == 0) ringE[(t % 3) * TH + r] = Eb;
+            if (has_above && r == 0) {
+                reinterpret_cast<float4 *>(edge_mine + (int64_t)j * NS)[q] = w;
+                if (q == 0) edgeE_mine[j] = Eb;
+            }
+            // forward values of this cell
+            const float4 f = reinterpret_cast<const float4 *>(fst + (t & 1) * TH * NS + r * NS)[q];
+            const int Ef = fstE[(t & 1) * TH + r];
+            if (Ef > EXP_NONE && Eb > EXP_NONE) {
+                int d = Ef + Eb - Ep;
+                if (d > 126) { d = 126; atomicOr(P.status + p, PHMM_ST_SCALE_CLAMP); }
+                const float sc = ldexpf(rfrac, max(d, -200));
+                ftv = f4scale(f, sc);
+                // transition-count successor operand for the quad's own dest slots
+                const float *ws = (qt == T_M) ? wM : (qt == T_I) ? wI : (qt == T_D) ? wD : nullptr;
+                const int wst = (qt == T_M) ? sM : (qt == T_I) ? sI : sD;
+                const int wex = (qt == T_M) ? EM_ : (qt == T_I) ? EI_ : ED_;
+                if (ws != nullptr && wex > EXP_NONE) {
+                    const float us = pow2f(min(wex - Eb, 126));
+                    for (int u = 0; u < 4; ++u) {
+                        const float val = ws[(4 * q + u) * wst] * us;
+                        if (u == 0) utv.x = val; else if (u == 1) utv.y = val;
+                        else if (u == 2) utv.z = val; else utv.w = val;
+                    }
+                }
+            }
+            // posteriors -> per-group character bins
+            const float4 post4 = make_float4(ftv.x * b.x, ftv.y * b.y, ftv.z * b.z, ftv.w * b.w);
+            if (qt != T_NONE) {
+                for (int u = 0; u < 4; ++u) {
+                    const int k = 4 * q + u;
+                    const int kt = P.slot_type[k];
+                    const float pv = f4get(post4, u);
+                    if (pv == 0.f || !(kt == T_M || kt == T_I || kt == T_D)) continue;
+                    const int g = P.slot_group[k];
+                    int bi;
+                    if (kt == T_M) bi = g * NBIN + xi * 21 + ys[j];
+                    else if (kt == T_I) bi = g * NBIN + 441 + ys[j];
+                    else bi = g * NBIN + 462 + xi;
+                    atomicAdd(bins + bi, (double)pv);
+                }
+            }
+            if (terminal) {  // expected End transitions (dp/hmm.py:1969-1971)
+                for (int u = 0; u < 4; ++u) {
+                    const int os = P.slot_orig[4 * q + u];
+                    if (os >= 0) atomicAdd(P.n_trans + ((int64_t)p * N + os) * N + P.e_idx,
+                                           (double)f4get(post4, u));
+                }
+            }
+            if (P.post || P.B_log) {
+                const int64_t cell = m.tab_base + (int64_t)i * (Ly + 1) + j;
+                for (int u = 0; u < 4; ++u) {
+                    const int os = P.slot_orig[4 * q + u];
+                    if (os < 0) continue;
+                    if (P.post) P.post[cell * N + os] = (double)f4get(post4, u);
+                    if (P.B_log) {
+                        const float x = f4get(b, u);
+                        P.B_log[cell * N + os] = (x > 0.f && Eb > EXP_NONE)
+                            ? log((double)x) + (double)Eb * LN2 : NEG_INF_LL;
+                    }
+                }
+            }
+        }
+        ft4[r * NQ + q] = ftv;
+        ut4[r * NQ + q] = utv;
+        __syncthreads();
+        // ---- publish top-row progress for the stripe above
+        if (has_above && tid == 0 && t <= Ly && (t % HC) == 0) {
+            __threadfence();
+            st_release(prog_mine, Ly + 1 - t);
+        }
+        // ---- phase C: transition-count outer products over the diagonal's cells
+        if (counter_role) {
+            float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = p0, p2 = p0, p3 = p0;
+            for (int rr = rg; rr < nrows; rr += RG) {
+                const float4 fv = ft4[rr * NQ + sq];
+                const float4 uv = ut4[rr * NQ + kq];
+                p0.x = fmaf(fv.x, uv.x, p0.x); p0.y = fmaf(fv.x, uv.y, p0.y);
+                p0.z = fmaf(fv.x, uv.z, p0.z); p0.w = fmaf(fv.x, uv.w, p0.w);
+                p1.x = fmaf(fv.y, uv.x, p1.x); p1.y = fmaf(fv.y, uv.y, p1.y);
+                p1.z = fmaf(fv.y, uv.z, p1.z); p1.w = fmaf(fv.y, uv.w, p1.w);
+                p2.x = fmaf(fv.z, uv.x, p2.x); p2.y = fmaf(fv.z, uv.y, p2.y);
+                p2.z = fmaf(fv.z, uv.z, p2.z); p2.w = fmaf(fv.z, uv.w, p2.w);
+                p3.x = fmaf(fv.w, uv.x, p3.x); p3.y = fmaf(fv.w, uv.y, p3.y);
+                p3.z = fmaf(fv.w, uv.z, p3.z); p3.w = fmaf(fv.w, uv.w, p3.w);
+            }
+            const float pv[16] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w,
+                                  p2.x, p2.y, p2.z, p2.w, p3.x, p3.y, p3.z, p3.w};
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {  // Kahan compensated accumulation
+                const float y = pv[u] - ccomp[u];
+                const float tt = csum[u] + y;
+                ccomp[u] = (tt - csum[u]) - y;
+                csum[u] = tt;
+            }
+        }
+    }
+    if (aborted) {
+        if (tid == 0) {
+            atomicOr(P.status + p, PHMM_ST_TIMEOUT);
+            if (has_above) { __threadfence(); st_release(prog_mine, Ly + 1); }
+        }
+        cp_wait1();
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncthreads();
+        return;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    // ---- flush transition counts: n[s,k] = chi[s,k] * sum f~ u~
+    if (counter_role) {
+        const float *chi = P.chi + (int64_t)p * P.chi_stride;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            const int s = 4 * sq + (u >> 2), k = 4 * kq + (u & 3);
+            const int os = P.slot_orig[s], ok = P.slot_orig[k];
+            const int kt = P.slot_type[k];
+            const float val = csum[u] - ccomp[u];
+            if (os < 0 || ok < 0 || !(kt == T_M || kt == T_I || kt == T_D) || val == 0.f) continue;
+            const double c = (double)__ldg(chi + os * N + ok);
+            atomicAdd(P.n_trans + ((int64_t)p * N + os) * N + ok, (double)val * c);
+        }
+    }
+    __syncthreads();
+    // ---- flush emission bins
+    for (int idx = tid; idx < G * NBIN; idx += nt) {
+        const double v = bins[idx];
+        if (v == 0.0) continue;
+        const int g = idx / NBIN, b = idx % NBIN;
+        if (b < 441) atomicAdd(P.cntM + ((int64_t)p * G + g) * 441 + b, v);
+        else if (b < 462) atomicAdd(P.cntI + ((int64_t)p * G + g) * 21 + (b - 441), v);
+        else atomicAdd(P.cntD + ((int64_t)p * G + g) * 21 + (b - 462), v);
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(512) backward_kernel(const KParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_item;
+    __shared__ int s_flag;
+    float *sm = reinterpret_cast<float *>(smem_raw);
+    const SmemLayout L = make_layout(P.NS, P.NQ, P.G, P.max_ly, true);
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(P.counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= P.n_items) break;
+        const int2 w = P.items[it];
+        backward_stripe(P, w.x, w.y, L, sm, smem_raw, &s_flag);
+    }
+}
+
+__global__ void fill_f64(double *p, int64_t n, double v) {
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (int64_t)gridDim.x * blockDim.x)
+        p[idx] = v;
+}
+
+// ---------------------------------------------------------------- host side
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (expr);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return fail(PHMM_E_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+}  // namespace
+
+struct phmm_plan {
+    KParams base;
+    int sm_count = 0;
+    int launches = 0;
+    // device scratch (grown on demand)
+    void *meta = nullptr; size_t meta_cap = 0;
+    void *items = nullptr; size_t items_cap = 0;
+    int *counters = nullptr;
+    float *lat = nullptr; size_t lat_cap = 0;
+    int *lat_exp = nullptr; size_t latE_cap = 0;
+    float *edge = nullptr; size_t edge_cap = 0;
+    int *edge_exp = nullptr; size_t edgeE_cap = 0;
+    int *progress = nullptr; size_t prog_cap = 0;
+    std::vector<PairMeta> h_meta;
+    std::vector<int2> h_items;
+    // optional per-kernel CUDA-event timing on the launching stream
+    bool timing = false;
+    bool timed_bwd = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace {
+
+template <typename T>
+int ensure(T **ptr, size_t *cap, size_t n) {
+    if (n <= *cap && *ptr) return 0;
+    size_t want = std::max(n, (size_t)(*cap * 3 / 2));
+    if (*ptr) { cudaDeviceSynchronize(); cudaFree(*ptr); *ptr = nullptr; *cap = 0; }
+    cudaError_t e = cudaMalloc((void **)ptr, std::max<size_t>(want, 1) * sizeof(T));
+    if (e != cudaSuccess) return fail(PHMM_E_CUDA, std::string("cudaMalloc scratch: ") + cudaGetErrorString(e));
+    *cap = want;
+    return 0;
+}
+
+int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_trans,
+        double *cntM, double *cntI, double *cntD, int32_t *status, double *F_log, double *B_log,
+        double *post, void *stream_) {
+    if (!plan || !b) return fail(PHMM_E_ARG, "null plan or batch");
+    cudaStream_t stream = (cudaStream_t)stream_;
+    plan->launches = 0;
+    const int P_ = b->n_pairs;
+    if (P_ < 0) return fail(PHMM_E_ARG, "n_pairs < 0");
+    if (P_ == 0) return 0;
+    if (!b->Lx_host || !b->Ly_host || !b->x_off_host || !b->y_off_host || !b->residues || !b->chi ||
+        !b->emit_M || !b->emit_I || !b->emit_D || !ll || !status)
+        return fail(PHMM_E_ARG, "null batch pointer");
+    if (estep && (!n_trans || !cntM || !cntI || !cntD)) return fail(PHMM_E_ARG, "null E-step output");
+    KParams K = plan->base;
+    const int N = K.N, NS = K.NS, G = K.G;
+    // ---- plan: stripes, offsets, longest-first order
+    std::vector<int> order(P_);
+    for (int p = 0; p < P_; ++p) {
+        if (b->Lx_host[p] < 0 || b->Ly_host[p] < 0) return fail(PHMM_E_ARG, "negative length");
+        order[p] = p;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+        return (int64_t)(b->Lx_host[a] + 1) * (b->Ly_host[a] + 1) >
+               (int64_t)(b->Lx_host[c] + 1) * (b->Ly_host[c] + 1);
+    });
+    plan->h_meta.resize(P_);
+    int64_t lat_cells = 0, edge_cells = 0, tab_cells = 0;
+    int stripes = 0, max_ly = 0;
+    for (int p = 0; p < P_; ++p) {
+        PairMeta &m = plan->h_meta[p];
+        m.Lx = b->Lx_host[p];
+        m.Ly = b->Ly_host[p];
+        m.x_off = b->x_off_host[p];
+        m.y_off = b->y_off_host[p];
+        m.n_stripes = (m.Lx + 1 + TH - 1) / TH;
+        m.stripe_base = stripes;
+        m.lat_base = lat_cells;
+        m.edge_base = edge_cells;
+        m.tab_base = tab_cells;
+        stripes += m.n_stripes;
+        if (estep) lat_cells += (int64_t)m.n_stripes * (TH + m.Ly) * TH;
+        edge_cells += (int64_t)m.n_stripes * (m.Ly + 1);
+        tab_cells += (int64_t)(m.Lx + 1) * (m.Ly + 1);
+        max_ly = std::max(max_ly, m.Ly);
+    }
+    plan->h_items.clear();
+    for (int p : order)
+        for (int s = 0; s < plan->h_meta[p].n_stripes; ++s) plan->h_items.push_back(make_int2(p, s));
+    const int n_items = (int)plan->h_items.size();
+    int rc;
+    if ((rc = ensure((char **)&plan->meta, &plan->meta_cap, sizeof(PairMeta) * P_))) return rc;
+    if ((rc = ensure((char **)&plan->items, &plan->items_cap, sizeof(int2) * 2 * n_items))) return rc;
+    if ((rc = ensure(&plan->edge, &plan->edge_cap, (size_t)edge_cells * NS))) return rc;
+    if ((rc = ensure(&plan->edge_exp, &plan->edgeE_cap, (size_t)edge_cells))) return rc;
+    if ((rc = ensure(&plan->progress, &plan->prog_cap, (size_t)2 * stripes))) return rc;
+    if (estep) {
+        if ((rc = ensure(&plan->lat, &plan->lat_cap, (size_t)lat_cells * NS))) return rc;
+        if ((rc = ensure(&plan->lat_exp, &plan->latE_cap, (size_t)lat_cells))) return rc;
+    }
+    // backward items: same pair order, stripes bottom-up
+    std::vector<int2> bitems;
+    if (estep) {
+        for (int p : order)
+            for (int s = plan->h_meta[p].n_stripes - 1; s >= 0; --s) bitems.push_back(make_int2(p, s));
+    }
+    CUDA_TRY(cudaMemcpyAsync(plan->meta, plan->h_meta.data(), sizeof(PairMeta) * P_, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(plan->items, plan->h_items.data(), sizeof(int2) * n_items, cudaMemcpyHostToDevice, stream));
+    if (estep)
+        CUDA_TRY(cudaMemcpyAsync((int2 *)plan->items + n_items, bitems.data(), sizeof(int2) * n_items,
+                                 cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 2 * sizeof(int), stream));
+    CUDA_TRY(cudaMemsetAsync(plan->progress, 0, sizeof(int) * 2 * stripes, stream));
+    CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int32_t) * P_, stream));
+    if (estep) {
+        CUDA_TRY(cudaMemsetAsync(n_trans, 0, sizeof(double) * (size_t)P_ * N * N, stream));
+        CUDA_TRY(cudaMemsetAsync(cntM, 0, sizeof(double) * (size_t)P_ * G * 441, stream));
+        CUDA_TRY(cudaMemsetAsync(cntI, 0, sizeof(double) * (size_t)P_ * G * 21, stream));
+        CUDA_TRY(cudaMemsetAsync(cntD, 0, sizeof(double) * (size_t)P_ * G * 21, stream));
+    }
+    if (F_log) { fill_f64<<<256, 256, 0, stream>>>(F_log, tab_cells * N, NEG_INF_LL); plan->launches++; }
+    if (B_log) { fill_f64<<<256, 256, 0, stream>>>(B_log, tab_cells * N, NEG_INF_LL); plan->launches++; }
+    if (post) CUDA_TRY(cudaMemsetAsync(post, 0, sizeof(double) * (size_t)tab_cells * N, stream));
+
+    K.res = b->residues;
+    K.meta = (const PairMeta *)plan->meta;
+    K.n_items = n_items;
+    K.chi = b->chi;
+    K.chi_stride = b->chi_per_pair ? (int64_t)N * N : 0;
+    K.eM = b->emit_M;
+    K.eI = b->emit_I;
+    K.eD = b->emit_D;
+    K.eM_stride = b->emit_per_pair ? (int64_t)G * 441 : 0;
+    K.eID_stride = b->emit_per_pair ? (int64_t)G * 21 : 0;
+    K.lat = estep ? plan->lat : nullptr;
+    K.lat_exp = estep ? plan->lat_exp : nullptr;
+    K.edge = plan->edge;
+    K.edge_exp = plan->edge_exp;
+    K.ll = ll;
+    K.status = status;
+    K.n_trans = n_trans;
+    K.cntM = cntM;
+    K.cntI = cntI;
+    K.cntD = cntD;
+    K.F_log = F_log;
+    K.B_log = B_log;
+    K.post = post;
+    K.max_ly = max_ly;
+    K.spin_limit = 40LL * 1000 * 1000;
+    const int threads = 32 * K.NQ;
+    // forward
+    {
+        const SmemLayout L = make_layout(K.NS, K.NQ, G, max_ly, false);
+        CUDA_TRY(cudaFuncSetAttribute(forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
+        int occ = 0;
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, forward_kernel, threads, L.bytes));
+        if (occ < 1) return fail(PHMM_E_ARG, "forward kernel does not fit on an SM (shared memory)");
+        K.items = (const int2 *)plan->items;
+        K.counter = plan->counters;
+        K.progress = plan->progress;
+        const int grid = std::min(n_items, plan->sm_count * occ);
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
+        forward_kernel<<<grid, threads, L.bytes, stream>>>(K);
+        CUDA_TRY(cudaGetLastError());
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[1], stream));
+        plan->launches++;
+    }
+    if (estep) {
+        const SmemLayout L = make_layout(K.NS, K.NQ, G, max_ly, true);
+        CUDA_TRY(cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
+        int occ = 0;
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, backward_kernel, threads, L.bytes));
+        if (occ < 1) return fail(PHMM_E_ARG, "backward kernel does not fit on an SM (shared memory)");
+        K.items = (const int2 *)plan->items + n_items;
+        K.counter = plan->counters + 1;
+        K.progress = plan->progress + stripes;
+        const int grid = std::min(n_items, plan->sm_count * occ);
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[2], stream));
+        backward_kernel<<<grid, threads, L.bytes, stream>>>(K);
+        CUDA_TRY(cudaGetLastError());
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[3], stream));
+        plan->launches++;
+    }
+    plan->timed_bwd = estep;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int phmm_version(void) { return 1; }
+
+int phmm_last_error(char *buf, size_t len) {
+    if (buf && len) {
+        size_t n = std::min(len - 1, g_err.size());
+        memcpy(buf, g_err.data(), n);
+        buf[n] = 0;
+    }
+    return (int)g_err.size();
+}
+
+int phmm_plan_create(const phmm_model_desc *md, phmm_plan **out) {
+    if (!md || !out || !md->state_types || md->n_states < 2) return fail(PHMM_E_ARG, "bad model description");
+    const int N = md->n_states;
+    if (md->state_types[0] != T_S) return fail(PHMM_E_ARG, "state 0 must be the start state (type S)");
+    int e_idx = -1;
+    for (int k = 0; k < N; ++k)
+        if (md->state_types[k] == T_E) { e_idx = k; break; }
+    if (e_idx < 0) return fail(PHMM_E_ARG, "no End (type E) state");
+    if (md->n_groups < 1 || md->n_groups > 64) return fail(PHMM_E_ARG, "n_groups must be in 1..64");
+    std::vector<int> byType[3];
+    for (int k = 0; k < N; ++k) {
+        int t = md->state_types[k];
+        if (t == T_M || t == T_I || t == T_D) {
+            int g = md->state_group ? md->state_group[k] : 0;
+            if (g < 0 || g >= md->n_groups) return fail(PHMM_E_ARG, "state group out of range");
+            byType[t - 1].push_back(k);
+        } else if (t < 0 || t > T_E) {
+            return fail(PHMM_E_ARG, "unknown state type");
+        }
+    }
+    KParams K;
+    memset(&K, 0, sizeof(K));
+    std::vector<int> slot_orig, slot_type;
+    int s_slot = -1;
+    for (int ty = 0; ty < 3; ++ty) {
+        K.kbeg[ty] = (int)slot_orig.size();
+        for (int k : byType[ty]) { slot_orig.push_back(k); slot_type.push_back(ty + 1); }
+        while (slot_orig.size() % 4) {
+            if (s_slot < 0) { s_slot = (int)slot_orig.size(); slot_orig.push_back(0); slot_type.push_back(T_S); }
+            else { slot_orig.push_back(-1); slot_type.push_back(T_NONE); }
+        }
+        K.kend[ty] = (int)slot_orig.size();
+    }
+    if (s_slot < 0) {
+        s_slot = (int)slot_orig.size();
+        slot_orig.push_back(0); slot_type.push_back(T_S);
+        while (slot_orig.size() % 4) { slot_orig.push_back(-1); slot_type.push_back(T_NONE); }
+    }
+    const int NS = (int)slot_orig.size();
+    if (NS > MAXS) return fail(PHMM_E_ARG, "too many emitting states for this build (max 60)");
+    K.N = N;
+    K.NS = NS;
+    K.NQ = NS / 4;
+    K.G = md->n_groups;
+    K.e_idx = e_idx;
+    K.s_slot = s_slot;
+    for (int s = 0; s < NS; ++s) {
+        K.slot_orig[s] = (int16_t)slot_orig[s];
+        K.slot_type[s] = (int8_t)slot_type[s];
+        int g = 0;
+        if (slot_type[s] >= T_M && slot_type[s] <= T_D && md->state_group) g = md->state_group[slot_orig[s]];
+        K.slot_group[s] = (int16_t)g;
+    }
+    for (int q = 0; q < K.NQ; ++q) {
+        int t = T_NONE;
+        for (int ty = 0; ty < 3; ++ty)
+            if (4 * q >= K.kbeg[ty] && 4 * q < K.kend[ty]) t = ty + 1;
+        K.quad_type[q] = (int8_t)t;
+    }
+    phmm_plan *plan = new phmm_plan();
+    plan->base = K;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&plan->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&plan->counters, 4 * sizeof(int));
+    if (e != cudaSuccess) {
+        delete plan;
+        return fail(PHMM_E_CUDA, std::string("plan create: ") + cudaGetErrorString(e));
+    }
+    *out = plan;
+    return 0;
+}
+
+int phmm_set_timing(phmm_plan *plan, int enable) {
+    if (!plan) return fail(PHMM_E_ARG, "null plan");
+    if (enable && !plan->ev[0]) {
+        for (int k = 0; k < 4; ++k) CUDA_TRY(cudaEventCreate(&plan->ev[k]));
+    }
+    plan->timing = enable != 0;
+    return 0;
+}
+
+int phmm_kernel_times(phmm_plan *plan, float *fwd_ms, float *bwd_ms) {
+    if (!plan || !plan->timing) return fail(PHMM_E_ARG, "timing is not enabled on this plan");
+    float a = 0.f, b = 0.f;
+    CUDA_TRY(cudaEventSynchronize(plan->ev[1]));
+    CUDA_TRY(cudaEventElapsedTime(&a, plan->ev[0], plan->ev[1]));
+    if (plan->timed_bwd) {
+        CUDA_TRY(cudaEventSynchronize(plan->ev[3]));
+        CUDA_TRY(cudaEventElapsedTime(&b, plan->ev[2], plan->ev[3]));
+    }
+    if (fwd_ms) *fwd_ms = a;
+    if (bwd_ms) *bwd_ms = b;
+    return 0;
+}
+
+void phmm_plan_destroy(phmm_plan *plan) {
+    if (!plan) return;
+    cudaDeviceSynchronize();
+    for (int k = 0; k < 4; ++k)
+        if (plan->ev[k]) cudaEventDestroy(plan->ev[k]);
+    cudaFree(plan->meta);
+    cudaFree(plan->items);
+    cudaFree(plan->counters);
+    cudaFree(plan->lat);
+    cudaFree(plan->lat_exp);
+    cudaFree(plan->edge);
+    cudaFree(plan->edge_exp);
+    cudaFree(plan->progress);
+    delete plan;
+}
+
+int phmm_forward(phmm_plan *plan, const phmm_batch *batch, double *ll_out, int32_t *status_out,
+                 void *stream) {
+    return run(plan, batch, false, ll_out, nullptr, nullptr, nullptr, nullptr, status_out, nullptr,
+               nullptr, nullptr, stream);
+}
+
+int phmm_estep(phmm_plan *plan, const phmm_batch *batch, double *ll_out, double *n_trans, double *cnt_M,
+               double *cnt_I, double *cnt_D, int32_t *status_out, void *stream) {
+    return run(plan, batch, true, ll_out, n_trans, cnt_M, cnt_I, cnt_D, status_out, nullptr, nullptr,
+               nullptr, stream);
+}
+
+int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch, double *ll_out, double *n_trans,
+                      double *cnt_M, double *cnt_I, double *cnt_D, int32_t *status_out, double *log_F,
+                      double *log_B, double *post, void *stream) {
+    return run(plan, batch, true, ll_out, n_trans, cnt_M, cnt_I, cnt_D, status_out, log_F, log_B, post,
+               stream);
+}
+
+int phmm_last_launch_count(const phmm_plan *plan) { return plan ? plan->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,274 @@
+"""ctypes binding of the C ABI in include/pairhmm.h.
+
+This is the only place the Python host touches the CUDA library.  Every
+compute call goes through ``libpairhmm.so``; when the library is missing the
+calls raise instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from .build import LIB_PATH
+
+_LIB = None
+
+EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep',
+           'phmm_estep_tables', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_last_launch_count',
+           'phmm_last_error', 'phmm_version')
+
+
+class ModelDesc(ctypes.Structure):
+    _fields_ = [('n_states', ctypes.c_int32),
+                ('state_types', ctypes.POINTER(ctypes.c_int8)),
+                ('state_group', ctypes.POINTER(ctypes.c_int32)),
+                ('n_groups', ctypes.c_int32)]
+
+
+class Batch(ctypes.Structure):
+    _fields_ = [('n_pairs', ctypes.c_int32),
+                ('Lx_host', ctypes.POINTER(ctypes.c_int32)),
+                ('Ly_host', ctypes.POINTER(ctypes.c_int32)),
+                ('residues', ctypes.c_void_p),
+                ('x_off_host', ctypes.POINTER(ctypes.c_int64)),
+                ('y_off_host', ctypes.POINTER(ctypes.c_int64)),
+                ('chi', ctypes.c_void_p),
+                ('chi_per_pair', ctypes.c_int32),
+                ('emit_M', ctypes.c_void_p),
+                ('emit_I', ctypes.c_void_p),
+                ('emit_D', ctypes.c_void_p),
+                ('emit_per_pair', ctypes.c_int32)]
+
+
+class PairHMMError(RuntimeError):
+    pass
+
+
+def load(path=None):
+    """Load libpairhmm.so (built in-tree by pairhmm.build / __graft_entry__.build)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise PairHMMError(f'CUDA library not built: {path} is missing '
+                           '(run `python -c "import __graft_entry__ as g; g.build()"`)')
+    lib = ctypes.CDLL(path)
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+    lib.phmm_plan_create.argtypes = [ctypes.POINTER(ModelDesc), ctypes.POINTER(vp)]
+    lib.phmm_plan_create.restype = ctypes.c_int
+    lib.phmm_plan_destroy.argtypes = [vp]
+    lib.phmm_plan_destroy.restype = None
+    lib.phmm_forward.argtypes = [vp, ctypes.POINTER(Batch), vp, vp, vp]
+    lib.phmm_forward.restype = ctypes.c_int
+    lib.phmm_estep.argtypes = [vp, ctypes.POINTER(Batch), vp, vp, vp, vp, vp, vp, vp]
+    lib.phmm_estep.restype = ctypes.c_int
+    lib.phmm_estep_tables.argtypes = [vp, ctypes.POINTER(Batch)] + [vp] * 10
+    lib.phmm_estep_tables.restype = ctypes.c_int
+    lib.phmm_set_timing.argtypes = [vp, ctypes.c_int]
+    lib.phmm_set_timing.restype = ctypes.c_int
+    lib.phmm_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+    lib.phmm_kernel_times.restype = ctypes.c_int
+    lib.phmm_last_launch_count.argtypes = [vp]
+    lib.phmm_last_launch_count.restype = ctypes.c_int
+    lib.phmm_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    lib.phmm_last_error.restype = ctypes.c_int
+    lib.phmm_version.argtypes = []
+    lib.phmm_version.restype = ctypes.c_int
+    _LIB = lib
+    return lib
+
+
+def last_error():
+    lib = load()
+    buf = ctypes.create_string_buffer(1024)
+    lib.phmm_last_error(buf, 1024)
+    return buf.value.decode()
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise PairHMMError(f'{what} failed ({rc}): {last_error()}')
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+class Plan:
+    """A plan for one pair-HMM state space (phmm_plan_create)."""
+
+    def __init__(self, state_types, state_groups, n_groups):
+        self.lib = load()
+        st = np.ascontiguousarray(np.asarray(state_types, dtype=np.int8))
+        gr = np.ascontiguousarray(np.asarray(state_groups, dtype=np.int32))
+        self.n_states = int(st.size)
+        self.n_groups = int(n_groups)
+        self._st, self._gr = st, gr
+        desc = ModelDesc(self.n_states, st.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)),
+                         gr.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), self.n_groups)
+        h = ctypes.c_void_p()
+        _check(self.lib.phmm_plan_create(ctypes.byref(desc), ctypes.byref(h)), 'phmm_plan_create')
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, 'handle', None)
+        if h is not None and h.value:
+            try:
+                self.lib.phmm_plan_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    @property
+    def launches(self):
+        return self.lib.phmm_last_launch_count(self.handle)
+
+    def set_timing(self, enable=True):
+        _check(self.lib.phmm_set_timing(self.handle, int(enable)), 'phmm_set_timing')
+
+    def kernel_times(self):
+        """(forward_ms, backward_ms) of the last call (CUDA events on its stream)."""
+        a, b = ctypes.c_float(), ctypes.c_float()
+        _check(self.lib.phmm_kernel_times(self.handle, ctypes.byref(a), ctypes.byref(b)),
+               'phmm_kernel_times')
+        return float(a.value), float(b.value)
+
+
+@dataclass
+class DeviceBatch:
+    """Device-resident inputs of one batch plus the host length arrays."""
+    Lx: np.ndarray
+    Ly: np.ndarray
+    x_off: np.ndarray
+    y_off: np.ndarray
+    residues: torch.Tensor      # uint8 [total]
+    chi: torch.Tensor           # float32 [P or 1, N, N]
+    emit_M: torch.Tensor        # float32 [P or 1, G, 21, 21]
+    emit_I: torch.Tensor        # float32 [P or 1, G, 21]
+    emit_D: torch.Tensor        # float32 [P or 1, G, 21]
+    _struct: Batch = field(default=None, repr=False)
+
+    @property
+    def n_pairs(self):
+        return int(self.Lx.size)
+
+    def struct(self):
+        if self._struct is None:
+            P = self.n_pairs
+            self._struct = Batch(
+                P,
+                self.Lx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                self.Ly.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                ctypes.c_void_p(self.residues.data_ptr()),
+                self.x_off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                self.y_off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                ctypes.c_void_p(self.chi.data_ptr()),
+                int(self.chi.shape[0] == P),
+                ctypes.c_void_p(self.emit_M.data_ptr()),
+                ctypes.c_void_p(self.emit_I.data_ptr()),
+                ctypes.c_void_p(self.emit_D.data_ptr()),
+                int(self.emit_M.shape[0] == P))
+        return self._struct
+
+
+def pack_residues(xs, ys):
+    """Concatenate residues of all pairs: [x_0, y_0, x_1, y_1, ...] (uint8)."""
+    parts, xo, yo = [], [], []
+    off = 0
+    for x, y in zip(xs, ys):
+        x = np.asarray(x, dtype=np.int64)
+        y = np.asarray(y, dtype=np.int64)
+        if (x.size and (x.min() < 0 or x.max() > 20)) or (y.size and (y.min() < 0 or y.max() > 20)):
+            raise ValueError('residues must be integers in 0..20 (20 = wildcard)')
+        xo.append(off)
+        parts.append(x.astype(np.uint8))
+        off += x.size
+        yo.append(off)
+        parts.append(y.astype(np.uint8))
+        off += y.size
+    buf = np.concatenate(parts) if parts else np.zeros(0, np.uint8)
+    if buf.size == 0:
+        buf = np.zeros(16, np.uint8)
+    return (buf, np.asarray(xo, np.int64), np.asarray(yo, np.int64),
+            np.asarray([len(x) for x in xs], np.int32), np.asarray([len(y) for y in ys], np.int32))
+
+
+def make_batch(xs, ys, chi, emit_M, emit_I, emit_D, device='cuda'):
+    """Build a DeviceBatch from host sequences and float tables.
+
+    chi: [P or 1, N, N]; emit_*: [P or 1, G, ...] (numpy or torch, any float)."""
+    buf, xo, yo, Lx, Ly = pack_residues(xs, ys)
+
+    def dev(a, dt):
+        t = torch.as_tensor(np.asarray(a) if not isinstance(a, torch.Tensor) else a)
+        return t.to(device=device, dtype=dt).contiguous()
+    return DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo,
+                       residues=dev(buf, torch.uint8), chi=dev(chi, torch.float32),
+                       emit_M=dev(emit_M, torch.float32), emit_I=dev(emit_I, torch.float32),
+                       emit_D=dev(emit_D, torch.float32))
+
+
+def forward(plan, batch, stream=None):
+    """phmm_forward -> (ll float64 [P] tensor, status int32 [P] tensor) on the device."""
+    P = batch.n_pairs
+    dev = batch.residues.device
+    ll = torch.empty(P, dtype=torch.float64, device=dev)
+    st = torch.empty(P, dtype=torch.int32, device=dev)
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    _check(plan.lib.phmm_forward(plan.handle, ctypes.byref(batch.struct()), _ptr(ll), _ptr(st),
+                                 ctypes.c_void_p(s.cuda_stream)), 'phmm_forward')
+    return ll, st
+
+
+def estep(plan, batch, stream=None, out=None):
+    """phmm_estep -> dict of device tensors (ll, n_trans, cnt_M, cnt_I, cnt_D, status)."""
+    P = batch.n_pairs
+    N, G = plan.n_states, plan.n_groups
+    dev = batch.residues.device
+    if out is None:
+        out = {
+            'll': torch.empty(P, dtype=torch.float64, device=dev),
+            'n_trans': torch.empty(P, N, N, dtype=torch.float64, device=dev),
+            'cnt_M': torch.empty(P, G, 21, 21, dtype=torch.float64, device=dev),
+            'cnt_I': torch.empty(P, G, 21, dtype=torch.float64, device=dev),
+            'cnt_D': torch.empty(P, G, 21, dtype=torch.float64, device=dev),
+            'status': torch.empty(P, dtype=torch.int32, device=dev),
+        }
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    _check(plan.lib.phmm_estep(plan.handle, ctypes.byref(batch.struct()), _ptr(out['ll']),
+                               _ptr(out['n_trans']), _ptr(out['cnt_M']), _ptr(out['cnt_I']),
+                               _ptr(out['cnt_D']), _ptr(out['status']),
+                               ctypes.c_void_p(s.cuda_stream)), 'phmm_estep')
+    return out
+
+
+def estep_tables(plan, batch, want_F=True, want_B=True, want_post=True, stream=None):
+    """phmm_estep_tables: E-step plus full lattice tables (API-parity path)."""
+    P = batch.n_pairs
+    N = plan.n_states
+    dev = batch.residues.device
+    cells = int(((batch.Lx.astype(np.int64) + 1) * (batch.Ly.astype(np.int64) + 1)).sum())
+    G = plan.n_groups
+    out = {
+        'll': torch.empty(P, dtype=torch.float64, device=dev),
+        'n_trans': torch.empty(P, N, N, dtype=torch.float64, device=dev),
+        'cnt_M': torch.empty(P, G, 21, 21, dtype=torch.float64, device=dev),
+        'cnt_I': torch.empty(P, G, 21, dtype=torch.float64, device=dev),
+        'cnt_D': torch.empty(P, G, 21, dtype=torch.float64, device=dev),
+        'status': torch.empty(P, dtype=torch.int32, device=dev),
+        'log_F': torch.empty(cells, N, dtype=torch.float64, device=dev) if want_F else None,
+        'log_B': torch.empty(cells, N, dtype=torch.float64, device=dev) if want_B else None,
+        'post': torch.empty(cells, N, dtype=torch.float64, device=dev) if want_post else None,
+    }
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    _check(plan.lib.phmm_estep_tables(
+        plan.handle, ctypes.byref(batch.struct()), _ptr(out['ll']), _ptr(out['n_trans']),
+        _ptr(out['cnt_M']), _ptr(out['cnt_I']), _ptr(out['cnt_D']), _ptr(out['status']),
+        _ptr(out['log_F']), _ptr(out['log_B']), _ptr(out['post']),
+        ctypes.c_void_p(s.cuda_stream)), 'phmm_estep_tables')
+    return out

@@ -1,0 +1,502 @@
+"""Reference-facing API of the 2D pair-HMM hot path.
+
+Drop-in counterparts (same names, argument meaning, output layouts and dict
+keys) of the reference's 2D pair-HMM entry points in
+evoldoers/tkf-mixdom python/tkfmixdom/jax:
+
+  forward_2d, backward_2d, forward_backward_2d   (dp/hmm.py:1775-1973)
+  e_step, e_step_mixdom2, observed_ll           (train/likelihood.py:49-460)
+  mixdom2_log_prob, tkf91_log_prob, tkf92_log_prob (train/vjp.py: custom VJPs)
+  estep_batch_tkf92, estep_batch_tkf92_forward_only (train/tkf92_svi_bw.py:263-365)
+
+plus the batched MixDom2 E-step ``estep_batch_mixdom2`` that replaces the
+bucketed jit(vmap(...)) callers (train_pfam.py:1674-1741, 2672-2907).
+
+All dynamic programming runs in the CUDA library (libpairhmm.so) through
+the C ABI; this module only builds float64 model tables (pairhmm.models),
+packs batches and runs float64 epilogues.  Numerical failure is reported the
+reference's way: a log-likelihood of NEG_INF (-1e30).
+"""
+from __future__ import annotations
+
+import functools
+import math
+import os
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import models as pm
+
+NEG_INF = -1e30
+S, M, I, D, E = pm.S, pm.M, pm.I, pm.D, pm.E
+
+
+def _device():
+    if not torch.cuda.is_available():
+        raise _lib.PairHMMError('the pair-HMM library needs a CUDA device')
+    return torch.device('cuda', torch.cuda.current_device())
+
+
+# ---------------------------------------------------------------- padding semantics
+def _make_geom_bins(base=4, max_bin=4096, mult=1.2):
+    """Geometric bins of dp/hmm.py:43-63 (used only to shape padded outputs)."""
+    bins = [int(base)]
+    val = float(base)
+    while val < max_bin:
+        val *= mult
+        b = int(round(val))
+        if b > bins[-1]:
+            bins.append(b)
+    if bins[-1] < max_bin:
+        bins.append(int(max_bin))
+    return bins
+
+
+_GEOM_BINS = [0, 1, 2, 3] + _make_geom_bins()
+
+
+def pad_to_bin(n):
+    """Padded size of dp/hmm.py:66-91 (TKFMIXDOM_MAX_PAD honoured)."""
+    n = max(int(n), 1)
+    cap = os.environ.get('TKFMIXDOM_MAX_PAD')
+    if cap is not None:
+        cap = int(cap)
+        if n > cap:
+            raise ValueError(f'_pad_to_bin: n={n} exceeds TKFMIXDOM_MAX_PAD={cap}')
+        return max(min(((n + 31) // 32) * 32, cap), 1)
+    for b in _GEOM_BINS:
+        if b >= n:
+            return b
+    return int(2 ** math.ceil(math.log2(n)))
+
+
+# ---------------------------------------------------------------- plans
+@functools.lru_cache(maxsize=64)
+def _plan(state_types_key, groups_key, G):
+    return _lib.Plan(np.frombuffer(state_types_key, dtype=np.int8),
+                     np.frombuffer(groups_key, dtype=np.int32), G)
+
+
+def get_plan(state_types, groups, G):
+    st = np.ascontiguousarray(np.asarray(state_types, dtype=np.int8))
+    gr = np.ascontiguousarray(np.asarray(groups, dtype=np.int32))
+    return _plan(st.tobytes(), gr.tobytes(), int(G))
+
+
+def _chi_from_log(log_trans):
+    lt = np.asarray(log_trans, dtype=np.float64)
+    return np.where(lt > -1e29, np.exp(np.minimum(lt, 700.0)), 0.0)
+
+
+def _groups_from_table(log_emit, state_types, x, y):
+    """Recover per-group character tables from a (Lx+1, Ly+1, N) log
+    emission table whose entries depend on the cell only through its
+    characters (true of every emission builder of the reference)."""
+    st = np.asarray(state_types)
+    Lx, Ly = len(x), len(y)
+    em = np.exp(np.asarray(log_emit, dtype=np.float64)[:Lx + 1, :Ly + 1])
+    xg = np.concatenate([[0], np.asarray(x, int)])
+    yg = np.concatenate([[0], np.asarray(y, int)])
+    groups = np.zeros(st.size, dtype=np.int32)
+    tabs = []
+    keys = []
+    for k in range(st.size):
+        if st[k] not in (M, I, D):
+            continue
+        TM = np.ones((21, 21))
+        TI = np.ones(21)
+        TD = np.ones(21)
+        if st[k] == M:
+            v = em[1:, 1:, k]
+            TM[xg[1:, None], yg[None, 1:]] = v
+            ok = np.allclose(TM[xg[1:, None], yg[None, 1:]], v, rtol=1e-12, atol=0)
+        elif st[k] == I:
+            v = em[:, 1:, k]
+            TI[yg[1:]] = v[0]
+            ok = np.allclose(TI[yg[1:]][None, :], v, rtol=1e-12, atol=0)
+        else:
+            v = em[1:, :, k]
+            TD[xg[1:]] = v[:, 0]
+            ok = np.allclose(TD[xg[1:]][:, None], v, rtol=1e-12, atol=0)
+        if not ok:
+            raise NotImplementedError('log_emit_table entries must depend on the cell only '
+                                      'through its characters (per-cell tables are not supported)')
+        key = (st[k], TM.tobytes() if st[k] == M else (TI.tobytes() if st[k] == I else TD.tobytes()))
+        # one group per state keeps the M/I/D tables of a group independent
+        tabs.append((st[k], TM, TI, TD))
+        keys.append(key)
+        groups[k] = len(tabs) - 1
+    G = max(len(tabs), 1)
+    EM = np.ones((G, 21, 21))
+    EI = np.ones((G, 21))
+    ED = np.ones((G, 21))
+    for g, (t, TM, TI, TD) in enumerate(tabs):
+        EM[g], EI[g], ED[g] = TM, TI, TD
+    return groups, EM, EI, ED
+
+
+def _run_single_tables(chi, st, groups, EM, EI, ED, x, y, forward_only=False):
+    dev = _device()
+    plan = get_plan(st, groups, EM.shape[0])
+    b = _lib.make_batch([x], [y], np.asarray(chi)[None], np.asarray(EM)[None],
+                        np.asarray(EI)[None], np.asarray(ED)[None], device=dev)
+    out = _lib.estep_tables(plan, b, want_F=True, want_B=not forward_only,
+                            want_post=not forward_only)
+    Lx, Ly = len(x), len(y)
+    N = len(st)
+    res = {'ll': float(out['ll'][0]), 'status': int(out['status'][0]),
+           'n_trans': out['n_trans'][0].cpu().numpy(),
+           'cnt_M': out['cnt_M'][0].cpu().numpy(), 'cnt_I': out['cnt_I'][0].cpu().numpy(),
+           'cnt_D': out['cnt_D'][0].cpu().numpy(),
+           'F': out['log_F'].cpu().numpy().reshape(Lx + 1, Ly + 1, N)}
+    if not forward_only:
+        res['B'] = out['log_B'].cpu().numpy().reshape(Lx + 1, Ly + 1, N)
+        res['post'] = out['post'].cpu().numpy().reshape(Lx + 1, Ly + 1, N)
+    return res
+
+
+def _tkf_tables(sub_matrix, pi):
+    EM, EI, ED = pm.tables_tkf(sub_matrix, pi)
+    return EM.numpy(), EI.numpy(), ED.numpy()
+
+
+# ---------------------------------------------------------------- dp/hmm.py API
+def forward_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi):
+    """(log P(x,y), F (Lx+1, Ly+1, N) log forward table) -- dp/hmm.py:1775-1801."""
+    st = np.asarray(state_types)
+    EM, EI, ED = _tkf_tables(sub_matrix, pi)
+    r = _run_single_tables(_chi_from_log(log_trans), st, np.zeros(st.size, np.int32), EM, EI, ED,
+                           np.asarray(x_seq), np.asarray(y_seq), forward_only=True)
+    return r['ll'], r['F']
+
+
+def backward_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi):
+    """B (Lx+1, Ly+1, N) log backward table -- dp/hmm.py:1804-1824.  Rows of
+    states that are neither emitting nor the start state are NEG_INF."""
+    st = np.asarray(state_types)
+    EM, EI, ED = _tkf_tables(sub_matrix, pi)
+    r = _run_single_tables(_chi_from_log(log_trans), st, np.zeros(st.size, np.int32), EM, EI, ED,
+                           np.asarray(x_seq), np.asarray(y_seq))
+    return r['B']
+
+
+def forward_backward_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi,
+                        log_emit_table=None, real_Lx=None, real_Ly=None, forward_only=False):
+    """(log_prob, posteriors, expected_trans) -- dp/hmm.py:1834-1973.
+
+    Posteriors are returned at the reference's padded shape
+    (pad_to_bin(Lx)+1, pad_to_bin(Ly)+1, N), zero outside the real region.
+    real_Lx/real_Ly mark x_seq/y_seq as pre-padded."""
+    st = np.asarray(state_types)
+    x = np.asarray(x_seq)
+    y = np.asarray(y_seq)
+    Lx_arr, Ly_arr = x.shape[0], y.shape[0]
+    Lx = Lx_arr if real_Lx is None else int(real_Lx)
+    Ly = Ly_arr if real_Ly is None else int(real_Ly)
+    xr, yr = x[:Lx], y[:Ly]
+    if log_emit_table is not None:
+        groups, EM, EI, ED = _groups_from_table(log_emit_table, st, xr, yr)
+    else:
+        groups = np.zeros(st.size, np.int32)
+        EM, EI, ED = _tkf_tables(sub_matrix, pi)
+    r = _run_single_tables(_chi_from_log(log_trans), st, groups, EM, EI, ED, xr, yr,
+                           forward_only=forward_only)
+    if forward_only:
+        return r['ll']
+    post = np.zeros((pad_to_bin(Lx_arr) + 1, pad_to_bin(Ly_arr) + 1, st.size))
+    post[:Lx + 1, :Ly + 1] = r['post']
+    return r['ll'], post, r['n_trans']
+
+
+# ---------------------------------------------------------------- E-steps
+def _tkf_model(model, params):
+    t = params['t']
+    if model in ('tkf91',):
+        chi = pm.tkf91_trans(params['ins_rate'], params['del_rate'], t)
+    elif model == 'tkf92':
+        chi = pm.tkf92_trans(params['ins_rate'], params['del_rate'], t, params['ext'])
+    else:
+        raise ValueError(f'Unknown model: {model}')
+    sub = pm.transition_matrix(params['Q'], t)
+    EM, EI, ED = pm.tables_tkf(sub, params['pi'])
+    st = np.array([S, M, I, D, E], np.int8)
+    return chi.numpy(), st, np.zeros(5, np.int32), EM.numpy(), EI.numpy(), ED.numpy()
+
+
+def _mixdom1_model(params):
+    t = params['t']
+    K = len(params['dom_ins'])
+    F = np.asarray(params['frag_weights']).shape[1]
+    chi = pm.build_nested_trans(params['main_ins'], params['main_del'], t, params['dom_ins'],
+                                params['dom_del'], params['dom_weights'], params['frag_weights'],
+                                params['ext_rates'])
+    sub = pm.transition_matrix(params['Q'], t)
+    EM, EI, ED = pm.tables_tkf(sub, params['pi'])
+    return (chi.numpy(), pm.mixdom_state_types(K, F), np.zeros(pm.mixdom_n_states(K, F), np.int32),
+            EM.numpy(), EI.numpy(), ED.numpy())
+
+
+def e_step(model, params, x, y):
+    """E-step (train/likelihood.py:49-140): (LL, n_trans, ss) with
+    ss = {'match_pairs': [(a, b, w)], 'pi_obs_counts': {...}} for
+    tkf91/tkf92/mixdom; dispatches to e_step_mixdom2 for 'mixdom2'."""
+    if model == 'mixdom2':
+        return e_step_mixdom2(params, x, y)
+    if model == 'mixdom':
+        chi, st, groups, EM, EI, ED = _mixdom1_model(params)
+    else:
+        chi, st, groups, EM, EI, ED = _tkf_model(model, params)
+    x = np.asarray(x)
+    y = np.asarray(y)
+    r = _run_single_tables(chi, st, groups, EM, EI, ED, x, y)
+    post = r['post']
+    Lx, Ly = len(x), len(y)
+    mpost = post[1:, 1:, st == M].sum(axis=2)
+    ii, jj = np.nonzero(mpost > 1e-8)
+    match_pairs = list(zip(x[ii].astype(int).tolist(), y[jj].astype(int).tolist(),
+                           mpost[ii, jj].astype(np.float64).tolist()))
+    A = int(np.asarray(params['pi']).shape[0])
+    cM, cI, cD = r['cnt_M'].sum(axis=0), r['cnt_I'].sum(axis=0), r['cnt_D'].sum(axis=0)
+    pi_obs = {'match_anc_count': cM[:A, :].sum(axis=1), 'insert_count': cI[:A].copy(),
+              'delete_count': cD[:A].copy()}
+    return r['ll'], r['n_trans'], {'match_pairs': match_pairs, 'pi_obs_counts': pi_obs}
+
+
+def class_split(params, cM, cI, cD, csubs=None):
+    """Per-class MixDom2 counts from per-(d,f) character tables
+    (train/likelihood.py:279-344), float64 torch, batched over leading dims.
+
+    The class posterior q[c | type, d, f, i, j] depends on the cell only
+    through its characters, so the lattice-sized joints of the reference
+    collapse to 21x21 character tables.  Character 20 (wildcard) reads the
+    class factors at index A-1 (JAX gather clamp) and is dropped from the
+    character-indexed outputs (one-hot over A)."""
+    cp = pm._t(params['class_pis'], device=cM.device)
+    cd = pm._t(params['classdist'], device=cM.device)
+    if csubs is None:
+        csubs = pm.class_subs(params['class_S_exch'], cp, params['t']).to(cM.device)
+    K, F, C = cd.shape
+    A = cp.shape[1]
+    cdg = cd.reshape(K * F, C)
+    idx = torch.clamp(torch.arange(21, device=cM.device), max=A - 1)
+    fM = cp[:, idx][:, :, None] * csubs[..., :, idx, :][..., idx]            # [...,C,21,21]
+    fI = cp[:, idx]                                                         # [C,21]
+    jM = cdg[:, :, None, None] * fM[..., None, :, :, :]                     # [...,G,C,21,21]
+    qM = jM / (jM.sum(dim=-3, keepdim=True) + 1e-300)
+    jI = cdg[:, :, None] * fI[None]
+    qI = jI / (jI.sum(dim=-2, keepdim=True) + 1e-300)                       # [G,C,21]
+    wM = cM[..., :, None, :, :] * qM
+    wI = cI[..., :, None, :] * qI
+    wD = cD[..., :, None, :] * qI
+    return {
+        'class_match_counts': wM.sum(dim=-4)[..., :A, :A],
+        'class_insert_counts': wI.sum(dim=-3)[..., :A],
+        'class_delete_counts': wD.sum(dim=-3)[..., :A],
+        'classdist_counts': (wM.sum(dim=(-2, -1)) + wI.sum(dim=-1) + wD.sum(dim=-1)).reshape(
+            *wM.shape[:-4], K, F, C),
+    }
+
+
+def holmes_rubin_weighted_stats(Q, pi, t, mc):
+    """W[i], U[i,j] (core/ctmc.py:173-230, 285-326), float64 torch."""
+    Q, pi, mc = pm._t(Q), pm._t(pi), pm._t(mc)
+    sp = torch.sqrt(pi)
+    Sm = Q * (sp[:, None] / sp[None, :])
+    Sm = (Sm + Sm.T) / 2
+    lam, V = torch.linalg.eigh(Sm)
+    ex = torch.exp(lam * t)
+    diff = lam[:, None] - lam[None, :]
+    deg = diff.abs() < 1e-10
+    J = torch.where(deg, t * ex[:, None], (ex[:, None] - ex[None, :]) / torch.where(deg, torch.ones_like(diff), diff))
+    VV = V[:, None, :] * V[None, :, :]
+    I_sym = torch.einsum('aik,kl,jbl->aibj', VV, J, VV)
+    pf = torch.sqrt((pi[None, None, :, None] * pi[None, :, None, None])
+                    / (pi[:, None, None, None] * pi[None, None, None, :] + 1e-30))
+    Iab = I_sym.permute(0, 2, 1, 3) * pf.permute(0, 2, 1, 3)
+    Mt = ((V * ex[None, :]) @ V.T) * (sp[None, :] / sp[:, None])
+    ratio = mc / torch.where(Mt.abs() < 1e-30, torch.ones_like(Mt), Mt)
+    W = torch.einsum('ab,abii->i', ratio, Iab)
+    U = Q * torch.einsum('ab,abij->ij', ratio, Iab)
+    return W, U - torch.diag(torch.diag(U))
+
+
+def _mixdom2_tables(params, ts, device):
+    K = len(params['dom_ins'])
+    F = np.asarray(params['frag_weights']).shape[1]
+    ts = pm._t(ts, device=device)
+    chi = pm.build_nested_trans(params['main_ins'], params['main_del'], ts.cpu(), params['dom_ins'],
+                                params['dom_del'], params['dom_weights'], params['frag_weights'],
+                                params['ext_rates']).to(device)
+    csubs = pm.class_subs(pm._t(params['class_S_exch'], device), pm._t(params['class_pis'], device), ts)
+    EM, EI, ED = pm.tables_per_class(csubs, pm._t(params['class_pis'], device),
+                                     pm._t(params['classdist'], device))
+    return K, F, chi, csubs, EM, EI, ED
+
+
+def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True):
+    """Batched MixDom2 E-step over pairs of any lengths in one persistent
+    launch (replaces the bucketed jit(vmap(forward_backward_2d)) callers).
+
+    Returns a dict of device tensors: log_p [P], n_trans [P,N,N], cnt_M
+    [P,G,21,21], cnt_I/cnt_D [P,G,21], status [P] and, with
+    with_class_counts, the per-pair class counts of e_step_mixdom2."""
+    dev = _device()
+    K, F, chi, csubs, EM, EI, ED = _mixdom2_tables(params, ts, dev)
+    plan = get_plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)
+    b = _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev)
+    out = _lib.estep(plan, b)
+    res = {'log_p': out['ll'], 'n_trans': out['n_trans'], 'cnt_M': out['cnt_M'],
+           'cnt_I': out['cnt_I'], 'cnt_D': out['cnt_D'], 'status': out['status']}
+    if with_class_counts:
+        res.update(class_split(params, out['cnt_M'], out['cnt_I'], out['cnt_D'], csubs=csubs))
+    return res
+
+
+def e_step_mixdom2(params, x, y):
+    """MixDom2 E-step (train/likelihood.py:143-373): (LL, n_trans, dict with
+    class_W, class_U, class_match_counts, class_insert_counts,
+    class_delete_counts, classdist_counts)."""
+    r = estep_batch_mixdom2(params, [np.asarray(x)], [np.asarray(y)], np.array([params['t']]))
+    cp = pm._t(params['class_pis'])
+    cS = pm._t(params['class_S_exch'])
+    ss = {k: r[k][0].cpu() for k in ('class_match_counts', 'class_insert_counts',
+                                     'class_delete_counts', 'classdist_counts')}
+    W, U = [], []
+    for c in range(cp.shape[0]):
+        Qc = pm.build_class_Q(cS[c], cp[c])
+        w, u = holmes_rubin_weighted_stats(Qc, cp[c], float(params['t']), ss['class_match_counts'][c])
+        W.append(w)
+        U.append(u)
+    out = {'class_W': torch.stack(W).numpy(), 'class_U': torch.stack(U).numpy()}
+    out.update({k: v.numpy() for k, v in ss.items()})
+    return float(r['log_p'][0]), r['n_trans'][0].cpu().numpy(), out
+
+
+# ---------------------------------------------------------------- differentiable log-likelihood
+class PairHMMLogLik(torch.autograd.Function):
+    """Sum of per-pair log-likelihoods with the score-identity adjoint.
+
+    forward runs the CUDA E-step; backward returns
+      dLL/dchi[s,k]   = n_trans[s,k] / chi[s,k]
+      dLL/dEM[g,a,b]  = cnt_M[g,a,b] / EM[g,a,b]   (and I, D alike)
+    so torch autograd through the float64 builders of chi(theta) and the
+    emission tables delivers dLL/dtheta for every parameter -- the score
+    identity the reference's custom VJPs implement (train/vjp.py:130-329,
+    388-458, 682-818)."""
+
+    @staticmethod
+    def forward(ctx, chi, EM, EI, ED, plan, xs, ys):
+        dev = chi.device
+        b = _lib.make_batch(xs, ys, chi.detach(), EM.detach(), EI.detach(), ED.detach(), device=dev)
+        out = _lib.estep(plan, b)
+        ctx.save_for_backward(chi, EM, EI, ED, out['n_trans'], out['cnt_M'], out['cnt_I'], out['cnt_D'])
+        ctx.per_pair = (chi.shape[0] == len(xs), EM.shape[0] == len(xs))
+        ctx.status = out['status']
+        return out['ll']
+
+    @staticmethod
+    def backward(ctx, g):
+        chi, EM, EI, ED, n, cM, cI, cD = ctx.saved_tensors
+        gw = g.to(torch.float64)
+
+        def ratio(cnt, tab, per_pair):
+            r = torch.where(tab > 0, cnt / torch.where(tab > 0, tab, torch.ones_like(tab)),
+                            torch.zeros_like(cnt))
+            shape = (-1,) + (1,) * (cnt.dim() - 1)
+            r = r * gw.reshape(shape)
+            return r if per_pair else r.sum(dim=0, keepdim=True)
+        pc, pe = ctx.per_pair
+        return (ratio(n, chi, pc).to(chi.dtype), ratio(cM, EM, pe).to(EM.dtype),
+                ratio(cI, EI, pe).to(EI.dtype), ratio(cD, ED, pe).to(ED.dtype), None, None, None)
+
+
+def mixdom2_log_prob(main_ins_rate, main_del_rate, t, dom_ins_rates, dom_del_rates, dom_weights,
+                     frag_weights, ext_rates, class_pis, class_S_exch, class_dist, x_seq, y_seq):
+    """log P(x, y) under MixDom2 with gradients for every tensor argument
+    (train/vjp.py:627-680).  Arguments may be float64 torch tensors with
+    requires_grad; x_seq/y_seq may also be lists of sequences, in which case
+    t is a [P] tensor of per-pair times and the result is [P]."""
+    dev = _device()
+    batched = isinstance(x_seq, (list, tuple))
+    xs = list(x_seq) if batched else [np.asarray(x_seq)]
+    ys = list(y_seq) if batched else [np.asarray(y_seq)]
+    tt = pm._t(t, device=dev).reshape(-1)
+    f = lambda v: pm._t(v, device=dev)
+    K, F = f(frag_weights).shape
+    chi = pm.build_nested_trans(f(main_ins_rate), f(main_del_rate), tt, f(dom_ins_rates),
+                                f(dom_del_rates), f(dom_weights), f(frag_weights), f(ext_rates))
+    csubs = pm.class_subs(f(class_S_exch), f(class_pis), tt)
+    EM, EI, ED = pm.tables_per_class(csubs, f(class_pis), f(class_dist))
+    plan = get_plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)
+    ll = PairHMMLogLik.apply(chi, EM, EI, ED, plan, xs, ys)
+    return ll if batched else ll[0]
+
+
+def _tkf_log_prob(model, ins_rate, del_rate, t, ext, Q, pi, x_seq, y_seq):
+    dev = _device()
+    f = lambda v: pm._t(v, device=dev)
+    tt = f(t).reshape(-1)
+    if model == 'tkf91':
+        chi = pm.tkf91_trans(f(ins_rate), f(del_rate), tt)
+    else:
+        chi = pm.tkf92_trans(f(ins_rate), f(del_rate), tt, f(ext))
+    sub = pm.transition_matrix(f(Q), tt)
+    EM, EI, ED = pm.tables_tkf(sub, f(pi))
+    plan = get_plan(np.array([S, M, I, D, E]), np.zeros(5, np.int32), 1)
+    return PairHMMLogLik.apply(chi, EM, EI, ED, plan, [np.asarray(x_seq)], [np.asarray(y_seq)])[0]
+
+
+def tkf91_log_prob(ins_rate, del_rate, t, Q, pi, x_seq, y_seq):
+    """log P(x,y) under TKF91, differentiable in all float arguments (train/vjp.py:109-194)."""
+    return _tkf_log_prob('tkf91', ins_rate, del_rate, t, None, Q, pi, x_seq, y_seq)
+
+
+def tkf92_log_prob(ins_rate, del_rate, t, ext, Q, pi, x_seq, y_seq):
+    """log P(x,y) under TKF92, differentiable in all float arguments (train/vjp.py:252-329)."""
+    return _tkf_log_prob('tkf92', ins_rate, del_rate, t, ext, Q, pi, x_seq, y_seq)
+
+
+def observed_ll(model, params, x, y):
+    """log P(x, y | theta), differentiable (train/likelihood.py:415-460)."""
+    if model == 'tkf91':
+        return tkf91_log_prob(params['ins_rate'], params['del_rate'], params['t'], params['Q'],
+                              params['pi'], x, y)
+    if model == 'tkf92':
+        return tkf92_log_prob(params['ins_rate'], params['del_rate'], params['t'], params['ext'],
+                              params['Q'], params['pi'], x, y)
+    if model == 'mixdom2':
+        return mixdom2_log_prob(params['main_ins'], params['main_del'], params['t'], params['dom_ins'],
+                                params['dom_del'], params['dom_weights'], params['frag_weights'],
+                                params['ext_rates'], params['class_pis'], params['class_S_exch'],
+                                params['classdist'], x, y)
+    raise ValueError(f'Unknown model: {model}')
+
+
+# ---------------------------------------------------------------- batched TKF92 (train/tkf92_svi_bw.py)
+def _tkf92_batch(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, ext, Q, pi):
+    dev = _device()
+    ts = pm._t(np.asarray(ts, dtype=np.float64), device=dev)
+    chi = pm.tkf92_trans(lam, mu, ts.cpu(), ext).clamp_min(1e-30).to(dev)   # log(max(tau,1e-30)), tkf92_svi_bw.py:164
+    sub = pm.transition_matrix(pm._t(Q, dev), ts)
+    EM, EI, ED = pm.tables_tkf(sub, pm._t(pi, dev))
+    xs = [np.asarray(xs_pad[b])[:int(Lx_real[b])] for b in range(len(ts))]
+    ys = [np.asarray(ys_pad[b])[:int(Ly_real[b])] for b in range(len(ts))]
+    plan = get_plan(np.array([S, M, I, D, E]), np.zeros(5, np.int32), 1)
+    return plan, _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev)
+
+
+def estep_batch_tkf92_forward_only(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, ext, Q, pi):
+    """Per-pair log_p of pre-padded pairs (train/tkf92_svi_bw.py:337-365)."""
+    plan, b = _tkf92_batch(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, ext, Q, pi)
+    ll, st = _lib.forward(plan, b)
+    return ll
+
+
+def estep_batch_tkf92(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, ext, Q, pi):
+    """Batched TKF92 E-step: {'log_p', 'n_chi_diag'} (the chi counts of
+    train/tkf92_svi_bw.py:263-334; its BDI statistics are a later epilogue)."""
+    plan, b = _tkf92_batch(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, ext, Q, pi)
+    out = _lib.estep(plan, b)
+    return {'log_p': out['ll'], 'n_chi_diag': out['n_trans'], 'status': out['status']}

@@ -1,0 +1,61 @@
+"""In-tree build of the CUDA library (``libpairhmm.so``) for sm_103a.
+
+``python -m pairhmm.build`` (or ``build()``) compiles
+``csrc/pairhmm.cu`` with nvcc into ``pairhmm/libpairhmm.so`` next to this
+file.  The build is skipped when the library is newer than its sources.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+PROJECT_DIR = os.path.dirname(PKG_DIR)
+REPO_DIR = os.path.dirname(PROJECT_DIR)
+CSRC = os.path.join(PROJECT_DIR, 'csrc')
+INCLUDE = os.path.join(REPO_DIR, 'include')
+LIB_PATH = os.path.join(PKG_DIR, 'libpairhmm.so')
+SOURCES = [os.path.join(CSRC, 'pairhmm.cu')]
+ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
+
+
+def nvcc_path():
+    cand = shutil.which('nvcc')
+    if cand:
+        return cand
+    for p in ('/usr/local/cuda/bin/nvcc',):
+        if os.path.exists(p):
+            return p
+    raise RuntimeError('nvcc not found')
+
+
+def _stale(out, deps):
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force=False, verbose=False, extra=()):
+    deps = SOURCES + [os.path.join(INCLUDE, 'pairhmm.h')]
+    if not force and not _stale(LIB_PATH, deps):
+        return LIB_PATH
+    tmp = LIB_PATH + '.tmp'
+    cmd = [nvcc_path(), *ARCH_FLAGS, '-O3', '-lineinfo', '-std=c++17', '-shared',
+           '-Xcompiler', '-fPIC', '-I', INCLUDE, *extra, *SOURCES, '-o', tmp]
+    if verbose:
+        print(' '.join(cmd), file=sys.stderr)
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError('nvcc failed:\n' + res.stdout + res.stderr)
+    if verbose and res.stderr:
+        print(res.stderr, file=sys.stderr)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == '__main__':
+    build(force='--force' in sys.argv, verbose=True,
+          extra=['-Xptxas', '-v'] if '--ptxas' in sys.argv else ())

@@ -124,6 +124,13 @@ int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch,
 int phmm_set_timing(phmm_plan *plan, int enable);
 int phmm_kernel_times(phmm_plan *plan, float *fwd_ms, float *bwd_ms);
 
+/* Kernel family: 0 = automatic (default), 1 = generic kernels (any state
+ * space of up to 60 emitting states), 2 = register-resident warp kernels
+ * (state spaces with a compiled shape).  phmm_last_variant reports the family
+ * the last call used.  No counterpart in the reference (it has no kernels). */
+int phmm_set_variant(phmm_plan *plan, int variant);
+int phmm_last_variant(const phmm_plan *plan);
+
 /* Number of kernel launches issued by the last call on this plan. */
 int phmm_last_launch_count(const phmm_plan *plan);
 

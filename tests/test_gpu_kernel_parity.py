@@ -61,17 +61,25 @@ def related_pair(rng, Lx, Ly):
     return x, y
 
 
-def run_kernel(chi, st, groups, EM, EI, ED, xs, ys, per_pair=None):
-    """per_pair: optional list of (chi, EM, EI, ED) per pair."""
+def run_kernel(chi, st, groups, EM, EI, ED, xs, ys, per_pair=None, variant=0):
+    """per_pair: optional list of (chi, EM, EI, ED) per pair; variant 1 =
+    generic kernels, 2 = register-resident warp kernels, 0 = automatic."""
     from pairhmm import _lib
     G = EM.shape[0]
     plan = _lib.Plan(st, groups, G)
+    if variant:
+        try:
+            plan.set_variant(variant)
+        except _lib.PairHMMError:
+            pytest.skip('no kernel of this family for the state space')
     if per_pair is not None:
         chis, EMs, EIs, EDs = (np.stack(v) for v in zip(*per_pair))
     else:
         chis, EMs, EIs, EDs = chi[None], EM[None], EI[None], ED[None]
     b = _lib.make_batch(xs, ys, chis, EMs, EIs, EDs)
     out = _lib.estep(plan, b)
+    if variant:
+        assert plan.last_variant == variant
     return {k: v.cpu().numpy() for k, v in out.items()}, plan
 
 
@@ -94,12 +102,14 @@ def assert_counts(got, want, rtol=CNT_RTOL):
 
 
 LENGTHS = [(0, 0), (0, 5), (6, 0), (1, 1), (7, 9), (31, 33), (32, 32), (33, 31),
-           (65, 40), (40, 97), (130, 120)]
+           (63, 10), (64, 64), (65, 40), (40, 97), (130, 120), (129, 3)]
 
 
+@pytest.mark.parametrize('variant', [1, 2])
 @pytest.mark.parametrize('model,K,F,C', [('tkf91', 1, 1, 1), ('mixdom2', 3, 1, 1),
-                                         ('mixdom2', 2, 2, 2), ('mixdom2', 4, 2, 2)])
-def test_estep_matches_oracle(cuda_lib, model, K, F, C):
+                                         ('mixdom2', 2, 2, 2), ('mixdom2', 4, 2, 2),
+                                         ('mixdom2', 1, 1, 2), ('mixdom2', 2, 1, 1)])
+def test_estep_matches_oracle(cuda_lib, model, K, F, C, variant):
     rng = np.random.default_rng(7 + K * 10 + F + C)
     chi, st, groups, EM, EI, ED = oracle_case(model, rng, K, F, C)
     xs, ys = [], []
@@ -107,7 +117,7 @@ def test_estep_matches_oracle(cuda_lib, model, K, F, C):
         x, y = related_pair(rng, Lx, Ly)
         xs.append(x)
         ys.append(y)
-    out, _ = run_kernel(chi, st, groups, EM, EI, ED, xs, ys)
+    out, _ = run_kernel(chi, st, groups, EM, EI, ED, xs, ys, variant=variant)
     assert (out['status'] == 0).all(), out['status']
     for b, (x, y) in enumerate(zip(xs, ys)):
         ll, n, cM, cI, cD = oracle_estep(chi, st, groups, EM, EI, ED, x, y)
@@ -131,7 +141,8 @@ def test_forward_only_matches_estep_ll(cuda_lib):
     np.testing.assert_array_equal(ll_f.cpu().numpy(), out['ll'].cpu().numpy())
 
 
-def test_per_pair_chi_and_wildcards(cuda_lib):
+@pytest.mark.parametrize('variant', [1, 2])
+def test_per_pair_chi_and_wildcards(cuda_lib, variant):
     rng = np.random.default_rng(11)
     base = mixdom2_params(rng, 2, 1, 1)
     xs, ys, per_pair, lls = [], [], [], []
@@ -147,7 +158,7 @@ def test_per_pair_chi_and_wildcards(cuda_lib):
         per_pair.append((chi, EM, EI, ED))
         lls.append(oracle_estep(chi, st, groups, EM, EI, ED, x, y))
     # t changes both chi and the class P_c(t) tables: one set per pair
-    out, _ = run_kernel(None, st, groups, EM, EI, ED, xs, ys, per_pair=per_pair)
+    out, _ = run_kernel(None, st, groups, EM, EI, ED, xs, ys, per_pair=per_pair, variant=variant)
     for b in range(3):
         ll, n, cM, cI, cD = lls[b]
         assert abs(out['ll'][b] - ll) <= LL_RTOL * abs(ll)
@@ -155,12 +166,13 @@ def test_per_pair_chi_and_wildcards(cuda_lib):
         assert_counts(out['cnt_M'][b], cM)
 
 
-def test_long_pair_pipelined_stripes(cuda_lib):
-    """A pair spanning many 32-row stripes, against the oracle."""
+@pytest.mark.parametrize('variant', [1, 2])
+def test_long_pair_pipelined_stripes(cuda_lib, variant):
+    """A pair spanning many stripes (pipelined through the edge rows), against the oracle."""
     rng = np.random.default_rng(5)
     chi, st, groups, EM, EI, ED = oracle_case('mixdom2', rng, 3, 1, 1)
     x, y = related_pair(rng, 300, 280)
-    out, _ = run_kernel(chi, st, groups, EM, EI, ED, [x], [y])
+    out, _ = run_kernel(chi, st, groups, EM, EI, ED, [x], [y], variant=variant)
     ll, n, cM, cI, cD = oracle_estep(chi, st, groups, EM, EI, ED, x, y)
     assert abs(out['ll'][0] - ll) <= LL_RTOL * abs(ll)
     assert_counts(out['n_trans'][0], n)

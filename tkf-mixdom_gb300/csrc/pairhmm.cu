@@ -70,6 +70,8 @@ struct KParams {
     int8_t slot_type[MAXS];             // T_M/T_I/T_D dest, T_S start, T_NONE pad
     int16_t slot_group[MAXS];
     int8_t quad_type[MAXQ];
+    int16_t w_orig[MAXS];               // warp kernels: source slot -> state (start last)
+    int16_t w_group[MAXS];              // warp kernels: dest slot -> emission group
     const uint8_t *res;
     const PairMeta *meta;
     const int2 *items;
@@ -817,6 +819,12 @@ __global__ void fill_f64(double *p, int64_t n, double v) {
         p[idx] = v;
 }
 
+}  // namespace
+
+#include "estep_warp.cuh"
+
+namespace {
+
 // ---------------------------------------------------------------- host side
 thread_local std::string g_err;
 
@@ -853,6 +861,10 @@ struct phmm_plan {
     bool timing = false;
     bool timed_bwd = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // register-resident warp kernels for this state space (null: generic kernels)
+    int w_nm = 0, w_ni = 0, w_nd = 0;
+    int variant = 0;        // 0 automatic, 1 generic quad kernels, 2 warp kernels
+    int last_variant = 0;
 };
 
 namespace {
@@ -866,6 +878,34 @@ int ensure(T **ptr, size_t *cap, size_t n) {
     if (e != cudaSuccess) return fail(PHMM_E_CUDA, std::string("cudaMalloc scratch: ") + cudaGetErrorString(e));
     *cap = want;
     return 0;
+}
+
+// ---- launchers of the register-resident warp kernels, one per state-space shape
+using WarpLauncher = int (*)(phmm_plan *, KParams &, int, int, bool, cudaStream_t);
+
+template <class SH>
+int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, bool bwd, cudaStream_t stream);
+
+template <int NM, int NI, int ND>
+int launch_warp_shape(phmm_plan *plan, KParams &K, int n_items, int max_ly, bool bwd, cudaStream_t stream) {
+    return launch_warp<warp2::Shape<NM, NI, ND>>(plan, K, n_items, max_ly, bwd, stream);
+}
+
+struct WarpShapeEntry { int nm, ni, nd; WarpLauncher fn; };
+const WarpShapeEntry kWarpShapes[] = {
+    {1, 1, 1, launch_warp_shape<1, 1, 1>},   // TKF91 / TKF92
+    {1, 2, 2, launch_warp_shape<1, 2, 2>},   // MixDom K=1 F=1
+    {2, 2, 2, launch_warp_shape<2, 2, 2>},   // MixFrag F=2
+    {3, 3, 3, launch_warp_shape<3, 3, 3>},   // MixFrag F=3
+    {2, 4, 4, launch_warp_shape<2, 4, 4>},   // MixDom K*F=2
+    {3, 6, 6, launch_warp_shape<3, 6, 6>},   // MixDom K*F=3 (17 states)
+    {4, 8, 8, launch_warp_shape<4, 8, 8>},   // MixDom K*F=4 (22 states)
+};
+
+WarpLauncher find_warp_launcher(int nm, int ni, int nd) {
+    for (const auto &e : kWarpShapes)
+        if (e.nm == nm && e.ni == ni && e.nd == nd) return e.fn;
+    return nullptr;
 }
 
 int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_trans,
@@ -882,7 +922,16 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
         return fail(PHMM_E_ARG, "null batch pointer");
     if (estep && (!n_trans || !cntM || !cntI || !cntD)) return fail(PHMM_E_ARG, "null E-step output");
     KParams K = plan->base;
-    const int N = K.N, NS = K.NS, G = K.G;
+    const int N = K.N, G = K.G;
+    // kernel family: register-resident warp kernels when the shape has one and
+    // no lattice tables are requested; the generic quad kernels otherwise
+    WarpLauncher wl = nullptr;
+    if (plan->variant != 1 && !F_log && !B_log && !post)
+        wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
+    if (plan->variant == 2 && !wl) return fail(PHMM_E_ARG, "no warp kernel for this state space");
+    const int rows = wl ? warp2::ROWS : TH;
+    const int stride = wl ? ((plan->w_nm + plan->w_ni + plan->w_nd + 1 + 3) & ~3) : K.NS;
+    plan->last_variant = wl ? 2 : 1;
     // ---- plan: stripes, offsets, longest-first order
     std::vector<int> order(P_);
     for (int p = 0; p < P_; ++p) {
@@ -902,13 +951,13 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
         m.Ly = b->Ly_host[p];
         m.x_off = b->x_off_host[p];
         m.y_off = b->y_off_host[p];
-        m.n_stripes = (m.Lx + 1 + TH - 1) / TH;
+        m.n_stripes = (m.Lx + 1 + rows - 1) / rows;
         m.stripe_base = stripes;
         m.lat_base = lat_cells;
         m.edge_base = edge_cells;
         m.tab_base = tab_cells;
         stripes += m.n_stripes;
-        if (estep) lat_cells += (int64_t)m.n_stripes * (TH + m.Ly) * TH;
+        if (estep) lat_cells += (int64_t)m.n_stripes * (rows + m.Ly) * rows;
         edge_cells += (int64_t)m.n_stripes * (m.Ly + 1);
         tab_cells += (int64_t)(m.Lx + 1) * (m.Ly + 1);
         max_ly = std::max(max_ly, m.Ly);
@@ -917,27 +966,22 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     for (int p : order)
         for (int s = 0; s < plan->h_meta[p].n_stripes; ++s) plan->h_items.push_back(make_int2(p, s));
     const int n_items = (int)plan->h_items.size();
+    if (estep)
+        for (int p : order)
+            for (int s = plan->h_meta[p].n_stripes - 1; s >= 0; --s) plan->h_items.push_back(make_int2(p, s));
     int rc;
     if ((rc = ensure((char **)&plan->meta, &plan->meta_cap, sizeof(PairMeta) * P_))) return rc;
-    if ((rc = ensure((char **)&plan->items, &plan->items_cap, sizeof(int2) * 2 * n_items))) return rc;
-    if ((rc = ensure(&plan->edge, &plan->edge_cap, (size_t)edge_cells * NS))) return rc;
+    if ((rc = ensure((char **)&plan->items, &plan->items_cap, sizeof(int2) * plan->h_items.size()))) return rc;
+    if ((rc = ensure(&plan->edge, &plan->edge_cap, (size_t)edge_cells * stride))) return rc;
     if ((rc = ensure(&plan->edge_exp, &plan->edgeE_cap, (size_t)edge_cells))) return rc;
     if ((rc = ensure(&plan->progress, &plan->prog_cap, (size_t)2 * stripes))) return rc;
     if (estep) {
-        if ((rc = ensure(&plan->lat, &plan->lat_cap, (size_t)lat_cells * NS))) return rc;
+        if ((rc = ensure(&plan->lat, &plan->lat_cap, (size_t)lat_cells * stride))) return rc;
         if ((rc = ensure(&plan->lat_exp, &plan->latE_cap, (size_t)lat_cells))) return rc;
     }
-    // backward items: same pair order, stripes bottom-up
-    std::vector<int2> bitems;
-    if (estep) {
-        for (int p : order)
-            for (int s = plan->h_meta[p].n_stripes - 1; s >= 0; --s) bitems.push_back(make_int2(p, s));
-    }
     CUDA_TRY(cudaMemcpyAsync(plan->meta, plan->h_meta.data(), sizeof(PairMeta) * P_, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(plan->items, plan->h_items.data(), sizeof(int2) * n_items, cudaMemcpyHostToDevice, stream));
-    if (estep)
-        CUDA_TRY(cudaMemcpyAsync((int2 *)plan->items + n_items, bitems.data(), sizeof(int2) * n_items,
-                                 cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(plan->items, plan->h_items.data(), sizeof(int2) * plan->h_items.size(),
+                             cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 2 * sizeof(int), stream));
     CUDA_TRY(cudaMemsetAsync(plan->progress, 0, sizeof(int) * 2 * stripes, stream));
     CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int32_t) * P_, stream));
@@ -976,41 +1020,44 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     K.post = post;
     K.max_ly = max_ly;
     K.spin_limit = 40LL * 1000 * 1000;
-    const int threads = 32 * K.NQ;
-    // forward
-    {
-        const SmemLayout L = make_layout(K.NS, K.NQ, G, max_ly, false);
-        CUDA_TRY(cudaFuncSetAttribute(forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
-        int occ = 0;
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, forward_kernel, threads, L.bytes));
-        if (occ < 1) return fail(PHMM_E_ARG, "forward kernel does not fit on an SM (shared memory)");
-        K.items = (const int2 *)plan->items;
-        K.counter = plan->counters;
-        K.progress = plan->progress;
-        const int grid = std::min(n_items, plan->sm_count * occ);
-        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
-        forward_kernel<<<grid, threads, L.bytes, stream>>>(K);
-        CUDA_TRY(cudaGetLastError());
-        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[1], stream));
-        plan->launches++;
-    }
-    if (estep) {
-        const SmemLayout L = make_layout(K.NS, K.NQ, G, max_ly, true);
-        CUDA_TRY(cudaFuncSetAttribute(backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
-        int occ = 0;
-        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, backward_kernel, threads, L.bytes));
-        if (occ < 1) return fail(PHMM_E_ARG, "backward kernel does not fit on an SM (shared memory)");
-        K.items = (const int2 *)plan->items + n_items;
-        K.counter = plan->counters + 1;
-        K.progress = plan->progress + stripes;
-        const int grid = std::min(n_items, plan->sm_count * occ);
-        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[2], stream));
-        backward_kernel<<<grid, threads, L.bytes, stream>>>(K);
-        CUDA_TRY(cudaGetLastError());
-        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[3], stream));
+    for (int pass = 0; pass < (estep ? 2 : 1); ++pass) {
+        const bool bwd = pass == 1;
+        K.items = (const int2 *)plan->items + (bwd ? n_items : 0);
+        K.counter = plan->counters + (bwd ? 1 : 0);
+        K.progress = plan->progress + (bwd ? stripes : 0);
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[bwd ? 2 : 0], stream));
+        if (wl) {
+            if ((rc = wl(plan, K, n_items, max_ly, bwd, stream))) return rc;
+        } else {
+            const int threads = 32 * K.NQ;
+            const SmemLayout L = make_layout(K.NS, K.NQ, G, max_ly, bwd);
+            auto kern = bwd ? backward_kernel : forward_kernel;
+            CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
+            int occ = 0;
+            CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, L.bytes));
+            if (occ < 1) return fail(PHMM_E_ARG, "kernel does not fit on an SM (shared memory)");
+            const int grid = std::min(n_items, plan->sm_count * occ);
+            kern<<<grid, threads, L.bytes, stream>>>(K);
+            CUDA_TRY(cudaGetLastError());
+        }
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[bwd ? 3 : 1], stream));
         plan->launches++;
     }
     plan->timed_bwd = estep;
+    return 0;
+}
+
+template <class SH>
+int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, bool bwd, cudaStream_t stream) {
+    const warp2::SmemW L = warp2::make_smem_w(SH::SP, SH::KP, SH::NI, K.G, max_ly, bwd);
+    auto kern = bwd ? warp2::backward_warp_kernel<SH> : warp2::forward_warp_kernel<SH>;
+    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
+    int occ = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32, L.bytes));
+    if (occ < 1) return fail(PHMM_E_ARG, "warp kernel does not fit on an SM (shared memory)");
+    const int grid = std::min(n_items, plan->sm_count * occ);
+    kern<<<grid, 32, L.bytes, stream>>>(K);
+    CUDA_TRY(cudaGetLastError());
     return 0;
 }
 
@@ -1088,8 +1135,22 @@ int phmm_plan_create(const phmm_model_desc *md, phmm_plan **out) {
             if (4 * q >= K.kbeg[ty] && 4 * q < K.kend[ty]) t = ty + 1;
         K.quad_type[q] = (int8_t)t;
     }
+    // warp-kernel slot layout: M, I, D states in order, then the start state
+    {
+        int ns = 0;
+        for (int ty = 0; ty < 3; ++ty)
+            for (int k : byType[ty]) {
+                K.w_orig[ns] = (int16_t)k;
+                K.w_group[ns] = (int16_t)(md->state_group ? md->state_group[k] : 0);
+                ++ns;
+            }
+        if (ns + 1 <= MAXS) K.w_orig[ns] = 0;
+    }
     phmm_plan *plan = new phmm_plan();
     plan->base = K;
+    plan->w_nm = (int)byType[0].size();
+    plan->w_ni = (int)byType[1].size();
+    plan->w_nd = (int)byType[2].size();
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&plan->sm_count, cudaDevAttrMultiProcessorCount, dev);
@@ -1161,5 +1222,15 @@ int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch, double *ll_out, 
 }
 
 int phmm_last_launch_count(const phmm_plan *plan) { return plan ? plan->launches : 0; }
+
+int phmm_set_variant(phmm_plan *plan, int variant) {
+    if (!plan || variant < 0 || variant > 2) return fail(PHMM_E_ARG, "bad variant");
+    if (variant == 2 && !find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd))
+        return fail(PHMM_E_ARG, "no warp kernel for this state space");
+    plan->variant = variant;
+    return 0;
+}
+
+int phmm_last_variant(const phmm_plan *plan) { return plan ? plan->last_variant : 0; }
 
 }  // extern "C"

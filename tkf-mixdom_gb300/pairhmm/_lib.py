@@ -18,7 +18,8 @@ from .build import LIB_PATH
 _LIB = None
 
 EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep',
-           'phmm_estep_tables', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_last_launch_count',
+           'phmm_estep_tables', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_set_variant',
+           'phmm_last_variant', 'phmm_last_launch_count',
            'phmm_last_error', 'phmm_version')
 
 
@@ -73,6 +74,10 @@ def load(path=None):
     lib.phmm_set_timing.restype = ctypes.c_int
     lib.phmm_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
     lib.phmm_kernel_times.restype = ctypes.c_int
+    lib.phmm_set_variant.argtypes = [vp, ctypes.c_int]
+    lib.phmm_set_variant.restype = ctypes.c_int
+    lib.phmm_last_variant.argtypes = [vp]
+    lib.phmm_last_variant.restype = ctypes.c_int
     lib.phmm_last_launch_count.argtypes = [vp]
     lib.phmm_last_launch_count.restype = ctypes.c_int
     lib.phmm_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
@@ -127,6 +132,14 @@ class Plan:
     @property
     def launches(self):
         return self.lib.phmm_last_launch_count(self.handle)
+
+    def set_variant(self, variant):
+        """0 automatic, 1 generic kernels, 2 register-resident warp kernels."""
+        _check(self.lib.phmm_set_variant(self.handle, int(variant)), 'phmm_set_variant')
+
+    @property
+    def last_variant(self):
+        return self.lib.phmm_last_variant(self.handle)
 
     def set_timing(self, enable=True):
         _check(self.lib.phmm_set_timing(self.handle, int(enable)), 'phmm_set_timing')

@@ -324,7 +324,7 @@ def main():
                 'traffic': profile_traffic(),
                 'peak_source': f'{SMS} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 FLOP x sm_max_mhz '
                                f'({peaks.get("sm_max_mhz")} MHz, {src} MEASURED_PEAKS.json); '
-                               'the DP has no tensor-core or HBM bound (see DESIGN.md)',
+                               'the DP is a dense FP32 CUDA-core contraction: no tensor-core or HBM bound',
                 'flop_per_cell': (4 if dom == 'backward_kernel' else 2) * N * N,
                 'fwd_kernel_ms': fwd_avg, 'bwd_kernel_ms': bwd_avg,
                 'hbm_peak_gbs': peaks.get('hbm_gbs')}

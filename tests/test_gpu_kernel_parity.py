@@ -1,6 +1,6 @@
 """CUDA E-step kernel vs the FP64 oracle, through the C ABI.
 
-Bars (the benchmark spec): per-pair log-likelihood within 1e-6 relative,
+Bars: per-pair log-likelihood within 1e-6 relative,
 expected counts within 1e-5 relative (entries above 1e-6 of the largest).
 The kernel runs in float32 probability space; the oracle in float64 log space.
 """

@@ -116,6 +116,37 @@ int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch,
                       double *cnt_I, double *cnt_D, int32_t *status_out,
                       double *log_F, double *log_B, double *post, void *stream);
 
+/* E-step that allocates nothing: no cudaMalloc, cudaFree or other allocating
+ * call.  No counterpart in the reference.
+ *
+ * Who needs it: a caller whose process already owns the GPU's memory.  The
+ * reference's own training code runs under JAX, whose runtime by default
+ * reserves most of the device memory for its own pool when it starts, and
+ * serving processes often run under a framework allocator with a fixed
+ * budget; a cudaMalloc issued behind such an allocator's back can fail or
+ * fragment its pool, so these callers cannot rely on phmm_plan_create /
+ * phmm_estep growing scratch on demand.
+ *
+ * How: the kernels of phmm_estep run with all their scratch (work list,
+ * progress counters, edge rows, forward lattice) in one file-scope
+ * __device__ array of PHMM_STATIC_SCRATCH_BYTES, which every GPU that loads
+ * this library holds until the process exits.  The caller still provides the
+ * inputs and outputs (same meaning as phmm_estep; the model is passed
+ * directly, no plan).  The first call on a device looks the array's device
+ * address up (cudaGetSymbolAddress, with that device current); make that
+ * first call before any stream capture.  A batch whose scratch would exceed
+ * the array is rejected with PHMM_E_ARG and a message giving the bytes it
+ * needs (at 17 states a call holds about 0.4 M lattice cells, e.g. 16 pairs
+ * of 150 x 150).  Every call shares the array and the static host staging
+ * it uses, and the array keeps the last call's contents: each call clears
+ * the counters it needs, but calls that overlap -- on the GPU, on different
+ * streams, or from different host threads -- race and must be serialised by
+ * the caller. */
+#define PHMM_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int phmm_estep_static(const phmm_model_desc *model, const phmm_batch *batch,
+                      double *ll_out, double *n_trans, double *cnt_M, double *cnt_I,
+                      double *cnt_D, int32_t *status_out, void *stream);
+
 /* Per-kernel CUDA-event timing on the launching stream (diagnostics and
  * benchmarking; no counterpart in the reference, which has no kernels).
  * phmm_kernel_times waits for the last call's events and returns the forward

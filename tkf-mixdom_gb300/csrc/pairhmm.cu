@@ -1234,3 +1234,254 @@ int phmm_set_variant(phmm_plan *plan, int variant) {
 int phmm_last_variant(const phmm_plan *plan) { return plan ? plan->last_variant : 0; }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- allocation-free E-step
+//
+// phmm_estep_static runs the same kernels as phmm_estep with every scratch
+// buffer carved out of one file-scope __device__ array, for callers that
+// cannot allocate device memory.  The array is PHMM_STATIC_SCRATCH_BYTES
+// large and lives on every GPU that loads this library until the process
+// exits.  Host code cannot pass the array's name to a kernel (on the host it
+// is only a stand-in for the symbol); its device address is looked up with
+// cudaGetSymbolAddress once per device, with that device current, by the
+// first call made on that device.
+namespace {
+
+__device__ __align__(256) unsigned char g_static_scratch[PHMM_STATIC_SCRATCH_BYTES];
+
+constexpr int kStaticMaxDevices = 64;
+constexpr int kStaticMaxPairs = 4096;
+constexpr int kStaticMaxItems = 2 * 32768;
+unsigned char *g_static_dev[kStaticMaxDevices] = {};
+int g_static_sms[kStaticMaxDevices] = {};
+// host staging of the per-call work description (static: no heap either)
+PairMeta g_static_meta[kStaticMaxPairs];
+int2 g_static_items[kStaticMaxItems];
+int g_static_order[kStaticMaxPairs];
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// Model slot tables for a description (same layout as phmm_plan_create).
+int static_model(const phmm_model_desc *md, KParams *K, int *nm, int *ni, int *nd) {
+    if (!md || !md->state_types || md->n_states < 2) return fail(PHMM_E_ARG, "bad model description");
+    const int N = md->n_states;
+    if (md->state_types[0] != T_S) return fail(PHMM_E_ARG, "state 0 must be the start state (type S)");
+    int e_idx = -1;
+    for (int k = 0; k < N; ++k)
+        if (md->state_types[k] == T_E) { e_idx = k; break; }
+    if (e_idx < 0) return fail(PHMM_E_ARG, "no End (type E) state");
+    if (md->n_groups < 1 || md->n_groups > 64) return fail(PHMM_E_ARG, "n_groups must be in 1..64");
+    int byType[3][MAXS];
+    int cnt[3] = {0, 0, 0};
+    for (int k = 0; k < N; ++k) {
+        const int t = md->state_types[k];
+        if (t == T_M || t == T_I || t == T_D) {
+            const int g = md->state_group ? md->state_group[k] : 0;
+            if (g < 0 || g >= md->n_groups) return fail(PHMM_E_ARG, "state group out of range");
+            if (cnt[t - 1] >= MAXS) return fail(PHMM_E_ARG, "too many emitting states");
+            byType[t - 1][cnt[t - 1]++] = k;
+        } else if (t < 0 || t > T_E) {
+            return fail(PHMM_E_ARG, "unknown state type");
+        }
+    }
+    memset(K, 0, sizeof(*K));
+    int ns = 0, s_slot = -1;
+    int slot_orig[2 * MAXS], slot_type[2 * MAXS];
+    for (int ty = 0; ty < 3; ++ty) {
+        K->kbeg[ty] = ns;
+        for (int q = 0; q < cnt[ty]; ++q) {
+            if (ns >= MAXS) return fail(PHMM_E_ARG, "too many emitting states for this build (max 60)");
+            slot_orig[ns] = byType[ty][q]; slot_type[ns] = ty + 1; ++ns;
+        }
+        while (ns % 4) {
+            if (ns >= MAXS) return fail(PHMM_E_ARG, "too many emitting states for this build (max 60)");
+            if (s_slot < 0) { s_slot = ns; slot_orig[ns] = 0; slot_type[ns] = T_S; }
+            else { slot_orig[ns] = -1; slot_type[ns] = T_NONE; }
+            ++ns;
+        }
+        K->kend[ty] = ns;
+    }
+    if (s_slot < 0) {
+        if (ns + 4 > MAXS) return fail(PHMM_E_ARG, "too many emitting states for this build (max 60)");
+        s_slot = ns; slot_orig[ns] = 0; slot_type[ns] = T_S; ++ns;
+        while (ns % 4) { slot_orig[ns] = -1; slot_type[ns] = T_NONE; ++ns; }
+    }
+    K->N = N;
+    K->NS = ns;
+    K->NQ = ns / 4;
+    K->G = md->n_groups;
+    K->e_idx = e_idx;
+    K->s_slot = s_slot;
+    for (int s = 0; s < ns; ++s) {
+        K->slot_orig[s] = (int16_t)slot_orig[s];
+        K->slot_type[s] = (int8_t)slot_type[s];
+        int g = 0;
+        if (slot_type[s] >= T_M && slot_type[s] <= T_D && md->state_group) g = md->state_group[slot_orig[s]];
+        K->slot_group[s] = (int16_t)g;
+    }
+    for (int q = 0; q < K->NQ; ++q) {
+        int t = T_NONE;
+        for (int ty = 0; ty < 3; ++ty)
+            if (4 * q >= K->kbeg[ty] && 4 * q < K->kend[ty]) t = ty + 1;
+        K->quad_type[q] = (int8_t)t;
+    }
+    int w = 0;
+    for (int ty = 0; ty < 3; ++ty)
+        for (int q = 0; q < cnt[ty]; ++q) {
+            const int k = byType[ty][q];
+            K->w_orig[w] = (int16_t)k;
+            K->w_group[w] = (int16_t)(md->state_group ? md->state_group[k] : 0);
+            ++w;
+        }
+    if (w < MAXS) K->w_orig[w] = 0;
+    *nm = cnt[0];
+    *ni = cnt[1];
+    *nd = cnt[2];
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int phmm_estep_static(const phmm_model_desc *md, const phmm_batch *b, double *ll,
+                                 double *n_trans, double *cntM, double *cntI, double *cntD,
+                                 int32_t *status, void *stream_) {
+    if (!b) return fail(PHMM_E_ARG, "null batch");
+    KParams K;
+    int nm = 0, ni = 0, nd = 0, rc;
+    if ((rc = static_model(md, &K, &nm, &ni, &nd))) return rc;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    const int P_ = b->n_pairs;
+    if (P_ < 0) return fail(PHMM_E_ARG, "n_pairs < 0");
+    if (P_ == 0) return 0;
+    if (!b->Lx_host || !b->Ly_host || !b->x_off_host || !b->y_off_host || !b->residues || !b->chi ||
+        !b->emit_M || !b->emit_I || !b->emit_D || !ll || !status || !n_trans || !cntM || !cntI || !cntD)
+        return fail(PHMM_E_ARG, "null batch pointer or output");
+    if (P_ > kStaticMaxPairs) return fail(PHMM_E_ARG, "phmm_estep_static: more than 4096 pairs in one call");
+    // ---- device set-up, once per device (the first call on a device does it)
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kStaticMaxDevices) return fail(PHMM_E_ARG, "device ordinal out of range");
+    if (!g_static_dev[dev]) {
+        void *ptr = nullptr;
+        CUDA_TRY(cudaGetSymbolAddress(&ptr, g_static_scratch));
+        int sms = 0;
+        CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        g_static_sms[dev] = sms;
+        g_static_dev[dev] = (unsigned char *)ptr;
+    }
+    unsigned char *base = g_static_dev[dev];
+    const int N = K.N, G = K.G;
+    const WarpLauncher wl = find_warp_launcher(nm, ni, nd);
+    const int rows = wl ? warp2::ROWS : TH;
+    const int stride = wl ? ((nm + ni + nd + 1 + 3) & ~3) : K.NS;
+    // ---- work description and scratch layout
+    int64_t lat_cells = 0, edge_cells = 0;
+    int stripes = 0, max_ly = 0;
+    for (int p = 0; p < P_; ++p) {
+        if (b->Lx_host[p] < 0 || b->Ly_host[p] < 0) return fail(PHMM_E_ARG, "negative length");
+        PairMeta &m = g_static_meta[p];
+        m.Lx = b->Lx_host[p];
+        m.Ly = b->Ly_host[p];
+        m.x_off = b->x_off_host[p];
+        m.y_off = b->y_off_host[p];
+        m.n_stripes = (m.Lx + 1 + rows - 1) / rows;
+        m.stripe_base = stripes;
+        m.lat_base = lat_cells;
+        m.edge_base = edge_cells;
+        m.tab_base = 0;
+        stripes += m.n_stripes;
+        lat_cells += (int64_t)m.n_stripes * (rows + m.Ly) * rows;
+        edge_cells += (int64_t)m.n_stripes * (m.Ly + 1);
+        max_ly = std::max(max_ly, m.Ly);
+        g_static_order[p] = p;
+    }
+    if (2 * (int64_t)stripes > kStaticMaxItems)
+        return fail(PHMM_E_ARG, "phmm_estep_static: batch has more than 32768 row stripes");
+    const size_t off_meta = 0;
+    const size_t off_items = align256(off_meta + sizeof(PairMeta) * P_);
+    const size_t off_cnt = align256(off_items + sizeof(int2) * 2 * stripes);
+    const size_t off_prog = align256(off_cnt + 4 * sizeof(int));
+    const size_t off_edge = align256(off_prog + sizeof(int) * 2 * stripes);
+    const size_t off_edgeE = align256(off_edge + sizeof(float) * (size_t)edge_cells * stride);
+    const size_t off_lat = align256(off_edgeE + sizeof(int) * (size_t)edge_cells);
+    const size_t off_latE = align256(off_lat + sizeof(float) * (size_t)lat_cells * stride);
+    const size_t need = align256(off_latE + sizeof(int) * (size_t)lat_cells);
+    if (need > (size_t)PHMM_STATIC_SCRATCH_BYTES) {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "phmm_estep_static: batch needs %zu bytes of scratch, more than the %zu bytes the "
+                 "allocation-free entry point holds; split the batch or use phmm_estep",
+                 need, (size_t)PHMM_STATIC_SCRATCH_BYTES);
+        return fail(PHMM_E_ARG, msg);
+    }
+    std::sort(g_static_order, g_static_order + P_, [&](int a, int c) {
+        const int64_t ca = (int64_t)(b->Lx_host[a] + 1) * (b->Ly_host[a] + 1);
+        const int64_t cc = (int64_t)(b->Lx_host[c] + 1) * (b->Ly_host[c] + 1);
+        return ca != cc ? ca > cc : a < c;
+    });
+    int n_items = 0;
+    for (int q = 0; q < P_; ++q) {
+        const int p = g_static_order[q];
+        for (int s = 0; s < g_static_meta[p].n_stripes; ++s) g_static_items[n_items++] = make_int2(p, s);
+    }
+    for (int q = 0; q < P_; ++q) {
+        const int p = g_static_order[q];
+        for (int s = g_static_meta[p].n_stripes - 1; s >= 0; --s) g_static_items[n_items++] = make_int2(p, s);
+    }
+    // ---- copy the work description, clear what must start at zero
+    CUDA_TRY(cudaMemcpyAsync(base + off_meta, g_static_meta, sizeof(PairMeta) * P_, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(base + off_items, g_static_items, sizeof(int2) * 2 * stripes,
+                             cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemsetAsync(base + off_cnt, 0, 4 * sizeof(int), stream));
+    CUDA_TRY(cudaMemsetAsync(base + off_prog, 0, sizeof(int) * 2 * stripes, stream));
+    CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int32_t) * P_, stream));
+    CUDA_TRY(cudaMemsetAsync(n_trans, 0, sizeof(double) * (size_t)P_ * N * N, stream));
+    CUDA_TRY(cudaMemsetAsync(cntM, 0, sizeof(double) * (size_t)P_ * G * 441, stream));
+    CUDA_TRY(cudaMemsetAsync(cntI, 0, sizeof(double) * (size_t)P_ * G * 21, stream));
+    CUDA_TRY(cudaMemsetAsync(cntD, 0, sizeof(double) * (size_t)P_ * G * 21, stream));
+    K.res = b->residues;
+    K.meta = (const PairMeta *)(base + off_meta);
+    K.n_items = stripes;
+    K.chi = b->chi;
+    K.chi_stride = b->chi_per_pair ? (int64_t)N * N : 0;
+    K.eM = b->emit_M;
+    K.eI = b->emit_I;
+    K.eD = b->emit_D;
+    K.eM_stride = b->emit_per_pair ? (int64_t)G * 441 : 0;
+    K.eID_stride = b->emit_per_pair ? (int64_t)G * 21 : 0;
+    K.lat = (float *)(base + off_lat);
+    K.lat_exp = (int *)(base + off_latE);
+    K.edge = (float *)(base + off_edge);
+    K.edge_exp = (int *)(base + off_edgeE);
+    K.ll = ll;
+    K.status = status;
+    K.n_trans = n_trans;
+    K.cntM = cntM;
+    K.cntI = cntI;
+    K.cntD = cntD;
+    K.F_log = K.B_log = K.post = nullptr;
+    K.max_ly = max_ly;
+    K.spin_limit = 40LL * 1000 * 1000;
+    phmm_plan launch_ctx;   // carries the SM count for the shared launchers; owns no memory
+    launch_ctx.sm_count = g_static_sms[dev];
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool bwd = pass == 1;
+        K.items = (const int2 *)(base + off_items) + (bwd ? stripes : 0);
+        K.counter = (int *)(base + off_cnt) + (bwd ? 1 : 0);
+        K.progress = (int *)(base + off_prog) + (bwd ? stripes : 0);
+        if (wl) {
+            if ((rc = wl(&launch_ctx, K, stripes, max_ly, bwd, stream))) return rc;
+        } else {
+            const int threads = 32 * K.NQ;
+            const SmemLayout L = make_layout(K.NS, K.NQ, G, max_ly, bwd);
+            auto kern = bwd ? backward_kernel : forward_kernel;
+            CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
+            int occ = 0;
+            CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, L.bytes));
+            if (occ < 1) return fail(PHMM_E_ARG, "kernel does not fit on an SM (shared memory)");
+            kern<<<std::min(stripes, g_static_sms[dev] * occ), threads, L.bytes, stream>>>(K);
+            CUDA_TRY(cudaGetLastError());
+        }
+    }
+    return 0;
+}

@@ -18,7 +18,7 @@ from .build import LIB_PATH
 _LIB = None
 
 EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep',
-           'phmm_estep_tables', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_set_variant',
+           'phmm_estep_tables', 'phmm_estep_static', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_set_variant',
            'phmm_last_variant', 'phmm_last_launch_count',
            'phmm_last_error', 'phmm_version')
 
@@ -68,6 +68,8 @@ def load(path=None):
     lib.phmm_forward.restype = ctypes.c_int
     lib.phmm_estep.argtypes = [vp, ctypes.POINTER(Batch), vp, vp, vp, vp, vp, vp, vp]
     lib.phmm_estep.restype = ctypes.c_int
+    lib.phmm_estep_static.argtypes = [ctypes.POINTER(ModelDesc), ctypes.POINTER(Batch)] + [vp] * 7
+    lib.phmm_estep_static.restype = ctypes.c_int
     lib.phmm_estep_tables.argtypes = [vp, ctypes.POINTER(Batch)] + [vp] * 10
     lib.phmm_estep_tables.restype = ctypes.c_int
     lib.phmm_set_timing.argtypes = [vp, ctypes.c_int]

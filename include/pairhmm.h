@@ -156,8 +156,9 @@ int phmm_set_timing(phmm_plan *plan, int enable);
 int phmm_kernel_times(phmm_plan *plan, float *fwd_ms, float *bwd_ms);
 
 /* Kernel family: 0 = automatic (default), 1 = generic kernels (any state
- * space of up to 60 emitting states), 2 = register-resident warp kernels
- * (state spaces with a compiled shape).  phmm_last_variant reports the family
+ * space of up to 60 emitting states), 2 = register-resident warp kernels,
+ * 3 = quad-per-warp block kernels (2 and 3 for state spaces with a compiled
+ * shape).  phmm_last_variant reports the family
  * the last call used.  No counterpart in the reference (it has no kernels). */
 int phmm_set_variant(phmm_plan *plan, int variant);
 int phmm_last_variant(const phmm_plan *plan);

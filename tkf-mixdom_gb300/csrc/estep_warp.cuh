@@ -23,7 +23,8 @@ namespace warp2 {
 
 constexpr int R = 2;          // rows per lane
 constexpr int ROWS = 32 * R;  // rows per stripe
-constexpr int HCW = 32;       // halo chunk width
+constexpr int HCW = 32;       // (layout) halo staging width
+constexpr int PUB = 4;        // edge-row progress is published every PUB columns
 
 template <int NM_, int NI_, int ND_>
 struct Shape {
@@ -158,8 +159,6 @@ __device__ void fwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
     load_model_w<SH>(P, p, m, L, sm, smb, false);
     const unsigned char *ys = smb + L.ys;
     const float4 *chi4 = reinterpret_cast<const float4 *>(sm + L.chi);
-    const float *halo = sm + L.halo;
-    const int *haloE = reinterpret_cast<const int *>(sm) + L.haloE;
 
     // per-row constants: emission bases
     int rowi[R], xch[R];
@@ -187,21 +186,34 @@ __device__ void fwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
     Eprev[0] = Eprev[1] = EXP_NONE;
     const int T_last = (nrows - 1) + Ly;
     bool aborted = false;
+    // halo prefetch state (lane 0 of a stripe that has one above)
+    float hx[SP];
+#pragma unroll
+    for (int s = 0; s < SP; ++s) hx[s] = 0.f;
+    int hxE = EXP_NONE, hx_col = -1, pv = 0;
+    if (si > 0 && lane == 0) pv = ld_acquire(prog_above);
 
     for (int t = 0; t <= T_last; ++t) {
-        // ---- halo chunk (row i0-1) for lane 0's cell A at column t
-        if (si > 0 && (t % HCW) == 0 && t <= Ly) {
-            const int cbeg = t, cend = min(t + HCW, Ly + 1);
+        // ---- halo (row i0-1, column t) for lane 0's cell A: normally prefetched
+        // into registers during step t-1; fetched synchronously otherwise
+        if (si > 0 && t <= Ly) {
             int ok = 1;
-            if (lane == 0) ok = wait_geq(prog_above, cend, P.spin_limit) ? 1 : 0;
+            if (lane == 0 && hx_col != t) {
+                if (!wait_geq(prog_above, t + 1, P.spin_limit)) {
+                    ok = 0;
+                } else {
+                    const float4 *src = reinterpret_cast<const float4 *>(edge_above + (int64_t)t * SP);
+#pragma unroll
+                    for (int q = 0; q < SP / 4; ++q) {
+                        const float4 v = __ldcg(src + q);
+                        hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
+                    }
+                    hxE = __ldcg(edgeE_above + t);
+                    hx_col = t;
+                }
+            }
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) { aborted = true; break; }
-            float *hb = sm + L.halo;
-            int *hbE = reinterpret_cast<int *>(sm) + L.haloE;
-            const int n = (cend - cbeg) * SP;
-            for (int idx = lane; idx < n; idx += 32) hb[idx] = __ldcg(edge_above + (int64_t)cbeg * SP + idx);
-            for (int col = lane; col < cend - cbeg; col += 32) hbE[col] = __ldcg(edgeE_above + cbeg + col);
-            __syncwarp();
         }
         int jc[R];
         bool valid[R];
@@ -213,7 +225,7 @@ __device__ void fwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
         // ---- predecessor exponents
         int EdA = __shfl_up_sync(0xffffffffu, Eprev[R - 1], 1);
         const bool lane0_halo = (lane == 0) && (si > 0) && (t <= Ly);
-        if (lane == 0) EdA = lane0_halo ? haloE[t % HCW] : EXP_NONE;
+        if (lane == 0) EdA = lane0_halo ? hxE : EXP_NONE;
         // existence of predecessors
         const bool hasI0 = jc[0] >= 1, hasD0 = rowi[0] >= 1, hasM0 = hasI0 && hasD0;
         const bool hasI1 = jc[1] >= 1, hasD1 = rowi[1] >= 1, hasM1 = hasI1 && hasD1;
@@ -229,7 +241,7 @@ __device__ void fwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
 #pragma unroll
         for (int s = 0; s < NSRC; ++s) {
             float dA = __shfl_up_sync(0xffffffffu, prev[R - 1][s], 1);
-            if (lane == 0) dA = lane0_halo ? halo[(t % HCW) * SP + s] : 0.f;
+            if (lane == 0) dA = lane0_halo ? hx[s] : 0.f;
             d0[s] = dA;
             const float pI0 = prev[0][s], pD0 = dA, pM0 = m0[s];
             const float pI1 = prev[1][s], pD1 = prev[0][s], pM1 = pp[s];
@@ -324,7 +336,7 @@ __device__ void fwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
                 }
                 edgeE_mine[jc[c]] = Enew[c];
                 const int jb = jc[c];
-                if (((jb + 1) % HCW) == 0 || jb == Ly) st_release(prog_mine, jb + 1);
+                if (((jb + 1) % PUB) == 0 || jb == Ly) st_release(prog_mine, jb + 1);
             }
             if (rowi[c] == Lx && jc[c] == Ly && si + 1 == m.n_stripes) {
                 double a = 0.0;
@@ -349,6 +361,20 @@ __device__ void fwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
         Epp = Eprev[0];
         Eprev[0] = Enew[0];
         Eprev[1] = Enew[1];
+        // ---- prefetch halo column t+1 when the progress read last step covers it
+        if (si > 0 && lane == 0 && t + 1 <= Ly) {
+            if (pv > t + 1) {
+                const float4 *src = reinterpret_cast<const float4 *>(edge_above + (int64_t)(t + 1) * SP);
+#pragma unroll
+                for (int q = 0; q < SP / 4; ++q) {
+                    const float4 v = __ldcg(src + q);
+                    hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
+                }
+                hxE = __ldcg(edgeE_above + t + 1);
+                hx_col = t + 1;
+            }
+            pv = ld_acquire(prog_above);
+        }
     }
     if (aborted) {
         if (lane == 31 && has_below) st_release(prog_mine, Ly + 1);
@@ -411,8 +437,6 @@ __device__ void bwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
     load_model_w<SH>(P, p, m, L, sm, smb, true);
     const unsigned char *ys = smb + L.ys;
     const float4 *chiB4 = reinterpret_cast<const float4 *>(sm + L.chi);   // chiB[k][s]
-    const float *halo = sm + L.halo;
-    const int *haloE = reinterpret_cast<const int *>(sm) + L.haloE;
     float *fst = sm + L.fst;
     int *fstE = reinterpret_cast<int *>(sm) + L.fstE;
     float *ust = sm + L.ust;
@@ -473,23 +497,36 @@ __device__ void bwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
     };
     prefetch(T_last);
     bool aborted = false;
+    // halo prefetch state (lane 31 of a stripe that has one below)
+    float hx[SP];
+#pragma unroll
+    for (int s = 0; s < SP; ++s) hx[s] = 0.f;
+    int hxE = EXP_NONE, hx_col = -1, pv = 0;
+    if (has_below && lane == 31) pv = ld_acquire(prog_below);
 
     for (int t = T_last; t >= 0; --t) {
         prefetch(t - 1);
-        // ---- halo chunk (row i0+64) for lane 31's cell B at column t-63
+        // ---- halo (row i0+64, column t-63) for lane 31's cell B: normally
+        // prefetched into registers during step t+1; fetched synchronously otherwise
         const int jb = t - (ROWS - 1);
-        if (has_below && jb >= 0 && jb <= Ly && (jb == Ly || (jb % HCW) == HCW - 1)) {
-            const int cbeg = (jb / HCW) * HCW, cend = jb + 1;
+        if (has_below && jb >= 0 && jb <= Ly) {
             int ok = 1;
-            if (lane == 0) ok = wait_geq(prog_below, Ly + 1 - cbeg, P.spin_limit) ? 1 : 0;
-            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (lane == 31 && hx_col != jb) {
+                if (!wait_geq(prog_below, Ly + 1 - jb, P.spin_limit)) {
+                    ok = 0;
+                } else {
+                    const float4 *src = reinterpret_cast<const float4 *>(edge_below + (int64_t)jb * SP);
+#pragma unroll
+                    for (int q = 0; q < SP / 4; ++q) {
+                        const float4 v = __ldcg(src + q);
+                        hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
+                    }
+                    hxE = __ldcg(edgeE_below + jb);
+                    hx_col = jb;
+                }
+            }
+            ok = __shfl_sync(0xffffffffu, ok, 31);
             if (!ok) { aborted = true; break; }
-            float *hb = sm + L.halo;
-            int *hbE = reinterpret_cast<int *>(sm) + L.haloE;
-            const int n = (cend - cbeg) * SP;
-            for (int idx = lane; idx < n; idx += 32) hb[idx] = __ldcg(edge_below + (int64_t)cbeg * SP + idx);
-            for (int col = lane; col < cend - cbeg; col += 32) hbE[col] = __ldcg(edgeE_below + cbeg + col);
-            __syncwarp();
         }
         int jc[R];
         bool valid[R];
@@ -500,7 +537,7 @@ __device__ void bwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
         }
         const bool lane31_halo = (lane == 31) && has_below && jc[1] >= 0 && jc[1] <= Ly;
         int EdRn = __shfl_down_sync(0xffffffffu, Ewn[0], 1);
-        if (lane == 31) EdRn = lane31_halo ? haloE[jc[1] % HCW] : EXP_NONE;
+        if (lane == 31) EdRn = lane31_halo ? hxE : EXP_NONE;
         // successor existence and exponents
         const bool term0 = valid[0] && rowi[0] == Lx && jc[0] == Ly;
         const bool term1 = valid[1] && rowi[1] == Lx && jc[1] == Ly;
@@ -521,7 +558,7 @@ __device__ void bwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
 #pragma unroll
         for (int k = 0; k < NE; ++k) {
             float dk = __shfl_down_sync(0xffffffffu, wn[0][k], 1);
-            if (lane == 31) dk = lane31_halo ? halo[(jc[1] % HCW) * SP + k] : 0.f;
+            if (lane == 31) dk = lane31_halo ? hx[k] : 0.f;
             dR[k] = dk;
             const int ty = SH::type_of(k);
             const float w0 = ty == T_M ? wnn1[k] * sM0 : (ty == T_I ? wn[0][k] * sI0 : wn[1][k] * sD0);
@@ -665,7 +702,7 @@ __device__ void bwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
                         dst[q] = make_float4(v[0], v[1], v[2], v[3]);
                     }
                     edgeE_mine[jc[c]] = Eb[c];
-                    if ((jc[c] % HCW) == 0) st_release(prog_mine, Ly + 1 - jc[c]);
+                    if ((jc[c] % PUB) == 0) st_release(prog_mine, Ly + 1 - jc[c]);
                 }
             }
         }
@@ -717,6 +754,20 @@ __device__ void bwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
         Ewnn1 = Ewn[1];
         Ewn[0] = valid[0] ? Eb[0] : EXP_NONE;
         Ewn[1] = valid[1] ? Eb[1] : EXP_NONE;
+        // ---- prefetch halo column jb-1 when the progress read last step covers it
+        if (has_below && lane == 31 && jb - 1 >= 0 && jb - 1 <= Ly) {
+            if (pv >= Ly + 1 - (jb - 1)) {
+                const float4 *src = reinterpret_cast<const float4 *>(edge_below + (int64_t)(jb - 1) * SP);
+#pragma unroll
+                for (int q = 0; q < SP / 4; ++q) {
+                    const float4 v = __ldcg(src + q);
+                    hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
+                }
+                hxE = __ldcg(edgeE_below + jb - 1);
+                hx_col = jb - 1;
+            }
+            pv = ld_acquire(prog_below);
+        }
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
     if (aborted) {

@@ -822,6 +822,7 @@ __global__ void fill_f64(double *p, int64_t n, double v) {
 }  // namespace
 
 #include "estep_warp.cuh"
+#include "estep_block.cuh"
 
 namespace {
 
@@ -863,7 +864,7 @@ struct phmm_plan {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // register-resident warp kernels for this state space (null: generic kernels)
     int w_nm = 0, w_ni = 0, w_nd = 0;
-    int variant = 0;        // 0 automatic, 1 generic quad kernels, 2 warp kernels
+    int variant = 0;        // 0 automatic, 1 generic, 2 warp kernels, 3 block kernels
     int last_variant = 0;
 };
 
@@ -902,6 +903,26 @@ const WarpShapeEntry kWarpShapes[] = {
     {4, 8, 8, launch_warp_shape<4, 8, 8>},   // MixDom K*F=4 (22 states)
 };
 
+// ---- launchers of the quad-per-warp block kernels, one per padded state count
+using BlockLauncher = int (*)(phmm_plan *, KParams &, int, int, bool, cudaStream_t);
+
+template <class SH>
+int launch_block(phmm_plan *plan, KParams &K, int n_items, int max_ly, bool bwd, cudaStream_t stream);
+
+struct BlockShapeEntry { int ns; BlockLauncher fn; };
+const BlockShapeEntry kBlockShapes[] = {
+    {12, launch_block<blk::BShape<12>>},   // TKF91/92, MixDom K*F=1..2 with few states
+    {20, launch_block<blk::BShape<20>>},   // MixDom K*F=3 (17 states)
+    {24, launch_block<blk::BShape<24>>},   // MixDom K*F=4 (22 states)
+    {44, launch_block<blk::BShape<44>>},   // MixDom K*F=8 (42 states)
+};
+
+BlockLauncher find_block_launcher(int ns) {
+    for (const auto &e : kBlockShapes)
+        if (e.ns == ns) return e.fn;
+    return nullptr;
+}
+
 WarpLauncher find_warp_launcher(int nm, int ni, int nd) {
     for (const auto &e : kWarpShapes)
         if (e.nm == nm && e.ni == ni && e.nd == nd) return e.fn;
@@ -926,12 +947,27 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     // kernel family: register-resident warp kernels when the shape has one and
     // no lattice tables are requested; the generic quad kernels otherwise
     WarpLauncher wl = nullptr;
-    if (plan->variant != 1 && !F_log && !B_log && !post)
-        wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
+    BlockLauncher bl = nullptr;
+    const bool tables = F_log || B_log || post;
+    // automatic choice (measured on GB300, 17 states): the block kernels have
+    // the shorter forward step, the warp kernels the faster fused backward
+    if (!tables && plan->variant == 0) {
+        if (estep) {
+            wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
+            if (!wl) bl = find_block_launcher(K.NS);
+        } else {
+            bl = find_block_launcher(K.NS);
+            if (!bl) wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
+        }
+    }
+    if (!tables && plan->variant == 3) bl = find_block_launcher(K.NS);
+    if (!tables && plan->variant == 2) wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
     if (plan->variant == 2 && !wl) return fail(PHMM_E_ARG, "no warp kernel for this state space");
-    const int rows = wl ? warp2::ROWS : TH;
-    const int stride = wl ? ((plan->w_nm + plan->w_ni + plan->w_nd + 1 + 3) & ~3) : K.NS;
-    plan->last_variant = wl ? 2 : 1;
+    if (plan->variant == 3 && !bl) return fail(PHMM_E_ARG, "no block kernel for this state space");
+    const int rows = bl ? blk::ROWS : (wl ? warp2::ROWS : TH);
+    const int stride = bl ? K.NS : (wl ? ((plan->w_nm + plan->w_ni + plan->w_nd + 1 + 3) & ~3) : K.NS);
+    const int estride = bl ? blk::nbp_of(K.NS / 4) : 1;   // exponents per cell
+    plan->last_variant = bl ? 3 : (wl ? 2 : 1);
     // ---- plan: stripes, offsets, longest-first order
     std::vector<int> order(P_);
     for (int p = 0; p < P_; ++p) {
@@ -973,11 +1009,11 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     if ((rc = ensure((char **)&plan->meta, &plan->meta_cap, sizeof(PairMeta) * P_))) return rc;
     if ((rc = ensure((char **)&plan->items, &plan->items_cap, sizeof(int2) * plan->h_items.size()))) return rc;
     if ((rc = ensure(&plan->edge, &plan->edge_cap, (size_t)edge_cells * stride))) return rc;
-    if ((rc = ensure(&plan->edge_exp, &plan->edgeE_cap, (size_t)edge_cells))) return rc;
+    if ((rc = ensure(&plan->edge_exp, &plan->edgeE_cap, (size_t)edge_cells * estride))) return rc;
     if ((rc = ensure(&plan->progress, &plan->prog_cap, (size_t)2 * stripes))) return rc;
     if (estep) {
         if ((rc = ensure(&plan->lat, &plan->lat_cap, (size_t)lat_cells * stride))) return rc;
-        if ((rc = ensure(&plan->lat_exp, &plan->latE_cap, (size_t)lat_cells))) return rc;
+        if ((rc = ensure(&plan->lat_exp, &plan->latE_cap, (size_t)lat_cells * estride))) return rc;
     }
     CUDA_TRY(cudaMemcpyAsync(plan->meta, plan->h_meta.data(), sizeof(PairMeta) * P_, cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(plan->items, plan->h_items.data(), sizeof(int2) * plan->h_items.size(),
@@ -1026,7 +1062,9 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
         K.counter = plan->counters + (bwd ? 1 : 0);
         K.progress = plan->progress + (bwd ? stripes : 0);
         if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[bwd ? 2 : 0], stream));
-        if (wl) {
+        if (bl) {
+            if ((rc = bl(plan, K, n_items, max_ly, bwd, stream))) return rc;
+        } else if (wl) {
             if ((rc = wl(plan, K, n_items, max_ly, bwd, stream))) return rc;
         } else {
             const int threads = 32 * K.NQ;
@@ -1044,6 +1082,21 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
         plan->launches++;
     }
     plan->timed_bwd = estep;
+    return 0;
+}
+
+template <class SH>
+int launch_block(phmm_plan *plan, KParams &K, int n_items, int max_ly, bool bwd, cudaStream_t stream) {
+    const blk::SmemB L = blk::make_smem_b(SH::NS, SH::NB, 1, K.G, max_ly, bwd);
+    auto kern = bwd ? blk::backward_block_kernel<SH> : blk::forward_block_kernel<SH>;
+    const int threads = 32 * (SH::NB + (bwd ? blk::NCW : 0));
+    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
+    int occ = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, L.bytes));
+    if (occ < 1) return fail(PHMM_E_ARG, "block kernel does not fit on an SM (shared memory)");
+    const int grid = std::min(n_items, plan->sm_count * occ);
+    kern<<<grid, threads, L.bytes, stream>>>(K);
+    CUDA_TRY(cudaGetLastError());
     return 0;
 }
 
@@ -1224,9 +1277,11 @@ int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch, double *ll_out, 
 int phmm_last_launch_count(const phmm_plan *plan) { return plan ? plan->launches : 0; }
 
 int phmm_set_variant(phmm_plan *plan, int variant) {
-    if (!plan || variant < 0 || variant > 2) return fail(PHMM_E_ARG, "bad variant");
+    if (!plan || variant < 0 || variant > 3) return fail(PHMM_E_ARG, "bad variant");
     if (variant == 2 && !find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd))
         return fail(PHMM_E_ARG, "no warp kernel for this state space");
+    if (variant == 3 && !find_block_launcher(plan->base.NS))
+        return fail(PHMM_E_ARG, "no block kernel for this state space");
     plan->variant = variant;
     return 0;
 }

@@ -136,7 +136,7 @@ class Plan:
         return self.lib.phmm_last_launch_count(self.handle)
 
     def set_variant(self, variant):
-        """0 automatic, 1 generic kernels, 2 register-resident warp kernels."""
+        """0 automatic, 1 generic, 2 register-resident warp, 3 quad-per-warp block kernels."""
         _check(self.lib.phmm_set_variant(self.handle, int(variant)), 'phmm_set_variant')
 
     @property

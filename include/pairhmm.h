@@ -116,6 +116,27 @@ int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch,
                       double *cnt_I, double *cnt_D, int32_t *status_out,
                       double *log_F, double *log_B, double *post, void *stream);
 
+/* Caller-owned workspace.  phmm_workspace_bytes stores in *bytes the device
+ * scratch one phmm_forward_ws (estep 0) or phmm_estep_ws (estep 1) call on
+ * this batch needs; only the batch's host fields (n_pairs, Lx_host, Ly_host,
+ * x_off_host, y_off_host) are read.  The _ws calls then run exactly as
+ * phmm_forward / phmm_estep, with all scratch carved from `workspace`
+ * (256-byte aligned, at least that many bytes) instead of plan-owned
+ * buffers, and allocate nothing.  Calls on one plan with distinct workspaces
+ * may be in flight on different streams at the same time (issue them from
+ * one host thread).  No counterpart in the reference, whose XLA runtime owns
+ * the scratch; this is what a serving loop budgets HBM with when it admits
+ * requests. */
+int phmm_workspace_bytes(phmm_plan *plan, const phmm_batch *batch, int estep,
+                         size_t *bytes);
+int phmm_forward_ws(phmm_plan *plan, const phmm_batch *batch, void *workspace,
+                    size_t workspace_bytes, double *ll_out, int32_t *status_out,
+                    void *stream);
+int phmm_estep_ws(phmm_plan *plan, const phmm_batch *batch, void *workspace,
+                  size_t workspace_bytes, double *ll_out, double *n_trans,
+                  double *cnt_M, double *cnt_I, double *cnt_D,
+                  int32_t *status_out, void *stream);
+
 /* E-step that allocates nothing: no cudaMalloc, cudaFree or other allocating
  * call.  No counterpart in the reference.
  *

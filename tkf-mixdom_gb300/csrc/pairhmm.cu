@@ -929,19 +929,30 @@ WarpLauncher find_warp_launcher(int nm, int ni, int nd) {
     return nullptr;
 }
 
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// One call of the forward (estep false) or E-step kernels.  Scratch comes from
+// the plan (grown on demand) unless the caller passes a workspace `ws` of
+// `ws_bytes`; with `ws_need` set, nothing runs and the workspace size the
+// call would need is stored there (only the host fields of the batch are read).
 int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_trans,
         double *cntM, double *cntI, double *cntD, int32_t *status, double *F_log, double *B_log,
-        double *post, void *stream_) {
+        double *post, void *stream_, void *ws = nullptr, size_t ws_bytes = 0, size_t *ws_need = nullptr) {
     if (!plan || !b) return fail(PHMM_E_ARG, "null plan or batch");
     cudaStream_t stream = (cudaStream_t)stream_;
-    plan->launches = 0;
+    if (!ws_need) plan->launches = 0;
     const int P_ = b->n_pairs;
     if (P_ < 0) return fail(PHMM_E_ARG, "n_pairs < 0");
+    if (ws_need) *ws_need = 0;
     if (P_ == 0) return 0;
-    if (!b->Lx_host || !b->Ly_host || !b->x_off_host || !b->y_off_host || !b->residues || !b->chi ||
-        !b->emit_M || !b->emit_I || !b->emit_D || !ll || !status)
-        return fail(PHMM_E_ARG, "null batch pointer");
-    if (estep && (!n_trans || !cntM || !cntI || !cntD)) return fail(PHMM_E_ARG, "null E-step output");
+    if (!b->Lx_host || !b->Ly_host || !b->x_off_host || !b->y_off_host)
+        return fail(PHMM_E_ARG, "null batch length or offset array");
+    if (!ws_need) {
+        if (!b->residues || !b->chi || !b->emit_M || !b->emit_I || !b->emit_D || !ll || !status)
+            return fail(PHMM_E_ARG, "null batch pointer");
+        if (estep && (!n_trans || !cntM || !cntI || !cntD)) return fail(PHMM_E_ARG, "null E-step output");
+        if (ws && ((uintptr_t)ws & 255)) return fail(PHMM_E_ARG, "workspace must be 256-byte aligned");
+    }
     KParams K = plan->base;
     const int N = K.N, G = K.G;
     // kernel family: register-resident warp kernels when the shape has one and
@@ -967,7 +978,7 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     const int rows = bl ? blk::ROWS : (wl ? warp2::ROWS : TH);
     const int stride = bl ? K.NS : (wl ? ((plan->w_nm + plan->w_ni + plan->w_nd + 1 + 3) & ~3) : K.NS);
     const int estride = bl ? blk::nbp_of(K.NS / 4) : 1;   // exponents per cell
-    plan->last_variant = bl ? 3 : (wl ? 2 : 1);
+    if (!ws_need) plan->last_variant = bl ? 3 : (wl ? 2 : 1);
     // ---- plan: stripes, offsets, longest-first order
     std::vector<int> order(P_);
     for (int p = 0; p < P_; ++p) {
@@ -1006,20 +1017,60 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
         for (int p : order)
             for (int s = plan->h_meta[p].n_stripes - 1; s >= 0; --s) plan->h_items.push_back(make_int2(p, s));
     int rc;
-    if ((rc = ensure((char **)&plan->meta, &plan->meta_cap, sizeof(PairMeta) * P_))) return rc;
-    if ((rc = ensure((char **)&plan->items, &plan->items_cap, sizeof(int2) * plan->h_items.size()))) return rc;
-    if ((rc = ensure(&plan->edge, &plan->edge_cap, (size_t)edge_cells * stride))) return rc;
-    if ((rc = ensure(&plan->edge_exp, &plan->edgeE_cap, (size_t)edge_cells * estride))) return rc;
-    if ((rc = ensure(&plan->progress, &plan->prog_cap, (size_t)2 * stripes))) return rc;
-    if (estep) {
-        if ((rc = ensure(&plan->lat, &plan->lat_cap, (size_t)lat_cells * stride))) return rc;
-        if ((rc = ensure(&plan->lat_exp, &plan->latE_cap, (size_t)lat_cells * estride))) return rc;
+    // ---- scratch: plan-owned buffers, or carved from the caller's workspace
+    const size_t o_meta = 0;
+    const size_t o_items = align256(o_meta + sizeof(PairMeta) * P_);
+    const size_t o_cnt = align256(o_items + sizeof(int2) * plan->h_items.size());
+    const size_t o_prog = align256(o_cnt + 4 * sizeof(int));
+    const size_t o_edge = align256(o_prog + sizeof(int) * 2 * (size_t)stripes);
+    const size_t o_edgeE = align256(o_edge + sizeof(float) * (size_t)edge_cells * stride);
+    const size_t o_lat = align256(o_edgeE + sizeof(int) * (size_t)edge_cells * estride);
+    const size_t o_latE = align256(o_lat + (estep ? sizeof(float) * (size_t)lat_cells * stride : 0));
+    const size_t need = align256(o_latE + (estep ? sizeof(int) * (size_t)lat_cells * estride : 0));
+    if (ws_need) { *ws_need = need; return 0; }
+    void *d_meta, *d_items;
+    int *d_counters, *d_progress, *d_edge_exp, *d_lat_exp;
+    float *d_edge, *d_lat;
+    if (ws) {
+        if (ws_bytes < need) {
+            char msg[200];
+            snprintf(msg, sizeof msg, "workspace of %zu bytes is too small: this batch needs %zu bytes", ws_bytes,
+                     need);
+            return fail(PHMM_E_ARG, msg);
+        }
+        unsigned char *w = (unsigned char *)ws;
+        d_meta = w + o_meta;
+        d_items = w + o_items;
+        d_counters = (int *)(w + o_cnt);
+        d_progress = (int *)(w + o_prog);
+        d_edge = (float *)(w + o_edge);
+        d_edge_exp = (int *)(w + o_edgeE);
+        d_lat = estep ? (float *)(w + o_lat) : nullptr;
+        d_lat_exp = estep ? (int *)(w + o_latE) : nullptr;
+    } else {
+        if ((rc = ensure((char **)&plan->meta, &plan->meta_cap, sizeof(PairMeta) * P_))) return rc;
+        if ((rc = ensure((char **)&plan->items, &plan->items_cap, sizeof(int2) * plan->h_items.size()))) return rc;
+        if ((rc = ensure(&plan->edge, &plan->edge_cap, (size_t)edge_cells * stride))) return rc;
+        if ((rc = ensure(&plan->edge_exp, &plan->edgeE_cap, (size_t)edge_cells * estride))) return rc;
+        if ((rc = ensure(&plan->progress, &plan->prog_cap, (size_t)2 * stripes))) return rc;
+        if (estep) {
+            if ((rc = ensure(&plan->lat, &plan->lat_cap, (size_t)lat_cells * stride))) return rc;
+            if ((rc = ensure(&plan->lat_exp, &plan->latE_cap, (size_t)lat_cells * estride))) return rc;
+        }
+        d_meta = plan->meta;
+        d_items = plan->items;
+        d_counters = plan->counters;
+        d_progress = plan->progress;
+        d_edge = plan->edge;
+        d_edge_exp = plan->edge_exp;
+        d_lat = plan->lat;
+        d_lat_exp = plan->lat_exp;
     }
-    CUDA_TRY(cudaMemcpyAsync(plan->meta, plan->h_meta.data(), sizeof(PairMeta) * P_, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(plan->items, plan->h_items.data(), sizeof(int2) * plan->h_items.size(),
+    CUDA_TRY(cudaMemcpyAsync(d_meta, plan->h_meta.data(), sizeof(PairMeta) * P_, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_items, plan->h_items.data(), sizeof(int2) * plan->h_items.size(),
                              cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemsetAsync(plan->counters, 0, 2 * sizeof(int), stream));
-    CUDA_TRY(cudaMemsetAsync(plan->progress, 0, sizeof(int) * 2 * stripes, stream));
+    CUDA_TRY(cudaMemsetAsync(d_counters, 0, 2 * sizeof(int), stream));
+    CUDA_TRY(cudaMemsetAsync(d_progress, 0, sizeof(int) * 2 * stripes, stream));
     CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int32_t) * P_, stream));
     if (estep) {
         CUDA_TRY(cudaMemsetAsync(n_trans, 0, sizeof(double) * (size_t)P_ * N * N, stream));
@@ -1032,7 +1083,7 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     if (post) CUDA_TRY(cudaMemsetAsync(post, 0, sizeof(double) * (size_t)tab_cells * N, stream));
 
     K.res = b->residues;
-    K.meta = (const PairMeta *)plan->meta;
+    K.meta = (const PairMeta *)d_meta;
     K.n_items = n_items;
     K.chi = b->chi;
     K.chi_stride = b->chi_per_pair ? (int64_t)N * N : 0;
@@ -1041,10 +1092,10 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     K.eD = b->emit_D;
     K.eM_stride = b->emit_per_pair ? (int64_t)G * 441 : 0;
     K.eID_stride = b->emit_per_pair ? (int64_t)G * 21 : 0;
-    K.lat = estep ? plan->lat : nullptr;
-    K.lat_exp = estep ? plan->lat_exp : nullptr;
-    K.edge = plan->edge;
-    K.edge_exp = plan->edge_exp;
+    K.lat = estep ? d_lat : nullptr;
+    K.lat_exp = estep ? d_lat_exp : nullptr;
+    K.edge = d_edge;
+    K.edge_exp = d_edge_exp;
     K.ll = ll;
     K.status = status;
     K.n_trans = n_trans;
@@ -1058,9 +1109,9 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     K.spin_limit = 40LL * 1000 * 1000;
     for (int pass = 0; pass < (estep ? 2 : 1); ++pass) {
         const bool bwd = pass == 1;
-        K.items = (const int2 *)plan->items + (bwd ? n_items : 0);
-        K.counter = plan->counters + (bwd ? 1 : 0);
-        K.progress = plan->progress + (bwd ? stripes : 0);
+        K.items = (const int2 *)d_items + (bwd ? n_items : 0);
+        K.counter = d_counters + (bwd ? 1 : 0);
+        K.progress = d_progress + (bwd ? stripes : 0);
         if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[bwd ? 2 : 0], stream));
         if (bl) {
             if ((rc = bl(plan, K, n_items, max_ly, bwd, stream))) return rc;
@@ -1274,6 +1325,27 @@ int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch, double *ll_out, 
                stream);
 }
 
+int phmm_workspace_bytes(phmm_plan *plan, const phmm_batch *batch, int estep, size_t *bytes) {
+    if (!bytes) return fail(PHMM_E_ARG, "null output");
+    return run(plan, batch, estep != 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+               nullptr, nullptr, nullptr, 0, bytes);
+}
+
+int phmm_forward_ws(phmm_plan *plan, const phmm_batch *batch, void *workspace, size_t workspace_bytes,
+                    double *ll_out, int32_t *status_out, void *stream) {
+    if (!workspace) return fail(PHMM_E_ARG, "null workspace");
+    return run(plan, batch, false, ll_out, nullptr, nullptr, nullptr, nullptr, status_out, nullptr, nullptr,
+               nullptr, stream, workspace, workspace_bytes);
+}
+
+int phmm_estep_ws(phmm_plan *plan, const phmm_batch *batch, void *workspace, size_t workspace_bytes,
+                  double *ll_out, double *n_trans, double *cnt_M, double *cnt_I, double *cnt_D,
+                  int32_t *status_out, void *stream) {
+    if (!workspace) return fail(PHMM_E_ARG, "null workspace");
+    return run(plan, batch, true, ll_out, n_trans, cnt_M, cnt_I, cnt_D, status_out, nullptr, nullptr, nullptr,
+               stream, workspace, workspace_bytes);
+}
+
 int phmm_last_launch_count(const phmm_plan *plan) { return plan ? plan->launches : 0; }
 
 int phmm_set_variant(phmm_plan *plan, int variant) {
@@ -1313,8 +1385,6 @@ int g_static_sms[kStaticMaxDevices] = {};
 PairMeta g_static_meta[kStaticMaxPairs];
 int2 g_static_items[kStaticMaxItems];
 int g_static_order[kStaticMaxPairs];
-
-size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // Model slot tables for a description (same layout as phmm_plan_create).
 int static_model(const phmm_model_desc *md, KParams *K, int *nm, int *ni, int *nd) {

@@ -18,7 +18,8 @@ from .build import LIB_PATH
 _LIB = None
 
 EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep',
-           'phmm_estep_tables', 'phmm_estep_static', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_set_variant',
+           'phmm_estep_tables', 'phmm_workspace_bytes', 'phmm_forward_ws', 'phmm_estep_ws',
+           'phmm_estep_static', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_set_variant',
            'phmm_last_variant', 'phmm_last_launch_count',
            'phmm_last_error', 'phmm_version')
 
@@ -72,6 +73,12 @@ def load(path=None):
     lib.phmm_estep_static.restype = ctypes.c_int
     lib.phmm_estep_tables.argtypes = [vp, ctypes.POINTER(Batch)] + [vp] * 10
     lib.phmm_estep_tables.restype = ctypes.c_int
+    lib.phmm_workspace_bytes.argtypes = [vp, ctypes.POINTER(Batch), ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
+    lib.phmm_workspace_bytes.restype = ctypes.c_int
+    lib.phmm_forward_ws.argtypes = [vp, ctypes.POINTER(Batch), vp, ctypes.c_size_t, vp, vp, vp]
+    lib.phmm_forward_ws.restype = ctypes.c_int
+    lib.phmm_estep_ws.argtypes = [vp, ctypes.POINTER(Batch), vp, ctypes.c_size_t] + [vp] * 7
+    lib.phmm_estep_ws.restype = ctypes.c_int
     lib.phmm_set_timing.argtypes = [vp, ctypes.c_int]
     lib.phmm_set_timing.restype = ctypes.c_int
     lib.phmm_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
@@ -259,6 +266,54 @@ def estep(plan, batch, stream=None, out=None):
                                _ptr(out['n_trans']), _ptr(out['cnt_M']), _ptr(out['cnt_I']),
                                _ptr(out['cnt_D']), _ptr(out['status']),
                                ctypes.c_void_p(s.cuda_stream)), 'phmm_estep')
+    return out
+
+
+def workspace_bytes(plan, batch, estep=True):
+    """phmm_workspace_bytes: device scratch one *_ws call on `batch` needs.
+
+    `batch` is a DeviceBatch or anything with a ``struct()`` giving the C
+    struct; only its host length and offset arrays are read."""
+    n = ctypes.c_size_t()
+    _check(plan.lib.phmm_workspace_bytes(plan.handle, ctypes.byref(batch.struct()), int(bool(estep)),
+                                         ctypes.byref(n)), 'phmm_workspace_bytes')
+    return int(n.value)
+
+
+def host_batch(Lx, Ly):
+    """A length-only batch descriptor (no device data) for workspace queries."""
+    Lx = np.ascontiguousarray(Lx, dtype=np.int32)
+    Ly = np.ascontiguousarray(Ly, dtype=np.int32)
+    xo = np.zeros(Lx.size, np.int64)
+    yo = np.zeros(Lx.size, np.int64)
+    z = torch.zeros(0)
+    return DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo, residues=z, chi=z, emit_M=z, emit_I=z, emit_D=z)
+
+
+def estep_ws(plan, batch, workspace, stream=None, out=None):
+    """phmm_estep_ws: phmm_estep with scratch carved from `workspace` (a uint8
+    device tensor or a (pointer, bytes) pair); allocates nothing."""
+    P = batch.n_pairs
+    N, G = plan.n_states, plan.n_groups
+    dev = batch.residues.device
+    if out is None:
+        out = {
+            'll': torch.empty(P, dtype=torch.float64, device=dev),
+            'n_trans': torch.empty(P, N, N, dtype=torch.float64, device=dev),
+            'cnt_M': torch.empty(P, G, 21, 21, dtype=torch.float64, device=dev),
+            'cnt_I': torch.empty(P, G, 21, dtype=torch.float64, device=dev),
+            'cnt_D': torch.empty(P, G, 21, dtype=torch.float64, device=dev),
+            'status': torch.empty(P, dtype=torch.int32, device=dev),
+        }
+    if isinstance(workspace, torch.Tensor):
+        wptr, wbytes = workspace.data_ptr(), workspace.numel() * workspace.element_size()
+    else:
+        wptr, wbytes = workspace
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    _check(plan.lib.phmm_estep_ws(plan.handle, ctypes.byref(batch.struct()), ctypes.c_void_p(wptr),
+                                  ctypes.c_size_t(wbytes), _ptr(out['ll']), _ptr(out['n_trans']),
+                                  _ptr(out['cnt_M']), _ptr(out['cnt_I']), _ptr(out['cnt_D']),
+                                  _ptr(out['status']), ctypes.c_void_p(s.cuda_stream)), 'phmm_estep_ws')
     return out
 
 

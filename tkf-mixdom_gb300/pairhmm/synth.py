@@ -195,6 +195,112 @@ def make_tkf91_workload(name, n_pairs, law, seed=0):
     return Workload(name, 'tkf91', p, xs, ys, ts, meta={'law': law, 'seed': seed})
 
 
+def _fast_walk(rng, x, chi, st, groups, m_cdf, i_cdf):
+    """walk_descendant with precomputed cumulative tables (for long streams).
+
+    m_cdf[g, a] is the cumulative descendant distribution of an M state of
+    group g over ancestor residue a; i_cdf[g] the insert distribution."""
+    Lx = len(x)
+    N = chi.shape[0]
+    e_idx = int(np.argmax(st == pm.E))
+    w_open = chi.copy()
+    w_open[:, e_idx] = 0.0
+    w_open[:, st == pm.S] = 0.0
+    w_end = chi.copy()
+    w_end[:, (st == pm.M) | (st == pm.D) | (st == pm.S)] = 0.0
+    c_open = np.cumsum(w_open, axis=1)
+    c_end = np.cumsum(w_end, axis=1)
+    u = rng.random(3 * (Lx + 50) * 4)
+    k_u = 0
+    cur, pos, y = 0, 0, []
+    for _ in range(10 * Lx + 1000):
+        c = c_open[cur] if pos < Lx else c_end[cur]
+        if c[-1] <= 0.0:
+            break
+        if k_u + 2 >= u.size:
+            u = rng.random(u.size)
+            k_u = 0
+        k = min(int(np.searchsorted(c, u[k_u] * c[-1], side='right')), N - 1)
+        k_u += 1
+        if k == e_idx:
+            break
+        g = groups[k]
+        if st[k] == pm.M:
+            cm = m_cdf[g, int(x[pos])]
+            y.append(int(np.searchsorted(cm, u[k_u] * cm[-1], side='right')))
+            k_u += 1
+            pos += 1
+        elif st[k] == pm.I:
+            ci = i_cdf[g]
+            y.append(int(np.searchsorted(ci, u[k_u] * ci[-1], side='right')))
+            k_u += 1
+        elif st[k] == pm.D:
+            pos += 1
+        cur = k
+    return np.minimum(np.asarray(y, dtype=np.int64), A - 1)
+
+
+SERVING_MODELS = (('tkf92', 'tkf92', None), ('mixdom2_k3f1c1', 'mixdom2', (3, 1, 1)),
+                  ('mixdom2_k4f2c2', 'mixdom2', (4, 2, 2)))
+
+
+def make_serving_stream(n_requests, rate=5000.0, law=('loguniform', 20, 2000), seed=0):
+    """The serving workload: Poisson arrivals at `rate` requests/s of single
+    pair E-step jobs, the model drawn uniformly from TKF92 (5 states) and
+    MixDom2 with K*F = 3 (17 states) and K*F = 8 (42 states), ancestor
+    lengths from `law`, per-request t ~ LogUniform(0.05, 2), descendants by
+    the conditioned pair-HMM walk of each model.
+
+    Returns (models, requests, offsets): models maps a name to (kind,
+    params); requests is a list of (model name, x, y, t); offsets are the
+    arrival times in seconds from the start."""
+    rng = np.random.default_rng(seed)
+    models = {}
+    for name, kind, shape in SERVING_MODELS:
+        if kind == 'tkf92':
+            models[name] = (kind, tkf_params(rng, ext=float(rng.uniform(0.3, 0.9))))
+        else:
+            models[name] = (kind, mixdom2_params(rng, *shape))
+    names = [m[0] for m in SERVING_MODELS]
+    which = rng.integers(0, len(names), n_requests)
+    Lx = _lengths(rng, law, n_requests)
+    ts = np.exp(rng.uniform(np.log(0.05), np.log(2.0), n_requests))
+    offsets = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    reqs = []
+    for j in range(n_requests):
+        name = names[which[j]]
+        kind, p = models[name]
+        t = torch.as_tensor([ts[j]], dtype=torch.float64)
+        if kind == 'tkf92':
+            st = np.array([pm.S, pm.M, pm.I, pm.D, pm.E])
+            groups = np.zeros(5, np.int64)
+            chi = pm.tkf92_trans(p['ins_rate'], p['del_rate'], t, p['ext'])[0].numpy()
+            sub = pm.transition_matrix(p['Q'], t)[0].numpy()
+            m_cdf = np.cumsum(sub, axis=1)[None]
+            i_cdf = np.cumsum(p['pi'])[None]
+            anc = p['pi']
+        else:
+            K, F = len(p['dom_ins']), p['frag_weights'].shape[1]
+            C = p['class_pis'].shape[0]
+            st = pm.mixdom_state_types(K, F).astype(np.int64)
+            groups = pm.mixdom_state_groups(K, F)
+            chi = pm.build_nested_trans(p['main_ins'], p['main_del'], t, p['dom_ins'], p['dom_del'],
+                                        p['dom_weights'], p['frag_weights'], p['ext_rates'])[0].numpy()
+            cs = pm.class_subs(p['class_S_exch'], p['class_pis'], t)[0].numpy()        # [C,A,A]
+            cd = p['classdist'].reshape(K * F, C)
+            cpi = p['class_pis']
+            wc = cd[:, :, None] * cpi[None, :, :]                                     # [G,C,A]
+            wc = wc / wc.sum(axis=1, keepdims=True)
+            rows = np.einsum('gca,cab->gab', wc, cs)                                  # [G,A,A]
+            m_cdf = np.cumsum(rows, axis=2)
+            i_cdf = np.cumsum((cd[:, :, None] * cpi[None]).sum(axis=1), axis=1)
+            anc = (cd.mean(axis=0)[:, None] * cpi).sum(axis=0)
+        x = rng.choice(A, size=int(Lx[j]), p=anc / anc.sum())
+        y = _fast_walk(rng, x, chi, st, groups, m_cdf, i_cdf)
+        reqs.append((name, x.astype(np.int64), y, float(ts[j])))
+    return models, reqs, offsets
+
+
 # The benchmark configurations (synthetic stand-ins with the stated shapes).
 CONFIGS = {
     'tkf91_64pairs_len50-150': lambda seed=0: make_tkf91_workload(

@@ -50,6 +50,9 @@ def parse_args():
     ap.add_argument('--pairs', type=int, default=0,
                     help='use only the first P pairs (small case for ncu captures)')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    ap.add_argument('--serving-requests', type=int, default=2000,
+                    help='requests in the serving-stream leg (0: skip it)')
+    ap.add_argument('--serving-rate', type=float, default=5000.0)
     return ap.parse_args()
 
 
@@ -203,6 +206,45 @@ def run_reference(args, rank, ws):
     print(json.dumps(line))
 
 
+def serving_leg(n_requests, rate, seed=0):
+    """The serving stream: Poisson arrivals of single-pair E-step requests,
+    models mixed uniformly over TKF92 / MixDom2 K*F=3 / MixDom2 K*F=8,
+    ancestor lengths LogUniform(20, 2000); continuous batching against
+    one-launch-per-request, on the same arrival times."""
+    import torch
+    from pairhmm import synth
+    from pairhmm.serving import Request, Server, ServedModel, latency_summary, run_stream
+    t0 = time.perf_counter()
+    models, reqs, offsets = synth.make_serving_stream(n_requests, rate=rate, seed=seed)
+    gen_s = time.perf_counter() - t0
+    served = [ServedModel(name, kind, p) for name, (kind, p) in models.items()]
+    n_states = {'tkf92': 5, 'mixdom2_k3f1c1': 17, 'mixdom2_k4f2c2': 42}
+    cs = float(sum((len(x) + 1) * (len(y) + 1) * n_states[m] for m, x, y, _ in reqs))
+
+    def one(max_inflight, max_batch):
+        srv = Server(served, arena_bytes=8 << 30, max_inflight=max_inflight, max_batch=max_batch)
+        warm = [Request(-1 - i, m, x, y, t) for i, (m, x, y, t) in enumerate(reqs[:12])]
+        for r in warm:
+            srv.submit(r)
+        srv.drain()
+        torch.cuda.synchronize()
+        rs = [Request(i, m, x, y, t) for i, (m, x, y, t) in enumerate(reqs)]
+        out, wall = run_stream(srv.sched, rs, offsets)
+        summ = latency_summary(out, wall)
+        summ['cell_states_per_s'] = cs / wall
+        summ['batches'] = srv.sched.batches
+        summ['mean_batch'] = float(np.mean(srv.sched.batch_sizes)) if srv.sched.batch_sizes else 0.0
+        summ['peak_arena_bytes'] = int(srv.sched.peak_bytes)
+        return summ
+    cont = one(max_inflight=8, max_batch=64)
+    plain = one(max_inflight=1, max_batch=1)
+    return {'workload': f'Poisson {rate:g} req/s, {n_requests} requests, model uniform over TKF92 (5) / '
+                        'MixDom2 K3F1C1 (17) / MixDom2 K4F2C2 (42), ancestor LogUniform(20,2000)',
+            'arrival_span_s': float(offsets[-1]), 'cell_states': cs,
+            'continuous': cont, 'plain_one_launch_per_request': plain,
+            'arena_bytes': 8 << 30, 'stream_generation_s': gen_s}
+
+
 def main():
     args = parse_args()
     ws, rank, local = dist_setup(args)
@@ -314,9 +356,13 @@ def main():
     peaks, src = measured_peaks()
     fwd_avg, bwd_avg = float(np.mean(fwd_ms)), float(np.mean(bwd_ms))
     total_cells = float(cells.sum())
-    dom = 'backward_kernel' if bwd_avg >= fwd_avg else 'forward_kernel'
-    flop = (4.0 if dom == 'backward_kernel' else 2.0) * N * N * total_cells
-    dur = bwd_avg if dom == 'backward_kernel' else fwd_avg
+    fam = {1: ('forward_kernel', 'backward_kernel'),
+           2: ('warp2::forward_warp_kernel', 'warp2::backward_warp_kernel'),
+           3: ('blk::forward_block_kernel', 'blk::backward_block_kernel')}[plan.last_variant]
+    dom = fam[1] if bwd_avg >= fwd_avg else fam[0]
+    is_bwd = dom == fam[1]
+    flop = (4.0 if is_bwd else 2.0) * N * N * total_cells
+    dur = bwd_avg if is_bwd else fwd_avg
     achieved = flop / (dur / 1e3) / 1e12
     fp32_peak = SMS * FP32_LANES_PER_SM * 2 * peaks.get('sm_max_mhz', 2070.0) * 1e6 / 1e12
     roofline = {'bound': 'fp32', 'kernel': dom, 'achieved': achieved, 'peak': fp32_peak,
@@ -325,9 +371,12 @@ def main():
                 'peak_source': f'{SMS} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 FLOP x sm_max_mhz '
                                f'({peaks.get("sm_max_mhz")} MHz, {src} MEASURED_PEAKS.json); '
                                'the DP is a dense FP32 CUDA-core contraction: no tensor-core or HBM bound',
-                'flop_per_cell': (4 if dom == 'backward_kernel' else 2) * N * N,
+                'flop_per_cell': (4 if is_bwd else 2) * N * N,
                 'fwd_kernel_ms': fwd_avg, 'bwd_kernel_ms': bwd_avg,
                 'hbm_peak_gbs': peaks.get('hbm_gbs')}
+    serving = None
+    if rank == 0 and args.serving_requests > 0:
+        serving = serving_leg(args.serving_requests, args.serving_rate)
     if rank == 0:
         cpu = cpu_baseline(w, args.cpu_seconds) if args.cpu_seconds > 0 else None
         line = {
@@ -344,7 +393,7 @@ def main():
             'e2e': {'value': e2e_value, 'unit': 'cell-state updates/s', 'h2d_bytes_per_step': h2d,
                     'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_total / args.steps,
                     'api': 'pairhmm.api.estep_batch_mixdom2'},
-            'plain': plain, 'gpu_launches': 2 * args.steps, 'clocks': clocks,
+            'plain': plain, 'serving': serving, 'gpu_launches': 2 * args.steps, 'clocks': clocks,
         }
         print(json.dumps(line))
     if ws > 1:

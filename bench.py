@@ -275,6 +275,7 @@ def main():
     for _ in range(max(3, args.warmup)):
         out = _lib.estep(plan, batch, out=out)
     torch.cuda.synchronize()
+    launches_per_step = plan.launches
     status = out['status'].cpu().numpy()
     try:
         gid = str(torch.cuda.get_device_properties(dev).uuid)
@@ -286,7 +287,7 @@ def main():
     if ws > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    step_ms, fwd_ms, bwd_ms = [], [], []
+    step_ms, fwd_ms, bwd_ms, cnt_ms = [], [], [], []
     for k in range(args.steps):
         flush.fill_(k & 0xff)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -297,6 +298,7 @@ def main():
         a, b = plan.kernel_times()
         fwd_ms.append(a)
         bwd_ms.append(b)
+        cnt_ms.append(plan.kernel_time(2))
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
     torch.cuda.synchronize()
@@ -354,15 +356,20 @@ def main():
                  'note': 'same pairs, one phmm_estep call (forward + backward launch) per pair'}
     # ---- roofline of the dominant kernel
     peaks, src = measured_peaks()
-    fwd_avg, bwd_avg = float(np.mean(fwd_ms)), float(np.mean(bwd_ms))
+    fwd_avg, bwd_avg, cnt_avg = float(np.mean(fwd_ms)), float(np.mean(bwd_ms)), float(np.mean(cnt_ms))
     total_cells = float(cells.sum())
-    fam = {1: ('forward_kernel', 'backward_kernel'),
-           2: ('warp2::forward_warp_kernel', 'warp2::backward_warp_kernel'),
-           3: ('blk::forward_block_kernel', 'blk::backward_block_kernel')}[plan.last_variant]
-    dom = fam[1] if bwd_avg >= fwd_avg else fam[0]
-    is_bwd = dom == fam[1]
-    flop = (4.0 if is_bwd else 2.0) * N * N * total_cells
-    dur = bwd_avg if is_bwd else fwd_avg
+    # (kernel name, algorithmic FLOP per cell) of forward, backward, count pass
+    fam = {1: (('forward_kernel', 2), ('backward_kernel', 4), (None, 0)),
+           2: (('warp2::forward_warp_kernel', 2), ('warp2::backward_warp_kernel', 4), (None, 0)),
+           3: (('blk::forward_block_kernel', 2), ('blk::backward_block_kernel', 4), (None, 0)),
+           4: (('warp2::forward_warp_kernel', 2), ('warp2::backward_rec_warp_kernel', 2),
+               ('warp2::count_warp_kernel', 2))}[plan.last_variant]
+    durs = [fwd_avg, bwd_avg, cnt_avg]
+    di = int(np.argmax(durs))
+    dom, fpc = fam[di]
+    is_bwd = di == 1
+    flop = fpc * N * N * total_cells
+    dur = durs[di]
     achieved = flop / (dur / 1e3) / 1e12
     fp32_peak = SMS * FP32_LANES_PER_SM * 2 * peaks.get('sm_max_mhz', 2070.0) * 1e6 / 1e12
     roofline = {'bound': 'fp32', 'kernel': dom, 'achieved': achieved, 'peak': fp32_peak,
@@ -371,8 +378,9 @@ def main():
                 'peak_source': f'{SMS} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 FLOP x sm_max_mhz '
                                f'({peaks.get("sm_max_mhz")} MHz, {src} MEASURED_PEAKS.json); '
                                'the DP is a dense FP32 CUDA-core contraction: no tensor-core or HBM bound',
-                'flop_per_cell': (4 if is_bwd else 2) * N * N,
-                'fwd_kernel_ms': fwd_avg, 'bwd_kernel_ms': bwd_avg,
+                'flop_per_cell': fpc * N * N,
+                'fwd_kernel_ms': fwd_avg, 'bwd_kernel_ms': bwd_avg, 'count_kernel_ms': cnt_avg,
+                'kernels': [f[0] for f in fam if f[0]],
                 'hbm_peak_gbs': peaks.get('hbm_gbs')}
     serving = None
     if rank == 0 and args.serving_requests > 0:
@@ -393,7 +401,7 @@ def main():
             'e2e': {'value': e2e_value, 'unit': 'cell-state updates/s', 'h2d_bytes_per_step': h2d,
                     'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_total / args.steps,
                     'api': 'pairhmm.api.estep_batch_mixdom2'},
-            'plain': plain, 'serving': serving, 'gpu_launches': 2 * args.steps, 'clocks': clocks,
+            'plain': plain, 'serving': serving, 'gpu_launches': launches_per_step * args.steps, 'clocks': clocks,
         }
         print(json.dumps(line))
     if ws > 1:

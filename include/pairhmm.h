@@ -122,7 +122,8 @@ int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch,
  * x_off_host, y_off_host) are read.  The _ws calls then run exactly as
  * phmm_forward / phmm_estep, with all scratch carved from `workspace`
  * (256-byte aligned, at least that many bytes) instead of plan-owned
- * buffers, and allocate nothing.  Calls on one plan with distinct workspaces
+ * buffers, and allocate no device memory (the split E-step creates one side
+ * stream and two events per caller stream, once).  Calls on one plan with distinct workspaces
  * may be in flight on different streams at the same time (issue them from
  * one host thread).  No counterpart in the reference, whose XLA runtime owns
  * the scratch; this is what a serving loop budgets HBM with when it admits
@@ -175,12 +176,18 @@ int phmm_estep_static(const phmm_model_desc *model, const phmm_batch *batch,
  * phmm_forward). */
 int phmm_set_timing(phmm_plan *plan, int enable);
 int phmm_kernel_times(phmm_plan *plan, float *fwd_ms, float *bwd_ms);
+/* Device time of one kernel of the last timed call: which = 0 forward,
+ * 1 backward (fused backward + counts, or the backward recursion of the
+ * split E-step), 2 the split E-step's count pass (0 when it did not run). */
+int phmm_kernel_time(phmm_plan *plan, int which, float *ms);
 
 /* Kernel family: 0 = automatic (default), 1 = generic kernels (any state
  * space of up to 60 emitting states), 2 = register-resident warp kernels,
- * 3 = quad-per-warp block kernels (2 and 3 for state spaces with a compiled
- * shape).  phmm_last_variant reports the family
- * the last call used.  No counterpart in the reference (it has no kernels). */
+ * 3 = quad-per-warp block kernels, 4 = split E-step on the warp kernels
+ * (forward and backward recursion at the same time on two streams, then a
+ * count pass over both lattices), 5 = split E-step on the block kernels
+ * (2 to 5 for state spaces with a compiled shape).  phmm_last_variant reports the family the last call used.  No
+ * counterpart in the reference (it has no kernels). */
 int phmm_set_variant(phmm_plan *plan, int variant);
 int phmm_last_variant(const phmm_plan *plan);
 

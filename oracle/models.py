@@ -94,6 +94,25 @@ def tkf91_trans(lam, mu, t):
     return tau
 
 
+def tkf91_trans_cond(lam, mu, t):
+    """TKF91 matrix conditioned on the ancestor length (core/params.py:57-90):
+    kappa removed from the M/D entries and (1 - kappa) from the E entries."""
+    a = tkf_alpha(mu, t)
+    b = tkf_beta(lam, mu, t)
+    g = tkf_gamma(lam, mu, t)
+    tau = np.zeros((5, 5))
+    for src in (S, M, I):
+        tau[src, M] = (1 - b) * a
+        tau[src, I] = b
+        tau[src, D] = (1 - b) * (1 - a)
+        tau[src, E] = 1 - b
+    tau[D, M] = (1 - g) * a
+    tau[D, I] = g
+    tau[D, D] = (1 - g) * (1 - a)
+    tau[D, E] = 1 - g
+    return tau
+
+
 def tkf92_trans(lam, mu, t, ext):
     """5x5 TKF92 matrix: fragment self-loops on M,I,D (core/params.py:92-124)."""
     t91 = tkf91_trans(lam, mu, t)

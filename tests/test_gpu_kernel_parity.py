@@ -63,7 +63,8 @@ def related_pair(rng, Lx, Ly):
 
 def run_kernel(chi, st, groups, EM, EI, ED, xs, ys, per_pair=None, variant=0):
     """per_pair: optional list of (chi, EM, EI, ED) per pair; variant 1 =
-    generic kernels, 2 = register-resident warp kernels, 0 = automatic."""
+    generic kernels, 2 = register-resident warp kernels, 3 = block kernels,
+    4 = split warp E-step, 5 = split block E-step, 0 = automatic."""
     from pairhmm import _lib
     G = EM.shape[0]
     plan = _lib.Plan(st, groups, G)
@@ -105,7 +106,7 @@ LENGTHS = [(0, 0), (0, 5), (6, 0), (1, 1), (7, 9), (31, 33), (32, 32), (33, 31),
            (63, 10), (64, 64), (65, 40), (40, 97), (130, 120), (129, 3)]
 
 
-@pytest.mark.parametrize('variant', [1, 2, 3])
+@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5])
 @pytest.mark.parametrize('model,K,F,C', [('tkf91', 1, 1, 1), ('mixdom2', 3, 1, 1),
                                          ('mixdom2', 2, 2, 2), ('mixdom2', 4, 2, 2),
                                          ('mixdom2', 1, 1, 2), ('mixdom2', 2, 1, 1)])
@@ -141,7 +142,7 @@ def test_forward_only_matches_estep_ll(cuda_lib):
     np.testing.assert_array_equal(ll_f.cpu().numpy(), out['ll'].cpu().numpy())
 
 
-@pytest.mark.parametrize('variant', [1, 2, 3])
+@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5])
 def test_per_pair_chi_and_wildcards(cuda_lib, variant):
     rng = np.random.default_rng(11)
     base = mixdom2_params(rng, 2, 1, 1)
@@ -166,7 +167,7 @@ def test_per_pair_chi_and_wildcards(cuda_lib, variant):
         assert_counts(out['cnt_M'][b], cM)
 
 
-@pytest.mark.parametrize('variant', [1, 2, 3])
+@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5])
 def test_long_pair_pipelined_stripes(cuda_lib, variant):
     """A pair spanning many stripes (pipelined through the edge rows), against the oracle."""
     rng = np.random.default_rng(5)

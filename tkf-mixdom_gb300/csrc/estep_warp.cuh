@@ -49,7 +49,8 @@ struct SmemW {
     int bytes;
 };
 
-__host__ __device__ inline SmemW make_smem_w(int SP, int KP, int NI, int G, int max_ly, bool bwd) {
+// bwd: transposed chi; counts: the count-phase staging of the fused backward
+__host__ __device__ inline SmemW make_smem_w(int SP, int KP, int NI, int G, int max_ly, bool bwd, bool counts) {
     SmemW L;
     int o = 0;
     const int SPP = SP + 4, KPP = KP + 4;
@@ -59,7 +60,7 @@ __host__ __device__ inline SmemW make_smem_w(int SP, int KP, int NI, int G, int 
     L.tI = o; o += al4(G * 21);
     L.tD = o; o += al4(G * 21);
     L.halo = o; o += HCW * al4(KP > SP ? KP : SP);
-    if (bwd) {
+    if (counts) {
         L.fst = o; o += 2 * ROWS * SPP;
         L.ust = o; o += ROWS * KPP;
         L.bins = o; o += al4(G * 21);
@@ -68,12 +69,16 @@ __host__ __device__ inline SmemW make_smem_w(int SP, int KP, int NI, int G, int 
         L.fst = L.ust = L.bins = L.colI = -1;
     }
     L.haloE = o; o += HCW;
-    if (bwd) { L.fstE = o; o += 2 * ROWS; } else { L.fstE = -1; }
+    if (counts) { L.fstE = o; o += 2 * ROWS; } else { L.fstE = -1; }
     int bytes = o * 4;
     L.ys = bytes;
     bytes += max_ly + 1;
     L.bytes = (bytes + 15) & ~15;
     return L;
+}
+
+__host__ __device__ inline SmemW make_smem_w(int SP, int KP, int NI, int G, int max_ly, bool bwd) {
+    return make_smem_w(SP, KP, NI, G, max_ly, bwd, bwd);
 }
 
 // Per-stripe model load into shared memory (one warp).  Forward layout:
@@ -109,7 +114,7 @@ __device__ void load_model_w(const KParams &P, int p, const PairMeta &m, const S
         }
         ys[j] = (unsigned char)c;
     }
-    if (bwd) {
+    if (L.bins >= 0) {
         for (int idx = lane; idx < G * 21; idx += 32) sm[L.bins + idx] = 0.f;
         for (int idx = lane; idx < ROWS * (SH::NI > 0 ? SH::NI : 1); idx += 32) sm[L.colI + idx] = 0.f;
     }

@@ -83,6 +83,8 @@ struct KParams {
     int64_t eM_stride, eID_stride;
     float *lat;
     int *lat_exp;
+    float *blat;                        // split E-step: backward lattice
+    int *blat_exp;
     float *edge;
     int *edge_exp;
     int *progress;
@@ -822,7 +824,9 @@ __global__ void fill_f64(double *p, int64_t n, double v) {
 }  // namespace
 
 #include "estep_warp.cuh"
+#include "estep_split.cuh"
 #include "estep_block.cuh"
+#include "estep_block_split.cuh"
 
 namespace {
 
@@ -856,15 +860,23 @@ struct phmm_plan {
     float *edge = nullptr; size_t edge_cap = 0;
     int *edge_exp = nullptr; size_t edgeE_cap = 0;
     int *progress = nullptr; size_t prog_cap = 0;
+    float *blat = nullptr; size_t blat_cap = 0;      // split E-step
+    int *blat_exp = nullptr; size_t blatE_cap = 0;
+    float *bedge = nullptr; size_t bedge_cap = 0;
+    int *bedge_exp = nullptr; size_t bedgeE_cap = 0;
+    // split E-step: one side stream (+ fork / join events) per caller stream
+    struct Side { cudaStream_t user, side; cudaEvent_t fork, join; };
+    std::vector<Side> sides;
     std::vector<PairMeta> h_meta;
     std::vector<int2> h_items;
     // optional per-kernel CUDA-event timing on the launching stream
     bool timing = false;
     bool timed_bwd = false;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool timed_count = false;
     // register-resident warp kernels for this state space (null: generic kernels)
     int w_nm = 0, w_ni = 0, w_nd = 0;
-    int variant = 0;        // 0 automatic, 1 generic, 2 warp kernels, 3 block kernels
+    int variant = 0;        // 0 automatic, 1 generic, 2 warp, 3 block, 4 split warp E-step, 5 split block E-step
     int last_variant = 0;
 };
 
@@ -882,14 +894,15 @@ int ensure(T **ptr, size_t *cap, size_t n) {
 }
 
 // ---- launchers of the register-resident warp kernels, one per state-space shape
-using WarpLauncher = int (*)(phmm_plan *, KParams &, int, int, bool, cudaStream_t);
+// kind: 0 forward, 1 fused backward + counts, 2 backward recursion (split), 3 counts (split)
+using WarpLauncher = int (*)(phmm_plan *, KParams &, int, int, int, cudaStream_t);
 
 template <class SH>
-int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, bool bwd, cudaStream_t stream);
+int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, cudaStream_t stream);
 
 template <int NM, int NI, int ND>
-int launch_warp_shape(phmm_plan *plan, KParams &K, int n_items, int max_ly, bool bwd, cudaStream_t stream) {
-    return launch_warp<warp2::Shape<NM, NI, ND>>(plan, K, n_items, max_ly, bwd, stream);
+int launch_warp_shape(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, cudaStream_t stream) {
+    return launch_warp<warp2::Shape<NM, NI, ND>>(plan, K, n_items, max_ly, kind, stream);
 }
 
 struct WarpShapeEntry { int nm, ni, nd; WarpLauncher fn; };
@@ -904,10 +917,11 @@ const WarpShapeEntry kWarpShapes[] = {
 };
 
 // ---- launchers of the quad-per-warp block kernels, one per padded state count
-using BlockLauncher = int (*)(phmm_plan *, KParams &, int, int, bool, cudaStream_t);
+// kind: as for the warp kernels
+using BlockLauncher = int (*)(phmm_plan *, KParams &, int, int, int, cudaStream_t);
 
 template <class SH>
-int launch_block(phmm_plan *plan, KParams &K, int n_items, int max_ly, bool bwd, cudaStream_t stream);
+int launch_block(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, cudaStream_t stream);
 
 struct BlockShapeEntry { int ns; BlockLauncher fn; };
 const BlockShapeEntry kBlockShapes[] = {
@@ -930,6 +944,65 @@ WarpLauncher find_warp_launcher(int nm, int ni, int nd) {
 }
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// The split E-step: forward on the caller's stream and backward recursion on
+// a side stream at the same time, then the count pass once both are done.
+int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, int n_items, int n_citems, int stripes, int max_ly,
+                 void *d_items, int *d_counters, int *d_progress, float *d_bedge, int *d_bedge_exp,
+                 cudaStream_t stream) {
+    phmm_plan::Side *sd = nullptr;
+    for (auto &e : plan->sides)
+        if (e.user == stream) { sd = &e; break; }
+    if (!sd) {
+        phmm_plan::Side e{stream, nullptr, nullptr, nullptr};
+        CUDA_TRY(cudaStreamCreateWithFlags(&e.side, cudaStreamNonBlocking));
+        CUDA_TRY(cudaEventCreateWithFlags(&e.fork, cudaEventDisableTiming));
+        CUDA_TRY(cudaEventCreateWithFlags(&e.join, cudaEventDisableTiming));
+        plan->sides.push_back(e);
+        sd = &plan->sides.back();
+    }
+    int rc;
+    CUDA_TRY(cudaEventRecord(sd->fork, stream));
+    CUDA_TRY(cudaStreamWaitEvent(sd->side, sd->fork, 0));
+    // forward (caller's stream)
+    KParams F = K;
+    F.items = (const int2 *)d_items;
+    F.n_items = n_items;
+    F.counter = d_counters;
+    F.progress = d_progress;
+    F.blat = nullptr;
+    F.blat_exp = nullptr;
+    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
+    if ((rc = wl(plan, F, n_items, max_ly, 0, stream))) return rc;
+    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[1], stream));
+    // backward recursion (side stream): own edge rows and progress counters
+    KParams B = K;
+    B.items = (const int2 *)d_items + n_items;
+    B.n_items = n_items;
+    B.counter = d_counters + 1;
+    B.progress = d_progress + stripes;
+    B.edge = d_bedge;
+    B.edge_exp = d_bedge_exp;
+    B.lat = nullptr;
+    B.lat_exp = nullptr;
+    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[2], sd->side));
+    if ((rc = wl(plan, B, n_items, max_ly, 2, sd->side))) return rc;
+    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[3], sd->side));
+    CUDA_TRY(cudaEventRecord(sd->join, sd->side));
+    CUDA_TRY(cudaStreamWaitEvent(stream, sd->join, 0));
+    // counts from both lattices (caller's stream)
+    KParams C = K;
+    C.items = (const int2 *)d_items + 2 * n_items;
+    C.n_items = n_citems;
+    C.counter = d_counters + 2;
+    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[4], stream));
+    if ((rc = wl(plan, C, n_citems, max_ly, 3, stream))) return rc;
+    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[5], stream));
+    plan->launches += 3;
+    plan->timed_bwd = true;
+    plan->timed_count = true;
+    return 0;
+}
 
 // One call of the forward (estep false) or E-step kernels.  Scratch comes from
 // the plan (grown on demand) unless the caller passes a workspace `ws` of
@@ -959,26 +1032,30 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     // no lattice tables are requested; the generic quad kernels otherwise
     WarpLauncher wl = nullptr;
     BlockLauncher bl = nullptr;
+    bool split = false;   // E-step as forward || backward recursion, then counts
     const bool tables = F_log || B_log || post;
     // automatic choice (measured on GB300, 17 states): the block kernels have
-    // the shorter forward step, the warp kernels the faster fused backward
+    // the shorter forward step; for the E-step the split warp kernels
     if (!tables && plan->variant == 0) {
         if (estep) {
             wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
             if (!wl) bl = find_block_launcher(K.NS);
+            split = wl != nullptr || bl != nullptr;
         } else {
             bl = find_block_launcher(K.NS);
             if (!bl) wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
         }
     }
-    if (!tables && plan->variant == 3) bl = find_block_launcher(K.NS);
-    if (!tables && plan->variant == 2) wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
-    if (plan->variant == 2 && !wl) return fail(PHMM_E_ARG, "no warp kernel for this state space");
-    if (plan->variant == 3 && !bl) return fail(PHMM_E_ARG, "no block kernel for this state space");
+    if (!tables && (plan->variant == 3 || plan->variant == 5)) bl = find_block_launcher(K.NS);
+    if (!tables && plan->variant == 5) split = estep && bl != nullptr;
+    if (!tables && (plan->variant == 2 || plan->variant == 4)) wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
+    if (!tables && plan->variant == 4) split = estep && wl != nullptr;
+    if ((plan->variant == 2 || plan->variant == 4) && !wl) return fail(PHMM_E_ARG, "no warp kernel for this state space");
+    if ((plan->variant == 3 || plan->variant == 5) && !bl) return fail(PHMM_E_ARG, "no block kernel for this state space");
     const int rows = bl ? blk::ROWS : (wl ? warp2::ROWS : TH);
     const int stride = bl ? K.NS : (wl ? ((plan->w_nm + plan->w_ni + plan->w_nd + 1 + 3) & ~3) : K.NS);
     const int estride = bl ? blk::nbp_of(K.NS / 4) : 1;   // exponents per cell
-    if (!ws_need) plan->last_variant = bl ? 3 : (wl ? 2 : 1);
+    if (!ws_need) plan->last_variant = bl ? (split ? 5 : 3) : (split ? 4 : (wl ? 2 : 1));
     // ---- plan: stripes, offsets, longest-first order
     std::vector<int> order(P_);
     for (int p = 0; p < P_; ++p) {
@@ -1016,6 +1093,19 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     if (estep)
         for (int p : order)
             for (int s = plan->h_meta[p].n_stripes - 1; s >= 0; --s) plan->h_items.push_back(make_int2(p, s));
+    int n_citems = 0;
+    if (split) {   // count chunks: (pair, stripe << 12 | chunk)
+        for (int p : order) {
+            const PairMeta &m = plan->h_meta[p];
+            for (int s = 0; s < m.n_stripes; ++s) {
+                const int nrows = std::min(rows, m.Lx + 1 - s * rows);
+                const int nch = (nrows + m.Ly + warp2::CCH - 1) / warp2::CCH;
+                if (nch > 4096 || s >= (1 << 19)) return fail(PHMM_E_ARG, "pair too long for the count chunk index");
+                for (int c = 0; c < nch; ++c) plan->h_items.push_back(make_int2(p, (s << 12) | c));
+                n_citems += nch;
+            }
+        }
+    }
     int rc;
     // ---- scratch: plan-owned buffers, or carved from the caller's workspace
     const size_t o_meta = 0;
@@ -1026,11 +1116,15 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     const size_t o_edgeE = align256(o_edge + sizeof(float) * (size_t)edge_cells * stride);
     const size_t o_lat = align256(o_edgeE + sizeof(int) * (size_t)edge_cells * estride);
     const size_t o_latE = align256(o_lat + (estep ? sizeof(float) * (size_t)lat_cells * stride : 0));
-    const size_t need = align256(o_latE + (estep ? sizeof(int) * (size_t)lat_cells * estride : 0));
+    const size_t o_blat = align256(o_latE + (estep ? sizeof(int) * (size_t)lat_cells * estride : 0));
+    const size_t o_blatE = align256(o_blat + (split ? sizeof(float) * (size_t)lat_cells * stride : 0));
+    const size_t o_bedge = align256(o_blatE + (split ? sizeof(int) * (size_t)lat_cells * estride : 0));
+    const size_t o_bedgeE = align256(o_bedge + (split ? sizeof(float) * (size_t)edge_cells * stride : 0));
+    const size_t need = align256(o_bedgeE + (split ? sizeof(int) * (size_t)edge_cells * estride : 0));
     if (ws_need) { *ws_need = need; return 0; }
     void *d_meta, *d_items;
-    int *d_counters, *d_progress, *d_edge_exp, *d_lat_exp;
-    float *d_edge, *d_lat;
+    int *d_counters, *d_progress, *d_edge_exp, *d_lat_exp, *d_blat_exp = nullptr, *d_bedge_exp = nullptr;
+    float *d_edge, *d_lat, *d_blat = nullptr, *d_bedge = nullptr;
     if (ws) {
         if (ws_bytes < need) {
             char msg[200];
@@ -1047,6 +1141,12 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
         d_edge_exp = (int *)(w + o_edgeE);
         d_lat = estep ? (float *)(w + o_lat) : nullptr;
         d_lat_exp = estep ? (int *)(w + o_latE) : nullptr;
+        if (split) {
+            d_blat = (float *)(w + o_blat);
+            d_blat_exp = (int *)(w + o_blatE);
+            d_bedge = (float *)(w + o_bedge);
+            d_bedge_exp = (int *)(w + o_bedgeE);
+        }
     } else {
         if ((rc = ensure((char **)&plan->meta, &plan->meta_cap, sizeof(PairMeta) * P_))) return rc;
         if ((rc = ensure((char **)&plan->items, &plan->items_cap, sizeof(int2) * plan->h_items.size()))) return rc;
@@ -1065,11 +1165,21 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
         d_edge_exp = plan->edge_exp;
         d_lat = plan->lat;
         d_lat_exp = plan->lat_exp;
+        if (split) {
+            if ((rc = ensure(&plan->blat, &plan->blat_cap, (size_t)lat_cells * stride))) return rc;
+            if ((rc = ensure(&plan->blat_exp, &plan->blatE_cap, (size_t)lat_cells * estride))) return rc;
+            if ((rc = ensure(&plan->bedge, &plan->bedge_cap, (size_t)edge_cells * stride))) return rc;
+            if ((rc = ensure(&plan->bedge_exp, &plan->bedgeE_cap, (size_t)edge_cells * estride))) return rc;
+            d_blat = plan->blat;
+            d_blat_exp = plan->blat_exp;
+            d_bedge = plan->bedge;
+            d_bedge_exp = plan->bedge_exp;
+        }
     }
     CUDA_TRY(cudaMemcpyAsync(d_meta, plan->h_meta.data(), sizeof(PairMeta) * P_, cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(d_items, plan->h_items.data(), sizeof(int2) * plan->h_items.size(),
                              cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemsetAsync(d_counters, 0, 2 * sizeof(int), stream));
+    CUDA_TRY(cudaMemsetAsync(d_counters, 0, 3 * sizeof(int), stream));
     CUDA_TRY(cudaMemsetAsync(d_progress, 0, sizeof(int) * 2 * stripes, stream));
     CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int32_t) * P_, stream));
     if (estep) {
@@ -1094,6 +1204,8 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     K.eID_stride = b->emit_per_pair ? (int64_t)G * 21 : 0;
     K.lat = estep ? d_lat : nullptr;
     K.lat_exp = estep ? d_lat_exp : nullptr;
+    K.blat = d_blat;
+    K.blat_exp = d_blat_exp;
     K.edge = d_edge;
     K.edge_exp = d_edge_exp;
     K.ll = ll;
@@ -1107,6 +1219,8 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     K.post = post;
     K.max_ly = max_ly;
     K.spin_limit = 40LL * 1000 * 1000;
+    if (split) return launch_split(plan, K, wl ? wl : bl, n_items, n_citems, stripes, max_ly, d_items, d_counters,
+                                   d_progress, d_bedge, d_bedge_exp, stream);
     for (int pass = 0; pass < (estep ? 2 : 1); ++pass) {
         const bool bwd = pass == 1;
         K.items = (const int2 *)d_items + (bwd ? n_items : 0);
@@ -1133,34 +1247,52 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
         plan->launches++;
     }
     plan->timed_bwd = estep;
+    plan->timed_count = false;
     return 0;
 }
 
 template <class SH>
-int launch_block(phmm_plan *plan, KParams &K, int n_items, int max_ly, bool bwd, cudaStream_t stream) {
-    const blk::SmemB L = blk::make_smem_b(SH::NS, SH::NB, 1, K.G, max_ly, bwd);
-    auto kern = bwd ? blk::backward_block_kernel<SH> : blk::forward_block_kernel<SH>;
-    const int threads = 32 * (SH::NB + (bwd ? blk::NCW : 0));
-    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
+int launch_block(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, cudaStream_t stream) {
+    void (*kern)(const KParams) = nullptr;
+    int bytes = 0, threads = 0;
+    if (kind == 3) {
+        bytes = blk::make_smem_cb(SH::NS, K.G, max_ly).bytes;
+        kern = blk::count_block_kernel<SH>;
+        threads = blk::CNT_THREADS;
+    } else {
+        bytes = blk::make_smem_b(SH::NS, SH::NB, 1, K.G, max_ly, kind == 1).bytes;
+        kern = kind == 0 ? blk::forward_block_kernel<SH>
+                         : (kind == 1 ? blk::backward_block_kernel<SH> : blk::backward_rec_block_kernel<SH>);
+        threads = 32 * (SH::NB + (kind == 1 ? blk::NCW : 0));
+    }
+    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     int occ = 0;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, L.bytes));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, bytes));
     if (occ < 1) return fail(PHMM_E_ARG, "block kernel does not fit on an SM (shared memory)");
     const int grid = std::min(n_items, plan->sm_count * occ);
-    kern<<<grid, threads, L.bytes, stream>>>(K);
+    kern<<<grid, threads, bytes, stream>>>(K);
     CUDA_TRY(cudaGetLastError());
     return 0;
 }
 
 template <class SH>
-int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, bool bwd, cudaStream_t stream) {
-    const warp2::SmemW L = warp2::make_smem_w(SH::SP, SH::KP, SH::NI, K.G, max_ly, bwd);
-    auto kern = bwd ? warp2::backward_warp_kernel<SH> : warp2::forward_warp_kernel<SH>;
-    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes));
+int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, cudaStream_t stream) {
+    void (*kern)(const KParams) = nullptr;
+    int bytes = 0;
+    if (kind == 3) {
+        bytes = warp2::make_smem_c(SH::SP, SH::KP, SH::NI, K.G, max_ly).bytes;
+        kern = warp2::count_warp_kernel<SH>;
+    } else {
+        bytes = warp2::make_smem_w(SH::SP, SH::KP, SH::NI, K.G, max_ly, kind != 0, kind == 1).bytes;
+        kern = kind == 0 ? warp2::forward_warp_kernel<SH>
+                         : (kind == 1 ? warp2::backward_warp_kernel<SH> : warp2::backward_rec_warp_kernel<SH>);
+    }
+    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     int occ = 0;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32, L.bytes));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32, bytes));
     if (occ < 1) return fail(PHMM_E_ARG, "warp kernel does not fit on an SM (shared memory)");
     const int grid = std::min(n_items, plan->sm_count * occ);
-    kern<<<grid, 32, L.bytes, stream>>>(K);
+    kern<<<grid, 32, bytes, stream>>>(K);
     CUDA_TRY(cudaGetLastError());
     return 0;
 }
@@ -1270,9 +1402,18 @@ int phmm_plan_create(const phmm_model_desc *md, phmm_plan **out) {
 int phmm_set_timing(phmm_plan *plan, int enable) {
     if (!plan) return fail(PHMM_E_ARG, "null plan");
     if (enable && !plan->ev[0]) {
-        for (int k = 0; k < 4; ++k) CUDA_TRY(cudaEventCreate(&plan->ev[k]));
+        for (int k = 0; k < 6; ++k) CUDA_TRY(cudaEventCreate(&plan->ev[k]));
     }
     plan->timing = enable != 0;
+    return 0;
+}
+
+int phmm_kernel_time(phmm_plan *plan, int which, float *ms) {
+    if (!plan || !plan->timing) return fail(PHMM_E_ARG, "timing is not enabled on this plan");
+    if (!ms || which < 0 || which > 2) return fail(PHMM_E_ARG, "bad kernel index");
+    if ((which == 1 && !plan->timed_bwd) || (which == 2 && !plan->timed_count)) { *ms = 0.f; return 0; }
+    CUDA_TRY(cudaEventSynchronize(plan->ev[2 * which + 1]));
+    CUDA_TRY(cudaEventElapsedTime(ms, plan->ev[2 * which], plan->ev[2 * which + 1]));
     return 0;
 }
 
@@ -1293,8 +1434,17 @@ int phmm_kernel_times(phmm_plan *plan, float *fwd_ms, float *bwd_ms) {
 void phmm_plan_destroy(phmm_plan *plan) {
     if (!plan) return;
     cudaDeviceSynchronize();
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < 6; ++k)
         if (plan->ev[k]) cudaEventDestroy(plan->ev[k]);
+    for (auto &e : plan->sides) {
+        cudaEventDestroy(e.fork);
+        cudaEventDestroy(e.join);
+        cudaStreamDestroy(e.side);
+    }
+    cudaFree(plan->blat);
+    cudaFree(plan->blat_exp);
+    cudaFree(plan->bedge);
+    cudaFree(plan->bedge_exp);
     cudaFree(plan->meta);
     cudaFree(plan->items);
     cudaFree(plan->counters);
@@ -1349,10 +1499,10 @@ int phmm_estep_ws(phmm_plan *plan, const phmm_batch *batch, void *workspace, siz
 int phmm_last_launch_count(const phmm_plan *plan) { return plan ? plan->launches : 0; }
 
 int phmm_set_variant(phmm_plan *plan, int variant) {
-    if (!plan || variant < 0 || variant > 3) return fail(PHMM_E_ARG, "bad variant");
-    if (variant == 2 && !find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd))
+    if (!plan || variant < 0 || variant > 5) return fail(PHMM_E_ARG, "bad variant");
+    if ((variant == 2 || variant == 4) && !find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd))
         return fail(PHMM_E_ARG, "no warp kernel for this state space");
-    if (variant == 3 && !find_block_launcher(plan->base.NS))
+    if ((variant == 3 || variant == 5) && !find_block_launcher(plan->base.NS))
         return fail(PHMM_E_ARG, "no block kernel for this state space");
     plan->variant = variant;
     return 0;

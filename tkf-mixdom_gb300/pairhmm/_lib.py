@@ -19,7 +19,8 @@ _LIB = None
 
 EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep',
            'phmm_estep_tables', 'phmm_workspace_bytes', 'phmm_forward_ws', 'phmm_estep_ws',
-           'phmm_estep_static', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_set_variant',
+           'phmm_estep_static', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_kernel_time',
+           'phmm_set_variant',
            'phmm_last_variant', 'phmm_last_launch_count',
            'phmm_last_error', 'phmm_version')
 
@@ -83,6 +84,8 @@ def load(path=None):
     lib.phmm_set_timing.restype = ctypes.c_int
     lib.phmm_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
     lib.phmm_kernel_times.restype = ctypes.c_int
+    lib.phmm_kernel_time.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+    lib.phmm_kernel_time.restype = ctypes.c_int
     lib.phmm_set_variant.argtypes = [vp, ctypes.c_int]
     lib.phmm_set_variant.restype = ctypes.c_int
     lib.phmm_last_variant.argtypes = [vp]
@@ -143,7 +146,9 @@ class Plan:
         return self.lib.phmm_last_launch_count(self.handle)
 
     def set_variant(self, variant):
-        """0 automatic, 1 generic, 2 register-resident warp, 3 quad-per-warp block kernels."""
+        """0 automatic, 1 generic, 2 register-resident warp, 3 quad-per-warp block
+        kernels, 4 split warp E-step (forward || backward recursion, then counts),
+        5 split block E-step."""
         _check(self.lib.phmm_set_variant(self.handle, int(variant)), 'phmm_set_variant')
 
     @property
@@ -152,6 +157,13 @@ class Plan:
 
     def set_timing(self, enable=True):
         _check(self.lib.phmm_set_timing(self.handle, int(enable)), 'phmm_set_timing')
+
+    def kernel_time(self, which):
+        """Device ms of kernel `which` (0 forward, 1 backward, 2 split count pass)
+        of the last timed call."""
+        a = ctypes.c_float()
+        _check(self.lib.phmm_kernel_time(self.handle, int(which), ctypes.byref(a)), 'phmm_kernel_time')
+        return float(a.value)
 
     def kernel_times(self):
         """(forward_ms, backward_ms) of the last call (CUDA events on its stream)."""

@@ -434,12 +434,37 @@ def mixdom2_log_prob(main_ins_rate, main_del_rate, t, dom_ins_rates, dom_del_rat
     return ll if batched else ll[0]
 
 
+def mixdom_log_prob(main_ins_rate, main_del_rate, t, dom_ins_rates, dom_del_rates, dom_weights,
+                    frag_weights, ext_rates, Q, pi, x_seq, y_seq):
+    """log P(x, y) under the nested MixDom pair HMM with one substitution
+    model (train/vjp.py:351-458): chi from build_nested_trans, every M/I/D
+    state emitting through pair_hmm_emissions(P(t), pi).  Gradients for every
+    tensor argument through the score identity, as mixdom2_log_prob."""
+    dev = _device()
+    batched = isinstance(x_seq, (list, tuple))
+    xs = list(x_seq) if batched else [np.asarray(x_seq)]
+    ys = list(y_seq) if batched else [np.asarray(y_seq)]
+    tt = pm._t(t, device=dev).reshape(-1)
+    f = lambda v: pm._t(v, device=dev)
+    K, F = f(frag_weights).shape
+    chi = pm.build_nested_trans(f(main_ins_rate), f(main_del_rate), tt, f(dom_ins_rates),
+                                f(dom_del_rates), f(dom_weights), f(frag_weights), f(ext_rates))
+    sub = pm.transition_matrix(f(Q), tt)
+    EM, EI, ED = pm.tables_tkf(sub, f(pi))
+    st = pm.mixdom_state_types(K, F)
+    plan = get_plan(st, np.zeros(len(st), np.int32), 1)
+    ll = PairHMMLogLik.apply(chi, EM, EI, ED, plan, xs, ys)
+    return ll if batched else ll[0]
+
+
 def _tkf_log_prob(model, ins_rate, del_rate, t, ext, Q, pi, x_seq, y_seq):
     dev = _device()
     f = lambda v: pm._t(v, device=dev)
     tt = f(t).reshape(-1)
     if model == 'tkf91':
         chi = pm.tkf91_trans(f(ins_rate), f(del_rate), tt)
+    elif model == 'tkf91_cond':
+        chi = pm.tkf91_trans_cond(f(ins_rate), f(del_rate), tt)
     else:
         chi = pm.tkf92_trans(f(ins_rate), f(del_rate), tt, f(ext))
     sub = pm.transition_matrix(f(Q), tt)
@@ -451,6 +476,12 @@ def _tkf_log_prob(model, ins_rate, del_rate, t, ext, Q, pi, x_seq, y_seq):
 def tkf91_log_prob(ins_rate, del_rate, t, Q, pi, x_seq, y_seq):
     """log P(x,y) under TKF91, differentiable in all float arguments (train/vjp.py:109-194)."""
     return _tkf_log_prob('tkf91', ins_rate, del_rate, t, None, Q, pi, x_seq, y_seq)
+
+
+def tkf91_log_prob_cond(ins_rate, del_rate, t, Q, pi, x_seq, y_seq):
+    """log P(x,y | ancestor length) + const under TKF91 (train/vjp.py:198-249),
+    differentiable in all float arguments."""
+    return _tkf_log_prob('tkf91_cond', ins_rate, del_rate, t, None, Q, pi, x_seq, y_seq)
 
 
 def tkf92_log_prob(ins_rate, del_rate, t, ext, Q, pi, x_seq, y_seq):

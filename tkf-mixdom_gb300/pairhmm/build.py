@@ -39,7 +39,8 @@ def _stale(out, deps):
 
 
 def build(force=False, verbose=False, extra=()):
-    deps = SOURCES + [os.path.join(INCLUDE, 'pairhmm.h')]
+    deps = SOURCES + [os.path.join(INCLUDE, 'pairhmm.h')] + [
+        os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(('.cuh', '.h'))]
     if not force and not _stale(LIB_PATH, deps):
         return LIB_PATH
     tmp = LIB_PATH + '.tmp'

@@ -72,6 +72,18 @@ def tkf91_trans(lam, mu, t):
     return torch.stack([row, row, row, rowD, zero], dim=-2)
 
 
+def tkf91_trans_cond(lam, mu, t):
+    """[..., 5, 5] TKF91 matrices conditioned on the ancestor length
+    (core/params.py:57-90): no kappa on M/D entries, no (1-kappa) on E."""
+    lam, mu, t = torch.broadcast_tensors(_t(lam), _t(mu), _t(t))
+    a, b, g = tkf_alpha(mu, t), tkf_beta(lam, mu, t), tkf_gamma(lam, mu, t)
+    z = torch.zeros_like(a)
+    row = torch.stack([z, (1 - b) * a, b, (1 - b) * (1 - a), 1 - b], dim=-1)
+    rowD = torch.stack([z, (1 - g) * a, g, (1 - g) * (1 - a), 1 - g], dim=-1)
+    zero = torch.zeros_like(row)
+    return torch.stack([row, row, row, rowD, zero], dim=-2)
+
+
 def tkf92_trans(lam, mu, t, ext):
     """TKF92: M/I/D rows scaled by (1-ext) with ext added on the diagonal."""
     t91 = tkf91_trans(lam, mu, t)

@@ -33,6 +33,19 @@ for _p in (ROOT, PKG_DIR):
         sys.path.insert(0, _p)
 
 WORKLOAD = 'mixdom2_k3f1c1_200pairs_len30-600'
+# per workload: what one step runs and what the metric counts
+WORKLOADS = {
+    'mixdom2_k3f1c1_200pairs_len30-600': {
+        'forward_only': False, 'metric': 'pair-HMM E-step cell-state updates/s',
+        'model': 'MixDom2 n_dom=3 n_frag=1 n_classes=1', 'e2e_api': 'pairhmm.api.estep_batch_mixdom2'},
+    'mixdom2_k4f2c2_32pairs_len200-1500': {
+        'forward_only': False, 'metric': 'pair-HMM E-step cell-state updates/s',
+        'model': 'MixDom2 n_dom=4 n_frag=2 n_classes=2',
+        'e2e_api': 'pairhmm.api.mixdom2_log_prob(...).sum().backward() (gradient of the summed LL)'},
+    'tkf91_64pairs_len50-150': {
+        'forward_only': True, 'metric': 'pair-HMM forward cell-state updates/s',
+        'model': 'TKF91', 'e2e_api': 'pairhmm.api.estep_batch_tkf92_forward_only (ext = 0)'},
+}
 PROFILE_SUMMARY = os.path.join(ROOT, 'profiles', 'estep_kernels_mixdom2_k3f1c1.md')
 SMS = 152
 FP32_LANES_PER_SM = 128
@@ -125,42 +138,66 @@ class ClockSampler:
                 'reasons': sorted(reasons), 'samples': len(sm)}
 
 
-def cpu_baseline(workload, seconds, threads=1):
-    """The FP64 oracle on a bounded sample of the same pairs (host cores)."""
-    from oracle import models as om, dp as odp, estep as oe
-    p = workload.params
+def _oracle_model(workload, b):
+    """(chi, state types, groups, EM, EI, ED) of pair b under the oracle."""
+    from oracle import estep as oe
+    p = dict(workload.params)
+    p['t'] = float(workload.ts[b])
+    if workload.model == 'mixdom2':
+        return oe.mixdom2_model(p)[:6]
+    return oe.tkf_model(workload.model, p)[:6]
+
+
+def _oracle_pair(workload, b, forward_only):
+    """Oracle log-likelihood and expected transition counts (None when forward only)."""
+    from oracle import models as om, dp as odp
+    chi, st, groups, EM, EI, ED = _oracle_model(workload, b)
+    emit = odp.log_emission_table(st, groups, workload.xs[b], workload.ys[b], EM, EI, ED)
+    if forward_only:
+        return odp.forward_table(om.safe_log(chi), st, emit)[0], None
+    ll, _, n, _, _ = odp.forward_backward(om.safe_log(chi), st, emit)
+    return ll, n
+
+
+def cpu_baseline(workload, seconds, forward_only, gpu_ll=None, gpu_n=None, threads=1):
+    """The FP64 oracle on a bounded sample of the same pairs (host cores),
+    smallest pairs first; with the GPU's outputs it also reports their
+    error against the oracle on the sampled pairs."""
     done_cells = 0
     t0 = time.perf_counter()
     order = np.argsort(workload.cells())
     n = 0
+    ll_err, n_err = [], []
     for b in order:
-        x, y, t = workload.xs[b], workload.ys[b], float(workload.ts[b])
-        pb = dict(p)
-        pb['t'] = t
-        chi, st, groups, EM, EI, ED, _ = oe.mixdom2_model(pb)
-        emit = odp.log_emission_table(st, groups, x, y, EM, EI, ED)
-        odp.forward_backward(om.safe_log(chi), st, emit)
-        done_cells += (len(x) + 1) * (len(y) + 1)
+        ll, nt = _oracle_pair(workload, b, forward_only)
+        done_cells += (len(workload.xs[b]) + 1) * (len(workload.ys[b]) + 1)
         n += 1
+        if gpu_ll is not None:
+            ll_err.append(abs(gpu_ll[b] - ll) / max(abs(ll), 1e-300))
+            if nt is not None and gpu_n is not None:
+                n_err.append(np.abs(gpu_n[b] - nt).max() / max(np.abs(nt).max(), 1e-300))
         if time.perf_counter() - t0 > seconds:
             break
     el = time.perf_counter() - t0
     N = workload.n_states
-    return {'value': done_cells * N / el, 'unit': 'cell-state updates/s', 'cores': threads,
+    what = 'forward' if forward_only else 'forward+backward+counts'
+    base = {'value': done_cells * N / el, 'unit': 'cell-state updates/s', 'cores': threads,
             'kind': 'port',
             'sample': f'{n} smallest pairs of the workload ({done_cells} cells), FP64 NumPy oracle '
-                      f'forward+backward+counts, {el:.1f} s'}
+                      f'{what}, {el:.1f} s'}
+    acc = None
+    if ll_err:
+        acc = {'pairs': n, 'll_max_rel_err': float(np.max(ll_err)), 'll_median_rel_err': float(np.median(ll_err)),
+               'n_trans_max_rel_err': float(np.max(n_err)) if n_err else None,
+               'against': 'FP64 NumPy oracle (pinned to the reference outputs)'}
+    return base, acc
 
 
 def _ref_worker(args):
-    import numpy as _np
     sys.path[:0] = [ROOT, PKG_DIR]
-    from oracle import models as om, dp as odp, estep as oe
-    p, x, y = args
-    chi, st, groups, EM, EI, ED, _ = oe.mixdom2_model(p)
-    emit = odp.log_emission_table(st, groups, x, y, EM, EI, ED)
-    odp.forward_backward(om.safe_log(chi), st, emit)
-    return (len(x) + 1) * (len(y) + 1)
+    workload, b, forward_only = args
+    _oracle_pair(workload, b, forward_only)
+    return (len(workload.xs[b]) + 1) * (len(workload.ys[b]) + 1)
 
 
 def run_reference(args, rank, ws):
@@ -172,12 +209,13 @@ def run_reference(args, rank, ws):
     w = synth.CONFIGS[args.workload](seed=0)
     cores = len(os.sched_getaffinity(0))
     order = np.argsort(w.cells())
+    fwd_only = WORKLOADS[args.workload]['forward_only']
     # bounded sample: the smallest pairs up to ~2e5 cells per step
     sample, cells = [], 0
+    from pairhmm.synth import Workload
     for b in order:
-        pb = dict(w.params)
-        pb['t'] = float(w.ts[b])
-        sample.append((pb, w.xs[b], w.ys[b]))
+        one = Workload(w.name, w.model, w.params, [w.xs[b]], [w.ys[b]], w.ts[b:b + 1], w.K, w.F, w.C)
+        sample.append((one, 0, fwd_only))
         cells += w.cells()[b]
         if cells > 2.0e5 * max(1, cores // 4):
             break
@@ -192,7 +230,7 @@ def run_reference(args, rank, ws):
         el = time.perf_counter() - t0
     N = w.n_states
     val = tot * N / el
-    line = {'metric': 'pair-HMM E-step cell-state updates/s', 'value': val, 'unit': 'cell-state updates/s',
+    line = {'metric': WORKLOADS[args.workload]['metric'], 'value': val, 'unit': 'cell-state updates/s',
             'impl': 'reference', 'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': el / args.steps * 1e3, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
@@ -245,6 +283,39 @@ def serving_leg(n_requests, rate, seed=0):
             'arena_bytes': 8 << 30, 'stream_generation_s': gen_s}
 
 
+def e2e_function(workload, w, api, torch):
+    """The public call a user makes for this workload, host inputs to host outputs."""
+    if workload == 'tkf91_64pairs_len50-150':
+        Lx = np.array([len(x) for x in w.xs])
+        Ly = np.array([len(y) for y in w.ys])
+        xp = np.zeros((len(w.xs), Lx.max()), np.int64)
+        yp = np.zeros((len(w.ys), Ly.max()), np.int64)
+        for b, (x, y) in enumerate(zip(w.xs, w.ys)):
+            xp[b, :len(x)] = x
+            yp[b, :len(y)] = y
+        p = w.params
+        return lambda: {'log_p': api.estep_batch_tkf92_forward_only(
+            xp, yp, w.ts, Lx, Ly, p['ins_rate'], p['del_rate'], 0.0, p['Q'], p['pi']).cpu().numpy()}
+    if workload == 'mixdom2_k4f2c2_32pairs_len200-1500':
+        names = ['main_ins', 'main_del', 'dom_ins', 'dom_del', 'dom_weights', 'frag_weights', 'ext_rates',
+                 'class_pis', 'class_S_exch', 'classdist']
+
+        def grad_call():
+            tens = {k: torch.tensor(np.asarray(w.params[k], float), dtype=torch.float64, requires_grad=True)
+                    for k in names}
+            tt = torch.tensor(np.asarray(w.ts, float), dtype=torch.float64, requires_grad=True)
+            ll = api.mixdom2_log_prob(tens['main_ins'], tens['main_del'], tt, tens['dom_ins'], tens['dom_del'],
+                                      tens['dom_weights'], tens['frag_weights'], tens['ext_rates'],
+                                      tens['class_pis'], tens['class_S_exch'], tens['classdist'], w.xs, w.ys)
+            ll.sum().backward()
+            out = {k: v.grad.numpy() for k, v in tens.items()}
+            out['t'] = tt.grad.numpy()
+            out['log_p'] = ll.detach().cpu().numpy()
+            return out
+        return grad_call
+    return lambda: {kk: v.cpu().numpy() for kk, v in api.estep_batch_mixdom2(w.params, w.xs, w.ys, w.ts).items()}
+
+
 def main():
     args = parse_args()
     ws, rank, local = dist_setup(args)
@@ -261,19 +332,33 @@ def main():
     w = synth.CONFIGS[args.workload](seed=rank)
     if args.pairs:
         w.xs, w.ys, w.ts = w.xs[:args.pairs], w.ys[:args.pairs], w.ts[:args.pairs]
+    spec = WORKLOADS[args.workload]
+    fwd_only = spec['forward_only']
     N = w.n_states
     cells = w.cells()
     cell_states = float((cells * N).sum())
     # ---- inputs resident in HBM
-    K, F, chi, csubs, EM, EI, ED = api._mixdom2_tables(w.params, w.ts, dev)
-    plan = api.get_plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)
+    if w.model == 'mixdom2':
+        K, F, chi, csubs, EM, EI, ED = api._mixdom2_tables(w.params, w.ts, dev)
+        plan = api.get_plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)
+    else:
+        tt = torch.as_tensor(np.asarray(w.ts, np.float64), device=dev)
+        chi = pm.tkf91_trans(w.params['ins_rate'], w.params['del_rate'], tt.cpu()).to(dev)
+        EM, EI, ED = pm.tables_tkf(pm.transition_matrix(pm._t(w.params['Q'], dev), tt), pm._t(w.params['pi'], dev))
+        plan = api.get_plan(np.array([pm.S, pm.M, pm.I, pm.D, pm.E]), np.zeros(5, np.int32), 1)
     batch = _lib.make_batch(w.xs, w.ys, chi, EM, EI, ED, device=dev)
     plan.set_timing(True)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
+
+    def step(out):
+        if fwd_only:
+            ll, st = _lib.forward(plan, batch)
+            return {'ll': ll, 'status': st}
+        return _lib.estep(plan, batch, out=out)
     out = None
     for _ in range(max(3, args.warmup)):
-        out = _lib.estep(plan, batch, out=out)
+        out = step(out)
     torch.cuda.synchronize()
     launches_per_step = plan.launches
     status = out['status'].cpu().numpy()
@@ -293,7 +378,7 @@ def main():
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        out = _lib.estep(plan, batch, out=out)
+        out = step(out)
         e1.record(stream)
         a, b = plan.kernel_times()
         fwd_ms.append(a)
@@ -312,16 +397,18 @@ def main():
         total_ms = float(t.item())
     value = cell_states * ws * args.steps / (total_ms / 1e3)
     ms_step = total_ms / args.steps
+    gpu_ll = out['ll'].cpu().numpy()
+    gpu_n = None if fwd_only else out['n_trans'].cpu().numpy()
     # ---- end to end through the public API (host sequences -> host results)
     e2e_ms = []
     h2d = int(sum(len(x) + len(y) for x, y in zip(w.xs, w.ys)) + 8 * len(w.ts))
     d2h = 0
+    e2e_call = e2e_function(args.workload, w, api, torch)
     for k in range(0 if args.no_e2e else args.warmup + args.steps):
         flush.fill_(k & 0xff)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = api.estep_batch_mixdom2(w.params, w.xs, w.ys, w.ts)
-        host = {kk: v.cpu().numpy() for kk, v in r.items()}
+        host = e2e_call()
         t1 = time.perf_counter()
         if k >= args.warmup:
             e2e_ms.append((t1 - t0) * 1e3)
@@ -334,7 +421,7 @@ def main():
     e2e_value = cell_states * ws * args.steps / (e2e_total / 1e3)
     # ---- plain: one launch sequence per pair (the single-pair path)
     plain = None
-    if not args.no_plain and rank == 0:
+    if not args.no_plain and rank == 0 and not fwd_only:
         subs = []
         for b in range(len(w.xs)):
             subs.append(_lib.make_batch([w.xs[b]], [w.ys[b]], chi[b:b + 1], EM[b:b + 1],
@@ -363,7 +450,9 @@ def main():
            2: (('warp2::forward_warp_kernel', 2), ('warp2::backward_warp_kernel', 4), (None, 0)),
            3: (('blk::forward_block_kernel', 2), ('blk::backward_block_kernel', 4), (None, 0)),
            4: (('warp2::forward_warp_kernel', 2), ('warp2::backward_rec_warp_kernel', 2),
-               ('warp2::count_warp_kernel', 2))}[plan.last_variant]
+               ('warp2::count_warp_kernel', 2)),
+           5: (('blk::forward_block_kernel', 2), ('blk::backward_rec_block_kernel', 2),
+               ('blk::count_block_kernel', 2))}[plan.last_variant]
     durs = [fwd_avg, bwd_avg, cnt_avg]
     di = int(np.argmax(durs))
     dom, fpc = fam[di]
@@ -383,24 +472,25 @@ def main():
                 'kernels': [f[0] for f in fam if f[0]],
                 'hbm_peak_gbs': peaks.get('hbm_gbs')}
     serving = None
-    if rank == 0 and args.serving_requests > 0:
+    if rank == 0 and args.serving_requests > 0 and args.workload == WORKLOAD:
         serving = serving_leg(args.serving_requests, args.serving_rate)
     if rank == 0:
-        cpu = cpu_baseline(w, args.cpu_seconds) if args.cpu_seconds > 0 else None
+        cpu, acc = (cpu_baseline(w, args.cpu_seconds, fwd_only, gpu_ll, gpu_n) if args.cpu_seconds > 0
+                    else (None, None))
         line = {
-            'metric': 'pair-HMM E-step cell-state updates/s', 'value': value,
+            'metric': spec['metric'], 'value': value,
             'unit': 'cell-state updates/s', 'n_gpus': ws, 'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': ms_step, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
             'dtype': 'f32', 'data': 'synthetic',
-            'config': {'workload': args.workload, 'model': 'MixDom2 n_dom=3 n_frag=1 n_classes=1',
+            'config': {'workload': args.workload, 'model': spec['model'],
                        'n_states': N, 'pairs_per_gpu': len(w.xs), 'cells_per_gpu': int(total_cells),
                        'cell_states_per_step_per_gpu': cell_states, 'pairs_per_s': len(w.xs) * ws / (ms_step / 1e3),
                        'l2': 'flushed (256 MiB write) between timed steps', 'parallelism': f'replicas x{ws}',
                        'status_nonzero': int((status != 0).sum())},
-            'roofline': roofline, 'cpu_baseline': cpu,
+            'roofline': roofline, 'cpu_baseline': cpu, 'accuracy': acc,
             'e2e': {'value': e2e_value, 'unit': 'cell-state updates/s', 'h2d_bytes_per_step': h2d,
                     'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_total / args.steps,
-                    'api': 'pairhmm.api.estep_batch_mixdom2'},
+                    'api': spec['e2e_api']},
             'plain': plain, 'serving': serving, 'gpu_launches': launches_per_step * args.steps, 'clocks': clocks,
         }
         print(json.dumps(line))

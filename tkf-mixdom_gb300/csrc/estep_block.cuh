@@ -59,6 +59,7 @@ struct BShape {
 struct SmemB {
     int chi, chiE, tM, tI, tD, ring, halo;        // float offsets
     int ringE, haloE, misc;                       // int offsets
+    int zvec, zvecE;                              // an all-zero vector (float) and its exponents (int)
     int cst_b, cst_u, cst_bE, cst_uE, fst, fstE;  // backward count ring (float / int offsets)
     int colI, binsI;                              // backward emission-count scratch
     int ys;                                       // byte offset
@@ -85,6 +86,8 @@ __host__ __device__ inline SmemB make_smem_b(int NS, int NB, int NI, int G, int 
     L.ringE = o; o += 3 * ROWS * NBP;
     L.haloE = o; o += 3 * NBP;
     L.misc = o; o += 4 * 32;
+    L.zvec = o; o += al4(NS);
+    L.zvecE = o; o += NBP;
     if (bwd) {
         L.cst_b = o; o += KSTAGE * ROWS * SPR;
         L.cst_u = o; o += KSTAGE * ROWS * SPR;
@@ -131,6 +134,8 @@ __device__ void load_model_b(const KParams &P, int p, const PairMeta &m, const S
         sm[L.tI + idx] = __ldg(eI + idx);
         sm[L.tD + idx] = __ldg(eD + idx);
     }
+    for (int s = tid; s < NS; s += nt) sm[L.zvec + s] = 0.f;
+    for (int b = tid; b < nbp_of(NS / 4); b += nt) reinterpret_cast<int *>(sm)[L.zvecE + b] = EXP_NONE;
     unsigned char *ys = smb + L.ys;
     for (int j = tid; j <= m.Ly; j += nt) {
         int c = 0;
@@ -223,6 +228,52 @@ __device__ __forceinline__ int quad_contract(const float *vec, const int *vecE, 
     }
     out = make_float4(a0, a1, a2, a3);
     return Eref;
+}
+
+// quad_contract for the two cells of a lane at once: every transition
+// operand loaded (or held in registers) serves both cells.  A missing
+// predecessor is the zero vector with EXP_NONE exponents (no branches).
+template <class SH>
+__device__ __forceinline__ void quad_contract2(const float *v0, const int *e0, const float *v1, const int *e1,
+                                               const float (&cq)[SH::CHI_REG ? SH::NS : 1][4], const float4 *chi4q,
+                                               float4 &o0, float4 &o1, int &Eref0, int &Eref1) {
+    constexpr int NB = SH::NB, NS = SH::NS, NBP = SH::NBP;
+    int E0[NBP], E1[NBP];
+#pragma unroll
+    for (int i = 0; i < NBP / 4; ++i) {
+        const int4 a = reinterpret_cast<const int4 *>(e0)[i];
+        const int4 b = reinterpret_cast<const int4 *>(e1)[i];
+        E0[4 * i] = a.x; E0[4 * i + 1] = a.y; E0[4 * i + 2] = a.z; E0[4 * i + 3] = a.w;
+        E1[4 * i] = b.x; E1[4 * i + 1] = b.y; E1[4 * i + 2] = b.z; E1[4 * i + 3] = b.w;
+    }
+    Eref0 = EXP_NONE;
+    Eref1 = EXP_NONE;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) { Eref0 = max(Eref0, E0[b]); Eref1 = max(Eref1, E1[b]); }
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const float s0 = pow2n(E0[b] - Eref0), s1 = pow2n(E1[b] - Eref1);
+        const float4 x = *reinterpret_cast<const float4 *>(v0 + 4 * b);
+        const float4 y = *reinterpret_cast<const float4 *>(v1 + 4 * b);
+        const float xs[4] = {x.x * s0, x.y * s0, x.z * s0, x.w * s0};
+        const float ysv[4] = {y.x * s1, y.y * s1, y.z * s1, y.w * s1};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int s = 4 * b + i;
+            float k0, k1, k2, k3;
+            if constexpr (SH::CHI_REG) {
+                k0 = cq[s][0]; k1 = cq[s][1]; k2 = cq[s][2]; k3 = cq[s][3];
+            } else {
+                const float4 cv = chi4q[s * (NS / 4)];
+                k0 = cv.x; k1 = cv.y; k2 = cv.z; k3 = cv.w;
+            }
+            a0 = fmaf(xs[i], k0, a0); a1 = fmaf(xs[i], k1, a1); a2 = fmaf(xs[i], k2, a2); a3 = fmaf(xs[i], k3, a3);
+            c0 = fmaf(ysv[i], k0, c0); c1 = fmaf(ysv[i], k1, c1); c2 = fmaf(ysv[i], k2, c2); c3 = fmaf(ysv[i], k3, c3);
+        }
+    }
+    o0 = make_float4(a0, a1, a2, a3);
+    o1 = make_float4(c0, c1, c2, c3);
 }
 
 __device__ __forceinline__ void copy_edge_cell(const float *v, const int *e, float *gv, int *ge, int NS, int NBP) {
@@ -329,7 +380,35 @@ __device__ void fwd_stripe_b(const KParams &P, int p, int si, const SmemB &L, fl
             }
             pv = ld_acquire(prog_above);
         }
-        // ---- compute my quad for both cells
+        // ---- my quad for both cells: predecessors, then one merged contraction
+        const float *pvp[R];
+        const int *pep[R];
+#pragma unroll
+        for (int c = 0; c < R; ++c) {
+            const int rho = lane + 32 * c;
+            const int j = t - rho;
+            const int i = rowi[c];
+            const bool valid = rho < nrows && j >= 0 && j <= Ly;
+            pvp[c] = sm + L.zvec;
+            pep[c] = reinterpret_cast<const int *>(sm) + L.zvecE;
+            if (!valid) continue;
+            if (qt == T_I) {
+                if (j >= 1) { pvp[c] = ring + ((t + 2) % 3) * ROWS * SPR + rho * SPR; pep[c] = ringE + ((t + 2) % 3) * ROWS * NBP + rho * NBP; }
+            } else if (qt == T_D) {
+                if (i >= 1) {
+                    if (rho >= 1) { pvp[c] = ring + ((t + 2) % 3) * ROWS * SPR + (rho - 1) * SPR; pep[c] = ringE + ((t + 2) % 3) * ROWS * NBP + (rho - 1) * NBP; }
+                    else { pvp[c] = halo + (j % 3) * NS; pep[c] = haloE + (j % 3) * NBP; }
+                }
+            } else if (qt == T_M) {
+                if (i >= 1 && j >= 1) {
+                    if (rho >= 1) { pvp[c] = ring + ((t + 1) % 3) * ROWS * SPR + (rho - 1) * SPR; pep[c] = ringE + ((t + 1) % 3) * ROWS * NBP + (rho - 1) * NBP; }
+                    else { pvp[c] = halo + ((j - 1) % 3) * NS; pep[c] = haloE + ((j - 1) % 3) * NBP; }
+                }
+            }
+        }
+        float4 oc[R];
+        int Erc[R];
+        quad_contract2<SH>(pvp[0], pep[0], pvp[1], pep[1], cq, chi4q, oc[0], oc[1], Erc[0], Erc[1]);
 #pragma unroll
         for (int c = 0; c < R; ++c) {
             const int rho = lane + 32 * c;
@@ -337,28 +416,11 @@ __device__ void fwd_stripe_b(const KParams &P, int p, int si, const SmemB &L, fl
             const bool valid = rho < nrows && j >= 0 && j <= Ly;
             if (!valid) continue;
             const int i = rowi[c];
-            const float *pv_ptr = nullptr;
-            const int *pe_ptr = nullptr;
-            bool has = false;
-            if (qt == T_I) {
-                if (j >= 1) { has = true; pv_ptr = ring + ((t + 2) % 3) * ROWS * SPR + rho * SPR; pe_ptr = ringE + ((t + 2) % 3) * ROWS * NBP + rho * NBP; }
-            } else if (qt == T_D) {
-                if (i >= 1) {
-                    has = true;
-                    if (rho >= 1) { pv_ptr = ring + ((t + 2) % 3) * ROWS * SPR + (rho - 1) * SPR; pe_ptr = ringE + ((t + 2) % 3) * ROWS * NBP + (rho - 1) * NBP; }
-                    else { pv_ptr = halo + (j % 3) * NS; pe_ptr = haloE + (j % 3) * NBP; }
-                }
-            } else if (qt == T_M) {
-                if (i >= 1 && j >= 1) {
-                    has = true;
-                    if (rho >= 1) { pv_ptr = ring + ((t + 1) % 3) * ROWS * SPR + (rho - 1) * SPR; pe_ptr = ringE + ((t + 1) % 3) * ROWS * NBP + (rho - 1) * NBP; }
-                    else { pv_ptr = halo + ((j - 1) % 3) * NS; pe_ptr = haloE + ((j - 1) % 3) * NBP; }
-                }
-            }
             float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
             int Eo = EXP_NONE;
-            if (has) {
-                const int Eref = quad_contract<SH>(pv_ptr, pe_ptr, cq, chi4q, o);
+            {
+                const int Eref = Erc[c];
+                o = oc[c];
                 const float4 e = quad_emit_vals(sm, qe[c], ys[j]);
                 o = make_float4(o.x * e.x, o.y * e.y, o.z * e.z, o.w * e.w);
                 const float mx = f4max(o);

@@ -30,12 +30,13 @@ __device__ void bwd_rec_stripe_b(const KParams &P, int p, int si, const SmemB &L
     const int nrows = min(ROWS, Lx + 1 - i0);
     const bool has_below = si + 1 < m.n_stripes;
     const bool has_above = si > 0;
-    const int *prog_below = has_below ? P.progress + m.stripe_base + si + 1 : nullptr;
-    int *prog_mine = P.progress + m.stripe_base + si;
-    const float *edge_below = P.edge + (m.edge_base + (int64_t)(si + 1) * (Ly + 1)) * NS;
-    const int *edgeE_below = P.edge_exp + (m.edge_base + (int64_t)(si + 1) * (Ly + 1)) * NBP;
-    float *edge_mine = P.edge + (m.edge_base + (int64_t)si * (Ly + 1)) * NS;
-    int *edgeE_mine = P.edge_exp + (m.edge_base + (int64_t)si * (Ly + 1)) * NBP;
+    // the backward direction's own progress counters and edge rows
+    const int *prog_below = has_below ? P.bprogress + m.stripe_base + si + 1 : nullptr;
+    int *prog_mine = P.bprogress + m.stripe_base + si;
+    const float *edge_below = P.bedge + (m.edge_base + (int64_t)(si + 1) * (Ly + 1)) * NS;
+    const int *edgeE_below = P.bedge_exp + (m.edge_base + (int64_t)(si + 1) * (Ly + 1)) * NBP;
+    float *edge_mine = P.bedge + (m.edge_base + (int64_t)si * (Ly + 1)) * NS;
+    int *edgeE_mine = P.bedge_exp + (m.edge_base + (int64_t)si * (Ly + 1)) * NBP;
     const int64_t latc = m.lat_base + (int64_t)si * (ROWS + Ly) * ROWS;
 
     load_model_b(P, p, m, L, sm, smb, true);
@@ -115,74 +116,103 @@ __device__ void bwd_rec_stripe_b(const KParams &P, int p, int si, const SmemB &L
             pv = ld_acquire(prog_below);
         }
         if (tid == 0) misc[(k + 1) & 1] = 0;   // every warp read it two barriers ago
+        // ---- successor vectors of both cells (the zero vector when one does not exist)
+        const float *zv = sm + L.zvec;
+        const int *ze = reinterpret_cast<const int *>(sm) + L.zvecE;
+        const float *vI[R], *vD[R], *vM[R];
+        const int *eI[R], *eD[R], *eM[R];
+        bool valid[R], term[R];
 #pragma unroll
         for (int c = 0; c < R; ++c) {
             const int rho = lane + 32 * c;
             const int j = t - rho;
-            const bool valid = rho < nrows && j >= 0 && j <= Ly;
+            const int i = rowi[c];
+            valid[c] = rho < nrows && j >= 0 && j <= Ly;
+            term[c] = valid[c] && i == Lx && j == Ly;
+            vI[c] = vD[c] = vM[c] = zv;
+            eI[c] = eD[c] = eM[c] = ze;
+            if (!valid[c] || term[c]) continue;
+            const bool hI = j + 1 <= Ly, hD = i + 1 <= Lx, hM = hI && hD;
+            if (hI) { vI[c] = ring + ((t + 1) % 3) * ROWS * SPR + rho * SPR; eI[c] = ringE + ((t + 1) % 3) * ROWS * NBP + rho * NBP; }
+            if (hD) {
+                if (rho + 1 < nrows) { vD[c] = ring + ((t + 1) % 3) * ROWS * SPR + (rho + 1) * SPR; eD[c] = ringE + ((t + 1) % 3) * ROWS * NBP + (rho + 1) * NBP; }
+                else { vD[c] = halo + (j % 3) * NS; eD[c] = haloE + (j % 3) * NBP; }
+            }
+            if (hM) {
+                if (rho + 1 < nrows) { vM[c] = ring + ((t + 2) % 3) * ROWS * SPR + (rho + 1) * SPR; eM[c] = ringE + ((t + 2) % 3) * ROWS * NBP + (rho + 1) * NBP; }
+                else { vM[c] = halo + ((j + 1) % 3) * NS; eM[c] = haloE + ((j + 1) % 3) * NBP; }
+            }
+        }
+        // ---- b[4q+u] = sum over destination quads d of chi[4q+u][d..] w_succ(type d)[d..],
+        // both cells in one pass over the transition operands
+        int Ed[R][NB];
+        int Eref[R];
+#pragma unroll
+        for (int c = 0; c < R; ++c) {
+            int EvM[NBP], EvI[NBP], EvD[NBP];
+#pragma unroll
+            for (int ii = 0; ii < NBP / 4; ++ii) {
+                const int4 a = reinterpret_cast<const int4 *>(eM[c])[ii];
+                const int4 b = reinterpret_cast<const int4 *>(eI[c])[ii];
+                const int4 d4 = reinterpret_cast<const int4 *>(eD[c])[ii];
+                EvM[4 * ii] = a.x; EvM[4 * ii + 1] = a.y; EvM[4 * ii + 2] = a.z; EvM[4 * ii + 3] = a.w;
+                EvI[4 * ii] = b.x; EvI[4 * ii + 1] = b.y; EvI[4 * ii + 2] = b.z; EvI[4 * ii + 3] = b.w;
+                EvD[4 * ii] = d4.x; EvD[4 * ii + 1] = d4.y; EvD[4 * ii + 2] = d4.z; EvD[4 * ii + 3] = d4.w;
+            }
+            Eref[c] = EXP_NONE;
+#pragma unroll
+            for (int d = 0; d < NB; ++d) {
+                const int dt = P.quad_type[d];
+                Ed[c][d] = dt == T_M ? EvM[d] : (dt == T_I ? EvI[d] : (dt == T_D ? EvD[d] : EXP_NONE));
+                Eref[c] = max(Eref[c], Ed[c][d]);
+            }
+        }
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f;
+#pragma unroll
+        for (int d = 0; d < NB; ++d) {
+            const int dt = P.quad_type[d];
+            const float *v0 = dt == T_M ? vM[0] : (dt == T_I ? vI[0] : (dt == T_D ? vD[0] : zv));
+            const float *v1 = dt == T_M ? vM[1] : (dt == T_I ? vI[1] : (dt == T_D ? vD[1] : zv));
+            const float s0 = pow2n(Ed[0][d] - Eref[0]), s1 = pow2n(Ed[1][d] - Eref[1]);
+            const float4 x = *reinterpret_cast<const float4 *>(v0 + 4 * d);
+            const float4 y = *reinterpret_cast<const float4 *>(v1 + 4 * d);
+            const float xs[4] = {x.x * s0, x.y * s0, x.z * s0, x.w * s0};
+            const float yv[4] = {y.x * s1, y.y * s1, y.z * s1, y.w * s1};
+#pragma unroll
+            for (int ii = 0; ii < 4; ++ii) {
+                const int kk = 4 * d + ii;
+                float c0, c1, c2, c3;
+                if constexpr (SH::CHI_REG) {
+                    c0 = cq[kk][0]; c1 = cq[kk][1]; c2 = cq[kk][2]; c3 = cq[kk][3];
+                } else {
+                    const float4 cv = chi4q[kk * (NS / 4)];
+                    c0 = cv.x; c1 = cv.y; c2 = cv.z; c3 = cv.w;
+                }
+                a0 = fmaf(xs[ii], c0, a0); a1 = fmaf(xs[ii], c1, a1); a2 = fmaf(xs[ii], c2, a2); a3 = fmaf(xs[ii], c3, a3);
+                g0 = fmaf(yv[ii], c0, g0); g1 = fmaf(yv[ii], c1, g1); g2 = fmaf(yv[ii], c2, g2); g3 = fmaf(yv[ii], c3, g3);
+            }
+        }
+        const float4 accv[R] = {make_float4(a0, a1, a2, a3), make_float4(g0, g1, g2, g3)};
+#pragma unroll
+        for (int c = 0; c < R; ++c) {
+            const int rho = lane + 32 * c;
+            const int j = t - rho;
             float4 bq = make_float4(0.f, 0.f, 0.f, 0.f), wq = bq;
             int Eb = EXP_NONE;
-            if (valid) {
-                const int i = rowi[c];
-                const bool term = (i == Lx && j == Ly);
-                const bool hI = j + 1 <= Ly, hD = i + 1 <= Lx, hM = hI && hD;
-                const float *vI = hI ? ring + ((t + 1) % 3) * ROWS * SPR + rho * SPR : nullptr;
-                const int *eI = hI ? ringE + ((t + 1) % 3) * ROWS * NBP + rho * NBP : nullptr;
-                const float *vD = nullptr, *vM = nullptr;
-                const int *eD = nullptr, *eM = nullptr;
-                if (hD) {
-                    if (rho + 1 < nrows) { vD = ring + ((t + 1) % 3) * ROWS * SPR + (rho + 1) * SPR; eD = ringE + ((t + 1) % 3) * ROWS * NBP + (rho + 1) * NBP; }
-                    else { vD = halo + (j % 3) * NS; eD = haloE + (j % 3) * NBP; }
+            if (valid[c]) {
+                int Er = Eref[c];
+                if (term[c]) {
+                    bq = *reinterpret_cast<const float4 *>(sm + L.chiE + 4 * q);
+                    Er = 0;
+                } else {
+                    bq = accv[c];
                 }
-                if (hM) {
-                    if (rho + 1 < nrows) { vM = ring + ((t + 2) % 3) * ROWS * SPR + (rho + 1) * SPR; eM = ringE + ((t + 2) % 3) * ROWS * NBP + (rho + 1) * NBP; }
-                    else { vM = halo + ((j + 1) % 3) * NS; eM = haloE + ((j + 1) % 3) * NBP; }
-                }
-                int Ed[NB];
-                int Eref = EXP_NONE;
-#pragma unroll
-                for (int d = 0; d < NB; ++d) {
-                    const int dt = P.quad_type[d];
-                    const int *ee = dt == T_M ? eM : (dt == T_I ? eI : (dt == T_D ? eD : nullptr));
-                    Ed[d] = ee ? ee[d] : EXP_NONE;
-                    Eref = max(Eref, Ed[d]);
-                }
-                float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-                if (term) {
-                    const float4 ce = *reinterpret_cast<const float4 *>(sm + L.chiE + 4 * q);
-                    a0 = ce.x; a1 = ce.y; a2 = ce.z; a3 = ce.w;
-                    Eref = 0;
-                } else if (Eref > EXP_NONE) {
-#pragma unroll
-                    for (int d = 0; d < NB; ++d) {
-                        if (Ed[d] <= EXP_NONE) continue;
-                        const int dt = P.quad_type[d];
-                        const float *vv = dt == T_M ? vM : (dt == T_I ? vI : vD);
-                        const float sc = pow2n(Ed[d] - Eref);
-                        const float4 w4 = *reinterpret_cast<const float4 *>(vv + 4 * d);
-                        const float ws[4] = {w4.x * sc, w4.y * sc, w4.z * sc, w4.w * sc};
-#pragma unroll
-                        for (int ii = 0; ii < 4; ++ii) {
-                            const int kk = 4 * d + ii;
-                            float c0, c1, c2, c3;
-                            if constexpr (SH::CHI_REG) {
-                                c0 = cq[kk][0]; c1 = cq[kk][1]; c2 = cq[kk][2]; c3 = cq[kk][3];
-                            } else {
-                                const float4 cv = chi4q[kk * (NS / 4)];
-                                c0 = cv.x; c1 = cv.y; c2 = cv.z; c3 = cv.w;
-                            }
-                            a0 = fmaf(ws[ii], c0, a0); a1 = fmaf(ws[ii], c1, a1);
-                            a2 = fmaf(ws[ii], c2, a2); a3 = fmaf(ws[ii], c3, a3);
-                        }
-                    }
-                }
-                bq = make_float4(a0, a1, a2, a3);
                 const float mx = f4max(bq);
-                if (mx > 0.f && Eref > EXP_NONE) {
+                if (mx > 0.f && Er > EXP_NONE) {
                     const int eb = warp2::exp_of(mx);
                     if (-eb >= -126 && -eb <= 127) bq = f4scale(bq, pow2f(-eb));
                     else bq = make_float4(ldexpf(bq.x, -eb), ldexpf(bq.y, -eb), ldexpf(bq.z, -eb), ldexpf(bq.w, -eb));
-                    Eb = Eref + eb;
+                    Eb = Er + eb;
                 } else {
                     bq = make_float4(0.f, 0.f, 0.f, 0.f);
                 }
@@ -210,8 +240,15 @@ __device__ void bwd_rec_stripe_b(const KParams &P, int p, int si, const SmemB &L
     bar_sync(BAR_STEP, NB * 32);
 }
 
+// Both wavefronts of the split E-step in one persistent launch: the work list
+// interleaves forward stripes and backward stripes (bit 30 of the stripe
+// field marks a backward item), each direction in its own longest-pair-first
+// order, so the two share the GPU's CTA slots as they free up.  A stripe waits
+// only for a stripe of its own direction popped before it.
+constexpr int BWD_ITEM = 1 << 30;
+
 template <class SH>
-__global__ void __launch_bounds__(32 * SH::NB) backward_rec_block_kernel(const KParams P) {
+__global__ void __launch_bounds__(32 * SH::NB) fwdbwd_block_kernel(const KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
     float *sm = reinterpret_cast<float *>(smem_raw);
@@ -223,7 +260,8 @@ __global__ void __launch_bounds__(32 * SH::NB) backward_rec_block_kernel(const K
         const int it = s_item;
         if (it >= P.n_items) break;
         const int2 w = P.items[it];
-        bwd_rec_stripe_b<SH>(P, w.x, w.y, L, sm, smem_raw);
+        if (w.y & BWD_ITEM) bwd_rec_stripe_b<SH>(P, w.x, w.y & ~BWD_ITEM, L, sm, smem_raw);
+        else fwd_stripe_b<SH>(P, w.x, w.y, L, sm, smem_raw);
     }
 }
 
@@ -234,7 +272,11 @@ struct SmemCB {
     int bytes;
 };
 
-__host__ __device__ inline SmemCB make_smem_cb(int NS, int G, int max_ly) {
+// Emission-count bins are indexed by slot (M: [row][M slot][y], I: [column
+// mod 64][I slot], D: [row][D slot]): a cell's slots are owned by one thread
+// each and the cells of one step have distinct rows and columns, so the bins
+// need no atomics.  wM / wI / wD are the slot widths of the three types.
+__host__ __device__ inline SmemCB make_smem_cb(int NS, int G, int max_ly, int wM, int wI, int wD) {
     const int SPR = spr_of(NS);
     SmemCB L;
     int o = 0;
@@ -243,9 +285,9 @@ __host__ __device__ inline SmemCB make_smem_cb(int NS, int G, int max_ly) {
     L.tD = o; o += al4(G * 21);
     L.fst = o; o += ROWS * SPR;
     L.ust = o; o += ROWS * SPR;
-    L.rowM = o; o += ROWS * al4(G * 21);
-    L.rowD = o; o += al4(ROWS * G);
-    L.colI = o; o += al4(ROWS * G);
+    L.rowM = o; o += al4(ROWS * wM * 21);
+    L.rowD = o; o += al4(ROWS * wD);
+    L.colI = o; o += al4(ROWS * wI);
     L.binsI = o; o += al4(G * 21);
     int bytes = o * 4;
     L.ys = bytes;
@@ -296,7 +338,8 @@ __device__ void count_chunk_b(const KParams &P, int p, int si, int ch, const Sme
     const double lam = llv / LN2;
     const int Ep = (int)floor(lam);
     const float rfrac = (float)exp2(-(lam - floor(lam)));
-    const int GR = al4(G * 21);
+    const int mb = P.kbeg[0], ib = P.kbeg[1], db = P.kbeg[2];
+    const int wM = P.kend[0] - mb, wI = P.kend[1] - ib, wD = P.kend[2] - db;
     {
         const float *eM = P.eM + (int64_t)p * P.eM_stride;
         const float *eI = P.eI + (int64_t)p * P.eID_stride;
@@ -307,8 +350,9 @@ __device__ void count_chunk_b(const KParams &P, int p, int si, int ch, const Sme
             sm[L.tD + idx] = __ldg(eDg + idx);
             sm[L.binsI + idx] = 0.f;
         }
-        for (int idx = tid; idx < ROWS * GR; idx += CNT_THREADS) sm[L.rowM + idx] = 0.f;
-        for (int idx = tid; idx < ROWS * G; idx += CNT_THREADS) { sm[L.rowD + idx] = 0.f; sm[L.colI + idx] = 0.f; }
+        for (int idx = tid; idx < ROWS * wM * 21; idx += CNT_THREADS) sm[L.rowM + idx] = 0.f;
+        for (int idx = tid; idx < ROWS * wD; idx += CNT_THREADS) sm[L.rowD + idx] = 0.f;
+        for (int idx = tid; idx < ROWS * wI; idx += CNT_THREADS) sm[L.colI + idx] = 0.f;
         unsigned char *ysw = smb + L.ys;
         const int jlo = max(0, t0 - (ROWS - 1)), jhi = min(Ly, t_hi + 1);
         for (int j = jlo + tid; j <= jhi; j += CNT_THREADS) {
@@ -340,28 +384,49 @@ __device__ void count_chunk_b(const KParams &P, int p, int si, int ch, const Sme
 #pragma unroll
         for (int u = 0; u < 16; ++u) { csum[a][u] = 0.f; ccomp[a][u] = 0.f; }
 
+    // lattice loads of one step for this thread's cell and quads; issued a step
+    // ahead (before the outer products of the current step) so their latency
+    // hides behind phase B
+    int Ef[QPT], Eb[QPT], Es[QPT];
+    float4 fv[QPT], bv[QPT], sv[QPT];
+    auto issue = [&](int t) {
+        const int j = t - rho;
+        const bool valid = t >= t0 && rho < nrows && j >= 0 && j <= Ly;
+        const int64_t cell = latc + (int64_t)t * ROWS + rho;
+        const bool hI = j + 1 <= Ly, hD = irow + 1 <= Lx, hM = hI && hD;
+#pragma unroll
+        for (int a = 0; a < QPT; ++a) {
+            const int q = sub + 4 * a;
+            Ef[a] = EXP_NONE; Eb[a] = EXP_NONE; Es[a] = EXP_NONE;
+            fv[a] = make_float4(0.f, 0.f, 0.f, 0.f); bv[a] = fv[a]; sv[a] = fv[a];
+            if (!valid || q >= NB) continue;
+            // every quad of a valid cell is written (zero values with EXP_NONE)
+            Ef[a] = __ldg(P.lat_exp + cell * NBP + q);
+            Eb[a] = __ldg(P.blat_exp + cell * NBP + q);
+            fv[a] = __ldg(reinterpret_cast<const float4 *>(P.lat + cell * NS) + q);
+            bv[a] = __ldg(reinterpret_cast<const float4 *>(P.blat + cell * NS) + q);
+            const int qt = P.quad_type[q];
+            int64_t sc = -1;
+            if (qt == T_I && hI) sc = latc + (int64_t)(t + 1) * ROWS + rho;
+            else if (qt == T_D && hD && (rho + 1 < nrows || has_below))
+                sc = rho + 1 < nrows ? latc + (int64_t)(t + 1) * ROWS + rho + 1 : latb + (int64_t)j * ROWS;
+            else if (qt == T_M && hM && (rho + 1 < nrows || has_below))
+                sc = rho + 1 < nrows ? latc + (int64_t)(t + 2) * ROWS + rho + 1 : latb + (int64_t)(j + 1) * ROWS;
+            if (sc >= 0) {
+                Es[a] = __ldg(P.blat_exp + sc * NBP + q);
+                sv[a] = __ldg(reinterpret_cast<const float4 *>(P.blat + sc * NS) + q);
+            }
+        }
+    };
+    issue(t_hi);
     for (int t = t_hi; t >= t0; --t) {
         // ================= phase A: one cell per 4 threads
         {
             const int j = t - rho;
             const bool valid = rho < nrows && j >= 0 && j <= Ly;
-            const int64_t cell = latc + (int64_t)t * ROWS + rho;
-            int Ef[QPT], Eb[QPT];
-            float4 fv[QPT], bv[QPT];
             int Efl = EXP_NONE;
 #pragma unroll
-            for (int a = 0; a < QPT; ++a) {
-                const int q = sub + 4 * a;
-                Ef[a] = EXP_NONE; Eb[a] = EXP_NONE;
-                fv[a] = make_float4(0.f, 0.f, 0.f, 0.f); bv[a] = fv[a];
-                if (valid && q < NB) {
-                    Ef[a] = __ldg(P.lat_exp + cell * NBP + q);
-                    Eb[a] = __ldg(P.blat_exp + cell * NBP + q);
-                    if (Ef[a] > EXP_NONE) fv[a] = __ldg(reinterpret_cast<const float4 *>(P.lat + cell * NS) + q);
-                    if (Eb[a] > EXP_NONE) bv[a] = __ldg(reinterpret_cast<const float4 *>(P.blat + cell * NS) + q);
-                    Efl = max(Efl, Ef[a]);
-                }
-            }
+            for (int a = 0; a < QPT; ++a) Efl = max(Efl, Ef[a]);
             Efl = max(Efl, __shfl_xor_sync(0xffffffffu, Efl, 1));
             const int Efm = max(Efl, __shfl_xor_sync(0xffffffffu, Efl, 2));
             const bool live = valid && Efm > EXP_NONE;
@@ -388,51 +453,40 @@ __device__ void count_chunk_b(const KParams &P, int p, int si, int ch, const Sme
                             const int st = P.slot_type[s];
                             const float pv = pk[u];
                             if (pv == 0.f) continue;
-                            if (st == T_M) atomicAdd(rowM + rho * GR + P.slot_group[s] * 21 + yj, pv);
-                            else if (st == T_I) atomicAdd(colI + (j % ROWS) * G + P.slot_group[s], pv);
-                            else if (st == T_D) atomicAdd(rowD + rho * G + P.slot_group[s], pv);
+                            if (st == T_M) rowM[(rho * wM + s - mb) * 21 + yj] += pv;
+                            else if (st == T_I) colI[(j % ROWS) * wI + s - ib] += pv;
+                            else if (st == T_D) rowD[rho * wD + s - db] += pv;
                             if (term && P.slot_orig[s] >= 0)
                                 atomicAdd(P.n_trans + ((int64_t)p * N + P.slot_orig[s]) * N + P.e_idx, (double)pv);
                         }
                     }
                     // successor operand of my destination quad
-                    const int qt = P.quad_type[q];
-                    const bool hI = j + 1 <= Ly, hD = irow + 1 <= Lx, hM = hI && hD;
-                    bool has = false;
-                    int64_t sc = 0;
-                    int xi = 0, yy = 0;
-                    if (qt == T_I && hI) { has = true; sc = latc + (int64_t)(t + 1) * ROWS + rho; xi = xc; yy = yn; }
-                    else if (qt == T_D && hD) {
-                        has = true; xi = xn; yy = yj;
-                        sc = rho + 1 < nrows ? latc + (int64_t)(t + 1) * ROWS + rho + 1 : latb + (int64_t)j * ROWS;
-                    } else if (qt == T_M && hM) {
-                        has = true; xi = xn; yy = yn;
-                        sc = rho + 1 < nrows ? latc + (int64_t)(t + 2) * ROWS + rho + 1 : latb + (int64_t)(j + 1) * ROWS;
-                    }
-                    if (has && !term && (rho + 1 < nrows || qt == T_I || has_below)) {
-                        const int Es = __ldg(P.blat_exp + sc * NBP + q);
-                        if (Es > EXP_NONE) {
-                            int du = Es + Efm - Ep;
-                            if (du > 126) { du = 126; atomicOr(P.status + p, PHMM_ST_SCALE_CLAMP); }
-                            const float us = fminf(warp2::scale_pow2(rfrac, max(du, -200)), 3e38f);
-                            const float4 b4 = __ldg(reinterpret_cast<const float4 *>(P.blat + sc * NS) + q);
-                            const float4 e4 = quad_emit_at(P, sm, L, q, xi, yy);
-                            uu = make_float4(b4.x * e4.x * us, b4.y * e4.y * us, b4.z * e4.z * us, b4.w * e4.w * us);
-                        }
+                    if (Es[a] > EXP_NONE && !term) {
+                        const int qt = P.quad_type[q];
+                        const int xi = qt == T_I ? xc : xn;
+                        const int yy = qt == T_D ? yj : yn;
+                        int du = Es[a] + Efm - Ep;
+                        if (du > 126) { du = 126; atomicOr(P.status + p, PHMM_ST_SCALE_CLAMP); }
+                        const float us = fminf(warp2::scale_pow2(rfrac, max(du, -200)), 3e38f);
+                        const float4 e4 = quad_emit_at(P, sm, L, q, xi, yy);
+                        uu = make_float4(sv[a].x * e4.x * us, sv[a].y * e4.y * us, sv[a].z * e4.z * us,
+                                         sv[a].w * e4.w * us);
                     }
                 }
                 *reinterpret_cast<float4 *>(fst + rho * SPR + 4 * q) = ft;
                 *reinterpret_cast<float4 *>(ust + rho * SPR + 4 * q) = uu;
             }
         }
+        issue(t - 1);
         __syncthreads();
         // column t is complete once row 0 visited it: I-type bins
         if (tid == 0 && t <= Ly) {
             const int slot = t % ROWS;
             const int yj = ys[t];
-            for (int g = 0; g < G; ++g) {
-                binsI[g * 21 + yj] += colI[slot * G + g];
-                colI[slot * G + g] = 0.f;
+            for (int k = 0; k < wI; ++k) {
+                const int s = ib + k;
+                if (P.slot_type[s] == T_I) binsI[P.slot_group[s] * 21 + yj] += colI[slot * wI + k];
+                colI[slot * wI + k] = 0.f;
             }
         }
         // ================= phase B: outer products of the step's cells
@@ -484,30 +538,30 @@ __device__ void count_chunk_b(const KParams &P, int p, int si, int ch, const Sme
             atomicAdd(P.n_trans + ((int64_t)p * N + os) * N + ok, (double)val * (double)__ldg(chi + os * N + ok));
         }
     }
-    for (int idx = tid; idx < ROWS * G * 21; idx += CNT_THREADS) {
-        const int r = idx / (G * 21), gy = idx % (G * 21);
-        const float v = rowM[r * GR + gy];
+    for (int idx = tid; idx < ROWS * wM * 21; idx += CNT_THREADS) {
+        const int r = idx / (wM * 21), k = (idx / 21) % wM, y = idx % 21;
+        const float v = rowM[idx];
         const int ir = i0 + r;
-        if (v != 0.f && ir >= 1 && ir <= Lx) {
+        if (v != 0.f && ir >= 1 && ir <= Lx && P.slot_type[mb + k] == T_M) {
             const int xr = min((int)P.res[m.x_off + ir - 1], 20);
-            atomicAdd(P.cntM + ((int64_t)p * G + gy / 21) * 441 + xr * 21 + gy % 21, (double)v);
+            atomicAdd(P.cntM + ((int64_t)p * G + P.slot_group[mb + k]) * 441 + xr * 21 + y, (double)v);
         }
     }
-    for (int idx = tid; idx < ROWS * G; idx += CNT_THREADS) {
-        const int r = idx / G, g = idx % G;
+    for (int idx = tid; idx < ROWS * wD; idx += CNT_THREADS) {
+        const int r = idx / wD, k = idx % wD;
         const float v = rowD[idx];
         const int ir = i0 + r;
-        if (v != 0.f && ir >= 1 && ir <= Lx) {
+        if (v != 0.f && ir >= 1 && ir <= Lx && P.slot_type[db + k] == T_D) {
             const int xr = min((int)P.res[m.x_off + ir - 1], 20);
-            atomicAdd(P.cntD + ((int64_t)p * G + g) * 21 + xr, (double)v);
+            atomicAdd(P.cntD + ((int64_t)p * G + P.slot_group[db + k]) * 21 + xr, (double)v);
         }
     }
     // I-type columns not completed inside the chunk
-    for (int idx = tid; idx < ROWS * G; idx += CNT_THREADS) {
-        const int jj = max(0, t0 - (ROWS - 1)) + idx / G, g = idx % G;
-        if (jj > min(Ly, t0 - 1)) continue;
-        const float v = colI[(jj % ROWS) * G + g];
-        if (v != 0.f) atomicAdd(P.cntI + ((int64_t)p * G + g) * 21 + ys[jj], (double)v);
+    for (int idx = tid; idx < ROWS * wI; idx += CNT_THREADS) {
+        const int jj = max(0, t0 - (ROWS - 1)) + idx / wI, k = idx % wI;
+        if (jj > min(Ly, t0 - 1) || P.slot_type[ib + k] != T_I) continue;
+        const float v = colI[(jj % ROWS) * wI + k];
+        if (v != 0.f) atomicAdd(P.cntI + ((int64_t)p * G + P.slot_group[ib + k]) * 21 + ys[jj], (double)v);
     }
     for (int idx = tid; idx < G * 21; idx += CNT_THREADS) {
         const float v = binsI[idx];
@@ -517,11 +571,12 @@ __device__ void count_chunk_b(const KParams &P, int p, int si, int ch, const Sme
 }
 
 template <class SH>
-__global__ void __launch_bounds__(CNT_THREADS) count_block_kernel(const KParams P) {
+__global__ void __launch_bounds__(CNT_THREADS, 2) count_block_kernel(const KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
     float *sm = reinterpret_cast<float *>(smem_raw);
-    const SmemCB L = make_smem_cb(SH::NS, P.G, P.max_ly);
+    const SmemCB L = make_smem_cb(SH::NS, P.G, P.max_ly, P.kend[0] - P.kbeg[0], P.kend[1] - P.kbeg[1],
+                                  P.kend[2] - P.kbeg[2]);
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_item = atomicAdd(P.counter, 1);

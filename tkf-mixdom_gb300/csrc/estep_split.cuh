@@ -259,9 +259,14 @@ __global__ void __launch_bounds__(32) backward_rec_warp_kernel(const KParams P) 
 }
 
 // ---------------------------------------------------------------- counts from both lattices
+// One warp per chunk of CCH anti-diagonal steps of one stripe.  The forward
+// and backward lattice rows of step t-1 are copied into shared memory with
+// cp.async while step t is processed (double buffer); lane 31's successor in
+// the first row of the stripe below is loaded one step ahead into registers.
 struct SmemC {
-    int tM, tI, tD, fst, ust, bins, colI, rowM;   // float offsets
-    int ys;                                       // byte offset
+    int tM, tI, tD, fbuf, bbuf, ust, bins, colI;   // float offsets
+    int fE, bE;                                    // int offsets
+    int ys;                                        // byte offset
     int bytes;
 };
 
@@ -271,50 +276,18 @@ __host__ __device__ inline SmemC make_smem_c(int SP, int KP, int NI, int G, int 
     L.tM = o; o += al4(G * 441);
     L.tI = o; o += al4(G * 21);
     L.tD = o; o += al4(G * 21);
-    L.fst = o; o += ROWS * (SP + 4);
+    L.fbuf = o; o += 2 * ROWS * (SP + 4);
+    L.bbuf = o; o += 2 * ROWS * (SP + 4);
     L.ust = o; o += ROWS * (KP + 4);
     L.bins = o; o += al4(G * 21);
     L.colI = o; o += al4(ROWS * (NI > 0 ? NI : 1));
-    L.rowM = o; o += ROWS * al4(G * 21);
+    L.fE = o; o += 2 * ROWS;
+    L.bE = o; o += 2 * ROWS;
     int bytes = o * 4;
     L.ys = bytes;
-    bytes += max_ly + 1;
+    bytes += max_ly + 4;
     L.bytes = (bytes + 15) & ~15;
     return L;
-}
-
-// w~ = e * b~ of one cell from the backward lattice (zero when the cell is
-// outside the pair or has no backward mass); returns the exponent
-template <class SH>
-__device__ __forceinline__ int load_w(const KParams &P, const float *sm, const SmemC &L, int64_t cell, bool ok,
-                                      const int (&offM)[SH::NM > 0 ? SH::NM : 1], const int *offI,
-                                      const float (&eD)[SH::ND > 0 ? SH::ND : 1], int yj, float (&w)[SH::NE],
-                                      float (&b)[SH::SP]) {
-    constexpr int NE = SH::NE, NM = SH::NM, NI = SH::NI, SP = SH::SP;
-    int E = EXP_NONE;
-    if (ok) E = __ldg(P.blat_exp + cell);
-    const bool live = ok && E > EXP_NONE;
-    if (live) {
-        const float4 *src = reinterpret_cast<const float4 *>(P.blat + cell * SP);
-#pragma unroll
-        for (int q = 0; q < SP / 4; ++q) {
-            const float4 v = __ldg(src + q);
-            b[4 * q] = v.x; b[4 * q + 1] = v.y; b[4 * q + 2] = v.z; b[4 * q + 3] = v.w;
-        }
-    } else {
-#pragma unroll
-        for (int s = 0; s < SP; ++s) b[s] = 0.f;
-    }
-#pragma unroll
-    for (int k = 0; k < NE; ++k) {
-        const int ty = SH::type_of(k);
-        float ev;
-        if (ty == T_M) ev = sm[offM[k] + yj];
-        else if (ty == T_I) ev = sm[offI[k - NM] + yj];
-        else ev = eD[k - NM - NI];
-        w[k] = live ? b[k] * ev : 0.f;
-    }
-    return live ? E : EXP_NONE;
 }
 
 template <class SH>
@@ -334,13 +307,36 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
     const int T_last = (nrows - 1) + Ly;
     const int t0 = ch * CCH;
     const int t_hi = min(T_last, t0 + CCH - 1);
+    const int t_top = min(T_last, t_hi + 2);   // two steps of successor history first
     const double llv = P.ll[p];
     if (!(llv > -1e29) || t0 > T_last) return;   // uniform over the warp
     const double lam = llv / LN2;
     const double Epd = floor(lam);
     const int Ep = (int)Epd;
     const float rfrac = (float)exp2(-(lam - Epd));
-
+    float *fbuf = sm + L.fbuf, *bbuf = sm + L.bbuf, *ust = sm + L.ust, *bins = sm + L.bins, *colI = sm + L.colI;
+    int *fEb = reinterpret_cast<int *>(sm) + L.fE;
+    int *bEb = reinterpret_cast<int *>(sm) + L.bE;
+    // the lattice rows of step t (all 64 rows; rows outside the pair hold stale
+    // data that is never used unguarded)
+    auto prefetch = [&](int t) {
+        if (t >= t0) {
+            const int buf = t & 1;
+            const float *srcF = P.lat + (latc + (int64_t)t * ROWS) * SP;
+            const float *srcB = P.blat + (latc + (int64_t)t * ROWS) * SP;
+            for (int idx = lane; idx < ROWS * SP / 4; idx += 32) {
+                const int r = idx / (SP / 4), q = idx % (SP / 4);
+                if (t <= t_hi) cp_async16(fbuf + buf * ROWS * SPP + r * SPP + 4 * q, srcF + 4 * idx);
+                cp_async16(bbuf + buf * ROWS * SPP + r * SPP + 4 * q, srcB + 4 * idx);
+            }
+            for (int idx = lane; idx < ROWS / 4; idx += 32) {
+                if (t <= t_hi) cp_async16(fEb + buf * ROWS + 4 * idx, P.lat_exp + latc + (int64_t)t * ROWS + 4 * idx);
+                cp_async16(bEb + buf * ROWS + 4 * idx, P.blat_exp + latc + (int64_t)t * ROWS + 4 * idx);
+            }
+        }
+        cp_commit();
+    };
+    prefetch(t_top);
     // ---- tables, y characters of the chunk's columns, zeroed bins
     {
         const float *eM = P.eM + (int64_t)p * P.eM_stride;
@@ -359,14 +355,10 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
             if (j >= 1) c = min((int)P.res[m.y_off + j - 1], 20);
             ysw[j] = (unsigned char)c;
         }
-        for (int idx = lane; idx < ROWS * (NI > 0 ? NI : 1); idx += 32) sm[L.colI + idx] = 0.f;
-        for (int idx = lane; idx < ROWS * al4(G * 21); idx += 32) sm[L.rowM + idx] = 0.f;
+        for (int idx = lane; idx < ROWS * (NI > 0 ? NI : 1); idx += 32) colI[idx] = 0.f;
         __syncwarp();
     }
     const unsigned char *ys = smb + L.ys;
-    float *fst = sm + L.fst, *ust = sm + L.ust, *bins = sm + L.bins, *colI = sm + L.colI;
-    float *rowM = sm + L.rowM;
-    const int GR = al4(G * 21);
 
     int rowi[R], xch[R];
     float eD[R][ND > 0 ? ND : 1];
@@ -393,6 +385,7 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
 #pragma unroll
         for (int k = 0; k < ND; ++k) eDb[k] = sm[L.tD + P.w_group[NM + NI + k] * 21 + xb];
     }
+    double *cntM_pair = P.cntM + (int64_t)p * G * 441;
 
     float dcnt[R][ND > 0 ? ND : 1], dcmp[R][ND > 0 ? ND : 1];
 #pragma unroll
@@ -413,9 +406,34 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
     int Ewn[R] = {EXP_NONE, EXP_NONE}, Ewnn1 = EXP_NONE, EdR = EXP_NONE;
 #pragma unroll
     for (int k = 0; k < NE; ++k) { wn[0][k] = 0.f; wn[1][k] = 0.f; wnn1[k] = 0.f; dR[k] = 0.f; }
+    // lane 31: b~ of row i0+64 at column (t - 63), loaded one step ahead
+    float bbv[SP];
+    int bbE = EXP_NONE;
+    auto load_below = [&](int t) {
+        const int jb = t - (ROWS - 1);
+        bbE = EXP_NONE;
+        if (lane == 31 && has_below && t >= t0 && jb >= 0 && jb <= Ly) {
+            const int64_t cell = latb + (int64_t)jb * ROWS;
+            bbE = __ldg(P.blat_exp + cell);
+            const float4 *src = reinterpret_cast<const float4 *>(P.blat + cell * SP);
+#pragma unroll
+            for (int q = 0; q < SP / 4; ++q) {
+                const float4 v = __ldg(src + q);
+                bbv[4 * q] = v.x; bbv[4 * q + 1] = v.y; bbv[4 * q + 2] = v.z; bbv[4 * q + 3] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int s = 0; s < SP; ++s) bbv[s] = 0.f;
+        }
+    };
+    load_below(t_top);
 
-    for (int t = min(T_last, t_hi + 2); t >= t0; --t) {
+    for (int t = t_top; t >= t0; --t) {
         const bool count = t <= t_hi;
+        const int buf = t & 1;
+        prefetch(t - 1);
+        cp_wait1();
+        __syncwarp();
         int jc[R];
         bool valid[R];
 #pragma unroll
@@ -423,14 +441,25 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
             jc[c] = t - (R * lane + c);
             valid[c] = (R * lane + c < nrows) && jc[c] >= 0 && jc[c] <= Ly;
         }
-        // ---- w~ and b~ of my two cells at step t
-        float wcur[R][NE], bcur[R][SP];
+        // ---- b~ and w~ = e b~ of my two cells at step t
+        float wcur[R][NE];
         int Eb[R];
 #pragma unroll
         for (int c = 0; c < R; ++c) {
             const int rho = R * lane + c;
-            Eb[c] = load_w<SH>(P, sm, L, latc + (int64_t)t * ROWS + rho, valid[c], offM[c], offI, eD[c],
-                               valid[c] ? ys[jc[c]] : 0, wcur[c], bcur[c]);
+            const int E = valid[c] ? bEb[buf * ROWS + rho] : EXP_NONE;
+            Eb[c] = E > EXP_NONE ? E : EXP_NONE;
+            const int yj = valid[c] ? ys[jc[c]] : 0;
+            const float *br = bbuf + buf * ROWS * SPP + rho * SPP;
+#pragma unroll
+            for (int k = 0; k < NE; ++k) {
+                const int ty = SH::type_of(k);
+                float ev;
+                if (ty == T_M) ev = sm[offM[c][k] + yj];
+                else if (ty == T_I) ev = sm[offI[k - NM] + yj];
+                else ev = eD[c][k - NM - NI];
+                wcur[c][k] = Eb[c] > EXP_NONE ? br[k] * ev : 0.f;
+            }
         }
         // D-successor of cell B (row 2L+2, column jc[1]): lane L+1's cell A at t+1,
         // or for lane 31 the first row of the stripe below at column jc[1]
@@ -439,11 +468,20 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
 #pragma unroll
         for (int k = 0; k < NE; ++k) dnew[k] = __shfl_down_sync(0xffffffffu, wn[0][k], 1);
         if (lane == 31) {
-            const bool okb = has_below && jc[1] >= 0 && jc[1] <= Ly;
-            float btmp[SP];
-            Ednew = load_w<SH>(P, sm, L, latb + (int64_t)jc[1] * ROWS, okb, offMb, offI, eDb, okb ? ys[jc[1]] : 0,
-                               dnew, btmp);
+            const bool okb = has_below && jc[1] >= 0 && jc[1] <= Ly && bbE > EXP_NONE;
+            const int yb = okb ? ys[jc[1]] : 0;
+#pragma unroll
+            for (int k = 0; k < NE; ++k) {
+                const int ty = SH::type_of(k);
+                float ev;
+                if (ty == T_M) ev = sm[offMb[k] + yb];
+                else if (ty == T_I) ev = sm[offI[k - NM] + yb];
+                else ev = eDb[k - NM - NI];
+                dnew[k] = okb ? bbv[k] * ev : 0.f;
+            }
+            Ednew = okb ? bbE : EXP_NONE;
         }
+        load_below(t - 1);
         if (count) {
             const bool term0 = valid[0] && rowi[0] == Lx && jc[0] == Ly;
             const bool term1 = valid[1] && rowi[1] == Lx && jc[1] == Ly;
@@ -458,34 +496,29 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
 #pragma unroll
             for (int c = 0; c < R; ++c) {
                 const int rho = R * lane + c;
-                const int64_t cell = latc + (int64_t)t * ROWS + rho;
-                int Ef = EXP_NONE;
-                if (valid[c]) Ef = __ldg(P.lat_exp + cell);
+                const int Ef = valid[c] ? fEb[buf * ROWS + rho] : EXP_NONE;
                 float fsc = 0.f;
                 if (valid[c] && Ef > EXP_NONE && Eb[c] > EXP_NONE) {
                     int d = Ef + Eb[c] - Ep;
                     if (d > 126) { d = 126; atomicOr(P.status + p, PHMM_ST_SCALE_CLAMP); }
                     fsc = scale_pow2(rfrac, max(d, -200));
                 }
-                float ft[SP];
-                if (fsc > 0.f) {
-                    const float4 *src = reinterpret_cast<const float4 *>(P.lat + cell * SP);
-#pragma unroll
-                    for (int q = 0; q < SP / 4; ++q) {
-                        const float4 v = __ldg(src + q);
-                        ft[4 * q] = v.x * fsc; ft[4 * q + 1] = v.y * fsc;
-                        ft[4 * q + 2] = v.z * fsc; ft[4 * q + 3] = v.w * fsc;
-                    }
-                } else {
-#pragma unroll
-                    for (int s = 0; s < SP; ++s) ft[s] = 0.f;
-                }
+                // f~ scaled in place (the outer products read it from the buffer)
+                float *fr = fbuf + buf * ROWS * SPP + rho * SPP;
+                const float *br = bbuf + buf * ROWS * SPP + rho * SPP;
+                float ft[NSRC];
 #pragma unroll
                 for (int q = 0; q < SP / 4; ++q) {
-                    float v[4];
+                    const float4 v = reinterpret_cast<const float4 *>(fr)[q];
+                    const float va[4] = {v.x, v.y, v.z, v.w};
+                    float o[4];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) v[u] = (4 * q + u < NSRC) ? ft[4 * q + u] : 0.f;
-                    reinterpret_cast<float4 *>(fst + rho * SPP)[q] = make_float4(v[0], v[1], v[2], v[3]);
+                    for (int u = 0; u < 4; ++u) {
+                        const int s = 4 * q + u;
+                        o[u] = (s < NSRC && fsc > 0.f) ? va[u] * fsc : 0.f;
+                        if (s < NSRC) ft[s] = o[u];
+                    }
+                    reinterpret_cast<float4 *>(fr)[q] = make_float4(o[0], o[1], o[2], o[3]);
                 }
                 // u~[k] = w~_succ(k)[k] * 2^(E_succ - Eb)
                 const int EM = c == 0 ? EM0 : EM1, EI = c == 0 ? EI0 : EI1, ED = c == 0 ? ED0 : ED1;
@@ -511,13 +544,12 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
                 }
                 if (live) {
                     const int yj = ys[jc[c]];
-                    float *rm = rowM + rho * GR;
 #pragma unroll
                     for (int k = 0; k < NE; ++k) {
-                        const float pk = ft[k] * bcur[c][k];
+                        const float pk = ft[k] * br[k];
                         const int ty = SH::type_of(k);
                         if (ty == T_M) {
-                            rm[P.w_group[k] * 21 + yj] += pk;
+                            if (pk != 0.f) atomicAdd(cntM_pair + P.w_group[k] * 441 + xch[c] * 21 + yj, (double)pk);
                         } else if (ty == T_I) {
                             colI[(jc[c] % ROWS) * NI + (k - NM)] += pk;
                         } else {
@@ -532,7 +564,7 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
 #pragma unroll
                         for (int s = 0; s < NSRC; ++s)
                             atomicAdd(P.n_trans + ((int64_t)p * N + P.w_orig[s]) * N + P.e_idx,
-                                      (double)(ft[s] * bcur[c][s]));
+                                      (double)(ft[s] * br[s]));
                     }
                 }
             }
@@ -551,9 +583,10 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
                 float pz[16];
 #pragma unroll
                 for (int u = 0; u < 16; ++u) pz[u] = 0.f;
+                const float *fb = fbuf + buf * ROWS * SPP;
                 const int r0 = grp * ROWS / SH::GROUPS, r1 = (grp + 1) * ROWS / SH::GROUPS;
                 for (int rr = r0; rr < r1; ++rr) {
-                    const float4 fv = reinterpret_cast<const float4 *>(fst + rr * SPP)[bs];
+                    const float4 fv = reinterpret_cast<const float4 *>(fb + rr * SPP)[bs];
                     const float4 uv = reinterpret_cast<const float4 *>(ust + rr * KPP)[bk];
                     const float fa[4] = {fv.x, fv.y, fv.z, fv.w};
                     const float ua[4] = {uv.x, uv.y, uv.z, uv.w};
@@ -570,8 +603,8 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
                     csum[u] = tt;
                 }
             }
-            __syncwarp();
         }
+        __syncwarp();   // the buffers of step t are free for the prefetch of step t-2
         // ---- shift histories
 #pragma unroll
         for (int k = 0; k < NE; ++k) {
@@ -585,6 +618,7 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
         Ewn[0] = Eb[0];
         Ewn[1] = Eb[1];
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     // ---- flush the chunk's partial counts (float64 reductions)
     __syncwarp();
     if (counter) {
@@ -606,11 +640,6 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
         for (int k = 0; k < ND; ++k) {
             const float v = dcnt[c][k] - dcmp[c][k];
             if (v != 0.f) atomicAdd(P.cntD + ((int64_t)p * G + P.w_group[NM + NI + k]) * 21 + xch[c], (double)v);
-        }
-        const float *rm = rowM + rho * GR;
-        for (int idx = 0; idx < G * 21; ++idx) {
-            const float v = rm[idx];
-            if (v != 0.f) atomicAdd(P.cntM + ((int64_t)p * G + idx / 21) * 441 + xch[c] * 21 + idx % 21, (double)v);
         }
     }
     // I-type columns not completed inside the chunk (touched by rows below row 0)

@@ -1,0 +1,621 @@
+// estep_wide.cuh -- E-step kernels for large state spaces (more than 64
+// padded slots, up to WMAXS: MixDom2 with K*F up to 33, e.g. n_dom=8,
+// n_frag=4 -> 162 states).  Included by pairhmm.cu.
+//
+// At this size one cell is a 4NQ x NS contraction (about 26 k multiply-adds
+// at 162 states), so a stripe step is a small GEMM: out[row][k] =
+// sum_s pred_type(k)[row][s] chi[s][k].  A CTA sweeps a stripe of RW = 32
+// rows along anti-diagonals; thread (row group rg, destination quad q) owns
+// the 4 x 4 output tile rows 4rg..4rg+3 x states 4q..4q+3 and loops over the
+// NS sources with two float4 loads (four rows of the predecessor, four
+// transition entries) per 16 FMAs.  Lane layout: lane = 8 * (quad within the
+// warp) + rg, so a warp's predecessor loads hit 8 consecutive float4s and its
+// transition loads 4 consecutive float4s (one wavefront each).
+//
+// Predecessor rings in shared memory, source-major so rows are contiguous:
+//   A[2][NS][RW]      row r at index r       (I-type predecessor: same row);
+//   B[3][NS][RW + 4]  row r at index r + 1   (D / M predecessors: row r-1),
+//                     index 0 = the halo row of the stripe above.
+// Scaling: one power-of-two exponent per cell plus the cell's maximum value
+// (E[4][RW+4], MX[4][RW+4], atomicMax on the float bits).  A cell's output
+// takes exponent E_out = max over its predecessors of (E_pred +
+// exponent(max_pred)), so stored values stay below ~NS and no cross-thread
+// renormalisation is needed: one __syncthreads per step.
+//
+// The backward recursion (bwd_rec) is the transpose: out[row][s] = sum_k
+// chi[s][k] w_succ(type k)[row][k], with successor rings of w = e b over the
+// 4NQ destination slots (A: row r at index r, B: row r at index r + 3, halo
+// row RW at index RW + 3).  Both write full lattices (values + exponent +
+// maximum per cell) for the count pass.
+
+namespace wide {
+
+constexpr int RW = 32;           // rows per stripe
+constexpr int WMAXS = 168;       // largest padded slot count
+constexpr int WPUB = 4;          // edge progress published every WPUB columns
+
+__host__ __device__ inline int ls_of(int NS) { return NS + 4; }   // lattice / edge record (floats)
+
+struct SmemWd {
+    int chi, chiE, A, B, E, MX, llp, misc;   // float / int offsets (llp: double index)
+    int ys;                                   // byte offset
+    int bytes;
+};
+
+// KS: destination slots (4 x destination quads); NSRC: sources of the ring
+__host__ __device__ inline SmemWd make_smem_wd(int NS, int KS, int max_ly, bool bwd) {
+    SmemWd L;
+    const int NSRC = bwd ? KS : NS;          // ring vectors: forward sources / backward w of dests
+    int o = 0;
+    L.chi = o; o += bwd ? KS * KS : NS * KS;  // forward chi[s][k]; backward chiB[k][s] (s < KS)
+    L.chiE = o; o += (NS + 3) & ~3;
+    L.A = o; o += 2 * NSRC * RW;
+    L.B = o; o += 3 * NSRC * (RW + 4);
+    L.E = o; o += 4 * (RW + 4);
+    L.MX = o; o += 4 * (RW + 4);
+    o = (o + 1) & ~1;
+    L.llp = o / 2; o += 2 * (KS / 4 + 4);
+    L.misc = o; o += 8;
+    int bytes = o * 4;
+    L.ys = bytes;
+    bytes += max_ly + 2;
+    L.bytes = (bytes + 15) & ~15;
+    return L;
+}
+
+__device__ __forceinline__ int exp_of_max(int mbits) {   // exponent of a positive float given as bits
+    return warp2::exp_of(__int_as_float(mbits));
+}
+
+__device__ __forceinline__ float pow2d(int d) {   // 2^d for any d (0 far below the float range)
+    if (d >= -126 && d <= 127) return pow2f(d);
+    return d < -149 ? 0.f : ldexpf(1.f, d);
+}
+
+// emission factor of destination slot k at characters (x, y) from the global tables
+__device__ __forceinline__ float emit_g(const KParams &P, const float *eM, const float *eI, const float *eD, int k,
+                                        int x, int y) {
+    const int kt = P.slot_type[k];
+    const int g = P.slot_group[k];
+    if (kt == T_M) return __ldg(eM + g * 441 + x * 21 + y);
+    if (kt == T_I) return __ldg(eI + g * 21 + y);
+    if (kt == T_D) return __ldg(eD + g * 21 + x);
+    return 0.f;
+}
+
+// ---------------------------------------------------------------- forward
+__device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, float *sm, unsigned char *smb) {
+    const int NS = P.NS, KS = P.kend[2], NQd = KS / 4, N = P.N;
+    const PairMeta m = P.meta[p];
+    const int Lx = m.Lx, Ly = m.Ly;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    const int rg = lane & 7, qd = 4 * warp + (lane >> 3);
+    const bool active = qd < NQd;
+    const int r0 = 4 * rg;
+    const int i0 = si * RW;
+    const int nrows = min(RW, Lx + 1 - i0);
+    const bool has_above = si > 0, has_below = si + 1 < m.n_stripes;
+    const int ES = ls_of(NS);
+    const int *prog_above = has_above ? P.progress + m.stripe_base + si - 1 : nullptr;
+    int *prog_mine = P.progress + m.stripe_base + si;
+    const float *edge_above = P.edge + (m.edge_base + (int64_t)(si - 1) * (Ly + 1)) * ES;
+    float *edge_mine = P.edge + (m.edge_base + (int64_t)si * (Ly + 1)) * ES;
+    const int64_t latc = m.lat_base + (int64_t)si * (RW + Ly) * RW;
+    float *chiS = sm + L.chi, *A = sm + L.A, *B = sm + L.B;
+    int *E = reinterpret_cast<int *>(sm) + L.E;
+    int *MX = reinterpret_cast<int *>(sm) + L.MX;
+    int *misc = reinterpret_cast<int *>(sm) + L.misc;
+    double *llp = reinterpret_cast<double *>(sm) + L.llp;
+    unsigned char *ys = smb + L.ys;
+    const int BW = RW + 4;
+    // ---- model, rings, residues
+    {
+        const float *chi = P.chi + (int64_t)p * P.chi_stride;
+        for (int idx = tid; idx < NS * KS; idx += nt) {
+            const int s = idx / KS, k = idx % KS;
+            const int os = P.slot_orig[s], ok = P.slot_orig[k];
+            const int kt = P.slot_type[k];
+            float v = 0.f;
+            if (os >= 0 && ok >= 0 && (kt == T_M || kt == T_I || kt == T_D)) v = __ldg(chi + os * N + ok);
+            chiS[idx] = v;
+        }
+        for (int s = tid; s < NS; s += nt) {
+            const int os = P.slot_orig[s];
+            sm[L.chiE + s] = os >= 0 ? __ldg(chi + os * N + P.e_idx) : 0.f;
+        }
+        for (int idx = tid; idx < 2 * NS * RW; idx += nt) A[idx] = 0.f;
+        for (int idx = tid; idx < 3 * NS * BW; idx += nt) B[idx] = 0.f;
+        for (int idx = tid; idx < 4 * BW; idx += nt) { E[idx] = EXP_NONE; MX[idx] = 0; }
+        for (int j = tid; j <= Ly; j += nt) {
+            int c = 0;
+            if (j >= 1) {
+                c = P.res[m.y_off + j - 1];
+                if (c > 20) { c = 20; atomicOr(P.status + p, PHMM_ST_BAD_RESIDUE); }
+            }
+            ys[j] = (unsigned char)c;
+        }
+        if (tid == 0) { misc[0] = 0; misc[1] = 0; }
+    }
+    const float *eMg = P.eM + (int64_t)p * P.eM_stride;
+    const float *eIg = P.eI + (int64_t)p * P.eID_stride;
+    const float *eDg = P.eD + (int64_t)p * P.eID_stride;
+    int xr[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int row = i0 + r0 + i;
+        xr[i] = (row >= 1 && row <= Lx) ? min((int)P.res[m.x_off + row - 1], 20) : 0;
+    }
+    const int qt = active ? P.quad_type[qd] : T_NONE;
+    const int T_last = (nrows - 1) + Ly;
+    // halo column t of row i0-1 goes to B[(t-1) % 3][s][0] (row -1 at step t-1);
+    // warp 0 fetches column t+1 during step t, column 0 before the loop
+    // (B slot (col - 1) % 3, exponent / maximum slot (col - 1) & 3)
+    auto fetch_halo = [&](int col) -> bool {
+        if (!has_above || col > Ly) return true;
+        int ok = 1;
+        if (lane == 0) ok = wait_geq(prog_above, col + 1, P.spin_limit) ? 1 : 0;
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) return false;
+        const int bs = (col + 2) % 3, es = (col + 3) & 3;
+        const float *src = edge_above + (int64_t)col * ES;
+        for (int s = lane; s < NS; s += 32) B[(bs * NS + s) * BW] = __ldcg(src + s);
+        if (lane == 0) {
+            E[es * BW] = __ldcg(reinterpret_cast<const int *>(src) + NS);
+            MX[es * BW] = __ldcg(reinterpret_cast<const int *>(src) + NS + 1);
+        }
+        return true;
+    };
+    __syncthreads();
+    if (warp == 0 && !fetch_halo(0)) misc[0] = 1;
+    double llv = 0.0;
+    int llE = EXP_NONE;
+    bool aborted = false;
+    int k = 0;
+    for (int t = 0; t <= T_last; ++t, ++k) {
+        __syncthreads();
+        if (misc[k & 1]) { aborted = true; break; }
+        if (tid == 0) misc[(k + 1) & 1] = 0;
+        // maxima of step t+1 start at zero (slot last read at step t-1)
+        for (int r = tid; r < RW; r += nt) MX[((t + 1) & 3) * BW + r + 1] = 0;
+        // the origin's start-state entries live two (A) / three (B) steps
+        if (si == 0 && tid == 0) {
+            if (t == 2) A[(0 * NS + P.s_slot) * RW + 0] = 0.f;
+            if (t == 3) B[(0 * NS + P.s_slot) * BW + 1] = 0.f;
+        }
+        // ---- bottom row of step t-1 -> edge row for the stripe below (warp 1)
+        if (warp == (nt > 32 ? 1 : 0) && has_below && t >= 1) {
+            const int jb = t - 1 - (RW - 1);
+            if (jb >= 0 && jb <= Ly) {
+                const int sl = (t - 1) % 3;
+                float *dst = edge_mine + (int64_t)jb * ES;
+                for (int s = lane; s < NS; s += 32) dst[s] = B[(sl * NS + s) * BW + RW];
+                if (lane == 0) {
+                    reinterpret_cast<int *>(dst)[NS] = E[((t - 1) & 3) * BW + RW];
+                    reinterpret_cast<int *>(dst)[NS + 1] = MX[((t - 1) & 3) * BW + RW];
+                }
+                __threadfence();
+                __syncwarp();
+                if (lane == 0 && (((jb + 1) % WPUB) == 0 || jb == Ly)) st_release(prog_mine, jb + 1);
+            }
+        }
+        // ---- compute my 4 x 4 tile
+        if (active) {
+            int Eo[4];
+            float sc[4];
+            bool valid[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = r0 + i, row = i0 + r, j = t - r;
+                valid[i] = r < nrows && j >= 0 && j <= Ly;
+                int EI = EXP_NONE, ED = EXP_NONE, EM = EXP_NONE;
+                if (valid[i]) {
+                    if (j >= 1) {
+                        const int mb = MX[((t - 1) & 3) * BW + r + 1];
+                        const int e = E[((t - 1) & 3) * BW + r + 1];
+                        if (mb > 0 && e > EXP_NONE) EI = e + exp_of_max(mb);
+                    }
+                    if (row >= 1) {
+                        const int mb = MX[((t - 1) & 3) * BW + r];
+                        const int e = E[((t - 1) & 3) * BW + r];
+                        if (mb > 0 && e > EXP_NONE) ED = e + exp_of_max(mb);
+                    }
+                    if (row >= 1 && j >= 1) {
+                        const int mb = MX[((t - 2) & 3) * BW + r];
+                        const int e = E[((t - 2) & 3) * BW + r];
+                        if (mb > 0 && e > EXP_NONE) EM = e + exp_of_max(mb);
+                    }
+                }
+                const int Eout = max(max(EI, ED), EM);
+                Eo[i] = Eout;
+                int Emine = qt == T_I ? EI : (qt == T_D ? ED : EM);
+                const int Eraw = qt == T_I ? E[((t - 1) & 3) * BW + r + 1]
+                                           : (qt == T_D ? E[((t - 1) & 3) * BW + r] : E[((t - 2) & 3) * BW + r]);
+                sc[i] = (Emine > EXP_NONE && Eout > EXP_NONE) ? pow2d(Eraw - Eout) : 0.f;
+            }
+            const float *base = qt == T_I ? A + ((t - 1) & 1) * NS * RW + r0
+                                          : (qt == T_D ? B + ((t + 2) % 3) * NS * BW + r0 : B + ((t + 1) % 3) * NS * BW + r0);
+            const int stride = qt == T_I ? RW : BW;
+            float acc[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) acc[i][u] = 0.f;
+            const float4 *ch4 = reinterpret_cast<const float4 *>(chiS) + qd;
+#pragma unroll 4
+            for (int s = 0; s < NS; ++s) {
+                const float4 pv = *reinterpret_cast<const float4 *>(base + s * stride);
+                const float4 cv = ch4[s * NQd];
+                const float pa[4] = {pv.x, pv.y, pv.z, pv.w};
+                const float ca[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) acc[i][u] = fmaf(pa[i], ca[u], acc[i][u]);
+            }
+            // emissions, scale, outputs
+            float mxr[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = r0 + i, j = t - r;
+                const int yj = valid[i] ? ys[j] : 0;
+                mxr[i] = 0.f;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    float v = 0.f;
+                    if (valid[i] && sc[i] > 0.f) v = acc[i][u] * sc[i] * emit_g(P, eMg, eIg, eDg, 4 * qd + u, xr[i], yj);
+                    acc[i][u] = v;
+                    mxr[i] = fmaxf(mxr[i], v);
+                }
+            }
+            const int sa = t & 1, sb = t % 3;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int s = 4 * qd + u;
+                *reinterpret_cast<float4 *>(A + (sa * NS + s) * RW + r0) =
+                    make_float4(acc[0][u], acc[1][u], acc[2][u], acc[3][u]);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) B[(sb * NS + s) * BW + r0 + i + 1] = acc[i][u];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = r0 + i, row = i0 + r, j = t - r;
+                const bool origin = valid[i] && row == 0 && j == 0;
+                if (qd == 0) E[(t & 3) * BW + r + 1] = origin ? 0 : Eo[i];
+                if (mxr[i] > 0.f) atomicMax(MX + (t & 3) * BW + r + 1, __float_as_int(mxr[i]));
+                if (valid[i] && P.lat) {
+                    const int64_t cell = latc + (int64_t)t * RW + r;
+                    float *rec = P.lat + cell * ES;
+                    *reinterpret_cast<float4 *>(rec + 4 * qd) = make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+                    if (qd == 0) {
+                        for (int s2 = KS; s2 < NS; ++s2) rec[s2] = (origin && s2 == P.s_slot) ? 1.f : 0.f;
+                        reinterpret_cast<int *>(rec)[NS] = origin ? 0 : Eo[i];
+                    }
+                }
+                if (valid[i] && row == Lx && j == Ly && si + 1 == m.n_stripes) {   // P(x,y): my quad's share
+                    double a = 0.0;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) a += (double)acc[i][u] * (double)sm[L.chiE + 4 * qd + u];
+                    llp[qd] = a;
+                    if (qd == 0) llE = origin ? 0 : Eo[i];
+                }
+            }
+            if (si == 0 && t == 0 && qd == 0 && rg == 0) {   // origin: F[0,0,start] = 1
+                A[(0 * NS + P.s_slot) * RW + 0] = 1.f;
+                B[(0 * NS + P.s_slot) * BW + 1] = 1.f;
+                atomicMax(MX + 0 * BW + 1, __float_as_int(1.f));
+            }
+        }
+        // ---- halo column t+1 for the next step (warp 0)
+        if (warp == 0 && t + 1 <= T_last && !fetch_halo(t + 1)) misc[(k + 1) & 1] = 1;
+    }
+    __syncthreads();
+    if (!aborted && has_below) {   // the last bottom-row cell(s) still to publish
+        const int t = T_last + 1;
+        const int jb = t - 1 - (RW - 1);
+        if (warp == (nt > 32 ? 1 : 0) && jb >= 0 && jb <= Ly) {
+            const int sl = (t - 1) % 3;
+            float *dst = edge_mine + (int64_t)jb * ES;
+            for (int s = lane; s < NS; s += 32) dst[s] = B[(sl * NS + s) * BW + RW];
+            if (lane == 0) {
+                reinterpret_cast<int *>(dst)[NS] = E[((t - 1) & 3) * BW + RW];
+                reinterpret_cast<int *>(dst)[NS + 1] = MX[((t - 1) & 3) * BW + RW];
+            }
+            __threadfence();
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        if (has_below) { __threadfence(); st_release(prog_mine, Ly + 1); }
+        if (aborted) {
+            atomicOr(P.status + p, PHMM_ST_TIMEOUT);
+            if (si + 1 == m.n_stripes) P.ll[p] = NEG_INF_LL;
+        }
+    }
+    // the terminal cell's exponent was kept by the qd == 0 thread of its row group
+    if (!aborted && si + 1 == m.n_stripes) {
+        int *Eterm = misc + 4;
+        const int rT = Lx - i0;
+        if (active && qd == 0 && rg == (rT >> 2)) *Eterm = llE;
+        __syncthreads();
+        if (tid == 0) {
+            double acc = 0.0;
+            for (int q = 0; q < NQd; ++q) acc += llp[q];
+            if (Lx == 0 && Ly == 0) acc += (double)sm[L.chiE + P.s_slot];   // the origin is the terminal
+            const int Et = *Eterm;
+            double ll = NEG_INF_LL;
+            if (acc > 0.0 && isfinite(acc) && Et > EXP_NONE) ll = log(acc) + (double)Et * LN2;
+            else atomicOr(P.status + p, PHMM_ST_ZERO_LL);
+            P.ll[p] = ll;
+        }
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------- backward recursion
+// b[row][s] = sum_k chi[s][k] w_succ(type k)[row][k] for the destination
+// slots s < KS (the count pass needs b only there); w = e b is what the
+// successor rings and the edge rows carry.  Edge records of the stripe
+// below are its top row, and progress counts published columns from the
+// right (Ly + 1 - column).
+__device__ void bwd_rec_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, float *sm, unsigned char *smb) {
+    const int NS = P.NS, KS = P.kend[2], NQd = KS / 4, N = P.N;
+    const PairMeta m = P.meta[p];
+    const int Lx = m.Lx, Ly = m.Ly;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    const int rg = lane & 7, qs = 4 * warp + (lane >> 3);   // output (source) quad
+    const bool active = qs < NQd;
+    const int r0 = 4 * rg;
+    const int i0 = si * RW;
+    const int nrows = min(RW, Lx + 1 - i0);
+    const bool has_above = si > 0, has_below = si + 1 < m.n_stripes;
+    const int ES = ls_of(NS);
+    const int *prog_below = has_below ? P.bprogress + m.stripe_base + si + 1 : nullptr;
+    int *prog_mine = P.bprogress + m.stripe_base + si;
+    const float *edge_below = P.bedge + (m.edge_base + (int64_t)(si + 1) * (Ly + 1)) * ES;
+    float *edge_mine = P.bedge + (m.edge_base + (int64_t)si * (Ly + 1)) * ES;
+    const int64_t latc = m.lat_base + (int64_t)si * (RW + Ly) * RW;
+    float *chiB = sm + L.chi, *A = sm + L.A, *B = sm + L.B;
+    int *E = reinterpret_cast<int *>(sm) + L.E;
+    int *MX = reinterpret_cast<int *>(sm) + L.MX;
+    int *misc = reinterpret_cast<int *>(sm) + L.misc;
+    unsigned char *ys = smb + L.ys;
+    const int BW = RW + 4;
+    {
+        const float *chi = P.chi + (int64_t)p * P.chi_stride;
+        for (int idx = tid; idx < KS * KS; idx += nt) {   // chiB[k][s]
+            const int k = idx / KS, s = idx % KS;
+            const int os = P.slot_orig[s], ok = P.slot_orig[k];
+            const int kt = P.slot_type[k];
+            float v = 0.f;
+            if (os >= 0 && ok >= 0 && (kt == T_M || kt == T_I || kt == T_D)) v = __ldg(chi + os * N + ok);
+            chiB[idx] = v;
+        }
+        for (int s = tid; s < NS; s += nt) {
+            const int os = P.slot_orig[s];
+            sm[L.chiE + s] = os >= 0 ? __ldg(chi + os * N + P.e_idx) : 0.f;
+        }
+        for (int idx = tid; idx < 2 * KS * RW; idx += nt) A[idx] = 0.f;
+        for (int idx = tid; idx < 3 * KS * BW; idx += nt) B[idx] = 0.f;
+        for (int idx = tid; idx < 4 * BW; idx += nt) { E[idx] = EXP_NONE; MX[idx] = 0; }
+        for (int j = tid; j <= Ly; j += nt) {
+            int c = 0;
+            if (j >= 1) c = min((int)P.res[m.y_off + j - 1], 20);
+            ys[j] = (unsigned char)c;
+        }
+        if (tid == 0) { misc[0] = 0; misc[1] = 0; }
+    }
+    const float *eMg = P.eM + (int64_t)p * P.eM_stride;
+    const float *eIg = P.eI + (int64_t)p * P.eID_stride;
+    const float *eDg = P.eD + (int64_t)p * P.eID_stride;
+    int xr[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int row = i0 + r0 + i;
+        xr[i] = (row >= 1 && row <= Lx) ? min((int)P.res[m.x_off + row - 1], 20) : 0;
+    }
+    const int kb0 = P.kbeg[0], ke0 = P.kend[0], kb1 = P.kbeg[1], ke1 = P.kend[1], kb2 = P.kbeg[2], ke2 = P.kend[2];
+    const int T_last = (nrows - 1) + Ly;
+    // halo: row i0+RW (the stripe below's top row) at column c sits at step c + RW:
+    // B slot (c + RW) % 3, index RW + 3; exponent / maximum slot (c + RW) & 3, index RW
+    auto fetch_halo = [&](int col) -> bool {
+        if (!has_below || col < 0 || col > Ly) return true;
+        int ok = 1;
+        if (lane == 0) ok = wait_geq(prog_below, Ly + 1 - col, P.spin_limit) ? 1 : 0;
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) return false;
+        const int bs = (col + RW) % 3, es = (col + RW) & 3;
+        const float *src = edge_below + (int64_t)col * ES;
+        for (int k = lane; k < KS; k += 32) B[(bs * KS + k) * BW + RW + 3] = __ldcg(src + k);
+        if (lane == 0) {
+            E[es * BW + RW] = __ldcg(reinterpret_cast<const int *>(src) + NS);
+            MX[es * BW + RW] = __ldcg(reinterpret_cast<const int *>(src) + NS + 1);
+        }
+        return true;
+    };
+    // top row of step t (column t) -> edge row for the stripe above
+    auto publish_top = [&](int t) {
+        if (!has_above || t < 0 || t > Ly) return;
+        float *dst = edge_mine + (int64_t)t * ES;
+        for (int k = lane; k < KS; k += 32) dst[k] = A[((t & 1) * KS + k) * RW + 0];
+        if (lane == 0) {
+            reinterpret_cast<int *>(dst)[NS] = E[(t & 3) * BW + 0];
+            reinterpret_cast<int *>(dst)[NS + 1] = MX[(t & 3) * BW + 0];
+        }
+        __threadfence();
+        __syncwarp();
+        if (lane == 0 && ((t % WPUB) == 0)) st_release(prog_mine, Ly + 1 - t);
+    };
+    __syncthreads();
+    if (warp == 0 && !fetch_halo(T_last - (RW - 1))) misc[0] = 1;
+    bool aborted = false;
+    int k = 0;
+    for (int t = T_last; t >= 0; --t, ++k) {
+        __syncthreads();
+        if (misc[k & 1]) { aborted = true; break; }
+        if (tid == 0) misc[(k + 1) & 1] = 0;
+        for (int r = tid; r < RW; r += nt) MX[((t - 1) & 3) * BW + r] = 0;   // maxima of step t-1
+        if (warp == (nt > 32 ? 1 : 0)) publish_top(t + 1);
+        if (active) {
+            // per row: successor exponent of each type and the output exponent
+            int Eo[4], EsM[4], EsI[4], EsD[4];
+            bool valid[4], term[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = r0 + i, row = i0 + r, j = t - r;
+                valid[i] = r < nrows && j >= 0 && j <= Ly;
+                term[i] = valid[i] && row == Lx && j == Ly;
+                int vI = EXP_NONE, vD = EXP_NONE, vM = EXP_NONE;
+                EsI[i] = EsD[i] = EsM[i] = EXP_NONE;
+                if (valid[i] && !term[i]) {
+                    if (j + 1 <= Ly) {
+                        const int mb = MX[((t + 1) & 3) * BW + r], e = E[((t + 1) & 3) * BW + r];
+                        if (mb > 0 && e > EXP_NONE) { EsI[i] = e; vI = e + exp_of_max(mb); }
+                    }
+                    if (row + 1 <= Lx) {
+                        const int mb = MX[((t + 1) & 3) * BW + r + 1], e = E[((t + 1) & 3) * BW + r + 1];
+                        if (mb > 0 && e > EXP_NONE) { EsD[i] = e; vD = e + exp_of_max(mb); }
+                    }
+                    if (row + 1 <= Lx && j + 1 <= Ly) {
+                        const int mb = MX[((t + 2) & 3) * BW + r + 1], e = E[((t + 2) & 3) * BW + r + 1];
+                        if (mb > 0 && e > EXP_NONE) { EsM[i] = e; vM = e + exp_of_max(mb); }
+                    }
+                }
+                Eo[i] = term[i] ? 0 : max(max(vI, vD), vM);
+            }
+            float aM[4][4], aI[4][4], aD[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) { aM[i][u] = 0.f; aI[i][u] = 0.f; aD[i][u] = 0.f; }
+            const float4 *cb4 = reinterpret_cast<const float4 *>(chiB) + qs;   // chiB[k][4qs..]
+            const int NQk = KS / 4;
+            {   // M destinations: successor (row+1, t+2)
+                const float *base = B + ((t + 2) % 3) * KS * BW + r0 + 4;
+#pragma unroll 2
+                for (int kk = kb0; kk < ke0; ++kk) {
+                    const float4 w = *reinterpret_cast<const float4 *>(base + kk * BW);
+                    const float4 c = cb4[kk * NQk];
+                    const float wa[4] = {w.x, w.y, w.z, w.w}, ca[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) aM[i][u] = fmaf(wa[i], ca[u], aM[i][u]);
+                }
+            }
+            {   // I destinations: successor (row, t+1)
+                const float *base = A + ((t + 1) & 1) * KS * RW + r0;
+#pragma unroll 2
+                for (int kk = kb1; kk < ke1; ++kk) {
+                    const float4 w = *reinterpret_cast<const float4 *>(base + kk * RW);
+                    const float4 c = cb4[kk * NQk];
+                    const float wa[4] = {w.x, w.y, w.z, w.w}, ca[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) aI[i][u] = fmaf(wa[i], ca[u], aI[i][u]);
+                }
+            }
+            {   // D destinations: successor (row+1, t+1)
+                const float *base = B + ((t + 1) % 3) * KS * BW + r0 + 4;
+#pragma unroll 2
+                for (int kk = kb2; kk < ke2; ++kk) {
+                    const float4 w = *reinterpret_cast<const float4 *>(base + kk * BW);
+                    const float4 c = cb4[kk * NQk];
+                    const float wa[4] = {w.x, w.y, w.z, w.w}, ca[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) aD[i][u] = fmaf(wa[i], ca[u], aD[i][u]);
+                }
+            }
+            float bv[4][4], mxr[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float sM = (EsM[i] > EXP_NONE) ? pow2d(EsM[i] - Eo[i]) : 0.f;
+                const float sI = (EsI[i] > EXP_NONE) ? pow2d(EsI[i] - Eo[i]) : 0.f;
+                const float sD = (EsD[i] > EXP_NONE) ? pow2d(EsD[i] - Eo[i]) : 0.f;
+                const int r = r0 + i, j = t - r;
+                const int yj = valid[i] ? ys[j] : 0;
+                mxr[i] = 0.f;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    float b = 0.f;
+                    if (valid[i]) {
+                        b = term[i] ? sm[L.chiE + 4 * qs + u] : aM[i][u] * sM + aI[i][u] * sI + aD[i][u] * sD;
+                        mxr[i] = fmaxf(mxr[i], b * emit_g(P, eMg, eIg, eDg, 4 * qs + u, xr[i], yj));
+                    }
+                    bv[i][u] = b;
+                }
+            }
+            // w = e b into the rings; b and its exponent into the lattice
+            const int sa = t & 1, sb = t % 3;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = r0 + i, j = t - r;
+                const int yj = valid[i] ? ys[j] : 0;
+                float wv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    wv[u] = valid[i] ? bv[i][u] * emit_g(P, eMg, eIg, eDg, 4 * qs + u, xr[i], yj) : 0.f;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    A[(sa * KS + 4 * qs + u) * RW + r] = wv[u];
+                    B[(sb * KS + 4 * qs + u) * BW + r + 3] = wv[u];
+                }
+                if (qs == 0) E[(t & 3) * BW + r] = valid[i] ? Eo[i] : EXP_NONE;
+                if (mxr[i] > 0.f) atomicMax(MX + (t & 3) * BW + r, __float_as_int(mxr[i]));
+                if (valid[i] && P.blat) {
+                    const int64_t cell = latc + (int64_t)t * RW + r;
+                    float *rec = P.blat + cell * ES;
+                    *reinterpret_cast<float4 *>(rec + 4 * qs) = make_float4(bv[i][0], bv[i][1], bv[i][2], bv[i][3]);
+                    if (qs == 0) reinterpret_cast<int *>(rec)[NS] = Eo[i];
+                }
+            }
+        }
+        if (warp == 0 && !fetch_halo(t - RW)) misc[(k + 1) & 1] = 1;
+    }
+    __syncthreads();
+    if (!aborted && warp == (nt > 32 ? 1 : 0)) publish_top(0);
+    __syncthreads();
+    if (tid == 0) {
+        if (has_above) { __threadfence(); st_release(prog_mine, Ly + 1); }
+        if (aborted) atomicOr(P.status + p, PHMM_ST_TIMEOUT);
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) fwdbwd_wide_kernel(const KParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_item;
+    float *sm = reinterpret_cast<float *>(smem_raw);
+    const SmemWd Lf = make_smem_wd(P.NS, P.kend[2], P.max_ly, false);
+    const SmemWd Lb = make_smem_wd(P.NS, P.kend[2], P.max_ly, true);
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(P.counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= P.n_items) break;
+        const int2 w = P.items[it];
+        if (w.y & blk::BWD_ITEM) bwd_rec_stripe_wd(P, w.x, w.y & ~blk::BWD_ITEM, Lb, sm, smem_raw);
+        else fwd_stripe_wd(P, w.x, w.y, Lf, sm, smem_raw);
+    }
+}
+
+__global__ void __launch_bounds__(1024) forward_wide_kernel(const KParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_item;
+    float *sm = reinterpret_cast<float *>(smem_raw);
+    const SmemWd L = make_smem_wd(P.NS, P.kend[2], P.max_ly, false);
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(P.counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= P.n_items) break;
+        const int2 w = P.items[it];
+        fwd_stripe_wd(P, w.x, w.y, L, sm, smem_raw);
+    }
+}
+
+}  // namespace wide

@@ -85,6 +85,9 @@ struct KParams {
     int *lat_exp;
     float *blat;                        // split E-step: backward lattice
     int *blat_exp;
+    int *bprogress;                     // split block E-step: backward edge pipeline
+    float *bedge;
+    int *bedge_exp;
     float *edge;
     int *edge_exp;
     int *progress;
@@ -876,6 +879,7 @@ struct phmm_plan {
     bool timed_count = false;
     // register-resident warp kernels for this state space (null: generic kernels)
     int w_nm = 0, w_ni = 0, w_nd = 0;
+    int grid_div = 1;       // persistent grids use 1/grid_div of the resident slots
     int variant = 0;        // 0 automatic, 1 generic, 2 warp, 3 block, 4 split warp E-step, 5 split block E-step
     int last_variant = 0;
 };
@@ -894,7 +898,8 @@ int ensure(T **ptr, size_t *cap, size_t n) {
 }
 
 // ---- launchers of the register-resident warp kernels, one per state-space shape
-// kind: 0 forward, 1 fused backward + counts, 2 backward recursion (split), 3 counts (split)
+// kind: 0 forward, 1 fused backward + counts, 2 backward recursion (split), 3 counts (split);
+// the block launchers take 4 for the combined forward + backward-recursion kernel
 using WarpLauncher = int (*)(phmm_plan *, KParams &, int, int, int, cudaStream_t);
 
 template <class SH>
@@ -947,9 +952,39 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // The split E-step: forward on the caller's stream and backward recursion on
 // a side stream at the same time, then the count pass once both are done.
-int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, int n_items, int n_citems, int stripes, int max_ly,
-                 void *d_items, int *d_counters, int *d_progress, float *d_bedge, int *d_bedge_exp,
+int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int n_items, int n_citems, int stripes,
+                 int max_ly, void *d_items, int *d_counters, int *d_progress, float *d_bedge, int *d_bedge_exp,
                  cudaStream_t stream) {
+    int rc;
+    if (combined) {
+        // one persistent launch pops forward and backward stripes from one list
+        KParams FB = K;
+        FB.items = (const int2 *)d_items;
+        FB.n_items = 2 * n_items;
+        FB.counter = d_counters;
+        FB.progress = d_progress;
+        FB.bprogress = d_progress + stripes;
+        FB.bedge = d_bedge;
+        FB.bedge_exp = d_bedge_exp;
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
+        if ((rc = wl(plan, FB, 2 * n_items, max_ly, 4, stream))) return rc;
+        if (plan->timing) {
+            CUDA_TRY(cudaEventRecord(plan->ev[1], stream));
+            CUDA_TRY(cudaEventRecord(plan->ev[2], stream));
+            CUDA_TRY(cudaEventRecord(plan->ev[3], stream));
+        }
+        KParams C = K;
+        C.items = (const int2 *)d_items + 2 * n_items;
+        C.n_items = n_citems;
+        C.counter = d_counters + 2;
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[4], stream));
+        if ((rc = wl(plan, C, n_citems, max_ly, 3, stream))) return rc;
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[5], stream));
+        plan->launches += 2;
+        plan->timed_bwd = true;
+        plan->timed_count = true;
+        return 0;
+    }
     phmm_plan::Side *sd = nullptr;
     for (auto &e : plan->sides)
         if (e.user == stream) { sd = &e; break; }
@@ -961,7 +996,6 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, int n_items, int n
         plan->sides.push_back(e);
         sd = &plan->sides.back();
     }
-    int rc;
     CUDA_TRY(cudaEventRecord(sd->fork, stream));
     CUDA_TRY(cudaStreamWaitEvent(sd->side, sd->fork, 0));
     // forward (caller's stream)
@@ -972,8 +1006,11 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, int n_items, int n
     F.progress = d_progress;
     F.blat = nullptr;
     F.blat_exp = nullptr;
+    // the two wavefronts share the GPU: each persistent grid takes half the
+    // resident slots, so neither waits for the other to drain
+    plan->grid_div = 2;
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
-    if ((rc = wl(plan, F, n_items, max_ly, 0, stream))) return rc;
+    if ((rc = wl(plan, F, n_items, max_ly, 0, stream))) { plan->grid_div = 1; return rc; }
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[1], stream));
     // backward recursion (side stream): own edge rows and progress counters
     KParams B = K;
@@ -986,7 +1023,9 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, int n_items, int n
     B.lat = nullptr;
     B.lat_exp = nullptr;
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[2], sd->side));
-    if ((rc = wl(plan, B, n_items, max_ly, 2, sd->side))) return rc;
+    rc = wl(plan, B, n_items, max_ly, 2, sd->side);
+    plan->grid_div = 1;
+    if (rc) return rc;
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[3], sd->side));
     CUDA_TRY(cudaEventRecord(sd->join, sd->side));
     CUDA_TRY(cudaStreamWaitEvent(stream, sd->join, 0));
@@ -1105,6 +1144,14 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
                 n_citems += nch;
             }
         }
+        if (bl) {   // one launch runs both wavefronts: interleave the two lists
+            std::vector<int2> both(2 * (size_t)n_items);
+            for (int i = 0; i < n_items; ++i) {
+                both[2 * i] = plan->h_items[i];
+                both[2 * i + 1] = make_int2(plan->h_items[n_items + i].x, plan->h_items[n_items + i].y | blk::BWD_ITEM);
+            }
+            std::copy(both.begin(), both.end(), plan->h_items.begin());
+        }
     }
     int rc;
     // ---- scratch: plan-owned buffers, or carved from the caller's workspace
@@ -1219,8 +1266,8 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     K.post = post;
     K.max_ly = max_ly;
     K.spin_limit = 40LL * 1000 * 1000;
-    if (split) return launch_split(plan, K, wl ? wl : bl, n_items, n_citems, stripes, max_ly, d_items, d_counters,
-                                   d_progress, d_bedge, d_bedge_exp, stream);
+    if (split) return launch_split(plan, K, wl ? wl : bl, bl != nullptr, n_items, n_citems, stripes, max_ly, d_items,
+                                   d_counters, d_progress, d_bedge, d_bedge_exp, stream);
     for (int pass = 0; pass < (estep ? 2 : 1); ++pass) {
         const bool bwd = pass == 1;
         K.items = (const int2 *)d_items + (bwd ? n_items : 0);
@@ -1256,20 +1303,21 @@ int launch_block(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind,
     void (*kern)(const KParams) = nullptr;
     int bytes = 0, threads = 0;
     if (kind == 3) {
-        bytes = blk::make_smem_cb(SH::NS, K.G, max_ly).bytes;
+        bytes = blk::make_smem_cb(SH::NS, K.G, max_ly, K.kend[0] - K.kbeg[0], K.kend[1] - K.kbeg[1],
+                                  K.kend[2] - K.kbeg[2]).bytes;
         kern = blk::count_block_kernel<SH>;
         threads = blk::CNT_THREADS;
     } else {
         bytes = blk::make_smem_b(SH::NS, SH::NB, 1, K.G, max_ly, kind == 1).bytes;
         kern = kind == 0 ? blk::forward_block_kernel<SH>
-                         : (kind == 1 ? blk::backward_block_kernel<SH> : blk::backward_rec_block_kernel<SH>);
+                         : (kind == 1 ? blk::backward_block_kernel<SH> : blk::fwdbwd_block_kernel<SH>);
         threads = 32 * (SH::NB + (kind == 1 ? blk::NCW : 0));
     }
     CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     int occ = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, bytes));
     if (occ < 1) return fail(PHMM_E_ARG, "block kernel does not fit on an SM (shared memory)");
-    const int grid = std::min(n_items, plan->sm_count * occ);
+    const int grid = std::min(n_items, std::max(1, plan->sm_count * occ / plan->grid_div));
     kern<<<grid, threads, bytes, stream>>>(K);
     CUDA_TRY(cudaGetLastError());
     return 0;
@@ -1291,7 +1339,7 @@ int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, 
     int occ = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32, bytes));
     if (occ < 1) return fail(PHMM_E_ARG, "warp kernel does not fit on an SM (shared memory)");
-    const int grid = std::min(n_items, plan->sm_count * occ);
+    const int grid = std::min(n_items, std::max(1, plan->sm_count * occ / plan->grid_div));
     kern<<<grid, 32, bytes, stream>>>(K);
     CUDA_TRY(cudaGetLastError());
     return 0;

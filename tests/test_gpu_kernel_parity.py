@@ -64,7 +64,7 @@ def related_pair(rng, Lx, Ly):
 def run_kernel(chi, st, groups, EM, EI, ED, xs, ys, per_pair=None, variant=0):
     """per_pair: optional list of (chi, EM, EI, ED) per pair; variant 1 =
     generic kernels, 2 = register-resident warp kernels, 3 = block kernels,
-    4 = split warp E-step, 5 = split block E-step, 0 = automatic."""
+    4 = split warp E-step, 5 = split block E-step, 6 = wide kernels, 0 = automatic."""
     from pairhmm import _lib
     G = EM.shape[0]
     plan = _lib.Plan(st, groups, G)
@@ -106,7 +106,7 @@ LENGTHS = [(0, 0), (0, 5), (6, 0), (1, 1), (7, 9), (31, 33), (32, 32), (33, 31),
            (63, 10), (64, 64), (65, 40), (40, 97), (130, 120), (129, 3)]
 
 
-@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5])
+@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5, 6])
 @pytest.mark.parametrize('model,K,F,C', [('tkf91', 1, 1, 1), ('mixdom2', 3, 1, 1),
                                          ('mixdom2', 2, 2, 2), ('mixdom2', 4, 2, 2),
                                          ('mixdom2', 1, 1, 2), ('mixdom2', 2, 1, 1)])
@@ -142,7 +142,7 @@ def test_forward_only_matches_estep_ll(cuda_lib):
     np.testing.assert_array_equal(ll_f.cpu().numpy(), out['ll'].cpu().numpy())
 
 
-@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5])
+@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5, 6])
 def test_per_pair_chi_and_wildcards(cuda_lib, variant):
     rng = np.random.default_rng(11)
     base = mixdom2_params(rng, 2, 1, 1)
@@ -167,7 +167,7 @@ def test_per_pair_chi_and_wildcards(cuda_lib, variant):
         assert_counts(out['cnt_M'][b], cM)
 
 
-@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5])
+@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5, 6])
 def test_long_pair_pipelined_stripes(cuda_lib, variant):
     """A pair spanning many stripes (pipelined through the edge rows), against the oracle."""
     rng = np.random.default_rng(5)
@@ -178,3 +178,45 @@ def test_long_pair_pipelined_stripes(cuda_lib, variant):
     assert abs(out['ll'][0] - ll) <= LL_RTOL * abs(ll)
     assert_counts(out['n_trans'][0], n)
     assert_counts(out['cnt_D'][0], cD)
+
+
+# Large state spaces (more than 64 padded slots) run on the wide kernels:
+# n_dom=4 n_frag=4 (82 states), n_dom=13 n_frag=1 (67 states: the start state
+# shares the last M quad), n_dom=8 n_frag=4 n_classes=4 (162 states).
+WIDE_LENGTHS = [(0, 0), (0, 5), (6, 0), (1, 1), (9, 7), (31, 33), (32, 32), (33, 31), (64, 10), (20, 65)]
+
+
+@pytest.mark.parametrize('K,F,C', [(4, 4, 1), (13, 1, 1), (8, 4, 4)])
+def test_wide_state_spaces_match_oracle(cuda_lib, K, F, C):
+    rng = np.random.default_rng(100 + K + F + C)
+    chi, st, groups, EM, EI, ED = oracle_case('mixdom2', rng, K, F, C)
+    lengths = WIDE_LENGTHS if K * F < 32 else WIDE_LENGTHS[:8]
+    xs, ys = zip(*[related_pair(rng, a, b) for a, b in lengths])
+    out, plan = run_kernel(chi, st, groups, EM, EI, ED, list(xs), list(ys))
+    assert plan.last_variant == 6
+    assert (out['status'] == 0).all(), out['status']
+    for b, (x, y) in enumerate(zip(xs, ys)):
+        ll, n, cM, cI, cD = oracle_estep(chi, st, groups, EM, EI, ED, x, y)
+        assert abs(out['ll'][b] - ll) <= LL_RTOL * abs(ll) + 1e-9, (b, out['ll'][b], ll)
+        assert_counts(out['n_trans'][b], n)
+        assert_counts(out['cnt_M'][b], cM)
+        assert_counts(out['cnt_I'][b], cI)
+        assert_counts(out['cnt_D'][b], cD)
+
+
+def test_wide_forward_only_and_long_pair(cuda_lib):
+    """phmm_forward on the wide kernels, and a pair spanning many 32-row stripes."""
+    from pairhmm import _lib
+    rng = np.random.default_rng(21)
+    chi, st, groups, EM, EI, ED = oracle_case('mixdom2', rng, 4, 4, 1)
+    x, y = related_pair(rng, 100, 90)
+    plan = _lib.Plan(st, groups, EM.shape[0])
+    b = _lib.make_batch([x], [y], chi[None], EM[None], EI[None], ED[None])
+    ll_f, st_f = _lib.forward(plan, b)
+    out = _lib.estep(plan, b)
+    ll, n, cM, cI, cD = oracle_estep(chi, st, groups, EM, EI, ED, x, y)
+    assert int(st_f.cpu()[0]) == 0
+    assert abs(float(ll_f.cpu()[0]) - ll) <= LL_RTOL * abs(ll)
+    assert abs(float(out['ll'].cpu()[0]) - ll) <= LL_RTOL * abs(ll)
+    assert_counts(out['n_trans'][0].cpu().numpy(), n)
+    assert_counts(out['cnt_M'][0].cpu().numpy(), cM)

@@ -167,7 +167,6 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
     };
     __syncthreads();
     if (warp == 0 && !fetch_halo(0)) misc[0] = 1;
-    double llv = 0.0;
     int llE = EXP_NONE;
     bool aborted = false;
     int k = 0;
@@ -177,8 +176,9 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
         if (tid == 0) misc[(k + 1) & 1] = 0;
         // maxima of step t+1 start at zero (slot last read at step t-1)
         for (int r = tid; r < RW; r += nt) MX[((t + 1) & 3) * BW + r + 1] = 0;
-        // the origin's start-state entries live two (A) / three (B) steps
-        if (si == 0 && tid == 0) {
+        // the origin's start-state entries (start slot outside the destination
+        // quads) live two (A) / three (B) steps
+        if (si == 0 && tid == 0 && P.s_slot >= KS) {
             if (t == 2) A[(0 * NS + P.s_slot) * RW + 0] = 0.f;
             if (t == 3) B[(0 * NS + P.s_slot) * BW + 1] = 0.f;
         }
@@ -258,11 +258,13 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
             for (int i = 0; i < 4; ++i) {
                 const int r = r0 + i, j = t - r;
                 const int yj = valid[i] ? ys[j] : 0;
+                const bool origin = valid[i] && i0 + r == 0 && j == 0;
                 mxr[i] = 0.f;
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     float v = 0.f;
                     if (valid[i] && sc[i] > 0.f) v = acc[i][u] * sc[i] * emit_g(P, eMg, eIg, eDg, 4 * qd + u, xr[i], yj);
+                    if (4 * qd + u == P.s_slot) v = origin ? 1.f : 0.f;   // F[0,0,start] = 1
                     acc[i][u] = v;
                     mxr[i] = fmaxf(mxr[i], v);
                 }
@@ -299,7 +301,7 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
                     if (qd == 0) llE = origin ? 0 : Eo[i];
                 }
             }
-            if (si == 0 && t == 0 && qd == 0 && rg == 0) {   // origin: F[0,0,start] = 1
+            if (si == 0 && t == 0 && qd == 0 && rg == 0 && P.s_slot >= KS) {   // origin: F[0,0,start] = 1
                 A[(0 * NS + P.s_slot) * RW + 0] = 1.f;
                 B[(0 * NS + P.s_slot) * BW + 1] = 1.f;
                 atomicMax(MX + 0 * BW + 1, __float_as_int(1.f));
@@ -340,7 +342,7 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
         if (tid == 0) {
             double acc = 0.0;
             for (int q = 0; q < NQd; ++q) acc += llp[q];
-            if (Lx == 0 && Ly == 0) acc += (double)sm[L.chiE + P.s_slot];   // the origin is the terminal
+            if (Lx == 0 && Ly == 0 && P.s_slot >= KS) acc += (double)sm[L.chiE + P.s_slot];   // origin = terminal
             const int Et = *Eterm;
             double ll = NEG_INF_LL;
             if (acc > 0.0 && isfinite(acc) && Et > EXP_NONE) ll = log(acc) + (double)Et * LN2;
@@ -584,7 +586,7 @@ __device__ void bwd_rec_stripe_wd(const KParams &P, int p, int si, const SmemWd 
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(1024) fwdbwd_wide_kernel(const KParams P) {
+__global__ void __launch_bounds__(512) fwdbwd_wide_kernel(const KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
     float *sm = reinterpret_cast<float *>(smem_raw);
@@ -602,7 +604,281 @@ __global__ void __launch_bounds__(1024) fwdbwd_wide_kernel(const KParams P) {
     }
 }
 
-__global__ void __launch_bounds__(1024) forward_wide_kernel(const KParams P) {
+// ---------------------------------------------------------------- counts from both lattices
+// One item = one stripe of one pair and one half (SPL = 2) of the source
+// slots; 512 threads.  Per anti-diagonal step: phase A (16 threads per cell)
+// forms f~ of the item's source slots and the successor operands
+//   u[k] = w~_succ(k)[k] 2^(E_succ + E_f - lambda)   (w~ = e b~)
+// for every destination slot; phase B accumulates the 32-cell outer products
+// in 4 x 4 tiles (Kahan).  The lattice loads of the next step are issued
+// before phase B.  Half 0 also forms the posteriors f~ b~ 2^(E_f + E_b -
+// lambda) for the emission counts (shared-memory tables by slot and
+// character, float64 reductions at the end of the stripe).
+constexpr int CT = 512;          // count CTA
+constexpr int SPL = 2;           // source-slot halves per stripe
+constexpr int CTPT = 2;          // outer-product tiles per thread (ceil(NQ/2) * NQd <= CT * CTPT)
+
+struct SmemWc {
+    int fst, ust, tM, tI, tD;   // float offsets
+    int bytes;
+};
+
+__host__ __device__ inline SmemWc make_smem_wc(int NS, int KS, int wM, int wI, int wD) {
+    SmemWc L;
+    const int SQ = ((NS / 4) + SPL - 1) / SPL;   // source quads per half
+    int o = 0;
+    L.fst = o; o += RW * (4 * SQ + 4);
+    L.ust = o; o += RW * (KS + 4);
+    L.tM = o; o += (wM * 441 + 3) & ~3;
+    L.tI = o; o += (wI * 21 + 3) & ~3;
+    L.tD = o; o += (wD * 21 + 3) & ~3;
+    L.bytes = o * 4;
+    return L;
+}
+
+__device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const SmemWc &L, float *sm) {
+    const int NS = P.NS, KS = P.kend[2], NQd = KS / 4, NQ = NS / 4, N = P.N, G = P.G;
+    const int SQ = (NQ + SPL - 1) / SPL;
+    const int sq0 = sp * SQ, sq1 = min(NQ, sq0 + SQ), nsq = sq1 - sq0;
+    const int FW = 4 * SQ + 4, UW = KS + 4;
+    const PairMeta m = P.meta[p];
+    const int Lx = m.Lx, Ly = m.Ly;
+    const int tid = threadIdx.x;
+    const int i0 = si * RW;
+    const int nrows = min(RW, Lx + 1 - i0);
+    const bool has_below = si + 1 < m.n_stripes;
+    const int ES = ls_of(NS);
+    const int64_t latc = m.lat_base + (int64_t)si * (RW + Ly) * RW;
+    const int64_t latb = m.lat_base + (int64_t)(si + 1) * (RW + Ly) * RW;
+    const int T_last = (nrows - 1) + Ly;
+    const double llv = P.ll[p];
+    if (!(llv > -1e29) || nsq <= 0) return;   // uniform over the CTA
+    const double lam = llv / LN2;
+    const int Ep = (int)floor(lam);
+    const float rfrac = (float)exp2(-(lam - floor(lam)));
+    const int mb = P.kbeg[0], ib = P.kbeg[1], db = P.kbeg[2];
+    const int wM = P.kend[0] - mb, wI = P.kend[1] - ib, wD = P.kend[2] - db;
+    const bool emis = sp == 0;
+    float *fst = sm + L.fst, *ust = sm + L.ust, *tM = sm + L.tM, *tI = sm + L.tI, *tD = sm + L.tD;
+    if (emis) {
+        for (int idx = tid; idx < wM * 441; idx += CT) tM[idx] = 0.f;
+        for (int idx = tid; idx < wI * 21; idx += CT) tI[idx] = 0.f;
+        for (int idx = tid; idx < wD * 21; idx += CT) tD[idx] = 0.f;
+    }
+    const float *eMg = P.eM + (int64_t)p * P.eM_stride;
+    const float *eIg = P.eI + (int64_t)p * P.eID_stride;
+    const float *eDg = P.eD + (int64_t)p * P.eID_stride;
+    // phase A role: cell row c, 16 threads per cell
+    const int c = tid >> 4, sub = tid & 15;
+    const int row = i0 + c;
+    const int xc = (row >= 1 && row <= Lx) ? min((int)P.res[m.x_off + row - 1], 20) : 0;
+    const int xn = (row + 1 <= Lx) ? min((int)P.res[m.x_off + row], 20) : 0;
+    // phase B role: tiles (source quad, destination quad)
+    const int ntile = nsq * NQd;
+    float csum[CTPT][16], ccomp[CTPT][16];
+#pragma unroll
+    for (int a = 0; a < CTPT; ++a)
+#pragma unroll
+        for (int u = 0; u < 16; ++u) { csum[a][u] = 0.f; ccomp[a][u] = 0.f; }
+    constexpr int KQ = 3;   // destination quads per phase-A thread: ceil(NQd / 16) <= KQ
+    constexpr int FQ = 2;   // source quads per phase-A thread: ceil(SQ / 16) <= FQ
+    // prefetched lattice data of one step
+    int Ef = EXP_NONE, Eb = EXP_NONE;
+    int Es[KQ];
+    float4 sv[KQ], fv[FQ], bo[KQ];
+    auto issue = [&](int t) {
+        const int j = t - c;
+        const bool valid = t >= 0 && c < nrows && j >= 0 && j <= Ly;
+        const int64_t cell = latc + (int64_t)t * RW + c;
+        Ef = EXP_NONE; Eb = EXP_NONE;
+#pragma unroll
+        for (int a = 0; a < FQ; ++a) fv[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int a = 0; a < KQ; ++a) { Es[a] = EXP_NONE; sv[a] = make_float4(0.f, 0.f, 0.f, 0.f); bo[a] = sv[a]; }
+        if (!valid) return;
+        Ef = __ldg(reinterpret_cast<const int *>(P.lat + cell * ES) + NS);
+        Eb = __ldg(reinterpret_cast<const int *>(P.blat + cell * ES) + NS);
+#pragma unroll
+        for (int a = 0; a < FQ; ++a) {
+            const int q = sq0 + sub + 16 * a;
+            if (q < sq1) fv[a] = __ldg(reinterpret_cast<const float4 *>(P.lat + cell * ES) + q);
+        }
+        const bool hI = j + 1 <= Ly, hD = row + 1 <= Lx, hM = hI && hD;
+        const bool below_ok = c + 1 < nrows || has_below;
+#pragma unroll
+        for (int a = 0; a < KQ; ++a) {
+            const int q = sub + 16 * a;
+            if (q >= NQd) continue;
+            if (emis) bo[a] = __ldg(reinterpret_cast<const float4 *>(P.blat + cell * ES) + q);
+            const int qt = P.quad_type[q];
+            int64_t sc = -1;
+            if (qt == T_I && hI) sc = latc + (int64_t)(t + 1) * RW + c;
+            else if (qt == T_D && hD && below_ok)
+                sc = c + 1 < nrows ? latc + (int64_t)(t + 1) * RW + c + 1 : latb + (int64_t)j * RW;
+            else if (qt == T_M && hM && below_ok)
+                sc = c + 1 < nrows ? latc + (int64_t)(t + 2) * RW + c + 1 : latb + (int64_t)(j + 1) * RW;
+            if (sc >= 0) {
+                Es[a] = __ldg(reinterpret_cast<const int *>(P.blat + sc * ES) + NS);
+                sv[a] = __ldg(reinterpret_cast<const float4 *>(P.blat + sc * ES) + q);
+            }
+        }
+    };
+    issue(T_last);
+    for (int t = T_last; t >= 0; --t) {
+        // ================= phase A
+        {
+            const int j = t - c;
+            const bool valid = c < nrows && j >= 0 && j <= Ly;
+            const bool live = valid && Ef > EXP_NONE;
+            const int yj = (valid && j >= 1) ? min((int)P.res[m.y_off + j - 1], 20) : 0;
+            const int yn = (valid && j + 1 <= Ly) ? min((int)P.res[m.y_off + j], 20) : 0;
+            const bool term = valid && row == Lx && j == Ly;
+#pragma unroll
+            for (int a = 0; a < FQ; ++a) {
+                const int q = sq0 + sub + 16 * a;
+                if (q < sq1) {
+                    const float4 f = live ? fv[a] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    *reinterpret_cast<float4 *>(fst + c * FW + 4 * (q - sq0)) = f;
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < KQ; ++a) {
+                const int q = sub + 16 * a;
+                if (q >= NQd) continue;
+                float4 uu = make_float4(0.f, 0.f, 0.f, 0.f);
+                const int qt = P.quad_type[q];
+                if (live && Es[a] > EXP_NONE && !term) {
+                    int du = Es[a] + Ef - Ep;
+                    if (du > 126) { du = 126; atomicOr(P.status + p, PHMM_ST_SCALE_CLAMP); }
+                    const float us = fminf(warp2::scale_pow2(rfrac, max(du, -200)), 3e38f);
+                    const int xi = qt == T_I ? xc : xn, yy = qt == T_D ? yj : yn;
+                    float e[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) e[u] = emit_g(P, eMg, eIg, eDg, 4 * q + u, xi, yy);
+                    uu = make_float4(sv[a].x * e[0] * us, sv[a].y * e[1] * us, sv[a].z * e[2] * us, sv[a].w * e[3] * us);
+                }
+                *reinterpret_cast<float4 *>(ust + c * UW + 4 * q) = uu;
+                // posteriors of my destination quad -> emission counts (half 0)
+                if (emis && live && Eb > EXP_NONE) {
+                    int dp = Ef + Eb - Ep;
+                    if (dp > 126) { dp = 126; atomicOr(P.status + p, PHMM_ST_SCALE_CLAMP); }
+                    const float ps = warp2::scale_pow2(rfrac, max(dp, -200));
+                    const float4 f4 = __ldg(reinterpret_cast<const float4 *>(P.lat + (latc + (int64_t)t * RW + c) * ES) + q);
+                    const float pk[4] = {f4.x * bo[a].x * ps, f4.y * bo[a].y * ps, f4.z * bo[a].z * ps, f4.w * bo[a].w * ps};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int s = 4 * q + u;
+                        const int st = P.slot_type[s];
+                        if (pk[u] == 0.f) continue;
+                        if (st == T_M) atomicAdd(tM + (s - mb) * 441 + xc * 21 + yj, pk[u]);
+                        else if (st == T_I) atomicAdd(tI + (s - ib) * 21 + yj, pk[u]);
+                        else if (st == T_D) atomicAdd(tD + (s - db) * 21 + xc, pk[u]);
+                    }
+                }
+            }
+            // expected End transitions: n[s][End] = f(term)[s] chi[s][End] / P
+            if (emis && term && live) {
+                const float *chi = P.chi + (int64_t)p * P.chi_stride;
+                const double fs = exp2((double)Ef - lam);
+                for (int s = sub; s < NS; s += 16) {
+                    const int os = P.slot_orig[s];
+                    if (os < 0) continue;
+                    const float f = __ldg(P.lat + (latc + (int64_t)t * RW + c) * ES + s);
+                    const double v = (double)f * (double)__ldg(chi + os * N + P.e_idx) * fs;
+                    if (v != 0.0) atomicAdd(P.n_trans + ((int64_t)p * N + os) * N + P.e_idx, v);
+                }
+            }
+        }
+        issue(t - 1);
+        __syncthreads();
+        // ================= phase B: 4 x 4 tiles over the step's 32 cells
+#pragma unroll
+        for (int a = 0; a < CTPT; ++a) {
+            const int tile = tid + a * CT;
+            if (tile >= ntile) continue;
+            const int bs = tile / NQd, bk = tile % NQd;
+            float pz[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) pz[u] = 0.f;
+#pragma unroll 4
+            for (int rr = 0; rr < RW; ++rr) {
+                const float4 fv4 = *reinterpret_cast<const float4 *>(fst + rr * FW + 4 * bs);
+                const float4 uv4 = *reinterpret_cast<const float4 *>(ust + rr * UW + 4 * bk);
+                const float fa[4] = {fv4.x, fv4.y, fv4.z, fv4.w};
+                const float ua[4] = {uv4.x, uv4.y, uv4.z, uv4.w};
+#pragma unroll
+                for (int x = 0; x < 4; ++x)
+#pragma unroll
+                    for (int y = 0; y < 4; ++y) pz[4 * x + y] = fmaf(fa[x], ua[y], pz[4 * x + y]);
+            }
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                const float y = pz[u] - ccomp[a][u];
+                const float tt = csum[a][u] + y;
+                ccomp[a][u] = (tt - csum[a][u]) - y;
+                csum[a][u] = tt;
+            }
+        }
+        __syncthreads();
+    }
+    // ================= flush (float64 reductions)
+    const float *chi = P.chi + (int64_t)p * P.chi_stride;
+#pragma unroll
+    for (int a = 0; a < CTPT; ++a) {
+        const int tile = tid + a * CT;
+        if (tile >= ntile) continue;
+        const int bs = tile / NQd, bk = tile % NQd;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            const int s = 4 * (sq0 + bs) + (u >> 2), kk = 4 * bk + (u & 3);
+            const int os = P.slot_orig[s], ok = P.slot_orig[kk];
+            const int kt = P.slot_type[kk];
+            const float val = csum[a][u] - ccomp[a][u];
+            if (os < 0 || ok < 0 || !(kt == T_M || kt == T_I || kt == T_D) || val == 0.f) continue;
+            atomicAdd(P.n_trans + ((int64_t)p * N + os) * N + ok, (double)val * (double)__ldg(chi + os * N + ok));
+        }
+    }
+    if (emis) {
+        for (int idx = tid; idx < wM * 441; idx += CT) {
+            const float v = tM[idx];
+            const int s = mb + idx / 441;
+            if (v != 0.f && P.slot_type[s] == T_M)
+                atomicAdd(P.cntM + ((int64_t)p * G + P.slot_group[s]) * 441 + idx % 441, (double)v);
+        }
+        for (int idx = tid; idx < wI * 21; idx += CT) {
+            const float v = tI[idx];
+            const int s = ib + idx / 21;
+            if (v != 0.f && P.slot_type[s] == T_I)
+                atomicAdd(P.cntI + ((int64_t)p * G + P.slot_group[s]) * 21 + idx % 21, (double)v);
+        }
+        for (int idx = tid; idx < wD * 21; idx += CT) {
+            const float v = tD[idx];
+            const int s = db + idx / 21;
+            if (v != 0.f && P.slot_type[s] == T_D)
+                atomicAdd(P.cntD + ((int64_t)p * G + P.slot_group[s]) * 21 + idx % 21, (double)v);
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(CT, 1) count_wide_kernel(const KParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_item;
+    float *sm = reinterpret_cast<float *>(smem_raw);
+    const SmemWc L = make_smem_wc(P.NS, P.kend[2], P.kend[0] - P.kbeg[0], P.kend[1] - P.kbeg[1],
+                                  P.kend[2] - P.kbeg[2]);
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(P.counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= P.n_items) break;
+        const int2 w = P.items[it];
+        count_stripe_wd(P, w.x, w.y >> 4, w.y & 15, L, sm);
+    }
+}
+
+__global__ void __launch_bounds__(512) forward_wide_kernel(const KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
     float *sm = reinterpret_cast<float *>(smem_raw);

@@ -45,7 +45,8 @@ namespace {
 
 constexpr int TH = 32;             // rows per stripe == lanes per warp
 constexpr int HC = 32;             // halo chunk width (columns)
-constexpr int MAXS = 64;           // max padded state slots (16 quads)
+constexpr int MAXS = 168;          // max padded state slots (42 quads): the wide kernels
+constexpr int GMAXS = 64;          // max padded slots of the generic, warp and block kernels
 constexpr int MAXQ = MAXS / 4;
 constexpr int NBIN = 441 + 21 + 21;
 constexpr int EXP_NONE = -(1 << 28);
@@ -830,6 +831,7 @@ __global__ void fill_f64(double *p, int64_t n, double v) {
 #include "estep_split.cuh"
 #include "estep_block.cuh"
 #include "estep_block_split.cuh"
+#include "estep_wide.cuh"
 
 namespace {
 
@@ -880,7 +882,7 @@ struct phmm_plan {
     // register-resident warp kernels for this state space (null: generic kernels)
     int w_nm = 0, w_ni = 0, w_nd = 0;
     int grid_div = 1;       // persistent grids use 1/grid_div of the resident slots
-    int variant = 0;        // 0 automatic, 1 generic, 2 warp, 3 block, 4 split warp E-step, 5 split block E-step
+    int variant = 0;        // 0 automatic, 1 generic, 2 warp, 3 block, 4/5 split warp/block E-step, 6 wide
     int last_variant = 0;
 };
 
@@ -889,7 +891,9 @@ namespace {
 template <typename T>
 int ensure(T **ptr, size_t *cap, size_t n) {
     if (n <= *cap && *ptr) return 0;
-    size_t want = std::max(n, (size_t)(*cap * 3 / 2));
+    // grow by half again for small buffers (fewer reallocations); exactly for
+    // buffers above 1 GiB, where the headroom would cost real HBM
+    size_t want = n * sizeof(T) > ((size_t)1 << 30) ? n : std::max(n, (size_t)(*cap * 3 / 2));
     if (*ptr) { cudaDeviceSynchronize(); cudaFree(*ptr); *ptr = nullptr; *cap = 0; }
     cudaError_t e = cudaMalloc((void **)ptr, std::max<size_t>(want, 1) * sizeof(T));
     if (e != cudaSuccess) return fail(PHMM_E_CUDA, std::string("cudaMalloc scratch: ") + cudaGetErrorString(e));
@@ -1043,6 +1047,202 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
     return 0;
 }
 
+// The wide kernels (estep_wide.cuh): forward and backward recursion in one
+// persistent launch, then the count pass; lattice and edge records of NS + 4
+// floats per cell (values, exponent, maximum).
+int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_trans, double *cntM,
+             double *cntI, double *cntD, int32_t *status, cudaStream_t stream, void *ws, size_t ws_bytes,
+             size_t *ws_need) {
+    KParams K = plan->base;
+    const int P_ = b->n_pairs, N = K.N, G = K.G, NS = K.NS;
+    const int KS = K.kend[2], NQd = KS / 4, NQ = NS / 4;
+    const int ES = wide::ls_of(NS);
+    const int rows = wide::RW;
+    if (NQd > 48 || ((NQ + wide::SPL - 1) / wide::SPL) * NQd > wide::CT * wide::CTPT)
+        return fail(PHMM_E_ARG, "state space too large for the wide kernels");
+    if (!ws_need) plan->last_variant = 6;
+    std::vector<int> order(P_);
+    for (int p = 0; p < P_; ++p) {
+        if (b->Lx_host[p] < 0 || b->Ly_host[p] < 0) return fail(PHMM_E_ARG, "negative length");
+        order[p] = p;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+        return (int64_t)(b->Lx_host[a] + 1) * (b->Ly_host[a] + 1) >
+               (int64_t)(b->Lx_host[c] + 1) * (b->Ly_host[c] + 1);
+    });
+    plan->h_meta.resize(P_);
+    int64_t lat_cells = 0, edge_cells = 0;
+    int stripes = 0, max_ly = 0;
+    for (int p = 0; p < P_; ++p) {
+        PairMeta &m = plan->h_meta[p];
+        m.Lx = b->Lx_host[p];
+        m.Ly = b->Ly_host[p];
+        m.x_off = b->x_off_host[p];
+        m.y_off = b->y_off_host[p];
+        m.n_stripes = (m.Lx + 1 + rows - 1) / rows;
+        m.stripe_base = stripes;
+        m.lat_base = lat_cells;
+        m.edge_base = edge_cells;
+        m.tab_base = 0;
+        stripes += m.n_stripes;
+        if (estep) lat_cells += (int64_t)m.n_stripes * (rows + m.Ly) * rows;
+        edge_cells += (int64_t)m.n_stripes * (m.Ly + 1);
+        max_ly = std::max(max_ly, m.Ly);
+    }
+    // work lists: forward / backward stripes interleaved, then the count items
+    plan->h_items.clear();
+    std::vector<int2> fw, bw;
+    for (int p : order)
+        for (int s = 0; s < plan->h_meta[p].n_stripes; ++s) fw.push_back(make_int2(p, s));
+    for (int p : order)
+        for (int s = plan->h_meta[p].n_stripes - 1; s >= 0; --s) bw.push_back(make_int2(p, s | blk::BWD_ITEM));
+    const int n_items = (int)fw.size();
+    if (estep) {
+        for (int i = 0; i < n_items; ++i) { plan->h_items.push_back(fw[i]); plan->h_items.push_back(bw[i]); }
+        for (int p : order)
+            for (int s = 0; s < plan->h_meta[p].n_stripes; ++s)
+                for (int h = 0; h < wide::SPL; ++h) plan->h_items.push_back(make_int2(p, (s << 4) | h));
+    } else {
+        plan->h_items = fw;
+    }
+    const int n_fb = estep ? 2 * n_items : n_items;
+    const int n_citems = estep ? n_items * wide::SPL : 0;
+    // ---- scratch
+    const size_t o_meta = 0;
+    const size_t o_items = align256(o_meta + sizeof(PairMeta) * P_);
+    const size_t o_cnt = align256(o_items + sizeof(int2) * plan->h_items.size());
+    const size_t o_prog = align256(o_cnt + 4 * sizeof(int));
+    const size_t o_edge = align256(o_prog + sizeof(int) * 2 * (size_t)stripes);
+    const size_t o_bedge = align256(o_edge + sizeof(float) * (size_t)edge_cells * ES);
+    const size_t o_lat = align256(o_bedge + (estep ? sizeof(float) * (size_t)edge_cells * ES : 0));
+    const size_t o_blat = align256(o_lat + (estep ? sizeof(float) * (size_t)lat_cells * ES : 0));
+    const size_t need = align256(o_blat + (estep ? sizeof(float) * (size_t)lat_cells * ES : 0));
+    if (ws_need) { *ws_need = need; return 0; }
+    void *d_meta, *d_items;
+    int *d_counters, *d_progress;
+    float *d_edge, *d_bedge = nullptr, *d_lat = nullptr, *d_blat = nullptr;
+    int rc;
+    if (ws) {
+        if (ws_bytes < need) {
+            char msg[200];
+            snprintf(msg, sizeof msg, "workspace of %zu bytes is too small: this batch needs %zu bytes", ws_bytes, need);
+            return fail(PHMM_E_ARG, msg);
+        }
+        unsigned char *w = (unsigned char *)ws;
+        d_meta = w + o_meta;
+        d_items = w + o_items;
+        d_counters = (int *)(w + o_cnt);
+        d_progress = (int *)(w + o_prog);
+        d_edge = (float *)(w + o_edge);
+        if (estep) {
+            d_bedge = (float *)(w + o_bedge);
+            d_lat = (float *)(w + o_lat);
+            d_blat = (float *)(w + o_blat);
+        }
+    } else {
+        if ((rc = ensure((char **)&plan->meta, &plan->meta_cap, sizeof(PairMeta) * P_))) return rc;
+        if ((rc = ensure((char **)&plan->items, &plan->items_cap, sizeof(int2) * plan->h_items.size()))) return rc;
+        if ((rc = ensure(&plan->edge, &plan->edge_cap, (size_t)edge_cells * ES))) return rc;
+        if ((rc = ensure(&plan->progress, &plan->prog_cap, (size_t)2 * stripes))) return rc;
+        if (estep) {
+            if ((rc = ensure(&plan->bedge, &plan->bedge_cap, (size_t)edge_cells * ES))) return rc;
+            if ((rc = ensure(&plan->lat, &plan->lat_cap, (size_t)lat_cells * ES))) return rc;
+            if ((rc = ensure(&plan->blat, &plan->blat_cap, (size_t)lat_cells * ES))) return rc;
+        }
+        d_meta = plan->meta;
+        d_items = plan->items;
+        d_counters = plan->counters;
+        d_progress = plan->progress;
+        d_edge = plan->edge;
+        d_bedge = plan->bedge;
+        d_lat = plan->lat;
+        d_blat = plan->blat;
+    }
+    CUDA_TRY(cudaMemcpyAsync(d_meta, plan->h_meta.data(), sizeof(PairMeta) * P_, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_items, plan->h_items.data(), sizeof(int2) * plan->h_items.size(),
+                             cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemsetAsync(d_counters, 0, 3 * sizeof(int), stream));
+    CUDA_TRY(cudaMemsetAsync(d_progress, 0, sizeof(int) * 2 * stripes, stream));
+    CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int32_t) * P_, stream));
+    if (estep) {
+        CUDA_TRY(cudaMemsetAsync(n_trans, 0, sizeof(double) * (size_t)P_ * N * N, stream));
+        CUDA_TRY(cudaMemsetAsync(cntM, 0, sizeof(double) * (size_t)P_ * G * 441, stream));
+        CUDA_TRY(cudaMemsetAsync(cntI, 0, sizeof(double) * (size_t)P_ * G * 21, stream));
+        CUDA_TRY(cudaMemsetAsync(cntD, 0, sizeof(double) * (size_t)P_ * G * 21, stream));
+    }
+    K.res = b->residues;
+    K.meta = (const PairMeta *)d_meta;
+    K.chi = b->chi;
+    K.chi_stride = b->chi_per_pair ? (int64_t)N * N : 0;
+    K.eM = b->emit_M;
+    K.eI = b->emit_I;
+    K.eD = b->emit_D;
+    K.eM_stride = b->emit_per_pair ? (int64_t)G * 441 : 0;
+    K.eID_stride = b->emit_per_pair ? (int64_t)G * 21 : 0;
+    K.lat = d_lat;
+    K.lat_exp = nullptr;
+    K.blat = d_blat;
+    K.blat_exp = nullptr;
+    K.edge = d_edge;
+    K.edge_exp = nullptr;
+    K.bedge = d_bedge;
+    K.bedge_exp = nullptr;
+    K.progress = d_progress;
+    K.bprogress = d_progress + stripes;
+    K.ll = ll;
+    K.status = status;
+    K.n_trans = n_trans;
+    K.cntM = cntM;
+    K.cntI = cntI;
+    K.cntD = cntD;
+    K.F_log = K.B_log = K.post = nullptr;
+    K.max_ly = max_ly;
+    K.spin_limit = 40LL * 1000 * 1000;
+    // ---- wavefronts
+    {
+        K.items = (const int2 *)d_items;
+        K.n_items = n_fb;
+        K.counter = d_counters;
+        const int threads = 32 * ((NQd + 3) / 4);
+        const int bytes = std::max(wide::make_smem_wd(NS, KS, max_ly, false).bytes,
+                                   estep ? wide::make_smem_wd(NS, KS, max_ly, true).bytes : 0);
+        auto kern = estep ? wide::fwdbwd_wide_kernel : wide::forward_wide_kernel;
+        CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        int occ = 0;
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, bytes));
+        if (occ < 1) return fail(PHMM_E_ARG, "wide kernel does not fit on an SM (shared memory)");
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
+        kern<<<std::min(n_fb, plan->sm_count * occ), threads, bytes, stream>>>(K);
+        CUDA_TRY(cudaGetLastError());
+        if (plan->timing) {
+            CUDA_TRY(cudaEventRecord(plan->ev[1], stream));
+            CUDA_TRY(cudaEventRecord(plan->ev[2], stream));
+            CUDA_TRY(cudaEventRecord(plan->ev[3], stream));
+        }
+        plan->launches++;
+    }
+    // ---- counts
+    if (estep) {
+        K.items = (const int2 *)d_items + n_fb;
+        K.n_items = n_citems;
+        K.counter = d_counters + 2;
+        const int bytes = wide::make_smem_wc(NS, KS, K.kend[0] - K.kbeg[0], K.kend[1] - K.kbeg[1],
+                                             K.kend[2] - K.kbeg[2]).bytes;
+        CUDA_TRY(cudaFuncSetAttribute(wide::count_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        int occ = 0;
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, wide::count_wide_kernel, wide::CT, bytes));
+        if (occ < 1) return fail(PHMM_E_ARG, "wide count kernel does not fit on an SM (shared memory)");
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[4], stream));
+        wide::count_wide_kernel<<<std::min(n_citems, plan->sm_count * occ), wide::CT, bytes, stream>>>(K);
+        CUDA_TRY(cudaGetLastError());
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[5], stream));
+        plan->launches++;
+    }
+    plan->timed_bwd = estep;
+    plan->timed_count = estep;
+    return 0;
+}
+
 // One call of the forward (estep false) or E-step kernels.  Scratch comes from
 // the plan (grown on demand) unless the caller passes a workspace `ws` of
 // `ws_bytes`; with `ws_need` set, nothing runs and the workspace size the
@@ -1067,6 +1267,12 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     }
     KParams K = plan->base;
     const int N = K.N, G = K.G;
+    // large state spaces (more than 64 padded slots) run on the wide kernels
+    if (K.NS > GMAXS || plan->variant == 6) {
+        if (F_log || B_log || post)
+            return fail(PHMM_E_ARG, "lattice tables are not available for state spaces of more than 60 emitting states");
+        return run_wide(plan, b, estep, ll, n_trans, cntM, cntI, cntD, status, stream, ws, ws_bytes, ws_need);
+    }
     // kernel family: register-resident warp kernels when the shape has one and
     // no lattice tables are requested; the generic quad kernels otherwise
     WarpLauncher wl = nullptr;
@@ -1345,6 +1551,65 @@ int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, 
     return 0;
 }
 
+// Batches whose scratch would not fit in the device memory that is free run
+// as consecutive groups of pairs (contiguous index ranges), one after the
+// other on the same stream, each within the budget.
+size_t plan_scratch_bytes(const phmm_plan *plan) {
+    return plan->meta_cap + plan->items_cap + sizeof(float) * (plan->lat_cap + plan->edge_cap + plan->blat_cap +
+           plan->bedge_cap) + sizeof(int) * (plan->latE_cap + plan->edgeE_cap + plan->prog_cap + plan->blatE_cap +
+           plan->bedgeE_cap);
+}
+
+int run_groups(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_trans, double *cntM,
+               double *cntI, double *cntD, int32_t *status, void *stream) {
+    if (!plan || !b) return fail(PHMM_E_ARG, "null plan or batch");
+    size_t need = 0;
+    int rc = run(plan, b, estep, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                 stream, nullptr, 0, &need);
+    if (rc) return rc;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = (size_t)-1 / 2;
+    const size_t budget = (size_t)((double)(free_b + plan_scratch_bytes(plan)) * 0.85);
+    if (need <= budget || b->n_pairs <= 1)
+        return run(plan, b, estep, ll, n_trans, cntM, cntI, cntD, status, nullptr, nullptr, nullptr, stream);
+    const int N = plan->base.N, G = plan->base.G;
+    int launches = 0, p0 = 0;
+    while (p0 < b->n_pairs) {
+        // the largest contiguous group from p0 that fits the budget (at least one pair)
+        int lo = 1, hi = b->n_pairs - p0;
+        phmm_batch g = *b;
+        auto group = [&](int n) {
+            g.n_pairs = n;
+            g.Lx_host = b->Lx_host + p0;
+            g.Ly_host = b->Ly_host + p0;
+            g.x_off_host = b->x_off_host + p0;
+            g.y_off_host = b->y_off_host + p0;
+            g.chi = b->chi + (b->chi_per_pair ? (int64_t)p0 * N * N : 0);
+            g.emit_M = b->emit_M + (b->emit_per_pair ? (int64_t)p0 * G * 441 : 0);
+            g.emit_I = b->emit_I + (b->emit_per_pair ? (int64_t)p0 * G * 21 : 0);
+            g.emit_D = b->emit_D + (b->emit_per_pair ? (int64_t)p0 * G * 21 : 0);
+        };
+        while (lo < hi) {   // binary search on the group size
+            const int mid = (lo + hi + 1) / 2;
+            group(mid);
+            size_t n2 = 0;
+            if ((rc = run(plan, &g, estep, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                          nullptr, stream, nullptr, 0, &n2)))
+                return rc;
+            if (n2 <= budget) lo = mid; else hi = mid - 1;
+        }
+        group(lo);
+        rc = run(plan, &g, estep, ll + p0, estep ? n_trans + (int64_t)p0 * N * N : nullptr,
+                 estep ? cntM + (int64_t)p0 * G * 441 : nullptr, estep ? cntI + (int64_t)p0 * G * 21 : nullptr,
+                 estep ? cntD + (int64_t)p0 * G * 21 : nullptr, status + p0, nullptr, nullptr, nullptr, stream);
+        if (rc) return rc;
+        launches += plan->launches;
+        p0 += lo;
+    }
+    plan->launches = launches;
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1399,7 +1664,7 @@ int phmm_plan_create(const phmm_model_desc *md, phmm_plan **out) {
         while (slot_orig.size() % 4) { slot_orig.push_back(-1); slot_type.push_back(T_NONE); }
     }
     const int NS = (int)slot_orig.size();
-    if (NS > MAXS) return fail(PHMM_E_ARG, "too many emitting states for this build (max 60)");
+    if (NS > MAXS) return fail(PHMM_E_ARG, "too many emitting states for this build (max 164)");
     K.N = N;
     K.NS = NS;
     K.NQ = NS / 4;
@@ -1506,14 +1771,12 @@ void phmm_plan_destroy(phmm_plan *plan) {
 
 int phmm_forward(phmm_plan *plan, const phmm_batch *batch, double *ll_out, int32_t *status_out,
                  void *stream) {
-    return run(plan, batch, false, ll_out, nullptr, nullptr, nullptr, nullptr, status_out, nullptr,
-               nullptr, nullptr, stream);
+    return run_groups(plan, batch, false, ll_out, nullptr, nullptr, nullptr, nullptr, status_out, stream);
 }
 
 int phmm_estep(phmm_plan *plan, const phmm_batch *batch, double *ll_out, double *n_trans, double *cnt_M,
                double *cnt_I, double *cnt_D, int32_t *status_out, void *stream) {
-    return run(plan, batch, true, ll_out, n_trans, cnt_M, cnt_I, cnt_D, status_out, nullptr, nullptr,
-               nullptr, stream);
+    return run_groups(plan, batch, true, ll_out, n_trans, cnt_M, cnt_I, cnt_D, status_out, stream);
 }
 
 int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch, double *ll_out, double *n_trans,
@@ -1547,7 +1810,7 @@ int phmm_estep_ws(phmm_plan *plan, const phmm_batch *batch, void *workspace, siz
 int phmm_last_launch_count(const phmm_plan *plan) { return plan ? plan->launches : 0; }
 
 int phmm_set_variant(phmm_plan *plan, int variant) {
-    if (!plan || variant < 0 || variant > 5) return fail(PHMM_E_ARG, "bad variant");
+    if (!plan || variant < 0 || variant > 6) return fail(PHMM_E_ARG, "bad variant");
     if ((variant == 2 || variant == 4) && !find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd))
         return fail(PHMM_E_ARG, "no warp kernel for this state space");
     if ((variant == 3 || variant == 5) && !find_block_launcher(plan->base.NS))
@@ -1613,11 +1876,11 @@ int static_model(const phmm_model_desc *md, KParams *K, int *nm, int *ni, int *n
     for (int ty = 0; ty < 3; ++ty) {
         K->kbeg[ty] = ns;
         for (int q = 0; q < cnt[ty]; ++q) {
-            if (ns >= MAXS) return fail(PHMM_E_ARG, "too many emitting states for this build (max 60)");
+            if (ns >= GMAXS) return fail(PHMM_E_ARG, "phmm_estep_static: at most 60 emitting states");
             slot_orig[ns] = byType[ty][q]; slot_type[ns] = ty + 1; ++ns;
         }
         while (ns % 4) {
-            if (ns >= MAXS) return fail(PHMM_E_ARG, "too many emitting states for this build (max 60)");
+            if (ns >= GMAXS) return fail(PHMM_E_ARG, "phmm_estep_static: at most 60 emitting states");
             if (s_slot < 0) { s_slot = ns; slot_orig[ns] = 0; slot_type[ns] = T_S; }
             else { slot_orig[ns] = -1; slot_type[ns] = T_NONE; }
             ++ns;
@@ -1625,7 +1888,7 @@ int static_model(const phmm_model_desc *md, KParams *K, int *nm, int *ni, int *n
         K->kend[ty] = ns;
     }
     if (s_slot < 0) {
-        if (ns + 4 > MAXS) return fail(PHMM_E_ARG, "too many emitting states for this build (max 60)");
+        if (ns + 4 > GMAXS) return fail(PHMM_E_ARG, "phmm_estep_static: at most 60 emitting states");
         s_slot = ns; slot_orig[ns] = 0; slot_type[ns] = T_S; ++ns;
         while (ns % 4) { slot_orig[ns] = -1; slot_type[ns] = T_NONE; ++ns; }
     }

@@ -309,4 +309,6 @@ CONFIGS = {
         'mixdom2_k3f1c1_200pairs_len30-600', 3, 1, 1, 200, ('loguniform', 30, 600), seed),
     'mixdom2_k4f2c2_32pairs_len200-1500': lambda seed=0: make_mixdom2_workload(
         'mixdom2_k4f2c2_32pairs_len200-1500', 4, 2, 2, 32, ('loguniform', 200, 1500), seed),
+    'mixdom2_k8f4c4_64pairs_len2000': lambda seed=0: make_mixdom2_workload(
+        'mixdom2_k8f4c4_64pairs_len2000', 8, 4, 4, 64, ('around', 2000, 0.1), seed),
 }

@@ -484,58 +484,43 @@ __device__ void bwd_rec_stripe_wd(const KParams &P, int p, int si, const SmemWd 
                 }
                 Eo[i] = term[i] ? 0 : max(max(vI, vD), vM);
             }
-            float aM[4][4], aI[4][4], aD[4][4];
+            // one accumulator over the destinations in slot order (M, I, D), each
+            // successor value pre-scaled by its type's power of two: the same
+            // rounding sequence as the forward's contraction, so the float32
+            // drift of the two recursions stays consistent for the posteriors
+            float sM[4], sI[4], sD[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                sM[i] = (EsM[i] > EXP_NONE) ? pow2d(EsM[i] - Eo[i]) : 0.f;
+                sI[i] = (EsI[i] > EXP_NONE) ? pow2d(EsI[i] - Eo[i]) : 0.f;
+                sD[i] = (EsD[i] > EXP_NONE) ? pow2d(EsD[i] - Eo[i]) : 0.f;
+            }
+            float acc[4][4];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
-                for (int u = 0; u < 4; ++u) { aM[i][u] = 0.f; aI[i][u] = 0.f; aD[i][u] = 0.f; }
+                for (int u = 0; u < 4; ++u) acc[i][u] = 0.f;
             const float4 *cb4 = reinterpret_cast<const float4 *>(chiB) + qs;   // chiB[k][4qs..]
             const int NQk = KS / 4;
-            {   // M destinations: successor (row+1, t+2)
-                const float *base = B + ((t + 2) % 3) * KS * BW + r0 + 4;
+            auto contract = [&](const float *base, int stride, int k0, int k1, const float (&sc)[4]) {
 #pragma unroll 2
-                for (int kk = kb0; kk < ke0; ++kk) {
-                    const float4 w = *reinterpret_cast<const float4 *>(base + kk * BW);
+                for (int kk = k0; kk < k1; ++kk) {
+                    const float4 w = *reinterpret_cast<const float4 *>(base + kk * stride);
                     const float4 c = cb4[kk * NQk];
-                    const float wa[4] = {w.x, w.y, w.z, w.w}, ca[4] = {c.x, c.y, c.z, c.w};
+                    const float wa[4] = {w.x * sc[0], w.y * sc[1], w.z * sc[2], w.w * sc[3]};
+                    const float ca[4] = {c.x, c.y, c.z, c.w};
 #pragma unroll
                     for (int i = 0; i < 4; ++i)
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) aM[i][u] = fmaf(wa[i], ca[u], aM[i][u]);
+                        for (int u = 0; u < 4; ++u) acc[i][u] = fmaf(wa[i], ca[u], acc[i][u]);
                 }
-            }
-            {   // I destinations: successor (row, t+1)
-                const float *base = A + ((t + 1) & 1) * KS * RW + r0;
-#pragma unroll 2
-                for (int kk = kb1; kk < ke1; ++kk) {
-                    const float4 w = *reinterpret_cast<const float4 *>(base + kk * RW);
-                    const float4 c = cb4[kk * NQk];
-                    const float wa[4] = {w.x, w.y, w.z, w.w}, ca[4] = {c.x, c.y, c.z, c.w};
-#pragma unroll
-                    for (int i = 0; i < 4; ++i)
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) aI[i][u] = fmaf(wa[i], ca[u], aI[i][u]);
-                }
-            }
-            {   // D destinations: successor (row+1, t+1)
-                const float *base = B + ((t + 1) % 3) * KS * BW + r0 + 4;
-#pragma unroll 2
-                for (int kk = kb2; kk < ke2; ++kk) {
-                    const float4 w = *reinterpret_cast<const float4 *>(base + kk * BW);
-                    const float4 c = cb4[kk * NQk];
-                    const float wa[4] = {w.x, w.y, w.z, w.w}, ca[4] = {c.x, c.y, c.z, c.w};
-#pragma unroll
-                    for (int i = 0; i < 4; ++i)
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) aD[i][u] = fmaf(wa[i], ca[u], aD[i][u]);
-                }
-            }
+            };
+            contract(B + ((t + 2) % 3) * KS * BW + r0 + 4, BW, kb0, ke0, sM);   // M: (row+1, t+2)
+            contract(A + ((t + 1) & 1) * KS * RW + r0, RW, kb1, ke1, sI);       // I: (row, t+1)
+            contract(B + ((t + 1) % 3) * KS * BW + r0 + 4, BW, kb2, ke2, sD);   // D: (row+1, t+1)
             float bv[4][4], mxr[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const float sM = (EsM[i] > EXP_NONE) ? pow2d(EsM[i] - Eo[i]) : 0.f;
-                const float sI = (EsI[i] > EXP_NONE) ? pow2d(EsI[i] - Eo[i]) : 0.f;
-                const float sD = (EsD[i] > EXP_NONE) ? pow2d(EsD[i] - Eo[i]) : 0.f;
                 const int r = r0 + i, j = t - r;
                 const int yj = valid[i] ? ys[j] : 0;
                 mxr[i] = 0.f;
@@ -543,7 +528,7 @@ __device__ void bwd_rec_stripe_wd(const KParams &P, int p, int si, const SmemWd 
                 for (int u = 0; u < 4; ++u) {
                     float b = 0.f;
                     if (valid[i]) {
-                        b = term[i] ? sm[L.chiE + 4 * qs + u] : aM[i][u] * sM + aI[i][u] * sI + aD[i][u] * sD;
+                        b = term[i] ? sm[L.chiE + 4 * qs + u] : acc[i][u];
                         mxr[i] = fmaxf(mxr[i], b * emit_g(P, eMg, eIg, eDg, 4 * qs + u, xr[i], yj));
                     }
                     bv[i][u] = b;

@@ -104,6 +104,27 @@ def test_batched_tkf92_forward_only(cuda_lib):
     np.testing.assert_allclose(lp, g['log_p'], rtol=LL_RTOL)
 
 
+def test_batched_tkf92_estep_bdi_statistics(cuda_lib):
+    """estep_batch_tkf92's full dict (log_p, BDI B/D/S, L, M, T, extension
+    counts) against the oracle E-step and its float64 epilogue."""
+    from pairhmm import api
+    from oracle import estep as oe, bdi as ob
+    g = load_golden('batch_tkf92_fwd')
+    lam, mu, ext = float(g['lam']), float(g['mu']), float(g['ext'])
+    r = api.estep_batch_tkf92(g['xs'], g['ys'], g['ts'], g['Lx'], g['Ly'], lam, mu, ext, g['Q'], g['pi'])
+    r = {k: v.cpu().numpy() for k, v in r.items()}
+    for b in range(len(g['ts'])):
+        x = np.asarray(g['xs'][b])[:int(g['Lx'][b])]
+        y = np.asarray(g['ys'][b])[:int(g['Ly'][b])]
+        p = {'ins_rate': lam, 'del_rate': mu, 't': float(g['ts'][b]), 'ext': ext, 'Q': g['Q'], 'pi': g['pi']}
+        ll, n, _ = oe.e_step('tkf92', p, x, y)
+        assert abs(r['log_p'][b] - ll) <= LL_RTOL * abs(ll)
+        want = ob.tkf92_epilogue(n, lam, mu, float(g['ts'][b]), ext)
+        for k, w in want.items():
+            assert abs(r[k][b] - w) <= CNT_RTOL * max(abs(w), 1.0), (k, b, r[k][b], w)
+        assert r['T'][b] == g['ts'][b]
+
+
 def test_empty_sequences(cuda_lib):
     from pairhmm import api
     g = load_golden('edges_tkf91')

@@ -526,8 +526,15 @@ def estep_batch_tkf92_forward_only(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu
 
 
 def estep_batch_tkf92(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, ext, Q, pi):
-    """Batched TKF92 E-step: {'log_p', 'n_chi_diag'} (the chi counts of
-    train/tkf92_svi_bw.py:263-334; its BDI statistics are a later epilogue)."""
+    """Batched TKF92 E-step (train/tkf92_svi_bw.py:263-334): dict of device
+    tensors 'log_p', 'B', 'D', 'S' (BDI statistics), 'L', 'M' (kappa
+    coefficients), 'T', 'ext_count', 'notext_count', 'n_chi_diag' [P,5,5]
+    and 'status'.  The DP runs on the GPU; the chi decomposition and the BDI
+    statistics are the float64 epilogue of pairhmm.bdi."""
+    from . import bdi
     plan, b = _tkf92_batch(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, ext, Q, pi)
     out = _lib.estep(plan, b)
-    return {'log_p': out['ll'], 'n_chi_diag': out['n_trans'], 'status': out['status']}
+    res = bdi.tkf92_bdi_epilogue(out['n_trans'], lam, mu, np.asarray(ts, np.float64), ext)
+    res.pop('n_trans_resolved')
+    res.update({'log_p': out['ll'], 'n_chi_diag': out['n_trans'], 'status': out['status']})
+    return res

@@ -177,12 +177,17 @@ def cpu_baseline(workload, seconds, forward_only, gpu_ll=None, gpu_n=None, threa
         cells_b = (len(workload.xs[b]) + 1) * (len(workload.ys[b]) + 1)
         if n == 0 and cells_b * N * N > 2e9:
             # one pair alone is far beyond the time budget: time its leading
-            # sub-rectangle (x[:a], y[:a]) instead, with ~2e9 / N^2 cells
-            a = max(8, int((2e9 / (N * N)) ** 0.5))
+            # a x a block (x[:a], y[:a]), a sized from a 16 x 16 calibration run
             from pairhmm.synth import Workload
-            sub = Workload(workload.name, workload.model, workload.params, [workload.xs[b][:a]],
-                           [workload.ys[b][:a]], workload.ts[b:b + 1], workload.K, workload.F, workload.C)
-            _oracle_pair(sub, 0, forward_only)
+            sub = lambda a: Workload(workload.name, workload.model, workload.params, [workload.xs[b][:a]],
+                                     [workload.ys[b][:a]], workload.ts[b:b + 1], workload.K, workload.F,
+                                     workload.C)
+            tc = time.perf_counter()
+            _oracle_pair(sub(16), 0, forward_only)
+            per_cell = (time.perf_counter() - tc) / 17 ** 2
+            a = int(max(16, min(len(workload.xs[b]), (seconds / per_cell) ** 0.5 - 1)))
+            t0 = time.perf_counter()
+            _oracle_pair(sub(a), 0, forward_only)
             done_cells += (a + 1) * (a + 1)
             n += 1
             truncated = a
@@ -278,11 +283,12 @@ def serving_leg(n_requests, rate, seed=0):
     models, reqs, offsets = synth.make_serving_stream(n_requests, rate=rate, seed=seed)
     gen_s = time.perf_counter() - t0
     served = [ServedModel(name, kind, p) for name, (kind, p) in models.items()]
+    ARENA = 48 << 30   # HBM arena of the request loop (workspaces, inputs, outputs)
     n_states = {'tkf92': 5, 'mixdom2_k3f1c1': 17, 'mixdom2_k4f2c2': 42}
     cs = float(sum((len(x) + 1) * (len(y) + 1) * n_states[m] for m, x, y, _ in reqs))
 
     def one(max_inflight, max_batch):
-        srv = Server(served, arena_bytes=8 << 30, max_inflight=max_inflight, max_batch=max_batch)
+        srv = Server(served, arena_bytes=ARENA, max_inflight=max_inflight, max_batch=max_batch)
         warm = [Request(-1 - i, m, x, y, t) for i, (m, x, y, t) in enumerate(reqs[:12])]
         for r in warm:
             srv.submit(r)
@@ -302,7 +308,7 @@ def serving_leg(n_requests, rate, seed=0):
                         'MixDom2 K3F1C1 (17) / MixDom2 K4F2C2 (42), ancestor LogUniform(20,2000)',
             'arrival_span_s': float(offsets[-1]), 'cell_states': cs,
             'continuous': cont, 'plain_one_launch_per_request': plain,
-            'arena_bytes': 8 << 30, 'stream_generation_s': gen_s}
+            'arena_bytes': ARENA, 'stream_generation_s': gen_s}
 
 
 def e2e_function(workload, w, api, torch):
@@ -473,8 +479,9 @@ def main():
            3: (('blk::forward_block_kernel', 2), ('blk::backward_block_kernel', 4), (None, 0)),
            4: (('warp2::forward_warp_kernel', 2), ('warp2::backward_rec_warp_kernel', 2),
                ('warp2::count_warp_kernel', 2)),
-           5: (('blk::forward_block_kernel', 2), ('blk::backward_rec_block_kernel', 2),
-               ('blk::count_block_kernel', 2))}[plan.last_variant]
+           5: (('blk::fwdbwd_block_kernel', 4), (None, 0), ('blk::count_block_kernel', 2)),
+           6: ((('wide::forward_wide_kernel', 2) if fwd_only else ('wide::fwdbwd_wide_kernel', 4)), (None, 0),
+               ('wide::count_wide_kernel', 2))}[plan.last_variant]
     durs = [fwd_avg, bwd_avg, cnt_avg]
     di = int(np.argmax(durs))
     dom, fpc = fam[di]

@@ -470,7 +470,9 @@ __device__ void fwd_stripe_b(const KParams &P, int p, int si, const SmemB &L, fl
             if (si + 1 == m.n_stripes) P.ll[p] = NEG_INF_LL;
         }
         if (tid == 0) cp_wait0();
+        __threadfence();
         bar_sync(BAR_STEP, NB * 32);
+        if (tid == 0) st_release(P.progress + m.stripe_base + si, Ly + 2);
         return;
     }
     // ---- log-likelihood: combine the per-quad partial sums of the terminal cell
@@ -496,7 +498,11 @@ __device__ void fwd_stripe_b(const KParams &P, int p, int si, const SmemB &L, fl
         else atomicOr(P.status + p, PHMM_ST_ZERO_LL);
         P.ll[p] = ll;
     }
+    // stripe complete (lattice and, for the last stripe, the log-likelihood):
+    // the count pass of the split E-step may start on it
+    __threadfence();
     bar_sync(BAR_STEP, NB * 32);
+    if (tid == 0) st_release(P.progress + m.stripe_base + si, Ly + 2);
 }
 
 template <class SH>

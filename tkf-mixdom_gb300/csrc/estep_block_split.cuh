@@ -237,7 +237,9 @@ __device__ void bwd_rec_stripe_b(const KParams &P, int p, int si, const SmemB &L
         }
         if (aborted) atomicOr(P.status + p, PHMM_ST_TIMEOUT);
     }
+    __threadfence();   // stripe complete: the count pass may start on it
     bar_sync(BAR_STEP, NB * 32);
+    if (tid == 0) st_release(prog_mine, Ly + 2);
 }
 
 // Both wavefronts of the split E-step in one persistent launch: the work list
@@ -333,8 +335,20 @@ __device__ void count_chunk_b(const KParams &P, int p, int si, int ch, const Sme
     const int T_last = (nrows - 1) + Ly;
     const int t0 = ch * CCHB;
     const int t_hi = min(T_last, t0 + CCHB - 1);
-    const double llv = P.ll[p];
-    if (!(llv > -1e29) || t0 > T_last) return;   // uniform over the CTA
+    if (t0 > T_last) return;
+    if (P.count_wait) {   // the wavefronts may still run: wait for the stripes read here
+        __shared__ int s_ok;
+        if (tid == 0) {
+            s_ok = count_ready(P, m, si) ? 1 : 0;
+            if (!s_ok) atomicOr(P.status + p, PHMM_ST_TIMEOUT);
+        }
+        __syncthreads();
+        const int ok = s_ok;
+        __syncthreads();
+        if (!ok) return;
+    }
+    const double llv = __ldcg(P.ll + p);
+    if (!(llv > -1e29)) return;   // uniform over the CTA
     const double lam = llv / LN2;
     const int Ep = (int)floor(lam);
     const float rfrac = (float)exp2(-(lam - floor(lam)));
@@ -401,10 +415,10 @@ __device__ void count_chunk_b(const KParams &P, int p, int si, int ch, const Sme
             fv[a] = make_float4(0.f, 0.f, 0.f, 0.f); bv[a] = fv[a]; sv[a] = fv[a];
             if (!valid || q >= NB) continue;
             // every quad of a valid cell is written (zero values with EXP_NONE)
-            Ef[a] = __ldg(P.lat_exp + cell * NBP + q);
-            Eb[a] = __ldg(P.blat_exp + cell * NBP + q);
-            fv[a] = __ldg(reinterpret_cast<const float4 *>(P.lat + cell * NS) + q);
-            bv[a] = __ldg(reinterpret_cast<const float4 *>(P.blat + cell * NS) + q);
+            Ef[a] = __ldcg(P.lat_exp + cell * NBP + q);
+            Eb[a] = __ldcg(P.blat_exp + cell * NBP + q);
+            fv[a] = __ldcg(reinterpret_cast<const float4 *>(P.lat + cell * NS) + q);
+            bv[a] = __ldcg(reinterpret_cast<const float4 *>(P.blat + cell * NS) + q);
             const int qt = P.quad_type[q];
             int64_t sc = -1;
             if (qt == T_I && hI) sc = latc + (int64_t)(t + 1) * ROWS + rho;
@@ -413,8 +427,8 @@ __device__ void count_chunk_b(const KParams &P, int p, int si, int ch, const Sme
             else if (qt == T_M && hM && (rho + 1 < nrows || has_below))
                 sc = rho + 1 < nrows ? latc + (int64_t)(t + 2) * ROWS + rho + 1 : latb + (int64_t)(j + 1) * ROWS;
             if (sc >= 0) {
-                Es[a] = __ldg(P.blat_exp + sc * NBP + q);
-                sv[a] = __ldg(reinterpret_cast<const float4 *>(P.blat + sc * NS) + q);
+                Es[a] = __ldcg(P.blat_exp + sc * NBP + q);
+                sv[a] = __ldcg(reinterpret_cast<const float4 *>(P.blat + sc * NS) + q);
             }
         }
     };

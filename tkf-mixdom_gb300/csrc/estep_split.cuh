@@ -240,7 +240,9 @@ __device__ void bwd_rec_stripe_w(const KParams &P, int p, int si, const SmemW &L
         atomicOr(P.status + p, PHMM_ST_TIMEOUT);
         if (has_above) st_release(prog_mine, Ly + 1);
     }
+    __threadfence();   // stripe complete: the count pass may start on it
     __syncwarp();
+    if (lane == 0) st_release(prog_mine, Ly + 2);
 }
 
 template <class SH>
@@ -308,8 +310,18 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
     const int t0 = ch * CCH;
     const int t_hi = min(T_last, t0 + CCH - 1);
     const int t_top = min(T_last, t_hi + 2);   // two steps of successor history first
-    const double llv = P.ll[p];
-    if (!(llv > -1e29) || t0 > T_last) return;   // uniform over the warp
+    if (t0 > T_last) return;
+    if (P.count_wait) {   // the wavefronts may still run: wait for the stripes read here
+        int ok = 1;
+        if (lane == 0) ok = count_ready(P, m, si) ? 1 : 0;
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) {
+            if (lane == 0) atomicOr(P.status + p, PHMM_ST_TIMEOUT);
+            return;
+        }
+    }
+    const double llv = __ldcg(P.ll + p);
+    if (!(llv > -1e29)) return;   // uniform over the warp
     const double lam = llv / LN2;
     const double Epd = floor(lam);
     const int Ep = (int)Epd;
@@ -414,11 +426,11 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
         bbE = EXP_NONE;
         if (lane == 31 && has_below && t >= t0 && jb >= 0 && jb <= Ly) {
             const int64_t cell = latb + (int64_t)jb * ROWS;
-            bbE = __ldg(P.blat_exp + cell);
+            bbE = __ldcg(P.blat_exp + cell);
             const float4 *src = reinterpret_cast<const float4 *>(P.blat + cell * SP);
 #pragma unroll
             for (int q = 0; q < SP / 4; ++q) {
-                const float4 v = __ldg(src + q);
+                const float4 v = __ldcg(src + q);
                 bbv[4 * q] = v.x; bbv[4 * q + 1] = v.y; bbv[4 * q + 2] = v.z; bbv[4 * q + 3] = v.w;
             }
         } else {

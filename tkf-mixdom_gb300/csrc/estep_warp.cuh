@@ -388,7 +388,11 @@ __device__ void fwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
             if (si + 1 == m.n_stripes) P.ll[p] = NEG_INF_LL;
         }
     }
+    // stripe complete (lattice and, for the last stripe, the log-likelihood):
+    // the count pass of the split E-step may start on it
+    __threadfence();
     __syncwarp();
+    if (lane == 0) st_release(prog_mine, Ly + 2);
 }
 
 template <class SH>

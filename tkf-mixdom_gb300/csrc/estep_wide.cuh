@@ -350,7 +350,11 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
             P.ll[p] = ll;
         }
     }
+    // stripe complete (lattice and, for the last stripe, the log-likelihood):
+    // the count pass may start on it
+    __threadfence();
     __syncthreads();
+    if (tid == 0) st_release(prog_mine, Ly + 2);
 }
 
 // ---------------------------------------------------------------- backward recursion
@@ -568,7 +572,9 @@ __device__ void bwd_rec_stripe_wd(const KParams &P, int p, int si, const SmemWd 
         if (has_above) { __threadfence(); st_release(prog_mine, Ly + 1); }
         if (aborted) atomicOr(P.status + p, PHMM_ST_TIMEOUT);
     }
+    __threadfence();   // stripe complete: the count pass may start on it
     __syncthreads();
+    if (tid == 0) st_release(prog_mine, Ly + 2);
 }
 
 __global__ void __launch_bounds__(512) fwdbwd_wide_kernel(const KParams P) {
@@ -636,8 +642,20 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
     const int64_t latc = m.lat_base + (int64_t)si * (RW + Ly) * RW;
     const int64_t latb = m.lat_base + (int64_t)(si + 1) * (RW + Ly) * RW;
     const int T_last = (nrows - 1) + Ly;
-    const double llv = P.ll[p];
-    if (!(llv > -1e29) || nsq <= 0) return;   // uniform over the CTA
+    if (nsq <= 0) return;
+    if (P.count_wait) {   // the wavefronts may still run: wait for the stripes read here
+        __shared__ int s_ok;
+        if (tid == 0) {
+            s_ok = count_ready(P, m, si) ? 1 : 0;
+            if (!s_ok) atomicOr(P.status + p, PHMM_ST_TIMEOUT);
+        }
+        __syncthreads();
+        const int ok = s_ok;
+        __syncthreads();
+        if (!ok) return;
+    }
+    const double llv = __ldcg(P.ll + p);
+    if (!(llv > -1e29)) return;   // uniform over the CTA
     const double lam = llv / LN2;
     const int Ep = (int)floor(lam);
     const float rfrac = (float)exp2(-(lam - floor(lam)));
@@ -681,12 +699,12 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
 #pragma unroll
         for (int a = 0; a < KQ; ++a) { Es[a] = EXP_NONE; sv[a] = make_float4(0.f, 0.f, 0.f, 0.f); bo[a] = sv[a]; }
         if (!valid) return;
-        Ef = __ldg(reinterpret_cast<const int *>(P.lat + cell * ES) + NS);
-        Eb = __ldg(reinterpret_cast<const int *>(P.blat + cell * ES) + NS);
+        Ef = __ldcg(reinterpret_cast<const int *>(P.lat + cell * ES) + NS);
+        Eb = __ldcg(reinterpret_cast<const int *>(P.blat + cell * ES) + NS);
 #pragma unroll
         for (int a = 0; a < FQ; ++a) {
             const int q = sq0 + sub + 16 * a;
-            if (q < sq1) fv[a] = __ldg(reinterpret_cast<const float4 *>(P.lat + cell * ES) + q);
+            if (q < sq1) fv[a] = __ldcg(reinterpret_cast<const float4 *>(P.lat + cell * ES) + q);
         }
         const bool hI = j + 1 <= Ly, hD = row + 1 <= Lx, hM = hI && hD;
         const bool below_ok = c + 1 < nrows || has_below;
@@ -694,7 +712,7 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
         for (int a = 0; a < KQ; ++a) {
             const int q = sub + 16 * a;
             if (q >= NQd) continue;
-            if (emis) bo[a] = __ldg(reinterpret_cast<const float4 *>(P.blat + cell * ES) + q);
+            if (emis) bo[a] = __ldcg(reinterpret_cast<const float4 *>(P.blat + cell * ES) + q);
             const int qt = P.quad_type[q];
             int64_t sc = -1;
             if (qt == T_I && hI) sc = latc + (int64_t)(t + 1) * RW + c;
@@ -703,8 +721,8 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
             else if (qt == T_M && hM && below_ok)
                 sc = c + 1 < nrows ? latc + (int64_t)(t + 2) * RW + c + 1 : latb + (int64_t)(j + 1) * RW;
             if (sc >= 0) {
-                Es[a] = __ldg(reinterpret_cast<const int *>(P.blat + sc * ES) + NS);
-                sv[a] = __ldg(reinterpret_cast<const float4 *>(P.blat + sc * ES) + q);
+                Es[a] = __ldcg(reinterpret_cast<const int *>(P.blat + sc * ES) + NS);
+                sv[a] = __ldcg(reinterpret_cast<const float4 *>(P.blat + sc * ES) + q);
             }
         }
     };
@@ -748,7 +766,7 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
                     int dp = Ef + Eb - Ep;
                     if (dp > 126) { dp = 126; atomicOr(P.status + p, PHMM_ST_SCALE_CLAMP); }
                     const float ps = warp2::scale_pow2(rfrac, max(dp, -200));
-                    const float4 f4 = __ldg(reinterpret_cast<const float4 *>(P.lat + (latc + (int64_t)t * RW + c) * ES) + q);
+                    const float4 f4 = __ldcg(reinterpret_cast<const float4 *>(P.lat + (latc + (int64_t)t * RW + c) * ES) + q);
                     const float pk[4] = {f4.x * bo[a].x * ps, f4.y * bo[a].y * ps, f4.z * bo[a].z * ps, f4.w * bo[a].w * ps};
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
@@ -768,7 +786,7 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
                 for (int s = sub; s < NS; s += 16) {
                     const int os = P.slot_orig[s];
                     if (os < 0) continue;
-                    const float f = __ldg(P.lat + (latc + (int64_t)t * RW + c) * ES + s);
+                    const float f = __ldcg(P.lat + (latc + (int64_t)t * RW + c) * ES + s);
                     const double v = (double)f * (double)__ldg(chi + os * N + P.e_idx) * fs;
                     if (v != 0.0) atomicAdd(P.n_trans + ((int64_t)p * N + os) * N + P.e_idx, v);
                 }

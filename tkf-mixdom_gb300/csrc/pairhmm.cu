@@ -86,9 +86,10 @@ struct KParams {
     int *lat_exp;
     float *blat;                        // split E-step: backward lattice
     int *blat_exp;
-    int *bprogress;                     // split block E-step: backward edge pipeline
+    int *bprogress;                     // split E-step: backward edge pipeline
     float *bedge;
     int *bedge_exp;
+    int count_wait;                     // count pass waits for the stripes it reads
     float *edge;
     int *edge_exp;
     int *progress;
@@ -166,6 +167,20 @@ __device__ bool wait_geq(const int *p, int need, long long limit) {
         __nanosleep(128);
     }
     return true;
+}
+
+// The split E-step's count pass runs while the wavefronts still run: an item
+// of stripe si of pair m may start once that stripe is complete in both
+// directions, the stripe below in the backward one (its first row is read),
+// and the pair's last forward stripe (the log-likelihood).  Wavefronts publish
+// completion as progress value Ly + 2.  Bounded like every other wait.
+__device__ bool count_ready(const KParams &P, const PairMeta &m, int si) {
+    const int done = m.Ly + 2;
+    const int *f = P.progress + m.stripe_base, *b = P.bprogress + m.stripe_base;
+    if (!wait_geq(f + si, done, P.spin_limit)) return false;
+    if (!wait_geq(b + si, done, P.spin_limit)) return false;
+    if (si + 1 < m.n_stripes && !wait_geq(b + si + 1, done, P.spin_limit)) return false;
+    return wait_geq(f + m.n_stripes - 1, done, P.spin_limit);
 }
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
@@ -870,7 +885,7 @@ struct phmm_plan {
     float *bedge = nullptr; size_t bedge_cap = 0;
     int *bedge_exp = nullptr; size_t bedgeE_cap = 0;
     // split E-step: one side stream (+ fork / join events) per caller stream
-    struct Side { cudaStream_t user, side; cudaEvent_t fork, join; };
+    struct Side { cudaStream_t user, side, side2; cudaEvent_t fork, join, join2; };
     std::vector<Side> sides;
     std::vector<PairMeta> h_meta;
     std::vector<int2> h_items;
@@ -956,10 +971,37 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // The split E-step: forward on the caller's stream and backward recursion on
 // a side stream at the same time, then the count pass once both are done.
+// side streams (and fork / join events) of one caller stream, created once
+int get_side(phmm_plan *plan, cudaStream_t stream, phmm_plan::Side **out) {
+    for (auto &e : plan->sides)
+        if (e.user == stream) { *out = &e; return 0; }
+    phmm_plan::Side e{stream, nullptr, nullptr, nullptr, nullptr, nullptr};
+    CUDA_TRY(cudaStreamCreateWithFlags(&e.side, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&e.side2, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&e.fork, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&e.join, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&e.join2, cudaEventDisableTiming));
+    plan->sides.push_back(e);
+    *out = &plan->sides.back();
+    return 0;
+}
+
 int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int n_items, int n_citems, int stripes,
                  int max_ly, void *d_items, int *d_counters, int *d_progress, float *d_bedge, int *d_bedge_exp,
                  cudaStream_t stream) {
     int rc;
+    phmm_plan::Side *sd = nullptr;
+    if ((rc = get_side(plan, stream, &sd))) return rc;
+    // the count pass of the warp kernels (second side stream) overlaps the
+    // wavefronts: its items wait for the stripes they read and its grid takes
+    // half the resident slots (one-warp CTAs, so the wavefronts keep room)
+    KParams C = K;
+    C.items = (const int2 *)d_items + 2 * n_items;
+    C.n_items = n_citems;
+    C.counter = d_counters + 2;
+    C.progress = d_progress;
+    C.bprogress = d_progress + stripes;
+    C.count_wait = 1;
     if (combined) {
         // one persistent launch pops forward and backward stripes from one list
         KParams FB = K;
@@ -970,6 +1012,9 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
         FB.bprogress = d_progress + stripes;
         FB.bedge = d_bedge;
         FB.bedge_exp = d_bedge_exp;
+        // the count pass follows on the same stream: a 256-thread count CTA
+        // holds half an SM's registers, so count CTAs waiting beside the
+        // wavefront kernel could crowd it out of the SMs
         if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
         if ((rc = wl(plan, FB, 2 * n_items, max_ly, 4, stream))) return rc;
         if (plan->timing) {
@@ -977,10 +1022,7 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
             CUDA_TRY(cudaEventRecord(plan->ev[2], stream));
             CUDA_TRY(cudaEventRecord(plan->ev[3], stream));
         }
-        KParams C = K;
-        C.items = (const int2 *)d_items + 2 * n_items;
-        C.n_items = n_citems;
-        C.counter = d_counters + 2;
+        C.count_wait = 0;
         if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[4], stream));
         if ((rc = wl(plan, C, n_citems, max_ly, 3, stream))) return rc;
         if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[5], stream));
@@ -989,19 +1031,9 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
         plan->timed_count = true;
         return 0;
     }
-    phmm_plan::Side *sd = nullptr;
-    for (auto &e : plan->sides)
-        if (e.user == stream) { sd = &e; break; }
-    if (!sd) {
-        phmm_plan::Side e{stream, nullptr, nullptr, nullptr};
-        CUDA_TRY(cudaStreamCreateWithFlags(&e.side, cudaStreamNonBlocking));
-        CUDA_TRY(cudaEventCreateWithFlags(&e.fork, cudaEventDisableTiming));
-        CUDA_TRY(cudaEventCreateWithFlags(&e.join, cudaEventDisableTiming));
-        plan->sides.push_back(e);
-        sd = &plan->sides.back();
-    }
     CUDA_TRY(cudaEventRecord(sd->fork, stream));
     CUDA_TRY(cudaStreamWaitEvent(sd->side, sd->fork, 0));
+    CUDA_TRY(cudaStreamWaitEvent(sd->side2, sd->fork, 0));
     // forward (caller's stream)
     KParams F = K;
     F.items = (const int2 *)d_items;
@@ -1032,15 +1064,16 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
     if (rc) return rc;
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[3], sd->side));
     CUDA_TRY(cudaEventRecord(sd->join, sd->side));
+    // counts from both lattices (second side stream, overlapping the wavefronts)
+    plan->grid_div = 2;
+    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[4], sd->side2));
+    rc = wl(plan, C, n_citems, max_ly, 3, sd->side2);
+    plan->grid_div = 1;
+    if (rc) return rc;
+    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[5], sd->side2));
+    CUDA_TRY(cudaEventRecord(sd->join2, sd->side2));
     CUDA_TRY(cudaStreamWaitEvent(stream, sd->join, 0));
-    // counts from both lattices (caller's stream)
-    KParams C = K;
-    C.items = (const int2 *)d_items + 2 * n_items;
-    C.n_items = n_citems;
-    C.counter = d_counters + 2;
-    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[4], stream));
-    if ((rc = wl(plan, C, n_citems, max_ly, 3, stream))) return rc;
-    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[5], stream));
+    CUDA_TRY(cudaStreamWaitEvent(stream, sd->join2, 0));
     plan->launches += 3;
     plan->timed_bwd = true;
     plan->timed_count = true;
@@ -1099,9 +1132,9 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     const int n_items = (int)fw.size();
     if (estep) {
         for (int i = 0; i < n_items; ++i) { plan->h_items.push_back(fw[i]); plan->h_items.push_back(bw[i]); }
-        for (int p : order)
-            for (int s = 0; s < plan->h_meta[p].n_stripes; ++s)
-                for (int h = 0; h < wide::SPL; ++h) plan->h_items.push_back(make_int2(p, (s << 4) | h));
+        for (auto it = order.rbegin(); it != order.rend(); ++it)   // shortest pairs first (ready first)
+            for (int s = 0; s < plan->h_meta[*it].n_stripes; ++s)
+                for (int h = 0; h < wide::SPL; ++h) plan->h_items.push_back(make_int2(*it, (s << 4) | h));
     } else {
         plan->h_items = fw;
     }
@@ -1198,7 +1231,9 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     K.F_log = K.B_log = K.post = nullptr;
     K.max_ly = max_ly;
     K.spin_limit = 40LL * 1000 * 1000;
-    // ---- wavefronts
+    // ---- wavefronts, then the count pass (both on the caller's stream: a wide
+    // wavefront CTA needs most of an SM's shared memory, so a count CTA waiting
+    // beside it would only take its place)
     {
         K.items = (const int2 *)d_items;
         K.n_items = n_fb;
@@ -1226,6 +1261,7 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         K.items = (const int2 *)d_items + n_fb;
         K.n_items = n_citems;
         K.counter = d_counters + 2;
+        K.count_wait = 0;
         const int bytes = wide::make_smem_wc(NS, KS, K.kend[0] - K.kbeg[0], K.kend[1] - K.kbeg[1],
                                              K.kend[2] - K.kbeg[2]).bytes;
         CUDA_TRY(cudaFuncSetAttribute(wide::count_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
@@ -1339,8 +1375,9 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
         for (int p : order)
             for (int s = plan->h_meta[p].n_stripes - 1; s >= 0; --s) plan->h_items.push_back(make_int2(p, s));
     int n_citems = 0;
-    if (split) {   // count chunks: (pair, stripe << 12 | chunk)
-        for (int p : order) {
+    if (split) {   // count chunks: (pair, stripe << 12 | chunk), shortest pairs first (ready first)
+        for (auto it = order.rbegin(); it != order.rend(); ++it) {
+            const int p = *it;
             const PairMeta &m = plan->h_meta[p];
             for (int s = 0; s < m.n_stripes; ++s) {
                 const int nrows = std::min(rows, m.Lx + 1 - s * rows);
@@ -1752,7 +1789,9 @@ void phmm_plan_destroy(phmm_plan *plan) {
     for (auto &e : plan->sides) {
         cudaEventDestroy(e.fork);
         cudaEventDestroy(e.join);
+        cudaEventDestroy(e.join2);
         cudaStreamDestroy(e.side);
+        cudaStreamDestroy(e.side2);
     }
     cudaFree(plan->blat);
     cudaFree(plan->blat_exp);

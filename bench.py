@@ -236,7 +236,7 @@ def run_reference(args, rank, ws):
     sample, cells = [], 0
     from pairhmm.synth import Workload
     N = w.n_states
-    a = max(8, int((2e9 / (N * N)) ** 0.5))   # pairs above ~2e9 FLOP are timed on their leading a x a block
+    a = max(8, int((4e7 / (N * N)) ** 0.5))   # pairs above ~2e9 FLOP are timed on their leading a x a block
     for b in order:
         x, y = w.xs[b], w.ys[b]
         if (len(x) + 1) * (len(y) + 1) * N * N > 2e9:

@@ -378,7 +378,7 @@ __device__ void fwd_stripe_b(const KParams &P, int p, int si, const SmemB &L, fl
                 cp_commit();
                 fetched = t + 2;
             }
-            pv = ld_acquire(prog_above);
+            if (pv <= t + 2) pv = ld_acquire(prog_above);   // only when the next prefetch needs more
         }
         // ---- my quad for both cells: predecessors, then one merged contraction
         const float *pvp[R];
@@ -650,7 +650,7 @@ __device__ void bwd_stripe_b(const KParams &P, int p, int si, const SmemB &L, fl
                     cp_commit();
                     fetched = jh - 1;
                 }
-                pv = ld_acquire(prog_below);
+                if (pv < Ly + 3 - jh) pv = ld_acquire(prog_below);   // only when the next prefetch needs more
             }
 #pragma unroll
             for (int c = 0; c < R; ++c) {

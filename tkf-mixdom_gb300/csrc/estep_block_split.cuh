@@ -113,7 +113,7 @@ __device__ void bwd_rec_stripe_b(const KParams &P, int p, int si, const SmemB &L
                 cp_commit();
                 fetched = jh - 1;
             }
-            pv = ld_acquire(prog_below);
+            if (pv < Ly + 3 - jh) pv = ld_acquire(prog_below);   // only when the next prefetch needs more
         }
         if (tid == 0) misc[(k + 1) & 1] = 0;   // every warp read it two barriers ago
         // ---- successor vectors of both cells (the zero vector when one does not exist)

@@ -233,7 +233,7 @@ __device__ void bwd_rec_stripe_w(const KParams &P, int p, int si, const SmemW &L
                 hxE = __ldcg(edgeE_below + jb - 1);
                 hx_col = jb - 1;
             }
-            pv = ld_acquire(prog_below);
+            if (pv < Ly + 3 - jb) pv = ld_acquire(prog_below);   // only when the next prefetch needs more
         }
     }
     if (aborted && lane == 0) {

@@ -378,7 +378,9 @@ __device__ void fwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
                 hxE = __ldcg(edgeE_above + t + 1);
                 hx_col = t + 1;
             }
-            pv = ld_acquire(prog_above);
+            // poll the stripe above only when its last known progress does not
+            // cover the next prefetch (an acquire load per step is costly)
+            if (pv <= t + 2) pv = ld_acquire(prog_above);
         }
     }
     if (aborted) {
@@ -775,7 +777,7 @@ __device__ void bwd_stripe_w(const KParams &P, int p, int si, const SmemW &L, fl
                 hxE = __ldcg(edgeE_below + jb - 1);
                 hx_col = jb - 1;
             }
-            pv = ld_acquire(prog_below);
+            if (pv < Ly + 3 - jb) pv = ld_acquire(prog_below);   // only when the next prefetch needs more
         }
     }
     asm volatile("cp.async.wait_all;" ::: "memory");

@@ -103,7 +103,9 @@ def bdi_stats(n_trans, ins_rate, del_rate, t, T=None):
 def tkf92_resolve(n_chi, ins_rate, del_rate, t, ext):
     """TKF92 chi counts [B, 5, 5] -> (resolved counts, ext_count, notext_count)."""
     n = pm._t(n_chi)
-    tau = pm.tkf92_trans(ins_rate, del_rate, pm._t(t, device=n.device).reshape(-1), ext).to(n.device)
+    # tau is built on the host from plain scalars; only the result moves to n's device
+    tau = pm.tkf92_trans(pm._t(float(ins_rate)), pm._t(float(del_rate)),
+                         pm._t(t).reshape(-1).cpu(), float(ext)).to(n.device)
     diag = torch.stack([tau[:, M, M], tau[:, I, I], tau[:, D, D]], dim=-1)
     frac = torch.where(diag > 1e-30, float(ext) / torch.clamp(diag, min=1e-30), torch.zeros_like(diag))
     frac = torch.clamp(frac, 0.0, 1.0)

@@ -49,7 +49,13 @@ WORKLOADS = {
         'forward_only': True, 'metric': 'pair-HMM forward cell-state updates/s',
         'model': 'TKF91', 'e2e_api': 'pairhmm.api.estep_batch_tkf92_forward_only (ext = 0)'},
 }
-PROFILE_SUMMARY = os.path.join(ROOT, 'profiles', 'estep_kernels_mixdom2_k3f1c1.md')
+# ncu summaries holding 'traffic_bytes_per_launch_full_workload[<kernel>]: <bytes>' lines
+PROFILE_SUMMARY = {
+    'mixdom2_k3f1c1_200pairs_len30-600': 'estep_kernels_mixdom2_k3f1c1.md',
+    'mixdom2_k4f2c2_32pairs_len200-1500': 'estep_kernels_mixdom2_k4f2c2.md',
+    'mixdom2_k8f4c4_64pairs_len2000': 'estep_kernels_mixdom2_k8f4c4.md',
+    'tkf91_64pairs_len50-150': 'forward_kernels_tkf91.md',
+}
 SMS = 152
 FP32_LANES_PER_SM = 128
 
@@ -65,6 +71,8 @@ def parse_args():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--pairs', type=int, default=0,
                     help='use only the first P pairs (small case for ncu captures)')
+    ap.add_argument('--max-len', type=int, default=0,
+                    help='truncate every sequence to at most L residues (small case for ncu captures)')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--serving-requests', type=int, default=2000,
                     help='requests in the serving-stream leg (0: skip it)')
@@ -87,13 +95,14 @@ def measured_peaks():
         return {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0, 'sm_max_mhz': 2070.0}, 'fallback'
 
 
-def profile_traffic():
-    """dram bytes per launch of the dominant kernel from the committed ncu summary."""
+def profile_traffic(workload, kernel):
+    """dram bytes per launch of `kernel` on `workload` from the committed ncu summary."""
+    key = f'traffic_bytes_per_launch_full_workload[{kernel.split("::")[-1]}]:'
     try:
-        for line in open(PROFILE_SUMMARY):
-            if line.startswith('traffic_bytes_per_launch_full_workload:'):
-                return float(line.split(':', 1)[1].split()[0])
-    except (OSError, ValueError):
+        for line in open(os.path.join(ROOT, 'profiles', PROFILE_SUMMARY[workload])):
+            if line.startswith(key):
+                return float(line[len(key):].split()[0])
+    except (OSError, ValueError, KeyError):
         pass
     return None
 
@@ -360,6 +369,9 @@ def main():
     w = synth.CONFIGS[args.workload](seed=rank)
     if args.pairs:
         w.xs, w.ys, w.ts = w.xs[:args.pairs], w.ys[:args.pairs], w.ts[:args.pairs]
+    if args.max_len:
+        w.xs = [x[:args.max_len] for x in w.xs]
+        w.ys = [y[:args.max_len] for y in w.ys]
     spec = WORKLOADS[args.workload]
     fwd_only = spec['forward_only']
     N = w.n_states
@@ -483,21 +495,24 @@ def main():
            6: ((('wide::forward_wide_kernel', 2) if fwd_only else ('wide::fwdbwd_wide_kernel', 4)), (None, 0),
                ('wide::count_wide_kernel', 2))}[plan.last_variant]
     durs = [fwd_avg, bwd_avg, cnt_avg]
-    di = int(np.argmax(durs))
+    # the overlapped count pass (variant 4) starts with the wavefronts and waits
+    # on their progress, so its event span is not its own duration
+    overlapped = plan.last_variant == 4
+    di = int(np.argmax(durs[:2] if overlapped else durs))
     dom, fpc = fam[di]
-    is_bwd = di == 1
     flop = fpc * N * N * total_cells
     dur = durs[di]
     achieved = flop / (dur / 1e3) / 1e12
     fp32_peak = SMS * FP32_LANES_PER_SM * 2 * peaks.get('sm_max_mhz', 2070.0) * 1e6 / 1e12
     roofline = {'bound': 'fp32', 'kernel': dom, 'achieved': achieved, 'peak': fp32_peak,
                 'unit': 'TFLOP/s', 'frac': achieved / fp32_peak,
-                'traffic': profile_traffic(),
+                'traffic': profile_traffic(args.workload, dom),
                 'peak_source': f'{SMS} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 FLOP x sm_max_mhz '
                                f'({peaks.get("sm_max_mhz")} MHz, {src} MEASURED_PEAKS.json); '
                                'the DP is a dense FP32 CUDA-core contraction: no tensor-core or HBM bound',
                 'flop_per_cell': fpc * N * N,
                 'fwd_kernel_ms': fwd_avg, 'bwd_kernel_ms': bwd_avg, 'count_kernel_ms': cnt_avg,
+                'count_overlaps_wavefronts': overlapped,
                 'kernels': [f[0] for f in fam if f[0]],
                 'hbm_peak_gbs': peaks.get('hbm_gbs')}
     serving = None

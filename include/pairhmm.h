@@ -169,6 +169,53 @@ int phmm_estep_static(const phmm_model_desc *model, const phmm_batch *batch,
                       double *ll_out, double *n_trans, double *cnt_M, double *cnt_I,
                       double *cnt_D, int32_t *status_out, void *stream);
 
+/* MixDom2 parameters (host float64 arrays), the parameter pytree of the
+ * reference's MixDom2 model (models/mixdom.py:52-77, train/likelihood.py:143-190):
+ * main_ins / main_del, dom_ins / dom_del / dom_weights [K], frag_weights
+ * [K][F], ext_rates [K][F][F] (fragment f to g extension; a [K][F] vector
+ * is its diagonal), class_pis [C][A], class_S_exch [C][A][A] (symmetric
+ * exchangeabilities), classdist [K][F][C]. */
+typedef struct phmm_mixdom2_params {
+    int32_t n_dom, n_frag, n_classes, alphabet;   /* K, F, C, A (A = 20) */
+    double main_ins, main_del;
+    const double *dom_ins, *dom_del, *dom_weights;
+    const double *frag_weights;
+    const double *ext_rates;
+    const double *class_pis;
+    const double *class_S_exch;
+    const double *classdist;
+} phmm_mixdom2_params;
+
+/* Device prologue of the MixDom2 E-step: from the parameters and per-pair
+ * times t (device [P] float64) write each pair's collapsed transition matrix
+ * chi (device float32 [P][N][N], N = 2 + 5KF), its emission tables
+ * (emit_M float32 [P][KF][21][21], emit_I / emit_D [P][KF][21], the layout
+ * phmm_batch takes with chi_per_pair = emit_per_pair = 1) and the class
+ * substitution matrices P_c(t) = expm(t Q_c) (device float64 [P][C][A][A],
+ * phmm_mixdom2_class_subs_count doubles).  Replaces the per-pair builders
+ * the reference runs inside its E-step (models/mixdom.py:104-423 via
+ * train/likelihood.py:143-190; core/ctmc.py:31-60; dp/hmm.py:673-783).
+ * Requires K*F <= 33; stream-ordered; allocates nothing. */
+size_t phmm_mixdom2_class_subs_count(const phmm_mixdom2_params *prm, int32_t n_pairs);
+int phmm_mixdom2_tables(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t,
+                        float *chi, float *emit_M, float *emit_I, float *emit_D,
+                        double *class_subs, void *stream);
+
+/* Device epilogue of the MixDom2 E-step: the per-class sufficient statistics
+ * of train/likelihood.py:279-344 from phmm_estep's per-group character
+ * counts (cnt_M [P][KF][21][21], cnt_I / cnt_D [P][KF][21]) and the
+ * class_subs phmm_mixdom2_tables wrote.  Outputs (device float64):
+ * class_match [P][C][20][20], class_insert / class_delete [P][C][20],
+ * classdist_counts [P][K][F][C].  The class posterior of a cell depends on
+ * it only through its characters, so no lattice-sized joint is formed;
+ * character 20 (wildcard) reads the class factors of character 19 (the
+ * reference's clamped gather) and is left out of the character-indexed
+ * outputs.  At most 8 classes. */
+int phmm_mixdom2_class_counts(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *class_subs,
+                              const double *cnt_M, const double *cnt_I, const double *cnt_D,
+                              double *class_match, double *class_insert, double *class_delete,
+                              double *classdist_counts, void *stream);
+
 /* Per-kernel CUDA-event timing on the launching stream (diagnostics and
  * benchmarking; no counterpart in the reference, which has no kernels).
  * phmm_kernel_times waits for the last call's events and returns the forward
@@ -178,7 +225,9 @@ int phmm_set_timing(phmm_plan *plan, int enable);
 int phmm_kernel_times(phmm_plan *plan, float *fwd_ms, float *bwd_ms);
 /* Device time of one kernel of the last timed call: which = 0 forward,
  * 1 backward (fused backward + counts, or the backward recursion of the
- * split E-step), 2 the split E-step's count pass (0 when it did not run). */
+ * split E-step), 2 the split E-step's count pass (0 when it did not run).
+ * A call that ran in groups (a batch larger than free memory) reports each
+ * kernel's time summed over its groups. */
 int phmm_kernel_time(phmm_plan *plan, int which, float *ms);
 
 /* Kernel family: 0 = automatic (default), 1 = generic kernels (any state

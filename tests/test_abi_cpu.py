@@ -12,7 +12,7 @@ from conftest import ROOT
 def declared_symbols():
     src = open(os.path.join(ROOT, 'include', 'pairhmm.h')).read()
     src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
-    return sorted(set(re.findall(r'\b(phmm_[a-z_]+)\s*\(', src)))
+    return sorted(set(re.findall(r'\b(phmm_[a-z0-9_]+)\s*\(', src)))
 
 
 @pytest.fixture(scope='module')
@@ -46,3 +46,25 @@ def test_version_and_error_reporting(lib):
     desc = _lib.ModelDesc(3, (ctypes.c_int8 * 3)(0, 1, 2), None, 1)
     assert lib.phmm_plan_create(ctypes.byref(desc), ctypes.byref(h)) == -1
     assert 'End' in _lib.last_error()
+
+
+def test_mixdom2_prologue_rejects_bad_shapes(lib):
+    """phmm_mixdom2_tables checks the parameter shapes before any CUDA call."""
+    import ctypes
+    import numpy as np
+    from pairhmm import _lib
+    K, F, C = 8, 5, 1
+    arrs = [np.ones(n) for n in (K, K, K, K * F, K * F * F, C * 20, C * 400, K * F * C)]
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    prm = _lib.MixDom2Params(K, F, C, 20, 0.03, 0.04, *[dp(a) for a in arrs])
+    null = ctypes.c_void_p(0)
+    assert lib.phmm_mixdom2_tables(ctypes.byref(prm), 4, *([null] * 7)) == -1
+    assert '33' in _lib.last_error()
+    prm = _lib.MixDom2Params(2, 1, 1, 4, 0.03, 0.04, *[dp(a) for a in arrs])
+    assert lib.phmm_mixdom2_tables(ctypes.byref(prm), 4, *([null] * 7)) == -1
+    assert 'alphabet' in _lib.last_error()
+    prm = _lib.MixDom2Params(2, 1, 1, 20, 0.03, 0.04, *[dp(a) for a in arrs])
+    assert lib.phmm_mixdom2_tables(ctypes.byref(prm), 4, *([null] * 7)) == -1
+    assert 'null device buffer' in _lib.last_error()
+    assert lib.phmm_mixdom2_tables(ctypes.byref(prm), 0, *([null] * 7)) == 0
+    assert lib.phmm_mixdom2_class_subs_count(ctypes.byref(prm), 10) == 10 * 400

@@ -867,6 +867,9 @@ int fail(int code, const std::string &msg) {
 
 }  // namespace
 
+// error channel shared with the other translation units of the library
+extern "C" __attribute__((visibility("hidden"))) void phmm_internal_set_error(const char *msg) { g_err = msg; }
+
 struct phmm_plan {
     KParams base;
     int sm_count = 0;
@@ -894,6 +897,9 @@ struct phmm_plan {
     bool timed_bwd = false;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     bool timed_count = false;
+    // a call that ran in groups (batch larger than free memory): summed per-kernel times
+    bool grouped = false;
+    float group_ms[3] = {0.f, 0.f, 0.f};
     // register-resident warp kernels for this state space (null: generic kernels)
     int w_nm = 0, w_ni = 0, w_nd = 0;
     int grid_div = 1;       // persistent grids use 1/grid_div of the resident slots
@@ -1289,6 +1295,7 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     if (!plan || !b) return fail(PHMM_E_ARG, "null plan or batch");
     cudaStream_t stream = (cudaStream_t)stream_;
     if (!ws_need) plan->launches = 0;
+    plan->grouped = false;
     const int P_ = b->n_pairs;
     if (P_ < 0) return fail(PHMM_E_ARG, "n_pairs < 0");
     if (ws_need) *ws_need = 0;
@@ -1611,6 +1618,8 @@ int run_groups(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, dou
         return run(plan, b, estep, ll, n_trans, cntM, cntI, cntD, status, nullptr, nullptr, nullptr, stream);
     const int N = plan->base.N, G = plan->base.G;
     int launches = 0, p0 = 0;
+    float acc[3] = {0.f, 0.f, 0.f};
+    bool any_bwd = false, any_count = false;
     while (p0 < b->n_pairs) {
         // the largest contiguous group from p0 that fits the budget (at least one pair)
         int lo = 1, hi = b->n_pairs - p0;
@@ -1641,9 +1650,26 @@ int run_groups(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, dou
                  estep ? cntD + (int64_t)p0 * G * 21 : nullptr, status + p0, nullptr, nullptr, nullptr, stream);
         if (rc) return rc;
         launches += plan->launches;
+        if (plan->timing) {   // each group's events are re-recorded by the next group: read them now
+            for (int w = 0; w < 3; ++w) {
+                if ((w == 1 && !plan->timed_bwd) || (w == 2 && !plan->timed_count)) continue;
+                float ms = 0.f;
+                CUDA_TRY(cudaEventSynchronize(plan->ev[2 * w + 1]));
+                CUDA_TRY(cudaEventElapsedTime(&ms, plan->ev[2 * w], plan->ev[2 * w + 1]));
+                acc[w] += ms;
+            }
+            any_bwd |= plan->timed_bwd;
+            any_count |= plan->timed_count;
+        }
         p0 += lo;
     }
     plan->launches = launches;
+    if (plan->timing) {
+        plan->grouped = true;
+        plan->timed_bwd = any_bwd;
+        plan->timed_count = any_count;
+        for (int w = 0; w < 3; ++w) plan->group_ms[w] = acc[w];
+    }
     return 0;
 }
 
@@ -1762,6 +1788,7 @@ int phmm_kernel_time(phmm_plan *plan, int which, float *ms) {
     if (!plan || !plan->timing) return fail(PHMM_E_ARG, "timing is not enabled on this plan");
     if (!ms || which < 0 || which > 2) return fail(PHMM_E_ARG, "bad kernel index");
     if ((which == 1 && !plan->timed_bwd) || (which == 2 && !plan->timed_count)) { *ms = 0.f; return 0; }
+    if (plan->grouped) { *ms = plan->group_ms[which]; return 0; }
     CUDA_TRY(cudaEventSynchronize(plan->ev[2 * which + 1]));
     CUDA_TRY(cudaEventElapsedTime(ms, plan->ev[2 * which], plan->ev[2 * which + 1]));
     return 0;
@@ -1770,6 +1797,11 @@ int phmm_kernel_time(phmm_plan *plan, int which, float *ms) {
 int phmm_kernel_times(phmm_plan *plan, float *fwd_ms, float *bwd_ms) {
     if (!plan || !plan->timing) return fail(PHMM_E_ARG, "timing is not enabled on this plan");
     float a = 0.f, b = 0.f;
+    if (plan->grouped) {
+        if (fwd_ms) *fwd_ms = plan->group_ms[0];
+        if (bwd_ms) *bwd_ms = plan->timed_bwd ? plan->group_ms[1] : 0.f;
+        return 0;
+    }
     CUDA_TRY(cudaEventSynchronize(plan->ev[1]));
     CUDA_TRY(cudaEventElapsedTime(&a, plan->ev[0], plan->ev[1]));
     if (plan->timed_bwd) {

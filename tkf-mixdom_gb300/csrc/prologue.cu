@@ -1,0 +1,609 @@
+// prologue.cu -- device builders of the MixDom2 E-step inputs, per pair time t.
+//
+// The reference builds these inside its jitted E-step for every pair
+// (train/likelihood.py:143-373 calls models/mixdom.py:104-423 for the
+// collapsed transition matrix chi, core/ctmc.py:31-60 / train/vjp.py:463-510
+// for P_c(t) = expm(t Q_c), and dp/hmm.py:673-783 for the per-class mixture
+// emission tables).  Here three launches do the same for a whole batch:
+//
+//   chi_kernel     one CTA per pair: TKF91 matrices of the main level and of
+//                  every domain (core/bdi.py:40-99 with its lambda ~ mu
+//                  branches), the null-domain closure (I - T_nn)^-1 applied
+//                  from the left by T_Nnull (one Gauss-Jordan solve with five
+//                  right-hand sides), T_exit_k, the effective 5x5 T, and the
+//                  N x N collapsed matrix written as float32;
+//   expm_kernel    one CTA per (pair, class): Q_c from (S_exch, pi), then
+//                  exp(t Q_c) by scaling and squaring with the degree-13 Pade
+//                  approximant of Higham, "The scaling and squaring method
+//                  for the matrix exponential revisited", SIAM J. Matrix
+//                  Anal. Appl. 26 (2005), Algorithm 2.3 (the method
+//                  jax.scipy.linalg.expm implements), float64;
+//   tables_kernel  one CTA per pair: EM[g][a][b] = sum_c w[g][c]
+//                  max(pi_c[a],1e-30) max(P_c[a][b],1e-30), EI = ED =
+//                  sum_c w[g][c] max(pi_c[a],1e-30), wildcard factor 1.
+//
+// All arithmetic is float64; chi and the tables are rounded to float32 once,
+// as the E-step consumes them.
+#include "pairhmm.h"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+extern "C" __attribute__((visibility("hidden"))) void phmm_internal_set_error(const char *msg);
+
+namespace pro {
+
+constexpr int S = 0, M = 1, I = 2, D = 3, E = 4;
+constexpr int NA = 20;                 // alphabet (residues 0..19)
+constexpr int MAXV = 3960;             // doubles of the by-value parameter block
+constexpr int MAXK = 33;               // K*F <= 33 keeps N <= 167
+constexpr int THREADS = 256;
+
+// Parameter block passed by value (kernel parameters hold up to 32 KB).
+struct Packed {
+    int K, F, C;
+    int o_dins, o_ddel, o_dw, o_fw, o_ext, o_pis, o_S, o_cd;
+    double main_ins, main_del;
+    double v[MAXV];
+};
+
+__device__ __constant__ int UV_U[5] = {M, M, M, I, D};
+__device__ __constant__ int UV_X[5] = {M, I, D, I, D};
+__device__ __constant__ int MID[3] = {M, I, D};
+
+// ---------------------------------------------------------------- TKF BDI (core/bdi.py:40-99)
+__device__ double tkf_beta(double lam, double mu, double t) {
+    const double s = mu * t;
+    const double eta = exp(-lam * t);
+    const double alpha = exp(-s);
+    const double numer = lam * (eta - alpha);
+    const double denom = mu * eta - lam * alpha;
+    const double general = fabs(denom) < 1e-30 ? 0.0 : numer / denom;
+    return fabs(1.0 - lam / mu) < 1e-4 ? s / (1.0 + s) : general;
+}
+
+__device__ double tkf_gamma(double lam, double mu, double t) {
+    const double s = mu * t;
+    const double alpha = exp(-mu * t);
+    const double beta = tkf_beta(lam, mu, t);
+    const double Phi = 1.0 - alpha;
+    const double general = fabs(Phi) < 1e-30 ? 0.0 : 1.0 - mu * beta / (lam * fmax(Phi, 1e-30));
+    const double phi = s < 1e-10 ? 1.0 - s / 2.0 : Phi / fmax(s, 1e-30);
+    const double limit = 1.0 - 1.0 / ((1.0 + s) * phi);
+    return fabs(1.0 - lam / mu) < 1e-4 ? limit : general;
+}
+
+// [5][5] TKF91 pair-HMM matrix, order S, M, I, D, E (core/params.py:29-55)
+__device__ void tkf91(double lam, double mu, double t, double *tau) {
+    const double a = exp(-mu * t), b = tkf_beta(lam, mu, t), g = tkf_gamma(lam, mu, t);
+    const double k = lam / mu;
+    const double row[5] = {0.0, (1 - b) * k * a, b, (1 - b) * k * (1 - a), (1 - b) * (1 - k)};
+    const double rowD[5] = {0.0, (1 - g) * k * a, g, (1 - g) * k * (1 - a), (1 - g) * (1 - k)};
+    for (int v = 0; v < 5; ++v) {
+        tau[S * 5 + v] = row[v];
+        tau[M * 5 + v] = row[v];
+        tau[I * 5 + v] = row[v];
+        tau[D * 5 + v] = rowD[v];
+        tau[E * 5 + v] = 0.0;
+    }
+}
+
+// ---------------------------------------------------------------- collapsed chi
+// Shared layout of chi_kernel (doubles).
+struct ChiSmem {
+    int K, n3, w;             // K, 3K, 3K + 5 (row width of the solve matrix)
+    double *tau, *tauK, *kap, *z, *Tex, *T, *TnN, *ent, *exi, *aug;
+    __device__ void carve(double *base, int K_) {
+        K = K_;
+        n3 = 3 * K_;
+        w = n3 + 5;
+        tau = base;                 // [25]
+        tauK = tau + 25;            // [K][25]
+        kap = tauK + 25 * K;        // [K]
+        z = kap + K;                // [3K]     null probability of flat index 3k+e
+        Tex = z + n3;               // [K][25]  T_exit_k
+        T = Tex + 25 * K;           // [25]     effective T
+        TnN = T + 25;               // [3K][5]  T_nullN
+        ent = TnN + 5 * n3;         // [K][5]   entry factors
+        exi = ent + 5 * K;          // [K][5]   exit factors (before notext)
+        aug = exi + 5 * K;          // [3K][3K+5] solve matrix
+    }
+    static size_t bytes(int K_) {
+        const size_t n3 = 3 * (size_t)K_;
+        return sizeof(double) * (25 + 25 * K_ + K_ + n3 + 25 * K_ + 25 + 5 * n3 + 10 * K_ + n3 * (n3 + 5));
+    }
+};
+
+__global__ void __launch_bounds__(THREADS)
+chi_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, int N, float *__restrict__ chi) {
+    extern __shared__ double smem_d[];
+    __shared__ int piv_row;
+    const int p = blockIdx.x, tid = threadIdx.x;
+    const int K = prm.K, F = prm.F;
+    const double t = ts[p];
+    const double *dins = prm.v + prm.o_dins, *ddel = prm.v + prm.o_ddel, *dw = prm.v + prm.o_dw;
+    const double *fw = prm.v + prm.o_fw, *ext = prm.v + prm.o_ext;
+    ChiSmem sm;
+    sm.carve(smem_d, K);
+    const int n3 = sm.n3, w = sm.w;
+
+    // TKF91 matrices of the main level and of each domain level
+    if (tid == 0) tkf91(prm.main_ins, prm.main_del, t, sm.tau);
+    for (int k = tid; k < K; k += blockDim.x) {
+        tkf91(dins[k], ddel[k], t, sm.tauK + 25 * k);
+        const double kap = dins[k] / ddel[k];
+        const double zt = (1.0 - kap) * (1.0 - tkf_beta(dins[k], ddel[k], t));
+        sm.kap[k] = kap;
+        sm.z[3 * k] = zt;
+        sm.z[3 * k + 1] = 1.0 - kap;
+        sm.z[3 * k + 2] = 1.0 - kap;
+    }
+    __syncthreads();
+
+    // null-domain quantities (models/mixdom.py:104-214): for flat index
+    // i = 3k + e (e over the M, I, D contexts), z(i) is the probability that
+    // domain k emits nothing, T_nullN[i] its exits to the main level
+    const double *tau = sm.tau;
+    const double tauE[3] = {tau[M * 5 + E], tau[M * 5 + E], tau[D * 5 + E]};
+    const int nullrow[3] = {M, M, D};
+    for (int i = tid; i < n3; i += blockDim.x) {
+        const int k = i / 3, e = i % 3;
+        const double z = sm.z[i];
+        const double nonnull = e == 0 ? 1.0 - z : sm.kap[k];
+        for (int v = 0; v < 5; ++v) sm.TnN[i * 5 + v] = 0.0;
+        sm.TnN[i * 5 + MID[e]] = nonnull;
+        sm.TnN[i * 5 + E] = z * tauE[e];
+        // row i of the solve matrix is column i of (I - T_nn):
+        // (I - T_nn)[j][i] = delta - z(j) dw[k(i)] tau[nullrow[e(j)]][MID[e(i)]]
+        for (int j = 0; j < n3; ++j)
+            sm.aug[i * w + j] = (i == j ? 1.0 : 0.0) - sm.z[j] * dw[k] * tau[nullrow[j % 3] * 5 + MID[e]];
+        // right-hand sides: T_Nnull[u][i] = tau[u][MID[e]] dw[k]
+        for (int u = 0; u < 5; ++u) sm.aug[i * w + n3 + u] = tau[u * 5 + MID[e]] * dw[k];
+    }
+    __syncthreads();
+
+    // Gauss-Jordan with partial pivoting: (I - T_nn)^T Y^T = T_Nnull^T
+    for (int c = 0; c < n3; ++c) {
+        if (tid == 0) {
+            int best = c;
+            double bv = fabs(sm.aug[c * w + c]);
+            for (int r = c + 1; r < n3; ++r) {
+                const double v = fabs(sm.aug[r * w + c]);
+                if (v > bv) { bv = v; best = r; }
+            }
+            piv_row = best;
+        }
+        __syncthreads();
+        const int pr = piv_row;
+        if (pr != c)
+            for (int j = tid; j < w; j += blockDim.x) {
+                const double a = sm.aug[c * w + j];
+                sm.aug[c * w + j] = sm.aug[pr * w + j];
+                sm.aug[pr * w + j] = a;
+            }
+        __syncthreads();
+        const double inv = 1.0 / sm.aug[c * w + c];
+        __syncthreads();
+        for (int j = tid; j < w; j += blockDim.x) sm.aug[c * w + j] *= inv;
+        __syncthreads();
+        for (int idx = tid; idx < n3 * w; idx += blockDim.x) {
+            const int r = idx / w, j = idx % w;
+            if (r == c || j == c) continue;
+            sm.aug[idx] -= sm.aug[r * w + c] * sm.aug[c * w + j];
+        }
+        __syncthreads();
+        for (int r = tid; r < n3; r += blockDim.x)
+            if (r != c) sm.aug[r * w + c] = 0.0;
+        __syncthreads();
+    }
+
+    // T_exit_k[k][u][v] = sum_e Y[u][3k+e] T_nullN[3k+e][v]; Y[u][i] = aug[i][3K+u]
+    for (int idx = tid; idx < 25 * K; idx += blockDim.x) {
+        const int k = idx / 25, u = (idx / 5) % 5, v = idx % 5;
+        double s = 0.0;
+        for (int e = 0; e < 3; ++e) s += sm.aug[(3 * k + e) * w + n3 + u] * sm.TnN[(3 * k + e) * 5 + v];
+        sm.Tex[idx] = s;
+    }
+    // entry / exit factors of each domain's five sub-states
+    for (int idx = tid; idx < 5 * K; idx += blockDim.x) {
+        const int k = idx / 5, j = idx % 5;
+        const double *tk = sm.tauK + 25 * k;
+        const double beta_d = fmax(1.0 - tk[S * 5 + E], 1e-30);
+        const bool isM = j < 3;
+        sm.ent[idx] = isM ? tk[S * 5 + UV_X[j]] / beta_d : 1.0;
+        sm.exi[idx] = isM ? tk[UV_X[j] * 5 + E] : 1.0 - sm.kap[k];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < 25; idx += blockDim.x) {
+        double s = (idx % 5 == E) ? tau[idx] : 0.0;
+        for (int k = 0; k < K; ++k) s += sm.Tex[25 * k + idx];
+        sm.T[idx] = s;
+    }
+    __syncthreads();
+
+    // chi (models/mixdom.py:252-423): state 0 = SS, 1 = EE, body state
+    // 2 + k*5F + j*F + f (domain k, sub-state j, fragment f)
+    const int bs = 5 * F;
+    float *out = chi + (size_t)p * N * N;
+    for (int idx = tid; idx < N * N; idx += blockDim.x) {
+        const int r = idx / N, c = idx % N;
+        double val = 0.0;
+        if (r == 0) {
+            if (c == 1) {
+                val = sm.T[S * 5 + E];
+            } else if (c >= 2) {
+                const int q = c - 2, kq = q / bs, jq = (q % bs) / F, fq = q % F;
+                val = sm.Tex[25 * kq + S * 5 + UV_U[jq]] * fw[kq * F + fq] * sm.ent[5 * kq + jq];
+            }
+        } else if (r >= 2 && c >= 1) {
+            const int pp = r - 2, kp = pp / bs, jp = (pp % bs) / F, fp = pp % F;
+            double notext = 1.0;
+            for (int g = 0; g < F; ++g) notext -= ext[(kp * F + fp) * F + g];
+            const double exit_full = notext * sm.exi[5 * kp + jp];
+            if (c == 1) {
+                val = exit_full * sm.T[UV_U[jp] * 5 + E];
+            } else {
+                const int q = c - 2, kq = q / bs, jq = (q % bs) / F, fq = q % F;
+                const double dest = fw[kq * F + fq] * sm.ent[5 * kq + jq];
+                val = exit_full * sm.Tex[25 * kq + UV_U[jp] * 5 + UV_U[jq]] * dest;
+                if (kp == kq) {
+                    const double e = ext[(kp * F + fp) * F + fq];
+                    if (jp < 3 && jq < 3)
+                        val += notext * sm.tauK[25 * kp + MID[jp] * 5 + MID[jq]] * fw[kp * F + fq] +
+                               (jp == jq ? e : 0.0);
+                    else if (jp == jq)
+                        val += notext * sm.kap[kp] * fw[kp * F + fq] + e;
+                }
+            }
+        }
+        out[idx] = (float)val;
+    }
+}
+
+// ---------------------------------------------------------------- expm (Pade 13)
+// b_j of the [13/13] Pade approximant of exp (Higham 2005, eq. 2.1 / Table 2.3)
+__device__ __constant__ double PADE13[14] = {
+    64764752532480000.0, 32382376266240000.0, 7771770303897600.0, 1187353796428800.0,
+    129060195264000.0, 10559470521600.0, 670442572800.0, 33522128640.0,
+    1323241920.0, 40840800.0, 960960.0, 16380.0, 182.0, 1.0};
+// theta_13 of the same paper: the 1-norm up to which degree 13 needs no scaling
+constexpr double THETA13 = 5.371920351148152;
+
+__device__ void mm(double *C, const double *A, const double *B, int n) {
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+        const int i = idx / n, j = idx % n;
+        double s = 0.0;
+        for (int k = 0; k < n; ++k) s += A[i * n + k] * B[k * n + j];
+        C[idx] = s;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(THREADS)
+expm_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, double *__restrict__ csubs) {
+    constexpr int n = NA, nn = NA * NA;
+    __shared__ double X[nn], A2[nn], A4[nn], A6[nn], W1[nn], W2[nn], U[nn], V[nn];
+    __shared__ double aug[n * 2 * n];
+    __shared__ double colsum[n];
+    __shared__ int piv_row, n_sq;
+    const int p = blockIdx.x / prm.C, c = blockIdx.x % prm.C, tid = threadIdx.x;
+    const double t = ts[p];
+    const double *Sx = prm.v + prm.o_S + (size_t)c * nn, *pi = prm.v + prm.o_pis + c * n;
+
+    // Q[a][b] = S[a][b] pi[b] off the diagonal, rows summing to zero (train/vjp.py:463-476)
+    for (int idx = tid; idx < nn; idx += blockDim.x) {
+        const int a = idx / n, b = idx % n;
+        X[idx] = a == b ? 0.0 : Sx[idx] * pi[b];
+    }
+    __syncthreads();
+    if (tid < n) {
+        double s = 0.0;
+        for (int b = 0; b < n; ++b) s += X[tid * n + b];
+        X[tid * n + tid] = -s;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < nn; idx += blockDim.x) X[idx] *= t;
+    __syncthreads();
+    if (tid < n) {
+        double s = 0.0;
+        for (int a = 0; a < n; ++a) s += fabs(X[a * n + tid]);
+        colsum[tid] = s;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double nrm = 0.0;
+        for (int b = 0; b < n; ++b) nrm = fmax(nrm, colsum[b]);
+        int s = 0;
+        if (nrm > THETA13) s = (int)ceil(log2(nrm / THETA13));
+        n_sq = s < 0 ? 0 : (s > 60 ? 60 : s);
+    }
+    __syncthreads();
+    const int s = n_sq;
+    for (int idx = tid; idx < nn; idx += blockDim.x) X[idx] = ldexp(X[idx], -s);
+    __syncthreads();
+    mm(A2, X, X, n);
+    mm(A4, A2, A2, n);
+    mm(A6, A4, A2, n);
+    const double *b = PADE13;
+    // W1 = b13 A6 + b11 A4 + b9 A2;  W2 = b12 A6 + b10 A4 + b8 A2
+    for (int idx = tid; idx < nn; idx += blockDim.x) {
+        W1[idx] = b[13] * A6[idx] + b[11] * A4[idx] + b[9] * A2[idx];
+        W2[idx] = b[12] * A6[idx] + b[10] * A4[idx] + b[8] * A2[idx];
+    }
+    __syncthreads();
+    mm(U, A6, W1, n);   // A6 W1
+    mm(V, A6, W2, n);   // A6 W2
+    for (int idx = tid; idx < nn; idx += blockDim.x) {
+        const double id = (idx / n == idx % n) ? 1.0 : 0.0;
+        W1[idx] = U[idx] + b[7] * A6[idx] + b[5] * A4[idx] + b[3] * A2[idx] + b[1] * id;
+        V[idx] = V[idx] + b[6] * A6[idx] + b[4] * A4[idx] + b[2] * A2[idx] + b[0] * id;
+    }
+    __syncthreads();
+    mm(U, X, W1, n);    // U = X (A6 W1 + ...)
+    // solve (V - U) R = (V + U)
+    for (int idx = tid; idx < nn; idx += blockDim.x) {
+        const int i = idx / n, j = idx % n;
+        aug[i * 2 * n + j] = V[idx] - U[idx];
+        aug[i * 2 * n + n + j] = V[idx] + U[idx];
+    }
+    __syncthreads();
+    const int w = 2 * n;
+    for (int cc = 0; cc < n; ++cc) {
+        if (tid == 0) {
+            int best = cc;
+            double bv = fabs(aug[cc * w + cc]);
+            for (int r = cc + 1; r < n; ++r) {
+                const double v = fabs(aug[r * w + cc]);
+                if (v > bv) { bv = v; best = r; }
+            }
+            piv_row = best;
+        }
+        __syncthreads();
+        const int pr = piv_row;
+        if (pr != cc)
+            for (int j = tid; j < w; j += blockDim.x) {
+                const double a = aug[cc * w + j];
+                aug[cc * w + j] = aug[pr * w + j];
+                aug[pr * w + j] = a;
+            }
+        __syncthreads();
+        const double inv = 1.0 / aug[cc * w + cc];
+        __syncthreads();
+        for (int j = tid; j < w; j += blockDim.x) aug[cc * w + j] *= inv;
+        __syncthreads();
+        for (int idx = tid; idx < n * w; idx += blockDim.x) {
+            const int r = idx / w, j = idx % w;
+            if (r == cc || j == cc) continue;
+            aug[idx] -= aug[r * w + cc] * aug[cc * w + j];
+        }
+        __syncthreads();
+        for (int r = tid; r < n; r += blockDim.x)
+            if (r != cc) aug[r * w + cc] = 0.0;
+        __syncthreads();
+    }
+    for (int idx = tid; idx < nn; idx += blockDim.x) W1[idx] = aug[(idx / n) * w + n + idx % n];
+    __syncthreads();
+    // undo the scaling: square s times
+    double *cur = W1, *nxt = W2;
+    for (int k = 0; k < s; ++k) {
+        mm(nxt, cur, cur, n);
+        double *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+    }
+    double *out = csubs + ((size_t)p * prm.C + c) * nn;
+    for (int idx = tid; idx < nn; idx += blockDim.x) out[idx] = cur[idx];
+}
+
+// ---------------------------------------------------------------- emission tables
+__global__ void __launch_bounds__(THREADS)
+tables_kernel(const __grid_constant__ Packed prm, const double *__restrict__ csubs, float *__restrict__ EM,
+              float *__restrict__ EI, float *__restrict__ ED) {
+    const int p = blockIdx.x, tid = threadIdx.x;
+    const int C = prm.C, G = prm.K * prm.F;
+    const double *cd = prm.v + prm.o_cd, *pis = prm.v + prm.o_pis;
+    const double *Pp = csubs + (size_t)p * C * NA * NA;
+    float *em = EM + (size_t)p * G * 441;
+    for (int idx = tid; idx < G * 441; idx += blockDim.x) {
+        const int g = idx / 441, a = (idx / 21) % 21, bb = idx % 21;
+        double s = 0.0;
+        for (int c = 0; c < C; ++c) {
+            const double lp = a < NA ? fmax(pis[c * NA + a], 1e-30) : 1.0;
+            const double ls = (a < NA && bb < NA) ? fmax(Pp[(c * NA + a) * NA + bb], 1e-30) : 1.0;
+            s += cd[g * C + c] * (lp * ls);
+        }
+        em[idx] = (float)s;
+    }
+    for (int idx = tid; idx < G * 21; idx += blockDim.x) {
+        const int g = idx / 21, a = idx % 21;
+        double s = 0.0;
+        for (int c = 0; c < C; ++c) s += cd[g * C + c] * (a < NA ? fmax(pis[c * NA + a], 1e-30) : 1.0);
+        EI[(size_t)p * G * 21 + idx] = (float)s;
+        ED[(size_t)p * G * 21 + idx] = (float)s;
+    }
+}
+
+// ---------------------------------------------------------------- class split (epilogue)
+// Per-class counts of train/likelihood.py:279-344 from the per-(d,f) character
+// tables: the class posterior of a cell depends on it only through its
+// characters, so with f_c[a][b] = pi_c[a'] P_c[a'][b'] (a' = min(a, A-1):
+// the reference's clamped gather for the wildcard) and w[g][c] = classdist,
+//   match[c][a][b] = sum_g cM[g][a][b] w[g][c] f_c[a][b] / sum_c' w[g][c'] f_c'[a][b]
+// (insert / delete alike with pi_c[a']), classdist[g][c] = the sum over all
+// 21 x 21 (and 21) characters of the same terms.  One CTA per pair.
+constexpr int CS_MAXC = 8;
+
+__global__ void __launch_bounds__(THREADS)
+class_split_kernel(const __grid_constant__ Packed prm, const double *__restrict__ csubs,
+                   const double *__restrict__ cM, const double *__restrict__ cI, const double *__restrict__ cD,
+                   double *__restrict__ match, double *__restrict__ ins, double *__restrict__ del,
+                   double *__restrict__ cdist) {
+    extern __shared__ double cs_acc[];   // [G][C] classdist partial sums
+    const int p = blockIdx.x, tid = threadIdx.x;
+    const int C = prm.C, G = prm.K * prm.F;
+    const double *cd = prm.v + prm.o_cd, *pis = prm.v + prm.o_pis;
+    const double *Pp = csubs + (size_t)p * C * NA * NA;
+    for (int i = tid; i < G * C; i += blockDim.x) cs_acc[i] = 0.0;
+    __syncthreads();
+    double loc[CS_MAXC];
+    // match-type cells
+    for (int ab = tid; ab < 441; ab += blockDim.x) {
+        const int a = ab / 21, b = ab % 21;
+        const int ac = a < NA ? a : NA - 1, bc = b < NA ? b : NA - 1;
+        double f[CS_MAXC], acc[CS_MAXC];
+        for (int c = 0; c < C; ++c) {
+            f[c] = pis[c * NA + ac] * Pp[(c * NA + ac) * NA + bc];
+            acc[c] = 0.0;
+        }
+        for (int g = 0; g < G; ++g) {
+            double den = 0.0;
+            for (int c = 0; c < C; ++c) den += cd[g * C + c] * f[c];
+            const double n = cM[((size_t)p * G + g) * 441 + ab];
+            for (int c = 0; c < C; ++c) {
+                const double wgc = n * (cd[g * C + c] * f[c] / (den + 1e-300));
+                acc[c] += wgc;
+                loc[c] = wgc;
+            }
+            for (int c = 0; c < C; ++c) atomicAdd(&cs_acc[g * C + c], loc[c]);
+        }
+        if (a < NA && b < NA)
+            for (int c = 0; c < C; ++c) match[(((size_t)p * C + c) * NA + a) * NA + b] = acc[c];
+    }
+    // insert / delete cells: the same posterior over pi_c
+    for (int ia = tid; ia < 2 * 21; ia += blockDim.x) {
+        const bool is_ins = ia < 21;
+        const int a = ia % 21, ac = a < NA ? a : NA - 1;
+        const double *cnt = is_ins ? cI : cD;
+        double acc[CS_MAXC];
+        for (int c = 0; c < C; ++c) acc[c] = 0.0;
+        for (int g = 0; g < G; ++g) {
+            double den = 0.0;
+            for (int c = 0; c < C; ++c) den += cd[g * C + c] * pis[c * NA + ac];
+            const double n = cnt[((size_t)p * G + g) * 21 + a];
+            for (int c = 0; c < C; ++c) {
+                const double wgc = n * (cd[g * C + c] * pis[c * NA + ac] / (den + 1e-300));
+                acc[c] += wgc;
+                atomicAdd(&cs_acc[g * C + c], wgc);
+            }
+        }
+        if (a < NA) {
+            double *out = is_ins ? ins : del;
+            for (int c = 0; c < C; ++c) out[((size_t)p * C + c) * NA + a] = acc[c];
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < G * C; i += blockDim.x) cdist[(size_t)p * G * C + i] = cs_acc[i];
+}
+
+}  // namespace pro
+
+static int pro_fail(int code, const char *msg) {
+    phmm_internal_set_error(msg);
+    return code;
+}
+
+static int pack_params(const phmm_mixdom2_params *prm, pro::Packed &pk, const char *who) {
+    using namespace pro;
+    char msg[160];
+    if (!prm) {
+        snprintf(msg, sizeof msg, "%s: null parameters", who);
+        return pro_fail(PHMM_E_ARG, msg);
+    }
+    const int K = prm->n_dom, F = prm->n_frag, C = prm->n_classes;
+    if (K < 1 || F < 1 || C < 1 || K * F > MAXK) {
+        snprintf(msg, sizeof msg, "%s: need n_dom, n_frag, n_classes >= 1 and n_dom*n_frag <= 33", who);
+        return pro_fail(PHMM_E_ARG, msg);
+    }
+    if (prm->alphabet != NA) {
+        snprintf(msg, sizeof msg, "%s: alphabet must be 20", who);
+        return pro_fail(PHMM_E_ARG, msg);
+    }
+    if (!prm->dom_ins || !prm->dom_del || !prm->dom_weights || !prm->frag_weights || !prm->ext_rates ||
+        !prm->class_pis || !prm->class_S_exch || !prm->classdist) {
+        snprintf(msg, sizeof msg, "%s: null host parameter array", who);
+        return pro_fail(PHMM_E_ARG, msg);
+    }
+    const int need = 3 * K + K * F + K * F * F + C * NA + C * NA * NA + K * F * C;
+    if (need > MAXV) {
+        snprintf(msg, sizeof msg, "%s: parameter block too large (reduce n_classes)", who);
+        return pro_fail(PHMM_E_ARG, msg);
+    }
+    std::memset(&pk, 0, sizeof(pk));
+    pk.K = K;
+    pk.F = F;
+    pk.C = C;
+    pk.main_ins = prm->main_ins;
+    pk.main_del = prm->main_del;
+    int o = 0;
+    auto put = [&](const double *src, int count) {
+        const int at = o;
+        std::memcpy(pk.v + o, src, sizeof(double) * count);
+        o += count;
+        return at;
+    };
+    pk.o_dins = put(prm->dom_ins, K);
+    pk.o_ddel = put(prm->dom_del, K);
+    pk.o_dw = put(prm->dom_weights, K);
+    pk.o_fw = put(prm->frag_weights, K * F);
+    pk.o_ext = put(prm->ext_rates, K * F * F);
+    pk.o_pis = put(prm->class_pis, C * NA);
+    pk.o_S = put(prm->class_S_exch, C * NA * NA);
+    pk.o_cd = put(prm->classdist, K * F * C);
+    return PHMM_OK;
+}
+
+extern "C" size_t phmm_mixdom2_class_subs_count(const phmm_mixdom2_params *prm, int32_t n_pairs) {
+    if (!prm || n_pairs < 0) return 0;
+    return (size_t)n_pairs * prm->n_classes * pro::NA * pro::NA;
+}
+
+extern "C" int phmm_mixdom2_tables(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t, float *chi,
+                                   float *emit_M, float *emit_I, float *emit_D, double *class_subs, void *stream) {
+    using namespace pro;
+    Packed pk;
+    int rc = pack_params(prm, pk, "phmm_mixdom2_tables");
+    if (rc) return rc;
+    if (n_pairs < 0) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_tables: negative n_pairs");
+    if (n_pairs == 0) return PHMM_OK;
+    if (!t || !chi || !emit_M || !emit_I || !emit_D || !class_subs)
+        return pro_fail(PHMM_E_ARG, "phmm_mixdom2_tables: null device buffer");
+    const int K = pk.K, F = pk.F, C = pk.C;
+    const int N = 2 + 5 * K * F;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t chi_smem = ChiSmem::bytes(K);
+    if (chi_smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(chi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chi_smem);
+        if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    }
+    chi_kernel<<<n_pairs, THREADS, chi_smem, st>>>(pk, t, N, chi);
+    expm_kernel<<<n_pairs * C, THREADS, 0, st>>>(pk, t, class_subs);
+    tables_kernel<<<n_pairs, THREADS, 0, st>>>(pk, class_subs, emit_M, emit_I, emit_D);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    return PHMM_OK;
+}
+
+extern "C" int phmm_mixdom2_class_counts(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *class_subs,
+                                         const double *cnt_M, const double *cnt_I, const double *cnt_D,
+                                         double *class_match, double *class_insert, double *class_delete,
+                                         double *classdist_counts, void *stream) {
+    using namespace pro;
+    Packed pk;
+    int rc = pack_params(prm, pk, "phmm_mixdom2_class_counts");
+    if (rc) return rc;
+    if (pk.C > CS_MAXC) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_class_counts: at most 8 classes");
+    if (n_pairs < 0) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_class_counts: negative n_pairs");
+    if (n_pairs == 0) return PHMM_OK;
+    if (!class_subs || !cnt_M || !cnt_I || !cnt_D || !class_match || !class_insert || !class_delete ||
+        !classdist_counts)
+        return pro_fail(PHMM_E_ARG, "phmm_mixdom2_class_counts: null device buffer");
+    const size_t smem = sizeof(double) * pk.K * pk.F * pk.C;
+    class_split_kernel<<<n_pairs, THREADS, smem, (cudaStream_t)stream>>>(
+        pk, class_subs, cnt_M, cnt_I, cnt_D, class_match, class_insert, class_delete, classdist_counts);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    return PHMM_OK;
+}

@@ -22,7 +22,8 @@ EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep'
            'phmm_estep_static', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_kernel_time',
            'phmm_set_variant',
            'phmm_last_variant', 'phmm_last_launch_count',
-           'phmm_last_error', 'phmm_version')
+           'phmm_last_error', 'phmm_version', 'phmm_mixdom2_class_subs_count', 'phmm_mixdom2_tables',
+           'phmm_mixdom2_class_counts')
 
 
 class ModelDesc(ctypes.Structure):
@@ -45,6 +46,15 @@ class Batch(ctypes.Structure):
                 ('emit_I', ctypes.c_void_p),
                 ('emit_D', ctypes.c_void_p),
                 ('emit_per_pair', ctypes.c_int32)]
+
+
+class MixDom2Params(ctypes.Structure):
+    _fields_ = [('n_dom', ctypes.c_int32), ('n_frag', ctypes.c_int32),
+                ('n_classes', ctypes.c_int32), ('alphabet', ctypes.c_int32),
+                ('main_ins', ctypes.c_double), ('main_del', ctypes.c_double)] + [
+        (name, ctypes.POINTER(ctypes.c_double)) for name in (
+            'dom_ins', 'dom_del', 'dom_weights', 'frag_weights', 'ext_rates', 'class_pis',
+            'class_S_exch', 'classdist')]
 
 
 class PairHMMError(RuntimeError):
@@ -94,6 +104,12 @@ def load(path=None):
     lib.phmm_last_launch_count.restype = ctypes.c_int
     lib.phmm_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     lib.phmm_last_error.restype = ctypes.c_int
+    lib.phmm_mixdom2_class_subs_count.argtypes = [ctypes.POINTER(MixDom2Params), ctypes.c_int32]
+    lib.phmm_mixdom2_class_subs_count.restype = ctypes.c_size_t
+    lib.phmm_mixdom2_tables.argtypes = [ctypes.POINTER(MixDom2Params), ctypes.c_int32] + [vp] * 7
+    lib.phmm_mixdom2_tables.restype = ctypes.c_int
+    lib.phmm_mixdom2_class_counts.argtypes = [ctypes.POINTER(MixDom2Params), ctypes.c_int32] + [vp] * 9
+    lib.phmm_mixdom2_class_counts.restype = ctypes.c_int
     lib.phmm_version.argtypes = []
     lib.phmm_version.restype = ctypes.c_int
     _LIB = lib
@@ -212,24 +228,24 @@ class DeviceBatch:
 
 def pack_residues(xs, ys):
     """Concatenate residues of all pairs: [x_0, y_0, x_1, y_1, ...] (uint8)."""
-    parts, xo, yo = [], [], []
-    off = 0
+    parts = []
     for x, y in zip(xs, ys):
-        x = np.asarray(x, dtype=np.int64)
-        y = np.asarray(y, dtype=np.int64)
-        if (x.size and (x.min() < 0 or x.max() > 20)) or (y.size and (y.min() < 0 or y.max() > 20)):
-            raise ValueError('residues must be integers in 0..20 (20 = wildcard)')
-        xo.append(off)
-        parts.append(x.astype(np.uint8))
-        off += x.size
-        yo.append(off)
-        parts.append(y.astype(np.uint8))
-        off += y.size
-    buf = np.concatenate(parts) if parts else np.zeros(0, np.uint8)
+        parts.append(np.asarray(x).reshape(-1))
+        parts.append(np.asarray(y).reshape(-1))
+    lens = np.fromiter((a.size for a in parts), dtype=np.int64, count=len(parts))
+    offs = np.zeros(len(parts), np.int64)
+    if len(parts) > 1:
+        np.cumsum(lens[:-1], out=offs[1:])
+    allr = np.concatenate(parts) if parts else np.zeros(0, np.int64)
+    if allr.dtype.kind not in 'iu':
+        allr = allr.astype(np.int64)
+    if allr.size and (allr.min() < 0 or allr.max() > 20):
+        raise ValueError('residues must be integers in 0..20 (20 = wildcard)')
+    buf = allr.astype(np.uint8)
     if buf.size == 0:
         buf = np.zeros(16, np.uint8)
-    return (buf, np.asarray(xo, np.int64), np.asarray(yo, np.int64),
-            np.asarray([len(x) for x in xs], np.int32), np.asarray([len(y) for y in ys], np.int32))
+    return (buf, offs[0::2].copy(), offs[1::2].copy(),
+            lens[0::2].astype(np.int32), lens[1::2].astype(np.int32))
 
 
 def make_batch(xs, ys, chi, emit_M, emit_I, emit_D, device='cuda'):
@@ -354,3 +370,80 @@ def estep_tables(plan, batch, want_F=True, want_B=True, want_post=True, stream=N
         _ptr(out['log_F']), _ptr(out['log_B']), _ptr(out['post']),
         ctypes.c_void_p(s.cuda_stream)), 'phmm_estep_tables')
     return out
+
+
+
+class MixDom2Prologue:
+    """phmm_mixdom2_tables for one MixDom2 parameter set: packs the host
+    parameter arrays once, then builds the E-step inputs of any batch of
+    per-pair times on the device.
+
+    params: the MixDom2 parameter dict (main_ins, main_del, dom_ins, dom_del,
+    dom_weights, frag_weights, ext_rates [K,F] or [K,F,F], class_pis,
+    class_S_exch, classdist)."""
+
+    KEYS = ('dom_ins', 'dom_del', 'dom_weights', 'frag_weights', 'ext_rates', 'class_pis',
+            'class_S_exch', 'classdist')
+
+    def __init__(self, params):
+        self.lib = load()
+        host = lambda v: v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else v
+        arr = {k: np.ascontiguousarray(np.asarray(host(params[k]), dtype=np.float64)) for k in self.KEYS}
+        self.K = arr['dom_ins'].size
+        self.F = arr['frag_weights'].shape[-1]
+        self.C, self.A = arr['class_pis'].shape
+        if arr['ext_rates'].ndim == 2:
+            arr['ext_rates'] = np.ascontiguousarray(np.einsum('kf,fg->kfg', arr['ext_rates'], np.eye(self.F)))
+        self._arr = arr   # the struct points into these arrays
+        dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        self.struct = MixDom2Params(self.K, self.F, self.C, self.A, float(host(params['main_ins'])),
+                                    float(host(params['main_del'])), *[dp(arr[k]) for k in self.KEYS])
+        self.N, self.G = 2 + 5 * self.K * self.F, self.K * self.F
+
+    def shapes(self, P):
+        """(chi, emit_M, emit_I, emit_D, class_subs) shapes for P pairs."""
+        N, G = self.N, self.G
+        return (P, N, N), (P, G, 21, 21), (P, G, 21), (P, G, 21), (P, self.C, self.A, self.A)
+
+    def run(self, t, chi, EM, EI, ED, csubs, stream=None):
+        """Write into caller tensors: t float64 [P] and the five outputs of shapes(P)."""
+        P = t.numel()
+        s = stream if stream is not None else torch.cuda.current_stream(t.device)
+        _check(self.lib.phmm_mixdom2_tables(ctypes.byref(self.struct), P, _ptr(t), _ptr(chi), _ptr(EM), _ptr(EI),
+                                            _ptr(ED), _ptr(csubs), ctypes.c_void_p(s.cuda_stream)),
+               'phmm_mixdom2_tables')
+
+    def class_counts(self, csubs, cnt_M, cnt_I, cnt_D, stream=None):
+        """phmm_mixdom2_class_counts: the per-class counts of e_step_mixdom2
+        (class_match_counts [P,C,20,20], class_insert_counts / class_delete_counts
+        [P,C,20], classdist_counts [P,K,F,C]) as float64 device tensors."""
+        P, dev, f64 = csubs.shape[0], csubs.device, torch.float64
+        C, A = self.C, self.A
+        out = {'class_match_counts': torch.empty(P, C, A, A, dtype=f64, device=dev),
+               'class_insert_counts': torch.empty(P, C, A, dtype=f64, device=dev),
+               'class_delete_counts': torch.empty(P, C, A, dtype=f64, device=dev),
+               'classdist_counts': torch.empty(P, self.K, self.F, C, dtype=f64, device=dev)}
+        s = stream if stream is not None else torch.cuda.current_stream(dev)
+        _check(self.lib.phmm_mixdom2_class_counts(
+            ctypes.byref(self.struct), P, _ptr(csubs), _ptr(cnt_M.contiguous()), _ptr(cnt_I.contiguous()),
+            _ptr(cnt_D.contiguous()), *[_ptr(v) for v in out.values()], ctypes.c_void_p(s.cuda_stream)),
+            'phmm_mixdom2_class_counts')
+        return out
+
+    def __call__(self, ts, device='cuda', stream=None):
+        if isinstance(ts, torch.Tensor):
+            t = ts.to(device=device, dtype=torch.float64).reshape(-1).contiguous()
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(np.asarray(ts, np.float64).reshape(-1))).to(device)
+        shp = self.shapes(t.numel())
+        f32, f64 = torch.float32, torch.float64
+        outs = [torch.empty(sh, dtype=f64 if i == 4 else f32, device=t.device) for i, sh in enumerate(shp)]
+        self.run(t, *outs, stream=stream)
+        return tuple(outs)
+
+
+def mixdom2_tables(params, ts, device='cuda', stream=None):
+    """The MixDom2 E-step inputs built on the device: (chi [P,N,N] f32,
+    EM [P,G,21,21] f32, EI [P,G,21] f32, ED [P,G,21] f32, csubs [P,C,20,20]
+    f64) for per-pair times ts."""
+    return MixDom2Prologue(params)(ts, device=device, stream=stream)

@@ -343,14 +343,19 @@ def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True):
     [P,G,21,21], cnt_I/cnt_D [P,G,21], status [P] and, with
     with_class_counts, the per-pair class counts of e_step_mixdom2."""
     dev = _device()
-    K, F, chi, csubs, EM, EI, ED = _mixdom2_tables(params, ts, dev)
+    pro = _lib.MixDom2Prologue(params)
+    chi, EM, EI, ED, csubs = pro(ts, device=dev)
+    K, F = pro.K, pro.F
     plan = get_plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)
     b = _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev)
     out = _lib.estep(plan, b)
     res = {'log_p': out['ll'], 'n_trans': out['n_trans'], 'cnt_M': out['cnt_M'],
            'cnt_I': out['cnt_I'], 'cnt_D': out['cnt_D'], 'status': out['status']}
     if with_class_counts:
-        res.update(class_split(params, out['cnt_M'], out['cnt_I'], out['cnt_D'], csubs=csubs))
+        if pro.C <= 8:
+            res.update(pro.class_counts(csubs, out['cnt_M'], out['cnt_I'], out['cnt_D']))
+        else:
+            res.update(class_split(params, out['cnt_M'], out['cnt_I'], out['cnt_D'], csubs=csubs))
     return res
 
 

@@ -278,10 +278,7 @@ class CudaExecutor:
             st = pm.mixdom_state_types(K, F)
             gr = pm.mixdom_state_groups(K, F)
             G = K * F
-            m.extra = {'K': K, 'F': F,
-                       'S_exch': pm._t(p['class_S_exch'], self.device),
-                       'cpis': pm._t(p['class_pis'], self.device),
-                       'cd': pm._t(p['classdist'], self.device)}
+            m.extra = {'K': K, 'F': F, 'prologue': _lib.MixDom2Prologue(p)}
         else:
             raise ValueError(f'unknown model kind {m.kind!r}')
         m.plan = get_plan(st, gr, G)
@@ -292,10 +289,14 @@ class CudaExecutor:
     def _io_sizes(self, m, Lx, Ly):
         """Byte sizes of the per-batch inputs and outputs, in carve order."""
         P, N, G = len(Lx), m.n_states, m.n_groups
-        return [('ll', 8 * P), ('n_trans', 8 * P * N * N), ('cnt_M', 8 * P * G * 441),
-                ('cnt_I', 8 * P * G * 21), ('cnt_D', 8 * P * G * 21), ('status', 4 * P),
-                ('residues', max(int(np.sum(Lx) + np.sum(Ly)), 16)), ('chi', 4 * P * N * N),
-                ('emit_M', 4 * P * G * 441), ('emit_I', 4 * P * G * 21), ('emit_D', 4 * P * G * 21)]
+        sizes = [('ll', 8 * P), ('n_trans', 8 * P * N * N), ('cnt_M', 8 * P * G * 441),
+                 ('cnt_I', 8 * P * G * 21), ('cnt_D', 8 * P * G * 21), ('status', 4 * P),
+                 ('residues', max(int(np.sum(Lx) + np.sum(Ly)), 16)), ('chi', 4 * P * N * N),
+                 ('emit_M', 4 * P * G * 441), ('emit_I', 4 * P * G * 21), ('emit_D', 4 * P * G * 21)]
+        if m.kind == 'mixdom2':
+            pro = m.extra['prologue']
+            sizes += [('t', 8 * P), ('csubs', 8 * P * pro.C * pro.A * pro.A)]
+        return sizes
 
     def _ws(self, m, Lx, Ly):
         return self._lib.workspace_bytes(m.plan, self._lib.host_batch(Lx, Ly), estep=True)
@@ -312,19 +313,13 @@ class CudaExecutor:
         return _al(self._ws(m, Lx, Ly)) + sum(_al(n) for _, n in self._io_sizes(m, Lx, Ly))
 
     # ---- device work
-    def _tables(self, m, ts):
-        """chi [P,N,N] and emission tables [P,G,...] in float64 (E-step prologue)."""
+    def _tkf_tables(self, m, ts):
+        """TKF92 chi [P,5,5] and emission tables [P,1,...] in float64."""
         pm, p = self.pm, m.params
-        if m.kind == 'tkf92':
-            chi = pm.tkf92_trans(p['ins_rate'], p['del_rate'], ts.cpu(), p.get('ext', 0.0)).clamp_min(1e-30)
-            sub = pm.transition_matrix(m.extra['Q'], ts)
-            EM, EI, ED = pm.tables_tkf(sub, m.extra['pi'])
-            return chi.to(self.device), EM, EI, ED, None
-        chi = pm.build_nested_trans(p['main_ins'], p['main_del'], ts.cpu(), p['dom_ins'], p['dom_del'],
-                                    p['dom_weights'], p['frag_weights'], p['ext_rates'])
-        csubs = pm.class_subs(m.extra['S_exch'], m.extra['cpis'], ts)
-        EM, EI, ED = pm.tables_per_class(csubs, m.extra['cpis'], m.extra['cd'])
-        return chi.to(self.device), EM, EI, ED, csubs
+        chi = pm.tkf92_trans(p['ins_rate'], p['del_rate'], ts.cpu(), p.get('ext', 0.0)).clamp_min(1e-30)
+        sub = pm.transition_matrix(m.extra['Q'], ts)
+        EM, EI, ED = pm.tables_tkf(sub, m.extra['pi'])
+        return chi.to(self.device), EM, EI, ED
 
     def launch(self, model, reqs, off, nbytes, slot):
         torch, _lib = self.torch, self._lib
@@ -345,31 +340,41 @@ class CudaExecutor:
                'cnt_M': f64(views['cnt_M'], G, 21, 21), 'cnt_I': f64(views['cnt_I'], G, 21),
                'cnt_D': f64(views['cnt_D'], G, 21), 'status': views['status'].view(torch.int32)}
         host_res = torch.from_numpy(buf).pin_memory()
+        host_t = torch.tensor([float(r.t) for r in reqs], dtype=torch.float64).pin_memory()
+        chi_v = f32(views['chi'], N, N)
+        eM, eI, eD = f32(views['emit_M'], G, 21, 21), f32(views['emit_I'], G, 21), f32(views['emit_D'], G, 21)
+        csubs = None
         with torch.cuda.stream(s):
-            ts = torch.as_tensor([float(r.t) for r in reqs], dtype=torch.float64, device=self.device)
-            chi, EM, EI, ED, csubs = self._tables(m, ts)
             res = views['residues'][:buf.size]
             res.copy_(host_res, non_blocking=True)
-            chi_v = f32(views['chi'], N, N)
-            chi_v.copy_(chi)
-            eM, eI, eD = f32(views['emit_M'], G, 21, 21), f32(views['emit_I'], G, 21), f32(views['emit_D'], G, 21)
-            eM.copy_(EM)
-            eI.copy_(EI)
-            eD.copy_(ED)
+            if m.kind == 'mixdom2':
+                # device prologue straight into the arena
+                pro = m.extra['prologue']
+                t_v = views['t'].view(torch.float64)
+                t_v.copy_(host_t, non_blocking=True)
+                csubs = views['csubs'].view(torch.float64).view(P, pro.C, pro.A, pro.A)
+                pro.run(t_v, chi_v, eM, eI, eD, csubs, stream=s)
+                chi = EM = EI = ED = None
+            else:
+                chi, EM, EI, ED = self._tkf_tables(m, host_t.to(self.device, non_blocking=True))
+                chi_v.copy_(chi)
+                eM.copy_(EM)
+                eI.copy_(EI)
+                eD.copy_(ED)
             batch = _lib.DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo, residues=res, chi=chi_v,
                                      emit_M=eM, emit_I=eI, emit_D=eD)
             _lib.estep_ws(m.plan, batch, (self.arena.data_ptr() + off, ws_n), stream=s, out=out)
             dev_out = dict(out)
             if m.kind == 'mixdom2' and m.class_counts:
-                from .api import class_split
-                dev_out.update(class_split(m.params, out['cnt_M'], out['cnt_I'], out['cnt_D'], csubs=csubs))
+                dev_out.update(m.extra['prologue'].class_counts(csubs, out['cnt_M'], out['cnt_I'], out['cnt_D'],
+                                                                stream=s))
             host = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in dev_out.items()}
             for k, v in dev_out.items():
                 host[k].copy_(v, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(s)
         # keep the host inputs and the temporaries alive until the batch retires
-        return {'event': ev, 'host': host, 'keep': (host_res, batch, chi, EM, EI, ED, csubs, dev_out)}
+        return {'event': ev, 'host': host, 'keep': (host_res, host_t, batch, chi, EM, EI, ED, csubs, dev_out)}
 
     def ready(self, h):
         return h['event'].query()

@@ -71,6 +71,8 @@ def parse_args():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--pairs', type=int, default=0,
                     help='use only the first P pairs (small case for ncu captures)')
+    ap.add_argument('--variant', type=int, default=0,
+                    help='kernel family (phmm_set_variant; 0 = automatic)')
     ap.add_argument('--max-len', type=int, default=0,
                     help='truncate every sequence to at most L residues (small case for ncu captures)')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
@@ -388,6 +390,8 @@ def main():
         plan = api.get_plan(np.array([pm.S, pm.M, pm.I, pm.D, pm.E]), np.zeros(5, np.int32), 1)
     batch = _lib.make_batch(w.xs, w.ys, chi, EM, EI, ED, device=dev)
     plan.set_timing(True)
+    if args.variant:
+        plan.set_variant(args.variant)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
 
@@ -493,11 +497,13 @@ def main():
                ('warp2::count_warp_kernel', 2)),
            5: (('blk::fwdbwd_block_kernel', 4), (None, 0), ('blk::count_block_kernel', 2)),
            6: ((('wide::forward_wide_kernel', 2) if fwd_only else ('wide::fwdbwd_wide_kernel', 4)), (None, 0),
-               ('wide::count_wide_kernel', 2))}[plan.last_variant]
+               ('wide::count_wide_kernel', 2)),
+           7: (('warp2::stripe_tw_kernel<...,0>', 2), ('warp2::stripe_tw_kernel<...,1>', 2),
+               ('warp2::count_warp_kernel', 2))}[plan.last_variant]
     durs = [fwd_avg, bwd_avg, cnt_avg]
-    # the overlapped count pass (variant 4) starts with the wavefronts and waits
+    # the overlapped count pass (variants 4, 7) starts with the wavefronts and waits
     # on their progress, so its event span is not its own duration
-    overlapped = plan.last_variant == 4
+    overlapped = plan.last_variant in (4, 7)
     di = int(np.argmax(durs[:2] if overlapped else durs))
     dom, fpc = fam[di]
     flop = fpc * N * N * total_cells

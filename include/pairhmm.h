@@ -237,7 +237,9 @@ int phmm_kernel_time(phmm_plan *plan, int which, float *ms);
  * count pass over both lattices), 5 = split E-step on the block kernels
  * (2 to 5 for state spaces with a compiled shape), 6 = the wide kernels
  * (any state space of up to 164 emitting states; the automatic choice above
- * 60 emitting states).  phmm_last_variant reports the family the last call used.  No
+ * 60 emitting states), 7 = split E-step on two-warp stripes (one lattice row
+ * per thread, 64-thread CTAs; the shapes of 2 and 4).  phmm_last_variant
+ * reports the family the last call used.  No
  * counterpart in the reference (it has no kernels). */
 int phmm_set_variant(phmm_plan *plan, int variant);
 int phmm_last_variant(const phmm_plan *plan);

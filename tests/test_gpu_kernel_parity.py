@@ -64,7 +64,8 @@ def related_pair(rng, Lx, Ly):
 def run_kernel(chi, st, groups, EM, EI, ED, xs, ys, per_pair=None, variant=0):
     """per_pair: optional list of (chi, EM, EI, ED) per pair; variant 1 =
     generic kernels, 2 = register-resident warp kernels, 3 = block kernels,
-    4 = split warp E-step, 5 = split block E-step, 6 = wide kernels, 0 = automatic."""
+    4 = split warp E-step, 5 = split block E-step, 6 = wide kernels, 7 = split
+    E-step on two-warp stripes, 0 = automatic."""
     from pairhmm import _lib
     G = EM.shape[0]
     plan = _lib.Plan(st, groups, G)
@@ -106,7 +107,7 @@ LENGTHS = [(0, 0), (0, 5), (6, 0), (1, 1), (7, 9), (31, 33), (32, 32), (33, 31),
            (63, 10), (64, 64), (65, 40), (40, 97), (130, 120), (129, 3)]
 
 
-@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5, 6, 7])
 @pytest.mark.parametrize('model,K,F,C', [('tkf91', 1, 1, 1), ('mixdom2', 3, 1, 1),
                                          ('mixdom2', 2, 2, 2), ('mixdom2', 4, 2, 2),
                                          ('mixdom2', 1, 1, 2), ('mixdom2', 2, 1, 1)])
@@ -129,6 +130,23 @@ def test_estep_matches_oracle(cuda_lib, model, K, F, C, variant):
         assert_counts(out['cnt_D'][b], cD)
 
 
+def test_two_warp_forward_only_matches_oracle(cuda_lib):
+    """phmm_forward on the two-warp stripe kernels (variant 7)."""
+    from pairhmm import _lib
+    rng = np.random.default_rng(11)
+    chi, st, groups, EM, EI, ED = oracle_case('mixdom2', rng, 3, 1, 1)
+    xs, ys = zip(*[related_pair(rng, a, b) for a, b in LENGTHS + [(200, 150)]])
+    plan = _lib.Plan(st, groups, EM.shape[0])
+    plan.set_variant(7)
+    b = _lib.make_batch(xs, ys, chi[None], EM[None], EI[None], ED[None])
+    ll_f, st_f = _lib.forward(plan, b)
+    assert plan.last_variant == 7
+    assert (st_f.cpu().numpy() == 0).all()
+    for k, (x, y) in enumerate(zip(xs, ys)):
+        ll = oracle_estep(chi, st, groups, EM, EI, ED, x, y)[0]
+        assert abs(ll_f[k].item() - ll) <= LL_RTOL * abs(ll) + 1e-9, (k, ll_f[k].item(), ll)
+
+
 def test_forward_only_matches_estep_ll(cuda_lib):
     from pairhmm import _lib
     rng = np.random.default_rng(3)
@@ -142,7 +160,7 @@ def test_forward_only_matches_estep_ll(cuda_lib):
     np.testing.assert_array_equal(ll_f.cpu().numpy(), out['ll'].cpu().numpy())
 
 
-@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5, 6, 7])
 def test_per_pair_chi_and_wildcards(cuda_lib, variant):
     rng = np.random.default_rng(11)
     base = mixdom2_params(rng, 2, 1, 1)
@@ -167,7 +185,7 @@ def test_per_pair_chi_and_wildcards(cuda_lib, variant):
         assert_counts(out['cnt_M'][b], cM)
 
 
-@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize('variant', [1, 2, 3, 4, 5, 6, 7])
 def test_long_pair_pipelined_stripes(cuda_lib, variant):
     """A pair spanning many stripes (pipelined through the edge rows), against the oracle."""
     rng = np.random.default_rng(5)

@@ -844,6 +844,7 @@ __global__ void fill_f64(double *p, int64_t n, double v) {
 
 #include "estep_warp.cuh"
 #include "estep_split.cuh"
+#include "estep_twowarp.cuh"
 #include "estep_block.cuh"
 #include "estep_block_split.cuh"
 #include "estep_wide.cuh"
@@ -903,7 +904,9 @@ struct phmm_plan {
     // register-resident warp kernels for this state space (null: generic kernels)
     int w_nm = 0, w_ni = 0, w_nd = 0;
     int grid_div = 1;       // persistent grids use 1/grid_div of the resident slots
-    int variant = 0;        // 0 automatic, 1 generic, 2 warp, 3 block, 4/5 split warp/block E-step, 6 wide
+    int variant = 0;        // 0 automatic, 1 generic, 2 warp, 3 block, 4/5 split warp/block E-step, 6 wide,
+                            // 7 split E-step on two-warp stripes
+    bool two_warp = false;  // the last warp-family call ran the two-warp stripe kernels
     int last_variant = 0;
 };
 
@@ -1051,8 +1054,9 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
     // the two wavefronts share the GPU: each persistent grid takes half the
     // resident slots, so neither waits for the other to drain
     plan->grid_div = 2;
+    const int kf = plan->two_warp ? 5 : 0, kb = plan->two_warp ? 6 : 2;
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
-    if ((rc = wl(plan, F, n_items, max_ly, 0, stream))) { plan->grid_div = 1; return rc; }
+    if ((rc = wl(plan, F, n_items, max_ly, kf, stream))) { plan->grid_div = 1; return rc; }
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[1], stream));
     // backward recursion (side stream): own edge rows and progress counters
     KParams B = K;
@@ -1065,7 +1069,7 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
     B.lat = nullptr;
     B.lat_exp = nullptr;
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[2], sd->side));
-    rc = wl(plan, B, n_items, max_ly, 2, sd->side);
+    rc = wl(plan, B, n_items, max_ly, kb, sd->side);
     plan->grid_div = 1;
     if (rc) return rc;
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[3], sd->side));
@@ -1322,28 +1326,44 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     BlockLauncher bl = nullptr;
     bool split = false;   // E-step as forward || backward recursion, then counts
     const bool tables = F_log || B_log || post;
-    // automatic choice (measured on GB300, 17 states): the block kernels have
-    // the shorter forward step; for the E-step the split warp kernels
+    // automatic choice (measured on GB300): the two-warp stripe kernels where
+    // the state space has a compiled warp shape -- the split E-step at 17
+    // states takes 2.95 ms per 200-pair batch against 3.5 ms on one-warp
+    // stripes and 8.7 ms on the block kernels; the TKF91 forward takes 0.21 ms
+    // per 64-pair batch against 0.30 ms on the block kernels -- else the block
+    // kernels
+    bool two_warp = false;
     if (!tables && plan->variant == 0) {
         if (estep) {
             wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
             if (!wl) bl = find_block_launcher(K.NS);
             split = wl != nullptr || bl != nullptr;
-        } else {
-            bl = find_block_launcher(K.NS);
-            if (!bl) wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
+            two_warp = wl != nullptr;
+        } else {   // forward only: the two-warp stripes where the shape has them
+            wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
+            two_warp = wl != nullptr;
+            if (!wl) bl = find_block_launcher(K.NS);
         }
     }
     if (!tables && (plan->variant == 3 || plan->variant == 5)) bl = find_block_launcher(K.NS);
     if (!tables && plan->variant == 5) split = estep && bl != nullptr;
     if (!tables && (plan->variant == 2 || plan->variant == 4)) wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
     if (!tables && plan->variant == 4) split = estep && wl != nullptr;
-    if ((plan->variant == 2 || plan->variant == 4) && !wl) return fail(PHMM_E_ARG, "no warp kernel for this state space");
+    if (!tables && plan->variant == 7) {
+        wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
+        split = estep && wl != nullptr;
+        two_warp = wl != nullptr;
+    }
+    if ((plan->variant == 2 || plan->variant == 4 || plan->variant == 7) && !wl)
+        return fail(PHMM_E_ARG, "no warp kernel for this state space");
     if ((plan->variant == 3 || plan->variant == 5) && !bl) return fail(PHMM_E_ARG, "no block kernel for this state space");
     const int rows = bl ? blk::ROWS : (wl ? warp2::ROWS : TH);
     const int stride = bl ? K.NS : (wl ? ((plan->w_nm + plan->w_ni + plan->w_nd + 1 + 3) & ~3) : K.NS);
     const int estride = bl ? blk::nbp_of(K.NS / 4) : 1;   // exponents per cell
-    if (!ws_need) plan->last_variant = bl ? (split ? 5 : 3) : (split ? 4 : (wl ? 2 : 1));
+    if (!ws_need) {
+        plan->last_variant = two_warp ? 7 : (bl ? (split ? 5 : 3) : (split ? 4 : (wl ? 2 : 1)));
+        plan->two_warp = two_warp;
+    }
     // ---- plan: stripes, offsets, longest-first order
     std::vector<int> order(P_);
     for (int p = 0; p < P_; ++p) {
@@ -1527,7 +1547,7 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
         if (bl) {
             if ((rc = bl(plan, K, n_items, max_ly, bwd, stream))) return rc;
         } else if (wl) {
-            if ((rc = wl(plan, K, n_items, max_ly, bwd, stream))) return rc;
+            if ((rc = wl(plan, K, n_items, max_ly, two_warp ? 5 : (int)bwd, stream))) return rc;
         } else {
             const int threads = 32 * K.NQ;
             const SmemLayout L = make_layout(K.NS, K.NQ, G, max_ly, bwd);
@@ -1576,10 +1596,14 @@ int launch_block(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind,
 template <class SH>
 int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, cudaStream_t stream) {
     void (*kern)(const KParams) = nullptr;
-    int bytes = 0;
+    int bytes = 0, threads = 32;
     if (kind == 3) {
         bytes = warp2::make_smem_c(SH::SP, SH::KP, SH::NI, K.G, max_ly).bytes;
         kern = warp2::count_warp_kernel<SH>;
+    } else if (kind == 5 || kind == 6) {   // two-warp stripes: forward / backward recursion
+        bytes = warp2::make_smem_tw(SH::SP, SH::KP, SH::NI, K.G, max_ly, kind == 6).bytes;
+        kern = kind == 5 ? warp2::stripe_tw_kernel<SH, false> : warp2::stripe_tw_kernel<SH, true>;
+        threads = warp2::TWT;
     } else {
         bytes = warp2::make_smem_w(SH::SP, SH::KP, SH::NI, K.G, max_ly, kind != 0, kind == 1).bytes;
         kern = kind == 0 ? warp2::forward_warp_kernel<SH>
@@ -1587,10 +1611,10 @@ int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, 
     }
     CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     int occ = 0;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32, bytes));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, bytes));
     if (occ < 1) return fail(PHMM_E_ARG, "warp kernel does not fit on an SM (shared memory)");
     const int grid = std::min(n_items, std::max(1, plan->sm_count * occ / plan->grid_div));
-    kern<<<grid, 32, bytes, stream>>>(K);
+    kern<<<grid, threads, bytes, stream>>>(K);
     CUDA_TRY(cudaGetLastError());
     return 0;
 }
@@ -1881,8 +1905,8 @@ int phmm_estep_ws(phmm_plan *plan, const phmm_batch *batch, void *workspace, siz
 int phmm_last_launch_count(const phmm_plan *plan) { return plan ? plan->launches : 0; }
 
 int phmm_set_variant(phmm_plan *plan, int variant) {
-    if (!plan || variant < 0 || variant > 6) return fail(PHMM_E_ARG, "bad variant");
-    if ((variant == 2 || variant == 4) && !find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd))
+    if (!plan || variant < 0 || variant > 7) return fail(PHMM_E_ARG, "bad variant");
+    if ((variant == 2 || variant == 4 || variant == 7) && !find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd))
         return fail(PHMM_E_ARG, "no warp kernel for this state space");
     if ((variant == 3 || variant == 5) && !find_block_launcher(plan->base.NS))
         return fail(PHMM_E_ARG, "no block kernel for this state space");

@@ -122,8 +122,8 @@ int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch,
  * x_off_host, y_off_host) are read.  The _ws calls then run exactly as
  * phmm_forward / phmm_estep, with all scratch carved from `workspace`
  * (256-byte aligned, at least that many bytes) instead of plan-owned
- * buffers, and allocate no device memory (the split E-step creates one side
- * stream and two events per caller stream, once).  Calls on one plan with distinct workspaces
+ * buffers, and allocate no device memory (the split E-step creates its side
+ * streams and events once per caller stream).  Calls on one plan with distinct workspaces
  * may be in flight on different streams at the same time (issue them from
  * one host thread).  No counterpart in the reference, whose XLA runtime owns
  * the scratch; this is what a serving loop budgets HBM with when it admits

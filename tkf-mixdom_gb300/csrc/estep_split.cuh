@@ -596,8 +596,7 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
 #pragma unroll
                 for (int u = 0; u < 16; ++u) pz[u] = 0.f;
                 const float *fb = fbuf + buf * ROWS * SPP;
-                const int r0 = grp * ROWS / SH::GROUPS, r1 = (grp + 1) * ROWS / SH::GROUPS;
-                for (int rr = r0; rr < r1; ++rr) {
+                auto row_outer = [&](int rr) {
                     const float4 fv = reinterpret_cast<const float4 *>(fb + rr * SPP)[bs];
                     const float4 uv = reinterpret_cast<const float4 *>(ust + rr * KPP)[bk];
                     const float fa[4] = {fv.x, fv.y, fv.z, fv.w};
@@ -606,6 +605,15 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
                     for (int a = 0; a < 4; ++a)
 #pragma unroll
                         for (int b = 0; b < 4; ++b) pz[4 * a + b] = fmaf(fa[a], ua[b], pz[4 * a + b]);
+                };
+                if constexpr (ROWS % SH::GROUPS == 0) {   // fixed trip count: unrolled
+                    constexpr int RPG = ROWS / SH::GROUPS;
+                    const int r0 = grp * RPG;
+#pragma unroll 4
+                    for (int rr = r0; rr < r0 + RPG; ++rr) row_outer(rr);
+                } else {
+                    const int r0 = grp * ROWS / SH::GROUPS, r1 = (grp + 1) * ROWS / SH::GROUPS;
+                    for (int rr = r0; rr < r1; ++rr) row_outer(rr);
                 }
 #pragma unroll
                 for (int u = 0; u < 16; ++u) {

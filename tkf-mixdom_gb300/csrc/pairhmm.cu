@@ -889,7 +889,7 @@ struct phmm_plan {
     float *bedge = nullptr; size_t bedge_cap = 0;
     int *bedge_exp = nullptr; size_t bedgeE_cap = 0;
     // split E-step: one side stream (+ fork / join events) per caller stream
-    struct Side { cudaStream_t user, side, side2; cudaEvent_t fork, join, join2; };
+    struct Side { cudaStream_t user, side, side2, side3; cudaEvent_t fork, join, join2, join3, fwd_done; };
     std::vector<Side> sides;
     std::vector<PairMeta> h_meta;
     std::vector<int2> h_items;
@@ -984,12 +984,15 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 int get_side(phmm_plan *plan, cudaStream_t stream, phmm_plan::Side **out) {
     for (auto &e : plan->sides)
         if (e.user == stream) { *out = &e; return 0; }
-    phmm_plan::Side e{stream, nullptr, nullptr, nullptr, nullptr, nullptr};
+    phmm_plan::Side e{stream, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     CUDA_TRY(cudaStreamCreateWithFlags(&e.side, cudaStreamNonBlocking));
     CUDA_TRY(cudaStreamCreateWithFlags(&e.side2, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&e.side3, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&e.fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&e.join, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&e.join2, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&e.join3, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&e.fwd_done, cudaEventDisableTiming));
     plan->sides.push_back(e);
     *out = &plan->sides.back();
     return 0;
@@ -1043,6 +1046,7 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
     CUDA_TRY(cudaEventRecord(sd->fork, stream));
     CUDA_TRY(cudaStreamWaitEvent(sd->side, sd->fork, 0));
     CUDA_TRY(cudaStreamWaitEvent(sd->side2, sd->fork, 0));
+    CUDA_TRY(cudaStreamWaitEvent(sd->side3, sd->fork, 0));
     // forward (caller's stream)
     KParams F = K;
     F.items = (const int2 *)d_items;
@@ -1058,6 +1062,7 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
     if ((rc = wl(plan, F, n_items, max_ly, kf, stream))) { plan->grid_div = 1; return rc; }
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[1], stream));
+    CUDA_TRY(cudaEventRecord(sd->fwd_done, stream));
     // backward recursion (side stream): own edge rows and progress counters
     KParams B = K;
     B.items = (const int2 *)d_items + n_items;
@@ -1080,11 +1085,21 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
     rc = wl(plan, C, n_citems, max_ly, 3, sd->side2);
     plan->grid_div = 1;
     if (rc) return rc;
-    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[5], sd->side2));
     CUDA_TRY(cudaEventRecord(sd->join2, sd->side2));
+    // the overlapped grid holds half the slots; once both wavefronts are done a
+    // second, full-size grid pops the remaining count items from the same
+    // counter (all of them ready, so it waits on nothing)
+    CUDA_TRY(cudaStreamWaitEvent(sd->side3, sd->fwd_done, 0));
+    CUDA_TRY(cudaStreamWaitEvent(sd->side3, sd->join, 0));
+    KParams C2 = C;
+    C2.count_wait = 0;
+    if ((rc = wl(plan, C2, n_citems, max_ly, 3, sd->side3))) return rc;
+    CUDA_TRY(cudaEventRecord(sd->join3, sd->side3));
     CUDA_TRY(cudaStreamWaitEvent(stream, sd->join, 0));
     CUDA_TRY(cudaStreamWaitEvent(stream, sd->join2, 0));
-    plan->launches += 3;
+    CUDA_TRY(cudaStreamWaitEvent(stream, sd->join3, 0));
+    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[5], stream));
+    plan->launches += 4;
     plan->timed_bwd = true;
     plan->timed_count = true;
     return 0;
@@ -1846,8 +1861,11 @@ void phmm_plan_destroy(phmm_plan *plan) {
         cudaEventDestroy(e.fork);
         cudaEventDestroy(e.join);
         cudaEventDestroy(e.join2);
+        cudaEventDestroy(e.join3);
+        cudaEventDestroy(e.fwd_done);
         cudaStreamDestroy(e.side);
         cudaStreamDestroy(e.side2);
+        cudaStreamDestroy(e.side3);
     }
     cudaFree(plan->blat);
     cudaFree(plan->blat_exp);

@@ -352,7 +352,7 @@ def e2e_function(workload, w, api, torch):
             out['log_p'] = ll.detach().cpu().numpy()
             return out
         return grad_call
-    return lambda: {kk: v.cpu().numpy() for kk, v in api.estep_batch_mixdom2(w.params, w.xs, w.ys, w.ts).items()}
+    return lambda: api.to_host(api.estep_batch_mixdom2(w.params, w.xs, w.ys, w.ts))
 
 
 def main():

@@ -551,3 +551,422 @@ __global__ void __launch_bounds__(TWT) stripe_tw_kernel(const KParams P) {
 }
 
 }  // namespace warp2
+
+// ---------------------------------------------------------------- two-warp count pass
+// count_chunk_w with one row per thread: a 64-thread CTA takes a chunk of CCH
+// anti-diagonal steps of one stripe, both warps sharing the model tables and
+// the double-buffered lattice rows.  Row r's D- and M-successors come from row
+// r+1 by __shfl_down inside a warp, through a shared slot across the two warps
+// (row 32 -> row 31) and from the stripe below for row 63.  The outer products
+// run over 64 threads: thread (group, block) owns a 4 x 4 tile of (source,
+// destination) for ROWS / groups rows.
+namespace warp2 {
+
+struct SmemCT {
+    SmemC c;
+    int slot;    // float offset: [2][SP] w~ of row 32 at the previous step
+    int slotE;   // int offset: [2]
+    int item;    // int offset: popped item
+    int bytes;
+};
+
+__host__ __device__ inline SmemCT make_smem_ct(int SP, int KP, int NI, int G, int max_ly) {
+    SmemCT L;
+    L.c = make_smem_c(SP, KP, NI, G, max_ly);
+    int o = L.c.bytes / 4;
+    L.slot = o; o += 2 * SP;
+    L.slotE = o; o += 4;
+    L.item = o; o += 4;
+    L.bytes = o * 4;
+    return L;
+}
+
+template <class SH>
+__device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const SmemCT &LT, float *sm,
+                               unsigned char *smb) {
+    constexpr int NE = SH::NE, NSRC = SH::NSRC, SP = SH::SP, KP = SH::KP, NM = SH::NM, NI = SH::NI;
+    constexpr int ND = SH::ND, SPP = SH::SPP, KPP = SH::KPP;
+    constexpr int GROUPS64 = TWT / SH::NBLK;   // outer-product row groups over 64 threads
+    const SmemC &L = LT.c;
+    const PairMeta m = P.meta[p];
+    const int N = P.N, G = P.G;
+    const int Lx = m.Lx, Ly = m.Ly;
+    const int r = threadIdx.x, lane = r & 31;
+    const int i0 = si * ROWS;
+    const int nrows = min(ROWS, Lx + 1 - i0);
+    const bool has_below = si + 1 < m.n_stripes;
+    const int64_t latc = m.lat_base + (int64_t)si * (ROWS + Ly) * ROWS;
+    const int64_t latb = m.lat_base + (int64_t)(si + 1) * (ROWS + Ly) * ROWS;   // stripe below (row 0)
+    const int T_last = (nrows - 1) + Ly;
+    const int t0 = ch * CCH;
+    const int t_hi = min(T_last, t0 + CCH - 1);
+    const int t_top = min(T_last, t_hi + 2);   // two steps of successor history first
+    if (t0 > T_last) return;                    // uniform over the CTA
+    int *s_flag = reinterpret_cast<int *>(sm) + LT.slotE + 2;
+    if (P.count_wait) {   // the wavefronts may still run: wait for the stripes read here
+        if (r == 0) *s_flag = count_ready(P, m, si) ? 1 : 0;
+        __syncthreads();
+        const int ok = *s_flag;
+        __syncthreads();
+        if (!ok) {
+            if (r == 0) atomicOr(P.status + p, PHMM_ST_TIMEOUT);
+            return;
+        }
+    }
+    const double llv = __ldcg(P.ll + p);
+    if (!(llv > -1e29)) return;   // uniform over the CTA
+    const double lam = llv / LN2;
+    const double Epd = floor(lam);
+    const int Ep = (int)Epd;
+    const float rfrac = (float)exp2(-(lam - Epd));
+    float *fbuf = sm + L.fbuf, *bbuf = sm + L.bbuf, *ust = sm + L.ust, *bins = sm + L.bins, *colI = sm + L.colI;
+    int *fEb = reinterpret_cast<int *>(sm) + L.fE;
+    int *bEb = reinterpret_cast<int *>(sm) + L.bE;
+    float *slot = sm + LT.slot;
+    int *slotE = reinterpret_cast<int *>(sm) + LT.slotE;
+    auto prefetch = [&](int t) {
+        if (t >= t0) {
+            const int buf = t & 1;
+            const float *srcF = P.lat + (latc + (int64_t)t * ROWS) * SP;
+            const float *srcB = P.blat + (latc + (int64_t)t * ROWS) * SP;
+            for (int idx = r; idx < ROWS * SP / 4; idx += TWT) {
+                const int rr = idx / (SP / 4), q = idx % (SP / 4);
+                if (t <= t_hi) cp_async16(fbuf + buf * ROWS * SPP + rr * SPP + 4 * q, srcF + 4 * idx);
+                cp_async16(bbuf + buf * ROWS * SPP + rr * SPP + 4 * q, srcB + 4 * idx);
+            }
+            if (r < ROWS / 4) {
+                if (t <= t_hi) cp_async16(fEb + buf * ROWS + 4 * r, P.lat_exp + latc + (int64_t)t * ROWS + 4 * r);
+                cp_async16(bEb + buf * ROWS + 4 * r, P.blat_exp + latc + (int64_t)t * ROWS + 4 * r);
+            }
+        }
+        cp_commit();
+    };
+    prefetch(t_top);
+    // ---- tables, y characters of the chunk's columns, zeroed bins and slots
+    {
+        const float *eM = P.eM + (int64_t)p * P.eM_stride;
+        const float *eI = P.eI + (int64_t)p * P.eID_stride;
+        const float *eDg = P.eD + (int64_t)p * P.eID_stride;
+        for (int idx = r; idx < G * 441; idx += TWT) sm[L.tM + idx] = __ldg(eM + idx);
+        for (int idx = r; idx < G * 21; idx += TWT) {
+            sm[L.tI + idx] = __ldg(eI + idx);
+            sm[L.tD + idx] = __ldg(eDg + idx);
+            sm[L.bins + idx] = 0.f;
+        }
+        unsigned char *ysw = smb + L.ys;
+        const int jlo = max(0, t0 - (ROWS - 1)), jhi = min(Ly, t_hi + 3);
+        for (int j = jlo + r; j <= jhi; j += TWT) {
+            int c = 0;
+            if (j >= 1) c = min((int)P.res[m.y_off + j - 1], 20);
+            ysw[j] = (unsigned char)c;
+        }
+        for (int idx = r; idx < ROWS * (NI > 0 ? NI : 1); idx += TWT) colI[idx] = 0.f;
+        if (r < 2 * SP) slot[r] = 0.f;
+        if (r < 2) slotE[r] = EXP_NONE;
+        __syncthreads();
+    }
+    const unsigned char *ys = smb + L.ys;
+
+    const int rowi = i0 + r;
+    const int xch = row_char(P, p, m, rowi);
+    float eD[ND > 0 ? ND : 1];
+    int offM[NM > 0 ? NM : 1];
+#pragma unroll
+    for (int k = 0; k < NM; ++k) offM[k] = L.tM + P.w_group[k] * 441 + xch * 21;
+#pragma unroll
+    for (int k = 0; k < ND; ++k) eD[k] = sm[L.tD + P.w_group[NM + NI + k] * 21 + xch];
+    int offI[NI > 0 ? NI : 1];
+#pragma unroll
+    for (int k = 0; k < NI; ++k) offI[k] = L.tI + P.w_group[NM + k] * 21;
+    // the first row of the stripe below (row 63's D / M successors)
+    int offMb[NM > 0 ? NM : 1];
+    float eDb[ND > 0 ? ND : 1];
+    {
+        const int xb = row_char(P, p, m, i0 + ROWS);
+#pragma unroll
+        for (int k = 0; k < NM; ++k) offMb[k] = L.tM + P.w_group[k] * 441 + xb * 21;
+#pragma unroll
+        for (int k = 0; k < ND; ++k) eDb[k] = sm[L.tD + P.w_group[NM + NI + k] * 21 + xb];
+    }
+    double *cntM_pair = P.cntM + (int64_t)p * G * 441;
+
+    float dcnt[ND > 0 ? ND : 1], dcmp[ND > 0 ? ND : 1];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) { dcnt[k] = 0.f; dcmp[k] = 0.f; }
+    const int blk = r % SH::NBLK, grp = r / SH::NBLK;
+    const bool counter = grp < GROUPS64;
+    const int bs = blk / SH::BK, bk = blk % SH::BK;
+    float csum[16], ccomp[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) { csum[u] = 0.f; ccomp[u] = 0.f; }
+
+    // successor histories: w~ of my cell at t+1 (wn) and the D-successor seen
+    // at step t+1 (dR), which is my M-successor at step t
+    float wn[NE], dR[NE];
+    int Ewn = EXP_NONE, EdR = EXP_NONE;
+#pragma unroll
+    for (int k = 0; k < NE; ++k) { wn[k] = 0.f; dR[k] = 0.f; }
+    // row 63: b~ of row i0+64 at column (t - 63), loaded one step ahead
+    float bbv[SP];
+    int bbE = EXP_NONE;
+    auto load_below = [&](int t) {
+        const int jb = t - (ROWS - 1);
+        bbE = EXP_NONE;
+        if (r == ROWS - 1 && has_below && t >= t0 && jb >= 0 && jb <= Ly) {
+            const int64_t cell = latb + (int64_t)jb * ROWS;
+            bbE = __ldcg(P.blat_exp + cell);
+            const float4 *src = reinterpret_cast<const float4 *>(P.blat + cell * SP);
+#pragma unroll
+            for (int q = 0; q < SP / 4; ++q) {
+                const float4 v = __ldcg(src + q);
+                bbv[4 * q] = v.x; bbv[4 * q + 1] = v.y; bbv[4 * q + 2] = v.z; bbv[4 * q + 3] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int s = 0; s < SP; ++s) bbv[s] = 0.f;
+        }
+    };
+    load_below(t_top);
+
+    for (int t = t_top; t >= t0; --t) {
+        const bool count = t <= t_hi;
+        const int buf = t & 1;
+        // step t's rows have landed (this thread's copies, then everyone's),
+        // and every thread is done with step t+1, whose buffer takes step t-1
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncthreads();
+        prefetch(t - 1);
+        const int jc = t - r;
+        const bool valid = r < nrows && jc >= 0 && jc <= Ly;
+        // ---- b~ and w~ = e b~ of my cell at step t
+        float wcur[NE];
+        const int Eb0 = valid ? bEb[buf * ROWS + r] : EXP_NONE;
+        const int Eb = Eb0 > EXP_NONE ? Eb0 : EXP_NONE;
+        const int yj = valid ? ys[jc] : 0;
+        const float *br = bbuf + buf * ROWS * SPP + r * SPP;
+#pragma unroll
+        for (int k = 0; k < NE; ++k) {
+            const int ty = SH::type_of(k);
+            float ev;
+            if (ty == T_M) ev = sm[offM[k] + yj];
+            else if (ty == T_I) ev = sm[offI[k - NM] + yj];
+            else ev = eD[k - NM - NI];
+            wcur[k] = Eb > EXP_NONE ? br[k] * ev : 0.f;
+        }
+        // D-successor (row r+1, column jc) = row r+1's w~ at step t+1: a shuffle
+        // inside a warp, the slot written by row 32 for row 31, the stripe
+        // below for row 63
+        float dnew[NE];
+        int Ednew = __shfl_down_sync(0xffffffffu, Ewn, 1);
+#pragma unroll
+        for (int k = 0; k < NE; ++k) dnew[k] = __shfl_down_sync(0xffffffffu, wn[k], 1);
+        if (r == 31) {
+            const int sb = (t + 1) & 1;
+#pragma unroll
+            for (int k = 0; k < NE; ++k) dnew[k] = slot[sb * SP + k];
+            Ednew = slotE[sb];
+        } else if (r == ROWS - 1) {
+            const bool okb = has_below && jc >= 0 && jc <= Ly && bbE > EXP_NONE;
+            const int yb = okb ? ys[jc] : 0;
+#pragma unroll
+            for (int k = 0; k < NE; ++k) {
+                const int ty = SH::type_of(k);
+                float ev;
+                if (ty == T_M) ev = sm[offMb[k] + yb];
+                else if (ty == T_I) ev = sm[offI[k - NM] + yb];
+                else ev = eDb[k - NM - NI];
+                dnew[k] = okb ? bbv[k] * ev : 0.f;
+            }
+            Ednew = okb ? bbE : EXP_NONE;
+        }
+        load_below(t - 1);
+        if (count) {
+            const bool term = valid && rowi == Lx && jc == Ly;
+            const bool hI = jc + 1 <= Ly, hD = rowi + 1 <= Lx, hM = hI && hD;
+            // successor exponents by type: I = mine at t+1, D = dnew, M = dR
+            const int EI = (hI && !term) ? Ewn : EXP_NONE, ED = (hD && !term) ? Ednew : EXP_NONE;
+            const int EM = (hM && !term) ? EdR : EXP_NONE;
+            const int Ef = valid ? fEb[buf * ROWS + r] : EXP_NONE;
+            float fsc = 0.f;
+            if (valid && Ef > EXP_NONE && Eb > EXP_NONE) {
+                int d = Ef + Eb - Ep;
+                if (d > 126) { d = 126; atomicOr(P.status + p, PHMM_ST_SCALE_CLAMP); }
+                fsc = scale_pow2(rfrac, max(d, -200));
+            }
+            // f~ scaled in place (the outer products read it from the buffer)
+            float *fr = fbuf + buf * ROWS * SPP + r * SPP;
+            float ft[NSRC];
+#pragma unroll
+            for (int q = 0; q < SP / 4; ++q) {
+                const float4 v = reinterpret_cast<const float4 *>(fr)[q];
+                const float va[4] = {v.x, v.y, v.z, v.w};
+                float o[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int s = 4 * q + u;
+                    o[u] = (s < NSRC && fsc > 0.f) ? va[u] * fsc : 0.f;
+                    if (s < NSRC) ft[s] = o[u];
+                }
+                reinterpret_cast<float4 *>(fr)[q] = make_float4(o[0], o[1], o[2], o[3]);
+            }
+            // u~[k] = w~_succ(k)[k] * 2^(E_succ - Eb)
+            const bool live = fsc > 0.f;
+            const float uM = (live && EM > EXP_NONE) ? fminf(scale_pow2(1.f, EM - Eb), 3e38f) : 0.f;
+            const float uI = (live && EI > EXP_NONE) ? fminf(scale_pow2(1.f, EI - Eb), 3e38f) : 0.f;
+            const float uD = (live && ED > EXP_NONE) ? fminf(scale_pow2(1.f, ED - Eb), 3e38f) : 0.f;
+#pragma unroll
+            for (int q = 0; q < KP / 4; ++q) {
+                float uq[4];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const int k = 4 * q + v;
+                    float u = 0.f;
+                    if (k < NE) {
+                        const int ty = SH::type_of(k);
+                        u = ty == T_M ? dR[k] * uM : (ty == T_I ? wn[k] * uI : dnew[k] * uD);
+                    }
+                    uq[v] = u;
+                }
+                reinterpret_cast<float4 *>(ust + r * KPP)[q] = make_float4(uq[0], uq[1], uq[2], uq[3]);
+            }
+            if (live) {
+#pragma unroll
+                for (int k = 0; k < NE; ++k) {
+                    const float pk = ft[k] * br[k];
+                    const int ty = SH::type_of(k);
+                    if (ty == T_M) {
+                        if (pk != 0.f) atomicAdd(cntM_pair + P.w_group[k] * 441 + xch * 21 + yj, (double)pk);
+                    } else if (ty == T_I) {
+                        colI[(jc % ROWS) * NI + (k - NM)] += pk;
+                    } else {
+                        const int kd = k - NM - NI;
+                        const float y = pk - dcmp[kd];
+                        const float tt = dcnt[kd] + y;
+                        dcmp[kd] = (tt - dcnt[kd]) - y;
+                        dcnt[kd] = tt;
+                    }
+                }
+                if (term) {   // expected End transitions
+#pragma unroll
+                    for (int s = 0; s < NSRC; ++s)
+                        atomicAdd(P.n_trans + ((int64_t)p * N + P.w_orig[s]) * N + P.e_idx, (double)(ft[s] * br[s]));
+                }
+            }
+        }
+        // row 32 hands its w~ at step t to row 31 for step t-1 (read after the
+        // next step's first barrier; the other parity is being read now)
+        if (r == 32) {
+#pragma unroll
+            for (int k = 0; k < NE; ++k) slot[(t & 1) * SP + k] = wcur[k];
+            slotE[t & 1] = Eb;
+        }
+        __syncthreads();   // ust, the scaled f~ rows and colI complete for step t
+        if (count) {
+            // column t is complete once row i0 (thread 0) has visited it
+            if (r == 0 && t <= Ly) {
+                const int sl = t % ROWS;
+                const int yt = ys[t];
+#pragma unroll
+                for (int k = 0; k < NI; ++k) {
+                    bins[P.w_group[NM + k] * 21 + yt] += colI[sl * NI + k];
+                    colI[sl * NI + k] = 0.f;
+                }
+            }
+            if (counter) {
+                float pz[16];
+#pragma unroll
+                for (int u = 0; u < 16; ++u) pz[u] = 0.f;
+                const float *fb = fbuf + buf * ROWS * SPP;
+                auto row_outer = [&](int rr) {
+                    const float4 fv = reinterpret_cast<const float4 *>(fb + rr * SPP)[bs];
+                    const float4 uv = reinterpret_cast<const float4 *>(ust + rr * KPP)[bk];
+                    const float fa[4] = {fv.x, fv.y, fv.z, fv.w};
+                    const float ua[4] = {uv.x, uv.y, uv.z, uv.w};
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) pz[4 * a + b] = fmaf(fa[a], ua[b], pz[4 * a + b]);
+                };
+                if constexpr (ROWS % GROUPS64 == 0) {
+                    constexpr int RPG = ROWS / GROUPS64;
+                    const int r0 = grp * RPG;
+#pragma unroll 4
+                    for (int rr = r0; rr < r0 + RPG; ++rr) row_outer(rr);
+                } else {
+                    const int r0 = grp * ROWS / GROUPS64, r1 = (grp + 1) * ROWS / GROUPS64;
+                    for (int rr = r0; rr < r1; ++rr) row_outer(rr);
+                }
+#pragma unroll
+                for (int u = 0; u < 16; ++u) {
+                    const float y = pz[u] - ccomp[u];
+                    const float tt = csum[u] + y;
+                    ccomp[u] = (tt - csum[u]) - y;
+                    csum[u] = tt;
+                }
+            }
+        }
+        // ---- shift histories
+#pragma unroll
+        for (int k = 0; k < NE; ++k) {
+            dR[k] = dnew[k];
+            wn[k] = wcur[k];
+        }
+        EdR = Ednew;
+        Ewn = Eb;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    // ---- flush the chunk's partial counts (float64 reductions)
+    if (counter) {
+        const float *chi = P.chi + (int64_t)p * P.chi_stride;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            const int s = 4 * bs + (u >> 2), k = 4 * bk + (u & 3);
+            const float val = csum[u] - ccomp[u];
+            if (s >= NSRC || k >= NE || val == 0.f) continue;
+            const int os = P.w_orig[s], ok = P.w_orig[k];
+            atomicAdd(P.n_trans + ((int64_t)p * N + os) * N + ok, (double)val * (double)__ldg(chi + os * N + ok));
+        }
+    }
+    if (r < nrows && rowi >= 1) {
+#pragma unroll
+        for (int k = 0; k < ND; ++k) {
+            const float v = dcnt[k] - dcmp[k];
+            if (v != 0.f) atomicAdd(P.cntD + ((int64_t)p * G + P.w_group[NM + NI + k]) * 21 + xch, (double)v);
+        }
+    }
+    // I-type columns not completed inside the chunk (touched by rows below row 0)
+    for (int j = max(0, t0 - (ROWS - 1)) + r; j <= min(Ly, t0 - 1); j += TWT) {
+        const int sl = j % ROWS;
+        const int yt = ys[j];
+#pragma unroll
+        for (int k = 0; k < NI; ++k) {
+            const float v = colI[sl * NI + k];
+            if (v != 0.f) atomicAdd(P.cntI + ((int64_t)p * G + P.w_group[NM + k]) * 21 + yt, (double)v);
+        }
+    }
+    for (int idx = r; idx < G * 21; idx += TWT) {
+        const float v = bins[idx];
+        if (v != 0.f) atomicAdd(P.cntI + (int64_t)p * G * 21 + idx, (double)v);
+    }
+    __syncthreads();
+}
+
+template <class SH>
+__global__ void __launch_bounds__(TWT) count_tw_kernel(const KParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *sm = reinterpret_cast<float *>(smem_raw);
+    const SmemCT L = make_smem_ct(SH::SP, SH::KP, SH::NI, P.G, P.max_ly);
+    int *s_item = reinterpret_cast<int *>(sm) + L.item;
+    for (;;) {
+        if (threadIdx.x == 0) *s_item = atomicAdd(P.counter, 1);
+        __syncthreads();
+        const int it = *s_item;
+        __syncthreads();
+        if (it >= P.n_items) break;
+        const int2 w = P.items[it];
+        count_chunk_tw<SH>(P, w.x, w.y >> 12, w.y & 4095, L, sm, smem_raw);
+    }
+}
+
+}  // namespace warp2

@@ -1612,7 +1612,11 @@ template <class SH>
 int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, cudaStream_t stream) {
     void (*kern)(const KParams) = nullptr;
     int bytes = 0, threads = 32;
-    if (kind == 3) {
+    if (kind == 3 && plan->two_warp) {   // count pass of the two-warp split E-step
+        bytes = warp2::make_smem_ct(SH::SP, SH::KP, SH::NI, K.G, max_ly).bytes;
+        kern = warp2::count_tw_kernel<SH>;
+        threads = warp2::TWT;
+    } else if (kind == 3) {
         bytes = warp2::make_smem_c(SH::SP, SH::KP, SH::NI, K.G, max_ly).bytes;
         kern = warp2::count_warp_kernel<SH>;
     } else if (kind == 5 || kind == 6) {   // two-warp stripes: forward / backward recursion

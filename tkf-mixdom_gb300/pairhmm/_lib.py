@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import threading
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -228,15 +229,19 @@ class DeviceBatch:
 
 def pack_residues(xs, ys):
     """Concatenate residues of all pairs: [x_0, y_0, x_1, y_1, ...] (uint8)."""
-    parts = []
-    for x, y in zip(xs, ys):
-        parts.append(np.asarray(x).reshape(-1))
-        parts.append(np.asarray(y).reshape(-1))
-    lens = np.fromiter((a.size for a in parts), dtype=np.int64, count=len(parts))
-    offs = np.zeros(len(parts), np.int64)
-    if len(parts) > 1:
+    P = len(xs)
+    if len(ys) != P:
+        raise ValueError('xs and ys must hold the same number of sequences')
+    parts = [None] * (2 * P)
+    parts[0::2] = xs
+    parts[1::2] = ys
+    lens = np.fromiter(map(len, parts), dtype=np.int64, count=2 * P)
+    offs = np.zeros(2 * P, np.int64)
+    if P:
         np.cumsum(lens[:-1], out=offs[1:])
-    allr = np.concatenate(parts) if parts else np.zeros(0, np.int64)
+    allr = np.concatenate(parts) if lens.sum() else np.zeros(0, np.int64)
+    if allr.ndim != 1:
+        raise ValueError('sequences must be one-dimensional')
     if allr.dtype.kind not in 'iu':
         allr = allr.astype(np.int64)
     if allr.size and (allr.min() < 0 or allr.max() > 20):
@@ -246,6 +251,46 @@ def pack_residues(xs, ys):
         buf = np.zeros(16, np.uint8)
     return (buf, offs[0::2].copy(), offs[1::2].copy(),
             lens[0::2].astype(np.int32), lens[1::2].astype(np.int32))
+
+
+_STAGE = {}
+_STAGE_LOCK = threading.Lock()
+
+
+def to_host(tensors):
+    """Copy a dict of device tensors to host numpy arrays with one
+    synchronisation: asynchronous copies into a reused pinned staging buffer
+    on the current stream, then one wait; the arrays returned are copies."""
+    items = [(k, v) for k, v in tensors.items() if isinstance(v, torch.Tensor)]
+    if not items:
+        return dict(tensors)
+    dev = items[0][1].device
+    if dev.type != 'cuda':
+        return {k: (v.numpy() if isinstance(v, torch.Tensor) else v) for k, v in tensors.items()}
+    with _STAGE_LOCK:
+        return _to_host_staged(tensors, items, dev)
+
+
+def _to_host_staged(tensors, items, dev):
+    sizes = [(v.numel() * v.element_size() + 255) // 256 * 256 for _, v in items]
+    total = sum(sizes)
+    buf = _STAGE.get(dev)
+    if buf is None or buf.numel() < total:
+        buf = torch.empty(max(total, 1 << 20), dtype=torch.uint8, pin_memory=True)
+        _STAGE[dev] = buf
+    views, o = {}, 0
+    for (k, v), n in zip(items, sizes):
+        nb = v.numel() * v.element_size()
+        hv = buf[o:o + nb].view(v.dtype).view(v.shape)
+        hv.copy_(v.contiguous(), non_blocking=True)
+        views[k] = hv
+        o += n
+    torch.cuda.current_stream(dev).synchronize()
+    out = {k: v.numpy().copy() for k, v in views.items()}
+    for k, v in tensors.items():
+        if k not in out:
+            out[k] = v
+    return out
 
 
 def make_batch(xs, ys, chi, emit_M, emit_I, emit_D, device='cuda'):

@@ -335,6 +335,12 @@ def _mixdom2_tables(params, ts, device):
     return K, F, chi, csubs, EM, EI, ED
 
 
+def to_host(result):
+    """A result dict of device tensors as host numpy arrays, copied with one
+    synchronisation (asynchronous copies into reused pinned memory)."""
+    return _lib.to_host(result)
+
+
 def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True):
     """Batched MixDom2 E-step over pairs of any lengths in one persistent
     launch (replaces the bucketed jit(vmap(forward_backward_2d)) callers).

@@ -62,7 +62,7 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
     int *bndE = reinterpret_cast<int *>(sm) + LT.bndE;
     volatile int *s_abort = reinterpret_cast<int *>(sm) + LT.flag;
 
-    if (r < 32) load_model_w<SH>(P, p, m, L, sm, smb, false);
+    if (r < 32) load_model_w<SH>(P, p, m, L, sm, smb, CHI_FWD_PAIRS);
     if (r < 2 * SP) bnd[r] = 0.f;
     if (r < 2) bndE[r] = EXP_NONE;
     if (r < 2) s_abort[r] = 0;
@@ -82,10 +82,15 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
 #pragma unroll
     for (int k = 0; k < NI; ++k) offI[k] = L.tI + P.w_group[NM + k] * 21;
 
-    float prev[NSRC], d0[NSRC], m0[NSRC];
+    // state vectors as pairs of sources (s, s+1): the contraction runs on
+    // paired FMAs (__ffma2_rn), even and odd sources in the two halves
+    constexpr int SQ = SP / 2;
+    float2 prev[SQ], d0[SQ], m0[SQ];
     int Eprev = EXP_NONE, Em0 = EXP_NONE;
 #pragma unroll
-    for (int s = 0; s < NSRC; ++s) { prev[s] = 0.f; d0[s] = 0.f; m0[s] = 0.f; }
+    for (int q = 0; q < SQ; ++q) {
+        prev[q] = make_float2(0.f, 0.f); d0[q] = make_float2(0.f, 0.f); m0[q] = make_float2(0.f, 0.f);
+    }
     const int T_last = (nrows - 1) + Ly;
     // M- and I-type emission factors of the cell of the next step, loaded one
     // step ahead (the y character and the table lookup are two dependent loads)
@@ -143,35 +148,41 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
         int EdA = __shfl_up_sync(0xffffffffu, Eprev, 1);
         EdA = l0 ? (top ? (halo ? hxE : EXP_NONE) : bndE[slot]) : EdA;
 #pragma unroll
-        for (int s = 0; s < NSRC; ++s) {
-            const float v = __shfl_up_sync(0xffffffffu, prev[s], 1);
-            d0[s] = l0 ? (top ? (halo ? hx[s] : 0.f) : bv[s]) : v;
+        for (int q = 0; q < SQ; ++q) {
+            if (2 * q >= NSRC) continue;   // padding pairs stay zero
+            const float vx = __shfl_up_sync(0xffffffffu, prev[q].x, 1);
+            const float vy = __shfl_up_sync(0xffffffffu, prev[q].y, 1);
+            d0[q].x = l0 ? (top ? (halo ? hx[2 * q] : 0.f) : bv[2 * q]) : vx;
+            d0[q].y = l0 ? (top ? (halo ? hx[2 * q + 1] : 0.f) : bv[2 * q + 1]) : vy;
         }
         const bool hasI = jc >= 1, hasD = rowi >= 1, hasM = hasI && hasD;
         const int EI = hasI ? Eprev : EXP_NONE, ED = hasD ? EdA : EXP_NONE, EM = hasM ? Em0 : EXP_NONE;
         const int Eref = max(max(EI, ED), EM);
-        float acc[NE];
+        float2 acc2[NE];
 #pragma unroll
-        for (int k = 0; k < NE; ++k) acc[k] = 0.f;
+        for (int k = 0; k < NE; ++k) acc2[k] = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int s = 0; s < NSRC; ++s) {
-            const float pI = prev[s], pD = d0[s], pM = m0[s];
-            const float4 *row = chi4 + s * (KP / 4);
+        for (int q = 0; q < SQ; ++q) {
+            if (2 * q >= NSRC) continue;
+            const float4 *row = chi4 + q * (KP / 2);   // sources 2q, 2q+1 for all destinations
 #pragma unroll
-            for (int kq = 0; kq < KP / 4; ++kq) {
-                const float4 cv = row[kq];
-                const float cvs[4] = {cv.x, cv.y, cv.z, cv.w};
+            for (int kp = 0; kp < KP / 2; ++kp) {
+                const float4 cv = row[kp];             // (k, k+1) x (2q, 2q+1)
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int k = 4 * kq + u;
+                for (int u = 0; u < 2; ++u) {
+                    const int k = 2 * kp + u;
                     if (k < NE) {
                         const int ty = SH::type_of(k);
-                        const float pk = ty == T_M ? pM : (ty == T_I ? pI : pD);
-                        acc[k] = fmaf(pk, cvs[u], acc[k]);
+                        const float2 pk = ty == T_M ? m0[q] : (ty == T_I ? prev[q] : d0[q]);
+                        acc2[k] = __ffma2_rn(pk, u == 0 ? make_float2(cv.x, cv.y) : make_float2(cv.z, cv.w),
+                                             acc2[k]);
                     }
                 }
             }
         }
+        float acc[NE];
+#pragma unroll
+        for (int k = 0; k < NE; ++k) acc[k] = acc2[k].x + acc2[k].y;
         // emissions, type scales, per-cell renormalisation
         const float sM = hasM ? pow2f(EM - Eref) : 0.f, sI = hasI ? pow2f(EI - Eref) : 0.f;
         const float sD = hasD ? pow2f(ED - Eref) : 0.f;
@@ -251,16 +262,19 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
         }
         // shift the register history
 #pragma unroll
-        for (int s = 0; s < NSRC; ++s) {
-            m0[s] = d0[s];
-            prev[s] = s < NE ? acc[s] : (s == NE ? sNew : 0.f);
+        for (int q = 0; q < SQ; ++q) {
+            m0[q] = d0[q];
+            const int s0 = 2 * q, s1 = 2 * q + 1;
+            prev[q].x = s0 < NE ? acc[s0] : (s0 == NE ? sNew : 0.f);
+            prev[q].y = s1 < NE ? acc[s1] : (s1 == NE ? sNew : 0.f);
         }
         Em0 = EdA;
         Eprev = Enew;
         // row 31 hands its new state to row 32 for step t+1
         if (r == 31) {
+            float2 *b2 = reinterpret_cast<float2 *>(bnd + (t & 1) * SP);
 #pragma unroll
-            for (int s = 0; s < SP; ++s) bnd[(t & 1) * SP + s] = s < NSRC ? prev[s] : 0.f;
+            for (int q = 0; q < SQ; ++q) b2[q] = prev[q];
             bndE[t & 1] = Eprev;
         }
         load_emit(t + 1);
@@ -299,7 +313,7 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
 template <class SH>
 __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT, float *sm,
                                   unsigned char *smb) {
-    constexpr int NE = SH::NE, NSRC = SH::NSRC, SP = SH::SP, NM = SH::NM, NI = SH::NI;
+    constexpr int NE = SH::NE, NSRC = SH::NSRC, SP = SH::SP, KP = SH::KP, NM = SH::NM, NI = SH::NI;
     const SmemW &L = LT.w;
     const PairMeta m = P.meta[p];
     const int Lx = m.Lx, Ly = m.Ly;
@@ -319,7 +333,7 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
     int *bndE = reinterpret_cast<int *>(sm) + LT.bndE;
     volatile int *s_abort = reinterpret_cast<int *>(sm) + LT.flag;
 
-    if (r < 32) load_model_w<SH>(P, p, m, L, sm, smb, true);
+    if (r < 32) load_model_w<SH>(P, p, m, L, sm, smb, CHI_BWD_PAIRS);
     if (r < 2 * SP) bnd[r] = 0.f;
     if (r < 2) bndE[r] = EXP_NONE;
     if (r < 2) s_abort[r] = 0;
@@ -341,10 +355,14 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
 
     // successors: I = own cell at step t+1 (wn), D = row r+1 at step t+1
     // (dR, received by shuffle or boundary slot), M = the D received at t+1 (mR)
-    float wn[NE], dR[NE], mR[NE];
+    // (as pairs of destinations (k, k+1): the contraction runs on paired FMAs)
+    constexpr int KQ = KP / 2;
+    float2 wn[KQ], dR[KQ], mR[KQ];
     int Ewn = EXP_NONE, EmR = EXP_NONE;
 #pragma unroll
-    for (int k = 0; k < NE; ++k) { wn[k] = 0.f; dR[k] = 0.f; mR[k] = 0.f; }
+    for (int q = 0; q < KQ; ++q) {
+        wn[q] = make_float2(0.f, 0.f); dR[q] = make_float2(0.f, 0.f); mR[q] = make_float2(0.f, 0.f);
+    }
 
     const int T_last = (nrows - 1) + Ly;
     // M- and I-type emission factors of the cell of the next step, loaded one step ahead
@@ -400,9 +418,12 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
         int EdRn = __shfl_down_sync(0xffffffffu, Ewn, 1);
         EdRn = l31 ? (bottom ? (halo ? hxE : EXP_NONE) : bndE[slot]) : EdRn;
 #pragma unroll
-        for (int k = 0; k < NE; ++k) {
-            const float v = __shfl_down_sync(0xffffffffu, wn[k], 1);
-            dR[k] = l31 ? (bottom ? (halo ? hx[k] : 0.f) : bv[k]) : v;
+        for (int q = 0; q < KQ; ++q) {
+            if (2 * q >= NE) continue;   // padding pairs stay zero
+            const float vx = __shfl_down_sync(0xffffffffu, wn[q].x, 1);
+            const float vy = __shfl_down_sync(0xffffffffu, wn[q].y, 1);
+            dR[q].x = l31 ? (bottom ? (halo ? hx[2 * q] : 0.f) : bv[2 * q]) : vx;
+            dR[q].y = l31 ? (bottom ? (halo ? hx[2 * q + 1] : 0.f) : bv[2 * q + 1]) : vy;
         }
         const bool term = valid && rowi == Lx && jc == Ly;
         const bool hI = jc + 1 <= Ly, hD = rowi + 1 <= Lx, hM = hI && hD;
@@ -410,26 +431,42 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
         const int Eref = term ? 0 : max(max(EI, ED), EM);
         const float sM = (hM && !term) ? pow2f(EM - Eref) : 0.f, sI = (hI && !term) ? pow2f(EI - Eref) : 0.f;
         const float sD = (hD && !term) ? pow2f(ED - Eref) : 0.f;
-        float acc[NSRC];
+        // successor weights w_k, paired (k, k+1)
+        float2 w2[KQ];
 #pragma unroll
-        for (int s = 0; s < NSRC; ++s) acc[s] = 0.f;
+        for (int q = 0; q < KQ; ++q) {
+            float wv[2];
 #pragma unroll
-        for (int k = 0; k < NE; ++k) {
-            const float dk = dR[k];
-            const int ty = SH::type_of(k);
-            const float w = ty == T_M ? mR[k] * sM : (ty == T_I ? wn[k] * sI : dk * sD);
-            const float4 *col = chiB4 + k * (SP / 4);
-#pragma unroll
-            for (int sq = 0; sq < SP / 4; ++sq) {
-                const float4 cv = col[sq];
-                const float cvs[4] = {cv.x, cv.y, cv.z, cv.w};
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int s = 4 * sq + u;
-                    if (s < NSRC) acc[s] = fmaf(w, cvs[u], acc[s]);
+            for (int u = 0; u < 2; ++u) {
+                const int k = 2 * q + u;
+                float w = 0.f;
+                if (k < NE) {
+                    const int ty = SH::type_of(k);
+                    const float vm = u ? mR[q].y : mR[q].x, vi = u ? wn[q].y : wn[q].x, vd = u ? dR[q].y : dR[q].x;
+                    w = ty == T_M ? vm * sM : (ty == T_I ? vi * sI : vd * sD);
                 }
+                wv[u] = w;
+            }
+            w2[q] = make_float2(wv[0], wv[1]);
+        }
+        float2 acc2[NSRC];
+#pragma unroll
+        for (int s2 = 0; s2 < NSRC; ++s2) acc2[s2] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < KQ; ++q) {
+            if (2 * q >= NE) continue;
+            const float4 *row = chiB4 + q * (SP / 2);   // destinations 2q, 2q+1 for all sources
+#pragma unroll
+            for (int sp = 0; sp < SP / 2; ++sp) {
+                const float4 cv = row[sp];             // (2q, 2q+1) x (s, s+1)
+                if (2 * sp < NSRC) acc2[2 * sp] = __ffma2_rn(w2[q], make_float2(cv.x, cv.y), acc2[2 * sp]);
+                if (2 * sp + 1 < NSRC)
+                    acc2[2 * sp + 1] = __ffma2_rn(w2[q], make_float2(cv.z, cv.w), acc2[2 * sp + 1]);
             }
         }
+        float acc[NSRC];
+#pragma unroll
+        for (int s2 = 0; s2 < NSRC; ++s2) acc[s2] = acc2[s2].x + acc2[s2].y;
         if (term) {
 #pragma unroll
             for (int s = 0; s < NSRC; ++s) acc[s] = sm[L.chiE + s];
@@ -491,16 +528,21 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
             }
         }
 #pragma unroll
-        for (int k = 0; k < NE; ++k) {
-            mR[k] = dR[k];
-            wn[k] = valid ? wnew[k] : 0.f;
+        for (int q = 0; q < KQ; ++q) {
+            mR[q] = dR[q];
+            const int k0 = 2 * q, k1 = 2 * q + 1;
+            wn[q].x = (valid && k0 < NE) ? wnew[k0] : 0.f;
+            wn[q].y = (valid && k1 < NE) ? wnew[k1] : 0.f;
         }
         EmR = EdRn;
         Ewn = valid ? Eb : EXP_NONE;
         // row 32 hands its new state to row 31 for step t-1
         if (r == 32) {
+            float2 *b2 = reinterpret_cast<float2 *>(bnd + (t & 1) * SP);
 #pragma unroll
-            for (int k = 0; k < SP; ++k) bnd[(t & 1) * SP + k] = k < NE ? wn[k] : 0.f;
+            for (int q = 0; q < KQ; ++q) b2[q] = wn[q];
+#pragma unroll
+            for (int q = KQ; q < SP / 2; ++q) b2[q] = make_float2(0.f, 0.f);
             bndE[t & 1] = Ewn;
         }
         load_emit(t - 1);

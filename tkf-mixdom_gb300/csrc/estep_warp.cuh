@@ -81,11 +81,16 @@ __host__ __device__ inline SmemW make_smem_w(int SP, int KP, int NI, int G, int 
     return make_smem_w(SP, KP, NI, G, max_ly, bwd, bwd);
 }
 
-// Per-stripe model load into shared memory (one warp).  Forward layout:
-// chi[s*KP + k]; backward layout (transposed): chi[k*SP + s].
+// Per-stripe model load into shared memory (one warp).  chi layouts:
+// 0 forward chi[s*KP + k]; 1 backward (transposed) chi[k*SP + s]; 2 forward
+// with source pairs interleaved, chi[(s/2)*2KP + 2k + s%2] (one float4 holds
+// sources s, s+1 for destinations k, k+1); 3 backward with destination pairs
+// interleaved, chi[(k/2)*2SP + 2s + k%2].
+constexpr int CHI_FWD = 0, CHI_BWD = 1, CHI_FWD_PAIRS = 2, CHI_BWD_PAIRS = 3;
+
 template <class SH>
 __device__ void load_model_w(const KParams &P, int p, const PairMeta &m, const SmemW &L, float *sm,
-                             unsigned char *smb, bool bwd) {
+                             unsigned char *smb, int layout) {
     const int lane = threadIdx.x & 31;
     const int N = P.N, G = P.G;
     const float *chi = P.chi + (int64_t)p * P.chi_stride;
@@ -93,7 +98,12 @@ __device__ void load_model_w(const KParams &P, int p, const PairMeta &m, const S
         const int s = idx / SH::KP, k = idx % SH::KP;
         float v = 0.f;
         if (s < SH::NSRC && k < SH::NE) v = __ldg(chi + P.w_orig[s] * N + P.w_orig[k]);
-        if (bwd) sm[L.chi + k * SH::SP + s] = v; else sm[L.chi + s * SH::KP + k] = v;
+        int at;
+        if (layout == CHI_FWD) at = s * SH::KP + k;
+        else if (layout == CHI_BWD) at = k * SH::SP + s;
+        else if (layout == CHI_FWD_PAIRS) at = (s >> 1) * (2 * SH::KP) + 2 * k + (s & 1);
+        else at = (k >> 1) * (2 * SH::SP) + 2 * s + (k & 1);
+        sm[L.chi + at] = v;
     }
     for (int s = lane; s < SH::SP; s += 32)
         sm[L.chiE + s] = (s < SH::NSRC) ? __ldg(chi + P.w_orig[s] * N + P.e_idx) : 0.f;

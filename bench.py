@@ -499,7 +499,7 @@ def main():
            6: ((('wide::forward_wide_kernel', 2) if fwd_only else ('wide::fwdbwd_wide_kernel', 4)), (None, 0),
                ('wide::count_wide_kernel', 2)),
            7: (('warp2::stripe_tw_kernel<...,0>', 2), ('warp2::stripe_tw_kernel<...,1>', 2),
-               ('warp2::count_warp_kernel', 2))}[plan.last_variant]
+               ('warp2::count_tw_kernel', 2))}[plan.last_variant]
     durs = [fwd_avg, bwd_avg, cnt_avg]
     # the overlapped count pass (variants 4, 7) starts with the wavefronts and waits
     # on their progress, so its event span is not its own duration

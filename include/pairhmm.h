@@ -201,6 +201,26 @@ int phmm_mixdom2_tables(const phmm_mixdom2_params *prm, int32_t n_pairs, const d
                         float *chi, float *emit_M, float *emit_I, float *emit_D,
                         double *class_subs, void *stream);
 
+/* TKF91 / TKF92 parameters (host float64): insertion and deletion rates,
+ * fragment extension probability (0 for TKF91), the substitution rate
+ * matrix Q [A][A] (rows summing to zero) and its equilibrium pi [A]; A = 20. */
+typedef struct phmm_tkf92_params {
+    double ins_rate, del_rate, ext;
+    int32_t alphabet;
+    const double *Q;
+    const double *pi;
+} phmm_tkf92_params;
+
+/* Device prologue of the batched TKF92 E-step / forward: for per-pair times
+ * t (device [P] float64) write chi (device float32 [P][5][5], the TKF92
+ * matrix floored at 1e-30 as train/tkf92_svi_bw.py:164 takes
+ * log(max(tau, 1e-30))), the emission tables (emit_M [P][1][21][21],
+ * emit_I / emit_D [P][1][21], dp/hmm.py:628-670) and P(t) = expm(t Q)
+ * (device float64 [P][A][A]).  Replaces the per-pair builders of
+ * train/tkf92_svi_bw.py:263-365.  Stream-ordered; allocates nothing. */
+int phmm_tkf92_tables(const phmm_tkf92_params *prm, int32_t n_pairs, const double *t, float *chi,
+                      float *emit_M, float *emit_I, float *emit_D, double *sub, void *stream);
+
 /* Device epilogue of the MixDom2 E-step: the per-class sufficient statistics
  * of train/likelihood.py:279-344 from phmm_estep's per-group character
  * counts (cnt_M [P][KF][21][21], cnt_I / cnt_D [P][KF][21]) and the

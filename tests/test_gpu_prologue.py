@@ -1,4 +1,5 @@
-"""Device prologue of the MixDom2 E-step (phmm_mixdom2_tables) against the
+"""Device prologues of the MixDom2 and TKF92 E-steps (phmm_mixdom2_tables,
+phmm_tkf92_tables) and the class-count epilogue against the
 float64 torch builders, which the oracle tests pin to the reference.
 
 Bars: chi and the emission tables are float32 roundings of float64 values,
@@ -113,3 +114,29 @@ def test_class_count_epilogue_matches_torch(cuda_lib, K, F, C):
     want = api.class_split(p, cM, cI, cD, csubs=cs)
     for k, v in want.items():
         torch.testing.assert_close(got[k], v, rtol=1e-12, atol=1e-12, msg=k)
+
+
+@pytest.mark.parametrize('ext,equal_rates', [(0.0, False), (0.4, False), (0.3, True)])
+def test_tkf92_prologue_matches_float64_builders(cuda_lib, ext, equal_rates):
+    """phmm_tkf92_tables against the float64 torch builders of the batched
+    TKF92 path (chi floored at 1e-30, expm(t Q), pair-HMM emission tables)."""
+    from pairhmm import synth, _lib
+    from pairhmm import models as pm
+    rng = np.random.default_rng(31 + int(10 * ext) + int(equal_rates))
+    p = synth.tkf_params(rng, ext=ext)
+    if equal_rates:
+        p['del_rate'] = p['ins_rate'] * (1 + 1e-6)
+    ts = np.concatenate([[1e-6, 0.01, 1.0, 30.0], np.exp(rng.uniform(-3, 1, 12))])
+    chi, EM, EI, ED, sub = _lib.tkf92_tables(p['ins_rate'], p['del_rate'], ext, p['Q'], p['pi'], ts,
+                                             device='cuda')
+    t = torch.as_tensor(ts)
+    rchi = pm.tkf92_trans(p['ins_rate'], p['del_rate'], t, ext).clamp_min(1e-30)
+    rsub = pm.transition_matrix(pm._t(p['Q']), t)
+    rEM, rEI, rED = pm.tables_tkf(rsub, pm._t(p['pi']))
+    torch.testing.assert_close(chi.cpu(), rchi.float(), rtol=F32_RTOL, atol=1e-14)
+    big = rsub.abs() > 1e-14
+    rel = ((sub.cpu() - rsub).abs() / rsub.abs().clamp_min(1e-300))[big]
+    assert rel.max().item() < EXPM_RTOL, rel.max().item()
+    torch.testing.assert_close(EM.cpu(), rEM.float(), rtol=F32_RTOL, atol=1e-14)
+    torch.testing.assert_close(EI.cpu(), rEI.float().expand_as(EI.cpu()), rtol=F32_RTOL, atol=1e-14)
+    torch.testing.assert_close(ED.cpu(), rED.float().expand_as(ED.cpu()), rtol=F32_RTOL, atol=1e-14)

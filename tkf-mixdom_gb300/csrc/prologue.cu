@@ -45,6 +45,7 @@ constexpr int THREADS = 256;
 // Parameter block passed by value (kernel parameters hold up to 32 KB).
 struct Packed {
     int K, F, C;
+    int q_direct;   // 1: v + o_S holds the rate matrix Q itself (TKF models), 0: exchangeabilities S
     int o_dins, o_ddel, o_dw, o_fw, o_ext, o_pis, o_S, o_cd;
     double main_ins, main_del;
     double v[MAXV];
@@ -293,16 +294,20 @@ expm_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, d
     const double t = ts[p];
     const double *Sx = prm.v + prm.o_S + (size_t)c * nn, *pi = prm.v + prm.o_pis + c * n;
 
-    // Q[a][b] = S[a][b] pi[b] off the diagonal, rows summing to zero (train/vjp.py:463-476)
-    for (int idx = tid; idx < nn; idx += blockDim.x) {
-        const int a = idx / n, b = idx % n;
-        X[idx] = a == b ? 0.0 : Sx[idx] * pi[b];
-    }
-    __syncthreads();
-    if (tid < n) {
-        double s = 0.0;
-        for (int b = 0; b < n; ++b) s += X[tid * n + b];
-        X[tid * n + tid] = -s;
+    if (prm.q_direct) {   // the caller's rate matrix (core/ctmc.py:31-60 takes Q as given)
+        for (int idx = tid; idx < nn; idx += blockDim.x) X[idx] = Sx[idx];
+    } else {
+        // Q[a][b] = S[a][b] pi[b] off the diagonal, rows summing to zero (train/vjp.py:463-476)
+        for (int idx = tid; idx < nn; idx += blockDim.x) {
+            const int a = idx / n, b = idx % n;
+            X[idx] = a == b ? 0.0 : Sx[idx] * pi[b];
+        }
+        __syncthreads();
+        if (tid < n) {
+            double s = 0.0;
+            for (int b = 0; b < n; ++b) s += X[tid * n + b];
+            X[tid * n + tid] = -s;
+        }
     }
     __syncthreads();
     for (int idx = tid; idx < nn; idx += blockDim.x) X[idx] *= t;
@@ -498,6 +503,46 @@ class_split_kernel(const __grid_constant__ Packed prm, const double *__restrict_
     for (int i = tid; i < G * C; i += blockDim.x) cdist[(size_t)p * G * C + i] = cs_acc[i];
 }
 
+// ---------------------------------------------------------------- TKF92 prologue
+// chi = TKF92 [5][5] (core/params.py:94-133: M/I/D rows scaled by 1 - ext,
+// ext added on their diagonal) with every entry floored at 1e-30, the
+// log(max(tau, 1e-30)) of train/tkf92_svi_bw.py:164; one thread per pair.
+__global__ void tkf92_chi_kernel(double lam, double mu, double ext, const double *__restrict__ ts, int P,
+                                 float *__restrict__ chi) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    double tau[25];
+    tkf91(lam, mu, ts[p], tau);
+    for (int u = 0; u < 5; ++u)
+        for (int v = 0; v < 5; ++v) {
+            const bool emit_row = u == M || u == I || u == D;
+            double x = emit_row ? tau[u * 5 + v] * (1.0 - ext) + (u == v ? ext : 0.0) : tau[u * 5 + v];
+            chi[(size_t)p * 25 + u * 5 + v] = (float)fmax(x, 1e-30);
+        }
+}
+
+// pair-HMM emission tables of one substitution model (dp/hmm.py:628-670):
+// EM[a][b] = (pi[a] + 1e-30)(P[a][b] + 1e-30), EI = ED = pi + 1e-30, wildcard 1
+struct TkfPi { double v[NA]; };
+
+__global__ void __launch_bounds__(THREADS)
+tkf_tables_kernel_v(const TkfPi pi, const double *__restrict__ sub, float *__restrict__ EM,
+                    float *__restrict__ EI, float *__restrict__ ED) {
+    const int p = blockIdx.x, tid = threadIdx.x;
+    const double *Pp = sub + (size_t)p * NA * NA;
+    for (int idx = tid; idx < 441; idx += blockDim.x) {
+        const int a = idx / 21, b = idx % 21;
+        const double lp = a < NA ? pi.v[a] + 1e-30 : 1.0;
+        const double ls = (a < NA && b < NA) ? Pp[a * NA + b] + 1e-30 : 1.0;
+        EM[(size_t)p * 441 + idx] = (float)(lp * ls);
+    }
+    for (int a = tid; a < 21; a += blockDim.x) {
+        const float v = (float)(a < NA ? pi.v[a] + 1e-30 : 1.0);
+        EI[(size_t)p * 21 + a] = v;
+        ED[(size_t)p * 21 + a] = v;
+    }
+}
+
 }  // namespace pro
 
 static int pro_fail(int code, const char *msg) {
@@ -603,6 +648,35 @@ extern "C" int phmm_mixdom2_class_counts(const phmm_mixdom2_params *prm, int32_t
     const size_t smem = sizeof(double) * pk.K * pk.F * pk.C;
     class_split_kernel<<<n_pairs, THREADS, smem, (cudaStream_t)stream>>>(
         pk, class_subs, cnt_M, cnt_I, cnt_D, class_match, class_insert, class_delete, classdist_counts);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    return PHMM_OK;
+}
+
+extern "C" int phmm_tkf92_tables(const phmm_tkf92_params *prm, int32_t n_pairs, const double *t, float *chi,
+                                 float *emit_M, float *emit_I, float *emit_D, double *sub, void *stream) {
+    using namespace pro;
+    if (!prm) return pro_fail(PHMM_E_ARG, "phmm_tkf92_tables: null parameters");
+    if (prm->alphabet != NA) return pro_fail(PHMM_E_ARG, "phmm_tkf92_tables: alphabet must be 20");
+    if (!prm->Q || !prm->pi) return pro_fail(PHMM_E_ARG, "phmm_tkf92_tables: null host parameter array");
+    if (!(prm->ins_rate > 0.0) || !(prm->del_rate > 0.0) || !(prm->ext >= 0.0 && prm->ext < 1.0))
+        return pro_fail(PHMM_E_ARG, "phmm_tkf92_tables: need ins_rate, del_rate > 0 and 0 <= ext < 1");
+    if (n_pairs < 0) return pro_fail(PHMM_E_ARG, "phmm_tkf92_tables: negative n_pairs");
+    if (n_pairs == 0) return PHMM_OK;
+    if (!t || !chi || !emit_M || !emit_I || !emit_D || !sub)
+        return pro_fail(PHMM_E_ARG, "phmm_tkf92_tables: null device buffer");
+    Packed pk;
+    std::memset(&pk, 0, sizeof(pk));
+    pk.C = 1;
+    pk.q_direct = 1;
+    pk.o_S = 0;
+    std::memcpy(pk.v, prm->Q, sizeof(double) * NA * NA);
+    TkfPi pv;
+    std::memcpy(pv.v, prm->pi, sizeof(double) * NA);
+    cudaStream_t st = (cudaStream_t)stream;
+    tkf92_chi_kernel<<<(n_pairs + 127) / 128, 128, 0, st>>>(prm->ins_rate, prm->del_rate, prm->ext, t, n_pairs, chi);
+    expm_kernel<<<n_pairs, THREADS, 0, st>>>(pk, t, sub);
+    tkf_tables_kernel_v<<<n_pairs, THREADS, 0, st>>>(pv, sub, emit_M, emit_I, emit_D);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
     return PHMM_OK;

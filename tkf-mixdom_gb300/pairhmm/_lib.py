@@ -24,7 +24,7 @@ EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep'
            'phmm_set_variant',
            'phmm_last_variant', 'phmm_last_launch_count',
            'phmm_last_error', 'phmm_version', 'phmm_mixdom2_class_subs_count', 'phmm_mixdom2_tables',
-           'phmm_mixdom2_class_counts')
+           'phmm_mixdom2_class_counts', 'phmm_tkf92_tables')
 
 
 class ModelDesc(ctypes.Structure):
@@ -56,6 +56,12 @@ class MixDom2Params(ctypes.Structure):
         (name, ctypes.POINTER(ctypes.c_double)) for name in (
             'dom_ins', 'dom_del', 'dom_weights', 'frag_weights', 'ext_rates', 'class_pis',
             'class_S_exch', 'classdist')]
+
+
+class Tkf92Params(ctypes.Structure):
+    _fields_ = [('ins_rate', ctypes.c_double), ('del_rate', ctypes.c_double), ('ext', ctypes.c_double),
+                ('alphabet', ctypes.c_int32), ('Q', ctypes.POINTER(ctypes.c_double)),
+                ('pi', ctypes.POINTER(ctypes.c_double))]
 
 
 class PairHMMError(RuntimeError):
@@ -111,6 +117,8 @@ def load(path=None):
     lib.phmm_mixdom2_tables.restype = ctypes.c_int
     lib.phmm_mixdom2_class_counts.argtypes = [ctypes.POINTER(MixDom2Params), ctypes.c_int32] + [vp] * 9
     lib.phmm_mixdom2_class_counts.restype = ctypes.c_int
+    lib.phmm_tkf92_tables.argtypes = [ctypes.POINTER(Tkf92Params), ctypes.c_int32] + [vp] * 7
+    lib.phmm_tkf92_tables.restype = ctypes.c_int
     lib.phmm_version.argtypes = []
     lib.phmm_version.restype = ctypes.c_int
     _LIB = lib
@@ -492,3 +500,30 @@ def mixdom2_tables(params, ts, device='cuda', stream=None):
     EM [P,G,21,21] f32, EI [P,G,21] f32, ED [P,G,21] f32, csubs [P,C,20,20]
     f64) for per-pair times ts."""
     return MixDom2Prologue(params)(ts, device=device, stream=stream)
+
+
+def tkf92_tables(ins_rate, del_rate, ext, Q, pi, ts, device='cuda', stream=None):
+    """phmm_tkf92_tables: the TKF92 (ext = 0: TKF91) E-step inputs built on the
+    device for per-pair times ts: (chi [P,5,5] f32, EM [P,1,21,21] f32, EI
+    [P,1,21] f32, ED [P,1,21] f32, sub [P,20,20] f64) device tensors."""
+    lib = load()
+    host = lambda v: v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else v
+    Qa = np.ascontiguousarray(np.asarray(host(Q), dtype=np.float64))
+    pa = np.ascontiguousarray(np.asarray(host(pi), dtype=np.float64).reshape(-1))
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    prm = Tkf92Params(float(host(ins_rate)), float(host(del_rate)), float(host(ext)), pa.size, dp(Qa), dp(pa))
+    if isinstance(ts, torch.Tensor):
+        t = ts.to(device=device, dtype=torch.float64).reshape(-1).contiguous()
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(np.asarray(ts, np.float64).reshape(-1))).to(device)
+    P = t.numel()
+    f32 = torch.float32
+    chi = torch.empty(P, 5, 5, dtype=f32, device=t.device)
+    EM = torch.empty(P, 1, 21, 21, dtype=f32, device=t.device)
+    EI = torch.empty(P, 1, 21, dtype=f32, device=t.device)
+    ED = torch.empty(P, 1, 21, dtype=f32, device=t.device)
+    sub = torch.empty(P, pa.size, pa.size, dtype=torch.float64, device=t.device)
+    s = stream if stream is not None else torch.cuda.current_stream(t.device)
+    _check(lib.phmm_tkf92_tables(ctypes.byref(prm), P, _ptr(t), _ptr(chi), _ptr(EM), _ptr(EI), _ptr(ED),
+                                 _ptr(sub), ctypes.c_void_p(s.cuda_stream)), 'phmm_tkf92_tables')
+    return chi, EM, EI, ED, sub

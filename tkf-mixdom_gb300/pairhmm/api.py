@@ -519,12 +519,13 @@ def observed_ll(model, params, x, y):
 # ---------------------------------------------------------------- batched TKF92 (train/tkf92_svi_bw.py)
 def _tkf92_batch(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, ext, Q, pi):
     dev = _device()
-    ts = pm._t(np.asarray(ts, dtype=np.float64), device=dev)
-    chi = pm.tkf92_trans(lam, mu, ts.cpu(), ext).clamp_min(1e-30).to(dev)   # log(max(tau,1e-30)), tkf92_svi_bw.py:164
-    sub = pm.transition_matrix(pm._t(Q, dev), ts)
-    EM, EI, ED = pm.tables_tkf(sub, pm._t(pi, dev))
-    xs = [np.asarray(xs_pad[b])[:int(Lx_real[b])] for b in range(len(ts))]
-    ys = [np.asarray(ys_pad[b])[:int(Ly_real[b])] for b in range(len(ts))]
+    # chi floored at 1e-30 (log(max(tau, 1e-30)), tkf92_svi_bw.py:164), P(t) and
+    # the emission tables: the device prologue phmm_tkf92_tables
+    chi, EM, EI, ED, _ = _lib.tkf92_tables(lam, mu, ext, Q, pi, ts, device=dev)
+    Lx_real = np.asarray(Lx_real).reshape(-1)
+    Ly_real = np.asarray(Ly_real).reshape(-1)
+    xs = [np.asarray(xs_pad[b])[:int(Lx_real[b])] for b in range(len(Lx_real))]
+    ys = [np.asarray(ys_pad[b])[:int(Ly_real[b])] for b in range(len(Ly_real))]
     plan = get_plan(np.array([S, M, I, D, E]), np.zeros(5, np.int32), 1)
     return plan, _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev)
 

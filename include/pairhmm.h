@@ -201,6 +201,21 @@ int phmm_mixdom2_tables(const phmm_mixdom2_params *prm, int32_t n_pairs, const d
                         float *chi, float *emit_M, float *emit_I, float *emit_D,
                         double *class_subs, void *stream);
 
+/* The collapsed chi alone (float32 and, when chi64 is not null, float64
+ * [P][N][N]) for the gradient path, and its vector-Jacobian product:
+ * grad[p][d] = sum_{s,k} grad_chi[p][s][k] dchi_p[s][k]/dtheta_d (device
+ * float64), one forward-mode pass per (pair, direction), for the directions
+ * 0 main_ins, 1 main_del, 2 the pair's t, 3 + j the j-th entry of
+ * (dom_ins, dom_del, dom_weights, frag_weights, ext_rates [K][F][F]) --
+ * phmm_mixdom2_chi_vjp_dirs of them.  With grad_chi = n_trans / chi (the
+ * score identity) this is the chi part of the gradient of the reference's
+ * mixdom2_log_prob custom VJP (train/vjp.py:627-680). */
+int phmm_mixdom2_chi(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t, float *chi,
+                     double *chi64, void *stream);
+int phmm_mixdom2_chi_vjp_dirs(const phmm_mixdom2_params *prm);
+int phmm_mixdom2_chi_vjp(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t,
+                         const double *grad_chi, double *grad, void *stream);
+
 /* TKF91 / TKF92 parameters (host float64): insertion and deletion rates,
  * fragment extension probability (0 for TKF91), the substitution rate
  * matrix Q [A][A] (rows summing to zero) and its equilibrium pi [A]; A = 20. */

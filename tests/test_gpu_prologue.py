@@ -140,3 +140,43 @@ def test_tkf92_prologue_matches_float64_builders(cuda_lib, ext, equal_rates):
     torch.testing.assert_close(EM.cpu(), rEM.float(), rtol=F32_RTOL, atol=1e-14)
     torch.testing.assert_close(EI.cpu(), rEI.float().expand_as(EI.cpu()), rtol=F32_RTOL, atol=1e-14)
     torch.testing.assert_close(ED.cpu(), rED.float().expand_as(ED.cpu()), rtol=F32_RTOL, atol=1e-14)
+
+
+@pytest.mark.parametrize('K,F,full_ext,equal_rates', [(3, 1, False, False), (4, 2, False, False),
+                                                      (2, 3, True, False), (3, 2, False, True)])
+def test_chi_vjp_matches_autograd(cuda_lib, K, F, full_ext, equal_rates):
+    """The device chi VJP (forward-mode duals) against torch autograd through
+    the float64 builder, for every chi parameter and the per-pair times."""
+    from pairhmm import synth, api, _lib
+    from pairhmm import models as pm
+    rng = np.random.default_rng(60 + K * F + int(full_ext) + 2 * int(equal_rates))
+    p = synth.mixdom2_params(rng, K, F, 1)
+    if full_ext:
+        p['ext_rates'] = rng.uniform(0.02, 0.2, (K, F, F))
+    if equal_rates:
+        p['dom_del'] = p['dom_ins'] * (1 + 2e-5)
+        p['main_del'] = p['main_ins'] * (1 + 2e-5)
+    P = 5
+    ts = np.exp(rng.uniform(-3, 1, P))
+    names = ['main_ins', 'main_del', 'dom_ins', 'dom_del', 'dom_weights', 'frag_weights', 'ext_rates']
+
+    def leaves(dev):
+        d = {k: torch.tensor(np.asarray(p[k], float), dtype=torch.float64, device=dev, requires_grad=True)
+             for k in names}
+        d['t'] = torch.tensor(ts, dtype=torch.float64, device=dev, requires_grad=True)
+        return d
+    G = torch.as_tensor(rng.normal(size=(P, 2 + 5 * K * F, 2 + 5 * K * F)), dtype=torch.float64)
+    a = leaves('cpu')
+    ref = pm.build_nested_trans(a['main_ins'], a['main_del'], a['t'], a['dom_ins'], a['dom_del'],
+                                a['dom_weights'], a['frag_weights'], a['ext_rates'])
+    (ref * G).sum().backward()
+    b = leaves('cuda')
+    pro = _lib.MixDom2Prologue(dict(p))
+    chi = api.MixDom2Chi.apply(pro, b['t'], b['main_ins'], b['main_del'], b['dom_ins'], b['dom_del'],
+                               b['dom_weights'], b['frag_weights'], b['ext_rates'])
+    torch.testing.assert_close(chi.cpu(), ref.detach(), rtol=1e-11, atol=1e-14)
+    (chi * G.cuda()).sum().backward()
+    for k in names + ['t']:
+        want = a[k].grad
+        scale = float(want.abs().max())
+        torch.testing.assert_close(b[k].grad.cpu(), want, rtol=1e-9, atol=1e-10 * scale + 1e-14, msg=k)

@@ -55,49 +55,98 @@ __device__ __constant__ int UV_U[5] = {M, M, M, I, D};
 __device__ __constant__ int UV_X[5] = {M, I, D, I, D};
 __device__ __constant__ int MID[3] = {M, I, D};
 
+// ---------------------------------------------------------------- scalars
+// The chi builder is written once for a scalar type T: double for the
+// values, Dual (value and one directional derivative, forward mode) for the
+// vector-Jacobian product of the gradient path.  Branches test values only
+// and evaluate the selected expression alone, so a derivative is the
+// derivative of the branch taken, as autograd through torch.where gives it.
+struct Dual {
+    double v, d;
+};
+__device__ __forceinline__ Dual mkd(double v, double d = 0.0) { return {v, d}; }
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a) { return {-a.v, -a.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
+    const double q = a.v / b.v;
+    return {q, (a.d - q * b.d) / b.v};
+}
+__device__ __forceinline__ Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
+__device__ __forceinline__ Dual operator+(double a, Dual b) { return {a + b.v, b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a, double b) { return {a.v - b, a.d}; }
+__device__ __forceinline__ Dual operator-(double a, Dual b) { return {a - b.v, -b.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, double b) { return {a.v * b, a.d * b}; }
+__device__ __forceinline__ Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
+__device__ __forceinline__ Dual operator/(Dual a, double b) { return {a.v / b, a.d / b}; }
+__device__ __forceinline__ Dual operator/(double a, Dual b) {
+    const double q = a / b.v;
+    return {q, -q * b.d / b.v};
+}
+__device__ __forceinline__ Dual texp(Dual a) {
+    const double e = exp(a.v);
+    return {e, e * a.d};
+}
+__device__ __forceinline__ double texp(double a) { return exp(a); }
+__device__ __forceinline__ double val(double a) { return a; }
+__device__ __forceinline__ double val(Dual a) { return a.v; }
+template <class T> __device__ __forceinline__ T cst(double c);
+template <> __device__ __forceinline__ double cst<double>(double c) { return c; }
+template <> __device__ __forceinline__ Dual cst<Dual>(double c) { return {c, 0.0}; }
+// max(a, c) for a constant floor c (clamp_min): the floor has no derivative
+template <class T> __device__ __forceinline__ T floor_at(T a, double c) { return val(a) > c ? a : cst<T>(c); }
+
 // ---------------------------------------------------------------- TKF BDI (core/bdi.py:40-99)
-__device__ double tkf_beta(double lam, double mu, double t) {
-    const double s = mu * t;
-    const double eta = exp(-lam * t);
-    const double alpha = exp(-s);
-    const double numer = lam * (eta - alpha);
-    const double denom = mu * eta - lam * alpha;
-    const double general = fabs(denom) < 1e-30 ? 0.0 : numer / denom;
-    return fabs(1.0 - lam / mu) < 1e-4 ? s / (1.0 + s) : general;
+template <class T>
+__device__ T tkf_beta(T lam, T mu, T t) {
+    const T s = mu * t;
+    if (fabs(1.0 - val(lam) / val(mu)) < 1e-4) return s / (1.0 + s);
+    const T eta = texp(-(lam * t));
+    const T alpha = texp(-s);
+    const T denom = mu * eta - lam * alpha;
+    if (fabs(val(denom)) < 1e-30) return cst<T>(0.0);
+    return lam * (eta - alpha) / denom;
 }
 
-__device__ double tkf_gamma(double lam, double mu, double t) {
-    const double s = mu * t;
-    const double alpha = exp(-mu * t);
-    const double beta = tkf_beta(lam, mu, t);
-    const double Phi = 1.0 - alpha;
-    const double general = fabs(Phi) < 1e-30 ? 0.0 : 1.0 - mu * beta / (lam * fmax(Phi, 1e-30));
-    const double phi = s < 1e-10 ? 1.0 - s / 2.0 : Phi / fmax(s, 1e-30);
-    const double limit = 1.0 - 1.0 / ((1.0 + s) * phi);
-    return fabs(1.0 - lam / mu) < 1e-4 ? limit : general;
+template <class T>
+__device__ T tkf_gamma(T lam, T mu, T t) {
+    const T s = mu * t;
+    const T alpha = texp(-(mu * t));
+    const T Phi = 1.0 - alpha;
+    if (fabs(1.0 - val(lam) / val(mu)) < 1e-4) {
+        const T phi = val(s) < 1e-10 ? 1.0 - s / 2.0 : Phi / floor_at(s, 1e-30);
+        return 1.0 - 1.0 / ((1.0 + s) * phi);
+    }
+    if (fabs(val(Phi)) < 1e-30) return cst<T>(0.0);
+    const T beta = tkf_beta(lam, mu, t);
+    return 1.0 - mu * beta / (lam * floor_at(Phi, 1e-30));
 }
 
 // [5][5] TKF91 pair-HMM matrix, order S, M, I, D, E (core/params.py:29-55)
-__device__ void tkf91(double lam, double mu, double t, double *tau) {
-    const double a = exp(-mu * t), b = tkf_beta(lam, mu, t), g = tkf_gamma(lam, mu, t);
-    const double k = lam / mu;
-    const double row[5] = {0.0, (1 - b) * k * a, b, (1 - b) * k * (1 - a), (1 - b) * (1 - k)};
-    const double rowD[5] = {0.0, (1 - g) * k * a, g, (1 - g) * k * (1 - a), (1 - g) * (1 - k)};
+template <class T>
+__device__ void tkf91(T lam, T mu, T t, T *tau) {
+    const T a = texp(-(mu * t)), b = tkf_beta(lam, mu, t), g = tkf_gamma(lam, mu, t);
+    const T k = lam / mu;
+    const T z = cst<T>(0.0);
+    const T row[5] = {z, (1.0 - b) * k * a, b, (1.0 - b) * k * (1.0 - a), (1.0 - b) * (1.0 - k)};
+    const T rowD[5] = {z, (1.0 - g) * k * a, g, (1.0 - g) * k * (1.0 - a), (1.0 - g) * (1.0 - k)};
     for (int v = 0; v < 5; ++v) {
         tau[S * 5 + v] = row[v];
         tau[M * 5 + v] = row[v];
         tau[I * 5 + v] = row[v];
         tau[D * 5 + v] = rowD[v];
-        tau[E * 5 + v] = 0.0;
+        tau[E * 5 + v] = z;
     }
 }
 
 // ---------------------------------------------------------------- collapsed chi
-// Shared layout of chi_kernel (doubles).
+// Shared layout of the chi builder (elements of T).
+template <class T>
 struct ChiSmem {
     int K, n3, w;             // K, 3K, 3K + 5 (row width of the solve matrix)
-    double *tau, *tauK, *kap, *z, *Tex, *T, *TnN, *ent, *exi, *aug;
-    __device__ void carve(double *base, int K_) {
+    T *tau, *tauK, *kap, *z, *Tex, *T5, *TnN, *ent, *exi, *aug;
+    __device__ void carve(T *base, int K_) {
         K = K_;
         n3 = 3 * K_;
         w = n3 + 5;
@@ -106,37 +155,38 @@ struct ChiSmem {
         kap = tauK + 25 * K;        // [K]
         z = kap + K;                // [3K]     null probability of flat index 3k+e
         Tex = z + n3;               // [K][25]  T_exit_k
-        T = Tex + 25 * K;           // [25]     effective T
-        TnN = T + 25;               // [3K][5]  T_nullN
+        T5 = Tex + 25 * K;          // [25]     effective T
+        TnN = T5 + 25;              // [3K][5]  T_nullN
         ent = TnN + 5 * n3;         // [K][5]   entry factors
         exi = ent + 5 * K;          // [K][5]   exit factors (before notext)
         aug = exi + 5 * K;          // [3K][3K+5] solve matrix
     }
-    static size_t bytes(int K_) {
+    __host__ __device__ static size_t elems(int K_) {
         const size_t n3 = 3 * (size_t)K_;
-        return sizeof(double) * (25 + 25 * K_ + K_ + n3 + 25 * K_ + 25 + 5 * n3 + 10 * K_ + n3 * (n3 + 5));
+        return 25 + 25 * K_ + K_ + n3 + 25 * K_ + 25 + 5 * n3 + 10 * K_ + n3 * (n3 + 5);
     }
 };
 
-__global__ void __launch_bounds__(THREADS)
-chi_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, int N, float *__restrict__ chi) {
-    extern __shared__ double smem_d[];
-    __shared__ int piv_row;
-    const int p = blockIdx.x, tid = threadIdx.x;
-    const int K = prm.K, F = prm.F;
-    const double t = ts[p];
-    const double *dins = prm.v + prm.o_dins, *ddel = prm.v + prm.o_ddel, *dw = prm.v + prm.o_dw;
-    const double *fw = prm.v + prm.o_fw, *ext = prm.v + prm.o_ext;
-    ChiSmem sm;
-    sm.carve(smem_d, K);
-    const int n3 = sm.n3, w = sm.w;
+// The chi parameters seen by the builder: main rates, pair time and the
+// packed domain arrays (dom_ins, dom_del, dom_w, frag_w, ext), as T.
+template <class T>
+struct ChiParams {
+    T main_ins, main_del, t;
+    const T *dins, *ddel, *dw, *fw, *ext;
+};
 
+// Build the N x N collapsed chi of one pair (models/mixdom.py:104-423) with
+// the CTA; emit(idx, value) receives every entry (row-major, idx = r*N + c).
+template <class T, class Emit>
+__device__ void build_chi(const ChiParams<T> &cp, int K, int F, int N, ChiSmem<T> &sm, int *piv_row, Emit emit) {
+    const int tid = threadIdx.x;
+    const int n3 = sm.n3, w = sm.w;
     // TKF91 matrices of the main level and of each domain level
-    if (tid == 0) tkf91(prm.main_ins, prm.main_del, t, sm.tau);
+    if (tid == 0) tkf91(cp.main_ins, cp.main_del, cp.t, sm.tau);
     for (int k = tid; k < K; k += blockDim.x) {
-        tkf91(dins[k], ddel[k], t, sm.tauK + 25 * k);
-        const double kap = dins[k] / ddel[k];
-        const double zt = (1.0 - kap) * (1.0 - tkf_beta(dins[k], ddel[k], t));
+        tkf91(cp.dins[k], cp.ddel[k], cp.t, sm.tauK + 25 * k);
+        const T kap = cp.dins[k] / cp.ddel[k];
+        const T zt = (1.0 - kap) * (1.0 - tkf_beta(cp.dins[k], cp.ddel[k], cp.t));
         sm.kap[k] = kap;
         sm.z[3 * k] = zt;
         sm.z[3 * k + 1] = 1.0 - kap;
@@ -147,22 +197,22 @@ chi_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, in
     // null-domain quantities (models/mixdom.py:104-214): for flat index
     // i = 3k + e (e over the M, I, D contexts), z(i) is the probability that
     // domain k emits nothing, T_nullN[i] its exits to the main level
-    const double *tau = sm.tau;
-    const double tauE[3] = {tau[M * 5 + E], tau[M * 5 + E], tau[D * 5 + E]};
+    const T *tau = sm.tau;
+    const T tauE[3] = {tau[M * 5 + E], tau[M * 5 + E], tau[D * 5 + E]};
     const int nullrow[3] = {M, M, D};
     for (int i = tid; i < n3; i += blockDim.x) {
         const int k = i / 3, e = i % 3;
-        const double z = sm.z[i];
-        const double nonnull = e == 0 ? 1.0 - z : sm.kap[k];
-        for (int v = 0; v < 5; ++v) sm.TnN[i * 5 + v] = 0.0;
+        const T z = sm.z[i];
+        const T nonnull = e == 0 ? 1.0 - z : sm.kap[k];
+        for (int v = 0; v < 5; ++v) sm.TnN[i * 5 + v] = cst<T>(0.0);
         sm.TnN[i * 5 + MID[e]] = nonnull;
         sm.TnN[i * 5 + E] = z * tauE[e];
         // row i of the solve matrix is column i of (I - T_nn):
         // (I - T_nn)[j][i] = delta - z(j) dw[k(i)] tau[nullrow[e(j)]][MID[e(i)]]
         for (int j = 0; j < n3; ++j)
-            sm.aug[i * w + j] = (i == j ? 1.0 : 0.0) - sm.z[j] * dw[k] * tau[nullrow[j % 3] * 5 + MID[e]];
+            sm.aug[i * w + j] = (i == j ? 1.0 : 0.0) - sm.z[j] * cp.dw[k] * tau[nullrow[j % 3] * 5 + MID[e]];
         // right-hand sides: T_Nnull[u][i] = tau[u][MID[e]] dw[k]
-        for (int u = 0; u < 5; ++u) sm.aug[i * w + n3 + u] = tau[u * 5 + MID[e]] * dw[k];
+        for (int u = 0; u < 5; ++u) sm.aug[i * w + n3 + u] = tau[u * 5 + MID[e]] * cp.dw[k];
     }
     __syncthreads();
 
@@ -170,97 +220,149 @@ chi_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, in
     for (int c = 0; c < n3; ++c) {
         if (tid == 0) {
             int best = c;
-            double bv = fabs(sm.aug[c * w + c]);
+            double bv = fabs(val(sm.aug[c * w + c]));
             for (int r = c + 1; r < n3; ++r) {
-                const double v = fabs(sm.aug[r * w + c]);
+                const double v = fabs(val(sm.aug[r * w + c]));
                 if (v > bv) { bv = v; best = r; }
             }
-            piv_row = best;
+            *piv_row = best;
         }
         __syncthreads();
-        const int pr = piv_row;
+        const int pr = *piv_row;
         if (pr != c)
             for (int j = tid; j < w; j += blockDim.x) {
-                const double a = sm.aug[c * w + j];
+                const T a = sm.aug[c * w + j];
                 sm.aug[c * w + j] = sm.aug[pr * w + j];
                 sm.aug[pr * w + j] = a;
             }
         __syncthreads();
-        const double inv = 1.0 / sm.aug[c * w + c];
+        const T inv = 1.0 / sm.aug[c * w + c];
         __syncthreads();
-        for (int j = tid; j < w; j += blockDim.x) sm.aug[c * w + j] *= inv;
+        for (int j = tid; j < w; j += blockDim.x) sm.aug[c * w + j] = sm.aug[c * w + j] * inv;
         __syncthreads();
         for (int idx = tid; idx < n3 * w; idx += blockDim.x) {
             const int r = idx / w, j = idx % w;
             if (r == c || j == c) continue;
-            sm.aug[idx] -= sm.aug[r * w + c] * sm.aug[c * w + j];
+            sm.aug[idx] = sm.aug[idx] - sm.aug[r * w + c] * sm.aug[c * w + j];
         }
         __syncthreads();
         for (int r = tid; r < n3; r += blockDim.x)
-            if (r != c) sm.aug[r * w + c] = 0.0;
+            if (r != c) sm.aug[r * w + c] = cst<T>(0.0);
         __syncthreads();
     }
 
     // T_exit_k[k][u][v] = sum_e Y[u][3k+e] T_nullN[3k+e][v]; Y[u][i] = aug[i][3K+u]
     for (int idx = tid; idx < 25 * K; idx += blockDim.x) {
         const int k = idx / 25, u = (idx / 5) % 5, v = idx % 5;
-        double s = 0.0;
-        for (int e = 0; e < 3; ++e) s += sm.aug[(3 * k + e) * w + n3 + u] * sm.TnN[(3 * k + e) * 5 + v];
+        T s = cst<T>(0.0);
+        for (int e = 0; e < 3; ++e) s = s + sm.aug[(3 * k + e) * w + n3 + u] * sm.TnN[(3 * k + e) * 5 + v];
         sm.Tex[idx] = s;
     }
     // entry / exit factors of each domain's five sub-states
     for (int idx = tid; idx < 5 * K; idx += blockDim.x) {
         const int k = idx / 5, j = idx % 5;
-        const double *tk = sm.tauK + 25 * k;
-        const double beta_d = fmax(1.0 - tk[S * 5 + E], 1e-30);
+        const T *tk = sm.tauK + 25 * k;
+        const T beta_d = floor_at(1.0 - tk[S * 5 + E], 1e-30);
         const bool isM = j < 3;
-        sm.ent[idx] = isM ? tk[S * 5 + UV_X[j]] / beta_d : 1.0;
+        sm.ent[idx] = isM ? tk[S * 5 + UV_X[j]] / beta_d : cst<T>(1.0);
         sm.exi[idx] = isM ? tk[UV_X[j] * 5 + E] : 1.0 - sm.kap[k];
     }
     __syncthreads();
     for (int idx = tid; idx < 25; idx += blockDim.x) {
-        double s = (idx % 5 == E) ? tau[idx] : 0.0;
-        for (int k = 0; k < K; ++k) s += sm.Tex[25 * k + idx];
-        sm.T[idx] = s;
+        T s = (idx % 5 == E) ? tau[idx] : cst<T>(0.0);
+        for (int k = 0; k < K; ++k) s = s + sm.Tex[25 * k + idx];
+        sm.T5[idx] = s;
     }
     __syncthreads();
 
     // chi (models/mixdom.py:252-423): state 0 = SS, 1 = EE, body state
     // 2 + k*5F + j*F + f (domain k, sub-state j, fragment f)
     const int bs = 5 * F;
-    float *out = chi + (size_t)p * N * N;
     for (int idx = tid; idx < N * N; idx += blockDim.x) {
         const int r = idx / N, c = idx % N;
-        double val = 0.0;
+        T v = cst<T>(0.0);
         if (r == 0) {
             if (c == 1) {
-                val = sm.T[S * 5 + E];
+                v = sm.T5[S * 5 + E];
             } else if (c >= 2) {
                 const int q = c - 2, kq = q / bs, jq = (q % bs) / F, fq = q % F;
-                val = sm.Tex[25 * kq + S * 5 + UV_U[jq]] * fw[kq * F + fq] * sm.ent[5 * kq + jq];
+                v = sm.Tex[25 * kq + S * 5 + UV_U[jq]] * cp.fw[kq * F + fq] * sm.ent[5 * kq + jq];
             }
         } else if (r >= 2 && c >= 1) {
             const int pp = r - 2, kp = pp / bs, jp = (pp % bs) / F, fp = pp % F;
-            double notext = 1.0;
-            for (int g = 0; g < F; ++g) notext -= ext[(kp * F + fp) * F + g];
-            const double exit_full = notext * sm.exi[5 * kp + jp];
+            T notext = cst<T>(1.0);
+            for (int g = 0; g < F; ++g) notext = notext - cp.ext[(kp * F + fp) * F + g];
+            const T exit_full = notext * sm.exi[5 * kp + jp];
             if (c == 1) {
-                val = exit_full * sm.T[UV_U[jp] * 5 + E];
+                v = exit_full * sm.T5[UV_U[jp] * 5 + E];
             } else {
                 const int q = c - 2, kq = q / bs, jq = (q % bs) / F, fq = q % F;
-                const double dest = fw[kq * F + fq] * sm.ent[5 * kq + jq];
-                val = exit_full * sm.Tex[25 * kq + UV_U[jp] * 5 + UV_U[jq]] * dest;
+                const T dest = cp.fw[kq * F + fq] * sm.ent[5 * kq + jq];
+                v = exit_full * sm.Tex[25 * kq + UV_U[jp] * 5 + UV_U[jq]] * dest;
                 if (kp == kq) {
-                    const double e = ext[(kp * F + fp) * F + fq];
+                    const T e = cp.ext[(kp * F + fp) * F + fq];
                     if (jp < 3 && jq < 3)
-                        val += notext * sm.tauK[25 * kp + MID[jp] * 5 + MID[jq]] * fw[kp * F + fq] +
-                               (jp == jq ? e : 0.0);
+                        v = v + notext * sm.tauK[25 * kp + MID[jp] * 5 + MID[jq]] * cp.fw[kp * F + fq] +
+                            (jp == jq ? e : cst<T>(0.0));
                     else if (jp == jq)
-                        val += notext * sm.kap[kp] * fw[kp * F + fq] + e;
+                        v = v + notext * sm.kap[kp] * cp.fw[kp * F + fq] + e;
                 }
             }
         }
-        out[idx] = (float)val;
+        emit(idx, v);
+    }
+}
+
+__global__ void __launch_bounds__(THREADS)
+chi_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, int N, float *__restrict__ chi,
+           double *__restrict__ chi64) {
+    extern __shared__ double smem_d[];
+    __shared__ int piv_row;
+    const int p = blockIdx.x;
+    ChiSmem<double> sm;
+    sm.carve(smem_d, prm.K);
+    const ChiParams<double> cp{prm.main_ins, prm.main_del, ts[p], prm.v + prm.o_dins, prm.v + prm.o_ddel,
+                               prm.v + prm.o_dw, prm.v + prm.o_fw, prm.v + prm.o_ext};
+    float *out = chi + (size_t)p * N * N;
+    double *out64 = chi64 ? chi64 + (size_t)p * N * N : nullptr;
+    build_chi(cp, prm.K, prm.F, N, sm, &piv_row, [&](int idx, double v) {
+        out[idx] = (float)v;
+        if (out64) out64[idx] = v;
+    });
+}
+
+// Vector-Jacobian product of chi: for pair p = blockIdx.x and parameter
+// direction d = blockIdx.y, grad[p][d] = sum_{s,k} G[p][s][k] dchi[s][k]/dtheta_d,
+// by one forward-mode (Dual) pass of the builder seeded on theta_d.
+// Directions: 0 main_ins, 1 main_del, 2 t, 3 + j the j-th entry of the packed
+// domain arrays (dom_ins[K], dom_del[K], dom_w[K], frag_w[K*F], ext[K*F*F]).
+__global__ void __launch_bounds__(THREADS)
+chi_vjp_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, int N,
+               const double *__restrict__ G, double *__restrict__ grad) {
+    extern __shared__ Dual smem_dual[];
+    __shared__ int piv_row;
+    __shared__ double red[THREADS / 32];
+    const int p = blockIdx.x, dir = blockIdx.y, nd = gridDim.y, tid = threadIdx.x;
+    const int K = prm.K, F = prm.F;
+    const int nparam = 3 * K + K * F + K * F * F;
+    ChiSmem<Dual> sm;
+    sm.carve(smem_dual, K);
+    Dual *pv = smem_dual + ChiSmem<Dual>::elems(K);   // the packed domain arrays as Duals
+    for (int j = tid; j < nparam; j += blockDim.x) pv[j] = mkd(prm.v[prm.o_dins + j], dir == 3 + j ? 1.0 : 0.0);
+    __syncthreads();
+    const ChiParams<Dual> cp{mkd(prm.main_ins, dir == 0 ? 1.0 : 0.0), mkd(prm.main_del, dir == 1 ? 1.0 : 0.0),
+                             mkd(ts[p], dir == 2 ? 1.0 : 0.0), pv, pv + K, pv + 2 * K, pv + 3 * K,
+                             pv + 3 * K + K * F};
+    const double *Gp = G + (size_t)p * N * N;
+    double acc = 0.0;
+    build_chi(cp, K, F, N, sm, &piv_row, [&](int idx, Dual v) { acc += Gp[idx] * v.d; });
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((tid & 31) == 0) red[tid >> 5] = acc;
+    __syncthreads();
+    if (tid == 0) {
+        double s = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
+        grad[(size_t)p * nd + dir] = s;
     }
 }
 
@@ -618,12 +720,12 @@ extern "C" int phmm_mixdom2_tables(const phmm_mixdom2_params *prm, int32_t n_pai
     const int K = pk.K, F = pk.F, C = pk.C;
     const int N = 2 + 5 * K * F;
     cudaStream_t st = (cudaStream_t)stream;
-    const size_t chi_smem = ChiSmem::bytes(K);
+    const size_t chi_smem = sizeof(double) * ChiSmem<double>::elems(K);
     if (chi_smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(chi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chi_smem);
         if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
     }
-    chi_kernel<<<n_pairs, THREADS, chi_smem, st>>>(pk, t, N, chi);
+    chi_kernel<<<n_pairs, THREADS, chi_smem, st>>>(pk, t, N, chi, nullptr);
     expm_kernel<<<n_pairs * C, THREADS, 0, st>>>(pk, t, class_subs);
     tables_kernel<<<n_pairs, THREADS, 0, st>>>(pk, class_subs, emit_M, emit_I, emit_D);
     cudaError_t e = cudaGetLastError();
@@ -677,6 +779,57 @@ extern "C" int phmm_tkf92_tables(const phmm_tkf92_params *prm, int32_t n_pairs, 
     tkf92_chi_kernel<<<(n_pairs + 127) / 128, 128, 0, st>>>(prm->ins_rate, prm->del_rate, prm->ext, t, n_pairs, chi);
     expm_kernel<<<n_pairs, THREADS, 0, st>>>(pk, t, sub);
     tkf_tables_kernel_v<<<n_pairs, THREADS, 0, st>>>(pv, sub, emit_M, emit_I, emit_D);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    return PHMM_OK;
+}
+
+extern "C" int phmm_mixdom2_chi(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t, float *chi,
+                                double *chi64, void *stream) {
+    using namespace pro;
+    Packed pk;
+    int rc = pack_params(prm, pk, "phmm_mixdom2_chi");
+    if (rc) return rc;
+    if (n_pairs < 0) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_chi: negative n_pairs");
+    if (n_pairs == 0) return PHMM_OK;
+    if (!t || !chi) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_chi: null device buffer");
+    const int N = 2 + 5 * pk.K * pk.F;
+    const size_t smem = sizeof(double) * ChiSmem<double>::elems(pk.K);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(chi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    }
+    chi_kernel<<<n_pairs, THREADS, smem, (cudaStream_t)stream>>>(pk, t, N, chi, chi64);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    return PHMM_OK;
+}
+
+extern "C" int phmm_mixdom2_chi_vjp_dirs(const phmm_mixdom2_params *prm) {
+    if (!prm) return 0;
+    const int K = prm->n_dom, F = prm->n_frag;
+    return 3 + 3 * K + K * F + K * F * F;
+}
+
+extern "C" int phmm_mixdom2_chi_vjp(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t,
+                                    const double *grad_chi, double *grad, void *stream) {
+    using namespace pro;
+    Packed pk;
+    int rc = pack_params(prm, pk, "phmm_mixdom2_chi_vjp");
+    if (rc) return rc;
+    if (n_pairs < 0) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_chi_vjp: negative n_pairs");
+    if (n_pairs == 0) return PHMM_OK;
+    if (!t || !grad_chi || !grad) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_chi_vjp: null device buffer");
+    const int K = pk.K, F = pk.F;
+    const int N = 2 + 5 * K * F;
+    const int nd = 3 + 3 * K + K * F + K * F * F;
+    const size_t smem = sizeof(Dual) * (ChiSmem<Dual>::elems(K) + (size_t)(nd - 3));
+    if (smem > 227 * 1024) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_chi_vjp: state space too large");
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(chi_vjp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    }
+    chi_vjp_kernel<<<dim3(n_pairs, nd), THREADS, smem, (cudaStream_t)stream>>>(pk, t, N, grad_chi, grad);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
     return PHMM_OK;

@@ -24,7 +24,8 @@ EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep'
            'phmm_set_variant',
            'phmm_last_variant', 'phmm_last_launch_count',
            'phmm_last_error', 'phmm_version', 'phmm_mixdom2_class_subs_count', 'phmm_mixdom2_tables',
-           'phmm_mixdom2_class_counts', 'phmm_tkf92_tables')
+           'phmm_mixdom2_class_counts', 'phmm_tkf92_tables', 'phmm_mixdom2_chi',
+           'phmm_mixdom2_chi_vjp_dirs', 'phmm_mixdom2_chi_vjp')
 
 
 class ModelDesc(ctypes.Structure):
@@ -117,6 +118,12 @@ def load(path=None):
     lib.phmm_mixdom2_tables.restype = ctypes.c_int
     lib.phmm_mixdom2_class_counts.argtypes = [ctypes.POINTER(MixDom2Params), ctypes.c_int32] + [vp] * 9
     lib.phmm_mixdom2_class_counts.restype = ctypes.c_int
+    lib.phmm_mixdom2_chi.argtypes = [ctypes.POINTER(MixDom2Params), ctypes.c_int32] + [vp] * 4
+    lib.phmm_mixdom2_chi.restype = ctypes.c_int
+    lib.phmm_mixdom2_chi_vjp_dirs.argtypes = [ctypes.POINTER(MixDom2Params)]
+    lib.phmm_mixdom2_chi_vjp_dirs.restype = ctypes.c_int
+    lib.phmm_mixdom2_chi_vjp.argtypes = [ctypes.POINTER(MixDom2Params), ctypes.c_int32] + [vp] * 4
+    lib.phmm_mixdom2_chi_vjp.restype = ctypes.c_int
     lib.phmm_tkf92_tables.argtypes = [ctypes.POINTER(Tkf92Params), ctypes.c_int32] + [vp] * 7
     lib.phmm_tkf92_tables.restype = ctypes.c_int
     lib.phmm_version.argtypes = []
@@ -483,6 +490,29 @@ class MixDom2Prologue:
             'phmm_mixdom2_class_counts')
         return out
 
+    def chi(self, t, stream=None):
+        """phmm_mixdom2_chi: (chi float32, chi float64) [P,N,N] for float64 device times t [P]."""
+        P = t.numel()
+        c32 = torch.empty(P, self.N, self.N, dtype=torch.float32, device=t.device)
+        c64 = torch.empty(P, self.N, self.N, dtype=torch.float64, device=t.device)
+        s = stream if stream is not None else torch.cuda.current_stream(t.device)
+        _check(self.lib.phmm_mixdom2_chi(ctypes.byref(self.struct), P, _ptr(t), _ptr(c32), _ptr(c64),
+                                         ctypes.c_void_p(s.cuda_stream)), 'phmm_mixdom2_chi')
+        return c32, c64
+
+    def chi_vjp(self, t, grad_chi, stream=None):
+        """phmm_mixdom2_chi_vjp: [P, n_dirs] float64 directional contractions
+        (directions: main_ins, main_del, t, then dom_ins, dom_del, dom_weights,
+        frag_weights, ext_rates [K,F,F] entries)."""
+        P = t.numel()
+        nd = self.lib.phmm_mixdom2_chi_vjp_dirs(ctypes.byref(self.struct))
+        g = grad_chi.to(torch.float64).contiguous()
+        out = torch.empty(P, nd, dtype=torch.float64, device=t.device)
+        s = stream if stream is not None else torch.cuda.current_stream(t.device)
+        _check(self.lib.phmm_mixdom2_chi_vjp(ctypes.byref(self.struct), P, _ptr(t), _ptr(g), _ptr(out),
+                                             ctypes.c_void_p(s.cuda_stream)), 'phmm_mixdom2_chi_vjp')
+        return out
+
     def __call__(self, ts, device='cuda', stream=None):
         if isinstance(ts, torch.Tensor):
             t = ts.to(device=device, dtype=torch.float64).reshape(-1).contiguous()
@@ -502,28 +532,46 @@ def mixdom2_tables(params, ts, device='cuda', stream=None):
     return MixDom2Prologue(params)(ts, device=device, stream=stream)
 
 
+class Tkf92Prologue:
+    """phmm_tkf92_tables for one TKF92 parameter set (ext = 0: TKF91): packs
+    the host parameters once, then builds the E-step inputs of any batch of
+    per-pair times on the device."""
+
+    def __init__(self, ins_rate, del_rate, ext, Q, pi):
+        self.lib = load()
+        host = lambda v: v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else v
+        self._Q = np.ascontiguousarray(np.asarray(host(Q), dtype=np.float64))
+        self._pi = np.ascontiguousarray(np.asarray(host(pi), dtype=np.float64).reshape(-1))
+        self.A = self._pi.size
+        dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        self.struct = Tkf92Params(float(host(ins_rate)), float(host(del_rate)), float(host(ext)), self.A,
+                                  dp(self._Q), dp(self._pi))
+
+    def shapes(self, P):
+        """(chi, emit_M, emit_I, emit_D, sub) shapes for P pairs."""
+        return (P, 5, 5), (P, 1, 21, 21), (P, 1, 21), (P, 1, 21), (P, self.A, self.A)
+
+    def run(self, t, chi, EM, EI, ED, sub, stream=None):
+        """Write into caller tensors: t float64 [P] and the five outputs of shapes(P)."""
+        P = t.numel()
+        s = stream if stream is not None else torch.cuda.current_stream(t.device)
+        _check(self.lib.phmm_tkf92_tables(ctypes.byref(self.struct), P, _ptr(t), _ptr(chi), _ptr(EM), _ptr(EI),
+                                          _ptr(ED), _ptr(sub), ctypes.c_void_p(s.cuda_stream)), 'phmm_tkf92_tables')
+
+    def __call__(self, ts, device='cuda', stream=None):
+        if isinstance(ts, torch.Tensor):
+            t = ts.to(device=device, dtype=torch.float64).reshape(-1).contiguous()
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(np.asarray(ts, np.float64).reshape(-1))).to(device)
+        shp = self.shapes(t.numel())
+        outs = [torch.empty(sh, dtype=torch.float64 if i == 4 else torch.float32, device=t.device)
+                for i, sh in enumerate(shp)]
+        self.run(t, *outs, stream=stream)
+        return tuple(outs)
+
+
 def tkf92_tables(ins_rate, del_rate, ext, Q, pi, ts, device='cuda', stream=None):
-    """phmm_tkf92_tables: the TKF92 (ext = 0: TKF91) E-step inputs built on the
-    device for per-pair times ts: (chi [P,5,5] f32, EM [P,1,21,21] f32, EI
-    [P,1,21] f32, ED [P,1,21] f32, sub [P,20,20] f64) device tensors."""
-    lib = load()
-    host = lambda v: v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else v
-    Qa = np.ascontiguousarray(np.asarray(host(Q), dtype=np.float64))
-    pa = np.ascontiguousarray(np.asarray(host(pi), dtype=np.float64).reshape(-1))
-    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    prm = Tkf92Params(float(host(ins_rate)), float(host(del_rate)), float(host(ext)), pa.size, dp(Qa), dp(pa))
-    if isinstance(ts, torch.Tensor):
-        t = ts.to(device=device, dtype=torch.float64).reshape(-1).contiguous()
-    else:
-        t = torch.from_numpy(np.ascontiguousarray(np.asarray(ts, np.float64).reshape(-1))).to(device)
-    P = t.numel()
-    f32 = torch.float32
-    chi = torch.empty(P, 5, 5, dtype=f32, device=t.device)
-    EM = torch.empty(P, 1, 21, 21, dtype=f32, device=t.device)
-    EI = torch.empty(P, 1, 21, dtype=f32, device=t.device)
-    ED = torch.empty(P, 1, 21, dtype=f32, device=t.device)
-    sub = torch.empty(P, pa.size, pa.size, dtype=torch.float64, device=t.device)
-    s = stream if stream is not None else torch.cuda.current_stream(t.device)
-    _check(lib.phmm_tkf92_tables(ctypes.byref(prm), P, _ptr(t), _ptr(chi), _ptr(EM), _ptr(EI), _ptr(ED),
-                                 _ptr(sub), ctypes.c_void_p(s.cuda_stream)), 'phmm_tkf92_tables')
-    return chi, EM, EI, ED, sub
+    """The TKF92 (ext = 0: TKF91) E-step inputs built on the device for per-pair
+    times ts: (chi [P,5,5] f32, EM [P,1,21,21] f32, EI [P,1,21] f32, ED
+    [P,1,21] f32, sub [P,20,20] f64) device tensors."""
+    return Tkf92Prologue(ins_rate, del_rate, ext, Q, pi)(ts, device=device, stream=stream)

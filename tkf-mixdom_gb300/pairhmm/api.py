@@ -423,6 +423,42 @@ class PairHMMLogLik(torch.autograd.Function):
                 ratio(cI, EI, pe).to(EI.dtype), ratio(cD, ED, pe).to(ED.dtype), None, None, None)
 
 
+class MixDom2Chi(torch.autograd.Function):
+    """The collapsed MixDom chi [P,N,N] (float64) built on the device
+    (phmm_mixdom2_chi), differentiable in main_ins, main_del, t, dom_ins,
+    dom_del, dom_weights, frag_weights and ext_rates: the backward pass is the
+    device vector-Jacobian product phmm_mixdom2_chi_vjp (forward-mode dual
+    numbers through the same builder), replacing autograd through the float64
+    torch builder of models/mixdom.py:104-423."""
+
+    @staticmethod
+    def forward(ctx, pro, t, main_ins, main_del, dom_ins, dom_del, dom_w, frag_w, ext):
+        tt = t.detach().to(torch.float64).reshape(-1).contiguous()
+        _, chi64 = pro.chi(tt)
+        ctx.pro = pro
+        ctx.ext_diag = ext.dim() == 2
+        ctx.shapes = [v.shape for v in (t, main_ins, main_del, dom_ins, dom_del, dom_w, frag_w, ext)]
+        ctx.save_for_backward(tt)
+        return chi64
+
+    @staticmethod
+    def backward(ctx, g):
+        tt, = ctx.saved_tensors
+        pro = ctx.pro
+        K, F = pro.K, pro.F
+        gr = pro.chi_vjp(tt, g)
+        sh = ctx.shapes
+        out = [gr[:, 2].reshape(sh[0]) if tt.numel() == int(np.prod(sh[0])) else gr[:, 2].sum().reshape(sh[0]),
+               gr[:, 0].sum().reshape(sh[1]), gr[:, 1].sum().reshape(sh[2])]
+        j = 3
+        for n, shape in ((K, sh[3]), (K, sh[4]), (K, sh[5]), (K * F, sh[6])):
+            out.append(gr[:, j:j + n].sum(0).reshape(shape))
+            j += n
+        gext = gr[:, j:j + K * F * F].sum(0).reshape(K, F, F)
+        out.append(torch.diagonal(gext, dim1=-2, dim2=-1).reshape(sh[7]) if ctx.ext_diag else gext.reshape(sh[7]))
+        return (None, *out)
+
+
 def mixdom2_log_prob(main_ins_rate, main_del_rate, t, dom_ins_rates, dom_del_rates, dom_weights,
                      frag_weights, ext_rates, class_pis, class_S_exch, class_dist, x_seq, y_seq):
     """log P(x, y) under MixDom2 with gradients for every tensor argument
@@ -436,8 +472,18 @@ def mixdom2_log_prob(main_ins_rate, main_del_rate, t, dom_ins_rates, dom_del_rat
     tt = pm._t(t, device=dev).reshape(-1)
     f = lambda v: pm._t(v, device=dev)
     K, F = f(frag_weights).shape
-    chi = pm.build_nested_trans(f(main_ins_rate), f(main_del_rate), tt, f(dom_ins_rates),
-                                f(dom_del_rates), f(dom_weights), f(frag_weights), f(ext_rates))
+    if K * F <= 33 and f(class_pis).shape[-1] == 20:
+        # chi and its gradient on the device (phmm_mixdom2_chi / _chi_vjp)
+        pro = _lib.MixDom2Prologue({
+            'main_ins': main_ins_rate, 'main_del': main_del_rate, 'dom_ins': dom_ins_rates,
+            'dom_del': dom_del_rates, 'dom_weights': dom_weights, 'frag_weights': frag_weights,
+            'ext_rates': ext_rates, 'class_pis': class_pis, 'class_S_exch': class_S_exch,
+            'classdist': class_dist})
+        chi = MixDom2Chi.apply(pro, tt, f(main_ins_rate), f(main_del_rate), f(dom_ins_rates), f(dom_del_rates),
+                               f(dom_weights), f(frag_weights), f(ext_rates))
+    else:
+        chi = pm.build_nested_trans(f(main_ins_rate), f(main_del_rate), tt, f(dom_ins_rates),
+                                    f(dom_del_rates), f(dom_weights), f(frag_weights), f(ext_rates))
     csubs = pm.class_subs(f(class_S_exch), f(class_pis), tt)
     EM, EI, ED = pm.tables_per_class(csubs, f(class_pis), f(class_dist))
     plan = get_plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)

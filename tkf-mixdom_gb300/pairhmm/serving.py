@@ -271,7 +271,8 @@ class CudaExecutor:
             st = np.array([pm.S, pm.M, pm.I, pm.D, pm.E], np.int8)
             gr = np.zeros(5, np.int32)
             G = 1
-            m.extra = {'Q': pm._t(p['Q'], self.device), 'pi': pm._t(p['pi'], self.device)}
+            m.extra = {'prologue': _lib.Tkf92Prologue(p['ins_rate'], p['del_rate'], p.get('ext', 0.0),
+                                                      p['Q'], p['pi'])}
         elif m.kind == 'mixdom2':
             K = len(np.asarray(p['dom_ins']))
             F = np.asarray(p['frag_weights']).shape[1]
@@ -293,9 +294,11 @@ class CudaExecutor:
                  ('cnt_I', 8 * P * G * 21), ('cnt_D', 8 * P * G * 21), ('status', 4 * P),
                  ('residues', max(int(np.sum(Lx) + np.sum(Ly)), 16)), ('chi', 4 * P * N * N),
                  ('emit_M', 4 * P * G * 441), ('emit_I', 4 * P * G * 21), ('emit_D', 4 * P * G * 21)]
+        pro = m.extra['prologue']
         if m.kind == 'mixdom2':
-            pro = m.extra['prologue']
             sizes += [('t', 8 * P), ('csubs', 8 * P * pro.C * pro.A * pro.A)]
+        else:
+            sizes += [('t', 8 * P), ('csubs', 8 * P * pro.A * pro.A)]
         return sizes
 
     def _ws(self, m, Lx, Ly):
@@ -313,14 +316,6 @@ class CudaExecutor:
         return _al(self._ws(m, Lx, Ly)) + sum(_al(n) for _, n in self._io_sizes(m, Lx, Ly))
 
     # ---- device work
-    def _tkf_tables(self, m, ts):
-        """TKF92 chi [P,5,5] and emission tables [P,1,...] in float64."""
-        pm, p = self.pm, m.params
-        chi = pm.tkf92_trans(p['ins_rate'], p['del_rate'], ts.cpu(), p.get('ext', 0.0)).clamp_min(1e-30)
-        sub = pm.transition_matrix(m.extra['Q'], ts)
-        EM, EI, ED = pm.tables_tkf(sub, m.extra['pi'])
-        return chi.to(self.device), EM, EI, ED
-
     def launch(self, model, reqs, off, nbytes, slot):
         torch, _lib = self.torch, self._lib
         m = self.models[model]
@@ -347,20 +342,16 @@ class CudaExecutor:
         with torch.cuda.stream(s):
             res = views['residues'][:buf.size]
             res.copy_(host_res, non_blocking=True)
+            # device prologue straight into the arena
+            pro = m.extra['prologue']
+            t_v = views['t'].view(torch.float64)
+            t_v.copy_(host_t, non_blocking=True)
             if m.kind == 'mixdom2':
-                # device prologue straight into the arena
-                pro = m.extra['prologue']
-                t_v = views['t'].view(torch.float64)
-                t_v.copy_(host_t, non_blocking=True)
                 csubs = views['csubs'].view(torch.float64).view(P, pro.C, pro.A, pro.A)
-                pro.run(t_v, chi_v, eM, eI, eD, csubs, stream=s)
-                chi = EM = EI = ED = None
             else:
-                chi, EM, EI, ED = self._tkf_tables(m, host_t.to(self.device, non_blocking=True))
-                chi_v.copy_(chi)
-                eM.copy_(EM)
-                eI.copy_(EI)
-                eD.copy_(ED)
+                csubs = views['csubs'].view(torch.float64).view(P, pro.A, pro.A)
+            pro.run(t_v, chi_v, eM, eI, eD, csubs, stream=s)
+            chi = EM = EI = ED = None
             batch = _lib.DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo, residues=res, chi=chi_v,
                                      emit_M=eM, emit_I=eI, emit_D=eD)
             _lib.estep_ws(m.plan, batch, (self.arena.data_ptr() + off, ws_n), stream=s, out=out)

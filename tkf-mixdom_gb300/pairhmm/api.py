@@ -341,13 +341,24 @@ def to_host(result):
     return _lib.to_host(result)
 
 
-def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True):
+def exact_suffstats_batch(n_chi_stack, main_ins, main_del, t_array, dom_ins, dom_del, dom_weights,
+                          frag_weights, ext_rates):
+    """Exact MixDom2 sufficient statistics from collapsed counts
+    (models/exact_suffstats_batch.py:485-541); see pairhmm.suffstats."""
+    from . import suffstats
+    return suffstats.exact_suffstats_batch(n_chi_stack, main_ins, main_del, t_array, dom_ins, dom_del,
+                                           dom_weights, frag_weights, ext_rates)
+
+
+def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True, exact_suffstats=False):
     """Batched MixDom2 E-step over pairs of any lengths in one persistent
     launch (replaces the bucketed jit(vmap(forward_backward_2d)) callers).
 
     Returns a dict of device tensors: log_p [P], n_trans [P,N,N], cnt_M
-    [P,G,21,21], cnt_I/cnt_D [P,G,21], status [P] and, with
-    with_class_counts, the per-pair class counts of e_step_mixdom2."""
+    [P,G,21,21], cnt_I/cnt_D [P,G,21], status [P]; with with_class_counts,
+    the per-pair class counts of e_step_mixdom2; with exact_suffstats, under
+    'suffstats', the per-pair exact sufficient statistics of the exploded
+    model (exact_suffstats_batch on n_trans)."""
     dev = _device()
     pro = _lib.MixDom2Prologue(params)
     chi, EM, EI, ED, csubs = pro(ts, device=dev)
@@ -362,6 +373,10 @@ def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True):
             res.update(pro.class_counts(csubs, out['cnt_M'], out['cnt_I'], out['cnt_D']))
         else:
             res.update(class_split(params, out['cnt_M'], out['cnt_I'], out['cnt_D'], csubs=csubs))
+    if exact_suffstats:
+        res['suffstats'] = exact_suffstats_batch(out['n_trans'], params['main_ins'], params['main_del'], ts,
+                                                 params['dom_ins'], params['dom_del'], params['dom_weights'],
+                                                 params['frag_weights'], params['ext_rates'])
     return res
 
 

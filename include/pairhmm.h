@@ -216,6 +216,40 @@ int phmm_mixdom2_chi_vjp_dirs(const phmm_mixdom2_params *prm);
 int phmm_mixdom2_chi_vjp(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t,
                          const double *grad_chi, double *grad, void *stream);
 
+/* 1D alignment-conditioned forward-backward (dp/hmm.py:127-250, 471-607):
+ * along a fixed alignment the pair HMM is an HMM over the alignment columns.
+ * Per pair p: columns off_host[p] .. off_host[p] + L_host[p] - 1 of emit
+ * (device float32 [columns][N], linear; 0 where the reference's log
+ * emission is NEG_INF); chi [P or 1][N][N] linear.  Outputs: ll_out [P]
+ * float64 (log P; logchi[init][final] for L = 0), n_trans [P][N][N] float64
+ * (initial, interior and terminal transition posteriors), posteriors
+ * (nullable, float32 [columns][N]), status [P].  N <= 64.  Scratch comes from
+ * the caller's workspace (phmm_fb1d_workspace_bytes, 256-byte aligned). */
+typedef struct phmm_fb1d_batch {
+    int32_t n_pairs, n_states;
+    const int32_t *L_host;
+    const int64_t *off_host;
+    const float *emit;
+    const float *chi;
+    int32_t chi_per_pair;
+    int32_t init_state, final_state;
+} phmm_fb1d_batch;
+int phmm_fb1d_workspace_bytes(const phmm_fb1d_batch *batch, size_t *bytes);
+int phmm_fb1d(const phmm_fb1d_batch *batch, void *workspace, size_t workspace_bytes, double *ll_out,
+              double *n_trans, float *posteriors, int32_t *status_out, void *stream);
+
+/* Per-column emissions of alignments for phmm_fb1d (dp/hmm.py:854-1082):
+ * cols / anc / desc are device uint8 per column (column type 1 M, 2 I, 3 D;
+ * characters 0..20, 20 the wildcard); a column of type c emits through the
+ * states of type c with the per-group tables of phmm_batch (M:
+ * emit_M[g][anc][desc], I: emit_I[g][desc], D: emit_D[g][anc]), every other
+ * state gets 0.  workspace: at least 16 * n_pairs bytes. */
+int phmm_fb1d_emissions(const phmm_model_desc *model, int32_t n_pairs, const int32_t *L_host,
+                        const int64_t *off_host, const uint8_t *cols, const uint8_t *anc,
+                        const uint8_t *desc, const float *emit_M, const float *emit_I,
+                        const float *emit_D, int32_t emit_per_pair, void *workspace,
+                        size_t workspace_bytes, float *emit, int32_t *status_out, void *stream);
+
 /* TKF91 / TKF92 parameters (host float64): insertion and deletion rates,
  * fragment extension probability (0 for TKF91), the substitution rate
  * matrix Q [A][A] (rows summing to zero) and its equilibrium pi [A]; A = 20. */

@@ -288,11 +288,39 @@ def cond(pred, tf, ff, *ops, **_):
     return tf(*ops) if bool(pred) else ff(*ops)
 
 
+def dynamic_slice(operand, start_indices, slice_sizes):
+    """jax.lax.dynamic_slice: start indices clamped so the slice stays inside."""
+    a = np.asarray(operand)
+    idx = []
+    for dim, st, n in zip(a.shape, start_indices, slice_sizes):
+        st = int(min(max(int(st), 0), dim - int(n)))
+        idx.append(slice(st, st + int(n)))
+    return _wrap(a[tuple(idx)])
+
+
+def associative_scan(fn, elems, reverse=False, axis=0):
+    """jax.lax.associative_scan as a sequential inclusive scan along axis 0
+    (the reduction order of a prefix scan; fn is associative)."""
+    if axis != 0:
+        raise NotImplementedError('associative_scan stand-in: axis 0 only')
+    n = _tree_len(elems)
+    order = range(n - 1, -1, -1) if reverse else range(n)
+    out = [None] * n
+    acc = None
+    for i in order:
+        e = _tree_index(elems, i)
+        acc = e if acc is None else (fn(e, acc) if reverse else fn(acc, e))
+        out[i] = acc
+    return _tree_leaves_stack(out)
+
+
 lax = types.ModuleType('jax.lax')
 lax.scan = scan
 lax.fori_loop = fori_loop
 lax.cond = cond
 lax.stop_gradient = lambda x: x
+lax.dynamic_slice = dynamic_slice
+lax.associative_scan = associative_scan
 
 
 # ---------------------------------------------------------------- transforms

@@ -25,7 +25,8 @@ EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep'
            'phmm_last_variant', 'phmm_last_launch_count',
            'phmm_last_error', 'phmm_version', 'phmm_mixdom2_class_subs_count', 'phmm_mixdom2_tables',
            'phmm_mixdom2_class_counts', 'phmm_tkf92_tables', 'phmm_mixdom2_chi',
-           'phmm_mixdom2_chi_vjp_dirs', 'phmm_mixdom2_chi_vjp')
+           'phmm_mixdom2_chi_vjp_dirs', 'phmm_mixdom2_chi_vjp', 'phmm_fb1d_workspace_bytes', 'phmm_fb1d',
+           'phmm_fb1d_emissions')
 
 
 class ModelDesc(ctypes.Structure):
@@ -63,6 +64,13 @@ class Tkf92Params(ctypes.Structure):
     _fields_ = [('ins_rate', ctypes.c_double), ('del_rate', ctypes.c_double), ('ext', ctypes.c_double),
                 ('alphabet', ctypes.c_int32), ('Q', ctypes.POINTER(ctypes.c_double)),
                 ('pi', ctypes.POINTER(ctypes.c_double))]
+
+
+class Fb1dBatch(ctypes.Structure):
+    _fields_ = [('n_pairs', ctypes.c_int32), ('n_states', ctypes.c_int32),
+                ('L_host', ctypes.POINTER(ctypes.c_int32)), ('off_host', ctypes.POINTER(ctypes.c_int64)),
+                ('emit', ctypes.c_void_p), ('chi', ctypes.c_void_p), ('chi_per_pair', ctypes.c_int32),
+                ('init_state', ctypes.c_int32), ('final_state', ctypes.c_int32)]
 
 
 class PairHMMError(RuntimeError):
@@ -126,6 +134,14 @@ def load(path=None):
     lib.phmm_mixdom2_chi_vjp.restype = ctypes.c_int
     lib.phmm_tkf92_tables.argtypes = [ctypes.POINTER(Tkf92Params), ctypes.c_int32] + [vp] * 7
     lib.phmm_tkf92_tables.restype = ctypes.c_int
+    lib.phmm_fb1d_workspace_bytes.argtypes = [ctypes.POINTER(Fb1dBatch), ctypes.POINTER(ctypes.c_size_t)]
+    lib.phmm_fb1d_workspace_bytes.restype = ctypes.c_int
+    lib.phmm_fb1d.argtypes = [ctypes.POINTER(Fb1dBatch), vp, ctypes.c_size_t, vp, vp, vp, vp, vp]
+    lib.phmm_fb1d.restype = ctypes.c_int
+    lib.phmm_fb1d_emissions.argtypes = [ctypes.POINTER(ModelDesc), ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                                        ctypes.POINTER(ctypes.c_int64), vp, vp, vp, vp, vp, vp, ctypes.c_int32,
+                                        vp, ctypes.c_size_t, vp, vp, vp]
+    lib.phmm_fb1d_emissions.restype = ctypes.c_int
     lib.phmm_version.argtypes = []
     lib.phmm_version.restype = ctypes.c_int
     _LIB = lib
@@ -575,3 +591,53 @@ def tkf92_tables(ins_rate, del_rate, ext, Q, pi, ts, device='cuda', stream=None)
     times ts: (chi [P,5,5] f32, EM [P,1,21,21] f32, EI [P,1,21] f32, ED
     [P,1,21] f32, sub [P,20,20] f64) device tensors."""
     return Tkf92Prologue(ins_rate, del_rate, ext, Q, pi)(ts, device=device, stream=stream)
+
+
+def fb1d(n_states, L, off, emit, chi, chi_per_pair, init_state, final_state, posteriors=False, stream=None):
+    """phmm_fb1d: (ll [P] f64, n_trans [P,N,N] f64, posteriors [cols,N] f32 or None,
+    status [P] i32) for per-pair column ranges of emit [cols, N] (device float32)."""
+    lib = load()
+    L = np.ascontiguousarray(np.asarray(L, np.int32))
+    off = np.ascontiguousarray(np.asarray(off, np.int64))
+    P = L.size
+    dev = emit.device
+    b = Fb1dBatch(P, n_states, L.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                  off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), emit.data_ptr(), chi.data_ptr(),
+                  int(chi_per_pair), int(init_state), int(final_state))
+    nb = ctypes.c_size_t(0)
+    _check(lib.phmm_fb1d_workspace_bytes(ctypes.byref(b), ctypes.byref(nb)), 'phmm_fb1d_workspace_bytes')
+    ws = torch.empty(max(int(nb.value), 256), dtype=torch.uint8, device=dev)
+    ll = torch.empty(P, dtype=torch.float64, device=dev)
+    nt = torch.empty(P, n_states, n_states, dtype=torch.float64, device=dev)
+    st = torch.empty(P, dtype=torch.int32, device=dev)
+    post = torch.zeros(emit.shape[0], n_states, dtype=torch.float32, device=dev) if posteriors else None
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    _check(lib.phmm_fb1d(ctypes.byref(b), _ptr(ws), ctypes.c_size_t(ws.numel()), _ptr(ll), _ptr(nt), _ptr(post),
+                         _ptr(st), ctypes.c_void_p(s.cuda_stream)), 'phmm_fb1d')
+    return ll, nt, post, st
+
+
+def fb1d_emissions(state_types, groups, G, L, off, cols, anc, desc, emit_M, emit_I, emit_D, per_pair,
+                   stream=None):
+    """phmm_fb1d_emissions: per-column emissions [cols, N] (device float32) of
+    alignments (device uint8 cols / anc / desc) from the per-group tables."""
+    lib = load()
+    st_arr = np.ascontiguousarray(np.asarray(state_types, np.int8))
+    gr = np.ascontiguousarray(np.asarray(groups, np.int32))
+    desc_m = ModelDesc(st_arr.size, st_arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)),
+                       gr.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), int(G))
+    L = np.ascontiguousarray(np.asarray(L, np.int32))
+    off = np.ascontiguousarray(np.asarray(off, np.int64))
+    P = L.size
+    dev = cols.device
+    n_cols = int(cols.numel())
+    out = torch.zeros(max(n_cols, 1), st_arr.size, dtype=torch.float32, device=dev)
+    ws = torch.empty(max(16 * P, 256), dtype=torch.uint8, device=dev)
+    status = torch.empty(max(P, 1), dtype=torch.int32, device=dev)
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    _check(lib.phmm_fb1d_emissions(ctypes.byref(desc_m), P, L.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                   off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _ptr(cols), _ptr(anc),
+                                   _ptr(desc), _ptr(emit_M), _ptr(emit_I), _ptr(emit_D), int(per_pair), _ptr(ws),
+                                   ctypes.c_size_t(ws.numel()), _ptr(out), _ptr(status),
+                                   ctypes.c_void_p(s.cuda_stream)), 'phmm_fb1d_emissions')
+    return out, status

@@ -341,6 +341,59 @@ def to_host(result):
     return _lib.to_host(result)
 
 
+def forward_backward_1d_batch(log_trans, log_emissions, seq_lengths, init_state=S, final_state=E):
+    """Batched forward_backward_1d_padded (dp/hmm.py:471-607) on the device.
+
+    log_trans: [N, N] or per pair [B, N, N] log transitions; log_emissions
+    [B, L_pad, N] with the real columns first; seq_lengths [B].  Returns
+    (log_prob [B], posteriors [B, L_pad, N] (0 at padded columns),
+    expected_trans [B, N, N]) as float64 device tensors."""
+    dev = _device()
+    le = torch.as_tensor(np.asarray(log_emissions) if not isinstance(log_emissions, torch.Tensor) else log_emissions)
+    le = le.to(device=dev, dtype=torch.float64)
+    B, Lp, N = le.shape
+    lens = np.asarray(seq_lengths, np.int64).reshape(-1)
+    lt = torch.as_tensor(np.asarray(log_trans) if not isinstance(log_trans, torch.Tensor) else log_trans)
+    lt = lt.to(device=dev, dtype=torch.float64)
+    chi = torch.where(lt > -1e29, torch.exp(lt), torch.zeros_like(lt)).to(torch.float32).contiguous()
+    mask = torch.arange(Lp, device=dev)[None, :] < torch.as_tensor(lens, device=dev)[:, None]
+    rows = torch.where(le > -1e29, torch.exp(le), torch.zeros_like(le)).to(torch.float32)[mask].contiguous()
+    off = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64)
+    ll, nt, post, _ = _lib.fb1d(N, lens, off, rows if rows.numel() else torch.zeros(1, N, device=dev), chi,
+                                chi.dim() == 3, init_state, final_state, posteriors=True)
+    posteriors = torch.zeros(B, Lp, N, dtype=torch.float64, device=dev)
+    if rows.numel():
+        posteriors[mask] = post[:int(lens.sum())].to(torch.float64)
+    return ll, posteriors, nt
+
+
+def estep_1d_mixdom2(params, cols, ancs, descs, ts, with_posteriors=False):
+    """Alignment-conditioned MixDom2 E-step (the 1D path of the reference's
+    training loop, dp/hmm.py:471-607 with pair_hmm_emissions_constrained_per_class,
+    dp/hmm.py:981-1082), batched over pairs: cols[p] the per-column state
+    types (1 M, 2 I, 3 D) of pair p's alignment, ancs[p] / descs[p] its
+    ancestor / descendant characters per column (used at M and D / M and I
+    columns; 20 = wildcard), ts[p] its time.  Returns device tensors log_p
+    [P], n_trans [P, N, N], status [P] and, with with_posteriors, posteriors
+    as a list of [L_p, N] float32."""
+    dev = _device()
+    pro = _lib.MixDom2Prologue(params)
+    chi, EM, EI, ED, _ = pro(ts, device=dev)
+    K, F = pro.K, pro.F
+    st = pm.mixdom_state_types(K, F)
+    gr = pm.mixdom_state_groups(K, F)
+    lens = np.array([len(c) for c in cols], np.int64)
+    off = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64)
+    cat = lambda xs: torch.from_numpy(np.concatenate([np.asarray(x, np.uint8).reshape(-1) for x in xs])
+                                      if lens.sum() else np.zeros(1, np.uint8)).to(dev)
+    emit, st1 = _lib.fb1d_emissions(st, gr, K * F, lens, off, cat(cols), cat(ancs), cat(descs), EM, EI, ED, True)
+    ll, nt, post, st2 = _lib.fb1d(len(st), lens, off, emit, chi, True, 0, 1, posteriors=with_posteriors)
+    res = {'log_p': ll, 'n_trans': nt, 'status': st1 | st2}
+    if with_posteriors:
+        res['posteriors'] = [post[o:o + n] for o, n in zip(off, lens)]
+    return res
+
+
 def exact_suffstats_batch(n_chi_stack, main_ins, main_del, t_array, dom_ins, dom_del, dom_weights,
                           frag_weights, ext_rates):
     """Exact MixDom2 sufficient statistics from collapsed counts

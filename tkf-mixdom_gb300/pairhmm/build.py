@@ -2,7 +2,8 @@
 
 ``python -m pairhmm.build`` (or ``build()``) compiles the translation units
 of ``csrc/`` (the E-step kernels and C ABI in ``pairhmm.cu``, the device
-prologue in ``prologue.cu``) in parallel with nvcc and links them into
+prologue in ``prologue.cu``, the 1D alignment-conditioned forward-backward in
+``fb1d.cu``) in parallel with nvcc and links them into
 ``pairhmm/libpairhmm.so`` next to this file.  The build is skipped when the
 library is newer than its sources.
 """
@@ -19,7 +20,7 @@ REPO_DIR = os.path.dirname(PROJECT_DIR)
 CSRC = os.path.join(PROJECT_DIR, 'csrc')
 INCLUDE = os.path.join(REPO_DIR, 'include')
 LIB_PATH = os.path.join(PKG_DIR, 'libpairhmm.so')
-SOURCES = [os.path.join(CSRC, 'pairhmm.cu'), os.path.join(CSRC, 'prologue.cu')]
+SOURCES = [os.path.join(CSRC, 'pairhmm.cu'), os.path.join(CSRC, 'prologue.cu'), os.path.join(CSRC, 'fb1d.cu')]
 OBJ_DIR = os.path.join(PKG_DIR, '_build')
 ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
 

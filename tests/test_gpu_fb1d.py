@@ -82,3 +82,49 @@ def test_random_alignments_against_oracle(cuda_lib):
         assert abs(res['log_p'][b].item() - lp) <= 1e-6 * abs(lp), (b, res['log_p'][b].item(), lp)
         got = res['n_trans'][b].cpu().numpy()
         assert np.abs(got - n).max() <= 1e-5 * np.abs(n).max(), b
+
+
+def test_constrained_log_prob_gradient_against_fd(cuda_lib):
+    """mixdom2_constrained_log_prob: log P and every parameter's gradient
+    against the float64 oracle (central differences, h = 1e-6 relative)."""
+    from pairhmm import api, synth
+    from pairhmm import models as pm
+    from oracle import fb1d, models as om
+    rng = np.random.default_rng(93)
+    K, F, C = 2, 2, 2
+    p = synth.mixdom2_params(rng, K, F, C)
+    L = 60
+    cols = rng.choice(np.array([1, 2, 3]), size=L, p=[0.6, 0.2, 0.2])
+    anc = rng.integers(0, 20, L)
+    desc = rng.integers(0, 20, L)
+    names = ['main_ins', 'main_del', 't', 'dom_ins', 'dom_del', 'dom_weights', 'frag_weights', 'ext_rates',
+             'class_S_exch', 'class_pis', 'classdist']
+    tens = {k: torch.tensor(np.asarray(p[k], float), dtype=torch.float64, requires_grad=True) for k in names}
+    ll = api.mixdom2_constrained_log_prob(*[tens[k] for k in names], cols, anc, desc, L)
+    ll.backward()
+    st = pm.mixdom_state_types(K, F)
+
+    def oracle_ll(q):
+        chi = om.build_nested_trans(q['main_ins'], q['main_del'], q['t'], q['dom_ins'], q['dom_del'],
+                                    q['dom_weights'], q['frag_weights'], q['ext_rates'])
+        cs = om.build_class_subs(q['class_S_exch'], q['class_pis'], q['t'])
+        return fb1d.estep_1d(chi, st, cols, anc, desc, cs, q['class_pis'], q['classdist'], K, F)[0]
+    want = oracle_ll(p)
+    assert abs(ll.item() - want) <= 1e-6 * abs(want)
+    for k in names:
+        v = np.asarray(p[k], float)
+        flat = v.reshape(-1)
+        for idx in rng.choice(flat.size, size=min(2, flat.size), replace=False):
+            if k == 'class_S_exch':   # only off-diagonal exchangeabilities enter Q
+                a_, b_ = divmod(int(idx) % 400, 20)
+                if a_ == b_:
+                    continue
+            h = 1e-6 * max(abs(flat[idx]), 1e-3)
+            pp, pm_ = dict(p), dict(p)
+            a = flat.copy(); a[idx] += h
+            b = flat.copy(); b[idx] -= h
+            pp[k] = a.reshape(v.shape) if v.ndim else float(a[0])
+            pm_[k] = b.reshape(v.shape) if v.ndim else float(b[0])
+            fd = (oracle_ll(pp) - oracle_ll(pm_)) / (2 * h)
+            got = tens[k].grad.numpy().reshape(-1)[idx]
+            assert abs(got - fd) <= 2e-4 * max(abs(fd), 1.0), (k, idx, got, fd)

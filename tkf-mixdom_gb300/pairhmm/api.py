@@ -394,6 +394,107 @@ def estep_1d_mixdom2(params, cols, ancs, descs, ts, with_posteriors=False):
     return res
 
 
+class ConstrainedLogLik(torch.autograd.Function):
+    """Sum of per-alignment 1D log-likelihoods (phmm_fb1d) with the
+    score-identity adjoint: dLL/dchi = n_trans/chi, dLL/dEM = cnt_M/EM (and I,
+    D alike), the character counts summed from the column posteriors -- the
+    gradient train/vjp.py:1325-1437 returns for the constrained DP."""
+
+    @staticmethod
+    def forward(ctx, chi, EM, EI, ED, st, gr, cols, ancs, descs):
+        dev = chi.device
+        P = len(cols)
+        N, G = len(st), EM.shape[1]
+        lens = np.array([len(c) for c in cols], np.int64)
+        off = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64)
+        cat = lambda xs: (np.concatenate([np.asarray(x, np.int64).reshape(-1) for x in xs])
+                          if lens.sum() else np.zeros(1, np.int64))
+        c_all, a_all, d_all = cat(cols), cat(ancs), cat(descs)
+        to_u8 = lambda a: torch.from_numpy(np.clip(a, 0, 255).astype(np.uint8)).to(dev)
+        f32 = lambda v: v.detach().to(torch.float32).contiguous()
+        per_pair = EM.shape[0] == P
+        emit, st1 = _lib.fb1d_emissions(st, gr, G, lens, off, to_u8(c_all), to_u8(a_all), to_u8(d_all),
+                                        f32(EM), f32(EI), f32(ED), per_pair)
+        ll, nt, post, st2 = _lib.fb1d(N, lens, off, emit, f32(chi), chi.shape[0] == P and chi.dim() == 3, 0, 1,
+                                      posteriors=True)
+        # character counts per pair from the column posteriors
+        ncol = int(lens.sum())
+        pair_of = torch.as_tensor(np.repeat(np.arange(P), lens), device=dev)
+        cM = torch.zeros(P * G * 441, dtype=torch.float64, device=dev)
+        cI = torch.zeros(P * G * 21, dtype=torch.float64, device=dev)
+        cD = torch.zeros(P * G * 21, dtype=torch.float64, device=dev)
+        if ncol:
+            pst = post[:ncol].to(torch.float64)
+            c_t = torch.as_tensor(c_all[:ncol], device=dev)
+            a_t = torch.as_tensor(np.minimum(a_all[:ncol], 20), device=dev)
+            d_t = torch.as_tensor(np.minimum(d_all[:ncol], 20), device=dev)
+            st_t = torch.as_tensor(np.asarray(st, np.int64), device=dev)
+            gr_t = torch.as_tensor(np.asarray(gr, np.int64), device=dev)
+            for typ, out, idx_fn in ((1, cM, lambda g: (pair_of[:, None] * G + g) * 441 + a_t[:, None] * 21
+                                      + d_t[:, None]),
+                                     (2, cI, lambda g: (pair_of[:, None] * G + g) * 21 + d_t[:, None]),
+                                     (3, cD, lambda g: (pair_of[:, None] * G + g) * 21 + a_t[:, None])):
+                sel = st_t == typ
+                if not bool(sel.any()):
+                    continue
+                w = pst[:, sel] * (c_t == typ)[:, None]
+                out.index_add_(0, idx_fn(gr_t[sel][None, :]).reshape(-1), w.reshape(-1))
+        cM, cI, cD = cM.view(P, G, 21, 21), cI.view(P, G, 21), cD.view(P, G, 21)
+        ctx.save_for_backward(chi, EM, EI, ED, nt, cM, cI, cD)
+        ctx.status = st1 | st2
+        return ll
+
+    @staticmethod
+    def backward(ctx, g):
+        chi, EM, EI, ED, n, cM, cI, cD = ctx.saved_tensors
+        gw = g.to(torch.float64)
+
+        def ratio(cnt, tab):
+            per_pair = tab.shape[0] == cnt.shape[0]
+            r = torch.where(tab > 0, cnt / torch.where(tab > 0, tab, torch.ones_like(tab)), torch.zeros_like(cnt))
+            r = r * gw.reshape((-1,) + (1,) * (cnt.dim() - 1))
+            return (r if per_pair else r.sum(dim=0, keepdim=True)).to(tab.dtype)
+        return (ratio(n, chi), ratio(cM, EM), ratio(cI, EI), ratio(cD, ED), None, None, None, None, None)
+
+
+def mixdom2_constrained_log_prob(main_ins_rate, main_del_rate, t, dom_ins_rates, dom_del_rates, dom_weights,
+                                 frag_weights, ext_rates, class_S_exch, class_pis, classdist, state_seq,
+                                 anc_chars, desc_chars, real_L=None):
+    """1D log P(x, y, A | params) under MixDom2 along fixed alignments
+    (train/vjp.py:1193-1229), differentiable in every parameter tensor.
+    state_seq / anc_chars / desc_chars: one alignment (arrays; real_L its
+    length) or lists of alignments, in which case t is [P] and the result [P]."""
+    dev = _device()
+    batched = isinstance(state_seq, (list, tuple))
+    if batched:
+        cols, ancs, descs = list(state_seq), list(anc_chars), list(desc_chars)
+    else:
+        Lr = len(state_seq) if real_L is None else int(real_L)
+        cols, ancs, descs = [np.asarray(state_seq)[:Lr]], [np.asarray(anc_chars)[:Lr]], [np.asarray(desc_chars)[:Lr]]
+    tt = pm._t(t, device=dev).reshape(-1)
+    f = lambda v: pm._t(v, device=dev)
+    K, F = f(frag_weights).shape
+    if K * F <= 12 and f(class_pis).shape[-1] == 20:
+        pro = _lib.MixDom2Prologue({
+            'main_ins': main_ins_rate, 'main_del': main_del_rate, 'dom_ins': dom_ins_rates,
+            'dom_del': dom_del_rates, 'dom_weights': dom_weights, 'frag_weights': frag_weights,
+            'ext_rates': ext_rates, 'class_pis': class_pis, 'class_S_exch': class_S_exch,
+            'classdist': classdist})
+        chi = MixDom2Chi.apply(pro, tt, f(main_ins_rate), f(main_del_rate), f(dom_ins_rates), f(dom_del_rates),
+                               f(dom_weights), f(frag_weights), f(ext_rates))
+    else:
+        chi = pm.build_nested_trans(f(main_ins_rate), f(main_del_rate), tt, f(dom_ins_rates),
+                                    f(dom_del_rates), f(dom_weights), f(frag_weights), f(ext_rates))
+    csubs = pm.class_subs(f(class_S_exch), f(class_pis), tt)
+    EM, EI, ED = pm.tables_per_class(csubs, f(class_pis), f(classdist))
+    if EI.dim() == 2:
+        EI, ED = EI.unsqueeze(0), ED.unsqueeze(0)
+    st = pm.mixdom_state_types(K, F)
+    gr = pm.mixdom_state_groups(K, F)
+    ll = ConstrainedLogLik.apply(chi, EM, EI, ED, st, gr, cols, ancs, descs)
+    return ll if batched else ll[0]
+
+
 def exact_suffstats_batch(n_chi_stack, main_ins, main_del, t_array, dom_ins, dom_del, dom_weights,
                           frag_weights, ext_rates):
     """Exact MixDom2 sufficient statistics from collapsed counts

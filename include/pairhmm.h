@@ -250,6 +250,23 @@ int phmm_fb1d_emissions(const phmm_model_desc *model, int32_t n_pairs, const int
                         const float *emit_D, int32_t emit_per_pair, void *workspace,
                         size_t workspace_bytes, float *emit, int32_t *status_out, void *stream);
 
+/* Viterbi path of each pair (dp/hmm.py:1976-2040), float64 log space: the
+ * batch's sequences (residues, offsets, lengths; chi_per_pair / emit_per_pair
+ * select per-pair or shared tables below), log_chi [P or 1][N][N] (NEG_INF
+ * = -1e30 for structural zeros), log emission tables per group log_emit_M
+ * [P or 1][G][21][21], log_emit_I / log_emit_D [P or 1][G][21] (index 20 the
+ * wildcard, log 1).  Outputs: ll_out [P] (log-probability of the best path),
+ * path [sum_p (Lx+Ly+1)][3] int32 (i, j, state) triples from (0, 0, S) to
+ * (Lx, Ly, best final state), pair p's block starting at sum_{q<p}
+ * (Lx_q+Ly_q+1), path_len [P] (entries used), status [P].  N <= 64.
+ * Scratch from the caller's workspace (phmm_viterbi_workspace_bytes:
+ * three diagonals and one backpointer byte per cell and state). */
+int phmm_viterbi_workspace_bytes(const phmm_model_desc *model, const phmm_batch *batch, size_t *bytes);
+int phmm_viterbi(const phmm_model_desc *model, const phmm_batch *batch, const double *log_chi,
+                 const double *log_emit_M, const double *log_emit_I, const double *log_emit_D,
+                 void *workspace, size_t workspace_bytes, double *ll_out, int32_t *path,
+                 int32_t *path_len, int32_t *status_out, void *stream);
+
 /* TKF91 / TKF92 parameters (host float64): insertion and deletion rates,
  * fragment extension probability (0 for TKF91), the substitution rate
  * matrix Q [A][A] (rows summing to zero) and its equilibrium pi [A]; A = 20. */

@@ -26,7 +26,7 @@ EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep'
            'phmm_last_error', 'phmm_version', 'phmm_mixdom2_class_subs_count', 'phmm_mixdom2_tables',
            'phmm_mixdom2_class_counts', 'phmm_tkf92_tables', 'phmm_mixdom2_chi',
            'phmm_mixdom2_chi_vjp_dirs', 'phmm_mixdom2_chi_vjp', 'phmm_fb1d_workspace_bytes', 'phmm_fb1d',
-           'phmm_fb1d_emissions')
+           'phmm_fb1d_emissions', 'phmm_viterbi_workspace_bytes', 'phmm_viterbi')
 
 
 class ModelDesc(ctypes.Structure):
@@ -142,6 +142,12 @@ def load(path=None):
                                         ctypes.POINTER(ctypes.c_int64), vp, vp, vp, vp, vp, vp, ctypes.c_int32,
                                         vp, ctypes.c_size_t, vp, vp, vp]
     lib.phmm_fb1d_emissions.restype = ctypes.c_int
+    lib.phmm_viterbi_workspace_bytes.argtypes = [ctypes.POINTER(ModelDesc), ctypes.POINTER(Batch),
+                                                 ctypes.POINTER(ctypes.c_size_t)]
+    lib.phmm_viterbi_workspace_bytes.restype = ctypes.c_int
+    lib.phmm_viterbi.argtypes = [ctypes.POINTER(ModelDesc), ctypes.POINTER(Batch)] + [vp] * 4 + \
+        [vp, ctypes.c_size_t, vp, vp, vp, vp, vp]
+    lib.phmm_viterbi.restype = ctypes.c_int
     lib.phmm_version.argtypes = []
     lib.phmm_version.restype = ctypes.c_int
     _LIB = lib
@@ -641,3 +647,40 @@ def fb1d_emissions(state_types, groups, G, L, off, cols, anc, desc, emit_M, emit
                                    ctypes.c_size_t(ws.numel()), _ptr(out), _ptr(status),
                                    ctypes.c_void_p(s.cuda_stream)), 'phmm_fb1d_emissions')
     return out, status
+
+
+def viterbi(state_types, groups, G, xs, ys, log_chi, log_M, log_I, log_D, device='cuda', stream=None):
+    """phmm_viterbi: (ll [P] float64 numpy, paths: list of [n_p, 3] int32 arrays of
+    (i, j, state)).  log_chi [P or 1, N, N] and the per-group log tables
+    [P or 1, G, ...] are float64 (torch or numpy)."""
+    lib = load()
+    st_arr = np.ascontiguousarray(np.asarray(state_types, np.int8))
+    gr = np.ascontiguousarray(np.asarray(groups, np.int32))
+    md = ModelDesc(st_arr.size, st_arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)),
+                   gr.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), int(G))
+    buf, xo, yo, Lx, Ly = pack_residues(xs, ys)
+    P = Lx.size
+    f64 = lambda a: (a if isinstance(a, torch.Tensor) else torch.as_tensor(np.asarray(a))).to(
+        device=device, dtype=torch.float64).contiguous()
+    lc, lm, li, ld = f64(log_chi), f64(log_M), f64(log_I), f64(log_D)
+    if lc.dim() == 2:
+        lc = lc.unsqueeze(0)
+    res_t = torch.from_numpy(buf).to(device)
+    b = DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo, residues=res_t, chi=lc, emit_M=lm, emit_I=li, emit_D=ld)
+    bs = b.struct()
+    nb = ctypes.c_size_t(0)
+    _check(lib.phmm_viterbi_workspace_bytes(ctypes.byref(md), ctypes.byref(bs), ctypes.byref(nb)),
+           'phmm_viterbi_workspace_bytes')
+    ws = torch.empty(max(int(nb.value), 256), dtype=torch.uint8, device=device)
+    ll = torch.empty(P, dtype=torch.float64, device=device)
+    n_path = int(np.sum(Lx.astype(np.int64) + Ly + 1))
+    path = torch.zeros(max(n_path, 1), 3, dtype=torch.int32, device=device)
+    plen = torch.zeros(P, dtype=torch.int32, device=device)
+    status = torch.zeros(P, dtype=torch.int32, device=device)
+    s = stream if stream is not None else torch.cuda.current_stream(torch.device(device))
+    _check(lib.phmm_viterbi(ctypes.byref(md), ctypes.byref(bs), _ptr(lc), _ptr(lm), _ptr(li), _ptr(ld), _ptr(ws),
+                            ctypes.c_size_t(ws.numel()), _ptr(ll), _ptr(path), _ptr(plen), _ptr(status),
+                            ctypes.c_void_p(s.cuda_stream)), 'phmm_viterbi')
+    ll_h, path_h, plen_h = ll.cpu().numpy(), path.cpu().numpy(), plen.cpu().numpy()
+    offs = np.concatenate([[0], np.cumsum(Lx.astype(np.int64) + Ly + 1)[:-1]])
+    return ll_h, [path_h[o:o + n] for o, n in zip(offs, plen_h)]

@@ -495,6 +495,40 @@ def mixdom2_constrained_log_prob(main_ins_rate, main_del_rate, t, dom_ins_rates,
     return ll if batched else ll[0]
 
 
+def _log_tkf_tables(sub_matrix, pi):
+    """The log emission terms of _pair_hmm_emission (dp/hmm.py:617-625) as per-group
+    tables: M[a][b] = log(pi_a + 1e-30) + log(P_ab + 1e-30), I/D[a] = log(pi_a + 1e-30),
+    index 20 (wildcard) log 1."""
+    sub = np.asarray(sub_matrix, np.float64)
+    pi_ = np.asarray(pi, np.float64)
+    A = pi_.size
+    lp = np.zeros(21)
+    lp[:A] = np.log(pi_ + 1e-30)
+    lM = np.zeros((21, 21))
+    lM[:A, :A] = np.log(pi_ + 1e-30)[:, None] + np.log(sub + 1e-30)
+    lM[:A, A:] = np.log(pi_ + 1e-30)[:, None]
+    return lM[None, None], lp[None, None], lp[None, None]
+
+
+def viterbi_2d_batch(log_trans, state_types, xs, ys, sub_matrix, pi):
+    """Batched viterbi_2d (dp/hmm.py:1976-2040) on the device: per pair the
+    log-probability of the best path and the path as (i, j, state) triples
+    from (0, 0, S) to (Lx, Ly, final state)."""
+    lt = np.asarray(log_trans, np.float64)
+    st = np.asarray(state_types)
+    lM, lI, lD = _log_tkf_tables(sub_matrix, pi)
+    ll, paths = _lib.viterbi(st, np.zeros(st.size, np.int32), 1, xs, ys, lt[None], lM, lI, lD,
+                             device=_device())
+    return ll, [[tuple(int(v) for v in row) for row in pth] for pth in paths]
+
+
+def viterbi_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi):
+    """viterbi_2d (dp/hmm.py:1976-2040): (log_prob, path as a list of (i, j, state))."""
+    ll, paths = viterbi_2d_batch(log_trans, state_types, [np.asarray(x_seq)], [np.asarray(y_seq)],
+                                 sub_matrix, pi)
+    return float(ll[0]), paths[0]
+
+
 def exact_suffstats_batch(n_chi_stack, main_ins, main_del, t_array, dom_ins, dom_del, dom_weights,
                           frag_weights, ext_rates):
     """Exact MixDom2 sufficient statistics from collapsed counts

@@ -322,6 +322,47 @@ def holmes_rubin_weighted_stats(Q, pi, t, mc):
     return W, U - torch.diag(torch.diag(U))
 
 
+def holmes_rubin_batch(class_S_exch, class_pis, ts, class_match_counts):
+    """Batched Holmes-Rubin statistics (core/ctmc.py:173-230, 285-326) for
+    per-pair times ts [P] and per-pair per-class match counts [P, C, A, A]:
+    W [P, C, A] (expected dwell times) and U [P, C, A, A] (expected
+    substitutions, zero diagonal), float64 on the counts' device.
+
+    Same quantities as holmes_rubin_weighted_stats, contracted without the
+    A^4 endpoint-conditioned tensor: with Q_c = D^-1/2 V diag(lam) V^T D^1/2
+    (D = diag(pi_c)), J[k,l] = (e^{lam_k t} - e^{lam_l t}) / (lam_k - lam_l)
+    (t e^{lam_k t} when equal) and R[a,b] = n[a,b] / P_ab(t) sqrt(pi_b / pi_a),
+    S = D^1/2 V (J o (V^T R V)) V^T D^-1/2; W = diag S, U = Q o S."""
+    mc = class_match_counts if isinstance(class_match_counts, torch.Tensor) else torch.as_tensor(
+        np.asarray(class_match_counts))
+    mc = mc.to(torch.float64)
+    dev = mc.device
+    # the class-level eigendecompositions on the host (C small matrices), the
+    # per-pair contractions on the counts' device
+    cp_h = pm._t(class_pis).cpu()
+    Q_h = pm.build_class_Q(pm._t(class_S_exch).cpu(), cp_h)                  # [C, A, A]
+    sp_h = torch.sqrt(cp_h)
+    Sm = Q_h * (sp_h[:, :, None] / sp_h[:, None, :])
+    lam, V = torch.linalg.eigh((Sm + Sm.transpose(1, 2)) / 2)              # [C, A], [C, A, A]
+    cp, Q, sp, lam, V = (v.to(dev) for v in (cp_h, Q_h, sp_h, lam, V))
+    t = pm._t(ts, device=dev).reshape(-1)                                  # [P]
+    ex = torch.exp(lam[None] * t[:, None, None])                           # [P, C, A]
+    diff = lam[:, :, None] - lam[:, None, :]                               # [C, A, A]
+    deg = diff.abs() < 1e-10
+    J = torch.where(deg[None], t[:, None, None, None] * ex[..., :, None],
+                    (ex[..., :, None] - ex[..., None, :]) / torch.where(deg, torch.ones_like(diff), diff)[None])
+    Mt = ((V[None] * ex[..., None, :]) @ V.transpose(1, 2)[None]) * (sp[:, None, :] / sp[:, :, None])[None]
+    ratio = mc / torch.where(Mt.abs() < 1e-30, torch.ones_like(Mt), Mt)
+    R = ratio * torch.sqrt(cp[:, None, :] / cp[:, :, None])[None]         # n/P * sqrt(pi_b / pi_a)
+    X = V.transpose(1, 2)[None] @ R @ V[None]
+    Z = V[None] @ (J * X) @ V.transpose(1, 2)[None]
+    Sij = Z * torch.sqrt(cp[:, :, None] / cp[:, None, :])[None]
+    W = torch.diagonal(Sij, dim1=-2, dim2=-1)
+    U = Q[None] * Sij
+    U = U - torch.diag_embed(torch.diagonal(U, dim1=-2, dim2=-1))
+    return W, U
+
+
 def _mixdom2_tables(params, ts, device):
     K = len(params['dom_ins'])
     F = np.asarray(params['frag_weights']).shape[1]
@@ -544,7 +585,8 @@ def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True, exact_suffst
 
     Returns a dict of device tensors: log_p [P], n_trans [P,N,N], cnt_M
     [P,G,21,21], cnt_I/cnt_D [P,G,21], status [P]; with with_class_counts,
-    the per-pair class counts of e_step_mixdom2; with exact_suffstats, under
+    the per-pair class counts of e_step_mixdom2 and their Holmes-Rubin
+    statistics class_W [P,C,A], class_U [P,C,A,A]; with exact_suffstats, under
     'suffstats', the per-pair exact sufficient statistics of the exploded
     model (exact_suffstats_batch on n_trans)."""
     dev = _device()
@@ -561,6 +603,8 @@ def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True, exact_suffst
             res.update(pro.class_counts(csubs, out['cnt_M'], out['cnt_I'], out['cnt_D']))
         else:
             res.update(class_split(params, out['cnt_M'], out['cnt_I'], out['cnt_D'], csubs=csubs))
+        res['class_W'], res['class_U'] = holmes_rubin_batch(params['class_S_exch'], params['class_pis'], ts,
+                                                            res['class_match_counts'])
     if exact_suffstats:
         res['suffstats'] = exact_suffstats_batch(out['n_trans'], params['main_ins'], params['main_del'], ts,
                                                  params['dom_ins'], params['dom_del'], params['dom_weights'],

@@ -302,6 +302,22 @@ int phmm_mixdom2_class_counts(const phmm_mixdom2_params *prm, int32_t n_pairs, c
                               double *class_match, double *class_insert, double *class_delete,
                               double *classdist_counts, void *stream);
 
+/* Holmes-Rubin substitution statistics of every (pair, class), float64 on
+ * the device (replaces core/ctmc.py:285-326 holmes_rubin_weighted_stats and
+ * its integrals core/ctmc.py:173-230, called once per class per pair by
+ * train/likelihood.py:279-344):
+ *   W[p,c,i]   = sum_ab n[p,c,a,b] I_c[a,b,i,i](t_p) / P_c,ab(t_p)
+ *   U[p,c,i,j] = Q_c[i,j] sum_ab n[p,c,a,b] I_c[a,b,i,j](t_p) / P_c,ab(t_p),
+ *                zero diagonal,
+ * contracted through the eigendecomposition of the symmetrised rate matrix
+ * (no A^4 integral tensor).  class_Q [C,A,A] and class_pis [C,A] are HOST
+ * arrays (Q reversible with respect to pi, pi > 0); t [P],
+ * class_match_counts [P,C,A,A], W [P,C,A] and U [P,C,A,A] are device
+ * arrays.  A <= 32.  Enqueued on the stream; PHMM_E_ARG on bad arguments. */
+int phmm_holmes_rubin(int32_t n_classes, int32_t alphabet, const double *class_Q, const double *class_pis,
+                      int32_t n_pairs, const double *t, const double *class_match_counts, double *W, double *U,
+                      void *stream);
+
 /* Per-kernel CUDA-event timing on the launching stream (diagnostics and
  * benchmarking; no counterpart in the reference, which has no kernels).
  * phmm_kernel_times waits for the last call's events and returns the forward

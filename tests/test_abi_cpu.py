@@ -68,3 +68,21 @@ def test_mixdom2_prologue_rejects_bad_shapes(lib):
     assert 'null device buffer' in _lib.last_error()
     assert lib.phmm_mixdom2_tables(ctypes.byref(prm), 0, *([null] * 7)) == 0
     assert lib.phmm_mixdom2_class_subs_count(ctypes.byref(prm), 10) == 10 * 400
+
+
+def test_holmes_rubin_rejects_bad_arguments(lib):
+    """phmm_holmes_rubin checks its arguments before any CUDA call."""
+    import ctypes
+    import numpy as np
+    from pairhmm import _lib
+    Q = np.zeros((1, 4, 4))
+    pi = np.full((1, 4), 0.25)
+    null = ctypes.c_void_p(0)
+    assert lib.phmm_holmes_rubin(1, 40, Q.ctypes.data, pi.ctypes.data, 3, null, null, null, null, null) == -1
+    assert 'alphabet' in _lib.last_error()
+    bad = np.array([[0.5, 0.5, 0.0, 0.0]])
+    assert lib.phmm_holmes_rubin(1, 4, Q.ctypes.data, bad.ctypes.data, 3, null, null, null, null, null) == -1
+    assert 'positive' in _lib.last_error()
+    assert lib.phmm_holmes_rubin(1, 4, Q.ctypes.data, pi.ctypes.data, 3, null, null, null, null, null) == -1
+    assert 'null device buffer' in _lib.last_error()
+    assert lib.phmm_holmes_rubin(1, 4, Q.ctypes.data, pi.ctypes.data, 0, null, null, null, null, null) == 0

@@ -687,7 +687,7 @@ __global__ void __launch_bounds__(32) count_warp_kernel(const KParams P) {
     const SmemC L = make_smem_c(SH::SP, SH::KP, SH::NI, P.G, P.max_ly);
     for (;;) {
         int it = 0;
-        if ((threadIdx.x & 31) == 0) it = atomicAdd(P.counter, 1);
+        if ((threadIdx.x & 31) == 0) it = count_claim(P);
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= P.n_items) break;
         const int2 w = P.items[it];

@@ -1001,7 +1001,7 @@ __global__ void __launch_bounds__(TWT) count_tw_kernel(const KParams P) {
     const SmemCT L = make_smem_ct(SH::SP, SH::KP, SH::NI, P.G, P.max_ly);
     int *s_item = reinterpret_cast<int *>(sm) + L.item;
     for (;;) {
-        if (threadIdx.x == 0) *s_item = atomicAdd(P.counter, 1);
+        if (threadIdx.x == 0) *s_item = count_claim(P);
         __syncthreads();
         const int it = *s_item;
         __syncthreads();

@@ -99,6 +99,7 @@ struct KParams {
     double *F_log, *B_log, *post;
     int max_ly;
     long long spin_limit;
+    const int *wave_ctr;                // overlapped count pass: forward, backward claim counters
 };
 
 struct SmemLayout {
@@ -181,6 +182,33 @@ __device__ bool count_ready(const KParams &P, const PairMeta &m, int si) {
     if (!wait_geq(b + si, done, P.spin_limit)) return false;
     if (si + 1 < m.n_stripes && !wait_geq(b + si + 1, done, P.spin_limit)) return false;
     return wait_geq(f + m.n_stripes - 1, done, P.spin_limit);
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Claim the next count item.  The overlapped count grid holds SM slots while
+// it waits for the wavefront kernels, and other work on the GPU (batches on
+// other streams) can keep those kernels from becoming resident at all, so an
+// overlapped CTA claims only once both wavefront kernels have claimed their
+// first stripe: a kernel that has claimed one is resident and drains its whole
+// list, so every later wait ends.  A CTA that sees no start within the window
+// leaves the remaining items to the tail grid, which runs after both
+// wavefronts on its own stream and waits on nothing.
+constexpr unsigned long long COUNT_START_WINDOW_NS = 200000;
+
+__device__ int count_claim(const KParams &P) {
+    if (P.count_wait) {
+        const unsigned long long t0 = globaltimer_ns();
+        while (ld_acquire(P.wave_ctr) == 0 || ld_acquire(P.wave_ctr + 1) == 0) {
+            if (globaltimer_ns() - t0 > COUNT_START_WINDOW_NS) return P.n_items;
+            __nanosleep(256);
+        }
+    }
+    return atomicAdd(P.counter, 1);
 }
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
@@ -1014,6 +1042,7 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
     C.progress = d_progress;
     C.bprogress = d_progress + stripes;
     C.count_wait = 1;
+    C.wave_ctr = d_counters;
     if (combined) {
         // one persistent launch pops forward and backward stripes from one list
         KParams FB = K;
@@ -1256,6 +1285,7 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     K.F_log = K.B_log = K.post = nullptr;
     K.max_ly = max_ly;
     K.spin_limit = 40LL * 1000 * 1000;
+    K.wave_ctr = nullptr;
     // ---- wavefronts, then the count pass (both on the caller's stream: a wide
     // wavefront CTA needs most of an SM's shared memory, so a count CTA waiting
     // beside it would only take its place)
@@ -1551,6 +1581,7 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     K.post = post;
     K.max_ly = max_ly;
     K.spin_limit = 40LL * 1000 * 1000;
+    K.wave_ctr = nullptr;
     if (split) return launch_split(plan, K, wl ? wl : bl, bl != nullptr, n_items, n_citems, stripes, max_ly, d_items,
                                    d_counters, d_progress, d_bedge, d_bedge_exp, stream);
     for (int pass = 0; pass < (estep ? 2 : 1); ++pass) {
@@ -2165,6 +2196,7 @@ extern "C" int phmm_estep_static(const phmm_model_desc *md, const phmm_batch *b,
     K.F_log = K.B_log = K.post = nullptr;
     K.max_ly = max_ly;
     K.spin_limit = 40LL * 1000 * 1000;
+    K.wave_ctr = nullptr;
     phmm_plan launch_ctx;   // carries the SM count for the shared launchers; owns no memory
     launch_ctx.sm_count = g_static_sms[dev];
     for (int pass = 0; pass < 2; ++pass) {

@@ -31,6 +31,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <deque>
+#include <mutex>
+#include <vector>
 
 extern "C" __attribute__((visibility("hidden"))) void phmm_internal_set_error(const char *msg);
 
@@ -830,6 +833,206 @@ extern "C" int phmm_mixdom2_chi_vjp(const phmm_mixdom2_params *prm, int32_t n_pa
         if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
     }
     chi_vjp_kernel<<<dim3(n_pairs, nd), THREADS, smem, (cudaStream_t)stream>>>(pk, t, N, grad_chi, grad);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    return PHMM_OK;
+}
+
+// ---------------------------------------------------------------- Holmes-Rubin statistics
+// Per (pair, class) endpoint-conditioned substitution statistics summed over
+// the pair's match counts (core/ctmc.py:173-230, 285-326):
+//   W[i]   = sum_ab n[a,b] I[a,b,i,i] / P_ab(t)
+//   U[i,j] = Q[i,j] sum_ab n[a,b] I[a,b,i,j] / P_ab(t)   (zero diagonal)
+// The reference builds the A^4 integral tensor I; with the symmetrised rate
+// matrix D^1/2 Q D^-1/2 = V diag(lam) V^T (D = diag(pi)) the same sums are
+// S = D^1/2 V (J o (V^T R V)) V^T D^-1/2, with R[a,b] = n[a,b] / P_ab(t)
+// sqrt(pi_b / pi_a) and J[k,l] = (e^{lam_k t} - e^{lam_l t}) / (lam_k - lam_l)
+// (t e^{lam_k t} where |lam_k - lam_l| < 1e-10, the reference's rule), so
+// W = diag S and U = Q o S: four A^3 products per (pair, class) instead of
+// an A^4 tensor.  The eigendecomposition is a property of the class, not of
+// the pair: it is computed on the host once per rate matrix (cyclic Jacobi)
+// and passed by value.
+namespace pro {
+
+constexpr int HR_MAXA = 32;
+constexpr int HR_THREADS = 128;
+
+struct HRClass {
+    int A;
+    double lam[HR_MAXA];
+    double V[HR_MAXA * HR_MAXA];   // row-major, column k = eigenvector k
+    double sp[HR_MAXA];            // sqrt(pi)
+    double Q[HR_MAXA * HR_MAXA];
+};
+
+__global__ void __launch_bounds__(HR_THREADS) hr_kernel(const __grid_constant__ HRClass hc, int c, int C,
+                                                        const double *__restrict__ t,
+                                                        const double *__restrict__ mc, double *__restrict__ W,
+                                                        double *__restrict__ U) {
+    __shared__ double V[HR_MAXA * HR_MAXA], R[HR_MAXA * HR_MAXA], T1[HR_MAXA * HR_MAXA], Y[HR_MAXA * HR_MAXA];
+    __shared__ double ex[HR_MAXA], lam[HR_MAXA], sp[HR_MAXA];
+    const int p = blockIdx.x, tid = threadIdx.x, A = hc.A, AA = A * A;
+    const double tp = t[p];
+    for (int i = tid; i < AA; i += HR_THREADS) V[i] = hc.V[i];
+    for (int i = tid; i < A; i += HR_THREADS) {
+        lam[i] = hc.lam[i];
+        sp[i] = hc.sp[i];
+        ex[i] = exp(hc.lam[i] * tp);
+    }
+    __syncthreads();
+    const size_t base = ((size_t)p * C + c) * AA;
+    const double *n = mc + base;
+    // R = n / P(t), P_ab(t) = sqrt(pi_b / pi_a) sum_k V[a,k] e^{lam_k t} V[b,k]
+    for (int i = tid; i < AA; i += HR_THREADS) {
+        const int a = i / A, b = i - a * A;
+        double s = 0.0;
+        for (int k = 0; k < A; ++k) s += V[a * A + k] * ex[k] * V[b * A + k];
+        const double r = sp[b] / sp[a];
+        const double Pab = s * r;
+        R[i] = n[i] / (fabs(Pab) < 1e-30 ? 1.0 : Pab) * r;
+    }
+    __syncthreads();
+    // T1 = V^T R
+    for (int i = tid; i < AA; i += HR_THREADS) {
+        const int k = i / A, b = i - k * A;
+        double s = 0.0;
+        for (int a = 0; a < A; ++a) s += V[a * A + k] * R[a * A + b];
+        T1[i] = s;
+    }
+    __syncthreads();
+    // Y = J o (T1 V)
+    for (int i = tid; i < AA; i += HR_THREADS) {
+        const int k = i / A, l = i - k * A;
+        double s = 0.0;
+        for (int b = 0; b < A; ++b) s += T1[k * A + b] * V[b * A + l];
+        const double d = lam[k] - lam[l];
+        const double j = fabs(d) < 1e-10 ? tp * ex[k] : (ex[k] - ex[l]) / d;
+        Y[i] = j * s;
+    }
+    __syncthreads();
+    // R = V Y
+    for (int i = tid; i < AA; i += HR_THREADS) {
+        const int a = i / A, l = i - a * A;
+        double s = 0.0;
+        for (int k = 0; k < A; ++k) s += V[a * A + k] * Y[k * A + l];
+        R[i] = s;
+    }
+    __syncthreads();
+    // S = D^1/2 (R V^T) D^-1/2; W = diag S, U = Q o S off the diagonal
+    for (int i = tid; i < AA; i += HR_THREADS) {
+        const int a = i / A, b = i - a * A;
+        double s = 0.0;
+        for (int l = 0; l < A; ++l) s += R[a * A + l] * V[b * A + l];
+        s *= sp[a] / sp[b];
+        U[base + i] = a == b ? 0.0 : hc.Q[i] * s;
+        if (a == b) W[((size_t)p * C + c) * A + a] = s;
+    }
+}
+
+// Eigenvalues and orthonormal eigenvectors of a symmetric n x n matrix by the
+// cyclic Jacobi method (Golub & Van Loan, Matrix Computations, sec. 8.5):
+// sweeps of plane rotations, each zeroing one off-diagonal entry with the
+// smaller rotation angle, until the off-diagonal mass is below roundoff.
+// a is overwritten; v receives the eigenvectors as columns.
+static void sym_eig_jacobi(int n, double *a, double *lam, double *v) {
+    for (int i = 0; i < n * n; ++i) v[i] = 0.0;
+    for (int i = 0; i < n; ++i) v[i * n + i] = 1.0;
+    double total = 0.0;
+    for (int i = 0; i < n * n; ++i) total += a[i] * a[i];
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) off += a[p * n + q] * a[p * n + q];
+        if (off <= 1e-36 * total || off == 0.0) break;
+        for (int p = 0; p < n; ++p) {
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = a[p * n + q];
+                if (apq == 0.0) continue;
+                const double theta = (a[q * n + q] - a[p * n + p]) / (2.0 * apq);
+                const double tn = (theta >= 0.0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double cs = 1.0 / std::sqrt(tn * tn + 1.0), sn = tn * cs;
+                for (int k = 0; k < n; ++k) {   // columns p, q
+                    const double akp = a[k * n + p], akq = a[k * n + q];
+                    a[k * n + p] = cs * akp - sn * akq;
+                    a[k * n + q] = sn * akp + cs * akq;
+                }
+                for (int k = 0; k < n; ++k) {   // rows p, q
+                    const double apk = a[p * n + k], aqk = a[q * n + k];
+                    a[p * n + k] = cs * apk - sn * aqk;
+                    a[q * n + k] = sn * apk + cs * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double vkp = v[k * n + p], vkq = v[k * n + q];
+                    v[k * n + p] = cs * vkp - sn * vkq;
+                    v[k * n + q] = sn * vkp + cs * vkq;
+                }
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i) lam[i] = a[i * n + i];
+}
+
+// The class-level part, cached by the exact rate matrix and frequencies (EM
+// calls the E-step many times between parameter updates).
+struct HRCacheEntry {
+    std::vector<double> key;
+    HRClass hc;
+};
+static std::mutex hr_mu;
+static std::deque<HRCacheEntry> hr_cache;
+constexpr size_t HR_CACHE = 32;
+
+static void hr_class(int A, const double *Q, const double *pi, HRClass &hc) {
+    std::vector<double> key(Q, Q + A * A);
+    key.insert(key.end(), pi, pi + A);
+    {
+        std::lock_guard<std::mutex> g(hr_mu);
+        for (const auto &e : hr_cache)
+            if (e.key.size() == key.size() && std::memcmp(e.key.data(), key.data(), sizeof(double) * key.size()) == 0) {
+                hc = e.hc;
+                return;
+            }
+    }
+    std::memset(&hc, 0, sizeof(hc));
+    hc.A = A;
+    for (int a = 0; a < A; ++a) hc.sp[a] = std::sqrt(pi[a]);
+    std::vector<double> sym(A * A);
+    for (int a = 0; a < A; ++a)
+        for (int b = 0; b < A; ++b) {
+            const double x = Q[a * A + b] * (hc.sp[a] / hc.sp[b]);
+            const double y = Q[b * A + a] * (hc.sp[b] / hc.sp[a]);
+            sym[a * A + b] = 0.5 * (x + y);
+        }
+    std::vector<double> v(A * A);
+    sym_eig_jacobi(A, sym.data(), hc.lam, v.data());
+    std::memcpy(hc.V, v.data(), sizeof(double) * A * A);
+    std::memcpy(hc.Q, Q, sizeof(double) * A * A);
+    std::lock_guard<std::mutex> g(hr_mu);
+    hr_cache.push_front(HRCacheEntry{std::move(key), hc});
+    if (hr_cache.size() > HR_CACHE) hr_cache.pop_back();
+}
+
+}  // namespace pro
+
+extern "C" int phmm_holmes_rubin(int32_t n_classes, int32_t alphabet, const double *class_Q, const double *class_pis,
+                                 int32_t n_pairs, const double *t, const double *class_match_counts, double *W,
+                                 double *U, void *stream) {
+    using namespace pro;
+    if (n_classes < 1 || alphabet < 1 || alphabet > HR_MAXA)
+        return pro_fail(PHMM_E_ARG, "phmm_holmes_rubin: need n_classes >= 1 and 1 <= alphabet <= 32");
+    if (!class_Q || !class_pis) return pro_fail(PHMM_E_ARG, "phmm_holmes_rubin: null host rate matrices");
+    if (n_pairs < 0) return pro_fail(PHMM_E_ARG, "phmm_holmes_rubin: negative n_pairs");
+    for (int i = 0; i < n_classes * alphabet; ++i)
+        if (!(class_pis[i] > 0.0))
+            return pro_fail(PHMM_E_ARG, "phmm_holmes_rubin: stationary frequencies must be positive");
+    if (n_pairs == 0) return PHMM_OK;
+    if (!t || !class_match_counts || !W || !U) return pro_fail(PHMM_E_ARG, "phmm_holmes_rubin: null device buffer");
+    const int A = alphabet;
+    for (int c = 0; c < n_classes; ++c) {
+        HRClass hc;
+        hr_class(A, class_Q + (size_t)c * A * A, class_pis + (size_t)c * A, hc);
+        hr_kernel<<<n_pairs, HR_THREADS, 0, (cudaStream_t)stream>>>(hc, c, n_classes, t, class_match_counts, W, U);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
     return PHMM_OK;

@@ -26,7 +26,7 @@ EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep'
            'phmm_last_error', 'phmm_version', 'phmm_mixdom2_class_subs_count', 'phmm_mixdom2_tables',
            'phmm_mixdom2_class_counts', 'phmm_tkf92_tables', 'phmm_mixdom2_chi',
            'phmm_mixdom2_chi_vjp_dirs', 'phmm_mixdom2_chi_vjp', 'phmm_fb1d_workspace_bytes', 'phmm_fb1d',
-           'phmm_fb1d_emissions', 'phmm_viterbi_workspace_bytes', 'phmm_viterbi')
+           'phmm_fb1d_emissions', 'phmm_viterbi_workspace_bytes', 'phmm_viterbi', 'phmm_holmes_rubin')
 
 
 class ModelDesc(ctypes.Structure):
@@ -148,6 +148,8 @@ def load(path=None):
     lib.phmm_viterbi.argtypes = [ctypes.POINTER(ModelDesc), ctypes.POINTER(Batch)] + [vp] * 4 + \
         [vp, ctypes.c_size_t, vp, vp, vp, vp, vp]
     lib.phmm_viterbi.restype = ctypes.c_int
+    lib.phmm_holmes_rubin.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int32, vp, vp, vp, vp, vp]
+    lib.phmm_holmes_rubin.restype = ctypes.c_int
     lib.phmm_version.argtypes = []
     lib.phmm_version.restype = ctypes.c_int
     _LIB = lib
@@ -597,6 +599,28 @@ def tkf92_tables(ins_rate, del_rate, ext, Q, pi, ts, device='cuda', stream=None)
     times ts: (chi [P,5,5] f32, EM [P,1,21,21] f32, EI [P,1,21] f32, ED
     [P,1,21] f32, sub [P,20,20] f64) device tensors."""
     return Tkf92Prologue(ins_rate, del_rate, ext, Q, pi)(ts, device=device, stream=stream)
+
+
+def holmes_rubin(class_Q, class_pis, t, class_match_counts, stream=None):
+    """phmm_holmes_rubin: (W [P,C,A], U [P,C,A,A]) float64 device tensors for
+    host rate matrices class_Q [C,A,A], frequencies class_pis [C,A], device
+    times t [P] and device match counts [P,C,A,A]."""
+    lib = load()
+    host = lambda v: v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else v
+    Q = np.ascontiguousarray(np.asarray(host(class_Q), np.float64))
+    pis = np.ascontiguousarray(np.asarray(host(class_pis), np.float64))
+    if Q.ndim == 2:
+        Q, pis = Q[None], pis.reshape(1, -1)
+    C, A = pis.shape
+    mc = class_match_counts.to(torch.float64).contiguous()
+    P = mc.shape[0]
+    tt = t.to(device=mc.device, dtype=torch.float64).reshape(-1).contiguous()
+    W = torch.empty(P, C, A, dtype=torch.float64, device=mc.device)
+    U = torch.empty(P, C, A, A, dtype=torch.float64, device=mc.device)
+    s = stream if stream is not None else torch.cuda.current_stream(mc.device)
+    _check(lib.phmm_holmes_rubin(C, A, Q.ctypes.data, pis.ctypes.data, P, _ptr(tt), _ptr(mc), _ptr(W), _ptr(U),
+                                 ctypes.c_void_p(s.cuda_stream)), 'phmm_holmes_rubin')
+    return W, U
 
 
 def fb1d(n_states, L, off, emit, chi, chi_per_pair, init_state, final_state, posteriors=False, stream=None):

@@ -300,67 +300,34 @@ def class_split(params, cM, cI, cD, csubs=None):
 
 
 def holmes_rubin_weighted_stats(Q, pi, t, mc):
-    """W[i], U[i,j] (core/ctmc.py:173-230, 285-326), float64 torch."""
-    Q, pi, mc = pm._t(Q), pm._t(pi), pm._t(mc)
-    sp = torch.sqrt(pi)
-    Sm = Q * (sp[:, None] / sp[None, :])
-    Sm = (Sm + Sm.T) / 2
-    lam, V = torch.linalg.eigh(Sm)
-    ex = torch.exp(lam * t)
-    diff = lam[:, None] - lam[None, :]
-    deg = diff.abs() < 1e-10
-    J = torch.where(deg, t * ex[:, None], (ex[:, None] - ex[None, :]) / torch.where(deg, torch.ones_like(diff), diff))
-    VV = V[:, None, :] * V[None, :, :]
-    I_sym = torch.einsum('aik,kl,jbl->aibj', VV, J, VV)
-    pf = torch.sqrt((pi[None, None, :, None] * pi[None, :, None, None])
-                    / (pi[:, None, None, None] * pi[None, None, None, :] + 1e-30))
-    Iab = I_sym.permute(0, 2, 1, 3) * pf.permute(0, 2, 1, 3)
-    Mt = ((V * ex[None, :]) @ V.T) * (sp[None, :] / sp[:, None])
-    ratio = mc / torch.where(Mt.abs() < 1e-30, torch.ones_like(Mt), Mt)
-    W = torch.einsum('ab,abii->i', ratio, Iab)
-    U = Q * torch.einsum('ab,abij->ij', ratio, Iab)
-    return W, U - torch.diag(torch.diag(U))
+    """W[i], U[i,j] (core/ctmc.py:173-230, 285-326) of one (Q, pi, t) and one
+    [A, A] match-count grid, float64 host tensors, through phmm_holmes_rubin."""
+    Qh = pm._t(Q).cpu().numpy()
+    pih = pm._t(pi).cpu().numpy()
+    dev = _device()
+    mcd = pm._t(mc).to(dev).reshape(1, 1, *Qh.shape)
+    W, U = _lib.holmes_rubin(Qh, pih, torch.tensor([float(t)], dtype=torch.float64, device=dev), mcd)
+    return W[0, 0].cpu(), U[0, 0].cpu()
 
 
 def holmes_rubin_batch(class_S_exch, class_pis, ts, class_match_counts):
     """Batched Holmes-Rubin statistics (core/ctmc.py:173-230, 285-326) for
     per-pair times ts [P] and per-pair per-class match counts [P, C, A, A]:
     W [P, C, A] (expected dwell times) and U [P, C, A, A] (expected
-    substitutions, zero diagonal), float64 on the counts' device.
-
-    Same quantities as holmes_rubin_weighted_stats, contracted without the
-    A^4 endpoint-conditioned tensor: with Q_c = D^-1/2 V diag(lam) V^T D^1/2
-    (D = diag(pi_c)), J[k,l] = (e^{lam_k t} - e^{lam_l t}) / (lam_k - lam_l)
-    (t e^{lam_k t} when equal) and R[a,b] = n[a,b] / P_ab(t) sqrt(pi_b / pi_a),
-    S = D^1/2 V (J o (V^T R V)) V^T D^-1/2; W = diag S, U = Q o S."""
+    substitutions, zero diagonal), float64 on the counts' device, by the
+    phmm_holmes_rubin kernel (one CTA per pair and class contracting the
+    eigendecomposition of the symmetrised class rate matrix; no A^4 endpoint
+    tensor)."""
     mc = class_match_counts if isinstance(class_match_counts, torch.Tensor) else torch.as_tensor(
         np.asarray(class_match_counts))
-    mc = mc.to(torch.float64)
-    dev = mc.device
-    # the class-level eigendecompositions on the host (C small matrices), the
-    # per-pair contractions on the counts' device
-    cp_h = pm._t(class_pis).cpu()
-    Q_h = pm.build_class_Q(pm._t(class_S_exch).cpu(), cp_h)                  # [C, A, A]
-    sp_h = torch.sqrt(cp_h)
-    Sm = Q_h * (sp_h[:, :, None] / sp_h[:, None, :])
-    lam, V = torch.linalg.eigh((Sm + Sm.transpose(1, 2)) / 2)              # [C, A], [C, A, A]
-    cp, Q, sp, lam, V = (v.to(dev) for v in (cp_h, Q_h, sp_h, lam, V))
-    t = pm._t(ts, device=dev).reshape(-1)                                  # [P]
-    ex = torch.exp(lam[None] * t[:, None, None])                           # [P, C, A]
-    diff = lam[:, :, None] - lam[:, None, :]                               # [C, A, A]
-    deg = diff.abs() < 1e-10
-    J = torch.where(deg[None], t[:, None, None, None] * ex[..., :, None],
-                    (ex[..., :, None] - ex[..., None, :]) / torch.where(deg, torch.ones_like(diff), diff)[None])
-    Mt = ((V[None] * ex[..., None, :]) @ V.transpose(1, 2)[None]) * (sp[:, None, :] / sp[:, :, None])[None]
-    ratio = mc / torch.where(Mt.abs() < 1e-30, torch.ones_like(Mt), Mt)
-    R = ratio * torch.sqrt(cp[:, None, :] / cp[:, :, None])[None]         # n/P * sqrt(pi_b / pi_a)
-    X = V.transpose(1, 2)[None] @ R @ V[None]
-    Z = V[None] @ (J * X) @ V.transpose(1, 2)[None]
-    Sij = Z * torch.sqrt(cp[:, :, None] / cp[:, None, :])[None]
-    W = torch.diagonal(Sij, dim1=-2, dim2=-1)
-    U = Q[None] * Sij
-    U = U - torch.diag_embed(torch.diagonal(U, dim1=-2, dim2=-1))
-    return W, U
+    S = np.asarray(pm._t(class_S_exch).cpu().numpy(), np.float64)
+    pis = np.asarray(pm._t(class_pis).cpu().numpy(), np.float64)
+    Q = S * pis[:, None, :]
+    for c in range(Q.shape[0]):
+        np.fill_diagonal(Q[c], 0.0)
+        np.fill_diagonal(Q[c], -Q[c].sum(axis=1))
+    t = ts if isinstance(ts, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(np.asarray(ts, np.float64)))
+    return _lib.holmes_rubin(Q, pis, t.to(mc.device), mc)
 
 
 def _mixdom2_tables(params, ts, device):
@@ -591,7 +558,9 @@ def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True, exact_suffst
     model (exact_suffstats_batch on n_trans)."""
     dev = _device()
     pro = _lib.MixDom2Prologue(params)
-    chi, EM, EI, ED, csubs = pro(ts, device=dev)
+    t_dev = (ts if isinstance(ts, torch.Tensor) else torch.from_numpy(
+        np.ascontiguousarray(np.asarray(ts, np.float64).reshape(-1)))).to(device=dev, dtype=torch.float64)
+    chi, EM, EI, ED, csubs = pro(t_dev, device=dev)
     K, F = pro.K, pro.F
     plan = get_plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)
     b = _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev)
@@ -603,7 +572,7 @@ def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True, exact_suffst
             res.update(pro.class_counts(csubs, out['cnt_M'], out['cnt_I'], out['cnt_D']))
         else:
             res.update(class_split(params, out['cnt_M'], out['cnt_I'], out['cnt_D'], csubs=csubs))
-        res['class_W'], res['class_U'] = holmes_rubin_batch(params['class_S_exch'], params['class_pis'], ts,
+        res['class_W'], res['class_U'] = holmes_rubin_batch(params['class_S_exch'], params['class_pis'], t_dev,
                                                             res['class_match_counts'])
     if exact_suffstats:
         res['suffstats'] = exact_suffstats_batch(out['n_trans'], params['main_ins'], params['main_del'], ts,
@@ -617,19 +586,11 @@ def e_step_mixdom2(params, x, y):
     class_W, class_U, class_match_counts, class_insert_counts,
     class_delete_counts, classdist_counts)."""
     r = estep_batch_mixdom2(params, [np.asarray(x)], [np.asarray(y)], np.array([params['t']]))
-    cp = pm._t(params['class_pis'])
-    cS = pm._t(params['class_S_exch'])
-    ss = {k: r[k][0].cpu() for k in ('class_match_counts', 'class_insert_counts',
-                                     'class_delete_counts', 'classdist_counts')}
-    W, U = [], []
-    for c in range(cp.shape[0]):
-        Qc = pm.build_class_Q(cS[c], cp[c])
-        w, u = holmes_rubin_weighted_stats(Qc, cp[c], float(params['t']), ss['class_match_counts'][c])
-        W.append(w)
-        U.append(u)
-    out = {'class_W': torch.stack(W).numpy(), 'class_U': torch.stack(U).numpy()}
-    out.update({k: v.numpy() for k, v in ss.items()})
-    return float(r['log_p'][0]), r['n_trans'][0].cpu().numpy(), out
+    keys = ('class_W', 'class_U', 'class_match_counts', 'class_insert_counts', 'class_delete_counts',
+            'classdist_counts')
+    host = to_host({k: r[k] for k in keys + ('log_p', 'n_trans')})
+    out = {k: host[k][0] for k in keys}
+    return float(host['log_p'][0]), host['n_trans'][0], out
 
 
 # ---------------------------------------------------------------- differentiable log-likelihood

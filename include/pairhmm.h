@@ -72,6 +72,17 @@ typedef struct phmm_batch {
     const float *emit_I;         /* device [P or 1][G][21] */
     const float *emit_D;         /* device [P or 1][G][21] */
     int32_t emit_per_pair;       /* 1: tables per pair, 0: shared */
+    /* device, may be NULL: one byte per lattice cell, pairs concatenated in
+     * batch order, each pair row-major (Lx+1) x (Ly+1); bit 0 lets the
+     * M-type states emit at the cell, bit 1 the I-type, bit 2 the D-type
+     * (a cleared bit is the reference's NEG_INF emission), and a zero byte
+     * at (0, 0) removes the start.  Expresses mask_emissions_match_aligned
+     * (dp/hmm.py:1085-1117: bit 0 only at the alignment's match cells) and
+     * the banded recursions (dp/hmm.py:2104-2492: zero bytes off the band).
+     * Honoured by the generic and two-warp kernels (variants 0, 1, 7; the
+     * automatic choice takes these for a masked batch) and by
+     * phmm_estep_tables. */
+    const uint8_t *cell_mask;
 } phmm_batch;
 
 typedef struct phmm_plan phmm_plan;

@@ -40,7 +40,9 @@ __host__ __device__ inline SmemTW make_smem_tw(int SP, int KP, int NI, int G, in
     return L;
 }
 
-template <class SH>
+// MK: the batch carries a cell mask (a separate instantiation, so the
+// unmasked recursion carries none of the mask's instructions)
+template <class SH, bool MK>
 __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT, float *sm,
                               unsigned char *smb) {
     constexpr int NE = SH::NE, NSRC = SH::NSRC, SP = SH::SP, KP = SH::KP, NM = SH::NM, NI = SH::NI;
@@ -94,14 +96,19 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
     const int T_last = (nrows - 1) + Ly;
     // M- and I-type emission factors of the cell of the next step, loaded one
     // step ahead (the y character and the table lookup are two dependent loads)
+    // (and the cell's type mask: bit 0 M, 1 I, 2 D may emit; 7 without a mask)
     float eMI[NM + NI > 0 ? NM + NI : 1];
+    int mbx = 7;
+    const unsigned char *mrow = MK ? P.cmask + m.tab_base + (int64_t)rowi * (Ly + 1) : nullptr;
     auto load_emit = [&](int tt) {
         const int j = tt - r;
-        const int yj = (r < nrows && j >= 0 && j <= Ly) ? ys[j] : 0;
+        const bool in = r < nrows && j >= 0 && j <= Ly;
+        const int yj = in ? ys[j] : 0;
 #pragma unroll
         for (int k = 0; k < NM; ++k) eMI[k] = sm[offM[k] + yj];
 #pragma unroll
         for (int k = 0; k < NI; ++k) eMI[NM + k] = sm[offI[k] + yj];
+        if (MK) mbx = in ? (int)__ldg(mrow + j) : 7;
     };
     load_emit(0);
     bool aborted = false;
@@ -155,7 +162,9 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
             d0[q].x = l0 ? (top ? (halo ? hx[2 * q] : 0.f) : bv[2 * q]) : vx;
             d0[q].y = l0 ? (top ? (halo ? hx[2 * q + 1] : 0.f) : bv[2 * q + 1]) : vy;
         }
-        const bool hasI = jc >= 1, hasD = rowi >= 1, hasM = hasI && hasD;
+        // a type that may not emit here contributes nothing (nor its exponent)
+        const bool hasI = jc >= 1 && (mbx & 2), hasD = rowi >= 1 && (mbx & 4);
+        const bool hasM = jc >= 1 && rowi >= 1 && (mbx & 1);
         const int EI = hasI ? Eprev : EXP_NONE, ED = hasD ? EdA : EXP_NONE, EM = hasM ? Em0 : EXP_NONE;
         const int Eref = max(max(EI, ED), EM);
         float2 acc2[NE];
@@ -218,7 +227,7 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
         }
         // origin: F[0,0,start] = 1
         float sNew = 0.f;
-        if (valid && rowi == 0 && jc == 0) { sNew = 1.f; Enew = 0; }
+        if (valid && rowi == 0 && jc == 0 && mbx != 0) { sNew = 1.f; Enew = 0; }
         if (valid) {
             if (P.lat) {
                 float4 *dst = reinterpret_cast<float4 *>(P.lat + (latc + (int64_t)t * ROWS + r) * SP);
@@ -310,7 +319,7 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
     if (r == 0) st_release(prog_mine, Ly + 2);
 }
 
-template <class SH>
+template <class SH, bool MK>
 __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT, float *sm,
                                   unsigned char *smb) {
     constexpr int NE = SH::NE, NSRC = SH::NSRC, SP = SH::SP, KP = SH::KP, NM = SH::NM, NI = SH::NI;
@@ -366,14 +375,24 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
 
     const int T_last = (nrows - 1) + Ly;
     // M- and I-type emission factors of the cell of the next step, loaded one step ahead
+    // (and the cell's type mask, as in the forward, folded into the factors
+    // here, off the step's dependency chain: eDc is eD with the D bit applied)
     float eMI[NM + NI > 0 ? NM + NI : 1];
+    float eDc[SH::ND > 0 ? SH::ND : 1];
+    int mbx = 7;
+    const unsigned char *mrow = MK ? P.cmask + m.tab_base + (int64_t)rowi * (Ly + 1) : nullptr;
     auto load_emit = [&](int tt) {
         const int j = tt - r;
-        const int yj = (r < nrows && j >= 0 && j <= Ly) ? ys[j] : 0;
+        const bool in = r < nrows && j >= 0 && j <= Ly;
+        const int yj = in ? ys[j] : 0;
+        if (MK) mbx = in ? (int)__ldg(mrow + j) : 7;
+        const float bM = (mbx & 1) ? 1.f : 0.f, bI = (mbx & 2) ? 1.f : 0.f, bD = (mbx & 4) ? 1.f : 0.f;
 #pragma unroll
-        for (int k = 0; k < NM; ++k) eMI[k] = sm[offM[k] + yj];
+        for (int k = 0; k < NM; ++k) eMI[k] = sm[offM[k] + yj] * bM;
 #pragma unroll
-        for (int k = 0; k < NI; ++k) eMI[NM + k] = sm[offI[k] + yj];
+        for (int k = 0; k < NI; ++k) eMI[NM + k] = sm[offI[k] + yj] * bI;
+#pragma unroll
+        for (int k = 0; k < SH::ND; ++k) eDc[k] = eD[k] * bD;
     };
     load_emit(T_last);
     bool aborted = false;
@@ -489,13 +508,22 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
             } else {
                 Eb = EXP_NONE;
             }
+            // a type that may not emit here gets w = e b = 0 (its factor is 0)
+            // and a stored b of 0, so neither its predecessors nor the count
+            // pass see it
 #pragma unroll
             for (int k = 0; k < NE; ++k) {
-                float ev;
                 const int ty = SH::type_of(k);
-                if (ty == T_M || ty == T_I) ev = eMI[k];
-                else ev = eD[k - NM - NI];
+                const float ev = (ty == T_M || ty == T_I) ? eMI[k] : eDc[k - NM - NI];
                 wnew[k] = acc[k] * ev;
+            }
+            if (MK && mbx != 7) {
+#pragma unroll
+                for (int k = 0; k < NE; ++k) {
+                    const int ty = SH::type_of(k);
+                    const int bit = ty == T_M ? 1 : (ty == T_I ? 2 : 4);
+                    if (!(mbx & bit)) acc[k] = 0.f;
+                }
             }
         }
         if (valid) {
@@ -535,7 +563,7 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
             wn[q].y = (valid && k1 < NE) ? wnew[k1] : 0.f;
         }
         EmR = EdRn;
-        Ewn = valid ? Eb : EXP_NONE;
+        Ewn = (valid && mbx != 0) ? Eb : EXP_NONE;
         // row 32 hands its new state to row 31 for step t-1
         if (r == 32) {
             float2 *b2 = reinterpret_cast<float2 *>(bnd + (t & 1) * SP);
@@ -575,7 +603,7 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
 
 // Persistent two-warp CTAs popping stripe items (forward: kind 5; backward
 // recursion: kind 6).
-template <class SH, bool BWD>
+template <class SH, bool BWD, bool MK>
 __global__ void __launch_bounds__(TWT) stripe_tw_kernel(const KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *sm = reinterpret_cast<float *>(smem_raw);
@@ -587,8 +615,8 @@ __global__ void __launch_bounds__(TWT) stripe_tw_kernel(const KParams P) {
         const int it = *s_item;
         if (it >= P.n_items) break;
         const int2 w = P.items[it];
-        if (BWD) bwd_rec_stripe_tw<SH>(P, w.x, w.y, L, sm, smem_raw);
-        else fwd_stripe_tw<SH>(P, w.x, w.y, L, sm, smem_raw);
+        if (BWD) bwd_rec_stripe_tw<SH, MK>(P, w.x, w.y, L, sm, smem_raw);
+        else fwd_stripe_tw<SH, MK>(P, w.x, w.y, L, sm, smem_raw);
     }
 }
 

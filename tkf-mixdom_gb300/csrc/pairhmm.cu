@@ -100,6 +100,7 @@ struct KParams {
     int max_ly;
     long long spin_limit;
     const int *wave_ctr;                // overlapped count pass: forward, backward claim counters
+    const unsigned char *cmask;         // per-cell type mask (bit 0 M, 1 I, 2 D) at tab_base, or null
 };
 
 struct SmemLayout {
@@ -358,13 +359,15 @@ __device__ void forward_stripe(const KParams &P, int p, int si, const SmemLayout
         const int j = t - r;
         const bool valid = (r < nrows) && (j >= 0) && (j <= Ly);
         int Eref = EXP_NONE;
+        const int mb = (P.cmask && valid) ? (int)P.cmask[m.tab_base + (int64_t)i * (Ly + 1) + j] : 7;
         if (valid) {
             const float *pp = nullptr;
             int pst = TH, Ep = EXP_NONE;
-            // I pred (i, j-1): diag t-1, row r
-            const bool hasI = j >= 1;
-            const bool hasD = i >= 1;
-            const bool hasM = hasD && hasI;
+            // I pred (i, j-1): diag t-1, row r; a type the cell mask rules out
+            // here takes no part (nor its exponent)
+            const bool hasI = j >= 1 && (mb & 2);
+            const bool hasD = i >= 1 && (mb & 4);
+            const bool hasM = i >= 1 && j >= 1 && (mb & 1);
             int EI_ = EXP_NONE, ED_ = EXP_NONE, EM_ = EXP_NONE;
             const float *pI = ring + ((t + 2) % 3) * NS * TH + r;
             const float *pD = nullptr, *pM = nullptr;
@@ -436,7 +439,7 @@ __device__ void forward_stripe(const KParams &P, int p, int si, const SmemLayout
             } else {
                 v = make_float4(0.f, 0.f, 0.f, 0.f);
             }
-            if (i == 0 && j == 0) {  // origin: F[0,0,start] = 1 (dp/hmm.py:1212)
+            if (i == 0 && j == 0 && mb != 0) {  // origin: F[0,0,start] = 1 (dp/hmm.py:1212)
                 v = make_float4(0.f, 0.f, 0.f, 0.f);
                 const int ss = P.s_slot;
                 if (ss / 4 == q) {
@@ -706,14 +709,21 @@ __device__ void backward_stripe(const KParams &P, int p, int si, const SmemLayou
             } else {
                 b = make_float4(0.f, 0.f, 0.f, 0.f);
             }
-            const float4 e4 = emit4(sm, eb, ys[j]);
+            float4 e4 = emit4(sm, eb, ys[j]);
+            int Ew = Eb;   // exponent of w; none where no type may emit
+            if (P.cmask) {   // a masked type emits nothing here: w = 0, so no predecessor sees it
+                const int mb = P.cmask[m.tab_base + (int64_t)i * (Ly + 1) + j];
+                const bool off = (qt == T_M && !(mb & 1)) || (qt == T_I && !(mb & 2)) || (qt == T_D && !(mb & 4));
+                if (off) e4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (mb == 0) Ew = EXP_NONE;
+            }
             const float4 w = make_float4(b.x * e4.x, b.y * e4.y, b.z * e4.z, b.w * e4.w);
             float *rg = ring + (t % 3) * NS * TH + (4 * q) * TH + r;
             rg[0] = w.x; rg[TH] = w.y; rg[2 * TH] = w.z; rg[3 * TH] = w.w;
-            if (q == 0) ringE[(t % 3) * TH + r] = Eb;
+            if (q == 0) ringE[(t % 3) * TH + r] = Ew;
             if (has_above && r == 0) {
                 reinterpret_cast<float4 *>(edge_mine + (int64_t)j * NS)[q] = w;
-                if (q == 0) edgeE_mine[j] = Eb;
+                if (q == 0) edgeE_mine[j] = Ew;
             }
             // forward values of this cell
             const float4 f = reinterpret_cast<const float4 *>(fst + (t & 1) * TH * NS + r * NS)[q];
@@ -1286,6 +1296,7 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     K.max_ly = max_ly;
     K.spin_limit = 40LL * 1000 * 1000;
     K.wave_ctr = nullptr;
+    K.cmask = nullptr;
     // ---- wavefronts, then the count pass (both on the caller's stream: a wide
     // wavefront CTA needs most of an SM's shared memory, so a count CTA waiting
     // beside it would only take its place)
@@ -1359,6 +1370,11 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     }
     KParams K = plan->base;
     const int N = K.N, G = K.G;
+    const bool masked = b->cell_mask != nullptr;
+    if (masked && (K.NS > GMAXS || plan->variant == 6))
+        return fail(PHMM_E_ARG, "cell masks need a state space of at most 60 emitting states");
+    if (masked && plan->variant >= 2 && plan->variant <= 5)
+        return fail(PHMM_E_ARG, "cell masks run on the generic (1) or two-warp (7) kernels only");
     // large state spaces (more than 64 padded slots) run on the wide kernels
     if (K.NS > GMAXS || plan->variant == 6) {
         if (F_log || B_log || post)
@@ -1381,13 +1397,13 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     if (!tables && plan->variant == 0) {
         if (estep) {
             wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
-            if (!wl) bl = find_block_launcher(K.NS);
+            if (!wl && !masked) bl = find_block_launcher(K.NS);
             split = wl != nullptr || bl != nullptr;
             two_warp = wl != nullptr;
         } else {   // forward only: the two-warp stripes where the shape has them
             wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
             two_warp = wl != nullptr;
-            if (!wl) bl = find_block_launcher(K.NS);
+            if (!wl && !masked) bl = find_block_launcher(K.NS);
         }
     }
     if (!tables && (plan->variant == 3 || plan->variant == 5)) bl = find_block_launcher(K.NS);
@@ -1582,6 +1598,7 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     K.max_ly = max_ly;
     K.spin_limit = 40LL * 1000 * 1000;
     K.wave_ctr = nullptr;
+    K.cmask = b->cell_mask;
     if (split) return launch_split(plan, K, wl ? wl : bl, bl != nullptr, n_items, n_citems, stripes, max_ly, d_items,
                                    d_counters, d_progress, d_bedge, d_bedge_exp, stream);
     for (int pass = 0; pass < (estep ? 2 : 1); ++pass) {
@@ -1652,7 +1669,8 @@ int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, 
         kern = warp2::count_warp_kernel<SH>;
     } else if (kind == 5 || kind == 6) {   // two-warp stripes: forward / backward recursion
         bytes = warp2::make_smem_tw(SH::SP, SH::KP, SH::NI, K.G, max_ly, kind == 6).bytes;
-        kern = kind == 5 ? warp2::stripe_tw_kernel<SH, false> : warp2::stripe_tw_kernel<SH, true>;
+        if (K.cmask) kern = kind == 5 ? warp2::stripe_tw_kernel<SH, false, true> : warp2::stripe_tw_kernel<SH, true, true>;
+        else kern = kind == 5 ? warp2::stripe_tw_kernel<SH, false, false> : warp2::stripe_tw_kernel<SH, true, false>;
         threads = warp2::TWT;
     } else {
         bytes = warp2::make_smem_w(SH::SP, SH::KP, SH::NI, K.G, max_ly, kind != 0, kind == 1).bytes;
@@ -1692,6 +1710,7 @@ int run_groups(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, dou
         return run(plan, b, estep, ll, n_trans, cntM, cntI, cntD, status, nullptr, nullptr, nullptr, stream);
     const int N = plan->base.N, G = plan->base.G;
     int launches = 0, p0 = 0;
+    int64_t mask_off = 0;   // cells of the pairs before p0 (the cell mask is concatenated per pair)
     float acc[3] = {0.f, 0.f, 0.f};
     bool any_bwd = false, any_count = false;
     while (p0 < b->n_pairs) {
@@ -1708,6 +1727,7 @@ int run_groups(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, dou
             g.emit_M = b->emit_M + (b->emit_per_pair ? (int64_t)p0 * G * 441 : 0);
             g.emit_I = b->emit_I + (b->emit_per_pair ? (int64_t)p0 * G * 21 : 0);
             g.emit_D = b->emit_D + (b->emit_per_pair ? (int64_t)p0 * G * 21 : 0);
+            g.cell_mask = b->cell_mask ? b->cell_mask + mask_off : nullptr;
         };
         while (lo < hi) {   // binary search on the group size
             const int mid = (lo + hi + 1) / 2;
@@ -1735,6 +1755,7 @@ int run_groups(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, dou
             any_bwd |= plan->timed_bwd;
             any_count |= plan->timed_count;
         }
+        for (int p = p0; p < p0 + lo; ++p) mask_off += (int64_t)(b->Lx_host[p] + 1) * (b->Ly_host[p] + 1);
         p0 += lo;
     }
     plan->launches = launches;
@@ -2091,6 +2112,7 @@ extern "C" int phmm_estep_static(const phmm_model_desc *md, const phmm_batch *b,
         !b->emit_M || !b->emit_I || !b->emit_D || !ll || !status || !n_trans || !cntM || !cntI || !cntD)
         return fail(PHMM_E_ARG, "null batch pointer or output");
     if (P_ > kStaticMaxPairs) return fail(PHMM_E_ARG, "phmm_estep_static: more than 4096 pairs in one call");
+    if (b->cell_mask) return fail(PHMM_E_ARG, "phmm_estep_static: cell masks are not supported (use phmm_estep)");
     // ---- device set-up, once per device (the first call on a device does it)
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));
@@ -2197,6 +2219,7 @@ extern "C" int phmm_estep_static(const phmm_model_desc *md, const phmm_batch *b,
     K.max_ly = max_ly;
     K.spin_limit = 40LL * 1000 * 1000;
     K.wave_ctr = nullptr;
+    K.cmask = nullptr;
     phmm_plan launch_ctx;   // carries the SM count for the shared launchers; owns no memory
     launch_ctx.sm_count = g_static_sms[dev];
     for (int pass = 0; pass < 2; ++pass) {

@@ -48,7 +48,8 @@ class Batch(ctypes.Structure):
                 ('emit_M', ctypes.c_void_p),
                 ('emit_I', ctypes.c_void_p),
                 ('emit_D', ctypes.c_void_p),
-                ('emit_per_pair', ctypes.c_int32)]
+                ('emit_per_pair', ctypes.c_int32),
+                ('cell_mask', ctypes.c_void_p)]
 
 
 class MixDom2Params(ctypes.Structure):
@@ -241,6 +242,7 @@ class DeviceBatch:
     emit_M: torch.Tensor        # float32 [P or 1, G, 21, 21]
     emit_I: torch.Tensor        # float32 [P or 1, G, 21]
     emit_D: torch.Tensor        # float32 [P or 1, G, 21]
+    cell_mask: torch.Tensor = None   # uint8 [sum (Lx+1)(Ly+1)]: bit 0 M, 1 I, 2 D may emit
     _struct: Batch = field(default=None, repr=False)
 
     @property
@@ -262,7 +264,8 @@ class DeviceBatch:
                 ctypes.c_void_p(self.emit_M.data_ptr()),
                 ctypes.c_void_p(self.emit_I.data_ptr()),
                 ctypes.c_void_p(self.emit_D.data_ptr()),
-                int(self.emit_M.shape[0] == P))
+                int(self.emit_M.shape[0] == P),
+                ctypes.c_void_p(self.cell_mask.data_ptr() if self.cell_mask is not None else 0))
         return self._struct
 
 
@@ -332,19 +335,31 @@ def _to_host_staged(tensors, items, dev):
     return out
 
 
-def make_batch(xs, ys, chi, emit_M, emit_I, emit_D, device='cuda'):
+def make_batch(xs, ys, chi, emit_M, emit_I, emit_D, device='cuda', cell_masks=None):
     """Build a DeviceBatch from host sequences and float tables.
 
-    chi: [P or 1, N, N]; emit_*: [P or 1, G, ...] (numpy or torch, any float)."""
+    chi: [P or 1, N, N]; emit_*: [P or 1, G, ...] (numpy or torch, any float);
+    cell_masks: optional list of per-pair uint8 arrays (Lx+1, Ly+1) (bit 0 M,
+    1 I, 2 D may emit at the cell)."""
     buf, xo, yo, Lx, Ly = pack_residues(xs, ys)
 
     def dev(a, dt):
         t = torch.as_tensor(np.asarray(a) if not isinstance(a, torch.Tensor) else a)
         return t.to(device=device, dtype=dt).contiguous()
+    cm = None
+    if cell_masks is not None:
+        if len(cell_masks) != Lx.size:
+            raise ValueError('one cell mask per pair')
+        for m, a, b in zip(cell_masks, Lx, Ly):
+            if tuple(np.shape(m)) != (int(a) + 1, int(b) + 1):
+                raise ValueError('cell mask of a pair must have shape (Lx+1, Ly+1)')
+        flat = np.concatenate([np.asarray(m, np.uint8).reshape(-1) for m in cell_masks]) if len(cell_masks) \
+            else np.zeros(1, np.uint8)
+        cm = dev(flat, torch.uint8)
     return DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo,
                        residues=dev(buf, torch.uint8), chi=dev(chi, torch.float32),
                        emit_M=dev(emit_M, torch.float32), emit_I=dev(emit_I, torch.float32),
-                       emit_D=dev(emit_D, torch.float32))
+                       emit_D=dev(emit_D, torch.float32), cell_mask=cm)
 
 
 def forward(plan, batch, stream=None):

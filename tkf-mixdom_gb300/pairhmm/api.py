@@ -93,55 +93,74 @@ def _chi_from_log(log_trans):
 def _groups_from_table(log_emit, state_types, x, y):
     """Recover per-group character tables from a (Lx+1, Ly+1, N) log
     emission table whose entries depend on the cell only through its
-    characters (true of every emission builder of the reference)."""
+    characters (true of every emission builder of the reference), up to
+    NEG_INF entries that cover every state of a type at a cell
+    (mask_emissions_match_aligned, dp/hmm.py:1085-1117, and the banded
+    recursions).  Returns (groups, EM, EI, ED, cell mask or None); the mask
+    holds bit 0 / 1 / 2 where the M / I / D states may emit."""
     st = np.asarray(state_types)
     Lx, Ly = len(x), len(y)
     em = np.exp(np.asarray(log_emit, dtype=np.float64)[:Lx + 1, :Ly + 1])
     xg = np.concatenate([[0], np.asarray(x, int)])
     yg = np.concatenate([[0], np.asarray(y, int)])
+    # per-type masks: a type is off at a cell when all its states emit 0 there
+    on = {}
+    for ty in (M, I, D):
+        ks = np.nonzero(st == ty)[0]
+        on[ty] = (em[:, :, ks] > 0).any(axis=2) if ks.size else np.ones((Lx + 1, Ly + 1), bool)
     groups = np.zeros(st.size, dtype=np.int32)
     tabs = []
-    keys = []
     for k in range(st.size):
         if st[k] not in (M, I, D):
             continue
         TM = np.ones((21, 21))
         TI = np.ones(21)
         TD = np.ones(21)
-        if st[k] == M:
-            v = em[1:, 1:, k]
-            TM[xg[1:, None], yg[None, 1:]] = v
-            ok = np.allclose(TM[xg[1:, None], yg[None, 1:]], v, rtol=1e-12, atol=0)
-        elif st[k] == I:
-            v = em[:, 1:, k]
-            TI[yg[1:]] = v[0]
-            ok = np.allclose(TI[yg[1:]][None, :], v, rtol=1e-12, atol=0)
-        else:
-            v = em[1:, :, k]
-            TD[xg[1:]] = v[:, 0]
-            ok = np.allclose(TD[xg[1:]][:, None], v, rtol=1e-12, atol=0)
-        if not ok:
-            raise NotImplementedError('log_emit_table entries must depend on the cell only '
-                                      'through its characters (per-cell tables are not supported)')
-        key = (st[k], TM.tobytes() if st[k] == M else (TI.tobytes() if st[k] == I else TD.tobytes()))
+        if st[k] == M:   # cells (i >= 1, j >= 1)
+            v, use = em[1:, 1:, k], on[M][1:, 1:]
+            ii, jj = np.nonzero(use)
+            TM[xg[ii + 1], yg[jj + 1]] = v[ii, jj]
+            got = TM[xg[1:, None], yg[None, 1:]]
+        elif st[k] == I:   # cells (i >= 0, j >= 1)
+            v, use = em[:, 1:, k], on[I][:, 1:]
+            ii, jj = np.nonzero(use)
+            TI[yg[jj + 1]] = v[ii, jj]
+            got = np.broadcast_to(TI[yg[1:]][None, :], v.shape)
+        else:   # cells (i >= 1, j >= 0)
+            v, use = em[1:, :, k], on[D][1:, :]
+            ii, jj = np.nonzero(use)
+            TD[xg[ii + 1]] = v[ii, jj]
+            got = np.broadcast_to(TD[xg[1:]][:, None], v.shape)
+        if not np.allclose(got[use], v[use], rtol=1e-12, atol=0):
+            raise NotImplementedError('log_emit_table entries must depend on the cell only through its '
+                                      'characters, up to NEG_INF over all states of a type')
         # one group per state keeps the M/I/D tables of a group independent
-        tabs.append((st[k], TM, TI, TD))
-        keys.append(key)
+        tabs.append((TM, TI, TD))
         groups[k] = len(tabs) - 1
     G = max(len(tabs), 1)
     EM = np.ones((G, 21, 21))
     EI = np.ones((G, 21))
     ED = np.ones((G, 21))
-    for g, (t, TM, TI, TD) in enumerate(tabs):
+    for g, (TM, TI, TD) in enumerate(tabs):
         EM[g], EI[g], ED[g] = TM, TI, TD
-    return groups, EM, EI, ED
+    mask = (on[M].astype(np.uint8) | (on[I].astype(np.uint8) << 1) | (on[D].astype(np.uint8) << 2))
+    # the lattice edges never use M (row/column 0), I (column 0) or D (row 0)
+    need = np.ones((Lx + 1, Ly + 1), np.uint8) * 7
+    need[0, :] &= ~np.uint8(5)
+    need[:, 0] &= ~np.uint8(3)
+    if np.all((mask & need) == need):
+        return groups, EM, EI, ED, None
+    mask[0, :] |= 5
+    mask[:, 0] |= 3
+    return groups, EM, EI, ED, mask
 
 
-def _run_single_tables(chi, st, groups, EM, EI, ED, x, y, forward_only=False):
+def _run_single_tables(chi, st, groups, EM, EI, ED, x, y, forward_only=False, cell_mask=None):
     dev = _device()
     plan = get_plan(st, groups, EM.shape[0])
     b = _lib.make_batch([x], [y], np.asarray(chi)[None], np.asarray(EM)[None],
-                        np.asarray(EI)[None], np.asarray(ED)[None], device=dev)
+                        np.asarray(EI)[None], np.asarray(ED)[None], device=dev,
+                        cell_masks=None if cell_mask is None else [cell_mask])
     out = _lib.estep_tables(plan, b, want_F=True, want_B=not forward_only,
                             want_post=not forward_only)
     Lx, Ly = len(x), len(y)
@@ -196,18 +215,105 @@ def forward_backward_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi,
     Lx = Lx_arr if real_Lx is None else int(real_Lx)
     Ly = Ly_arr if real_Ly is None else int(real_Ly)
     xr, yr = x[:Lx], y[:Ly]
+    mask = None
     if log_emit_table is not None:
-        groups, EM, EI, ED = _groups_from_table(log_emit_table, st, xr, yr)
+        groups, EM, EI, ED, mask = _groups_from_table(log_emit_table, st, xr, yr)
     else:
         groups = np.zeros(st.size, np.int32)
         EM, EI, ED = _tkf_tables(sub_matrix, pi)
     r = _run_single_tables(_chi_from_log(log_trans), st, groups, EM, EI, ED, xr, yr,
-                           forward_only=forward_only)
+                           forward_only=forward_only, cell_mask=mask)
     if forward_only:
         return r['ll']
     post = np.zeros((pad_to_bin(Lx_arr) + 1, pad_to_bin(Ly_arr) + 1, st.size))
     post[:Lx + 1, :Ly + 1] = r['post']
     return r['ll'], post, r['n_trans']
+
+
+def match_aligned_mask(Lx, Ly, match_i, match_j):
+    """Cell mask of mask_emissions_match_aligned (dp/hmm.py:1085-1117): uint8
+    (Lx+1, Ly+1) letting the M-type states emit only at the grid cells
+    (mi+1, mj+1) of the training alignment (I and D everywhere)."""
+    m = np.full((int(Lx) + 1, int(Ly) + 1), 6, np.uint8)
+    m[np.asarray(match_i, int) + 1, np.asarray(match_j, int) + 1] |= 1
+    return m
+
+
+def band_mask(Lx, Ly, band_center, band_width):
+    """Cell mask of the banded recursions (dp/hmm.py:2104-2492): uint8
+    (Lx+1, Ly+1), 7 where |j - c_i| <= W and 0 elsewhere, with
+    W = pad_to_bin(band_width) as forward_backward_2d_banded pads it."""
+    W = pad_to_bin(int(band_width))
+    c = np.asarray(band_center, int)[:int(Lx) + 1]
+    j = np.arange(int(Ly) + 1)
+    return np.where(np.abs(j[None, :] - c[:, None]) <= W, 7, 0).astype(np.uint8)
+
+
+def _to_band_layout(dense, band_center, W):
+    Lx, Ly, N = dense.shape[0] - 1, dense.shape[1] - 1, dense.shape[2]
+    Lp = pad_to_bin(Lx)
+    c = np.full(Lp + 1, Ly)
+    c[:Lx + 1] = np.asarray(band_center, int)[:Lx + 1]
+    jj = c[:, None] - W + np.arange(2 * W + 1)[None, :]                 # (Lp+1, BW)
+    ok = (jj >= 0) & (jj <= Ly) & (np.arange(Lp + 1)[:, None] <= Lx)
+    out = np.zeros((Lp + 1, 2 * W + 1, N))
+    ii, bb = np.nonzero(ok)
+    out[ii, bb] = dense[ii, jj[ii, bb]]
+    return out
+
+
+def forward_backward_2d_banded(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, band_center, band_width):
+    """(log_prob, posteriors_bands, expected_trans) -- dp/hmm.py:2395-2491.
+
+    The forward and backward recursions over the cells |j - c_i| <= W
+    (W = pad_to_bin(band_width)); posteriors in the reference's band layout
+    (pad_to_bin(Lx)+1, 2W+1, N), position (i, b) holding column c_i - W + b.
+    Runs the cell-masked E-step (cells off the band emit nothing).  For Lx
+    off a padding bin the reference's own backward starts from a terminal
+    band placed at row pad_to_bin(Lx) (dp/hmm.py:2337-2343) and its
+    posteriors and counts are not those of the banded model; these are."""
+    st = np.asarray(state_types)
+    x, y = np.asarray(x_seq), np.asarray(y_seq)
+    Lx, Ly = x.shape[0], y.shape[0]
+    W = pad_to_bin(int(band_width))
+    mask = band_mask(Lx, Ly, band_center, band_width)
+    EM, EI, ED = _tkf_tables(sub_matrix, pi)
+    r = _run_single_tables(_chi_from_log(log_trans), st, np.zeros(st.size, np.int32), EM, EI, ED, x, y,
+                           cell_mask=mask)
+    return r['ll'], _to_band_layout(r['post'], band_center, W), r['n_trans']
+
+
+def estep_batch_match_aligned(log_chi, state_types, xs, ys, match_is, match_js, sub_matrices, pis, n_dom, n_frag):
+    """Batched match-aligned MixDom E-step (train_pfam.py:1744-1800,
+    2946-2990: per-domain emissions, mask_emissions_match_aligned, the 2D
+    forward-backward and the per-domain count reductions) in one cell-masked
+    launch.
+
+    log_chi [N,N] shared or [P,N,N] per pair; sub_matrices [K,A,A] shared or
+    [P,K,A,A]; pis [K,A]; match_is / match_js: per-pair arrays of 0-based
+    aligned positions.  Returns a dict of device tensors: log_prob [P],
+    expected_trans [P,N,N], dom_match [P,K,20,20], dom_insert [P,K,20],
+    dom_delete [P,K,20], agg_match [P,20,20], status [P]."""
+    dev = _device()
+    st = np.asarray(state_types)
+    K, F = int(n_dom), int(n_frag)
+    N = st.size
+    groups = np.zeros(N, np.int32)
+    groups[2:] = np.arange(N - 2) // (5 * F)                 # domain of each body state (dp/hmm.py:820-823)
+    lc = np.asarray(log_chi.detach().cpu().numpy() if isinstance(log_chi, torch.Tensor) else log_chi, np.float64)
+    chi = _chi_from_log(lc)
+    if chi.ndim == 2:
+        chi = chi[None]
+    EM, EI, ED = pm.tables_per_domain(pm._t(sub_matrices), pm._t(pis))
+    if EM.dim() == 4:
+        EM, EI, ED = EM[None], EI[None], ED[None]
+    masks = [match_aligned_mask(len(x), len(y), mi, mj) for x, y, mi, mj in zip(xs, ys, match_is, match_js)]
+    b = _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev, cell_masks=masks)
+    out = _lib.estep(get_plan(st, groups, K), b)
+    dm = out['cnt_M'][:, :, :20, :20]
+    return {'log_prob': out['ll'], 'expected_trans': out['n_trans'], 'dom_match': dm,
+            'dom_insert': out['cnt_I'][:, :, :20], 'dom_delete': out['cnt_D'][:, :, :20],
+            'agg_match': dm.sum(dim=1), 'status': out['status']}
 
 
 # ---------------------------------------------------------------- E-steps

@@ -278,6 +278,25 @@ int phmm_viterbi(const phmm_model_desc *model, const phmm_batch *batch, const do
                  void *workspace, size_t workspace_bytes, double *ll_out, int32_t *path,
                  int32_t *path_len, int32_t *status_out, void *stream);
 
+/* Stochastic forward traceback (replaces dp/hmm.py:2043-2101
+ * sample_traceback_2d, batched over pairs and samples): the float64 log-space
+ * forward table of every pair (inputs as phmm_viterbi), then n_samples paths
+ * per pair drawn from the posterior over alignments -- the final state with
+ * probability proportional to exp(F[Lx][Ly][s] + logchi[s][E]), each
+ * predecessor state proportional to exp(F[pred][s] + logchi[s][k]).
+ * Random numbers come from a counter-based stream keyed by (seed, pair,
+ * sample, draw): the same seed gives the same paths.  Outputs: ll_out [P]
+ * (the forward log-likelihood), paths [sum_p n_samples (Lx+Ly+1)][3] int32
+ * (i, j, state) from (0, 0, S) on, sample s of pair p at triple
+ * n_samples * sum_{q<p} (Lx_q+Ly_q+1) + s (Lx_p+Ly_p+1), path_len
+ * [P][n_samples], status [P].  N <= 64.  Scratch (phmm_sample_workspace_bytes):
+ * the forward tables, (Lx+1)(Ly+1)N doubles per pair. */
+int phmm_sample_workspace_bytes(const phmm_model_desc *model, const phmm_batch *batch, size_t *bytes);
+int phmm_sample_paths(const phmm_model_desc *model, const phmm_batch *batch, const double *log_chi,
+                      const double *log_emit_M, const double *log_emit_I, const double *log_emit_D,
+                      int32_t n_samples, uint64_t seed, void *workspace, size_t workspace_bytes,
+                      double *ll_out, int32_t *paths, int32_t *path_len, int32_t *status_out, void *stream);
+
 /* TKF91 / TKF92 parameters (host float64): insertion and deletion rates,
  * fragment extension probability (0 for TKF91), the substitution rate
  * matrix Q [A][A] (rows summing to zero) and its equilibrium pi [A]; A = 20. */

@@ -26,7 +26,8 @@ EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep'
            'phmm_last_error', 'phmm_version', 'phmm_mixdom2_class_subs_count', 'phmm_mixdom2_tables',
            'phmm_mixdom2_class_counts', 'phmm_tkf92_tables', 'phmm_mixdom2_chi',
            'phmm_mixdom2_chi_vjp_dirs', 'phmm_mixdom2_chi_vjp', 'phmm_fb1d_workspace_bytes', 'phmm_fb1d',
-           'phmm_fb1d_emissions', 'phmm_viterbi_workspace_bytes', 'phmm_viterbi', 'phmm_holmes_rubin')
+           'phmm_fb1d_emissions', 'phmm_viterbi_workspace_bytes', 'phmm_viterbi', 'phmm_holmes_rubin',
+           'phmm_sample_workspace_bytes', 'phmm_sample_paths')
 
 
 class ModelDesc(ctypes.Structure):
@@ -149,6 +150,12 @@ def load(path=None):
     lib.phmm_viterbi.argtypes = [ctypes.POINTER(ModelDesc), ctypes.POINTER(Batch)] + [vp] * 4 + \
         [vp, ctypes.c_size_t, vp, vp, vp, vp, vp]
     lib.phmm_viterbi.restype = ctypes.c_int
+    lib.phmm_sample_workspace_bytes.argtypes = [ctypes.POINTER(ModelDesc), ctypes.POINTER(Batch),
+                                                ctypes.POINTER(ctypes.c_size_t)]
+    lib.phmm_sample_workspace_bytes.restype = ctypes.c_int
+    lib.phmm_sample_paths.argtypes = [ctypes.POINTER(ModelDesc), ctypes.POINTER(Batch)] + [vp] * 4 + \
+        [ctypes.c_int32, ctypes.c_uint64, vp, ctypes.c_size_t, vp, vp, vp, vp, vp]
+    lib.phmm_sample_paths.restype = ctypes.c_int
     lib.phmm_holmes_rubin.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int32, vp, vp, vp, vp, vp]
     lib.phmm_holmes_rubin.restype = ctypes.c_int
     lib.phmm_version.argtypes = []
@@ -614,6 +621,51 @@ def tkf92_tables(ins_rate, del_rate, ext, Q, pi, ts, device='cuda', stream=None)
     times ts: (chi [P,5,5] f32, EM [P,1,21,21] f32, EI [P,1,21] f32, ED
     [P,1,21] f32, sub [P,20,20] f64) device tensors."""
     return Tkf92Prologue(ins_rate, del_rate, ext, Q, pi)(ts, device=device, stream=stream)
+
+
+def sample_paths(state_types, groups, G, xs, ys, log_chi, log_M, log_I, log_D, n_samples, seed,
+                 device='cuda', stream=None):
+    """phmm_sample_paths: (ll [P] float64 numpy, paths: per pair a list of
+    n_samples [n, 3] int32 arrays of (i, j, state)).  Inputs as viterbi()."""
+    lib = load()
+    st_arr = np.ascontiguousarray(np.asarray(state_types, np.int8))
+    gr = np.ascontiguousarray(np.asarray(groups, np.int32))
+    md = ModelDesc(st_arr.size, st_arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)),
+                   gr.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), int(G))
+    buf, xo, yo, Lx, Ly = pack_residues(xs, ys)
+    P, S = Lx.size, int(n_samples)
+    f64 = lambda a: (a if isinstance(a, torch.Tensor) else torch.as_tensor(np.asarray(a))).to(
+        device=device, dtype=torch.float64).contiguous()
+    lc, lm, li, ld = f64(log_chi), f64(log_M), f64(log_I), f64(log_D)
+    if lc.dim() == 2:
+        lc = lc.unsqueeze(0)
+    res_t = torch.from_numpy(buf).to(device)
+    b = DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo, residues=res_t, chi=lc, emit_M=lm, emit_I=li, emit_D=ld)
+    bs = b.struct()
+    nb = ctypes.c_size_t(0)
+    _check(lib.phmm_sample_workspace_bytes(ctypes.byref(md), ctypes.byref(bs), ctypes.byref(nb)),
+           'phmm_sample_workspace_bytes')
+    ws = torch.empty(max(int(nb.value), 256), dtype=torch.uint8, device=device)
+    ll = torch.empty(P, dtype=torch.float64, device=device)
+    slots = (Lx.astype(np.int64) + Ly + 1)
+    paths = torch.zeros(max(int(S * slots.sum()), 1), 3, dtype=torch.int32, device=device)
+    plen = torch.zeros(max(P * S, 1), dtype=torch.int32, device=device)
+    status = torch.zeros(P, dtype=torch.int32, device=device)
+    s = stream if stream is not None else torch.cuda.current_stream(torch.device(device))
+    _check(lib.phmm_sample_paths(ctypes.byref(md), ctypes.byref(bs), _ptr(lc), _ptr(lm), _ptr(li), _ptr(ld), S,
+                                 ctypes.c_uint64(int(seed) & 0xFFFFFFFFFFFFFFFF), _ptr(ws),
+                                 ctypes.c_size_t(ws.numel()), _ptr(ll), _ptr(paths), _ptr(plen), _ptr(status),
+                                 ctypes.c_void_p(s.cuda_stream)), 'phmm_sample_paths')
+    h = to_host({'ll': ll, 'paths': paths, 'plen': plen})
+    offs = np.concatenate([[0], np.cumsum(S * slots)[:-1]])
+    out = []
+    for p in range(P):
+        one = []
+        for k in range(S):
+            o = offs[p] + k * slots[p]
+            one.append(h['paths'][o:o + h['plen'][p * S + k]])
+        out.append(one)
+    return h['ll'], out
 
 
 def holmes_rubin(class_Q, class_pis, t, class_match_counts, stream=None):

@@ -643,6 +643,41 @@ def viterbi_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi):
     return float(ll[0]), paths[0]
 
 
+def _seed_of(rng_key):
+    """A 64-bit seed from an int or an array of integers (e.g. a two-word
+    PRNG key), the words packed little end first."""
+    if isinstance(rng_key, (int, np.integer)):
+        return int(rng_key) & 0xFFFFFFFFFFFFFFFF
+    words = np.asarray(rng_key).astype(np.uint64).reshape(-1)
+    seed = 0
+    for k, w in enumerate(words[:2]):
+        seed |= (int(w) & 0xFFFFFFFF) << (32 * k)
+    return seed
+
+
+def sample_traceback_2d_batch(log_trans, state_types, xs, ys, sub_matrix, pi, n_samples, seed=0):
+    """Batched stochastic forward traceback (dp/hmm.py:2043-2101) on the
+    device: (log_prob [P] float64, paths: per pair a list of n_samples paths,
+    each a list of (i, j, state) from (0, 0, S) to (Lx, Ly, final state)),
+    drawn from the posterior over alignments.  The same seed gives the same
+    paths."""
+    lt = np.asarray(log_trans, np.float64)
+    st = np.asarray(state_types)
+    lM, lI, lD = _log_tkf_tables(sub_matrix, pi)
+    ll, paths = _lib.sample_paths(st, np.zeros(st.size, np.int32), 1, xs, ys, lt[None], lM, lI, lD,
+                                  int(n_samples), _seed_of(seed), device=_device())
+    return ll, [[[tuple(int(v) for v in row) for row in pth] for pth in per_pair] for per_pair in paths]
+
+
+def sample_traceback_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, rng_key):
+    """sample_traceback_2d (dp/hmm.py:2043-2101): (log_prob, one path sampled
+    from the posterior as a list of (i, j, state)).  rng_key: an int or an
+    integer array (a PRNG key) seeding the device stream."""
+    ll, paths = sample_traceback_2d_batch(log_trans, state_types, [np.asarray(x_seq)], [np.asarray(y_seq)],
+                                          sub_matrix, pi, 1, rng_key)
+    return float(ll[0]), paths[0][0]
+
+
 def exact_suffstats_batch(n_chi_stack, main_ins, main_del, t_array, dom_ins, dom_del, dom_weights,
                           frag_weights, ext_rates):
     """Exact MixDom2 sufficient statistics from collapsed counts

@@ -20,7 +20,7 @@ REPO_DIR = os.path.dirname(PROJECT_DIR)
 CSRC = os.path.join(PROJECT_DIR, 'csrc')
 INCLUDE = os.path.join(REPO_DIR, 'include')
 LIB_PATH = os.path.join(PKG_DIR, 'libpairhmm.so')
-SOURCES = [os.path.join(CSRC, f) for f in ('pairhmm.cu', 'prologue.cu', 'fb1d.cu', 'viterbi.cu')]
+SOURCES = [os.path.join(CSRC, f) for f in ('pairhmm.cu', 'prologue.cu', 'fb1d.cu', 'viterbi.cu', 'sample.cu')]
 OBJ_DIR = os.path.join(PKG_DIR, '_build')
 ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
 

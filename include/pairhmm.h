@@ -297,6 +297,30 @@ int phmm_sample_paths(const phmm_model_desc *model, const phmm_batch *batch, con
                       int32_t n_samples, uint64_t seed, void *workspace, size_t workspace_bytes,
                       double *ll_out, int32_t *paths, int32_t *path_len, int32_t *status_out, void *stream);
 
+/* Precompiled X/A/Y pair records (util/pair_format.py; the shards read by
+ * train_pfam.py:984-1029 once decompressed): JSON lines with the ancestor
+ * "x" and descendant "y" as letters of ACDEFGHIKLMNPQRSTVWY, the alignment
+ * "a" as M/I/D runs ("M5I1M3D2"), the time "t" and the family "fam".  A
+ * host-side reader in two passes: phmm_pairs_count gives the sizes,
+ * phmm_pairs_decode fills caller arrays -- residues in phmm_batch's layout
+ * (pair p: x at x_off[p], y at y_off[p] = x_off[p] + Lx[p]), t [P], and the
+ * alignment columns (n_cols / col_off per pair; col_state 1 M, 2 I, 3 D;
+ * col_anc / col_desc the column's characters, 20 where it has none), the
+ * family as a span of the text (fam_off = -1 without one).  A record that
+ * fails validate_record (util/pair_format.py:194-223) is PHMM_E_ARG with the
+ * line number in phmm_last_error.  Blank lines are skipped. */
+typedef struct phmm_pair_counts {
+    int32_t n_pairs;
+    int64_t n_residues;   /* sum of |x| + |y| */
+    int64_t n_columns;    /* sum of alignment columns */
+} phmm_pair_counts;
+
+int phmm_pairs_count(const char *text, size_t len, phmm_pair_counts *out);
+int phmm_pairs_decode(const char *text, size_t len, const phmm_pair_counts *sizes, int32_t *Lx, int32_t *Ly,
+                      int64_t *x_off, int64_t *y_off, uint8_t *residues, double *t, int32_t *n_cols,
+                      int64_t *col_off, int8_t *col_state, uint8_t *col_anc, uint8_t *col_desc,
+                      int64_t *fam_off, int32_t *fam_len);
+
 /* TKF91 / TKF92 parameters (host float64): insertion and deletion rates,
  * fragment extension probability (0 for TKF91), the substitution rate
  * matrix Q [A][A] (rows summing to zero) and its equilibrium pi [A]; A = 20. */

@@ -27,7 +27,7 @@ EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep'
            'phmm_mixdom2_class_counts', 'phmm_tkf92_tables', 'phmm_mixdom2_chi',
            'phmm_mixdom2_chi_vjp_dirs', 'phmm_mixdom2_chi_vjp', 'phmm_fb1d_workspace_bytes', 'phmm_fb1d',
            'phmm_fb1d_emissions', 'phmm_viterbi_workspace_bytes', 'phmm_viterbi', 'phmm_holmes_rubin',
-           'phmm_sample_workspace_bytes', 'phmm_sample_paths')
+           'phmm_sample_workspace_bytes', 'phmm_sample_paths', 'phmm_pairs_count', 'phmm_pairs_decode')
 
 
 class ModelDesc(ctypes.Structure):

@@ -3,7 +3,8 @@
 ``python -m pairhmm.build`` (or ``build()``) compiles the translation units
 of ``csrc/`` (the E-step kernels and C ABI in ``pairhmm.cu``, the device
 prologue in ``prologue.cu``, the 1D alignment-conditioned forward-backward in
-``fb1d.cu``, the Viterbi decoder in ``viterbi.cu``) in parallel with nvcc and links them into
+``fb1d.cu``, the Viterbi decoder in ``viterbi.cu``, the path sampler in
+``sample.cu``, the pair-record reader in ``pairs.cpp``) in parallel with nvcc and links them into
 ``pairhmm/libpairhmm.so`` next to this file.  The build is skipped when the
 library is newer than its sources.
 """
@@ -20,7 +21,7 @@ REPO_DIR = os.path.dirname(PROJECT_DIR)
 CSRC = os.path.join(PROJECT_DIR, 'csrc')
 INCLUDE = os.path.join(REPO_DIR, 'include')
 LIB_PATH = os.path.join(PKG_DIR, 'libpairhmm.so')
-SOURCES = [os.path.join(CSRC, f) for f in ('pairhmm.cu', 'prologue.cu', 'fb1d.cu', 'viterbi.cu', 'sample.cu')]
+SOURCES = [os.path.join(CSRC, f) for f in ('pairhmm.cu', 'prologue.cu', 'fb1d.cu', 'viterbi.cu', 'sample.cu', 'pairs.cpp')]
 OBJ_DIR = os.path.join(PKG_DIR, '_build')
 ARCH_FLAGS = ['-gencode', 'arch=compute_103a,code=sm_103a']
 

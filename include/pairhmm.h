@@ -83,6 +83,14 @@ typedef struct phmm_batch {
      * automatic choice takes these for a masked batch) and by
      * phmm_estep_tables. */
     const uint8_t *cell_mask;
+    /* > 0: beam pruning of the forward recursion (dp/hmm_beam.py:85-203):
+     * at every cell the states below the cell's maximum times
+     * exp(-beam_log_width) are set to zero, and the backward recursion then
+     * runs on the cells the pruned forward left active (hmm_beam.py:206-318;
+     * posteriors capped at 1).  0 = off.  Honoured by the generic kernels
+     * (variants 0 and 1; the automatic choice takes them for a pruned batch)
+     * and by phmm_estep_tables. */
+    double beam_log_width;
 } phmm_batch;
 
 typedef struct phmm_plan phmm_plan;

@@ -76,6 +76,21 @@ def main(ref_python):
         out[pre + 'F'] = np.asarray(F)
         out[pre + 'n_cells'] = np.int64(n_cells)
         assert lp_f == lp
+    # iterative refinement around the diagonal (hmm_beam.py:321-394)
+    Q, pi, _ = rand_Q_pi(rng)
+    t = 0.5
+    lam = 0.03
+    chi = np.asarray(cp.tkf91_trans(lam, lam * 1.2, t))
+    lt = np.log(np.maximum(chi, 1e-300))
+    st = np.array([0, 1, 2, 3, 4])
+    sub = np.asarray(ctmc.transition_matrix(Q, t))
+    x = rng.integers(0, 20, 26).astype(np.int32)
+    y = rng.integers(0, 20, 30).astype(np.int32)
+    lp, F, env = hb.iterative_beam_refinement(lt, st, x, y, sub, pi, beam_log_width=8.0, initial_band=3,
+                                              n_iterations=3, band_shrink=0.7)
+    for k, v in (('log_trans', lt), ('state_types', st), ('x', x), ('y', y), ('sub', sub), ('pi', pi),
+                 ('log_prob', np.float64(lp)), ('F', np.asarray(F)), ('envelope', env)):
+        out['refine_' + k] = v
     path = os.path.join(HERE, 'beam.npz')
     np.savez_compressed(path, **out)
     print('wrote', path, len(out), 'arrays')

@@ -1,0 +1,65 @@
+"""Beam-pruned forward-backward on the GPU (phmm_batch.beam_log_width and an
+envelope cell mask, generic kernels) against the reference's own
+dp/hmm_beam.py outputs (tests/golden/beam.npz): log-likelihood 1e-6
+relative, the pruned forward table 1e-5 where it lives (float32 DP against
+float64; the same cells live), posteriors 1e-5.  Iterative refinement
+reproduces the reference's final envelope and likelihood."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+CASES = ('tkf91_env', 'tkf91_beam', 'tkf91_both', 'mixdom_both', 'mixdom_beam')
+
+
+def _args(g, pre):
+    env = g[pre + 'envelope'] if pre + 'envelope' in g else None
+    return (g[pre + 'log_trans'], g[pre + 'state_types'], g[pre + 'x'], g[pre + 'y'], g[pre + 'sub'],
+            g[pre + 'pi'], float(g[pre + 'beam']), env)
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_beam_forward_backward_matches_reference(cuda_lib, name):
+    from pairhmm import api
+    g = load_golden('beam')
+    pre = name + '_'
+    lp, post, F = api.beam_forward_backward_2d(*_args(g, pre))
+    ref = float(g[pre + 'log_prob'])
+    assert abs(lp - ref) <= 1e-6 * abs(ref)
+    live = g[pre + 'F'] > -1e29
+    assert np.array_equal(F > -1e29, live)
+    np.testing.assert_allclose(F[live], g[pre + 'F'][live], rtol=1e-5, atol=1e-4)
+    np.testing.assert_allclose(post, g[pre + 'posteriors'], rtol=1e-5, atol=1e-6)
+    lp2, F2, n_cells = api.beam_forward_2d(*_args(g, pre))
+    assert lp2 == lp and n_cells == int(g[pre + 'n_cells'])
+
+
+def test_iterative_refinement_matches_reference(cuda_lib):
+    from pairhmm import api
+    g = load_golden('beam')
+    lp, F, env = api.iterative_beam_refinement(g['refine_log_trans'], g['refine_state_types'], g['refine_x'],
+                                               g['refine_y'], g['refine_sub'], g['refine_pi'], beam_log_width=8.0,
+                                               initial_band=3, n_iterations=3, band_shrink=0.7)
+    assert np.array_equal(env, g['refine_envelope'])
+    assert abs(lp - float(g['refine_log_prob'])) <= 1e-6 * abs(float(g['refine_log_prob']))
+
+
+def test_beam_refused_by_other_families(cuda_lib):
+    from pairhmm import api, synth, _lib
+    from oracle import dp, models as om
+    rng = np.random.default_rng(4)
+    Q, pi, _ = synth.rand_Q_pi(rng)
+    chi = om.tkf91_trans(0.03, 0.035, 0.4)
+    st = np.array([0, 1, 2, 3, 4], np.int8)
+    EM, EI, ED = dp.group_tables_tkf(om.transition_matrix(Q, 0.4), pi)
+    x, y = rng.integers(0, 20, 20), rng.integers(0, 20, 30)
+    plan = api.get_plan(st, np.zeros(5, np.int32), 1)
+    plan.set_variant(7)
+    try:
+        with pytest.raises(_lib.PairHMMError):
+            _lib.estep(plan, _lib.make_batch([x], [y], chi[None], EM, EI, ED, beam_log_width=5.0))
+    finally:
+        plan.set_variant(0)
+    out = _lib.estep(plan, _lib.make_batch([x], [y], chi[None], EM, EI, ED, beam_log_width=5.0))
+    assert plan.last_variant == 1 and int(out['status'][0]) == 0

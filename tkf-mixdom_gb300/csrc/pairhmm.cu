@@ -101,6 +101,7 @@ struct KParams {
     long long spin_limit;
     const int *wave_ctr;                // overlapped count pass: forward, backward claim counters
     const unsigned char *cmask;         // per-cell type mask (bit 0 M, 1 I, 2 D) at tab_base, or null
+    float beam_scale;                   // > 0: forward states below max * beam_scale pruned (generic kernels)
 };
 
 struct SmemLayout {
@@ -430,6 +431,11 @@ __device__ void forward_stripe(const KParams &P, int p, int si, const SmemLayout
             for (int qq = 0; qq < NQ; ++qq) mval = fmaxf(mval, mx[qq * TH + r]);
             const float *rw = raw + (4 * q) * TH + r;
             float4 v = make_float4(rw[0], rw[TH], rw[2 * TH], rw[3 * TH]);
+            if (P.beam_scale > 0.f) {   // beam: states below max * e^-width drop out (hmm_beam.py:188-195)
+                const float thr = mval * P.beam_scale;
+                v = make_float4(v.x < thr ? 0.f : v.x, v.y < thr ? 0.f : v.y, v.z < thr ? 0.f : v.z,
+                                v.w < thr ? 0.f : v.w);
+            }
             int Ecell = EXP_NONE;
             if (mval > 0.0f) {
                 int e;
@@ -717,6 +723,11 @@ __device__ void backward_stripe(const KParams &P, int p, int si, const SmemLayou
                 if (off) e4 = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (mb == 0) Ew = EXP_NONE;
             }
+            if (P.beam_scale > 0.f && fstE[(t & 1) * TH + r] <= EXP_NONE) {
+                // pruned run: a cell the forward left empty is no successor (hmm_beam.py:231, 270)
+                e4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                Ew = EXP_NONE;
+            }
             const float4 w = make_float4(b.x * e4.x, b.y * e4.y, b.z * e4.z, b.w * e4.w);
             float *rg = ring + (t % 3) * NS * TH + (4 * q) * TH + r;
             rg[0] = w.x; rg[TH] = w.y; rg[2 * TH] = w.z; rg[3 * TH] = w.w;
@@ -774,7 +785,10 @@ __device__ void backward_stripe(const KParams &P, int p, int si, const SmemLayou
                 for (int u = 0; u < 4; ++u) {
                     const int os = P.slot_orig[4 * q + u];
                     if (os < 0) continue;
-                    if (P.post) P.post[cell * N + os] = (double)f4get(post4, u);
+                    if (P.post) {
+                        const double pv = (double)f4get(post4, u);
+                        P.post[cell * N + os] = P.beam_scale > 0.f ? fmin(pv, 1.0) : pv;
+                    }
                     if (P.B_log) {
                         const float x = f4get(b, u);
                         P.B_log[cell * N + os] = (x > 0.f && Eb > EXP_NONE)
@@ -1297,6 +1311,7 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     K.spin_limit = 40LL * 1000 * 1000;
     K.wave_ctr = nullptr;
     K.cmask = nullptr;
+    K.beam_scale = 0.f;
     // ---- wavefronts, then the count pass (both on the caller's stream: a wide
     // wavefront CTA needs most of an SM's shared memory, so a count CTA waiting
     // beside it would only take its place)
@@ -1371,10 +1386,15 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     KParams K = plan->base;
     const int N = K.N, G = K.G;
     const bool masked = b->cell_mask != nullptr;
-    if (masked && (K.NS > GMAXS || plan->variant == 6))
-        return fail(PHMM_E_ARG, "cell masks need a state space of at most 60 emitting states");
+    const bool beam = b->beam_log_width > 0.0;
+    if (b->beam_log_width < 0.0 || b->beam_log_width != b->beam_log_width)
+        return fail(PHMM_E_ARG, "beam_log_width must be >= 0 (0 = no pruning)");
+    if ((masked || beam) && (K.NS > GMAXS || plan->variant == 6))
+        return fail(PHMM_E_ARG, "cell masks and beam pruning need a state space of at most 60 emitting states");
     if (masked && plan->variant >= 2 && plan->variant <= 5)
         return fail(PHMM_E_ARG, "cell masks run on the generic (1) or two-warp (7) kernels only");
+    if (beam && plan->variant >= 2)
+        return fail(PHMM_E_ARG, "beam pruning runs on the generic kernels (variant 1) only");
     // large state spaces (more than 64 padded slots) run on the wide kernels
     if (K.NS > GMAXS || plan->variant == 6) {
         if (F_log || B_log || post)
@@ -1394,7 +1414,7 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     // per 64-pair batch against 0.30 ms on the block kernels -- else the block
     // kernels
     bool two_warp = false;
-    if (!tables && plan->variant == 0) {
+    if (!tables && plan->variant == 0 && !beam) {
         if (estep) {
             wl = find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd);
             if (!wl && !masked) bl = find_block_launcher(K.NS);
@@ -1599,6 +1619,7 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     K.spin_limit = 40LL * 1000 * 1000;
     K.wave_ctr = nullptr;
     K.cmask = b->cell_mask;
+    K.beam_scale = b->beam_log_width > 0.0 ? (float)exp(-b->beam_log_width) : 0.f;
     if (split) return launch_split(plan, K, wl ? wl : bl, bl != nullptr, n_items, n_citems, stripes, max_ly, d_items,
                                    d_counters, d_progress, d_bedge, d_bedge_exp, stream);
     for (int pass = 0; pass < (estep ? 2 : 1); ++pass) {
@@ -2220,6 +2241,7 @@ extern "C" int phmm_estep_static(const phmm_model_desc *md, const phmm_batch *b,
     K.spin_limit = 40LL * 1000 * 1000;
     K.wave_ctr = nullptr;
     K.cmask = nullptr;
+    K.beam_scale = 0.f;
     phmm_plan launch_ctx;   // carries the SM count for the shared launchers; owns no memory
     launch_ctx.sm_count = g_static_sms[dev];
     for (int pass = 0; pass < 2; ++pass) {

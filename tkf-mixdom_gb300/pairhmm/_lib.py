@@ -8,7 +8,6 @@ from __future__ import annotations
 
 import ctypes
 import os
-import threading
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -50,7 +49,8 @@ class Batch(ctypes.Structure):
                 ('emit_I', ctypes.c_void_p),
                 ('emit_D', ctypes.c_void_p),
                 ('emit_per_pair', ctypes.c_int32),
-                ('cell_mask', ctypes.c_void_p)]
+                ('cell_mask', ctypes.c_void_p),
+                ('beam_log_width', ctypes.c_double)]
 
 
 class MixDom2Params(ctypes.Structure):
@@ -250,6 +250,7 @@ class DeviceBatch:
     emit_I: torch.Tensor        # float32 [P or 1, G, 21]
     emit_D: torch.Tensor        # float32 [P or 1, G, 21]
     cell_mask: torch.Tensor = None   # uint8 [sum (Lx+1)(Ly+1)]: bit 0 M, 1 I, 2 D may emit
+    beam_log_width: float = 0.0      # > 0: beam pruning of the forward (generic kernels)
     _struct: Batch = field(default=None, repr=False)
 
     @property
@@ -272,7 +273,8 @@ class DeviceBatch:
                 ctypes.c_void_p(self.emit_I.data_ptr()),
                 ctypes.c_void_p(self.emit_D.data_ptr()),
                 int(self.emit_M.shape[0] == P),
-                ctypes.c_void_p(self.cell_mask.data_ptr() if self.cell_mask is not None else 0))
+                ctypes.c_void_p(self.cell_mask.data_ptr() if self.cell_mask is not None else 0),
+                float(self.beam_log_width))
         return self._struct
 
 
@@ -302,47 +304,72 @@ def pack_residues(xs, ys):
             lens[0::2].astype(np.int32), lens[1::2].astype(np.int32))
 
 
-_STAGE = {}
-_STAGE_LOCK = threading.Lock()
-
-
 def to_host(tensors):
     """Copy a dict of device tensors to host numpy arrays with one
-    synchronisation: asynchronous copies into a reused pinned staging buffer
-    on the current stream, then one wait; the arrays returned are copies."""
+    synchronisation.  The arrays are views of one pinned block from torch's
+    caching host allocator (no host-side copy; the block returns to the cache
+    when the arrays are dropped).  Tensors that are contiguous views of one
+    device buffer (the batched E-steps' output arena) come back in a single
+    copy of that buffer; others are copied one by one into the block."""
     items = [(k, v) for k, v in tensors.items() if isinstance(v, torch.Tensor)]
     if not items:
         return dict(tensors)
     dev = items[0][1].device
     if dev.type != 'cuda':
         return {k: (v.numpy() if isinstance(v, torch.Tensor) else v) for k, v in tensors.items()}
-    with _STAGE_LOCK:
-        return _to_host_staged(tensors, items, dev)
-
-
-def _to_host_staged(tensors, items, dev):
-    sizes = [(v.numel() * v.element_size() + 255) // 256 * 256 for _, v in items]
-    total = sum(sizes)
-    buf = _STAGE.get(dev)
-    if buf is None or buf.numel() < total:
-        buf = torch.empty(max(total, 1 << 20), dtype=torch.uint8, pin_memory=True)
-        _STAGE[dev] = buf
-    views, o = {}, 0
-    for (k, v), n in zip(items, sizes):
-        nb = v.numel() * v.element_size()
-        hv = buf[o:o + nb].view(v.dtype).view(v.shape)
-        hv.copy_(v.contiguous(), non_blocking=True)
-        views[k] = hv
-        o += n
-    torch.cuda.current_stream(dev).synchronize()
-    out = {k: v.numpy().copy() for k, v in views.items()}
+    stream = torch.cuda.current_stream(dev)
+    stor = items[0][1].untyped_storage()
+    shared = all(v.device == dev and v.is_contiguous() and v.untyped_storage().data_ptr() == stor.data_ptr()
+                 for _, v in items)
+    views = {}
+    if shared:
+        nb = stor.nbytes()
+        host = torch.empty(nb, dtype=torch.uint8, pin_memory=True)
+        src = torch.empty(0, dtype=torch.uint8, device=dev).set_(stor, 0, (nb,))
+        host.copy_(src, non_blocking=True)
+        for k, v in items:
+            o = v.storage_offset() * v.element_size()
+            views[k] = host[o:o + v.numel() * v.element_size()].view(v.dtype).view(v.shape)
+    else:
+        sizes = [(v.numel() * v.element_size() + 255) // 256 * 256 for _, v in items]
+        host = torch.empty(max(sum(sizes), 1), dtype=torch.uint8, pin_memory=True)
+        o = 0
+        for (k, v), n in zip(items, sizes):
+            hv = host[o:o + v.numel() * v.element_size()].view(v.dtype).view(v.shape)
+            hv.copy_(v if v.is_contiguous() else v.contiguous(), non_blocking=True)
+            views[k] = hv
+            o += n
+    stream.synchronize()
+    out = {k: v.numpy() for k, v in views.items()}
     for k, v in tensors.items():
         if k not in out:
             out[k] = v
     return out
 
 
-def make_batch(xs, ys, chi, emit_M, emit_I, emit_D, device='cuda', cell_masks=None):
+class OutputArena:
+    """One device buffer carved into the output tensors of a call, so that
+    to_host brings them back in a single copy."""
+
+    def __init__(self, device, specs):
+        # specs: list of (name, shape, dtype); each slice 256-byte aligned
+        sizes = []
+        for _, shape, dt in specs:
+            n = int(np.prod(shape)) * torch.empty(0, dtype=dt).element_size()
+            sizes.append((n + 255) // 256 * 256)
+        self.buf = torch.empty(max(sum(sizes), 256), dtype=torch.uint8, device=device)
+        self.t, o = {}, 0
+        for (name, shape, dt), n in zip(specs, sizes):
+            cnt = int(np.prod(shape))
+            esz = torch.empty(0, dtype=dt).element_size()
+            self.t[name] = self.buf[o:o + cnt * esz].view(dt).view(*shape)
+            o += n
+
+    def __getitem__(self, name):
+        return self.t[name]
+
+
+def make_batch(xs, ys, chi, emit_M, emit_I, emit_D, device='cuda', cell_masks=None, beam_log_width=0.0):
     """Build a DeviceBatch from host sequences and float tables.
 
     chi: [P or 1, N, N]; emit_*: [P or 1, G, ...] (numpy or torch, any float);
@@ -366,7 +393,8 @@ def make_batch(xs, ys, chi, emit_M, emit_I, emit_D, device='cuda', cell_masks=No
     return DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo,
                        residues=dev(buf, torch.uint8), chi=dev(chi, torch.float32),
                        emit_M=dev(emit_M, torch.float32), emit_I=dev(emit_I, torch.float32),
-                       emit_D=dev(emit_D, torch.float32), cell_mask=cm)
+                       emit_D=dev(emit_D, torch.float32), cell_mask=cm,
+                       beam_log_width=float(beam_log_width))
 
 
 def forward(plan, batch, stream=None):
@@ -519,16 +547,19 @@ class MixDom2Prologue:
                                             _ptr(ED), _ptr(csubs), ctypes.c_void_p(s.cuda_stream)),
                'phmm_mixdom2_tables')
 
-    def class_counts(self, csubs, cnt_M, cnt_I, cnt_D, stream=None):
+    def class_count_shapes(self, P):
+        C, A = self.C, self.A
+        return {'class_match_counts': (P, C, A, A), 'class_insert_counts': (P, C, A),
+                'class_delete_counts': (P, C, A), 'classdist_counts': (P, self.K, self.F, C)}
+
+    def class_counts(self, csubs, cnt_M, cnt_I, cnt_D, stream=None, out=None):
         """phmm_mixdom2_class_counts: the per-class counts of e_step_mixdom2
         (class_match_counts [P,C,20,20], class_insert_counts / class_delete_counts
-        [P,C,20], classdist_counts [P,K,F,C]) as float64 device tensors."""
+        [P,C,20], classdist_counts [P,K,F,C]) as float64 device tensors (written
+        into `out` when given)."""
         P, dev, f64 = csubs.shape[0], csubs.device, torch.float64
-        C, A = self.C, self.A
-        out = {'class_match_counts': torch.empty(P, C, A, A, dtype=f64, device=dev),
-               'class_insert_counts': torch.empty(P, C, A, dtype=f64, device=dev),
-               'class_delete_counts': torch.empty(P, C, A, dtype=f64, device=dev),
-               'classdist_counts': torch.empty(P, self.K, self.F, C, dtype=f64, device=dev)}
+        if out is None:
+            out = {k: torch.empty(*sh, dtype=f64, device=dev) for k, sh in self.class_count_shapes(P).items()}
         s = stream if stream is not None else torch.cuda.current_stream(dev)
         _check(self.lib.phmm_mixdom2_class_counts(
             ctypes.byref(self.struct), P, _ptr(csubs), _ptr(cnt_M.contiguous()), _ptr(cnt_I.contiguous()),
@@ -668,7 +699,7 @@ def sample_paths(state_types, groups, G, xs, ys, log_chi, log_M, log_I, log_D, n
     return h['ll'], out
 
 
-def holmes_rubin(class_Q, class_pis, t, class_match_counts, stream=None):
+def holmes_rubin(class_Q, class_pis, t, class_match_counts, stream=None, out=None):
     """phmm_holmes_rubin: (W [P,C,A], U [P,C,A,A]) float64 device tensors for
     host rate matrices class_Q [C,A,A], frequencies class_pis [C,A], device
     times t [P] and device match counts [P,C,A,A]."""
@@ -682,8 +713,11 @@ def holmes_rubin(class_Q, class_pis, t, class_match_counts, stream=None):
     mc = class_match_counts.to(torch.float64).contiguous()
     P = mc.shape[0]
     tt = t.to(device=mc.device, dtype=torch.float64).reshape(-1).contiguous()
-    W = torch.empty(P, C, A, dtype=torch.float64, device=mc.device)
-    U = torch.empty(P, C, A, A, dtype=torch.float64, device=mc.device)
+    if out is not None:
+        W, U = out
+    else:
+        W = torch.empty(P, C, A, dtype=torch.float64, device=mc.device)
+        U = torch.empty(P, C, A, A, dtype=torch.float64, device=mc.device)
     s = stream if stream is not None else torch.cuda.current_stream(mc.device)
     _check(lib.phmm_holmes_rubin(C, A, Q.ctypes.data, pis.ctypes.data, P, _ptr(tt), _ptr(mc), _ptr(W), _ptr(U),
                                  ctypes.c_void_p(s.cuda_stream)), 'phmm_holmes_rubin')

@@ -155,12 +155,12 @@ def _groups_from_table(log_emit, state_types, x, y):
     return groups, EM, EI, ED, mask
 
 
-def _run_single_tables(chi, st, groups, EM, EI, ED, x, y, forward_only=False, cell_mask=None):
+def _run_single_tables(chi, st, groups, EM, EI, ED, x, y, forward_only=False, cell_mask=None, beam=0.0):
     dev = _device()
     plan = get_plan(st, groups, EM.shape[0])
     b = _lib.make_batch([x], [y], np.asarray(chi)[None], np.asarray(EM)[None],
                         np.asarray(EI)[None], np.asarray(ED)[None], device=dev,
-                        cell_masks=None if cell_mask is None else [cell_mask])
+                        cell_masks=None if cell_mask is None else [cell_mask], beam_log_width=beam)
     out = _lib.estep_tables(plan, b, want_F=True, want_B=not forward_only,
                             want_post=not forward_only)
     Lx, Ly = len(x), len(y)
@@ -281,6 +281,107 @@ def forward_backward_2d_banded(log_trans, state_types, x_seq, y_seq, sub_matrix,
     r = _run_single_tables(_chi_from_log(log_trans), st, np.zeros(st.size, np.int32), EM, EI, ED, x, y,
                            cell_mask=mask)
     return r['ll'], _to_band_layout(r['post'], band_center, W), r['n_trans']
+
+
+def msa_to_envelope(x_len, y_len, msa_x_row, msa_y_row, band_width, gap_token=-1):
+    """dp/hmm_beam.py:22-82: (x_len+1, y_len+1) bool envelope of the cells
+    whose j lies within band_width of the y range of the guide points with i
+    within band_width; (0, 0) and (x_len, y_len) always included."""
+    pts = [(0, 0)]
+    xi = yj = 0
+    for a, b in zip(np.asarray(msa_x_row), np.asarray(msa_y_row)):
+        xi += int(a) != gap_token
+        yj += int(b) != gap_token
+        pts.append((xi, yj))
+    pts.append((x_len, y_len))
+    pts = np.asarray(pts)
+    i = np.arange(x_len + 1)
+    near = np.abs(pts[None, :, 0] - i[:, None]) <= band_width               # (x_len+1, n_points)
+    lo = np.where(near, pts[None, :, 1], y_len).min(axis=1)
+    hi = np.where(near, pts[None, :, 1], 0).max(axis=1)
+    j = np.arange(y_len + 1)
+    env = (j[None, :] >= np.maximum(0, lo - band_width)[:, None]) & (j[None, :] <= np.minimum(y_len, hi + band_width)[:, None])
+    env[0, 0] = True
+    env[x_len, y_len] = True
+    return env
+
+
+def _beam_run(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, beam_log_width, envelope, forward_only):
+    st = np.asarray(state_types)
+    x, y = np.asarray(x_seq), np.asarray(y_seq)
+    w = float(beam_log_width)
+    beam = w if np.isfinite(w) else 0.0
+    if np.isfinite(w) and w <= 0:
+        raise ValueError('beam_log_width must be positive (np.inf for no pruning)')
+    mask = None
+    if envelope is not None:
+        env = np.asarray(envelope, bool)
+        mask = np.where(env, 7, 0).astype(np.uint8)
+        mask[0, 0] = 7                    # the start is never pruned (hmm_beam.py:122)
+    # the beam module's emissions: log max(pi, 1e-30), log max(P, 1e-30)
+    EM, EI, ED = pm.tables_per_domain(pm._t(np.asarray(sub_matrix, float))[None], pm._t(np.asarray(pi, float))[None])
+    r = _run_single_tables(_chi_from_log(log_trans), st, np.zeros(st.size, np.int32), EM.numpy(), EI.numpy(),
+                           ED.numpy(), x, y, forward_only=forward_only, cell_mask=mask, beam=beam)
+    n_cells = int(np.count_nonzero(envelope)) - 1 if envelope is not None else (x.size + 1) * (y.size + 1) - 1
+    return r, n_cells
+
+
+def beam_forward_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, beam_log_width=np.inf, envelope=None):
+    """(log_prob, F (Lx+1, Ly+1, N) log forward table, cells computed) --
+    dp/hmm_beam.py:85-203: the forward restricted to the envelope with every
+    state below its cell's maximum minus beam_log_width pruned."""
+    r, n_cells = _beam_run(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, beam_log_width, envelope, True)
+    return r['ll'], r['F'], n_cells
+
+
+def beam_forward_backward_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, beam_log_width=np.inf,
+                             envelope=None):
+    """(log_prob, posteriors (Lx+1, Ly+1, N), F) -- dp/hmm_beam.py:206-318:
+    the pruned forward, the backward on the cells it left active, posteriors
+    capped at 1 and 0 off the active cells."""
+    r, _ = _beam_run(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, beam_log_width, envelope, False)
+    if not r['ll'] > -1e29:
+        return r['ll'], np.zeros_like(r['F']), r['F']
+    # the reference caps the posteriors at 1 and leaves the origin out of its
+    # backward sweep (anti-diagonals Lx+Ly .. 1), so its posterior there is 0
+    post = np.minimum(r['post'], 1.0)
+    post[0, 0, :] = 0.0
+    return r['ll'], post, r['F']
+
+
+def iterative_beam_refinement(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, beam_log_width=10.0,
+                              initial_band=5, n_iterations=3, band_shrink=0.7):
+    """dp/hmm_beam.py:321-394: beam forwards over a diagonal band that widens
+    (x2) while the likelihood is empty and otherwise shrinks (x band_shrink,
+    at least 2) around the previous run's active cells.  Returns (log_prob, F,
+    envelope)."""
+    Lx, Ly = len(x_seq), len(y_seq)
+
+    def diagonal(band):
+        c = np.rint(np.arange(Lx + 1) * Ly / max(Lx, 1)).astype(int)
+        j = np.arange(Ly + 1)
+        return (j[None, :] >= np.maximum(0, c - band)[:, None]) & (j[None, :] <= np.minimum(Ly, c + band)[:, None])
+    band = initial_band
+    env = diagonal(band)
+    lp, F = -1e30, None
+    for it in range(n_iterations):
+        lp, F, _ = beam_forward_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, beam_log_width, env)
+        if not lp > -1e30 + 100:
+            band = int(band * 2)
+            env = diagonal(band)
+            continue
+        if it < n_iterations - 1:
+            active = np.any(F > -1e30 + 100, axis=2)
+            nb = max(2, int(band * band_shrink))
+            ii, jj = np.nonzero(active)
+            acc = np.zeros((Lx + 2, Ly + 2), np.int64)   # 2D difference array of the dilated boxes
+            np.add.at(acc, (np.maximum(ii - nb, 0), np.maximum(jj - nb, 0)), 1)
+            np.add.at(acc, (np.minimum(ii + nb, Lx) + 1, np.maximum(jj - nb, 0)), -1)
+            np.add.at(acc, (np.maximum(ii - nb, 0), np.minimum(jj + nb, Ly) + 1), -1)
+            np.add.at(acc, (np.minimum(ii + nb, Lx) + 1, np.minimum(jj + nb, Ly) + 1), 1)
+            env = acc.cumsum(axis=0).cumsum(axis=1)[:Lx + 1, :Ly + 1] > 0
+            band = nb
+    return lp, F, env
 
 
 def estep_batch_match_aligned(log_chi, state_types, xs, ys, match_is, match_js, sub_matrices, pis, n_dom, n_frag):
@@ -416,7 +517,7 @@ def holmes_rubin_weighted_stats(Q, pi, t, mc):
     return W[0, 0].cpu(), U[0, 0].cpu()
 
 
-def holmes_rubin_batch(class_S_exch, class_pis, ts, class_match_counts):
+def holmes_rubin_batch(class_S_exch, class_pis, ts, class_match_counts, out=None):
     """Batched Holmes-Rubin statistics (core/ctmc.py:173-230, 285-326) for
     per-pair times ts [P] and per-pair per-class match counts [P, C, A, A]:
     W [P, C, A] (expected dwell times) and U [P, C, A, A] (expected
@@ -433,7 +534,7 @@ def holmes_rubin_batch(class_S_exch, class_pis, ts, class_match_counts):
         np.fill_diagonal(Q[c], 0.0)
         np.fill_diagonal(Q[c], -Q[c].sum(axis=1))
     t = ts if isinstance(ts, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(np.asarray(ts, np.float64)))
-    return _lib.holmes_rubin(Q, pis, t.to(mc.device), mc)
+    return _lib.holmes_rubin(Q, pis, t.to(mc.device), mc, out=out)
 
 
 def _mixdom2_tables(params, ts, device):
@@ -705,16 +806,30 @@ def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True, exact_suffst
     K, F = pro.K, pro.F
     plan = get_plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)
     b = _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev)
-    out = _lib.estep(plan, b)
+    # every output in one device buffer: one copy brings them all to the host
+    P, N, G, C, A = b.n_pairs, 2 + 5 * K * F, K * F, pro.C, pro.A
+    f64 = torch.float64
+    specs = [('ll', (P,), f64), ('n_trans', (P, N, N), f64), ('cnt_M', (P, G, 21, 21), f64),
+             ('cnt_I', (P, G, 21), f64), ('cnt_D', (P, G, 21), f64), ('status', (P,), torch.int32)]
+    use_arena = with_class_counts and C <= 8
+    if use_arena:
+        specs += [(k, sh, f64) for k, sh in pro.class_count_shapes(P).items()]
+        specs += [('class_W', (P, C, A), f64), ('class_U', (P, C, A, A), f64)]
+    ar = _lib.OutputArena(dev, specs)
+    out = _lib.estep(plan, b, out={k: ar[k] for k in ('ll', 'n_trans', 'cnt_M', 'cnt_I', 'cnt_D', 'status')})
     res = {'log_p': out['ll'], 'n_trans': out['n_trans'], 'cnt_M': out['cnt_M'],
            'cnt_I': out['cnt_I'], 'cnt_D': out['cnt_D'], 'status': out['status']}
     if with_class_counts:
-        if pro.C <= 8:
-            res.update(pro.class_counts(csubs, out['cnt_M'], out['cnt_I'], out['cnt_D']))
+        if use_arena:
+            res.update(pro.class_counts(csubs, out['cnt_M'], out['cnt_I'], out['cnt_D'],
+                                        out={k: ar[k] for k in pro.class_count_shapes(P)}))
+            W, U = holmes_rubin_batch(params['class_S_exch'], params['class_pis'], t_dev,
+                                      res['class_match_counts'], out=(ar['class_W'], ar['class_U']))
         else:
             res.update(class_split(params, out['cnt_M'], out['cnt_I'], out['cnt_D'], csubs=csubs))
-        res['class_W'], res['class_U'] = holmes_rubin_batch(params['class_S_exch'], params['class_pis'], t_dev,
-                                                            res['class_match_counts'])
+            W, U = holmes_rubin_batch(params['class_S_exch'], params['class_pis'], t_dev,
+                                      res['class_match_counts'])
+        res['class_W'], res['class_U'] = W, U
     if exact_suffstats:
         res['suffstats'] = exact_suffstats_batch(out['n_trans'], params['main_ins'], params['main_del'], ts,
                                                  params['dom_ins'], params['dom_del'], params['dom_weights'],

@@ -15,7 +15,10 @@ Restates ``dp/hmm_beam.py`` in NumPy float64, log space:
   * ``beam_forward_backward_2d`` (hmm_beam.py:206-318): the backward only on
     cells the pruned forward left active (any state above NEG_INF + 100),
     from active successors, for every state of the cell; posteriors
-    exp(min(F + B - log P, 0)) on active cells, 0 elsewhere.
+    exp(min(F + B - log P, 0)) on active cells, 0 elsewhere;
+  * ``beam_viterbi_2d`` (hmm_beam.py:397-490): the Viterbi recursion on the
+    envelope, a state whose cell or predecessor cell lies outside keeping
+    NEG_INF and the pointer (0, 0, S).
 
 Pinned against ``tests/golden/beam.npz`` (the reference's own outputs,
 ``tests/golden/make_golden_beam.py``).
@@ -138,3 +141,43 @@ def beam_forward_backward(log_trans, state_types, x, y, sub, pi, beam_log_width=
     post = np.zeros_like(F)
     post[active] = np.exp(np.minimum(F[active] + B[active] - lp, 0.0))
     return lp, post, F
+
+
+def beam_viterbi(log_trans, state_types, x, y, sub, pi, envelope=None):
+    """(log P of the best path, path [(i, j, state), ...]) of beam_viterbi_2d
+    (hmm_beam.py:397-490): a state whose cell or predecessor cell is outside
+    the envelope keeps NEG_INF and the pointer (0, 0, S); first maximum wins."""
+    lt = np.asarray(log_trans, float)
+    st = np.asarray(state_types)
+    em = _emission_table(st, x, y, sub, pi)
+    Lx, Ly, N = em.shape[0] - 1, em.shape[1] - 1, st.size
+    V = np.full((Lx + 1, Ly + 1, N), NEG_INF)
+    V[0, 0, 0] = 0.0
+    TB = np.zeros((Lx + 1, Ly + 1, N, 3), np.int64)
+    step = {M: (1, 1), I: (0, 1), D: (1, 0)}
+    for d in range(1, Lx + Ly + 1):
+        for i in range(max(0, d - Ly), min(d, Lx) + 1):
+            j = d - i
+            if envelope is not None and not envelope[i, j]:
+                continue
+            for k in range(N):
+                if st[k] not in step:
+                    continue
+                pi_, pj_ = i - step[st[k]][0], j - step[st[k]][1]
+                if pi_ < 0 or pj_ < 0:
+                    continue
+                if envelope is not None and not envelope[pi_, pj_]:
+                    continue
+                sc = V[pi_, pj_] + lt[:, k]
+                b = int(np.argmax(sc))
+                V[i, j, k] = sc[b] + em[i, j, k]
+                TB[i, j, k] = (pi_, pj_, b)
+    e_idx = int(np.argmax(st == E))
+    fs = V[Lx, Ly] + lt[:, e_idx]
+    ck = int(np.argmax(fs))
+    path, ci, cj = [], Lx, Ly
+    while ci > 0 or cj > 0:
+        path.append((ci, cj, ck))
+        ci, cj, ck = (int(v) for v in TB[ci, cj, ck])
+    path.append((0, 0, 0))
+    return float(fs[int(np.argmax(fs))]), path[::-1]

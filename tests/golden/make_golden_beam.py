@@ -62,6 +62,9 @@ def main(ref_python):
             out[pre + 'msa_y'] = my
             out[pre + 'band_width'] = np.int64(bw)
             out[pre + 'envelope'] = env
+        vlp, vpath = hb.beam_viterbi_2d(lt, st, x, y, sub, pi, env)
+        out[pre + 'viterbi_log_prob'] = np.float64(vlp)
+        out[pre + 'viterbi_path'] = np.asarray(vpath, np.int64)
         lp_f, F_f, n_cells = hb.beam_forward_2d(lt, st, x, y, sub, pi, beam, env)
         lp, post, F = hb.beam_forward_backward_2d(lt, st, x, y, sub, pi, beam, env)
         out[pre + 'log_trans'] = lt

@@ -29,3 +29,15 @@ def test_beam_oracle_matches_reference(name):
     assert np.array_equal(live, F > -1e29)
     np.testing.assert_allclose(F[live], g[pre + 'F'][live], rtol=1e-12, atol=1e-10)
     np.testing.assert_allclose(post, g[pre + 'posteriors'], rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_beam_viterbi_oracle_matches_reference(name):
+    from oracle import beam
+    g = load_golden('beam')
+    pre = name + '_'
+    env = g[pre + 'envelope'] if pre + 'envelope' in g else None
+    lp, path = beam.beam_viterbi(g[pre + 'log_trans'], g[pre + 'state_types'], g[pre + 'x'], g[pre + 'y'],
+                                 g[pre + 'sub'], g[pre + 'pi'], env)
+    assert lp == float(g[pre + 'viterbi_log_prob'])
+    assert np.array_equal(np.asarray(path), g[pre + 'viterbi_path'])

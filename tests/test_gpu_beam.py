@@ -63,3 +63,18 @@ def test_beam_refused_by_other_families(cuda_lib):
         plan.set_variant(0)
     out = _lib.estep(plan, _lib.make_batch([x], [y], chi[None], EM, EI, ED, beam_log_width=5.0))
     assert plan.last_variant == 1 and int(out['status'][0]) == 0
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_beam_viterbi_matches_reference(cuda_lib, name):
+    """Envelope-constrained Viterbi (float64 on the device): the reference's
+    best path and its log-probability to 1e-12."""
+    from pairhmm import api
+    g = load_golden('beam')
+    pre = name + '_'
+    env = g[pre + 'envelope'] if pre + 'envelope' in g else None
+    lp, path = api.beam_viterbi_2d(g[pre + 'log_trans'], g[pre + 'state_types'], g[pre + 'x'], g[pre + 'y'],
+                                   g[pre + 'sub'], g[pre + 'pi'], env)
+    ref = float(g[pre + 'viterbi_log_prob'])
+    assert abs(lp - ref) <= 1e-12 * abs(ref)
+    assert np.array_equal(np.asarray(path), g[pre + 'viterbi_path'])

@@ -28,9 +28,13 @@ constexpr double NEG = -1e30;   // the reference's NEG_INF (dp/hmm.py:108)
 constexpr int TS = 0, TM = 1, TI = 2, TD = 3;
 
 struct Meta {
-    int64_t x_off, y_off, tb_off, diag_off, path_off;
+    int64_t x_off, y_off, tb_off, diag_off, path_off, mask_off;
     int32_t Lx, Ly;
 };
+
+// Backpointer of a state the envelope left out (hmm_beam.py:455-476 stores
+// the triple (0, 0, S) there): the traceback jumps to the origin.
+constexpr uint8_t BP_ORIGIN = 255;
 
 struct Desc {
     int N, G, e_idx, s_idx;
@@ -43,7 +47,8 @@ viterbi_kernel(const __grid_constant__ Desc d, const Meta *__restrict__ meta, co
                const double *__restrict__ lchi_all, int chi_pp, const double *__restrict__ lM,
                const double *__restrict__ lI, const double *__restrict__ lD, int emit_pp,
                double *__restrict__ diag, uint8_t *__restrict__ tb, double *__restrict__ ll_out,
-               int32_t *__restrict__ path, int32_t *__restrict__ path_len, int32_t *__restrict__ status) {
+               int32_t *__restrict__ path, int32_t *__restrict__ path_len, int32_t *__restrict__ status,
+               const uint8_t *__restrict__ env) {
     extern __shared__ double lchi[];   // [N][N]
     const int p = blockIdx.x, tid = threadIdx.x;
     const Meta m = meta[p];
@@ -74,9 +79,18 @@ viterbi_kernel(const __grid_constant__ Desc d, const Meta *__restrict__ meta, co
             }
             const int st = d.type[k];
             const double *pred = nullptr;
-            if (st == TM && i > 0 && j > 0) pred = d2 + (i - 1) * N;
-            else if (st == TI && j > 0) pred = d1 + i * N;
-            else if (st == TD && i > 0) pred = d1 + (i - 1) * N;
+            int pi_ = -1, pj_ = -1;
+            if (st == TM && i > 0 && j > 0) { pred = d2 + (i - 1) * N; pi_ = i - 1; pj_ = j - 1; }
+            else if (st == TI && j > 0) { pred = d1 + i * N; pi_ = i; pj_ = j - 1; }
+            else if (st == TD && i > 0) { pred = d1 + (i - 1) * N; pi_ = i - 1; pj_ = j; }
+            if (env) {   // envelope (beam_viterbi_2d): the cell and its predecessor must lie inside
+                const uint8_t *ep = env + m.mask_off;
+                if (!ep[cell] || (pred && !ep[(int64_t)pi_ * (Ly + 1) + pj_])) {
+                    cur[i * N + k] = NEG;
+                    bp[cell * N + k] = BP_ORIGIN;
+                    continue;
+                }
+            }
             if (!pred) {
                 cur[i * N + k] = NEG;
                 bp[cell * N + k] = 0;
@@ -119,10 +133,13 @@ viterbi_kernel(const __grid_constant__ Desc d, const Meta *__restrict__ meta, co
             ++n;
             const int st = d.type[ck];
             const int nk = bp[((int64_t)ci * (Ly + 1) + cj) * N + ck];
-            if (st == TM) { --ci; --cj; }
-            else if (st == TI) { --cj; }
-            else if (st == TD) { --ci; }
-            else { ci = 0; cj = 0; }   // a cell the reference left at zero pointers
+            if (nk == BP_ORIGIN) { ci = 0; cj = 0; ck = d.s_idx; break; }
+            // a state with no predecessor cell here (S/E, or M/I/D on the lattice
+            // edge) kept the reference's zero pointers: the walk ends at the origin
+            if (st == TM && ci > 0 && cj > 0) { --ci; --cj; }
+            else if (st == TI && cj > 0) { --cj; }
+            else if (st == TD && ci > 0) { --ci; }
+            else { ci = 0; cj = 0; }
             ck = nk;
         }
         pp[3 * n] = 0; pp[3 * n + 1] = 0; pp[3 * n + 2] = d.s_idx;
@@ -154,11 +171,12 @@ struct VitLayout {
 static int vit_layout(const phmm_batch *b, int N, VitLayout &L) {
     const int P = b->n_pairs;
     L.meta.resize(P);
-    int64_t tb = 0, dg = 0, pth = 0;
+    int64_t tb = 0, dg = 0, pth = 0, mk = 0;
     for (int p = 0; p < P; ++p) {
         const int Lx = b->Lx_host[p], Ly = b->Ly_host[p];
         if (Lx < 0 || Ly < 0) return vit_fail(PHMM_E_ARG, "phmm_viterbi: negative length");
-        L.meta[p] = vit::Meta{b->x_off_host[p], b->y_off_host[p], tb, dg, pth, Lx, Ly};
+        L.meta[p] = vit::Meta{b->x_off_host[p], b->y_off_host[p], tb, dg, pth, mk, Lx, Ly};
+        mk += (int64_t)(Lx + 1) * (Ly + 1);
         tb += (int64_t)(Lx + 1) * (Ly + 1) * N;
         dg += 3 * (int64_t)(Lx + 1) * N;
         pth += Lx + Ly + 1;
@@ -226,7 +244,7 @@ extern "C" int phmm_viterbi(const phmm_model_desc *model, const phmm_batch *batc
     viterbi_kernel<<<P, NT, smem, st>>>(d, (const Meta *)ws, batch->residues, log_chi, batch->chi_per_pair,
                                        log_emit_M, log_emit_I, log_emit_D, batch->emit_per_pair,
                                        (double *)(ws + L.o_diag), (uint8_t *)(ws + L.o_tb), ll_out, path, path_len,
-                                       status_out);
+                                       status_out, batch->cell_mask);
     e = cudaGetLastError();
     if (e != cudaSuccess) return vit_fail(PHMM_E_CUDA, cudaGetErrorString(e));
     return PHMM_OK;

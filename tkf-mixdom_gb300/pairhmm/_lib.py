@@ -774,10 +774,12 @@ def fb1d_emissions(state_types, groups, G, L, off, cols, anc, desc, emit_M, emit
     return out, status
 
 
-def viterbi(state_types, groups, G, xs, ys, log_chi, log_M, log_I, log_D, device='cuda', stream=None):
+def viterbi(state_types, groups, G, xs, ys, log_chi, log_M, log_I, log_D, device='cuda', stream=None,
+            envelopes=None):
     """phmm_viterbi: (ll [P] float64 numpy, paths: list of [n_p, 3] int32 arrays of
     (i, j, state)).  log_chi [P or 1, N, N] and the per-group log tables
-    [P or 1, G, ...] are float64 (torch or numpy)."""
+    [P or 1, G, ...] are float64 (torch or numpy); envelopes: optional per-pair
+    (Lx+1, Ly+1) boolean arrays (beam_viterbi_2d's band constraint)."""
     lib = load()
     st_arr = np.ascontiguousarray(np.asarray(state_types, np.int8))
     gr = np.ascontiguousarray(np.asarray(groups, np.int32))
@@ -791,7 +793,12 @@ def viterbi(state_types, groups, G, xs, ys, log_chi, log_M, log_I, log_D, device
     if lc.dim() == 2:
         lc = lc.unsqueeze(0)
     res_t = torch.from_numpy(buf).to(device)
-    b = DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo, residues=res_t, chi=lc, emit_M=lm, emit_I=li, emit_D=ld)
+    env = None
+    if envelopes is not None:
+        env = torch.from_numpy(np.concatenate([np.asarray(e, bool).reshape(-1) for e in envelopes]).astype(
+            np.uint8)).to(device)
+    b = DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo, residues=res_t, chi=lc, emit_M=lm, emit_I=li, emit_D=ld,
+                    cell_mask=env)
     bs = b.struct()
     nb = ctypes.c_size_t(0)
     _check(lib.phmm_viterbi_workspace_bytes(ctypes.byref(md), ctypes.byref(bs), ctypes.byref(nb)),

@@ -384,6 +384,31 @@ def iterative_beam_refinement(log_trans, state_types, x_seq, y_seq, sub_matrix, 
     return lp, F, env
 
 
+def beam_viterbi_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, envelope=None):
+    """(log_prob, path as a list of (i, j, state)) -- dp/hmm_beam.py:397-490:
+    the Viterbi recursion restricted to the envelope (a state whose cell or
+    predecessor cell lies outside keeps NEG_INF and a pointer to the origin),
+    emissions log max(pi, 1e-30) and log max(P, 1e-30)."""
+    st = np.asarray(state_types)
+    x, y = np.asarray(x_seq), np.asarray(y_seq)
+    sub = np.asarray(sub_matrix, np.float64)
+    p_ = np.asarray(pi, np.float64)
+    A = p_.size
+    lp = np.zeros(21)
+    lp[:A] = np.log(np.maximum(p_, 1e-30))
+    lM = np.zeros((21, 21))
+    lM[:A, :A] = lp[:A, None] + np.log(np.maximum(sub, 1e-30))
+    lM[:A, A:] = lp[:A, None]
+    env = None
+    if envelope is not None:
+        env = [np.asarray(envelope, bool)]
+        if env[0].shape != (x.size + 1, y.size + 1):
+            raise ValueError('envelope must have shape (Lx+1, Ly+1)')
+    ll, paths = _lib.viterbi(st, np.zeros(st.size, np.int32), 1, [x], [y], np.asarray(log_trans, np.float64)[None],
+                             lM[None, None], lp[None, None], lp[None, None], device=_device(), envelopes=env)
+    return float(ll[0]), [tuple(int(v) for v in row) for row in paths[0]]
+
+
 def estep_batch_match_aligned(log_chi, state_types, xs, ys, match_is, match_js, sub_matrices, pis, n_dom, n_frag):
     """Batched match-aligned MixDom E-step (train_pfam.py:1744-1800,
     2946-2990: per-domain emissions, mask_emissions_match_aligned, the 2D

@@ -86,3 +86,32 @@ def test_holmes_rubin_rejects_bad_arguments(lib):
     assert lib.phmm_holmes_rubin(1, 4, Q.ctypes.data, pi.ctypes.data, 3, null, null, null, null, null) == -1
     assert 'null device buffer' in _lib.last_error()
     assert lib.phmm_holmes_rubin(1, 4, Q.ctypes.data, pi.ctypes.data, 0, null, null, null, null, null) == 0
+
+
+def test_sample_paths_rejects_bad_arguments(lib):
+    """phmm_sample_paths checks its arguments before any CUDA call."""
+    import ctypes
+    import numpy as np
+    from pairhmm import _lib
+    st = (ctypes.c_int8 * 5)(0, 1, 2, 3, 4)
+    gr = (ctypes.c_int32 * 5)(0, 0, 0, 0, 0)
+    desc = _lib.ModelDesc(5, st, gr, 1)
+    Lx = np.array([3], np.int32)
+    Ly = np.array([4], np.int32)
+    off = np.array([0], np.int64)
+    b = _lib.Batch(1, Lx.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), Ly.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                   None, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                   off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), None, 0, None, None, None, 0, None, 0.0)
+    null = ctypes.c_void_p(0)
+    args = [null] * 4 + [8, 1, null, 0, null, null, null, null, null]
+    assert lib.phmm_sample_paths(ctypes.byref(desc), ctypes.byref(b), *args) == -1
+    assert 'null pointer' in _lib.last_error()
+    bad = [null] * 4 + [-1, 1, null, 0, null, null, null, null, null]
+    assert lib.phmm_sample_paths(ctypes.byref(desc), ctypes.byref(b), *bad) == -1
+    assert 'negative' in _lib.last_error()
+    big = _lib.ModelDesc(70, (ctypes.c_int8 * 70)(*([0] + [1] * 68 + [4])), (ctypes.c_int32 * 70)(), 1)
+    assert lib.phmm_sample_paths(ctypes.byref(big), ctypes.byref(b), *args) == -1
+    assert '2..64' in _lib.last_error()
+    nb = ctypes.c_size_t(0)
+    assert lib.phmm_sample_workspace_bytes(ctypes.byref(desc), ctypes.byref(b), ctypes.byref(nb)) == 0
+    assert nb.value >= 4 * 5 * 5 * 8

@@ -80,8 +80,9 @@ typedef struct phmm_batch {
      * (dp/hmm.py:1085-1117: bit 0 only at the alignment's match cells) and
      * the banded recursions (dp/hmm.py:2104-2492: zero bytes off the band).
      * Honoured by the generic and two-warp kernels (variants 0, 1, 7; the
-     * automatic choice takes these for a masked batch) and by
-     * phmm_estep_tables. */
+     * automatic choice takes these for a masked batch), by
+     * phmm_estep_tables, and by phmm_viterbi as an envelope (nonzero =
+     * inside). */
     const uint8_t *cell_mask;
     /* > 0: beam pruning of the forward recursion (dp/hmm_beam.py:85-203):
      * at every cell the states below the cell's maximum times
@@ -278,6 +279,9 @@ int phmm_fb1d_emissions(const phmm_model_desc *model, int32_t n_pairs, const int
  * path [sum_p (Lx+Ly+1)][3] int32 (i, j, state) triples from (0, 0, S) to
  * (Lx, Ly, best final state), pair p's block starting at sum_{q<p}
  * (Lx_q+Ly_q+1), path_len [P] (entries used), status [P].  N <= 64.
+ * With the batch's cell_mask set, a nonzero byte marks a cell inside the
+ * envelope of beam_viterbi_2d (dp/hmm_beam.py:397-490): a state whose cell
+ * or predecessor cell lies outside keeps NEG_INF and points to the origin.
  * Scratch from the caller's workspace (phmm_viterbi_workspace_bytes:
  * three diagonals and one backpointer byte per cell and state). */
 int phmm_viterbi_workspace_bytes(const phmm_model_desc *model, const phmm_batch *batch, size_t *bytes);

@@ -115,3 +115,24 @@ def test_sample_paths_rejects_bad_arguments(lib):
     nb = ctypes.c_size_t(0)
     assert lib.phmm_sample_workspace_bytes(ctypes.byref(desc), ctypes.byref(b), ctypes.byref(nb)) == 0
     assert nb.value >= 4 * 5 * 5 * 8
+
+
+def test_static_estep_refuses_masks_and_beam(lib):
+    """phmm_estep_static has no cell-mask or beam support and says so before
+    any CUDA call."""
+    import ctypes
+    import numpy as np
+    from pairhmm import _lib
+    st = (ctypes.c_int8 * 5)(0, 1, 2, 3, 4)
+    gr = (ctypes.c_int32 * 5)(0, 0, 0, 0, 0)
+    desc = _lib.ModelDesc(5, st, gr, 1)
+    Lx = np.array([3], np.int32)
+    off = np.array([0], np.int64)
+    dummy = np.zeros(64, np.float64)      # host memory standing in for device pointers: never read
+    vp = ctypes.c_void_p(dummy.ctypes.data)
+    i32 = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    i64 = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    for mask, beam, word in ((vp, 0.0, 'cell masks'), (None, 2.0, 'beam')):
+        b = _lib.Batch(1, i32(Lx), i32(Lx), vp, i64(off), i64(off), vp, 0, vp, vp, vp, 0, mask, beam)
+        rc = lib.phmm_estep_static(ctypes.byref(desc), ctypes.byref(b), *([vp] * 6), None)
+        assert rc == -1 and word in _lib.last_error()

@@ -2134,6 +2134,8 @@ extern "C" int phmm_estep_static(const phmm_model_desc *md, const phmm_batch *b,
         return fail(PHMM_E_ARG, "null batch pointer or output");
     if (P_ > kStaticMaxPairs) return fail(PHMM_E_ARG, "phmm_estep_static: more than 4096 pairs in one call");
     if (b->cell_mask) return fail(PHMM_E_ARG, "phmm_estep_static: cell masks are not supported (use phmm_estep)");
+    if (b->beam_log_width != 0.0)
+        return fail(PHMM_E_ARG, "phmm_estep_static: beam pruning is not supported (use phmm_estep)");
     // ---- device set-up, once per device (the first call on a device does it)
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));

@@ -82,3 +82,39 @@ def test_empty_and_blank_text(lib):
     from pairhmm import pair_format as pf
     assert pf.read_records('').n_pairs == 0
     assert pf.read_records('\n  \n').n_pairs == 0
+
+
+def test_native_reader_survives_mutated_records(lib):
+    """Truncated, mutated and random lines either parse to the same answer as
+    the Python decoder or raise PairHMMError; the reader never crashes."""
+    from pairhmm import pair_format as pf, _lib
+    rng = np.random.default_rng(2026)
+    lines = _text().strip().split('\n')
+    alphabet = list('{}[]":,. xaytfm0123456789MIDACDEFGHIKLMNPQRSTVWYBZ\\\t')
+    for trial in range(400):
+        line = lines[int(rng.integers(len(lines)))]
+        kind = trial % 4
+        if kind == 0:
+            line = line[:int(rng.integers(len(line) + 1))]
+        elif kind == 1:
+            pos = int(rng.integers(len(line)))
+            line = line[:pos] + alphabet[int(rng.integers(len(alphabet)))] + line[pos + 1:]
+        elif kind == 2:
+            pos = int(rng.integers(len(line)))
+            line = line[:pos] + line[pos + 1:]
+        else:
+            line = ''.join(alphabet[int(v)] for v in rng.integers(0, len(alphabet), int(rng.integers(1, 80))))
+        try:
+            r = pf.read_records(line + '\n')
+        except _lib.PairHMMError:
+            continue
+        if r.n_pairs == 0:
+            assert line.strip() == ''
+            continue
+        rec = json.loads(line)
+        ok, _ = pf.validate_record(rec)
+        assert ok
+        x, y, st, anc, desc, t = r.decoded(0)[:6]
+        rx, ry, rst, ranc, rdesc, rt = pf.decode_pair(rec)[:6]
+        assert np.array_equal(x, rx) and np.array_equal(y, ry) and st == rst and anc == ranc and desc == rdesc
+        assert t == rt

@@ -14,7 +14,10 @@
 // (M, I), 20 where the column has none.  Two passes over the text: a count
 // (sizes for the caller's buffers), then the fill.  Records failing the
 // consistency rules of validate_record (util/pair_format.py:194-223: M+D runs
-// = |x|, M+I runs = |y|, residues in the alphabet) are errors naming the line.
+// = |x|, M+I runs = |y|, residues in the alphabet) are errors naming the line,
+// and so is a line that is not one JSON object (the grammar of numbers,
+// literals, strings and escapes is checked; escaped characters are left as
+// written, so a residue string with an escape fails the alphabet check).
 #include "pairhmm.h"
 
 #include <cstdio>
@@ -56,12 +59,32 @@ struct Cur {
     }
 };
 
-// A JSON string: the raw span between the quotes (escapes left as written).
+static bool hexdigit(char ch) {
+    return (ch >= '0' && ch <= '9') || (ch >= 'a' && ch <= 'f') || (ch >= 'A' && ch <= 'F');
+}
+
+// A JSON string: the raw span between the quotes (escapes checked, left as
+// written); control characters and unknown escapes are errors, as in JSON.
 static bool str(Cur &c, Span &s) {
     if (c.p >= c.end || *c.p != '"') return false;
     const char *b = ++c.p;
     while (c.p < c.end && *c.p != '"') {
-        if (*c.p == '\\') ++c.p;
+        const unsigned char ch = (unsigned char)*c.p;
+        if (ch < 0x20) return false;
+        if (ch == '\\') {
+            if (c.p + 1 >= c.end) return false;
+            const char e = c.p[1];
+            if (e == 'u') {
+                if (c.end - c.p < 6) return false;
+                for (int k = 2; k < 6; ++k)
+                    if (!hexdigit(c.p[k])) return false;
+                c.p += 6;
+                continue;
+            }
+            if (e == 0 || !std::strchr("\"\\/bfnrt", e)) return false;
+            c.p += 2;
+            continue;
+        }
         ++c.p;
     }
     if (c.p >= c.end) return false;
@@ -71,16 +94,36 @@ static bool str(Cur &c, Span &s) {
     return true;
 }
 
+// A JSON number: -?(0|[1-9][0-9]*)(.[0-9]+)?([eE][+-]?[0-9]+)?
 static bool number(Cur &c, double &v) {
+    const char *b = c.p, *q = c.p;
+    auto digits = [&]() {
+        const char *d = q;
+        while (q < c.end && *q >= '0' && *q <= '9') ++q;
+        return q > d;
+    };
+    if (q < c.end && *q == '-') ++q;
+    if (q < c.end && *q == '0') ++q;
+    else if (!digits()) return false;
+    if (q < c.end && *q == '.') {
+        ++q;
+        if (!digits()) return false;
+    }
+    if (q < c.end && (*q == 'e' || *q == 'E')) {
+        ++q;
+        if (q < c.end && (*q == '+' || *q == '-')) ++q;
+        if (!digits()) return false;
+    }
+    const size_t n = (size_t)(q - b);
     char buf[64];
-    size_t n = 0;
-    while (c.p < c.end && n < sizeof(buf) - 1 && (std::strchr("+-.eE", *c.p) || (*c.p >= '0' && *c.p <= '9')))
-        buf[n++] = *c.p++;
-    if (n == 0) return false;
+    if (n >= sizeof buf) return false;
+    std::memcpy(buf, b, n);
     buf[n] = 0;
     char *e = nullptr;
     v = std::strtod(buf, &e);
-    return e == buf + n;
+    if (e != buf + n) return false;
+    c.p = q;
+    return true;
 }
 
 // Skip one JSON value of any kind.
@@ -115,9 +158,12 @@ static bool skip(Cur &c, int depth = 0) {
             return false;
         }
     }
-    if (ch == 't' || ch == 'f' || ch == 'n') {
-        while (c.p < c.end && *c.p >= 'a' && *c.p <= 'z') ++c.p;
-        return true;
+    for (const char *lit : {"true", "false", "null"}) {
+        const size_t n = std::strlen(lit);
+        if ((size_t)(c.end - c.p) >= n && std::memcmp(c.p, lit, n) == 0) {
+            c.p += n;
+            return true;
+        }
     }
     double v;
     return number(c, v);
@@ -157,6 +203,8 @@ static bool record(const char *b, const char *e, Rec &r, std::string &err) {
         err = "expected ',' or '}'";
         return false;
     }
+    c.ws();
+    if (c.p != c.end) { err = "text after the record"; return false; }
     if (!r.has_x || !r.has_a || !r.has_y || !r.has_t) { err = "record needs keys x, a, y and t"; return false; }
     return true;
 }

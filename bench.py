@@ -448,11 +448,15 @@ def main():
         dist.barrier()
     clocks = sampler.stop()
     total_ms = float(np.sum(step_ms))
+    cells_all = cell_states   # cell-state updates of one step over all ranks (each rank draws its own pairs)
     if ws > 1:
         t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
-    value = cell_states * ws * args.steps / (total_ms / 1e3)
+        c = torch.tensor([cell_states], device=dev, dtype=torch.float64)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        cells_all = float(c.item())
+    value = cells_all * args.steps / (total_ms / 1e3)
     ms_step = total_ms / args.steps
     gpu_ll = out['ll'].cpu().numpy()
     gpu_n = None if fwd_only else out['n_trans'].cpu().numpy()
@@ -475,7 +479,7 @@ def main():
         t = torch.tensor([e2e_total], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_total = float(t.item())
-    e2e_value = cell_states * ws * args.steps / (e2e_total / 1e3)
+    e2e_value = cells_all * args.steps / (e2e_total / 1e3)
     # ---- plain: one launch sequence per pair (the single-pair path)
     plain = None
     if not args.no_plain and rank == 0 and not fwd_only:

@@ -175,11 +175,27 @@ def _oracle_model(workload, b):
     return oe.tkf_model(workload.model, p)[:6]
 
 
+def _oracle_engine():
+    """'C' when the oracle's C half (oracle/fb2d.c, built by build()) loads,
+    else 'NumPy'."""
+    try:
+        from oracle import cdp
+        if cdp.available():
+            cdp._lib()
+            return 'C'
+    except Exception:
+        pass
+    return 'NumPy'
+
+
 def _oracle_pair(workload, b, forward_only):
     """Oracle log-likelihood and expected transition counts (None when forward only)."""
     from oracle import models as om, dp as odp
     chi, st, groups, EM, EI, ED = _oracle_model(workload, b)
     emit = odp.log_emission_table(st, groups, workload.xs[b], workload.ys[b], EM, EI, ED)
+    if _oracle_engine() == 'C':
+        from oracle import cdp
+        return cdp.forward_backward(om.safe_log(chi), st, emit, forward_only)
     if forward_only:
         return odp.forward_table(om.safe_log(chi), st, emit)[0], None
     ll, _, n, _, _ = odp.forward_backward(om.safe_log(chi), st, emit)
@@ -229,13 +245,14 @@ def cpu_baseline(workload, seconds, forward_only, gpu_ll=None, gpu_n=None, threa
     what = 'forward' if forward_only else 'forward+backward+counts'
     smp = (f'{n} smallest pairs of the workload ({done_cells} cells)' if truncated is None else
            f'the leading {truncated} x {truncated} block of the smallest pair ({done_cells} cells)')
+    eng = _oracle_engine()
     base = {'value': done_cells * N / el, 'unit': 'cell-state updates/s', 'cores': threads,
-            'kind': 'port', 'sample': f'{smp}, FP64 NumPy oracle {what}, {el:.1f} s'}
+            'kind': 'port', 'sample': f'{smp}, FP64 {eng} oracle {what}, {el:.1f} s'}
     acc = None
     if ll_err:
         acc = {'pairs': n, 'll_max_rel_err': float(np.max(ll_err)), 'll_median_rel_err': float(np.median(ll_err)),
                'n_trans_max_rel_err': float(np.max(n_err)) if n_err else None,
-               'against': 'FP64 NumPy oracle (pinned to the reference outputs)'}
+               'against': f'FP64 {eng} oracle (pinned to the reference outputs)'}
     return base, acc
 
 
@@ -270,6 +287,10 @@ def run_reference(args, rank, ws):
         cells += (len(x) + 1) * (len(y) + 1)
         if cells * N * N > 2.0e5 * 17 * 17 * max(1, cores // 4):
             break
+    # one process per core: keep each worker's BLAS to one thread (the
+    # workers inherit this environment), or they oversubscribe the cores
+    for var in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
+        os.environ.setdefault(var, '1')
     ctx = mp.get_context('spawn')
     with ctx.Pool(cores) as pool:
         for _ in range(args.warmup):
@@ -287,7 +308,7 @@ def run_reference(args, rank, ws):
             'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
             'config': {'workload': args.workload, 'sample_pairs': len(sample), 'sample_cells': int(cells),
                        'note': 'reference is JAX-only (not installable here); its algorithm is run '
-                               'as the FP64 NumPy restatement in oracle/'},
+                               f'as the FP64 {_oracle_engine()} restatement in oracle/'},
             'cpu_baseline': {'value': val, 'unit': 'cell-state updates/s', 'cores': cores, 'kind': 'port',
                              'sample': f'{len(sample)} smallest pairs, {int(cells)} cells per step'},
             'e2e': {'value': val, 'unit': 'cell-state updates/s', 'h2d_bytes_per_step': 0,

@@ -1,0 +1,110 @@
+/* FP64 oracle in C: 2D pair-HMM forward-backward (TEST INFRASTRUCTURE ONLY).
+ *
+ * The checker's fast twin of oracle/dp.py, used by the test-suite (against
+ * the NumPy oracle) and by bench.py's CPU legs; the product never links it.
+ * It restates the same log-space recursions of the reference
+ * (python/tkfmixdom/jax/dp/hmm.py):
+ *   forward  (dp/hmm.py:1120-1292): F[0,0,S] = 0; for M/I/D destination k at
+ *            (i, j), F = lse_s(F[pred_k, s] + logT[s, k]) + e[i, j, k] with
+ *            pred M (i-1, j-1), I (i, j-1), D (i-1, j); S/E destinations and
+ *            missing predecessors NEG_INF; LL = lse_s(F[Lx, Ly, s] + logT[s, E]);
+ *   backward (dp/hmm.py:1295-1437, 1695-1772): B[Lx, Ly, s] = logT[s, E];
+ *            elsewhere B[i, j, s] = lse over M/I/D successors k of
+ *            logT[s, k] + e[succ_k, k] + B[succ_k, k];
+ *   counts   (dp/hmm.py:1940-1971): n[s, k] = sum over cells of
+ *            exp(F[src, s] + logT[s, k] + e[dst, k] + B[dst, k] - LL), plus
+ *            n[s, E] += exp(F[Lx, Ly, s] + logT[s, E] - LL).
+ * NEG_INF is -1e30 and is summed like any other number, as the reference does.
+ * Cells in anti-diagonal order; all tables are caller-owned (no allocation).
+ * Built by oracle/build_oracle.py with the host C compiler. */
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#define NEG_INF (-1e30)
+
+enum { TS = 0, TM = 1, TI = 2, TD = 3, TE = 4 };
+
+static double lse(const double *v, int n) {
+    double m = v[0];
+    for (int k = 1; k < n; ++k)
+        if (v[k] > m) m = v[k];
+    double s = 0.0;
+    for (int k = 0; k < n; ++k) s += exp(v[k] - m);
+    return m + log(s);
+}
+
+/* F, B: (Lx+1)(Ly+1)N doubles each (B unused when forward_only); tmp: N
+ * doubles.  Returns the log-likelihood; n_trans (N*N, zeroed here) may be
+ * NULL when forward_only. */
+double oracle_fb2d(int N, const int8_t *st, const double *lt, int Lx, int Ly, const double *emit,
+                   int forward_only, double *F, double *B, double *n_trans, double *tmp) {
+    const int W = Ly + 1;
+    int e_idx = 0;
+    for (int k = 0; k < N; ++k)
+        if (st[k] == TE) { e_idx = k; break; }
+#define AT(T, i, j) ((T) + ((size_t)(i) * W + (size_t)(j)) * (size_t)N)
+    for (size_t q = 0; q < (size_t)(Lx + 1) * W * N; ++q) F[q] = NEG_INF;
+    F[0] = 0.0;   /* state 0 is the start */
+    for (int d = 1; d <= Lx + Ly; ++d) {
+        const int ilo = d - Ly > 0 ? d - Ly : 0, ihi = d < Lx ? d : Lx;
+        for (int i = ilo; i <= ihi; ++i) {
+            const int j = d - i;
+            double *out = AT(F, i, j);
+            const double *e = AT(emit, i, j);
+            for (int k = 0; k < N; ++k) {
+                const double *pred = NULL;
+                if (st[k] == TM && i >= 1 && j >= 1) pred = AT(F, i - 1, j - 1);
+                else if (st[k] == TI && j >= 1) pred = AT(F, i, j - 1);
+                else if (st[k] == TD && i >= 1) pred = AT(F, i - 1, j);
+                if (!pred) { out[k] = NEG_INF; continue; }
+                for (int s = 0; s < N; ++s) tmp[s] = pred[s] + lt[s * N + k];
+                out[k] = lse(tmp, N) + e[k];
+            }
+        }
+    }
+    const double *last = AT(F, Lx, Ly);
+    for (int s = 0; s < N; ++s) tmp[s] = last[s] + lt[s * N + e_idx];
+    const double ll = lse(tmp, N);
+    if (forward_only) return ll;
+    for (size_t q = 0; q < (size_t)(Lx + 1) * W * N; ++q) B[q] = NEG_INF;
+    for (int s = 0; s < N; ++s) AT(B, Lx, Ly)[s] = lt[s * N + e_idx];
+    for (int d = Lx + Ly - 1; d >= 0; --d) {
+        const int ilo = d - Ly > 0 ? d - Ly : 0, ihi = d < Lx ? d : Lx;
+        for (int i = ilo; i <= ihi; ++i) {
+            const int j = d - i;
+            double *out = AT(B, i, j);
+            for (int s = 0; s < N; ++s) {
+                int n = 0;
+                for (int k = 0; k < N; ++k) {
+                    int ni, nj;
+                    if (st[k] == TM) { ni = i + 1; nj = j + 1; }
+                    else if (st[k] == TI) { ni = i; nj = j + 1; }
+                    else if (st[k] == TD) { ni = i + 1; nj = j; }
+                    else continue;
+                    if (ni > Lx || nj > Ly) continue;
+                    tmp[n++] = lt[s * N + k] + AT(emit, ni, nj)[k] + AT(B, ni, nj)[k];
+                }
+                out[s] = n ? lse(tmp, n) : NEG_INF;
+            }
+        }
+    }
+    memset(n_trans, 0, sizeof(double) * (size_t)N * N);
+    for (int i = 0; i <= Lx; ++i)
+        for (int j = 0; j <= Ly; ++j) {
+            const double *f = AT(F, i, j);
+            for (int k = 0; k < N; ++k) {
+                int ni, nj;
+                if (st[k] == TM) { ni = i + 1; nj = j + 1; }
+                else if (st[k] == TI) { ni = i; nj = j + 1; }
+                else if (st[k] == TD) { ni = i + 1; nj = j; }
+                else continue;
+                if (ni > Lx || nj > Ly) continue;
+                const double w = AT(emit, ni, nj)[k] + AT(B, ni, nj)[k] - ll;
+                for (int s = 0; s < N; ++s) n_trans[s * N + k] += exp(f[s] + lt[s * N + k] + w);
+            }
+        }
+    for (int s = 0; s < N; ++s) n_trans[s * N + e_idx] += exp(last[s] + lt[s * N + e_idx] - ll);
+#undef AT
+    return ll;
+}

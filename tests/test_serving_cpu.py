@@ -175,3 +175,47 @@ def test_run_stream_with_fake_clock_reports_latency():
     assert summ['completed'] == 20 and summ['failed'] == 0
     assert 0 < summ['p50_ms'] <= summ['p99_ms']
     assert all(r.done >= r.arrival for r in out)
+
+
+def test_failed_launch_fails_its_batch_not_the_loop():
+    """A launch that raises (e.g. an allocation or CUDA error in the executor)
+    fails the requests of that batch, returns their memory and slot, and the
+    loop serves the rest."""
+    class FailingExecutor(FakeExecutor):
+        def __init__(self):
+            super().__init__(polls_to_finish=1)
+            self.calls = 0
+
+        def launch(self, model, reqs, off, nbytes, slot):
+            self.calls += 1
+            if self.calls == 1:
+                raise RuntimeError('injected launch failure')
+            return super().launch(model, reqs, off, nbytes, slot)
+
+    ex = FailingExecutor()
+    s = Scheduler(ex, arena_bytes=1 << 16, max_inflight=1, max_batch=2)
+    reqs = [s.submit(_req(i, 'a', 20)) for i in range(6)]
+    s.drain()
+    failed = [r for r in reqs if r.error is not None]
+    assert len(failed) == 2 and all('injected launch failure' in r.error for r in failed)
+    assert all(r.result is not None for r in reqs if r.error is None)
+    assert s.arena.used == 0 and s.idle()
+
+
+def test_per_request_error_flag_fails_only_that_request():
+    """An executor that reports a per-pair status (the kernels' status word)
+    fails that request alone; its batch-mates keep their results."""
+    class FlaggingExecutor(FakeExecutor):
+        def finish(self, h, reqs):
+            super().finish(h, reqs)
+            for r in reqs:
+                if r.rid == 3:
+                    r.error = 'kernel status 1'
+
+    ex = FlaggingExecutor(polls_to_finish=1)
+    s = Scheduler(ex, arena_bytes=1 << 16, max_inflight=2, max_batch=4)
+    reqs = [s.submit(_req(i, 'a', 15)) for i in range(8)]
+    s.drain()
+    assert [r.rid for r in reqs if r.error] == [3]
+    summ = latency_summary(reqs, 1.0)
+    assert summ['failed'] == 1 and summ['completed'] == 7

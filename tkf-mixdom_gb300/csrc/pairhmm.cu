@@ -30,6 +30,7 @@
 //    forward pass of an E-step stores the scaled forward lattice (stripe-
 //    diagonal layout, read back with cp.async one diagonal ahead).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -1364,6 +1365,13 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
 // the plan (grown on demand) unless the caller passes a workspace `ws` of
 // `ws_bytes`; with `ws_need` set, nothing runs and the workspace size the
 // call would need is stored there (only the host fields of the batch are read).
+// An NVTX range for the host side of one call (visible to a profiler that
+// attaches one; a pointer check otherwise).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
 int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_trans,
         double *cntM, double *cntI, double *cntD, int32_t *status, double *F_log, double *B_log,
         double *post, void *stream_, void *ws = nullptr, size_t ws_bytes = 0, size_t *ws_need = nullptr) {
@@ -1719,6 +1727,7 @@ size_t plan_scratch_bytes(const phmm_plan *plan) {
 
 int run_groups(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_trans, double *cntM,
                double *cntI, double *cntD, int32_t *status, void *stream) {
+    NvtxRange range(estep ? "phmm_estep" : "phmm_forward");
     if (!plan || !b) return fail(PHMM_E_ARG, "null plan or batch");
     size_t need = 0;
     int rc = run(plan, b, estep, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,

@@ -81,6 +81,8 @@ def main(ref_python):
             lp, post, nt = hmm.forward_backward_2d_banded(lt, w(st), w(x), w(y), w(sub), w(pi), w(bc), bw)
             out[pre + 'band_center'] = bc
             out[pre + 'band_width'] = np.int64(bw)
+            out[pre + 'msa_x'] = mx
+            out[pre + 'msa_y'] = my
         else:
             mi = np.array([mx[c] for c in range(len(states)) if states[c] == 1], np.int32)
             mj = np.array([my[c] for c in range(len(states)) if states[c] == 1], np.int32)

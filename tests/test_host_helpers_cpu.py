@@ -116,3 +116,29 @@ def test_output_arena_and_host_copy_on_cpu():
     ar['b'].fill_(7)
     host = _lib.to_host({'a': ar['a'], 'b': ar['b'], 'note': 'kept'})
     assert np.all(host['a'] == 1.5) and np.all(host['b'] == 7) and host['note'] == 'kept'
+
+
+@pytest.mark.parametrize('name', ['band_tkf91_a', 'band_tkf91_b', 'band_mixdom_a', 'band_tkf91_c', 'band_tkf91_d'])
+def test_msa_to_band_center_matches_reference(name):
+    from conftest import load_golden
+    from pairhmm import api
+    g = load_golden('masked')
+    pre = name + '_'
+    bc = api.msa_to_band_center(g[pre + 'msa_x'], g[pre + 'msa_y'], len(g[pre + 'x']))
+    assert bc.dtype == np.int32 and np.array_equal(bc, g[pre + 'band_center'])
+
+
+@pytest.mark.parametrize('name', ['match_tkf91_a', 'match_mixdom_a', 'match_tkf91_b'])
+def test_mask_emissions_match_aligned_matches_reference(name):
+    from conftest import load_golden
+    from pairhmm import api
+    from oracle import dp
+    g = load_golden('masked')
+    pre = name + '_'
+    st = g[pre + 'state_types']
+    EM, EI, ED = dp.group_tables_tkf(g[pre + 'sub'], g[pre + 'pi'])
+    emit = dp.log_emission_table(st, np.zeros(st.size, int), g[pre + 'x'], g[pre + 'y'], EM, EI, ED)
+    got = api.mask_emissions_match_aligned(emit, st, g[pre + 'match_i'], g[pre + 'match_j'])
+    ref = g[pre + 'log_emit']
+    assert np.array_equal(got > -1e29, ref > -1e29)
+    np.testing.assert_allclose(got, ref, rtol=1e-13, atol=1e-13)

@@ -239,6 +239,31 @@ def match_aligned_mask(Lx, Ly, match_i, match_j):
     return m
 
 
+def mask_emissions_match_aligned(emit, state_types, match_positions_i, match_positions_j):
+    """dp/hmm.py:1085-1117 on a host (Lx+1, Ly+1, N) log emission table: the
+    M-type entries off the alignment's match cells (mi+1, mj+1) get NEG_INF
+    added.  forward_backward_2d(..., log_emit_table=...) runs such a table on
+    the cell-masked kernels; match_aligned_mask gives the mask directly."""
+    em = np.array(emit, dtype=np.float64)
+    allowed = np.zeros(em.shape[:2], bool)
+    allowed[np.asarray(match_positions_i, int) + 1, np.asarray(match_positions_j, int) + 1] = True
+    isM = np.asarray(state_types) == M
+    em[:, :, isM] += np.where(allowed, 0.0, NEG_INF)[:, :, None]
+    return em
+
+
+def msa_to_band_center(msa_x_row, msa_y_row, Lx, gap_token=-1):
+    """dp/hmm.py:2494-2525: band centres (Lx+1,) int32 from a guide alignment --
+    for each i the j of the first point of the guide walk (0,0), (x_1, y_1), ...
+    whose i reaches i (the last point where none does)."""
+    has_x = np.asarray(msa_x_row).astype(np.int64) != gap_token
+    has_y = np.asarray(msa_y_row).astype(np.int64) != gap_token
+    gx = np.concatenate([[0], np.cumsum(has_x)])
+    gy = np.concatenate([[0], np.cumsum(has_y)])
+    idx = np.minimum(np.searchsorted(gx, np.arange(int(Lx) + 1), side='left'), gx.size - 1)
+    return gy[idx].astype(np.int32)
+
+
 def band_mask(Lx, Ly, band_center, band_width):
     """Cell mask of the banded recursions (dp/hmm.py:2104-2492): uint8
     (Lx+1, Ly+1), 7 where |j - c_i| <= W and 0 elsewhere, with

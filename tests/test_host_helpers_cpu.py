@@ -142,3 +142,40 @@ def test_mask_emissions_match_aligned_matches_reference(name):
     ref = g[pre + 'log_emit']
     assert np.array_equal(got > -1e29, ref > -1e29)
     np.testing.assert_allclose(got, ref, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize('name', ['mixdom2_k3f1c1', 'mixdom2_k2f2c2', 'mixdom2_k1f2c3_wild', 'mixdom1_d3f2'])
+def test_dense_emission_builders_match_reference(name):
+    """pair_hmm_emissions_per_class / _per_domain against the reference's own
+    tables in the MixDom fixtures (wildcards included)."""
+    from conftest import load_golden
+    from pairhmm import api
+    from pairhmm import models as pm
+    g = load_golden(name)
+    K, F = int(g['K']), int(g['F'])
+    st = pm.mixdom_state_types(K, F)
+    if name.startswith('mixdom2'):
+        got = api.pair_hmm_emissions_per_class(st, g['x'], g['y'], g['class_subs'], g['p_class_pis'],
+                                               g['p_classdist'], K, F)
+    else:
+        got = api.pair_hmm_emissions_per_domain(st, g['x'], g['y'], g['subs'], g['dom_pis'], K, F)
+    ref = g['log_emit'][:len(g['x']) + 1, :len(g['y']) + 1]
+    live = ref > -1e29
+    assert np.array_equal(live, got > -1e29)
+    np.testing.assert_allclose(got[live], ref[live], rtol=1e-12, atol=1e-12)
+
+
+def test_pair_hmm_emissions_matches_oracle():
+    from pairhmm import api
+    from oracle import dp
+    rng = np.random.default_rng(8)
+    pi = rng.dirichlet(np.ones(20))
+    sub = rng.dirichlet(np.ones(20), size=20)
+    st = np.array([0, 1, 2, 3, 4])
+    x, y = rng.integers(0, 21, 11), rng.integers(0, 21, 7)
+    EM, EI, ED = dp.group_tables_tkf(sub, pi)
+    want = dp.log_emission_table(st, np.zeros(5, int), x, y, EM, EI, ED)
+    got = api.pair_hmm_emissions(st, x, y, sub, pi)
+    emitting = np.isin(st, (1, 2, 3))
+    np.testing.assert_allclose(got[:, :, emitting], want[:, :, emitting], rtol=1e-13, atol=1e-13)
+    assert np.all(got[:, :, ~emitting] == 0.0)

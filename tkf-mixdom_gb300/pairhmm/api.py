@@ -230,6 +230,57 @@ def forward_backward_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi,
     return r['ll'], post, r['n_trans']
 
 
+def _dense_log_table(state_types, groups, x_seq, y_seq, EM, EI, ED):
+    """(Lx+1, Ly+1, N) log emission table from linear per-group tables: M
+    states log EM[g][x_i][y_j], I log EI[g][y_j], D log ED[g][x_i], row and
+    column 0 reading character 0, S / E states 0, log 0 as NEG_INF."""
+    st = np.asarray(state_types)
+    gr = np.asarray(groups, int)
+    lg = lambda t: np.log(np.maximum(np.asarray(t.detach().cpu().numpy() if isinstance(t, torch.Tensor) else t,
+                                                np.float64), 1e-320))
+    lM, lI, lD = lg(EM), lg(EI), lg(ED)
+    xg = np.concatenate([[0], np.asarray(x_seq, int)])
+    yg = np.concatenate([[0], np.asarray(y_seq, int)])
+    out = np.zeros((xg.size, yg.size, st.size))
+    for k in range(st.size):
+        if st[k] == M:
+            out[:, :, k] = lM[gr[k]][xg[:, None], yg[None, :]]
+        elif st[k] == I:
+            out[:, :, k] = lI[gr[k]][yg][None, :]
+        elif st[k] == D:
+            out[:, :, k] = lD[gr[k]][xg][:, None]
+    out[out < -700.0] = NEG_INF
+    return out
+
+
+def pair_hmm_emissions(state_types, x_seq, y_seq, sub_matrix, pi):
+    """dp/hmm.py:628-670: (Lx+1, Ly+1, N) log emissions log(pi+1e-30) +
+    log(P+1e-30), wildcard 20 with probability 1, S/E states 0."""
+    EM, EI, ED = pm.tables_tkf(pm._t(np.asarray(sub_matrix, np.float64)), pm._t(np.asarray(pi, np.float64)))
+    return _dense_log_table(state_types, np.zeros(len(state_types), int), x_seq, y_seq, EM, EI, ED)
+
+
+def pair_hmm_emissions_per_class(state_types, x_seq, y_seq, class_sub_matrices, class_pis, class_dist, n_dom,
+                                 n_frag):
+    """dp/hmm.py:673-783: the MixDom2 per-(domain, fragment) class-mixture
+    log emissions, (Lx+1, Ly+1, N)."""
+    EM, EI, ED = pm.tables_per_class(pm._t(np.asarray(class_sub_matrices, np.float64)),
+                                     pm._t(np.asarray(class_pis, np.float64)),
+                                     pm._t(np.asarray(class_dist, np.float64)))
+    return _dense_log_table(state_types, pm.mixdom_state_groups(int(n_dom), int(n_frag)), x_seq, y_seq, EM, EI, ED)
+
+
+def pair_hmm_emissions_per_domain(state_types, x_seq, y_seq, sub_matrices, pis, n_dom, n_frag):
+    """dp/hmm.py:786-851: per-domain log emissions (domain d uses (pi_d, P_d),
+    clamped at 1e-30), (Lx+1, Ly+1, N)."""
+    EM, EI, ED = pm.tables_per_domain(pm._t(np.asarray(sub_matrices, np.float64)),
+                                      pm._t(np.asarray(pis, np.float64)))
+    N = len(state_types)
+    groups = np.zeros(N, int)
+    groups[2:] = np.arange(N - 2) // (5 * int(n_frag))
+    return _dense_log_table(state_types, groups, x_seq, y_seq, EM, EI, ED)
+
+
 def match_aligned_mask(Lx, Ly, match_i, match_j):
     """Cell mask of mask_emissions_match_aligned (dp/hmm.py:1085-1117): uint8
     (Lx+1, Ly+1) letting the M-type states emit only at the grid cells

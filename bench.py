@@ -271,22 +271,27 @@ def run_reference(args, rank, ws):
     from pairhmm import synth
     w = synth.CONFIGS[args.workload](seed=0)
     cores = len(os.sched_getaffinity(0))
-    order = np.argsort(w.cells())
     fwd_only = WORKLOADS[args.workload]['forward_only']
-    # bounded sample: the smallest pairs up to ~2e5 cells per step
-    sample, cells = [], 0
     from pairhmm.synth import Workload
     N = w.n_states
-    a = max(8, int((4e7 / (N * N)) ** 0.5))   # pairs above ~2e9 FLOP are timed on their leading a x a block
-    for b in order:
-        x, y = w.xs[b], w.ys[b]
-        if (len(x) + 1) * (len(y) + 1) * N * N > 2e9:
-            x, y = x[:a], y[:a]
-        one = Workload(w.name, w.model, w.params, [x], [y], w.ts[b:b + 1], w.K, w.F, w.C)
+    # bounded sample with the workload's length mix: every stride-th pair in
+    # size order, about 2 s of oracle work per core per step; a pair longer
+    # than c on a side is timed on its leading block (at most c x c), so no
+    # task exceeds half a core's share of a step and the pool stays balanced
+    # cell-state updates per core per step (the oracle's cost per cell-state
+    # grows with N: ~2.8 M/s per core at 17 states, forward only ~3x that)
+    per_core = 5e6 * 17.0 / N * (3.0 if fwd_only else 1.0)
+    c = max(8, int((per_core / 2 / N) ** 0.5) - 1)
+    clipped = lambda b: (min(len(w.xs[b]), c), min(len(w.ys[b]), c))
+    work = lambda b: (clipped(b)[0] + 1) * (clipped(b)[1] + 1) * N
+    order = sorted(range(len(w.xs)), key=work, reverse=True)      # largest first
+    stride = max(1, int(np.ceil(sum(work(b) for b in order) / (per_core * cores))))
+    sample, cells = [], 0
+    for b in order[::stride]:
+        lx, ly = clipped(b)
+        one = Workload(w.name, w.model, w.params, [w.xs[b][:lx]], [w.ys[b][:ly]], w.ts[b:b + 1], w.K, w.F, w.C)
         sample.append((one, 0, fwd_only))
-        cells += (len(x) + 1) * (len(y) + 1)
-        if cells * N * N > 2.0e5 * 17 * 17 * max(1, cores // 4):
-            break
+        cells += (lx + 1) * (ly + 1)
     # one process per core: keep each worker's BLAS to one thread (the
     # workers inherit this environment), or they oversubscribe the cores
     for var in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
@@ -294,11 +299,11 @@ def run_reference(args, rank, ws):
     ctx = mp.get_context('spawn')
     with ctx.Pool(cores) as pool:
         for _ in range(args.warmup):
-            pool.map(_ref_worker, sample[:cores])
+            pool.map(_ref_worker, sample[-cores:], chunksize=1)
         t0 = time.perf_counter()
         tot = 0
         for _ in range(args.steps):
-            tot += sum(pool.map(_ref_worker, sample))
+            tot += sum(pool.imap_unordered(_ref_worker, sample, chunksize=1))
         el = time.perf_counter() - t0
     N = w.n_states
     val = tot * N / el
@@ -310,7 +315,8 @@ def run_reference(args, rank, ws):
                        'note': 'reference is JAX-only (not installable here); its algorithm is run '
                                f'as the FP64 {_oracle_engine()} restatement in oracle/'},
             'cpu_baseline': {'value': val, 'unit': 'cell-state updates/s', 'cores': cores, 'kind': 'port',
-                             'sample': f'{len(sample)} smallest pairs, {int(cells)} cells per step'},
+                             'sample': f'{len(sample)} pairs (every {stride}. in size order; sides above {c} '
+                                       f'clipped to their leading block), {int(cells)} cells per step'},
             'e2e': {'value': val, 'unit': 'cell-state updates/s', 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0}}
     print(json.dumps(line))

@@ -136,3 +136,49 @@ def test_static_estep_refuses_masks_and_beam(lib):
         b = _lib.Batch(1, i32(Lx), i32(Lx), vp, i64(off), i64(off), vp, 0, vp, vp, vp, 0, mask, beam)
         rc = lib.phmm_estep_static(ctypes.byref(desc), ctypes.byref(b), *([vp] * 6), None)
         assert rc == -1 and word in _lib.last_error()
+
+
+def test_fb1d_and_viterbi_and_pairs_reject_bad_arguments(lib):
+    """Argument checks of the 1D forward-backward, Viterbi and record-reader
+    entries, all before any CUDA call."""
+    import ctypes
+    import numpy as np
+    from pairhmm import _lib, pair_format as pf
+    null = ctypes.c_void_p(0)
+    L = np.array([3], np.int32)
+    off = np.array([0], np.int64)
+    b = _lib.Fb1dBatch(1, 70, L.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                       off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), None, None, 0, 0, 1)
+    assert lib.phmm_fb1d(ctypes.byref(b), null, 0, null, null, null, null, null) == -1
+    assert '2..64' in _lib.last_error()
+    b.n_states = 5
+    b.final_state = 9
+    assert lib.phmm_fb1d(ctypes.byref(b), null, 0, null, null, null, null, null) == -1
+    assert 'final state' in _lib.last_error()
+    b.final_state = 4
+    assert lib.phmm_fb1d(ctypes.byref(b), null, 0, null, null, null, null, null) == -1
+    assert 'null pointer' in _lib.last_error()
+    b.n_pairs = 0
+    assert lib.phmm_fb1d(ctypes.byref(b), null, 0, null, null, null, null, null) == 0
+    # Viterbi: state 0 must be S and one state E
+    st = (ctypes.c_int8 * 3)(1, 2, 3)
+    gr = (ctypes.c_int32 * 3)(0, 0, 0)
+    desc = _lib.ModelDesc(3, st, gr, 1)
+    Lx = np.array([2], np.int32)
+    dummy = np.zeros(16)
+    vp = ctypes.c_void_p(dummy.ctypes.data)
+    i32 = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    i64 = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    bt = _lib.Batch(1, i32(Lx), i32(Lx), vp, i64(off), i64(off), vp, 0, vp, vp, vp, 0, None, 0.0)
+    wsbuf = np.zeros(1024, np.uint8)
+    ws = ctypes.c_void_p((wsbuf.ctypes.data + 255) & ~255)   # 256-byte aligned, never read
+    args = [vp] * 4 + [ws, ctypes.c_size_t(512), vp, vp, vp, vp, null]
+    assert lib.phmm_viterbi(ctypes.byref(desc), ctypes.byref(bt), *args) == -1
+    assert 'state 0 must be S' in _lib.last_error()
+    # record reader: sizes that do not match the text
+    cnt = pf.PairCounts(2, 4, 2)
+    pf._bind(lib)
+    one = b'{"x": "AC", "a": "M2", "y": "AC", "t": 1}\n'
+    arrs = [np.zeros(8, np.int64) for _ in range(13)]
+    rc = lib.phmm_pairs_decode(one, len(one), ctypes.byref(cnt), *[ctypes.c_void_p(a.ctypes.data) for a in arrs])
+    assert rc == -1 and 'less than the counted sizes' in _lib.last_error()

@@ -26,13 +26,20 @@ def _lib():
         lib.oracle_fb2d.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int8), dp, ctypes.c_int, ctypes.c_int,
                                     dp, ctypes.c_int, dp, dp, dp, dp]
         lib.oracle_fb2d.restype = ctypes.c_double
+        i32 = ctypes.POINTER(ctypes.c_int32)
+        lib.oracle_char_counts.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int8), i32, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, i32, i32, dp, dp, ctypes.c_double,
+                                           dp, dp, dp]
+        lib.oracle_char_counts.restype = None
         _L = lib
     return _L
 
 
-def forward_backward(log_trans, state_types, emit, forward_only=False):
+def forward_backward(log_trans, state_types, emit, forward_only=False, counts=None):
     """(log-likelihood, expected transitions (N, N) or None) for a log
-    emission table emit (Lx+1, Ly+1, N)."""
+    emission table emit (Lx+1, Ly+1, N).  With counts = (groups, G, x, y) a
+    third value: the per-group character counts (cM [G,21,21], cI [G,21],
+    cD [G,21]) of oracle.estep.char_count_tables."""
     lt = np.ascontiguousarray(np.asarray(log_trans, np.float64))
     st = np.ascontiguousarray(np.asarray(state_types, np.int8))
     em = np.ascontiguousarray(np.asarray(emit, np.float64))
@@ -46,4 +53,18 @@ def forward_backward(log_trans, state_types, emit, forward_only=False):
     dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     ll = _lib().oracle_fb2d(N, st.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), dp(lt), Lx, Ly, dp(em),
                             int(bool(forward_only)), dp(F), dp(B) if B.size else None, dp(n), dp(tmp))
-    return float(ll), (None if forward_only else n)
+    if counts is None or forward_only:
+        return float(ll), (None if forward_only else n)
+    groups, G, x, y = counts
+    gr = np.ascontiguousarray(np.asarray(groups, np.int32))
+    xg = np.ascontiguousarray(np.concatenate([[0], np.asarray(x, np.int64)]).astype(np.int32))
+    yg = np.ascontiguousarray(np.concatenate([[0], np.asarray(y, np.int64)]).astype(np.int32))
+    emitting = np.isin(st, (1, 2, 3))
+    if xg.size != Lx + 1 or yg.size != Ly + 1 or xg.min() < 0 or xg.max() > 20 or yg.min() < 0 or \
+            yg.max() > 20 or gr.size != N or (emitting.any() and (gr[emitting].min() < 0 or gr[emitting].max() >= G)):
+        raise ValueError('counts: sequences must match the table and hold 0..20, emitting groups 0..G-1')
+    cM, cI, cD = np.zeros((G, 21, 21)), np.zeros((G, 21)), np.zeros((G, 21))
+    i32 = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    _lib().oracle_char_counts(N, st.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)), i32(gr), int(G), Lx, Ly,
+                              i32(xg), i32(yg), dp(F), dp(B), ll, dp(cM), dp(cI), dp(cD))
+    return float(ll), n, (cM, cI, cD)

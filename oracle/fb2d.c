@@ -108,3 +108,29 @@ double oracle_fb2d(int N, const int8_t *st, const double *lt, int Lx, int Ly, co
 #undef AT
     return ll;
 }
+
+/* Per-group character counts of the posteriors (the kernels' native emission
+ * counts; oracle/estep.py char_count_tables): for M states at i, j >= 1
+ * cM[g][x_i][y_j] += post, for I states at j >= 1 cI[g][y_j] += post, for D
+ * states at i >= 1 cD[g][x_i] += post, post = exp(F + B - LL).  xg / yg are
+ * the grid characters (index 0 the dummy character), 0..20.  cM (G*441), cI
+ * and cD (G*21) are zeroed here.  F and B as oracle_fb2d left them. */
+void oracle_char_counts(int N, const int8_t *st, const int32_t *groups, int G, int Lx, int Ly,
+                        const int32_t *xg, const int32_t *yg, const double *F, const double *B, double ll,
+                        double *cM, double *cI, double *cD) {
+    const int W = Ly + 1;
+    memset(cM, 0, sizeof(double) * (size_t)G * 441);
+    memset(cI, 0, sizeof(double) * (size_t)G * 21);
+    memset(cD, 0, sizeof(double) * (size_t)G * 21);
+    for (int i = 0; i <= Lx; ++i)
+        for (int j = 0; j <= Ly; ++j) {
+            const double *f = F + ((size_t)i * W + (size_t)j) * (size_t)N;
+            const double *b = B + ((size_t)i * W + (size_t)j) * (size_t)N;
+            for (int k = 0; k < N; ++k) {
+                const int g = groups[k];
+                if (st[k] == TM && i >= 1 && j >= 1) cM[(size_t)g * 441 + xg[i] * 21 + yg[j]] += exp(f[k] + b[k] - ll);
+                else if (st[k] == TI && j >= 1) cI[(size_t)g * 21 + yg[j]] += exp(f[k] + b[k] - ll);
+                else if (st[k] == TD && i >= 1) cD[(size_t)g * 21 + xg[i]] += exp(f[k] + b[k] - ll);
+            }
+        }
+}

@@ -66,3 +66,20 @@ def test_c_oracle_on_golden_pairs(cdp, name):
     ll_c, n_c = cdp.forward_backward(lt, st, emit)
     assert abs(ll_c - ll_ref) <= 1e-10 * abs(ll_ref)
     np.testing.assert_allclose(n_c, n_ref, rtol=1e-8, atol=1e-10)
+
+
+@pytest.mark.parametrize('kind', ['tkf91', 'mixdom17', 'mixdom42'])
+def test_c_oracle_char_counts_match_numpy(cdp, kind):
+    from oracle import dp, models as om, estep as oe
+    rng = np.random.default_rng({'tkf91': 4, 'mixdom17': 5, 'mixdom42': 6}[kind])
+    chi, st, groups, EM, EI, ED = _model(rng, kind)
+    lt = om.safe_log(chi)
+    G = int(np.max(groups)) + 1
+    for Lx, Ly in ((0, 3), (2, 0), (9, 12), (25, 21)):
+        x, y = rng.integers(0, 21, Lx), rng.integers(0, 21, Ly)
+        emit = dp.log_emission_table(st, groups, x, y, EM, EI, ED)
+        ll, post, n, _, _ = dp.forward_backward(lt, st, emit)
+        want = oe.char_count_tables(post, st, groups, x, y, G)
+        _, _, got = cdp.forward_backward(lt, st, emit, counts=(groups, G, x, y))
+        for a, b in zip(got, want):
+            np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-12)

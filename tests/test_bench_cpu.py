@@ -30,3 +30,19 @@ def test_every_workload_names_its_metric_and_api():
         assert {'forward_only', 'metric', 'model', 'e2e_api'} <= set(spec), name
     assert bench.WORKLOAD in bench.WORKLOADS
     assert os.path.exists(os.path.join(ROOT, 'bench.py'))
+
+
+def test_reference_arm_runs_on_the_cpu():
+    """`bench.py --impl reference` needs no GPU: one short run prints the
+    contract's line (impl, value, cpu_baseline, e2e with zero copies)."""
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, os.path.join(ROOT, 'bench.py'), '--impl', 'reference', '--workload',
+                          'tkf91_64pairs_len50-150', '--steps', '1', '--warmup', '1'],
+                         capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line['impl'] == 'reference' and line['value'] > 0 and line['unit'] == 'cell-state updates/s'
+    assert line['cpu_baseline']['kind'] == 'port' and line['cpu_baseline']['cores'] >= 1
+    assert line['e2e']['h2d_bytes_per_step'] == 0 and line['e2e']['d2h_bytes_per_step'] == 0
+    assert line['higher_is_better'] is True and line['n_gpus'] >= 1

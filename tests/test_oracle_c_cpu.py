@@ -83,3 +83,25 @@ def test_c_oracle_char_counts_match_numpy(cdp, kind):
         _, _, got = cdp.forward_backward(lt, st, emit, counts=(groups, G, x, y))
         for a, b in zip(got, want):
             np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize('kind', ['tkf91', 'mixdom17'])
+def test_tiny_lattices_exhaustively(cdp, kind):
+    """Every Lx, Ly in 0..4 (the edge cases of empty, single-residue and
+    narrow lattices): both halves of the oracle agree on the likelihood,
+    the expected transitions and the character counts."""
+    from oracle import dp, models as om, estep as oe
+    rng = np.random.default_rng(7 if kind == 'tkf91' else 8)
+    chi, st, groups, EM, EI, ED = _model(rng, kind)
+    lt = om.safe_log(chi)
+    G = int(np.max(groups)) + 1
+    for Lx in range(5):
+        for Ly in range(5):
+            x, y = rng.integers(0, 21, Lx), rng.integers(0, 21, Ly)
+            emit = dp.log_emission_table(st, groups, x, y, EM, EI, ED)
+            ll, post, n, _, _ = dp.forward_backward(lt, st, emit)
+            ll_c, n_c, cnt = cdp.forward_backward(lt, st, emit, counts=(groups, G, x, y))
+            assert abs(ll_c - ll) <= 1e-12 * max(1.0, abs(ll)), (Lx, Ly)
+            np.testing.assert_allclose(n_c, n, rtol=1e-10, atol=1e-12)
+            for a, b in zip(cnt, oe.char_count_tables(post, st, groups, x, y, G)):
+                np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-12)

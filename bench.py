@@ -76,6 +76,8 @@ def parse_args():
     ap.add_argument('--max-len', type=int, default=0,
                     help='truncate every sequence to at most L residues (small case for ncu captures)')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    ap.add_argument('--no-accuracy', action='store_true',
+                    help='skip the accuracy leg (every pair against the FP64 oracle)')
     ap.add_argument('--serving-requests', type=int, default=2000,
                     help='requests in the serving-stream leg (0: skip it)')
     ap.add_argument('--serving-rate', type=float, default=5000.0)
@@ -202,26 +204,27 @@ def _oracle_pair(workload, b, forward_only):
     return ll, n
 
 
-def cpu_baseline(workload, seconds, forward_only, gpu_ll=None, gpu_n=None, threads=1):
+def cpu_baseline(workload, seconds, forward_only, threads=1):
     """The FP64 oracle on a bounded sample of the same pairs (host cores),
-    smallest pairs first; with the GPU's outputs it also reports their
-    error against the oracle on the sampled pairs."""
+    smallest pairs first."""
     done_cells = 0
     t0 = time.perf_counter()
     order = np.argsort(workload.cells())
     n = 0
-    ll_err, n_err = [], []
     N = workload.n_states
     truncated = None
+    try:
+        from oracle import cdp
+        if cdp.available():
+            cdp.set_threads(threads)
+    except Exception:
+        pass
     for b in order:
         cells_b = (len(workload.xs[b]) + 1) * (len(workload.ys[b]) + 1)
         if n == 0 and cells_b * N * N > 2e9:
             # one pair alone is far beyond the time budget: time its leading
             # a x a block (x[:a], y[:a]), a sized from a 16 x 16 calibration run
-            from pairhmm.synth import Workload
-            sub = lambda a: Workload(workload.name, workload.model, workload.params, [workload.xs[b][:a]],
-                                     [workload.ys[b][:a]], workload.ts[b:b + 1], workload.K, workload.F,
-                                     workload.C)
+            sub = lambda a: _leading_block(workload, b, a)
             tc = time.perf_counter()
             _oracle_pair(sub(16), 0, forward_only)
             per_cell = (time.perf_counter() - tc) / 17 ** 2
@@ -232,13 +235,9 @@ def cpu_baseline(workload, seconds, forward_only, gpu_ll=None, gpu_n=None, threa
             n += 1
             truncated = a
             break
-        ll, nt = _oracle_pair(workload, b, forward_only)
+        _oracle_pair(workload, b, forward_only)
         done_cells += cells_b
         n += 1
-        if gpu_ll is not None:
-            ll_err.append(abs(gpu_ll[b] - ll) / max(abs(ll), 1e-300))
-            if nt is not None and gpu_n is not None:
-                n_err.append(np.abs(gpu_n[b] - nt).max() / max(np.abs(nt).max(), 1e-300))
         if time.perf_counter() - t0 > seconds:
             break
     el = time.perf_counter() - t0
@@ -246,14 +245,58 @@ def cpu_baseline(workload, seconds, forward_only, gpu_ll=None, gpu_n=None, threa
     smp = (f'{n} smallest pairs of the workload ({done_cells} cells)' if truncated is None else
            f'the leading {truncated} x {truncated} block of the smallest pair ({done_cells} cells)')
     eng = _oracle_engine()
-    base = {'value': done_cells * N / el, 'unit': 'cell-state updates/s', 'cores': threads,
+    return {'value': done_cells * N / el, 'unit': 'cell-state updates/s', 'cores': threads,
             'kind': 'port', 'sample': f'{smp}, FP64 {eng} oracle {what}, {el:.1f} s'}
-    acc = None
-    if ll_err:
-        acc = {'pairs': n, 'll_max_rel_err': float(np.max(ll_err)), 'll_median_rel_err': float(np.median(ll_err)),
-               'n_trans_max_rel_err': float(np.max(n_err)) if n_err else None,
-               'against': f'FP64 {eng} oracle (pinned to the reference outputs)'}
-    return base, acc
+
+
+def _leading_block(workload, b, a):
+    """Pair b of the workload cut to its leading a x a block (x[:a], y[:a])."""
+    from pairhmm.synth import Workload
+    return Workload(workload.name, workload.model, workload.params, [workload.xs[b][:a]],
+                    [workload.ys[b][:a]], workload.ts[b:b + 1], workload.K, workload.F, workload.C)
+
+
+def accuracy_leg(workload, gpu, forward_only, block=None, sample_pairs=None):
+    """Error of the GPU outputs against the FP64 C oracle over EVERY pair of the
+    workload (all host cores, one single-threaded oracle process per core,
+    largest pairs first), outside the timed region.  gpu: host arrays 'll'
+    (and 'n_trans', 'cnt_M', 'cnt_I', 'cnt_D') indexed like the workload.
+    block / sample_pairs: the workload is a sub-sample (the pairs' leading
+    blocks, run on the GPU as their own batch) -- said in the result."""
+    from oracle import pool
+    if _oracle_engine() != 'C':
+        return {'error': 'the C oracle is not built (build())'}
+    cores = len(os.sched_getaffinity(0))
+    P = len(workload.xs)
+    cases = [tuple(_oracle_model(workload, b)) + (workload.xs[b], workload.ys[b]) for b in range(P)]
+    t0 = time.perf_counter()
+    res = pool.estep_pairs(cases, forward_only, cores)
+    el = time.perf_counter() - t0
+    ll_err, n_abs, n_rel, c_abs, c_rel = [], [], [], [], []
+    for b, (ll, n, cnt) in enumerate(res):
+        ll_err.append(abs(float(gpu['ll'][b]) - ll) / max(abs(ll), 1e-300))
+        if n is None:
+            continue
+        a, r = pool.count_errors(gpu['n_trans'][b], n)
+        n_abs.append(a)
+        n_rel.append(r)
+        for key, want in zip(('cnt_M', 'cnt_I', 'cnt_D'), cnt):
+            a, r = pool.count_errors(gpu[key][b], want)
+            c_abs.append(a)
+            c_rel.append(r)
+    cells = int(sum((len(x) + 1) * (len(y) + 1) for x, y in zip(workload.xs, workload.ys)))
+    acc = {'pairs': P, 'cells': cells,
+           'max_pair': [int(max(len(x) for x in workload.xs)), int(max(len(y) for y in workload.ys))],
+           'll_max_rel_err': float(np.max(ll_err)), 'll_median_rel_err': float(np.median(ll_err)),
+           'against': 'FP64 C oracle (oracle/fb2d.c, pinned to the reference outputs)',
+           'oracle_s': round(el, 1), 'oracle_cores': cores}
+    if n_abs:
+        acc.update({'n_trans_max_err_of_max': float(np.max(n_abs)), 'n_trans_max_rel_err': float(np.max(n_rel)),
+                    'counts_max_err_of_max': float(np.max(c_abs)), 'counts_max_rel_err': float(np.max(c_rel)),
+                    'counts_rel_err_note': 'relative error over entries above 1e-6 of the pair\'s largest'})
+    acc['scope'] = ('every pair of the workload' if block is None else
+                    f'leading {block} x {block} blocks of {sample_pairs} pairs, run on the GPU as their own batch')
+    return acc
 
 
 def _ref_worker(args):
@@ -360,6 +403,32 @@ def serving_leg(n_requests, rate, seed=0):
             'arrival_span_s': float(offsets[-1]), 'cell_states': cs,
             'continuous': cont, 'plain_one_launch_per_request': plain,
             'arena_bytes': ARENA, 'stream_generation_s': gen_s}
+
+
+def accuracy_of_workload(args, w, plan, out, chi, EM, EI, ED, fwd_only, dev):
+    """The accuracy leg of this run: every pair against the oracle, except for
+    lattices the oracle cannot finish in about a minute (162 states at 2000 x
+    2000): those are checked on the leading block of two pairs, the GPU
+    running the same blocks as a batch of their own."""
+    import torch
+    from pairhmm import _lib
+    N = w.n_states
+    if float(w.cells().sum()) * N * N <= 1.5e11:
+        gpu = {k: v.cpu().numpy() for k, v in out.items()}
+        return accuracy_leg(w, gpu, fwd_only)
+    a = 600 if N * N * 601 * 601 <= 1e10 else 300
+    pick = [int(i) for i in np.argsort(w.cells())[:2]]
+    from pairhmm.synth import Workload
+    sub = Workload(w.name, w.model, w.params, [w.xs[b][:a] for b in pick], [w.ys[b][:a] for b in pick],
+                   np.asarray(w.ts)[pick], w.K, w.F, w.C)
+    idx = torch.as_tensor(pick, device=dev)
+    bt = _lib.make_batch(sub.xs, sub.ys, chi[idx], EM[idx], EI[idx], ED[idx], device=dev)
+    if fwd_only:
+        ll, st = _lib.forward(plan, bt)
+        gpu = {'ll': ll.cpu().numpy()}
+    else:
+        gpu = {k: v.cpu().numpy() for k, v in _lib.estep(plan, bt).items()}
+    return accuracy_leg(sub, gpu, fwd_only, block=a, sample_pairs=len(pick))
 
 
 def e2e_function(workload, w, api, torch):
@@ -485,8 +554,6 @@ def main():
         cells_all = float(c.item())
     value = cells_all * args.steps / (total_ms / 1e3)
     ms_step = total_ms / args.steps
-    gpu_ll = out['ll'].cpu().numpy()
-    gpu_n = None if fwd_only else out['n_trans'].cpu().numpy()
     # ---- end to end through the public API (host sequences -> host results)
     e2e_ms = []
     h2d = int(sum(len(x) + len(y) for x, y in zip(w.xs, w.ys)) + 8 * len(w.ts))
@@ -574,8 +641,13 @@ def main():
     if rank == 0 and args.serving_requests > 0 and args.workload == WORKLOAD:
         serving = serving_leg(args.serving_requests, args.serving_rate)
     if rank == 0:
-        cpu, acc = (cpu_baseline(w, args.cpu_seconds, fwd_only, gpu_ll, gpu_n) if args.cpu_seconds > 0
-                    else (None, None))
+        cpu = cpu_baseline(w, args.cpu_seconds, fwd_only) if args.cpu_seconds > 0 else None
+        acc = None
+        if not args.no_accuracy:
+            try:
+                acc = accuracy_of_workload(args, w, plan, out, chi, EM, EI, ED, fwd_only, dev)
+            except Exception as e:   # never lose the bench line to the checker
+                acc = {'error': repr(e)}
         line = {
             'metric': spec['metric'], 'value': value,
             'unit': 'cell-state updates/s', 'n_gpus': ws, 'steps': args.steps, 'warmup': args.warmup,

@@ -178,12 +178,18 @@ int phmm_estep_ws(phmm_plan *plan, const phmm_batch *batch, void *workspace,
  * address up (cudaGetSymbolAddress, with that device current); make that
  * first call before any stream capture.  A batch whose scratch would exceed
  * the array is rejected with PHMM_E_ARG and a message giving the bytes it
- * needs (at 17 states a call holds about 0.4 M lattice cells, e.g. 16 pairs
- * of 150 x 150).  Every call shares the array and the static host staging
- * it uses, and the array keeps the last call's contents: each call clears
- * the counters it needs, but calls that overlap -- on the GPU, on different
- * streams, or from different host threads -- race and must be serialised by
- * the caller. */
+ * needs.  Capacity at 17 states: the lattice is kept in 64-row stripes of
+ * (64 + Ly) x 64 cells at 68 bytes a cell (16 floats and an exponent), so
+ * the array holds about 490 k stripe cells -- e.g. 11 pairs of 150 x 150
+ * (3 stripes each), or one pair of about 1000 x 1000.  Every call shares the
+ * array and the static host staging it uses, and the array keeps the last
+ * call's contents: each call clears the counters it needs, but calls that
+ * overlap -- on the GPU, on different streams, or from different host
+ * threads -- race and must be serialised by the caller.  The device address
+ * is cached per device ordinal for the life of the process: after
+ * cudaDeviceReset (or any other re-creation of the device's primary
+ * context) the cached address belongs to the old context, and calls on that
+ * device are not supported. */
 #define PHMM_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
 int phmm_estep_static(const phmm_model_desc *model, const phmm_batch *batch,
                       double *ll_out, double *n_trans, double *cnt_M, double *cnt_I,
@@ -411,6 +417,15 @@ int phmm_kernel_time(phmm_plan *plan, int which, float *ms);
  * counterpart in the reference (it has no kernels). */
 int phmm_set_variant(phmm_plan *plan, int variant);
 int phmm_last_variant(const phmm_plan *plan);
+
+/* Bound of every inter-CTA wait of this plan's kernels, in polling
+ * iterations (each a poll and a 128 ns sleep); 0 restores the default of
+ * 40 M (about 5 s).  A wait that reaches the bound sets PHMM_ST_TIMEOUT on
+ * its pair, releases the stripes waiting on it and returns, so the launch
+ * always completes; after the call such a pair's log-likelihood is NEG_INF
+ * (-1e30) and its counts are undefined.  Diagnostic (a test shortens the
+ * bound to exercise that path); no counterpart in the reference. */
+int phmm_set_spin_limit(phmm_plan *plan, long long iterations);
 
 /* Number of kernel launches issued by the last call on this plan. */
 int phmm_last_launch_count(const phmm_plan *plan);

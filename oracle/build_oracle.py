@@ -1,5 +1,6 @@
 """Build the C half of the oracle (TEST INFRASTRUCTURE ONLY): oracle/fb2d.c
-compiled with the host C compiler into oracle/_build/liboracle.so.  Called by
+compiled with the host C compiler into oracle/_build/liboracle.so, with
+OpenMP where the compiler has it (serial otherwise).  Called by
 __graft_entry__.build(); skipped when the library is newer than its source."""
 from __future__ import annotations
 
@@ -20,8 +21,10 @@ def build(force=False):
         raise RuntimeError('no C compiler for the oracle')
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     tmp = LIB + '.tmp'
-    subprocess.run([cc, '-O2', '-fPIC', '-shared', '-std=c99', SRC, '-o', tmp, '-lm'], check=True,
-                   capture_output=True, text=True)
+    base = [cc, '-O2', '-fPIC', '-shared', '-std=c99', SRC, '-o', tmp]
+    res = subprocess.run(base[:1] + ['-fopenmp'] + base[1:] + ['-lm'], capture_output=True, text=True)
+    if res.returncode != 0:   # no OpenMP runtime: the serial build
+        subprocess.run(base + ['-lm'], check=True, capture_output=True, text=True)
     os.replace(tmp, LIB)
     return LIB
 

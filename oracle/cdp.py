@@ -31,8 +31,16 @@ def _lib():
                                            ctypes.c_int, ctypes.c_int, i32, i32, dp, dp, ctypes.c_double,
                                            dp, dp, dp]
         lib.oracle_char_counts.restype = None
+        lib.oracle_set_threads.argtypes = [ctypes.c_int]
+        lib.oracle_set_threads.restype = ctypes.c_int
         _L = lib
     return _L
+
+
+def set_threads(n):
+    """Host threads of the C oracle's anti-diagonal loops (1 = serial; the
+    library's OpenMP default is every core).  Returns the number in use."""
+    return int(_lib().oracle_set_threads(int(n)))
 
 
 def forward_backward(log_trans, state_types, emit, forward_only=False, counts=None):

@@ -15,15 +15,34 @@
  *            exp(F[src, s] + logT[s, k] + e[dst, k] + B[dst, k] - LL), plus
  *            n[s, E] += exp(F[Lx, Ly, s] + logT[s, E] - LL).
  * NEG_INF is -1e30 and is summed like any other number, as the reference does.
- * Cells in anti-diagonal order; all tables are caller-owned (no allocation).
- * Built by oracle/build_oracle.py with the host C compiler. */
+ * Cells in anti-diagonal order.  The cells of one anti-diagonal are
+ * independent, so with OpenMP (oracle/build_oracle.py builds with -fopenmp
+ * where the compiler has it) they run on oracle_set_threads() host threads;
+ * each cell's arithmetic is the same as in the serial loop, and the count
+ * sums are per-thread partials added in thread order.  The tables are
+ * caller-owned; only the per-thread count partials are allocated here. */
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define NEG_INF (-1e30)
 
 enum { TS = 0, TM = 1, TI = 2, TD = 3, TE = 4 };
+
+/* Host threads of the following calls (1 = serial); returns the number in use. */
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
 
 static double lse(const double *v, int n) {
     double m = v[0];
@@ -48,7 +67,9 @@ double oracle_fb2d(int N, const int8_t *st, const double *lt, int Lx, int Ly, co
     F[0] = 0.0;   /* state 0 is the start */
     for (int d = 1; d <= Lx + Ly; ++d) {
         const int ilo = d - Ly > 0 ? d - Ly : 0, ihi = d < Lx ? d : Lx;
+#pragma omp parallel for schedule(static) if (ihi - ilo >= 32)
         for (int i = ilo; i <= ihi; ++i) {
+            double tv[N];
             const int j = d - i;
             double *out = AT(F, i, j);
             const double *e = AT(emit, i, j);
@@ -58,8 +79,8 @@ double oracle_fb2d(int N, const int8_t *st, const double *lt, int Lx, int Ly, co
                 else if (st[k] == TI && j >= 1) pred = AT(F, i, j - 1);
                 else if (st[k] == TD && i >= 1) pred = AT(F, i - 1, j);
                 if (!pred) { out[k] = NEG_INF; continue; }
-                for (int s = 0; s < N; ++s) tmp[s] = pred[s] + lt[s * N + k];
-                out[k] = lse(tmp, N) + e[k];
+                for (int s = 0; s < N; ++s) tv[s] = pred[s] + lt[s * N + k];
+                out[k] = lse(tv, N) + e[k];
             }
         }
     }
@@ -71,7 +92,9 @@ double oracle_fb2d(int N, const int8_t *st, const double *lt, int Lx, int Ly, co
     for (int s = 0; s < N; ++s) AT(B, Lx, Ly)[s] = lt[s * N + e_idx];
     for (int d = Lx + Ly - 1; d >= 0; --d) {
         const int ilo = d - Ly > 0 ? d - Ly : 0, ihi = d < Lx ? d : Lx;
+#pragma omp parallel for schedule(static) if (ihi - ilo >= 32)
         for (int i = ilo; i <= ihi; ++i) {
+            double tv[N];
             const int j = d - i;
             double *out = AT(B, i, j);
             for (int s = 0; s < N; ++s) {
@@ -83,27 +106,47 @@ double oracle_fb2d(int N, const int8_t *st, const double *lt, int Lx, int Ly, co
                     else if (st[k] == TD) { ni = i + 1; nj = j; }
                     else continue;
                     if (ni > Lx || nj > Ly) continue;
-                    tmp[n++] = lt[s * N + k] + AT(emit, ni, nj)[k] + AT(B, ni, nj)[k];
+                    tv[n++] = lt[s * N + k] + AT(emit, ni, nj)[k] + AT(B, ni, nj)[k];
                 }
-                out[s] = n ? lse(tmp, n) : NEG_INF;
+                out[s] = n ? lse(tv, n) : NEG_INF;
             }
         }
     }
     memset(n_trans, 0, sizeof(double) * (size_t)N * N);
-    for (int i = 0; i <= Lx; ++i)
-        for (int j = 0; j <= Ly; ++j) {
-            const double *f = AT(F, i, j);
-            for (int k = 0; k < N; ++k) {
-                int ni, nj;
-                if (st[k] == TM) { ni = i + 1; nj = j + 1; }
-                else if (st[k] == TI) { ni = i; nj = j + 1; }
-                else if (st[k] == TD) { ni = i + 1; nj = j; }
-                else continue;
-                if (ni > Lx || nj > Ly) continue;
-                const double w = AT(emit, ni, nj)[k] + AT(B, ni, nj)[k] - ll;
-                for (int s = 0; s < N; ++s) n_trans[s * N + k] += exp(f[s] + lt[s * N + k] + w);
+    int nth = 1;
+#ifdef _OPENMP
+    nth = (Lx + 1) * (Ly + 1) >= 4096 ? omp_get_max_threads() : 1;
+#endif
+    double *part = nth > 1 ? (double *)calloc((size_t)nth * N * N, sizeof(double)) : NULL;
+    if (!part) nth = 1;
+#pragma omp parallel num_threads(nth) if (nth > 1)
+    {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        double *acc = nth > 1 ? part + (size_t)tid * N * N : n_trans;
+#pragma omp for schedule(static)
+        for (int i = 0; i <= Lx; ++i)
+            for (int j = 0; j <= Ly; ++j) {
+                const double *f = AT(F, i, j);
+                for (int k = 0; k < N; ++k) {
+                    int ni, nj;
+                    if (st[k] == TM) { ni = i + 1; nj = j + 1; }
+                    else if (st[k] == TI) { ni = i; nj = j + 1; }
+                    else if (st[k] == TD) { ni = i + 1; nj = j; }
+                    else continue;
+                    if (ni > Lx || nj > Ly) continue;
+                    const double w = AT(emit, ni, nj)[k] + AT(B, ni, nj)[k] - ll;
+                    for (int s = 0; s < N; ++s) acc[s * N + k] += exp(f[s] + lt[s * N + k] + w);
+                }
             }
-        }
+    }
+    if (nth > 1) {
+        for (int t = 0; t < nth; ++t)
+            for (size_t q = 0; q < (size_t)N * N; ++q) n_trans[q] += part[(size_t)t * N * N + q];
+        free(part);
+    }
     for (int s = 0; s < N; ++s) n_trans[s * N + e_idx] += exp(last[s] + lt[s * N + e_idx] - ll);
 #undef AT
     return ll;

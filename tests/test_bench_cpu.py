@@ -46,3 +46,28 @@ def test_reference_arm_runs_on_the_cpu():
     assert line['cpu_baseline']['kind'] == 'port' and line['cpu_baseline']['cores'] >= 1
     assert line['e2e']['h2d_bytes_per_step'] == 0 and line['e2e']['d2h_bytes_per_step'] == 0
     assert line['higher_is_better'] is True and line['n_gpus'] >= 1
+
+
+def test_accuracy_leg_every_pair_and_a_planted_error():
+    """bench.py's accuracy leg checks every pair: the oracle's own outputs
+    report zero error, and an error planted in one pair's copy is found."""
+    import numpy as np
+    bench = _bench()
+    from oracle import build_oracle, cdp
+    build_oracle.build()
+    from pairhmm import synth
+    w = synth.make_mixdom2_workload('small', 2, 1, 1, 20, ('loguniform', 5, 40), seed=3)
+    gpu = {'ll': np.zeros(20), 'n_trans': np.zeros((20, 12, 12)), 'cnt_M': np.zeros((20, 2, 21, 21)),
+           'cnt_I': np.zeros((20, 2, 21)), 'cnt_D': np.zeros((20, 2, 21))}
+    from oracle import pool
+    cases = [tuple(bench._oracle_model(w, b)) + (w.xs[b], w.ys[b]) for b in range(20)]
+    for b, (ll, n, (cM, cI, cD)) in enumerate(pool.estep_pairs(cases, cores=2)):
+        gpu['ll'][b], gpu['n_trans'][b], gpu['cnt_M'][b], gpu['cnt_I'][b], gpu['cnt_D'][b] = ll, n, cM, cI, cD
+    acc = bench.accuracy_leg(w, gpu, False)
+    assert acc['pairs'] == 20 and acc['scope'] == 'every pair of the workload'
+    assert acc['ll_max_rel_err'] == 0.0 and acc['n_trans_max_rel_err'] == 0.0 and acc['counts_max_rel_err'] == 0.0
+    gpu['ll'][7] *= 1 + 3e-6
+    gpu['cnt_I'][11] *= 1 + 2e-5
+    acc = bench.accuracy_leg(w, gpu, False)
+    assert 2e-6 < acc['ll_max_rel_err'] < 4e-6
+    assert 1e-5 < acc['counts_max_rel_err'] < 3e-5

@@ -4,10 +4,12 @@ It exists for callers whose process already owns the GPU memory (a JAX
 runtime that reserved most of the device, a serving framework's allocator):
 they cannot let this library cudaMalloc scratch.  The entry point runs the
 E-step kernels on a fixed file-scope device array instead.  This test calls
-it through the C ABI, twice in a row, and checks each result against
-phmm_estep (which allocates its scratch through a plan), with the bars the
-other GPU tests use; it also checks that an oversized batch is refused with
-a clear message.  The file is named to be collected last.
+it through the C ABI, twice in a row, and checks each result against the FP64
+oracle and against phmm_estep (which allocates its scratch through a plan),
+with the bars the other GPU tests use; it checks that repeated calls,
+including a larger batch that still fits, leave the device's free memory
+unchanged; and that an oversized batch is refused with a clear message.  The
+file is named to be collected last.
 """
 import ctypes
 
@@ -19,7 +21,7 @@ LL_RTOL = 1e-6
 CNT_RTOL = 1e-5
 
 
-def _model_and_batch(n_pairs, max_len, seed, fixed_len=None):
+def _model_and_batch(n_pairs, max_len, seed, fixed_len=None, with_oracle=False):
     import torch
     from pairhmm import _lib, synth
     from pairhmm import models as pm
@@ -36,7 +38,14 @@ def _model_and_batch(n_pairs, max_len, seed, fixed_len=None):
     st = pm.mixdom_state_types(3, 1)
     gr = pm.mixdom_state_groups(3, 1)
     batch = _lib.make_batch(xs, ys, chi, EM, EI, ED, device='cuda')
-    return st, gr, batch
+    if not with_oracle:
+        return st, gr, batch
+    from oracle import estep as oe, pool
+    cases = []
+    for b in range(n_pairs):
+        ochi, ost, ogr, oEM, oEI, oED, _ = oe.mixdom2_model(dict(p, t=float(ts[b])))
+        cases.append((ochi, ost, ogr, oEM, oEI, oED, xs[b], ys[b]))
+    return st, gr, batch, pool.estep_pairs(cases)
 
 
 def _outputs(P, N, G):
@@ -72,11 +81,12 @@ def _close(got, want, rtol):
     assert np.abs(got - want).max() <= rtol * scale + 1e-12
 
 
-def test_static_estep_matches_plan_estep_twice(cuda_lib):
+def test_static_estep_matches_oracle_and_plan_estep_twice(cuda_lib):
     import torch
     from pairhmm import _lib
+    from oracle import pool
     lib = cuda_lib
-    st, gr, batch = _model_and_batch(12, 120, seed=4)
+    st, gr, batch, oracle = _model_and_batch(12, 120, seed=4, with_oracle=True)
     N, G = len(st), 3
     plan = _lib.Plan(st, gr, G)
     want = _lib.estep(plan, batch)
@@ -93,6 +103,35 @@ def test_static_estep_matches_plan_estep_twice(cuda_lib):
         assert np.all(np.abs(ll - llw) <= LL_RTOL * np.abs(llw)), call
         for k in ('n_trans', 'cnt_M', 'cnt_I', 'cnt_D'):
             _close(out[k], want[k], CNT_RTOL)
+        # and against the FP64 oracle, pair by pair
+        host = {k: v.cpu().numpy() for k, v in out.items()}
+        for b, (oll, n, cnt) in enumerate(oracle):
+            assert abs(host['ll'][b] - oll) <= LL_RTOL * abs(oll), (call, b, host['ll'][b], oll)
+            for key, w in zip(('n_trans', 'cnt_M', 'cnt_I', 'cnt_D'), (n, *cnt)):
+                abs_of_max, rel = pool.count_errors(host[key][b], w)
+                assert abs_of_max <= CNT_RTOL and rel < CNT_RTOL, (call, b, key, abs_of_max, rel)
+
+
+def test_static_estep_allocates_nothing(cuda_lib):
+    """After a first call (which loads the kernels and looks the array up),
+    further calls -- among them a larger batch that still fits -- leave the
+    device's free memory exactly where it was."""
+    import torch
+    from pairhmm import _lib
+    lib = cuda_lib
+    st, gr, small = _model_and_batch(6, 90, seed=8)
+    _, _, large = _model_and_batch(10, 0, seed=9, fixed_len=150)   # about 410 k stripe cells
+    N, G = len(st), 3
+    outs = [_outputs(small.n_pairs, N, G), _outputs(large.n_pairs, N, G)]
+    assert _static_call(lib, st, gr, G, small, outs[0]) == 0, _lib.last_error()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for batch, out in ((large, outs[1]), (small, outs[0]), (large, outs[1])):
+        assert _static_call(lib, st, gr, G, batch, out) == 0, _lib.last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert (outs[1]['status'] == 0).all() and torch.isfinite(outs[1]['ll']).all()
 
 
 def test_static_estep_refuses_oversized_batch(cuda_lib):

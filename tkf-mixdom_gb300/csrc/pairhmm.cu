@@ -53,6 +53,9 @@ constexpr int NBIN = 441 + 21 + 21;
 constexpr int EXP_NONE = -(1 << 28);
 constexpr double LN2 = 0.69314718055994530942;
 constexpr double NEG_INF_LL = -1e30;  // reference NEG_INF (dp/hmm.py:108)
+// iterations of a bounded inter-CTA wait (each one poll plus a 128 ns sleep:
+// about 5 s) unless phmm_set_spin_limit chose another bound
+constexpr long long kSpinLimit = 40LL * 1000 * 1000;
 enum { T_S = 0, T_M = 1, T_I = 2, T_D = 3, T_E = 4, T_NONE = 5 };
 
 struct PairMeta {
@@ -961,6 +964,7 @@ struct phmm_plan {
                             // 7 split E-step on two-warp stripes
     bool two_warp = false;  // the last warp-family call ran the two-warp stripe kernels
     int last_variant = 0;
+    long long spin_limit = 0;   // bound of the inter-CTA waits (0: kSpinLimit)
 };
 
 namespace {
@@ -1309,7 +1313,7 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     K.cntD = cntD;
     K.F_log = K.B_log = K.post = nullptr;
     K.max_ly = max_ly;
-    K.spin_limit = 40LL * 1000 * 1000;
+    K.spin_limit = plan->spin_limit > 0 ? plan->spin_limit : kSpinLimit;
     K.wave_ctr = nullptr;
     K.cmask = nullptr;
     K.beam_scale = 0.f;
@@ -1372,9 +1376,9 @@ struct NvtxRange {
     ~NvtxRange() { nvtxRangePop(); }
 };
 
-int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_trans,
-        double *cntM, double *cntI, double *cntD, int32_t *status, double *F_log, double *B_log,
-        double *post, void *stream_, void *ws = nullptr, size_t ws_bytes = 0, size_t *ws_need = nullptr) {
+int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_trans,
+             double *cntM, double *cntI, double *cntD, int32_t *status, double *F_log, double *B_log,
+             double *post, void *stream_, void *ws, size_t ws_bytes, size_t *ws_need) {
     if (!plan || !b) return fail(PHMM_E_ARG, "null plan or batch");
     cudaStream_t stream = (cudaStream_t)stream_;
     if (!ws_need) plan->launches = 0;
@@ -1624,7 +1628,7 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     K.B_log = B_log;
     K.post = post;
     K.max_ly = max_ly;
-    K.spin_limit = 40LL * 1000 * 1000;
+    K.spin_limit = plan->spin_limit > 0 ? plan->spin_limit : kSpinLimit;
     K.wave_ctr = nullptr;
     K.cmask = b->cell_mask;
     K.beam_scale = b->beam_log_width > 0.0 ? (float)exp(-b->beam_log_width) : 0.f;
@@ -1658,6 +1662,35 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
     plan->timed_bwd = estep;
     plan->timed_count = false;
     return 0;
+}
+
+// A pair whose wavefront or count pass gave up a bounded wait (status bit
+// PHMM_ST_TIMEOUT, set by whichever kernel timed out) has incomplete lattices;
+// after the call's kernels its log-likelihood becomes the reference's failure
+// value NEG_INF, whatever the kernels wrote, so a caller filtering on the
+// log-likelihood (train_pfam.py:2859) drops it.
+__global__ void timeout_epilogue_kernel(double *ll, const int32_t *status, int n) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n && (status[p] & PHMM_ST_TIMEOUT)) ll[p] = NEG_INF_LL;
+}
+
+int launch_timeout_epilogue(double *ll, const int32_t *status, int n, cudaStream_t stream) {
+    if (n <= 0) return 0;
+    timeout_epilogue_kernel<<<(n + 255) / 256, 256, 0, stream>>>(ll, status, n);
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+// One call of the kernels (run_core) followed by the timeout epilogue.
+int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_trans,
+        double *cntM, double *cntI, double *cntD, int32_t *status, double *F_log, double *B_log,
+        double *post, void *stream_, void *ws = nullptr, size_t ws_bytes = 0, size_t *ws_need = nullptr) {
+    const int rc = run_core(plan, b, estep, ll, n_trans, cntM, cntI, cntD, status, F_log, B_log, post, stream_,
+                            ws, ws_bytes, ws_need);
+    if (rc || ws_need || b->n_pairs <= 0) return rc;
+    const int rc2 = launch_timeout_epilogue(ll, status, b->n_pairs, (cudaStream_t)stream_);
+    if (!rc2) plan->launches++;
+    return rc2;
 }
 
 template <class SH>
@@ -2020,6 +2053,12 @@ int phmm_set_variant(phmm_plan *plan, int variant) {
 
 int phmm_last_variant(const phmm_plan *plan) { return plan ? plan->last_variant : 0; }
 
+int phmm_set_spin_limit(phmm_plan *plan, long long iterations) {
+    if (!plan || iterations < 0) return fail(PHMM_E_ARG, "null plan or negative spin limit");
+    plan->spin_limit = iterations;
+    return 0;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------- allocation-free E-step
@@ -2130,6 +2169,7 @@ int static_model(const phmm_model_desc *md, KParams *K, int *nm, int *ni, int *n
 extern "C" int phmm_estep_static(const phmm_model_desc *md, const phmm_batch *b, double *ll,
                                  double *n_trans, double *cntM, double *cntI, double *cntD,
                                  int32_t *status, void *stream_) {
+    NvtxRange range("phmm_estep_static");
     if (!b) return fail(PHMM_E_ARG, "null batch");
     KParams K;
     int nm = 0, ni = 0, nd = 0, rc;
@@ -2249,7 +2289,7 @@ extern "C" int phmm_estep_static(const phmm_model_desc *md, const phmm_batch *b,
     K.cntD = cntD;
     K.F_log = K.B_log = K.post = nullptr;
     K.max_ly = max_ly;
-    K.spin_limit = 40LL * 1000 * 1000;
+    K.spin_limit = kSpinLimit;
     K.wave_ctr = nullptr;
     K.cmask = nullptr;
     K.beam_scale = 0.f;
@@ -2274,5 +2314,5 @@ extern "C" int phmm_estep_static(const phmm_model_desc *md, const phmm_batch *b,
             CUDA_TRY(cudaGetLastError());
         }
     }
-    return 0;
+    return launch_timeout_epilogue(ll, status, P_, stream);
 }

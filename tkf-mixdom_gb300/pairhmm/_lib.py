@@ -20,7 +20,7 @@ _LIB = None
 EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep',
            'phmm_estep_tables', 'phmm_workspace_bytes', 'phmm_forward_ws', 'phmm_estep_ws',
            'phmm_estep_static', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_kernel_time',
-           'phmm_set_variant',
+           'phmm_set_variant', 'phmm_set_spin_limit',
            'phmm_last_variant', 'phmm_last_launch_count',
            'phmm_last_error', 'phmm_version', 'phmm_mixdom2_class_subs_count', 'phmm_mixdom2_tables',
            'phmm_mixdom2_class_counts', 'phmm_tkf92_tables', 'phmm_mixdom2_chi',
@@ -114,6 +114,8 @@ def load(path=None):
     lib.phmm_kernel_times.restype = ctypes.c_int
     lib.phmm_kernel_time.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
     lib.phmm_kernel_time.restype = ctypes.c_int
+    lib.phmm_set_spin_limit.argtypes = [vp, ctypes.c_longlong]
+    lib.phmm_set_spin_limit.restype = ctypes.c_int
     lib.phmm_set_variant.argtypes = [vp, ctypes.c_int]
     lib.phmm_set_variant.restype = ctypes.c_int
     lib.phmm_last_variant.argtypes = [vp]
@@ -221,6 +223,12 @@ class Plan:
 
     def set_timing(self, enable=True):
         _check(self.lib.phmm_set_timing(self.handle, int(enable)), 'phmm_set_timing')
+
+    def set_spin_limit(self, iterations=0):
+        """Bound of the kernels' inter-CTA waits in polling iterations (0: the
+        default, about 5 s); a wait that reaches it marks its pair
+        PHMM_ST_TIMEOUT with a NEG_INF log-likelihood (phmm_set_spin_limit)."""
+        _check(self.lib.phmm_set_spin_limit(self.handle, int(iterations)), 'phmm_set_spin_limit')
 
     def kernel_time(self, which):
         """Device ms of kernel `which` (0 forward, 1 backward, 2 split count pass)

@@ -416,7 +416,7 @@ def accuracy_of_workload(args, w, plan, out, chi, EM, EI, ED, fwd_only, dev):
     if float(w.cells().sum()) * N * N <= 1.5e11:
         gpu = {k: v.cpu().numpy() for k, v in out.items()}
         return accuracy_leg(w, gpu, fwd_only)
-    a = 600 if N * N * 601 * 601 <= 1e10 else 300
+    a = 1000 if N * N * 1001 * 1001 <= 3e10 else 400
     pick = [int(i) for i in np.argsort(w.cells())[:2]]
     from pairhmm.synth import Workload
     sub = Workload(w.name, w.model, w.params, [w.xs[b][:a] for b in pick], [w.ys[b][:a] for b in pick],

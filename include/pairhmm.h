@@ -158,6 +158,22 @@ int phmm_estep_ws(phmm_plan *plan, const phmm_batch *batch, void *workspace,
                   double *cnt_M, double *cnt_I, double *cnt_D,
                   int32_t *status_out, void *stream);
 
+/* phmm_estep_ws in two halves, for a caller that captures the E-step in a
+ * CUDA graph: phmm_estep_ws_prepare copies the batch's work description
+ * (pair metadata and work lists, built on the host from the lengths) into
+ * the workspace, stream-ordered; phmm_estep_ws_launch then issues only the
+ * device work of phmm_estep_ws (clearing counters and outputs, the kernels)
+ * and copies nothing from the host, so it can be captured and replayed
+ * while the workspace keeps that description -- the same batch lengths,
+ * plan and workspace on every launch (the residues, tables and outputs may
+ * change between launches).  No counterpart in the reference, whose
+ * per-shape jit cache (train_pfam.py:1674-1741) plays this role. */
+int phmm_estep_ws_prepare(phmm_plan *plan, const phmm_batch *batch, void *workspace, size_t workspace_bytes,
+                          void *stream);
+int phmm_estep_ws_launch(phmm_plan *plan, const phmm_batch *batch, void *workspace, size_t workspace_bytes,
+                         double *ll_out, double *n_trans, double *cnt_M, double *cnt_I, double *cnt_D,
+                         int32_t *status_out, void *stream);
+
 /* E-step that allocates nothing: no cudaMalloc, cudaFree or other allocating
  * call.  No counterpart in the reference.
  *
@@ -226,6 +242,26 @@ size_t phmm_mixdom2_class_subs_count(const phmm_mixdom2_params *prm, int32_t n_p
 int phmm_mixdom2_tables(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t,
                         float *chi, float *emit_M, float *emit_I, float *emit_D,
                         double *class_subs, void *stream);
+
+/* The same prologue with the parameters in device memory, for a captured
+ * CUDA graph (a by-value parameter block would be frozen in the graph):
+ * phmm_mixdom2_param_block fills a host block of
+ * phmm_mixdom2_param_block_bytes() bytes from the parameters (the same
+ * checks as phmm_mixdom2_tables); the caller copies it to a device block
+ * (stream-ordered, e.g. from pinned memory inside the graph) and passes that
+ * to phmm_mixdom2_tables_dp / phmm_mixdom2_class_counts_dp with the n_dom,
+ * n_frag and n_classes it was filled from.  Outputs as phmm_mixdom2_tables
+ * and phmm_mixdom2_class_counts. */
+size_t phmm_mixdom2_param_block_bytes(void);
+int phmm_mixdom2_param_block(const phmm_mixdom2_params *prm, void *host_block, size_t bytes);
+int phmm_mixdom2_tables_dp(const void *param_block, int32_t n_dom, int32_t n_frag, int32_t n_classes,
+                           int32_t n_pairs, const double *t, float *chi, float *emit_M, float *emit_I,
+                           float *emit_D, double *class_subs, void *stream);
+int phmm_mixdom2_class_counts_dp(const void *param_block, int32_t n_dom, int32_t n_frag, int32_t n_classes,
+                                 int32_t n_pairs, const double *class_subs, const double *cnt_M,
+                                 const double *cnt_I, const double *cnt_D, double *class_match,
+                                 double *class_insert, double *class_delete, double *classdist_counts,
+                                 void *stream);
 
 /* The collapsed chi alone (float32 and, when chi64 is not null, float64
  * [P][N][N]) for the gradient path, and its vector-Jacobian product:
@@ -390,6 +426,17 @@ int phmm_holmes_rubin(int32_t n_classes, int32_t alphabet, const double *class_Q
                       int32_t n_pairs, const double *t, const double *class_match_counts, double *W, double *U,
                       void *stream);
 
+/* phmm_holmes_rubin with its per-class blocks (the host eigendecomposition
+ * of each class rate matrix) in device memory, for a captured CUDA graph:
+ * phmm_holmes_rubin_block fills phmm_holmes_rubin_block_bytes(n_classes)
+ * host bytes; the caller copies them to the device block passed to
+ * phmm_holmes_rubin_dp.  Results as phmm_holmes_rubin. */
+size_t phmm_holmes_rubin_block_bytes(int32_t n_classes);
+int phmm_holmes_rubin_block(int32_t n_classes, int32_t alphabet, const double *class_Q, const double *class_pis,
+                            void *host_block, size_t bytes);
+int phmm_holmes_rubin_dp(const void *block, int32_t n_classes, int32_t n_pairs, const double *t,
+                         const double *class_match_counts, double *W, double *U, void *stream);
+
 /* Per-kernel CUDA-event timing on the launching stream (diagnostics and
  * benchmarking; no counterpart in the reference, which has no kernels).
  * phmm_kernel_times waits for the last call's events and returns the forward
@@ -426,6 +473,45 @@ int phmm_last_variant(const phmm_plan *plan);
  * (-1e30) and its counts are undefined.  Diagnostic (a test shortens the
  * bound to exercise that path); no counterpart in the reference. */
 int phmm_set_spin_limit(phmm_plan *plan, long long iterations);
+
+/* Launch configuration of a plan (what the project's autotuner searches,
+ * pairhmm/autotune.py; no counterpart in the reference, whose XLA compiler
+ * chooses its own):
+ *   variant       kernel family as phmm_set_variant (0 automatic);
+ *   wave_per_sm   resident CTAs per SM of each persistent wavefront grid
+ *                 (0: half the slots each for the split E-step's two
+ *                 wavefronts, all of them for the wide family);
+ *   count_per_sm  CTAs per SM of the split E-step's count grid that runs
+ *                 beside the wavefronts (-1: half the slots; 0: none, every
+ *                 count item then runs once both wavefronts are done);
+ *   priorities    1: the wavefronts run on streams of the greatest priority
+ *                 and the count grids on streams of the least, so SM slots
+ *                 freed while both wait go to the critical path first.
+ *   checkpoint    E-step on the wide kernels (more than 60 emitting
+ *                 states): 1 keeps no lattice -- the wavefronts keep only
+ *                 the edge rows every 32 rows (the checkpoints, about
+ *                 sqrt(L) of them for L x L), and the count pass recomputes
+ *                 each stripe from the edge rows above and below it, in
+ *                 groups of two stripes per SM; scratch is the edge rows plus
+ *                 one group instead of two whole lattices, for about a third
+ *                 more arithmetic.  2 never does this (a batch larger than
+ *                 the free memory runs as consecutive groups of pairs);
+ *                 0 (automatic) does it when one pair's lattices alone
+ *                 exceed 40 % of the device's memory.  The reference keeps
+ *                 its 2D tables within memory by recomputation too
+ *                 (jax.checkpoint on its log-likelihood VJPs,
+ *                 train/vjp.py:109-124).
+ * Results do not depend on the tuning (the same kernels and arithmetic on
+ * the same work items).  Defaults {0, 0, -1, 0, 0}. */
+typedef struct phmm_tuning {
+    int32_t variant;
+    int32_t wave_per_sm;
+    int32_t count_per_sm;
+    int32_t priorities;
+    int32_t checkpoint;
+} phmm_tuning;
+int phmm_set_tuning(phmm_plan *plan, const phmm_tuning *tuning);
+int phmm_get_tuning(const phmm_plan *plan, phmm_tuning *tuning);
 
 /* Number of kernel launches issued by the last call on this plan. */
 int phmm_last_launch_count(const phmm_plan *plan);

@@ -100,7 +100,8 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
     int *prog_mine = P.progress + m.stripe_base + si;
     const float *edge_above = P.edge + (m.edge_base + (int64_t)(si - 1) * (Ly + 1)) * ES;
     float *edge_mine = P.edge + (m.edge_base + (int64_t)si * (Ly + 1)) * ES;
-    const int64_t latc = m.lat_base + (int64_t)si * (RW + Ly) * RW;
+    const int64_t latc = P.stripe_lat ? P.stripe_lat[m.stripe_base + si] : m.lat_base + (int64_t)si * (RW + Ly) * RW;
+    const bool pub = !P.recompute;   // a recomputed stripe publishes nothing (its edge rows exist)
     float *chiS = sm + L.chi, *A = sm + L.A, *B = sm + L.B;
     int *E = reinterpret_cast<int *>(sm) + L.E;
     int *MX = reinterpret_cast<int *>(sm) + L.MX;
@@ -153,7 +154,7 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
     auto fetch_halo = [&](int col) -> bool {
         if (!has_above || col > Ly) return true;
         int ok = 1;
-        if (lane == 0) ok = wait_geq(prog_above, col + 1, P.spin_limit) ? 1 : 0;
+        if (lane == 0 && pub) ok = wait_geq(prog_above, col + 1, P.spin_limit) ? 1 : 0;
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (!ok) return false;
         const int bs = (col + 2) % 3, es = (col + 3) & 3;
@@ -183,7 +184,7 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
             if (t == 3) B[(0 * NS + P.s_slot) * BW + 1] = 0.f;
         }
         // ---- bottom row of step t-1 -> edge row for the stripe below (warp 1)
-        if (warp == (nt > 32 ? 1 : 0) && has_below && t >= 1) {
+        if (pub && warp == (nt > 32 ? 1 : 0) && has_below && t >= 1) {
             const int jb = t - 1 - (RW - 1);
             if (jb >= 0 && jb <= Ly) {
                 const int sl = (t - 1) % 3;
@@ -241,17 +242,56 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
 #pragma unroll
                 for (int u = 0; u < 4; ++u) acc[i][u] = 0.f;
             const float4 *ch4 = reinterpret_cast<const float4 *>(chiS) + qd;
-#pragma unroll 4
-            for (int s = 0; s < NS; ++s) {
-                const float4 pv = *reinterpret_cast<const float4 *>(base + s * stride);
-                const float4 cv = ch4[s * NQd];
-                const float pa[4] = {pv.x, pv.y, pv.z, pv.w};
-                const float ca[4] = {cv.x, cv.y, cv.z, cv.w};
+            // Above 64 slots, compensated blocked summation: 8 sources into a
+            // block tile, the block tile into the accumulator with a Kahan
+            // correction, so small terms are not lost against a large running
+            // sum (sequential float32 sums of ~160 positive terms drop small
+            // addends with a bias that the posteriors inherit: counts off by
+            // ~1e-5 at 162 states).  At 64 slots or fewer the plain sequential
+            // sum is kept: its forward and backward errors cancel in the
+            // posteriors, which blocking would undo.
+            const bool blocked = NS > 64;
+            float cmp[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) cmp[i][u] = 0.f;
+            auto block = [&](int s0, int nb) {
+                float bt[4][4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) acc[i][u] = fmaf(pa[i], ca[u], acc[i][u]);
-            }
+                    for (int u = 0; u < 4; ++u) bt[i][u] = blocked ? 0.f : acc[i][u];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    if (q < nb) {
+                        const float4 pv = *reinterpret_cast<const float4 *>(base + (s0 + q) * stride);
+                        const float4 cv = ch4[(s0 + q) * NQd];
+                        const float pa[4] = {pv.x, pv.y, pv.z, pv.w};
+                        const float ca[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+                        for (int i = 0; i < 4; ++i)
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) bt[i][u] = fmaf(pa[i], ca[u], bt[i][u]);
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        if (blocked) {
+                            const float y = bt[i][u] - cmp[i][u];
+                            const float tt = acc[i][u] + y;
+                            cmp[i][u] = (tt - acc[i][u]) - y;
+                            acc[i][u] = tt;
+                        } else {
+                            acc[i][u] = bt[i][u];
+                        }
+                    }
+            };
+            int s8 = 0;
+            for (; s8 + 8 <= NS; s8 += 8) block(s8, 8);
+            if (s8 < NS) block(s8, NS - s8);
             // emissions, scale, outputs
             float mxr[4];
 #pragma unroll
@@ -293,7 +333,7 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
                         reinterpret_cast<int *>(rec)[NS] = origin ? 0 : Eo[i];
                     }
                 }
-                if (valid[i] && row == Lx && j == Ly && si + 1 == m.n_stripes) {   // P(x,y): my quad's share
+                if (pub && valid[i] && row == Lx && j == Ly && si + 1 == m.n_stripes) {   // P(x,y): my quad's share
                     double a = 0.0;
 #pragma unroll
                     for (int u = 0; u < 4; ++u) a += (double)acc[i][u] * (double)sm[L.chiE + 4 * qd + u];
@@ -311,6 +351,7 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
         if (warp == 0 && t + 1 <= T_last && !fetch_halo(t + 1)) misc[(k + 1) & 1] = 1;
     }
     __syncthreads();
+    if (!pub) return;   // recomputed: the lattice records are all this stripe writes
     if (!aborted && has_below) {   // the last bottom-row cell(s) still to publish
         const int t = T_last + 1;
         const int jb = t - 1 - (RW - 1);
@@ -379,7 +420,8 @@ __device__ void bwd_rec_stripe_wd(const KParams &P, int p, int si, const SmemWd 
     int *prog_mine = P.bprogress + m.stripe_base + si;
     const float *edge_below = P.bedge + (m.edge_base + (int64_t)(si + 1) * (Ly + 1)) * ES;
     float *edge_mine = P.bedge + (m.edge_base + (int64_t)si * (Ly + 1)) * ES;
-    const int64_t latc = m.lat_base + (int64_t)si * (RW + Ly) * RW;
+    const int64_t latc = P.stripe_lat ? P.stripe_lat[m.stripe_base + si] : m.lat_base + (int64_t)si * (RW + Ly) * RW;
+    const bool pub = !P.recompute;   // a recomputed stripe publishes nothing (its edge rows exist)
     float *chiB = sm + L.chi, *A = sm + L.A, *B = sm + L.B;
     int *E = reinterpret_cast<int *>(sm) + L.E;
     int *MX = reinterpret_cast<int *>(sm) + L.MX;
@@ -426,7 +468,7 @@ __device__ void bwd_rec_stripe_wd(const KParams &P, int p, int si, const SmemWd 
     auto fetch_halo = [&](int col) -> bool {
         if (!has_below || col < 0 || col > Ly) return true;
         int ok = 1;
-        if (lane == 0) ok = wait_geq(prog_below, Ly + 1 - col, P.spin_limit) ? 1 : 0;
+        if (lane == 0 && pub) ok = wait_geq(prog_below, Ly + 1 - col, P.spin_limit) ? 1 : 0;
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (!ok) return false;
         const int bs = (col + RW) % 3, es = (col + RW) & 3;
@@ -440,7 +482,7 @@ __device__ void bwd_rec_stripe_wd(const KParams &P, int p, int si, const SmemWd 
     };
     // top row of step t (column t) -> edge row for the stripe above
     auto publish_top = [&](int t) {
-        if (!has_above || t < 0 || t > Ly) return;
+        if (!pub || !has_above || t < 0 || t > Ly) return;
         float *dst = edge_mine + (int64_t)t * ES;
         for (int k = lane; k < KS; k += 32) dst[k] = A[((t & 1) * KS + k) * RW + 0];
         if (lane == 0) {
@@ -506,17 +548,49 @@ __device__ void bwd_rec_stripe_wd(const KParams &P, int p, int si, const SmemWd 
                 for (int u = 0; u < 4; ++u) acc[i][u] = 0.f;
             const float4 *cb4 = reinterpret_cast<const float4 *>(chiB) + qs;   // chiB[k][4qs..]
             const int NQk = KS / 4;
+            // compensated blocked summation above 64 slots, as in the forward
+            // (8 destinations per block tile); the plain sequential sum below
+            const bool blocked = P.NS > 64;
+            float cmp[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) cmp[i][u] = 0.f;
             auto contract = [&](const float *base, int stride, int k0, int k1, const float (&sc)[4]) {
-#pragma unroll 2
-                for (int kk = k0; kk < k1; ++kk) {
-                    const float4 w = *reinterpret_cast<const float4 *>(base + kk * stride);
-                    const float4 c = cb4[kk * NQk];
-                    const float wa[4] = {w.x * sc[0], w.y * sc[1], w.z * sc[2], w.w * sc[3]};
-                    const float ca[4] = {c.x, c.y, c.z, c.w};
+                for (int kb = k0; kb < k1; kb += 8) {
+                    const int nb = min(8, k1 - kb);
+                    float bt[4][4];
 #pragma unroll
                     for (int i = 0; i < 4; ++i)
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) acc[i][u] = fmaf(wa[i], ca[u], acc[i][u]);
+                        for (int u = 0; u < 4; ++u) bt[i][u] = blocked ? 0.f : acc[i][u];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        if (q < nb) {
+                            const int kk = kb + q;
+                            const float4 w = *reinterpret_cast<const float4 *>(base + kk * stride);
+                            const float4 c = cb4[kk * NQk];
+                            const float wa[4] = {w.x * sc[0], w.y * sc[1], w.z * sc[2], w.w * sc[3]};
+                            const float ca[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+                            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                                for (int u = 0; u < 4; ++u) bt[i][u] = fmaf(wa[i], ca[u], bt[i][u]);
+                        }
+                    }
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            if (blocked) {
+                                const float y = bt[i][u] - cmp[i][u];
+                                const float tt = acc[i][u] + y;
+                                cmp[i][u] = (tt - acc[i][u]) - y;
+                                acc[i][u] = tt;
+                            } else {
+                                acc[i][u] = bt[i][u];
+                            }
+                        }
                 }
             };
             contract(B + ((t + 2) % 3) * KS * BW + r0 + 4, BW, kb0, ke0, sM);   // M: (row+1, t+2)
@@ -568,6 +642,7 @@ __device__ void bwd_rec_stripe_wd(const KParams &P, int p, int si, const SmemWd 
     __syncthreads();
     if (!aborted && warp == (nt > 32 ? 1 : 0)) publish_top(0);
     __syncthreads();
+    if (!pub) return;   // recomputed: the lattice records are all this stripe writes
     if (tid == 0) {
         if (has_above) { __threadfence(); st_release(prog_mine, Ly + 1); }
         if (aborted) atomicOr(P.status + p, PHMM_ST_TIMEOUT);
@@ -639,8 +714,11 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
     const int nrows = min(RW, Lx + 1 - i0);
     const bool has_below = si + 1 < m.n_stripes;
     const int ES = ls_of(NS);
-    const int64_t latc = m.lat_base + (int64_t)si * (RW + Ly) * RW;
+    const int64_t latc = P.stripe_lat ? P.stripe_lat[m.stripe_base + si] : m.lat_base + (int64_t)si * (RW + Ly) * RW;
     const int64_t latb = m.lat_base + (int64_t)(si + 1) * (RW + Ly) * RW;
+    // with checkpoints the stripe below's lattice is not kept: its row 0 is its
+    // backward edge row, whose records hold w = e b (the emission already applied)
+    const float *bedge_below = P.bedge + (m.edge_base + (int64_t)(si + 1) * (Ly + 1)) * ES;
     const int T_last = (nrows - 1) + Ly;
     if (nsq <= 0) return;
     if (P.count_wait) {   // the wavefronts may still run: wait for the stripes read here
@@ -688,6 +766,7 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
     // prefetched lattice data of one step
     int Ef = EXP_NONE, Eb = EXP_NONE;
     int Es[KQ];
+    bool sw[KQ];   // the successor record holds w = e b (a backward edge row), not b
     float4 sv[KQ], fv[FQ], bo[KQ];
     auto issue = [&](int t) {
         const int j = t - c;
@@ -697,7 +776,9 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
 #pragma unroll
         for (int a = 0; a < FQ; ++a) fv[a] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int a = 0; a < KQ; ++a) { Es[a] = EXP_NONE; sv[a] = make_float4(0.f, 0.f, 0.f, 0.f); bo[a] = sv[a]; }
+        for (int a = 0; a < KQ; ++a) {
+            Es[a] = EXP_NONE; sv[a] = make_float4(0.f, 0.f, 0.f, 0.f); bo[a] = sv[a]; sw[a] = false;
+        }
         if (!valid) return;
         Ef = __ldcg(reinterpret_cast<const int *>(P.lat + cell * ES) + NS);
         Eb = __ldcg(reinterpret_cast<const int *>(P.blat + cell * ES) + NS);
@@ -714,15 +795,19 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
             if (q >= NQd) continue;
             if (emis) bo[a] = __ldcg(reinterpret_cast<const float4 *>(P.blat + cell * ES) + q);
             const int qt = P.quad_type[q];
-            int64_t sc = -1;
-            if (qt == T_I && hI) sc = latc + (int64_t)(t + 1) * RW + c;
+            const float *rec = nullptr;
+            if (qt == T_I && hI) rec = P.blat + (latc + (int64_t)(t + 1) * RW + c) * ES;
             else if (qt == T_D && hD && below_ok)
-                sc = c + 1 < nrows ? latc + (int64_t)(t + 1) * RW + c + 1 : latb + (int64_t)j * RW;
+                rec = c + 1 < nrows ? P.blat + (latc + (int64_t)(t + 1) * RW + c + 1) * ES
+                                    : (P.ckpt ? bedge_below + (int64_t)j * ES : P.blat + (latb + (int64_t)j * RW) * ES);
             else if (qt == T_M && hM && below_ok)
-                sc = c + 1 < nrows ? latc + (int64_t)(t + 2) * RW + c + 1 : latb + (int64_t)(j + 1) * RW;
-            if (sc >= 0) {
-                Es[a] = __ldcg(reinterpret_cast<const int *>(P.blat + sc * ES) + NS);
-                sv[a] = __ldcg(reinterpret_cast<const float4 *>(P.blat + sc * ES) + q);
+                rec = c + 1 < nrows ? P.blat + (latc + (int64_t)(t + 2) * RW + c + 1) * ES
+                                    : (P.ckpt ? bedge_below + (int64_t)(j + 1) * ES
+                                              : P.blat + (latb + (int64_t)(j + 1) * RW) * ES);
+            if (rec) {
+                Es[a] = __ldcg(reinterpret_cast<const int *>(rec) + NS);
+                sv[a] = __ldcg(reinterpret_cast<const float4 *>(rec) + q);
+                sw[a] = P.ckpt && c + 1 >= nrows && qt != T_I;
             }
         }
     };
@@ -757,7 +842,7 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
                     const int xi = qt == T_I ? xc : xn, yy = qt == T_D ? yj : yn;
                     float e[4];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) e[u] = emit_g(P, eMg, eIg, eDg, 4 * q + u, xi, yy);
+                    for (int u = 0; u < 4; ++u) e[u] = sw[a] ? 1.f : emit_g(P, eMg, eIg, eDg, 4 * q + u, xi, yy);
                     uu = make_float4(sv[a].x * e[0] * us, sv[a].y * e[1] * us, sv[a].z * e[2] * us, sv[a].w * e[3] * us);
                 }
                 *reinterpret_cast<float4 *>(ust + c * UW + 4 * q) = uu;

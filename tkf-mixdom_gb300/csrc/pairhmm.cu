@@ -106,6 +106,13 @@ struct KParams {
     const int *wave_ctr;                // overlapped count pass: forward, backward claim counters
     const unsigned char *cmask;         // per-cell type mask (bit 0 M, 1 I, 2 D) at tab_base, or null
     float beam_scale;                   // > 0: forward states below max * beam_scale pruned (generic kernels)
+    // wide kernels, stripe-edge checkpointing: lattice cell offset of each
+    // stripe (global stripe index) in the current group's scratch, or null
+    // for the full-lattice layout (PairMeta::lat_base)
+    const int64_t *stripe_lat;
+    int recompute;                      // 1: stripes recomputed from complete edge rows (no waits, no
+                                        // edge / progress / log-likelihood writes)
+    int ckpt;                           // count pass: row 0 of the stripe below from its backward edge row
 };
 
 struct SmemLayout {
@@ -944,8 +951,15 @@ struct phmm_plan {
     int *blat_exp = nullptr; size_t blatE_cap = 0;
     float *bedge = nullptr; size_t bedge_cap = 0;
     int *bedge_exp = nullptr; size_t bedgeE_cap = 0;
+    int64_t *slat = nullptr; size_t slat_cap = 0;    // checkpointed wide E-step: stripe offsets per group
     // split E-step: one side stream (+ fork / join events) per caller stream
-    struct Side { cudaStream_t user, side, side2, side3; cudaEvent_t fork, join, join2, join3, fwd_done; };
+    // (prio: the wavefront streams were created at the greatest priority and the
+    // count streams at the least, and the forward runs on sidef)
+    struct Side {
+        cudaStream_t user, side, side2, side3, sidef;
+        cudaEvent_t fork, join, join2, join3, fwd_done, joinf;
+        bool prio;
+    };
     std::vector<Side> sides;
     std::vector<PairMeta> h_meta;
     std::vector<int2> h_items;
@@ -960,11 +974,18 @@ struct phmm_plan {
     // register-resident warp kernels for this state space (null: generic kernels)
     int w_nm = 0, w_ni = 0, w_nd = 0;
     int grid_div = 1;       // persistent grids use 1/grid_div of the resident slots
+    int launch_per_sm = 0;  // > 0: the next launch takes this many resident CTAs per SM (at most occ)
+    phmm_tuning tuning = {0, 0, -1, 0, 0};   // phmm_set_tuning (variant is `variant` below)
     int variant = 0;        // 0 automatic, 1 generic, 2 warp, 3 block, 4/5 split warp/block E-step, 6 wide,
                             // 7 split E-step on two-warp stripes
     bool two_warp = false;  // the last warp-family call ran the two-warp stripe kernels
     int last_variant = 0;
     long long spin_limit = 0;   // bound of the inter-CTA waits (0: kSpinLimit)
+    size_t total_mem = 0;       // device memory (the automatic checkpointing rule)
+    int ckpt_groups = 0;        // stripe groups of the last checkpointed call (0: full lattices)
+    // checkpointed E-step of the wide kernels: the stripe groups (host)
+    std::vector<int64_t> h_stripe_lat;
+    int desc_mode = 0;   // 1: a _ws call writes the work description only; 2: it launches only
 };
 
 namespace {
@@ -1038,18 +1059,24 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 // The split E-step: forward on the caller's stream and backward recursion on
 // a side stream at the same time, then the count pass once both are done.
 // side streams (and fork / join events) of one caller stream, created once
-int get_side(phmm_plan *plan, cudaStream_t stream, phmm_plan::Side **out) {
+int get_side(phmm_plan *plan, cudaStream_t stream, bool prio, phmm_plan::Side **out) {
     for (auto &e : plan->sides)
-        if (e.user == stream) { *out = &e; return 0; }
-    phmm_plan::Side e{stream, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    CUDA_TRY(cudaStreamCreateWithFlags(&e.side, cudaStreamNonBlocking));
-    CUDA_TRY(cudaStreamCreateWithFlags(&e.side2, cudaStreamNonBlocking));
-    CUDA_TRY(cudaStreamCreateWithFlags(&e.side3, cudaStreamNonBlocking));
+        if (e.user == stream && e.prio == prio) { *out = &e; return 0; }
+    phmm_plan::Side e{};
+    e.user = stream;
+    e.prio = prio;
+    int least = 0, greatest = 0;
+    if (prio) CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CUDA_TRY(cudaStreamCreateWithPriority(&e.side, cudaStreamNonBlocking, greatest));
+    CUDA_TRY(cudaStreamCreateWithPriority(&e.side2, cudaStreamNonBlocking, least));
+    CUDA_TRY(cudaStreamCreateWithPriority(&e.side3, cudaStreamNonBlocking, least));
+    if (prio) CUDA_TRY(cudaStreamCreateWithPriority(&e.sidef, cudaStreamNonBlocking, greatest));
     CUDA_TRY(cudaEventCreateWithFlags(&e.fork, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&e.join, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&e.join2, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&e.join3, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&e.fwd_done, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&e.joinf, cudaEventDisableTiming));
     plan->sides.push_back(e);
     *out = &plan->sides.back();
     return 0;
@@ -1059,11 +1086,10 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
                  int max_ly, void *d_items, int *d_counters, int *d_progress, float *d_bedge, int *d_bedge_exp,
                  cudaStream_t stream) {
     int rc;
-    phmm_plan::Side *sd = nullptr;
-    if ((rc = get_side(plan, stream, &sd))) return rc;
+    const phmm_tuning &tu = plan->tuning;
     // the count pass of the warp kernels (second side stream) overlaps the
     // wavefronts: its items wait for the stripes they read and its grid takes
-    // half the resident slots (one-warp CTAs, so the wavefronts keep room)
+    // half the resident slots (or tu.count_per_sm CTAs per SM; none at 0)
     KParams C = K;
     C.items = (const int2 *)d_items + 2 * n_items;
     C.n_items = n_citems;
@@ -1086,7 +1112,10 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
         // holds half an SM's registers, so count CTAs waiting beside the
         // wavefront kernel could crowd it out of the SMs
         if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
-        if ((rc = wl(plan, FB, 2 * n_items, max_ly, 4, stream))) return rc;
+        plan->launch_per_sm = tu.wave_per_sm;
+        rc = wl(plan, FB, 2 * n_items, max_ly, 4, stream);
+        plan->launch_per_sm = 0;
+        if (rc) return rc;
         if (plan->timing) {
             CUDA_TRY(cudaEventRecord(plan->ev[1], stream));
             CUDA_TRY(cudaEventRecord(plan->ev[2], stream));
@@ -1101,11 +1130,19 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
         plan->timed_count = true;
         return 0;
     }
+    phmm_plan::Side *sd = nullptr;
+    const bool prio = tu.priorities != 0;
+    if ((rc = get_side(plan, stream, prio, &sd))) return rc;
     CUDA_TRY(cudaEventRecord(sd->fork, stream));
     CUDA_TRY(cudaStreamWaitEvent(sd->side, sd->fork, 0));
     CUDA_TRY(cudaStreamWaitEvent(sd->side2, sd->fork, 0));
     CUDA_TRY(cudaStreamWaitEvent(sd->side3, sd->fork, 0));
-    // forward (caller's stream)
+    // forward: on the caller's stream, or with priorities on a greatest-priority side stream
+    cudaStream_t fs = stream;
+    if (prio) {
+        fs = sd->sidef;
+        CUDA_TRY(cudaStreamWaitEvent(fs, sd->fork, 0));
+    }
     KParams F = K;
     F.items = (const int2 *)d_items;
     F.n_items = n_items;
@@ -1114,13 +1151,16 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
     F.blat = nullptr;
     F.blat_exp = nullptr;
     // the two wavefronts share the GPU: each persistent grid takes half the
-    // resident slots, so neither waits for the other to drain
+    // resident slots (or tu.wave_per_sm CTAs per SM), so neither waits for
+    // the other to drain
     plan->grid_div = 2;
+    plan->launch_per_sm = tu.wave_per_sm;
     const int kf = plan->two_warp ? 5 : 0, kb = plan->two_warp ? 6 : 2;
-    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
-    if ((rc = wl(plan, F, n_items, max_ly, kf, stream))) { plan->grid_div = 1; return rc; }
-    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[1], stream));
-    CUDA_TRY(cudaEventRecord(sd->fwd_done, stream));
+    auto reset = [&]() { plan->grid_div = 1; plan->launch_per_sm = 0; };
+    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], fs));
+    if ((rc = wl(plan, F, n_items, max_ly, kf, fs))) { reset(); return rc; }
+    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[1], fs));
+    CUDA_TRY(cudaEventRecord(sd->fwd_done, fs));
     // backward recursion (side stream): own edge rows and progress counters
     KParams B = K;
     B.items = (const int2 *)d_items + n_items;
@@ -1133,31 +1173,38 @@ int launch_split(phmm_plan *plan, KParams K, WarpLauncher wl, bool combined, int
     B.lat_exp = nullptr;
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[2], sd->side));
     rc = wl(plan, B, n_items, max_ly, kb, sd->side);
-    plan->grid_div = 1;
+    reset();
     if (rc) return rc;
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[3], sd->side));
     CUDA_TRY(cudaEventRecord(sd->join, sd->side));
     // counts from both lattices (second side stream, overlapping the wavefronts)
-    plan->grid_div = 2;
-    if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[4], sd->side2));
-    rc = wl(plan, C, n_citems, max_ly, 3, sd->side2);
-    plan->grid_div = 1;
-    if (rc) return rc;
+    int launched = 3;
+    if (tu.count_per_sm != 0) {
+        plan->grid_div = 2;
+        plan->launch_per_sm = tu.count_per_sm > 0 ? tu.count_per_sm : 0;
+        if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[4], sd->side2));
+        rc = wl(plan, C, n_citems, max_ly, 3, sd->side2);
+        reset();
+        if (rc) return rc;
+        ++launched;
+    }
     CUDA_TRY(cudaEventRecord(sd->join2, sd->side2));
-    // the overlapped grid holds half the slots; once both wavefronts are done a
-    // second, full-size grid pops the remaining count items from the same
-    // counter (all of them ready, so it waits on nothing)
+    // the overlapped grid holds part of the slots; once both wavefronts are
+    // done a second, full-size grid pops the remaining count items from the
+    // same counter (all of them ready, so it waits on nothing)
     CUDA_TRY(cudaStreamWaitEvent(sd->side3, sd->fwd_done, 0));
     CUDA_TRY(cudaStreamWaitEvent(sd->side3, sd->join, 0));
     KParams C2 = C;
     C2.count_wait = 0;
+    if (plan->timing && tu.count_per_sm == 0) CUDA_TRY(cudaEventRecord(plan->ev[4], sd->side3));
     if ((rc = wl(plan, C2, n_citems, max_ly, 3, sd->side3))) return rc;
     CUDA_TRY(cudaEventRecord(sd->join3, sd->side3));
+    if (prio) CUDA_TRY(cudaStreamWaitEvent(stream, sd->fwd_done, 0));
     CUDA_TRY(cudaStreamWaitEvent(stream, sd->join, 0));
     CUDA_TRY(cudaStreamWaitEvent(stream, sd->join2, 0));
     CUDA_TRY(cudaStreamWaitEvent(stream, sd->join3, 0));
     if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[5], stream));
-    plan->launches += 4;
+    plan->launches += launched;
     plan->timed_bwd = true;
     plan->timed_count = true;
     return 0;
@@ -1213,16 +1260,84 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     for (int p : order)
         for (int s = plan->h_meta[p].n_stripes - 1; s >= 0; --s) bw.push_back(make_int2(p, s | blk::BWD_ITEM));
     const int n_items = (int)fw.size();
+    // Stripe-edge checkpointing (E-step): the wavefronts keep no lattice, only
+    // the edge rows every RW rows (their halo exchange) and the log-likelihood;
+    // the count pass then runs in groups of stripes, each stripe's forward and
+    // backward recursion recomputed from the edge rows above and below it into
+    // a group scratch first.  Scratch: O(edge rows + group) instead of
+    // O(lattice).  On with tuning.checkpoint = 1; automatic (0) when one pair's
+    // two lattices alone exceed 40 % of the device's memory (a batch that is
+    // only too large as a whole runs in groups of pairs, which is faster).
+    bool ckpt = false;
+    if (estep) {
+        int64_t big = 0;
+        for (int p = 0; p < P_; ++p) {
+            const PairMeta &m = plan->h_meta[p];
+            big = std::max(big, (int64_t)m.n_stripes * (rows + m.Ly) * rows);
+        }
+        const double pair_bytes = 2.0 * sizeof(float) * (double)big * ES;
+        ckpt = plan->tuning.checkpoint == 1 ||
+               (plan->tuning.checkpoint == 0 && pair_bytes > 0.4 * (double)plan->total_mem);
+    }
+    struct CkGroup { size_t rc_off, n_rc, c_off, n_c; };
+    std::vector<CkGroup> groups;
+    int64_t grp_cells = 0;   // scratch cells of the largest group (each lattice)
+    plan->h_stripe_lat.clear();
     if (estep) {
         for (int i = 0; i < n_items; ++i) { plan->h_items.push_back(fw[i]); plan->h_items.push_back(bw[i]); }
-        for (auto it = order.rbegin(); it != order.rend(); ++it)   // shortest pairs first (ready first)
-            for (int s = 0; s < plan->h_meta[*it].n_stripes; ++s)
-                for (int h = 0; h < wide::SPL; ++h) plan->h_items.push_back(make_int2(*it, (s << 4) | h));
+        if (!ckpt) {
+            for (auto it = order.rbegin(); it != order.rend(); ++it)   // shortest pairs first (ready first)
+                for (int s = 0; s < plan->h_meta[*it].n_stripes; ++s)
+                    for (int h = 0; h < wide::SPL; ++h) plan->h_items.push_back(make_int2(*it, (s << 4) | h));
+        } else {
+            // groups of one wave of the recompute kernel (two items per stripe,
+            // forward and backward), longest pairs first
+            const int threads = 32 * ((NQd + 3) / 4);
+            const int rbytes = std::max(wide::make_smem_wd(NS, KS, max_ly, false).bytes,
+                                        wide::make_smem_wd(NS, KS, max_ly, true).bytes);
+            CUDA_TRY(cudaFuncSetAttribute(wide::fwdbwd_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          rbytes));
+            int rocc = 0;
+            CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rocc, wide::fwdbwd_wide_kernel, threads, rbytes));
+            const int gmax = std::max(1, plan->sm_count * std::max(rocc, 1) / 2);
+            std::vector<int2> members;
+            auto close = [&]() {
+                if (members.empty()) return;
+                CkGroup g;
+                std::vector<int64_t> tab(stripes, -1);
+                int64_t off = 0;
+                g.rc_off = plan->h_items.size();
+                for (const int2 &st : members) {
+                    const PairMeta &m = plan->h_meta[st.x];
+                    tab[m.stripe_base + st.y] = off;
+                    off += (int64_t)(rows + m.Ly) * rows;
+                    plan->h_items.push_back(make_int2(st.x, st.y));
+                    plan->h_items.push_back(make_int2(st.x, st.y | blk::BWD_ITEM));
+                }
+                g.n_rc = plan->h_items.size() - g.rc_off;
+                g.c_off = plan->h_items.size();
+                for (const int2 &st : members)
+                    for (int h = 0; h < wide::SPL; ++h) plan->h_items.push_back(make_int2(st.x, (st.y << 4) | h));
+                g.n_c = plan->h_items.size() - g.c_off;
+                plan->h_stripe_lat.insert(plan->h_stripe_lat.end(), tab.begin(), tab.end());
+                grp_cells = std::max(grp_cells, off);
+                groups.push_back(g);
+                members.clear();
+            };
+            for (int p : order)
+                for (int s = 0; s < plan->h_meta[p].n_stripes; ++s) {
+                    members.push_back(make_int2(p, s));
+                    if ((int)members.size() == gmax) close();
+                }
+            close();
+        }
     } else {
         plan->h_items = fw;
     }
+    if (!ws_need) plan->ckpt_groups = (int)groups.size();
     const int n_fb = estep ? 2 * n_items : n_items;
     const int n_citems = estep ? n_items * wide::SPL : 0;
+    if (ckpt) lat_cells = grp_cells;   // the lattices are one group's scratch
     // ---- scratch
     const size_t o_meta = 0;
     const size_t o_items = align256(o_meta + sizeof(PairMeta) * P_);
@@ -1232,11 +1347,13 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     const size_t o_bedge = align256(o_edge + sizeof(float) * (size_t)edge_cells * ES);
     const size_t o_lat = align256(o_bedge + (estep ? sizeof(float) * (size_t)edge_cells * ES : 0));
     const size_t o_blat = align256(o_lat + (estep ? sizeof(float) * (size_t)lat_cells * ES : 0));
-    const size_t need = align256(o_blat + (estep ? sizeof(float) * (size_t)lat_cells * ES : 0));
+    const size_t o_slat = align256(o_blat + (estep ? sizeof(float) * (size_t)lat_cells * ES : 0));
+    const size_t need = align256(o_slat + sizeof(int64_t) * plan->h_stripe_lat.size());
     if (ws_need) { *ws_need = need; return 0; }
     void *d_meta, *d_items;
     int *d_counters, *d_progress;
     float *d_edge, *d_bedge = nullptr, *d_lat = nullptr, *d_blat = nullptr;
+    int64_t *d_slat = nullptr;
     int rc;
     if (ws) {
         if (ws_bytes < need) {
@@ -1255,6 +1372,7 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
             d_lat = (float *)(w + o_lat);
             d_blat = (float *)(w + o_blat);
         }
+        if (ckpt) d_slat = (int64_t *)(w + o_slat);
     } else {
         if ((rc = ensure((char **)&plan->meta, &plan->meta_cap, sizeof(PairMeta) * P_))) return rc;
         if ((rc = ensure((char **)&plan->items, &plan->items_cap, sizeof(int2) * plan->h_items.size()))) return rc;
@@ -1265,6 +1383,10 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
             if ((rc = ensure(&plan->lat, &plan->lat_cap, (size_t)lat_cells * ES))) return rc;
             if ((rc = ensure(&plan->blat, &plan->blat_cap, (size_t)lat_cells * ES))) return rc;
         }
+        if (ckpt) {
+            if ((rc = ensure(&plan->slat, &plan->slat_cap, plan->h_stripe_lat.size()))) return rc;
+            d_slat = plan->slat;
+        }
         d_meta = plan->meta;
         d_items = plan->items;
         d_counters = plan->counters;
@@ -1274,9 +1396,16 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         d_lat = plan->lat;
         d_blat = plan->blat;
     }
-    CUDA_TRY(cudaMemcpyAsync(d_meta, plan->h_meta.data(), sizeof(PairMeta) * P_, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(d_items, plan->h_items.data(), sizeof(int2) * plan->h_items.size(),
-                             cudaMemcpyHostToDevice, stream));
+    if (plan->desc_mode != 2) {   // the work description (launch-only calls find it in the workspace)
+        CUDA_TRY(cudaMemcpyAsync(d_meta, plan->h_meta.data(), sizeof(PairMeta) * P_, cudaMemcpyHostToDevice,
+                                 stream));
+        CUDA_TRY(cudaMemcpyAsync(d_items, plan->h_items.data(), sizeof(int2) * plan->h_items.size(),
+                                 cudaMemcpyHostToDevice, stream));
+        if (ckpt)
+            CUDA_TRY(cudaMemcpyAsync(d_slat, plan->h_stripe_lat.data(), sizeof(int64_t) * plan->h_stripe_lat.size(),
+                                     cudaMemcpyHostToDevice, stream));
+    }
+    if (plan->desc_mode == 1) return 0;
     CUDA_TRY(cudaMemsetAsync(d_counters, 0, 3 * sizeof(int), stream));
     CUDA_TRY(cudaMemsetAsync(d_progress, 0, sizeof(int) * 2 * stripes, stream));
     CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int32_t) * P_, stream));
@@ -1295,9 +1424,9 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     K.eD = b->emit_D;
     K.eM_stride = b->emit_per_pair ? (int64_t)G * 441 : 0;
     K.eID_stride = b->emit_per_pair ? (int64_t)G * 21 : 0;
-    K.lat = d_lat;
+    K.lat = ckpt ? nullptr : d_lat;      // checkpointed: the wavefronts write edge rows only
     K.lat_exp = nullptr;
-    K.blat = d_blat;
+    K.blat = ckpt ? nullptr : d_blat;
     K.blat_exp = nullptr;
     K.edge = d_edge;
     K.edge_exp = nullptr;
@@ -1305,6 +1434,9 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     K.bedge_exp = nullptr;
     K.progress = d_progress;
     K.bprogress = d_progress + stripes;
+    K.stripe_lat = nullptr;
+    K.recompute = 0;
+    K.ckpt = 0;
     K.ll = ll;
     K.status = status;
     K.n_trans = n_trans;
@@ -1333,7 +1465,8 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, bytes));
         if (occ < 1) return fail(PHMM_E_ARG, "wide kernel does not fit on an SM (shared memory)");
         if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[0], stream));
-        kern<<<std::min(n_fb, plan->sm_count * occ), threads, bytes, stream>>>(K);
+        const int per_sm = plan->tuning.wave_per_sm > 0 ? std::min(plan->tuning.wave_per_sm, occ) : occ;
+        kern<<<std::min(n_fb, plan->sm_count * per_sm), threads, bytes, stream>>>(K);
         CUDA_TRY(cudaGetLastError());
         if (plan->timing) {
             CUDA_TRY(cudaEventRecord(plan->ev[1], stream));
@@ -1342,11 +1475,8 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         }
         plan->launches++;
     }
-    // ---- counts
+    // ---- counts (checkpointed: per group, the group's stripes recomputed first)
     if (estep) {
-        K.items = (const int2 *)d_items + n_fb;
-        K.n_items = n_citems;
-        K.counter = d_counters + 2;
         K.count_wait = 0;
         const int bytes = wide::make_smem_wc(NS, KS, K.kend[0] - K.kbeg[0], K.kend[1] - K.kbeg[1],
                                              K.kend[2] - K.kbeg[2]).bytes;
@@ -1355,10 +1485,46 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, wide::count_wide_kernel, wide::CT, bytes));
         if (occ < 1) return fail(PHMM_E_ARG, "wide count kernel does not fit on an SM (shared memory)");
         if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[4], stream));
-        wide::count_wide_kernel<<<std::min(n_citems, plan->sm_count * occ), wide::CT, bytes, stream>>>(K);
-        CUDA_TRY(cudaGetLastError());
+        if (!ckpt) {
+            K.items = (const int2 *)d_items + n_fb;
+            K.n_items = n_citems;
+            K.counter = d_counters + 2;
+            wide::count_wide_kernel<<<std::min(n_citems, plan->sm_count * occ), wide::CT, bytes, stream>>>(K);
+            CUDA_TRY(cudaGetLastError());
+            plan->launches++;
+        } else {
+            const int threads = 32 * ((NQd + 3) / 4);
+            const int rbytes = std::max(wide::make_smem_wd(NS, KS, max_ly, false).bytes,
+                                        wide::make_smem_wd(NS, KS, max_ly, true).bytes);
+            int rocc = 0;
+            CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rocc, wide::fwdbwd_wide_kernel, threads, rbytes));
+            if (rocc < 1) return fail(PHMM_E_ARG, "wide kernel does not fit on an SM (shared memory)");
+            K.lat = d_lat;
+            K.blat = d_blat;
+            for (size_t gi = 0; gi < groups.size(); ++gi) {
+                const CkGroup &g = groups[gi];
+                K.stripe_lat = d_slat + gi * (size_t)stripes;
+                CUDA_TRY(cudaMemsetAsync(d_counters, 0, 2 * sizeof(int), stream));
+                // recompute the group's stripes (both directions) from the edge rows
+                K.recompute = 1;
+                K.ckpt = 0;
+                K.items = (const int2 *)d_items + g.rc_off;
+                K.n_items = (int)g.n_rc;
+                K.counter = d_counters;
+                wide::fwdbwd_wide_kernel<<<std::min((int)g.n_rc, plan->sm_count * rocc), threads, rbytes, stream>>>(K);
+                CUDA_TRY(cudaGetLastError());
+                // counts of the group from its scratch lattices
+                K.recompute = 0;
+                K.ckpt = 1;
+                K.items = (const int2 *)d_items + g.c_off;
+                K.n_items = (int)g.n_c;
+                K.counter = d_counters + 1;
+                wide::count_wide_kernel<<<std::min((int)g.n_c, plan->sm_count * occ), wide::CT, bytes, stream>>>(K);
+                CUDA_TRY(cudaGetLastError());
+                plan->launches += 2;
+            }
+        }
         if (plan->timing) CUDA_TRY(cudaEventRecord(plan->ev[5], stream));
-        plan->launches++;
     }
     plan->timed_bwd = estep;
     plan->timed_count = estep;
@@ -1389,7 +1555,7 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     if (P_ == 0) return 0;
     if (!b->Lx_host || !b->Ly_host || !b->x_off_host || !b->y_off_host)
         return fail(PHMM_E_ARG, "null batch length or offset array");
-    if (!ws_need) {
+    if (!ws_need && plan->desc_mode != 1) {
         if (!b->residues || !b->chi || !b->emit_M || !b->emit_I || !b->emit_D || !ll || !status)
             return fail(PHMM_E_ARG, "null batch pointer");
         if (estep && (!n_trans || !cntM || !cntI || !cntD)) return fail(PHMM_E_ARG, "null E-step output");
@@ -1586,9 +1752,13 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
             d_bedge_exp = plan->bedge_exp;
         }
     }
-    CUDA_TRY(cudaMemcpyAsync(d_meta, plan->h_meta.data(), sizeof(PairMeta) * P_, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(d_items, plan->h_items.data(), sizeof(int2) * plan->h_items.size(),
-                             cudaMemcpyHostToDevice, stream));
+    if (plan->desc_mode != 2) {   // the work description (launch-only calls find it in the workspace)
+        CUDA_TRY(cudaMemcpyAsync(d_meta, plan->h_meta.data(), sizeof(PairMeta) * P_, cudaMemcpyHostToDevice,
+                                 stream));
+        CUDA_TRY(cudaMemcpyAsync(d_items, plan->h_items.data(), sizeof(int2) * plan->h_items.size(),
+                                 cudaMemcpyHostToDevice, stream));
+    }
+    if (plan->desc_mode == 1) return 0;
     CUDA_TRY(cudaMemsetAsync(d_counters, 0, 3 * sizeof(int), stream));
     CUDA_TRY(cudaMemsetAsync(d_progress, 0, sizeof(int) * 2 * stripes, stream));
     CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int32_t) * P_, stream));
@@ -1687,7 +1857,7 @@ int run(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, double *n_
         double *post, void *stream_, void *ws = nullptr, size_t ws_bytes = 0, size_t *ws_need = nullptr) {
     const int rc = run_core(plan, b, estep, ll, n_trans, cntM, cntI, cntD, status, F_log, B_log, post, stream_,
                             ws, ws_bytes, ws_need);
-    if (rc || ws_need || b->n_pairs <= 0) return rc;
+    if (rc || ws_need || b->n_pairs <= 0 || plan->desc_mode == 1) return rc;
     const int rc2 = launch_timeout_epilogue(ll, status, b->n_pairs, (cudaStream_t)stream_);
     if (!rc2) plan->launches++;
     return rc2;
@@ -1712,7 +1882,9 @@ int launch_block(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind,
     int occ = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, bytes));
     if (occ < 1) return fail(PHMM_E_ARG, "block kernel does not fit on an SM (shared memory)");
-    const int grid = std::min(n_items, std::max(1, plan->sm_count * occ / plan->grid_div));
+    const int grid = std::min(n_items, plan->launch_per_sm > 0
+                                           ? plan->sm_count * std::min(plan->launch_per_sm, occ)
+                                           : std::max(1, plan->sm_count * occ / plan->grid_div));
     kern<<<grid, threads, bytes, stream>>>(K);
     CUDA_TRY(cudaGetLastError());
     return 0;
@@ -1743,7 +1915,9 @@ int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, 
     int occ = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, bytes));
     if (occ < 1) return fail(PHMM_E_ARG, "warp kernel does not fit on an SM (shared memory)");
-    const int grid = std::min(n_items, std::max(1, plan->sm_count * occ / plan->grid_div));
+    const int grid = std::min(n_items, plan->launch_per_sm > 0
+                                           ? plan->sm_count * std::min(plan->launch_per_sm, occ)
+                                           : std::max(1, plan->sm_count * occ / plan->grid_div));
     kern<<<grid, threads, bytes, stream>>>(K);
     CUDA_TRY(cudaGetLastError());
     return 0;
@@ -1753,7 +1927,8 @@ int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, 
 // as consecutive groups of pairs (contiguous index ranges), one after the
 // other on the same stream, each within the budget.
 size_t plan_scratch_bytes(const phmm_plan *plan) {
-    return plan->meta_cap + plan->items_cap + sizeof(float) * (plan->lat_cap + plan->edge_cap + plan->blat_cap +
+    return plan->meta_cap + plan->items_cap + sizeof(int64_t) * plan->slat_cap +
+           sizeof(float) * (plan->lat_cap + plan->edge_cap + plan->blat_cap +
            plan->bedge_cap) + sizeof(int) * (plan->latE_cap + plan->edgeE_cap + plan->prog_cap + plan->blatE_cap +
            plan->bedgeE_cap);
 }
@@ -1924,6 +2099,10 @@ int phmm_plan_create(const phmm_model_desc *md, phmm_plan **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&plan->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) {
+        size_t fr = 0;
+        e = cudaMemGetInfo(&fr, &plan->total_mem);
+    }
     if (e == cudaSuccess) e = cudaMalloc((void **)&plan->counters, 4 * sizeof(int));
     if (e != cudaSuccess) {
         delete plan;
@@ -1982,6 +2161,8 @@ void phmm_plan_destroy(phmm_plan *plan) {
         cudaEventDestroy(e.join2);
         cudaEventDestroy(e.join3);
         cudaEventDestroy(e.fwd_done);
+        cudaEventDestroy(e.joinf);
+        if (e.sidef) cudaStreamDestroy(e.sidef);
         cudaStreamDestroy(e.side);
         cudaStreamDestroy(e.side2);
         cudaStreamDestroy(e.side3);
@@ -1998,6 +2179,7 @@ void phmm_plan_destroy(phmm_plan *plan) {
     cudaFree(plan->edge);
     cudaFree(plan->edge_exp);
     cudaFree(plan->progress);
+    cudaFree(plan->slat);
     delete plan;
 }
 
@@ -2039,6 +2221,27 @@ int phmm_estep_ws(phmm_plan *plan, const phmm_batch *batch, void *workspace, siz
                stream, workspace, workspace_bytes);
 }
 
+int phmm_estep_ws_prepare(phmm_plan *plan, const phmm_batch *batch, void *workspace, size_t workspace_bytes,
+                          void *stream) {
+    if (!plan || !workspace) return fail(PHMM_E_ARG, "null plan or workspace");
+    plan->desc_mode = 1;
+    const int rc = run(plan, batch, true, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                       nullptr, stream, workspace, workspace_bytes);
+    plan->desc_mode = 0;
+    return rc;
+}
+
+int phmm_estep_ws_launch(phmm_plan *plan, const phmm_batch *batch, void *workspace, size_t workspace_bytes,
+                         double *ll_out, double *n_trans, double *cnt_M, double *cnt_I, double *cnt_D,
+                         int32_t *status_out, void *stream) {
+    if (!plan || !workspace) return fail(PHMM_E_ARG, "null plan or workspace");
+    plan->desc_mode = 2;
+    const int rc = run(plan, batch, true, ll_out, n_trans, cnt_M, cnt_I, cnt_D, status_out, nullptr, nullptr,
+                       nullptr, stream, workspace, workspace_bytes);
+    plan->desc_mode = 0;
+    return rc;
+}
+
 int phmm_last_launch_count(const phmm_plan *plan) { return plan ? plan->launches : 0; }
 
 int phmm_set_variant(phmm_plan *plan, int variant) {
@@ -2052,6 +2255,25 @@ int phmm_set_variant(phmm_plan *plan, int variant) {
 }
 
 int phmm_last_variant(const phmm_plan *plan) { return plan ? plan->last_variant : 0; }
+
+int phmm_set_tuning(phmm_plan *plan, const phmm_tuning *t) {
+    if (!plan || !t) return fail(PHMM_E_ARG, "null plan or tuning");
+    if (t->wave_per_sm < 0 || t->wave_per_sm > 64 || t->count_per_sm < -1 || t->count_per_sm > 64 ||
+        t->priorities < 0 || t->priorities > 1 || t->checkpoint < 0 || t->checkpoint > 2)
+        return fail(PHMM_E_ARG, "tuning out of range (wave_per_sm 0..64, count_per_sm -1..64, priorities 0/1, "
+                                "checkpoint 0..2)");
+    int rc = phmm_set_variant(plan, t->variant);
+    if (rc) return rc;
+    plan->tuning = *t;
+    return 0;
+}
+
+int phmm_get_tuning(const phmm_plan *plan, phmm_tuning *t) {
+    if (!plan || !t) return fail(PHMM_E_ARG, "null plan or tuning");
+    *t = plan->tuning;
+    t->variant = plan->variant;
+    return 0;
+}
 
 int phmm_set_spin_limit(phmm_plan *plan, long long iterations) {
     if (!plan || iterations < 0) return fail(PHMM_E_ARG, "null plan or negative spin limit");

@@ -316,8 +316,7 @@ __device__ void build_chi(const ChiParams<T> &cp, int K, int F, int N, ChiSmem<T
     }
 }
 
-__global__ void __launch_bounds__(THREADS)
-chi_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, int N, float *__restrict__ chi,
+__device__ __forceinline__ void chi_kernel_body(const Packed &prm, const double *__restrict__ ts, int N, float *__restrict__ chi,
            double *__restrict__ chi64) {
     extern __shared__ double smem_d[];
     __shared__ int piv_row;
@@ -332,6 +331,18 @@ chi_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, in
         out[idx] = (float)v;
         if (out64) out64[idx] = v;
     });
+}
+
+__global__ void __launch_bounds__(THREADS)
+chi_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, int N, float *__restrict__ chi, double *__restrict__ chi64) {
+    chi_kernel_body(prm, ts, N, chi, chi64);
+}
+
+// the same with the parameter block in device memory (a captured graph
+// refreshes it by a copy before each replay)
+__global__ void __launch_bounds__(THREADS)
+chi_kernel_dp(const Packed *__restrict__ prm, const double *__restrict__ ts, int N, float *__restrict__ chi, double *__restrict__ chi64) {
+    chi_kernel_body(*prm, ts, N, chi, chi64);
 }
 
 // Vector-Jacobian product of chi: for pair p = blockIdx.x and parameter
@@ -388,8 +399,7 @@ __device__ void mm(double *C, const double *A, const double *B, int n) {
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(THREADS)
-expm_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, double *__restrict__ csubs) {
+__device__ __forceinline__ void expm_kernel_body(const Packed &prm, const double *__restrict__ ts, double *__restrict__ csubs) {
     constexpr int n = NA, nn = NA * NA;
     __shared__ double X[nn], A2[nn], A4[nn], A6[nn], W1[nn], W2[nn], U[nn], V[nn];
     __shared__ double aug[n * 2 * n];
@@ -508,9 +518,20 @@ expm_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, d
     for (int idx = tid; idx < nn; idx += blockDim.x) out[idx] = cur[idx];
 }
 
-// ---------------------------------------------------------------- emission tables
 __global__ void __launch_bounds__(THREADS)
-tables_kernel(const __grid_constant__ Packed prm, const double *__restrict__ csubs, float *__restrict__ EM,
+expm_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, double *__restrict__ csubs) {
+    expm_kernel_body(prm, ts, csubs);
+}
+
+// the same with the parameter block in device memory (a captured graph
+// refreshes it by a copy before each replay)
+__global__ void __launch_bounds__(THREADS)
+expm_kernel_dp(const Packed *__restrict__ prm, const double *__restrict__ ts, double *__restrict__ csubs) {
+    expm_kernel_body(*prm, ts, csubs);
+}
+
+// ---------------------------------------------------------------- emission tables
+__device__ __forceinline__ void tables_kernel_body(const Packed &prm, const double *__restrict__ csubs, float *__restrict__ EM,
               float *__restrict__ EI, float *__restrict__ ED) {
     const int p = blockIdx.x, tid = threadIdx.x;
     const int C = prm.C, G = prm.K * prm.F;
@@ -536,6 +557,18 @@ tables_kernel(const __grid_constant__ Packed prm, const double *__restrict__ csu
     }
 }
 
+__global__ void __launch_bounds__(THREADS)
+tables_kernel(const __grid_constant__ Packed prm, const double *__restrict__ csubs, float *__restrict__ EM, float *__restrict__ EI, float *__restrict__ ED) {
+    tables_kernel_body(prm, csubs, EM, EI, ED);
+}
+
+// the same with the parameter block in device memory (a captured graph
+// refreshes it by a copy before each replay)
+__global__ void __launch_bounds__(THREADS)
+tables_kernel_dp(const Packed *__restrict__ prm, const double *__restrict__ csubs, float *__restrict__ EM, float *__restrict__ EI, float *__restrict__ ED) {
+    tables_kernel_body(*prm, csubs, EM, EI, ED);
+}
+
 // ---------------------------------------------------------------- class split (epilogue)
 // Per-class counts of train/likelihood.py:279-344 from the per-(d,f) character
 // tables: the class posterior of a cell depends on it only through its
@@ -546,8 +579,7 @@ tables_kernel(const __grid_constant__ Packed prm, const double *__restrict__ csu
 // 21 x 21 (and 21) characters of the same terms.  One CTA per pair.
 constexpr int CS_MAXC = 8;
 
-__global__ void __launch_bounds__(THREADS)
-class_split_kernel(const __grid_constant__ Packed prm, const double *__restrict__ csubs,
+__device__ __forceinline__ void class_split_kernel_body(const Packed &prm, const double *__restrict__ csubs,
                    const double *__restrict__ cM, const double *__restrict__ cI, const double *__restrict__ cD,
                    double *__restrict__ match, double *__restrict__ ins, double *__restrict__ del,
                    double *__restrict__ cdist) {
@@ -606,6 +638,18 @@ class_split_kernel(const __grid_constant__ Packed prm, const double *__restrict_
     }
     __syncthreads();
     for (int i = tid; i < G * C; i += blockDim.x) cdist[(size_t)p * G * C + i] = cs_acc[i];
+}
+
+__global__ void __launch_bounds__(THREADS)
+class_split_kernel(const __grid_constant__ Packed prm, const double *__restrict__ csubs, const double *__restrict__ cM, const double *__restrict__ cI, const double *__restrict__ cD, double *__restrict__ match, double *__restrict__ ins, double *__restrict__ del, double *__restrict__ cdist) {
+    class_split_kernel_body(prm, csubs, cM, cI, cD, match, ins, del, cdist);
+}
+
+// the same with the parameter block in device memory (a captured graph
+// refreshes it by a copy before each replay)
+__global__ void __launch_bounds__(THREADS)
+class_split_kernel_dp(const Packed *__restrict__ prm, const double *__restrict__ csubs, const double *__restrict__ cM, const double *__restrict__ cI, const double *__restrict__ cD, double *__restrict__ match, double *__restrict__ ins, double *__restrict__ del, double *__restrict__ cdist) {
+    class_split_kernel_body(*prm, csubs, cM, cI, cD, match, ins, del, cdist);
 }
 
 // ---------------------------------------------------------------- TKF92 prologue
@@ -865,10 +909,9 @@ struct HRClass {
     double Q[HR_MAXA * HR_MAXA];
 };
 
-__global__ void __launch_bounds__(HR_THREADS) hr_kernel(const __grid_constant__ HRClass hc, int c, int C,
-                                                        const double *__restrict__ t,
-                                                        const double *__restrict__ mc, double *__restrict__ W,
-                                                        double *__restrict__ U) {
+__device__ __forceinline__ void hr_kernel_body(const HRClass &hc, int c, int C, const double *__restrict__ t,
+                                               const double *__restrict__ mc, double *__restrict__ W,
+                                               double *__restrict__ U) {
     __shared__ double V[HR_MAXA * HR_MAXA], R[HR_MAXA * HR_MAXA], T1[HR_MAXA * HR_MAXA], Y[HR_MAXA * HR_MAXA];
     __shared__ double ex[HR_MAXA], lam[HR_MAXA], sp[HR_MAXA];
     const int p = blockIdx.x, tid = threadIdx.x, A = hc.A, AA = A * A;
@@ -927,6 +970,22 @@ __global__ void __launch_bounds__(HR_THREADS) hr_kernel(const __grid_constant__ 
         U[base + i] = a == b ? 0.0 : hc.Q[i] * s;
         if (a == b) W[((size_t)p * C + c) * A + a] = s;
     }
+}
+
+__global__ void __launch_bounds__(HR_THREADS) hr_kernel(const __grid_constant__ HRClass hc, int c, int C,
+                                                        const double *__restrict__ t,
+                                                        const double *__restrict__ mc, double *__restrict__ W,
+                                                        double *__restrict__ U) {
+    hr_kernel_body(hc, c, C, t, mc, W, U);
+}
+
+// the same with the class blocks in device memory (hcs[c]; a captured graph
+// refreshes them by a copy before each replay)
+__global__ void __launch_bounds__(HR_THREADS) hr_kernel_dp(const HRClass *__restrict__ hcs, int c, int C,
+                                                           const double *__restrict__ t,
+                                                           const double *__restrict__ mc, double *__restrict__ W,
+                                                           double *__restrict__ U) {
+    hr_kernel_body(hcs[c], c, C, t, mc, W, U);
 }
 
 // Eigenvalues and orthonormal eigenvectors of a symmetric n x n matrix by the
@@ -1033,6 +1092,106 @@ extern "C" int phmm_holmes_rubin(int32_t n_classes, int32_t alphabet, const doub
         hr_class(A, class_Q + (size_t)c * A * A, class_pis + (size_t)c * A, hc);
         hr_kernel<<<n_pairs, HR_THREADS, 0, (cudaStream_t)stream>>>(hc, c, n_classes, t, class_match_counts, W, U);
     }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    return PHMM_OK;
+}
+
+// ---------------------------------------------------------------- parameter blocks in device memory
+// For a captured CUDA graph of the batched E-step: the by-value parameter
+// blocks above are baked into a graph's kernel nodes when it is captured, so
+// the graph's kernels take them from device memory instead, refreshed before
+// each replay by a copy from a host block that these functions fill.
+
+extern "C" size_t phmm_mixdom2_param_block_bytes(void) { return sizeof(pro::Packed); }
+
+extern "C" int phmm_mixdom2_param_block(const phmm_mixdom2_params *prm, void *host_block, size_t bytes) {
+    using namespace pro;
+    if (!host_block || bytes < sizeof(Packed))
+        return pro_fail(PHMM_E_ARG, "phmm_mixdom2_param_block: host block missing or smaller than "
+                                    "phmm_mixdom2_param_block_bytes()");
+    return pack_params(prm, *reinterpret_cast<Packed *>(host_block), "phmm_mixdom2_param_block");
+}
+
+extern "C" int phmm_mixdom2_tables_dp(const void *param_block, int32_t n_dom, int32_t n_frag, int32_t n_classes,
+                                      int32_t n_pairs, const double *t, float *chi, float *emit_M, float *emit_I,
+                                      float *emit_D, double *class_subs, void *stream) {
+    using namespace pro;
+    const int K = n_dom, F = n_frag, C = n_classes;
+    if (K < 1 || F < 1 || C < 1 || K * F > MAXK || n_pairs < 0)
+        return pro_fail(PHMM_E_ARG, "phmm_mixdom2_tables_dp: bad shape");
+    if (n_pairs == 0) return PHMM_OK;
+    if (!param_block || !t || !chi || !emit_M || !emit_I || !emit_D || !class_subs)
+        return pro_fail(PHMM_E_ARG, "phmm_mixdom2_tables_dp: null device buffer");
+    const Packed *pk = reinterpret_cast<const Packed *>(param_block);
+    const int N = 2 + 5 * K * F;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t chi_smem = sizeof(double) * ChiSmem<double>::elems(K);
+    if (chi_smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(chi_kernel_dp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chi_smem);
+        if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    }
+    chi_kernel_dp<<<n_pairs, THREADS, chi_smem, st>>>(pk, t, N, chi, nullptr);
+    expm_kernel_dp<<<n_pairs * C, THREADS, 0, st>>>(pk, t, class_subs);
+    tables_kernel_dp<<<n_pairs, THREADS, 0, st>>>(pk, class_subs, emit_M, emit_I, emit_D);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    return PHMM_OK;
+}
+
+extern "C" int phmm_mixdom2_class_counts_dp(const void *param_block, int32_t n_dom, int32_t n_frag,
+                                            int32_t n_classes, int32_t n_pairs, const double *class_subs,
+                                            const double *cnt_M, const double *cnt_I, const double *cnt_D,
+                                            double *class_match, double *class_insert, double *class_delete,
+                                            double *classdist_counts, void *stream) {
+    using namespace pro;
+    const int K = n_dom, F = n_frag, C = n_classes;
+    if (K < 1 || F < 1 || C < 1 || K * F > MAXK || C > CS_MAXC || n_pairs < 0)
+        return pro_fail(PHMM_E_ARG, "phmm_mixdom2_class_counts_dp: bad shape (at most 8 classes)");
+    if (n_pairs == 0) return PHMM_OK;
+    if (!param_block || !class_subs || !cnt_M || !cnt_I || !cnt_D || !class_match || !class_insert ||
+        !class_delete || !classdist_counts)
+        return pro_fail(PHMM_E_ARG, "phmm_mixdom2_class_counts_dp: null device buffer");
+    const size_t smem = sizeof(double) * K * F * C;
+    class_split_kernel_dp<<<n_pairs, THREADS, smem, (cudaStream_t)stream>>>(
+        reinterpret_cast<const Packed *>(param_block), class_subs, cnt_M, cnt_I, cnt_D, class_match, class_insert,
+        class_delete, classdist_counts);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    return PHMM_OK;
+}
+
+extern "C" size_t phmm_holmes_rubin_block_bytes(int32_t n_classes) {
+    return n_classes > 0 ? sizeof(pro::HRClass) * (size_t)n_classes : 0;
+}
+
+extern "C" int phmm_holmes_rubin_block(int32_t n_classes, int32_t alphabet, const double *class_Q,
+                                       const double *class_pis, void *host_block, size_t bytes) {
+    using namespace pro;
+    if (n_classes < 1 || alphabet < 1 || alphabet > HR_MAXA)
+        return pro_fail(PHMM_E_ARG, "phmm_holmes_rubin_block: need n_classes >= 1 and 1 <= alphabet <= 32");
+    if (!class_Q || !class_pis) return pro_fail(PHMM_E_ARG, "phmm_holmes_rubin_block: null host rate matrices");
+    if (!host_block || bytes < sizeof(HRClass) * (size_t)n_classes)
+        return pro_fail(PHMM_E_ARG, "phmm_holmes_rubin_block: host block smaller than phmm_holmes_rubin_block_bytes");
+    for (int i = 0; i < n_classes * alphabet; ++i)
+        if (!(class_pis[i] > 0.0))
+            return pro_fail(PHMM_E_ARG, "phmm_holmes_rubin_block: stationary frequencies must be positive");
+    HRClass *out = reinterpret_cast<HRClass *>(host_block);
+    const int A = alphabet;
+    for (int c = 0; c < n_classes; ++c) hr_class(A, class_Q + (size_t)c * A * A, class_pis + (size_t)c * A, out[c]);
+    return PHMM_OK;
+}
+
+extern "C" int phmm_holmes_rubin_dp(const void *block, int32_t n_classes, int32_t n_pairs, const double *t,
+                                    const double *class_match_counts, double *W, double *U, void *stream) {
+    using namespace pro;
+    if (n_classes < 1 || n_pairs < 0) return pro_fail(PHMM_E_ARG, "phmm_holmes_rubin_dp: bad shape");
+    if (n_pairs == 0) return PHMM_OK;
+    if (!block || !t || !class_match_counts || !W || !U)
+        return pro_fail(PHMM_E_ARG, "phmm_holmes_rubin_dp: null device buffer");
+    for (int c = 0; c < n_classes; ++c)
+        hr_kernel_dp<<<n_pairs, HR_THREADS, 0, (cudaStream_t)stream>>>(reinterpret_cast<const HRClass *>(block), c,
+                                                                       n_classes, t, class_match_counts, W, U);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
     return PHMM_OK;

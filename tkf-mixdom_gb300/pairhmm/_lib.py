@@ -20,13 +20,22 @@ _LIB = None
 EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep',
            'phmm_estep_tables', 'phmm_workspace_bytes', 'phmm_forward_ws', 'phmm_estep_ws',
            'phmm_estep_static', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_kernel_time',
-           'phmm_set_variant', 'phmm_set_spin_limit',
+           'phmm_set_variant', 'phmm_set_spin_limit', 'phmm_set_tuning', 'phmm_get_tuning',
            'phmm_last_variant', 'phmm_last_launch_count',
            'phmm_last_error', 'phmm_version', 'phmm_mixdom2_class_subs_count', 'phmm_mixdom2_tables',
            'phmm_mixdom2_class_counts', 'phmm_tkf92_tables', 'phmm_mixdom2_chi',
            'phmm_mixdom2_chi_vjp_dirs', 'phmm_mixdom2_chi_vjp', 'phmm_fb1d_workspace_bytes', 'phmm_fb1d',
            'phmm_fb1d_emissions', 'phmm_viterbi_workspace_bytes', 'phmm_viterbi', 'phmm_holmes_rubin',
-           'phmm_sample_workspace_bytes', 'phmm_sample_paths', 'phmm_pairs_count', 'phmm_pairs_decode')
+           'phmm_sample_workspace_bytes', 'phmm_sample_paths', 'phmm_pairs_count', 'phmm_pairs_decode',
+           'phmm_estep_ws_prepare', 'phmm_estep_ws_launch', 'phmm_mixdom2_param_block_bytes',
+           'phmm_mixdom2_param_block', 'phmm_mixdom2_tables_dp', 'phmm_mixdom2_class_counts_dp',
+           'phmm_holmes_rubin_block_bytes', 'phmm_holmes_rubin_block', 'phmm_holmes_rubin_dp')
+
+
+class Tuning(ctypes.Structure):
+    """phmm_tuning: the launch configuration the autotuner searches."""
+    _fields_ = [('variant', ctypes.c_int32), ('wave_per_sm', ctypes.c_int32),
+                ('count_per_sm', ctypes.c_int32), ('priorities', ctypes.c_int32), ('checkpoint', ctypes.c_int32)]
 
 
 class ModelDesc(ctypes.Structure):
@@ -114,6 +123,10 @@ def load(path=None):
     lib.phmm_kernel_times.restype = ctypes.c_int
     lib.phmm_kernel_time.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
     lib.phmm_kernel_time.restype = ctypes.c_int
+    lib.phmm_set_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    lib.phmm_set_tuning.restype = ctypes.c_int
+    lib.phmm_get_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    lib.phmm_get_tuning.restype = ctypes.c_int
     lib.phmm_set_spin_limit.argtypes = [vp, ctypes.c_longlong]
     lib.phmm_set_spin_limit.restype = ctypes.c_int
     lib.phmm_set_variant.argtypes = [vp, ctypes.c_int]
@@ -160,6 +173,24 @@ def load(path=None):
     lib.phmm_sample_paths.restype = ctypes.c_int
     lib.phmm_holmes_rubin.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp, ctypes.c_int32, vp, vp, vp, vp, vp]
     lib.phmm_holmes_rubin.restype = ctypes.c_int
+    lib.phmm_estep_ws_prepare.argtypes = [vp, ctypes.POINTER(Batch), vp, ctypes.c_size_t, vp]
+    lib.phmm_estep_ws_prepare.restype = ctypes.c_int
+    lib.phmm_estep_ws_launch.argtypes = [vp, ctypes.POINTER(Batch), vp, ctypes.c_size_t] + [vp] * 7
+    lib.phmm_estep_ws_launch.restype = ctypes.c_int
+    lib.phmm_mixdom2_param_block_bytes.argtypes = []
+    lib.phmm_mixdom2_param_block_bytes.restype = ctypes.c_size_t
+    lib.phmm_mixdom2_param_block.argtypes = [ctypes.POINTER(MixDom2Params), vp, ctypes.c_size_t]
+    lib.phmm_mixdom2_param_block.restype = ctypes.c_int
+    lib.phmm_mixdom2_tables_dp.argtypes = [vp] + [ctypes.c_int32] * 4 + [vp] * 7
+    lib.phmm_mixdom2_tables_dp.restype = ctypes.c_int
+    lib.phmm_mixdom2_class_counts_dp.argtypes = [vp] + [ctypes.c_int32] * 4 + [vp] * 9
+    lib.phmm_mixdom2_class_counts_dp.restype = ctypes.c_int
+    lib.phmm_holmes_rubin_block_bytes.argtypes = [ctypes.c_int32]
+    lib.phmm_holmes_rubin_block_bytes.restype = ctypes.c_size_t
+    lib.phmm_holmes_rubin_block.argtypes = [ctypes.c_int32, ctypes.c_int32, vp, vp, vp, ctypes.c_size_t]
+    lib.phmm_holmes_rubin_block.restype = ctypes.c_int
+    lib.phmm_holmes_rubin_dp.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, vp, vp, vp, vp, vp]
+    lib.phmm_holmes_rubin_dp.restype = ctypes.c_int
     lib.phmm_version.argtypes = []
     lib.phmm_version.restype = ctypes.c_int
     _LIB = lib
@@ -223,6 +254,21 @@ class Plan:
 
     def set_timing(self, enable=True):
         _check(self.lib.phmm_set_timing(self.handle, int(enable)), 'phmm_set_timing')
+
+    def set_tuning(self, variant=0, wave_per_sm=0, count_per_sm=-1, priorities=0, checkpoint=0):
+        """Launch configuration (phmm_set_tuning): kernel family, resident CTAs
+        per SM of each wavefront grid (0 automatic), of the overlapped count
+        grid (-1 automatic, 0 none), wavefront/count stream priorities, and
+        stripe-edge checkpointing of the wide kernels' E-step (0 automatic,
+        1 on, 2 off)."""
+        t = Tuning(int(variant), int(wave_per_sm), int(count_per_sm), int(priorities), int(checkpoint))
+        _check(self.lib.phmm_set_tuning(self.handle, ctypes.byref(t)), 'phmm_set_tuning')
+
+    def get_tuning(self):
+        t = Tuning()
+        _check(self.lib.phmm_get_tuning(self.handle, ctypes.byref(t)), 'phmm_get_tuning')
+        return {'variant': t.variant, 'wave_per_sm': t.wave_per_sm, 'count_per_sm': t.count_per_sm,
+                'priorities': t.priorities, 'checkpoint': t.checkpoint}
 
     def set_spin_limit(self, iterations=0):
         """Bound of the kernels' inter-CTA waits in polling iterations (0: the
@@ -541,6 +587,17 @@ class MixDom2Prologue:
         self.struct = MixDom2Params(self.K, self.F, self.C, self.A, float(host(params['main_ins'])),
                                     float(host(params['main_del'])), *[dp(arr[k]) for k in self.KEYS])
         self.N, self.G = 2 + 5 * self.K * self.F, self.K * self.F
+
+    def class_Q(self):
+        """The class rate matrices Q_c[a,b] = S_c[a,b] pi_c[b] with rows summing
+        to zero (train/vjp.py:463-476), float64 [C,A,A] on the host."""
+        if getattr(self, '_Q', None) is None:
+            Q = self._arr['class_S_exch'] * self._arr['class_pis'][:, None, :]
+            for c in range(Q.shape[0]):
+                np.fill_diagonal(Q[c], 0.0)
+                np.fill_diagonal(Q[c], -Q[c].sum(axis=1))
+            self._Q = np.ascontiguousarray(Q)
+        return self._Q
 
     def shapes(self, P):
         """(chi, emit_M, emit_I, emit_D, class_subs) shapes for P pairs."""

@@ -27,6 +27,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from . import autotune, graphs
 from . import models as pm
 
 NEG_INF = -1e30
@@ -901,12 +902,20 @@ def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True, exact_suffst
     model (exact_suffstats_batch on n_trans)."""
     dev = _device()
     pro = _lib.MixDom2Prologue(params)
+    K, F = pro.K, pro.F
+    plan = get_plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)
+    if with_class_counts and not exact_suffstats:
+        # a batch shape seen before replays its captured CUDA graph (pairhmm.graphs)
+        g = graphs.mixdom2_estep(pro, xs, ys, ts, dev, tuned_plan=plan)
+        if g is not None:
+            res = {'log_p': g['ll']}
+            res.update({k: v for k, v in g.items() if k != 'll'})
+            return res
     t_dev = (ts if isinstance(ts, torch.Tensor) else torch.from_numpy(
         np.ascontiguousarray(np.asarray(ts, np.float64).reshape(-1)))).to(device=dev, dtype=torch.float64)
     chi, EM, EI, ED, csubs = pro(t_dev, device=dev)
-    K, F = pro.K, pro.F
-    plan = get_plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)
     b = _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev)
+    autotune.apply_cached(plan, b)
     # every output in one device buffer: one copy brings them all to the host
     P, N, G, C, A = b.n_pairs, 2 + 5 * K * F, K * F, pro.C, pro.A
     f64 = torch.float64

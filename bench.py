@@ -76,6 +76,7 @@ def parse_args():
     ap.add_argument('--max-len', type=int, default=0,
                     help='truncate every sequence to at most L residues (small case for ncu captures)')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
+    ap.add_argument('--no-tune', action='store_true', help='skip the autotuner (library defaults)')
     ap.add_argument('--no-accuracy', action='store_true',
                     help='skip the accuracy leg (every pair against the FP64 oracle)')
     ap.add_argument('--serving-requests', type=int, default=2000,
@@ -398,10 +399,22 @@ def serving_leg(n_requests, rate, seed=0):
         return summ
     cont = one(max_inflight=8, max_batch=64)
     plain = one(max_inflight=1, max_batch=1)
+    # the same requests offered below saturation (arrival times stretched), so
+    # the latency of the batching itself shows apart from queueing
+    below = {}
+    base_offsets = offsets
+    for r in (1000.0, 2000.0, 3000.0):
+        if r >= rate:
+            continue
+        offsets = np.asarray(base_offsets) * (rate / r)
+        summ = one(max_inflight=8, max_batch=64)
+        below[f'{r:g}'] = {k: summ[k] for k in ('p50_ms', 'p99_ms', 'mean_ms', 'req_per_s', 'failed', 'mean_batch')}
+    offsets = base_offsets
     return {'workload': f'Poisson {rate:g} req/s, {n_requests} requests, model uniform over TKF92 (5) / '
                         'MixDom2 K3F1C1 (17) / MixDom2 K4F2C2 (42), ancestor LogUniform(20,2000)',
             'arrival_span_s': float(offsets[-1]), 'cell_states': cs,
             'continuous': cont, 'plain_one_launch_per_request': plain,
+            'continuous_below_saturation': below,
             'arena_bytes': ARENA, 'stream_generation_s': gen_s}
 
 
@@ -477,7 +490,21 @@ def main():
     from pairhmm import synth, api, _lib
     from pairhmm import models as pm
     dev = torch.device('cuda', local)
-    w = synth.CONFIGS[args.workload](seed=rank)
+    w = synth.CONFIGS[args.workload](seed=0)
+    shard = None
+    if ws > 1:
+        # one combined workload of ws x the configuration (seeds 0..ws-1), split
+        # over the ranks by longest-processing-time packing of the E-step cost:
+        # every rank holds about one configuration's work (weak scaling)
+        from pairhmm import replicas
+        parts = [w] + [synth.CONFIGS[args.workload](seed=s) for s in range(1, ws)]
+        allx = [x for q in parts for x in q.xs]
+        ally = [y for q in parts for y in q.ys]
+        allt = np.concatenate([np.asarray(q.ts) for q in parts])
+        shard = replicas.lpt_partition(replicas.pair_costs(allx, ally, w.n_states), ws)[rank]
+        w.xs = [allx[i] for i in shard]
+        w.ys = [ally[i] for i in shard]
+        w.ts = allt[shard]
     if args.pairs:
         w.xs, w.ys, w.ts = w.xs[:args.pairs], w.ys[:args.pairs], w.ts[:args.pairs]
     if args.max_len:
@@ -498,9 +525,24 @@ def main():
         EM, EI, ED = pm.tables_tkf(pm.transition_matrix(pm._t(w.params['Q'], dev), tt), pm._t(w.params['pi'], dev))
         plan = api.get_plan(np.array([pm.S, pm.M, pm.I, pm.D, pm.E]), np.zeros(5, np.int32), 1)
     batch = _lib.make_batch(w.xs, w.ys, chi, EM, EI, ED, device=dev)
-    plan.set_timing(True)
     if args.variant:
         plan.set_variant(args.variant)
+    # the project's autotuner (pairhmm.autotune) picks the launch configuration
+    # for this batch before anything is timed; skipped when one call is long
+    tuning = None
+    if not args.no_tune and not args.variant:
+        from pairhmm import autotune
+        t0 = time.perf_counter()
+        (_lib.forward(plan, batch) if fwd_only else _lib.estep(plan, batch))
+        torch.cuda.synchronize()
+        one_ms = (time.perf_counter() - t0) * 1e3
+        if one_ms < 200.0:
+            r = autotune.tune(plan, batch, forward_only=fwd_only)
+            tuning = {'chosen': r['tuning'], 'ms': r['ms'], 'default_ms': r['default_ms'],
+                      'evaluated': r['evaluated'], 'by': 'pairhmm.autotune (coordinate descent, CUDA events)'}
+        else:
+            tuning = {'chosen': plan.get_tuning(), 'skipped': f'one call takes {one_ms:.0f} ms'}
+    plan.set_timing(True)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
 
@@ -544,7 +586,7 @@ def main():
         dist.barrier()
     clocks = sampler.stop()
     total_ms = float(np.sum(step_ms))
-    cells_all = cell_states   # cell-state updates of one step over all ranks (each rank draws its own pairs)
+    cells_all = cell_states   # cell-state updates of one step over all ranks (each rank its LPT shard)
     if ws > 1:
         t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -656,7 +698,10 @@ def main():
             'config': {'workload': args.workload, 'model': spec['model'],
                        'n_states': N, 'pairs_per_gpu': len(w.xs), 'cells_per_gpu': int(total_cells),
                        'cell_states_per_step_per_gpu': cell_states, 'pairs_per_s': len(w.xs) * ws / (ms_step / 1e3),
-                       'l2': 'flushed (256 MiB write) between timed steps', 'parallelism': f'replicas x{ws}',
+                       'l2': 'flushed (256 MiB write) between timed steps',
+                       'parallelism': (f'replicas x{ws}, one combined workload of {ws} configurations '
+                                       'LPT-sharded by E-step cost' if ws > 1 else 'replicas x1'),
+                       'tuning': tuning,
                        'status_nonzero': int((status != 0).sum())},
             'roofline': roofline, 'roofline_hbm': roofline_hbm, 'cpu_baseline': cpu, 'accuracy': acc,
             'e2e': {'value': e2e_value, 'unit': 'cell-state updates/s', 'h2d_bytes_per_step': h2d,

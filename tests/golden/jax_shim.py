@@ -10,7 +10,11 @@ Semantics reproduced (with x64 enabled, as the reference requires):
     (set / add / multiply / min / max / get);
   * integer-array gathers clamp out-of-range indices (JAX's default gather
     mode), scatters into a copy;
-  * jit / checkpoint / custom_vjp are identity wrappers (forward values only);
+  * jit / checkpoint / custom_vjp are identity wrappers (forward values only;
+    a custom VJP's fwd / bwd functions are called directly by the fixture
+    scripts);
+  * grad is a Richardson-extrapolated central difference, for the closed-form
+    functions that the reference's VJP backward passes differentiate;
   * vmap / lax.scan / lax.fori_loop are Python loops with pytree stacking;
   * nn.logsumexp follows JAX's max-shift formula; nn.one_hot drops
     out-of-range classes.
@@ -365,8 +369,39 @@ def checkpoint(f=None, **_):
     return f
 
 
-def grad(*_, **__):
-    raise NotImplementedError('jax.grad is not available in the NumPy stand-in')
+def grad(f, argnums=0, **_):
+    """jax.grad for the small closed-form functions the reference's custom
+    VJP backward passes differentiate (sum n log chi(theta) and its t-only
+    variants), by central differences with two levels of Richardson
+    extrapolation from steps h, h/2, h/4 (error O(h^6)) at h = 1 % of the
+    entry.  The large step matters: the chi builders carry ~1e-13 of relative
+    rounding noise (a Gauss-Jordan solve), which small steps would amplify;
+    at this step the noise costs ~1e-8 relative and the truncation less."""
+    single = isinstance(argnums, int)
+    nums = (argnums,) if single else tuple(argnums)
+
+    def g(*args):
+        outs = []
+        for n in nums:
+            x0 = np.array(args[n], dtype=np.float64)
+            flat = x0.reshape(-1)
+            gflat = np.zeros_like(flat)
+            for i in range(flat.size):
+                def at(h, i=i):
+                    xx = flat.copy()
+                    xx[i] += h
+                    a = list(args)
+                    a[n] = _wrap(xx.reshape(x0.shape)) if x0.ndim else float(xx[0])
+                    return float(np.asarray(f(*a)))
+                h = 1e-2 * max(abs(flat[i]), 1e-3)
+                d = [(at(h / k) - at(-h / k)) / (2 * h / k) for k in (1, 2, 4)]
+                r1 = (4.0 * d[1] - d[0]) / 3.0
+                r2 = (4.0 * d[2] - d[1]) / 3.0
+                gflat[i] = (16.0 * r2 - r1) / 15.0
+            gx = gflat.reshape(x0.shape)
+            outs.append(_wrap(gx) if x0.ndim else float(gx))
+        return outs[0] if single else tuple(outs)
+    return g
 
 
 def install():

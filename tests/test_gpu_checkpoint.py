@@ -5,7 +5,7 @@ recomputes each stripe's forward and backward recursion from them in the
 count pass, in groups of one wave of the recompute kernel (76 stripes on 152
 SMs).  It runs the same arithmetic as the full-lattice E-step on the same
 inputs, so the log-likelihoods must be bit for bit the same and the counts
-equal to summation order (1e-12); against the FP64 oracle the usual bars
+equal up to the order of float32 atomic sums (2e-6); against the FP64 oracle the usual bars
 hold (LL 1e-6, counts 1e-5).  A batch of 320 stripes runs the count pass in
 several groups.  For one 8000 x 8000 pair the scratch it asks for must be a
 fraction of the full layout's.
@@ -43,9 +43,13 @@ def _setup(K, F, C, lengths, seed):
 
 
 def _same(a, b):
+    """Log-likelihoods bit for bit (the same forward arithmetic); counts to
+    2e-6 (the count pass sums emission posteriors with float32 atomics in
+    shared memory, so their order -- and the last bits -- vary from call to
+    call in either mode)."""
     assert np.array_equal(a['ll'], b['ll']) and (a['status'] == 0).all() and (b['status'] == 0).all()
     for k in ('n_trans', 'cnt_M', 'cnt_I', 'cnt_D'):
-        np.testing.assert_allclose(a[k], b[k], rtol=1e-12, atol=1e-13 * max(1.0, np.abs(b[k]).max()))
+        np.testing.assert_allclose(a[k], b[k], rtol=2e-6, atol=1e-9 * max(1.0, np.abs(b[k]).max()))
 
 
 @pytest.mark.parametrize('K,F,C', [(8, 4, 4), (4, 4, 1)])

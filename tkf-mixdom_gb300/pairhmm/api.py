@@ -1170,3 +1170,62 @@ def estep_batch_tkf92(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, ext, Q, pi)
     res.pop('n_trans_resolved')
     res.update({'log_p': out['ll'], 'n_chi_diag': out['n_trans'], 'status': out['status']})
     return res
+
+
+def _mixfrag_batch(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, exts, weights, Q, pi):
+    dev = _device()
+    F = int(np.asarray(exts).size)
+    tt = torch.as_tensor(np.asarray(ts, np.float64).reshape(-1))
+    # chi floored at 1e-30 as the reference takes log(max(tau, 1e-30)) (mixfrag_svi_bw.py:136)
+    chi = torch.clamp(pm.mixfrag_trans_batch(lam, mu, tt, exts, weights), min=1e-30)
+    EM, EI, ED = pm.tables_tkf(pm.transition_matrix(pm._t(Q), tt), pm._t(pi))
+    Lx_real = np.asarray(Lx_real).reshape(-1)
+    Ly_real = np.asarray(Ly_real).reshape(-1)
+    xs = [np.asarray(xs_pad[b])[:int(Lx_real[b])] for b in range(len(Lx_real))]
+    ys = [np.asarray(ys_pad[b])[:int(Ly_real[b])] for b in range(len(Ly_real))]
+    st = pm.mixfrag_state_types(F)
+    plan = get_plan(st, np.zeros(st.size, np.int32), 1)
+    return plan, _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev)
+
+
+def estep_batch_mixfrag_forward_only(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, exts, weights, Q, pi):
+    """Per-pair log_p of pre-padded pairs under MixFrag (TKF92 with F fragment
+    types; train/mixfrag_svi_bw.py:236-250)."""
+    plan, b = _mixfrag_batch(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, exts, weights, Q, pi)
+    ll, st = _lib.forward(plan, b)
+    return ll
+
+
+def estep_batch_mixfrag(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, exts, weights, Q, pi):
+    """Batched MixFrag E-step (train/mixfrag_svi_bw.py:194-232): dict of device
+    tensors 'log_p', 'B', 'D', 'S' (BDI statistics of the fragment-resolved
+    counts), 'L', 'M' (kappa coefficients), 'T', 'F_f' / 'E_f' [P, F]
+    (fragment-extension and fragment-end counts per fragment type), plus
+    'n_chi' [P, 3F+2, 3F+2] and 'status'.  The DP runs on the GPU; the
+    resolution and the BDI statistics are the float64 epilogue of pairhmm.bdi."""
+    from . import bdi
+    plan, b = _mixfrag_batch(xs_pad, ys_pad, ts, Lx_real, Ly_real, lam, mu, exts, weights, Q, pi)
+    out = _lib.estep(plan, b)
+    res = bdi.mixfrag_bdi_epilogue(out['n_trans'], lam, mu, np.asarray(ts, np.float64), exts, weights)
+    res.update({'log_p': out['ll'], 'n_chi': out['n_trans'], 'status': out['status']})
+    return res
+
+
+def tkf92_log_prob_fb(lam, mu, ext, t, Q, pi, x_seq, y_seq, real_Lx=None, real_Ly=None):
+    """log P(x, y | TKF92(lam, mu, ext), Q, pi, t) (train/tkf92_adam_fb.py:77-104):
+    the TKF92 matrix floored at 1e-30 in log space, differentiable in every
+    float argument (score identity over the CUDA E-step).  With real_Lx /
+    real_Ly the sequences are taken as padded and cut to those lengths."""
+    dev = _device()
+    f = lambda v: pm._t(v, device=dev)
+    x = np.asarray(x_seq)
+    y = np.asarray(y_seq)
+    if real_Lx is not None:
+        x = x[:int(real_Lx)]
+    if real_Ly is not None:
+        y = y[:int(real_Ly)]
+    tt = f(t).reshape(-1)
+    chi = torch.clamp(pm.tkf92_trans(f(lam), f(mu), tt, f(ext)), min=1e-30)
+    EM, EI, ED = pm.tables_tkf(pm.transition_matrix(f(Q), tt), f(pi))
+    plan = get_plan(np.array([S, M, I, D, E]), np.zeros(5, np.int32), 1)
+    return PairHMMLogLik.apply(chi, EM, EI, ED, plan, [x], [y])[0]

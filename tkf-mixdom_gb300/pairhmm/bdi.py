@@ -136,3 +136,51 @@ def tkf92_bdi_epilogue(n_chi, ins_rate, del_rate, t, ext, T=None):
     return {'B': torch.maximum(E_B, zero), 'D': torch.maximum(E_D, zero), 'S': torch.maximum(E_S, zero),
             'L': L, 'M': Mc, 'T': tt if T is None else pm._t(T, device=res.device).reshape(-1),
             'ext_count': ext_count, 'notext_count': notext, 'n_trans_resolved': res}
+
+
+def mixfrag_resolve(n_chi, ins_rate, del_rate, t, exts, weights):
+    """MixFrag chi counts [B, 3F+2, 3F+2] -> (resolved 5x5 TKF91-type counts
+    [B, 5, 5], F_f [B, F] fragment-extension counts, E_f [B, F] fragment-end
+    counts), train/mixfrag_svi_bw.py:59-110: the a_f -> a_f self-loop count
+    splits into extension, ext_f / (ext_f + (1 - ext_f) tau91[a, a] w_f) of it,
+    and a new fragment link; the resolved counts are summed over fragment
+    types."""
+    n = pm._t(n_chi)
+    dev = n.device
+    B, ns = n.shape[0], n.shape[1]
+    F = (ns - 2) // 3
+    exts = pm._t(exts, device=dev).reshape(-1)
+    w = pm._t(weights, device=dev).reshape(-1)
+    tau91 = pm.tkf91_trans(pm._t(float(ins_rate)), pm._t(float(del_rate)),
+                           pm._t(t).reshape(-1).cpu()).to(dev)
+    res = n.clone()
+    F_f = torch.zeros(B, F, dtype=F64, device=dev)
+    E_f = torch.zeros(B, F, dtype=F64, device=dev)
+    for k, ty in enumerate((M, I, D)):
+        diag = tau91[:, ty, ty]
+        for f in range(F):
+            a = 1 + k * F + f
+            loop = exts[f] + (1.0 - exts[f]) * diag * w[f]
+            frac = torch.where(loop > 1e-30, exts[f] / torch.clamp(loop, min=1e-30), torch.zeros_like(loop))
+            Faf = torch.clamp(frac, 0.0, 1.0) * n[:, a, a]
+            F_f[:, f] += Faf
+            E_f[:, f] += n[:, a, :].sum(-1)
+            res[:, a, a] -= Faf
+    E_f = E_f - F_f
+    types = torch.as_tensor(pm.mixfrag_state_types(F), device=dev)
+    agg = torch.zeros(5, ns, dtype=F64, device=dev)
+    agg[types, torch.arange(ns, device=dev)] = 1.0
+    return agg[None] @ res @ agg.T[None], F_f, E_f
+
+
+def mixfrag_bdi_epilogue(n_chi, ins_rate, del_rate, t, exts, weights):
+    """The dict of estep_batch_mixfrag beyond log_p (train/mixfrag_svi_bw.py:194-232):
+    B, D, S (BDI statistics of the resolved counts, floored at 0), L, M
+    (kappa coefficients), T (= t), F_f, E_f."""
+    res5, F_f, E_f = mixfrag_resolve(n_chi, ins_rate, del_rate, t, exts, weights)
+    L, Mc = kappa_coefficients(res5)
+    tt = pm._t(t, device=res5.device).reshape(-1)
+    E_B, E_D, E_S = bdi_stats(res5, ins_rate, del_rate, tt, tt)
+    zero = torch.zeros_like(E_B)
+    return {'B': torch.maximum(E_B, zero), 'D': torch.maximum(E_D, zero), 'S': torch.maximum(E_S, zero),
+            'L': L, 'M': Mc, 'T': tt, 'F_f': F_f, 'E_f': E_f}

@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import warnings
 from collections import OrderedDict
 
 import numpy as np
@@ -117,7 +118,9 @@ class MixDom2EStepGraph:
         parts = [None] * (2 * len(xs))
         parts[0::2] = xs
         parts[1::2] = ys
-        allr = np.concatenate([np.asarray(v).reshape(-1) for v in parts]) if parts else np.zeros(0, np.int64)
+        allr = np.concatenate(parts) if parts else np.zeros(0, np.int64)
+        if allr.ndim != 1:
+            raise ValueError('sequences must be one-dimensional')
         if allr.size != self.total or (allr.size and (allr.min() < 0 or allr.max() > 20)):
             raise ValueError('residues must be integers in 0..20 (20 = wildcard), with the captured lengths')
         self.h_res.numpy()[:allr.size] = allr
@@ -215,9 +218,11 @@ def mixdom2_estep(pro, xs, ys, ts, device, tuned_plan=None):
             if tuned_plan is not None:
                 g.tune_from(tuned_plan)
             g.capture(pro, xs, ys, ts)
-        except Exception:
+        except Exception as e:
             _SEEN[key] = -(1 << 30)   # never again for this shape
             torch.cuda.synchronize()
+            warnings.warn(f'CUDA graph capture of the batched E-step failed ({e!r}); this batch shape runs '
+                          'eagerly', RuntimeWarning)
             return None
         _GRAPHS[key] = g
         while len(_GRAPHS) > MAX_GRAPHS:

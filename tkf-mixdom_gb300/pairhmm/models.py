@@ -127,6 +127,34 @@ def mixfrag_trans(lam, mu, t, exts, weights):
     return torch.stack(rows)
 
 
+def mixfrag_state_types(F):
+    """Types of the (3F+2) MixFrag states S, M_1..M_F, I_1..I_F, D_1..D_F, E."""
+    return np.array([S] + [M] * F + [I] * F + [D] * F + [E])
+
+
+def mixfrag_trans_batch(lam, mu, t, exts, weights):
+    """[B, 3F+2, 3F+2] MixFrag matrices for times t [B] (core/params.py:136-179,
+    vectorised over t): entry (a, b) = row factor x TKF91[type a, type b] x
+    column factor, with row factor 1 for S and (1 - ext_f) for an emitting
+    state of fragment type f, column factor w_g for an emitting state of type
+    g, 1 for E and 0 for S, plus ext_f on the diagonal of each emitting state;
+    the E row is zero."""
+    t91 = tkf91_trans(lam, mu, _t(t).reshape(-1))
+    dev = t91.device
+    exts = _t(exts, device=dev).reshape(-1)
+    w = _t(weights, device=dev).reshape(-1)
+    F = exts.shape[0]
+    st = mixfrag_state_types(F)
+    idx = torch.as_tensor(st, device=dev)
+    base = t91[:, idx][:, :, idx]
+    one, zero = torch.ones((), dtype=F64, device=dev), torch.zeros((), dtype=F64, device=dev)
+    emit_f = [None] + list(range(F)) * 3 + [None]
+    colw = torch.stack([zero] + [w[g] for g in emit_f[1:-1]] + [one])
+    roww = torch.stack([one] + [1.0 - exts[f] for f in emit_f[1:-1]] + [zero])
+    loop = torch.stack([zero] + [exts[f] for f in emit_f[1:-1]] + [zero])
+    return roww[None, :, None] * base * colw[None, None, :] + torch.diag(loop)[None]
+
+
 # ---------------------------------------------------------------- MixDom
 _UV_EMIT = [M, I, D, I, D]
 _UV_U = [M, M, M, I, D]

@@ -49,13 +49,9 @@ WORKLOADS = {
         'forward_only': True, 'metric': 'pair-HMM forward cell-state updates/s',
         'model': 'TKF91', 'e2e_api': 'pairhmm.api.estep_batch_tkf92_forward_only (ext = 0)'},
 }
-# ncu summaries holding 'traffic_bytes_per_launch_full_workload[<kernel>]: <bytes>' lines
-PROFILE_SUMMARY = {
-    'mixdom2_k3f1c1_200pairs_len30-600': 'estep_kernels_mixdom2_k3f1c1.md',
-    'mixdom2_k4f2c2_32pairs_len200-1500': 'estep_kernels_mixdom2_k4f2c2.md',
-    'mixdom2_k8f4c4_64pairs_len2000': 'estep_kernels_mixdom2_k8f4c4.md',
-    'tkf91_64pairs_len50-150': 'forward_kernels_tkf91.md',
-}
+# DRAM bytes per launch of each kernel on each workload, from the committed ncu
+# captures (profiles/traffic.json; the Markdown summaries beside it give the commands)
+TRAFFIC_FILE = os.path.join(ROOT, 'profiles', 'traffic.json')
 SMS = 152
 FP32_LANES_PER_SM = 128
 
@@ -114,15 +110,13 @@ def hbm_roofline(kernel, n_states, total_cells, dur_ms, hbm_peak_gbs, traffic):
 
 
 def profile_traffic(workload, kernel):
-    """dram bytes per launch of `kernel` on `workload` from the committed ncu summary."""
-    key = f'traffic_bytes_per_launch_full_workload[{kernel.split("::")[-1]}]:'
+    """DRAM bytes per launch of `kernel` on `workload` from profiles/traffic.json
+    (None when no capture covers it)."""
     try:
-        for line in open(os.path.join(ROOT, 'profiles', PROFILE_SUMMARY[workload])):
-            if line.startswith(key):
-                return float(line[len(key):].split()[0])
-    except (OSError, ValueError, KeyError):
-        pass
-    return None
+        with open(TRAFFIC_FILE) as f:
+            return float(json.load(f)[workload][kernel.split('::')[-1]])
+    except (OSError, ValueError, KeyError, TypeError):
+        return None
 
 
 class ClockSampler:

@@ -2,7 +2,7 @@
 
 Usage (needs the reference checkout; writes tests/golden/*.npz):
 
-    python tests/golden/make_golden.py /root/reference/python
+    python tests/golden/make_golden.py <reference>/python
 
 The reference modules (``tkfmixdom/jax/dp/hmm.py``, ``models/mixdom.py``,
 ``core/params.py``, ``core/bdi.py``, ``core/ctmc.py``,
@@ -239,4 +239,6 @@ def main(ref_python):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference/python')
+    if len(sys.argv) != 2:
+        sys.exit('usage: python tests/golden/make_golden.py <reference checkout>/python')
+    main(sys.argv[1])

@@ -6,7 +6,7 @@ MixDom model with one substitution model.
 
 Usage (needs the reference checkout; writes tests/golden/beam.npz):
 
-    python tests/golden/make_golden_beam.py /root/reference/python
+    python tests/golden/make_golden_beam.py <reference>/python
 
 JAX is replaced by the NumPy stand-in of ``jax_shim.py`` (the beam module
 itself is NumPy).  Guide alignments are seeded random M/I/D strings.
@@ -100,4 +100,6 @@ def main(ref_python):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get('TKF_REFERENCE_PYTHON', ''))
+    if len(sys.argv) != 2:
+        sys.exit('usage: python tests/golden/make_golden_beam.py <reference checkout>/python')
+    main(sys.argv[1])

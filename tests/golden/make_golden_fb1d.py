@@ -7,7 +7,7 @@ by the reference's own modules: ``dp/hmm.py`` ``forward_backward_1d_padded``
 
 Usage (needs the reference checkout; writes tests/golden/fb1d.npz):
 
-    python tests/golden/make_golden_fb1d.py /root/reference/python
+    python tests/golden/make_golden_fb1d.py <reference>/python
 
 JAX is replaced by the NumPy stand-in of ``jax_shim.py``.  Alignments are
 seeded random column-type strings (M / I / D) with random characters.
@@ -95,4 +95,6 @@ def main(ref_python):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get('TKF_REFERENCE_PYTHON', ''))
+    if len(sys.argv) != 2:
+        sys.exit('usage: python tests/golden/make_golden_fb1d.py <reference checkout>/python')
+    main(sys.argv[1])

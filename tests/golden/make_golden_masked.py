@@ -7,7 +7,7 @@ substitution model (chi from ``models/mixdom.py`` ``build_nested_trans``).
 
 Usage (needs the reference checkout; writes tests/golden/masked.npz):
 
-    python tests/golden/make_golden_masked.py /root/reference/python
+    python tests/golden/make_golden_masked.py <reference>/python
 
 JAX is replaced by the NumPy stand-in of ``jax_shim.py``.  Guide alignments
 are seeded random M/I/D strings of the pair's lengths.
@@ -108,4 +108,6 @@ def main(ref_python):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get('TKF_REFERENCE_PYTHON', ''))
+    if len(sys.argv) != 2:
+        sys.exit('usage: python tests/golden/make_golden_masked.py <reference checkout>/python')
+    main(sys.argv[1])

@@ -7,7 +7,7 @@ them once decompressed), their ``decode_pair`` outputs, and the
 Usage (needs the reference checkout; writes tests/golden/pairs.jsonl and
 tests/golden/pairs.npz):
 
-    python tests/golden/make_golden_pairs.py /root/reference/python
+    python tests/golden/make_golden_pairs.py <reference>/python
 """
 from __future__ import annotations
 
@@ -74,4 +74,6 @@ def main(ref_python):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get('TKF_REFERENCE_PYTHON', ''))
+    if len(sys.argv) != 2:
+        sys.exit('usage: python tests/golden/make_golden_pairs.py <reference checkout>/python')
+    main(sys.argv[1])

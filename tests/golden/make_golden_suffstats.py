@@ -6,7 +6,7 @@ model of ``models/fully_exploded.py`` and walk the elimination chain of
 
 Usage (needs the reference checkout; writes tests/golden/exact_suffstats.npz):
 
-    python tests/golden/make_golden_suffstats.py /root/reference/python
+    python tests/golden/make_golden_suffstats.py <reference>/python
 
 JAX is replaced by the NumPy stand-in of ``jax_shim.py``.  The collapsed
 counts n_chi are seeded random non-negative matrices on the support of chi
@@ -73,4 +73,6 @@ def main(ref_python):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get('TKF_REFERENCE_PYTHON', ''))
+    if len(sys.argv) != 2:
+        sys.exit('usage: python tests/golden/make_golden_suffstats.py <reference checkout>/python')
+    main(sys.argv[1])

@@ -4,7 +4,7 @@ model, chi from ``models/mixdom.py`` ``build_nested_trans``).
 
 Usage (needs the reference checkout; writes tests/golden/viterbi.npz):
 
-    python tests/golden/make_golden_viterbi.py /root/reference/python
+    python tests/golden/make_golden_viterbi.py <reference>/python
 
 JAX is replaced by the NumPy stand-in of ``jax_shim.py``; the sequences hold
 no wildcard (the reference's viterbi_2d indexes a 20 x 20 matrix).
@@ -65,4 +65,6 @@ def main(ref_python):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get('TKF_REFERENCE_PYTHON', ''))
+    if len(sys.argv) != 2:
+        sys.exit('usage: python tests/golden/make_golden_viterbi.py <reference checkout>/python')
+    main(sys.argv[1])

@@ -162,9 +162,11 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
             d0[q].x = l0 ? (top ? (halo ? hx[2 * q] : 0.f) : bv[2 * q]) : vx;
             d0[q].y = l0 ? (top ? (halo ? hx[2 * q + 1] : 0.f) : bv[2 * q + 1]) : vy;
         }
-        // a type that may not emit here contributes nothing (nor its exponent)
-        const bool hasI = jc >= 1 && (mbx & 2), hasD = rowi >= 1 && (mbx & 4);
-        const bool hasM = jc >= 1 && rowi >= 1 && (mbx & 1);
+        // a type that may not emit here contributes nothing (nor its exponent);
+        // outside the lattice nothing emits, so the type scales below are zero
+        // there and no separate select clears the cell
+        const bool hasI = valid && jc >= 1 && (mbx & 2), hasD = valid && rowi >= 1 && (mbx & 4);
+        const bool hasM = valid && jc >= 1 && rowi >= 1 && (mbx & 1);
         const int EI = hasI ? Eprev : EXP_NONE, ED = hasD ? EdA : EXP_NONE, EM = hasM ? Em0 : EXP_NONE;
         const int Eref = max(max(EI, ED), EM);
         float2 acc2[NE];
@@ -206,7 +208,7 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
                 if (ty == T_M) e = eMI[k] * sM;
                 else if (ty == T_I) e = eMI[k] * sI;
                 else e = eD[k - NM - NI] * sD;
-                acc[k] = valid ? acc[k] * e : 0.f;
+                acc[k] = acc[k] * e;
                 mxs[k & 3] = fmaxf(mxs[k & 3], acc[k]);
             }
             mx = fmaxf(fmaxf(mxs[0], mxs[1]), fmaxf(mxs[2], mxs[3]));

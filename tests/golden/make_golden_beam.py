@@ -2,7 +2,8 @@
 the reference's own ``dp/hmm_beam.py``: ``msa_to_envelope`` around a guide
 alignment, ``beam_forward_2d`` and ``beam_forward_backward_2d`` with and
 without an envelope and with finite and infinite beam widths, for TKF91 and a
-MixDom model with one substitution model.
+MixDom model with one substitution model, and ``beam_sample_traceback`` paths
+drawn on each case's forward table with a seeded ``numpy.random.RandomState``.
 
 Usage (needs the reference checkout; writes tests/golden/beam.npz):
 
@@ -79,6 +80,14 @@ def main(ref_python):
         out[pre + 'F'] = np.asarray(F)
         out[pre + 'n_cells'] = np.int64(n_cells)
         assert lp_f == lp
+        # four consecutive draws from one seeded RandomState (hmm_beam.py:493-563)
+        seed = 1000 + len(out)
+        draw = np.random.RandomState(seed)
+        paths = [np.asarray(hb.beam_sample_traceback(lt, st, F, lp, x, y, sub, pi, draw, env), np.int64).reshape(-1, 3)
+                 for _ in range(4)]
+        out[pre + 'sample_seed'] = np.int64(seed)
+        out[pre + 'sample_lens'] = np.array([len(q) for q in paths], np.int64)
+        out[pre + 'sample_paths'] = np.concatenate(paths)
     # iterative refinement around the diagonal (hmm_beam.py:321-394)
     Q, pi, _ = rand_Q_pi(rng)
     t = 0.5

@@ -78,3 +78,22 @@ def test_beam_viterbi_matches_reference(cuda_lib, name):
     ref = float(g[pre + 'viterbi_log_prob'])
     assert abs(lp - ref) <= 1e-12 * abs(ref)
     assert np.array_equal(np.asarray(path), g[pre + 'viterbi_path'])
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_beam_sample_traceback_on_own_forward_table(cuda_lib, name):
+    """Paths drawn on the GPU's pruned forward table with the reference's
+    seed equal the reference's own draws on its float64 table (the tables
+    agree to float32 rounding, far from any draw's cumulative-weight edge)."""
+    from pairhmm import api
+    g = load_golden('beam')
+    pre = name + '_'
+    args = _args(g, pre)
+    lp, F, _ = api.beam_forward_2d(*args)
+    rng = np.random.RandomState(int(g[pre + 'sample_seed']))
+    lens = g[pre + 'sample_lens']
+    rows = g[pre + 'sample_paths']
+    ends = np.cumsum(lens)
+    for a, b in zip(np.r_[0, ends[:-1]], ends):
+        got = api.beam_sample_traceback(args[0], args[1], F, lp, args[2], args[3], args[4], args[5], rng, args[7])
+        assert np.array_equal(np.asarray(got, np.int64).reshape(-1, 3), rows[a:b])

@@ -486,6 +486,59 @@ def beam_viterbi_2d(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, envelo
     return float(ll[0]), [tuple(int(v) for v in row) for row in paths[0]]
 
 
+_PRED_STEP = {M: (1, 1), I: (0, 1), D: (1, 0)}
+
+
+def _draw_state(scores, rng):
+    """A state index drawn with probability proportional to exp(scores) by
+    rng.choice, or None when every score is within 100 of NEG_INF."""
+    top = np.max(scores)
+    if top <= NEG_INF + 100:
+        return None
+    w = np.exp(scores - top)
+    return int(rng.choice(scores.size, p=w / w.sum()))
+
+
+def beam_sample_traceback(log_trans, state_types, F, log_prob, x_seq, y_seq, sub_matrix, pi, rng, envelope=None):
+    """Alignment path [(i, j, state), ...] from (0, 0, S) to (Lx, Ly, .) drawn
+    from the posterior on a (beam-pruned) forward table -- dp/hmm_beam.py:493-563.
+
+    The end state is drawn from F[Lx, Ly] + log_trans[:, E], then each
+    predecessor from F[previous cell] + log_trans[:, current state], each draw
+    one rng.choice on the normalised weights, so with the reference's
+    numpy.random.RandomState and forward table the path is the same draw for
+    draw.  The walk stops early (the origin is still appended) at a state that
+    cannot step back from its cell, at a predecessor cell outside the
+    envelope, or where every predecessor score is at NEG_INF; an empty list
+    means the end cell itself is unreachable.  F is the (Lx+1, Ly+1, N) table
+    of beam_forward_2d; log_prob, the residues, sub_matrix and pi are not
+    read (the reference's signature)."""
+    lt = np.asarray(log_trans)
+    st = np.asarray(state_types)
+    F = np.asarray(F)
+    Lx, Ly = len(x_seq), len(y_seq)
+    k = _draw_state(F[Lx, Ly, :] + lt[:, int(np.argmax(st == E))], rng)
+    if k is None:
+        return []
+    i, j = Lx, Ly
+    path = []
+    while i > 0 or j > 0:
+        path.append((i, j, k))
+        di, dj = _PRED_STEP.get(int(st[k]), (i + 1, j + 1))
+        if di > i or dj > j:
+            break
+        pi_, pj = i - di, j - dj
+        if envelope is not None and not envelope[pi_, pj]:
+            break
+        prev = _draw_state(F[pi_, pj, :] + lt[:, k], rng)
+        if prev is None:
+            break
+        i, j, k = pi_, pj, prev
+    path.append((0, 0, int(S)))
+    path.reverse()
+    return path
+
+
 def estep_batch_match_aligned(log_chi, state_types, xs, ys, match_is, match_js, sub_matrices, pis, n_dom, n_frag):
     """Batched match-aligned MixDom E-step (train_pfam.py:1744-1800,
     2946-2990: per-domain emissions, mask_emissions_match_aligned, the 2D

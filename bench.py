@@ -78,6 +78,8 @@ def parse_args():
     ap.add_argument('--serving-requests', type=int, default=2000,
                     help='requests in the serving-stream leg (0: skip it)')
     ap.add_argument('--serving-rate', type=float, default=5000.0)
+    ap.add_argument('--banded-pairs', type=int, default=1024,
+                    help='pairs of the banded-vs-full E-step leg (0: skip)')
     return ap.parse_args()
 
 
@@ -412,6 +414,64 @@ def serving_leg(n_requests, rate, seed=0):
             'arena_bytes': ARENA, 'stream_generation_s': gen_s}
 
 
+def banded_leg(n_pairs, length=500, band=32, reps=7, seed=0):
+    """The banded E-step (phmm_estep_band: the reference's
+    forward_backward_2d_banded, dp/hmm.py:2395-2491, over a batch) against the
+    full-lattice E-step of the same pairs: TKF91 pairs of about
+    length x length, band of half-width `band` around the diagonal.  The
+    stripes skip the anti-diagonal steps off their rows' band, so the time
+    should follow the band's cells, not the lattice's."""
+    import torch
+    from pairhmm import _lib, api, synth
+    from pairhmm import models as pm
+    rng = np.random.default_rng(seed)
+    Q, pi, _ = synth.rand_Q_pi(rng)
+    t = 0.5
+    chi = pm.tkf91_trans(0.03, 0.035, t).numpy()
+    st = np.array([0, 1, 2, 3, 4], np.int8)
+    sub = pm.transition_matrix(pm._t(Q), t).numpy()
+    lens = [(int(length * rng.uniform(0.95, 1.05)), int(length * rng.uniform(0.95, 1.05))) for _ in range(n_pairs)]
+    xs = [rng.integers(0, 20, a) for a, _ in lens]
+    ys = [rng.integers(0, 20, b) for _, b in lens]
+    centers = [np.round(np.arange(a + 1) * b / a).astype(int) for a, b in lens]
+    W = api.pad_to_bin(band)
+    masks = [api.band_mask(a, b, c, band) for (a, b), c in zip(lens, centers)]
+    EM, EI, ED = api._tkf_tables(sub, pi)
+    plan = api.get_plan(st, np.zeros(5, np.int32), EM.shape[0])
+    mk = lambda m: _lib.make_batch(xs, ys, chi[None], np.asarray(EM)[None], np.asarray(EI)[None],
+                                   np.asarray(ED)[None], device='cuda', cell_masks=m)
+    bb, bf = mk(masks), mk(None)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device='cuda')
+
+    def timed(fn):
+        for _ in range(3):
+            out = fn()
+        torch.cuda.synchronize()
+        ts = []
+        for k in range(reps):
+            flush.fill_(k & 0xff)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts)), out
+    band_ms, ob = timed(lambda: _lib.estep_band(plan, bb, centers, W))
+    full_ms, of = timed(lambda: _lib.estep(plan, bf))
+    band_cells = int(sum(int(m.astype(bool).sum()) for m in masks))
+    full_cells = int(sum((a + 1) * (b + 1) for a, b in lens))
+    llb, llf = ob['ll'].cpu().numpy(), of['ll'].cpu().numpy()
+    return {'workload': f'TKF91, {n_pairs} pairs of about {length} x {length}, band half-width {W} '
+                        'around the diagonal', 'api': 'phmm_estep_band (pairhmm.api.estep_batch_banded)',
+            'band_cells': band_cells, 'full_cells': full_cells, 'band_ms': band_ms, 'full_ms': full_ms,
+            'speedup': full_ms / band_ms, 'cell_ratio': full_cells / band_cells,
+            'band_cell_states_per_s': band_cells * 5 / (band_ms / 1e3),
+            'status_nonzero': int((ob['status'] != 0).sum().item()),
+            'band_ll_below_full': bool(np.all(llb <= llf + 1e-9 * np.abs(llf)))}
+
+
 def accuracy_of_workload(args, w, plan, out, chi, EM, EI, ED, fwd_only, dev):
     """The accuracy leg of this run: every pair against the oracle, except for
     lattices the oracle cannot finish in about a minute (162 states at 2000 x
@@ -676,6 +736,12 @@ def main():
     serving = None
     if rank == 0 and args.serving_requests > 0 and args.workload == WORKLOAD:
         serving = serving_leg(args.serving_requests, args.serving_rate)
+    banded = None
+    if rank == 0 and args.banded_pairs > 0 and args.workload == WORKLOAD:
+        try:
+            banded = banded_leg(args.banded_pairs)
+        except Exception as e:   # never lose the bench line to this extra leg
+            banded = {'error': repr(e)}
     if rank == 0:
         cpu = cpu_baseline(w, args.cpu_seconds, fwd_only) if args.cpu_seconds > 0 else None
         acc = None
@@ -701,7 +767,7 @@ def main():
             'e2e': {'value': e2e_value, 'unit': 'cell-state updates/s', 'h2d_bytes_per_step': h2d,
                     'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_total / args.steps,
                     'api': spec['e2e_api']},
-            'plain': plain, 'serving': serving, 'gpu_launches': launches_per_step * args.steps, 'clocks': clocks,
+            'plain': plain, 'serving': serving, 'banded': banded, 'gpu_launches': launches_per_step * args.steps, 'clocks': clocks,
         }
         print(json.dumps(line))
     if ws > 1:

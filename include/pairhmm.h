@@ -136,6 +136,29 @@ int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch,
                       double *cnt_I, double *cnt_D, int32_t *status_out,
                       double *log_F, double *log_B, double *post, void *stream);
 
+/* E-step of a banded batch with the posteriors in band layout.  Replaces
+ * forward_backward_2d_banded (dp/hmm.py:2395-2491), which returns the
+ * log-likelihood, the band posteriors and the expected transitions of one
+ * pair; here for a batch.  batch->cell_mask must hold the band (nonzero
+ * where |j - band_center[i]| <= band_half_width); the E-step runs on the
+ * two-warp kernels, whose stripes skip the anti-diagonal steps outside their
+ * rows' band, so the work is O(L * W) per pair.
+ *   band_center     device int32, Lx+1 entries per pair, pairs concatenated
+ *   band_half_width W of the output layout (2W + 1 columns per row)
+ *   post_band       device float64 [sum over pairs of (Lx+1)][2W+1][N]:
+ *                   position (i, b) holds F B / P at column
+ *                   band_center[i] - W + b (0 off the lattice or off the band;
+ *                   the start state's posterior at the origin is 1)
+ * and ll_out, n_trans, cnt_*, status_out as phmm_estep.  Fails with
+ * PHMM_E_ARG when the state space has no two-warp kernels (use
+ * phmm_estep_tables on the generic kernels then), without a cell mask, or on
+ * a plan forced to another kernel family. */
+int phmm_estep_band(phmm_plan *plan, const phmm_batch *batch,
+                    const int32_t *band_center, int32_t band_half_width,
+                    double *ll_out, double *n_trans, double *cnt_M,
+                    double *cnt_I, double *cnt_D, int32_t *status_out,
+                    double *post_band, void *stream);
+
 /* Caller-owned workspace.  phmm_workspace_bytes stores in *bytes the device
  * scratch one phmm_forward_ws (estep 0) or phmm_estep_ws (estep 1) call on
  * this batch needs; only the batch's host fields (n_pairs, Lx_host, Ly_host,
@@ -501,14 +524,20 @@ int phmm_set_spin_limit(phmm_plan *plan, long long iterations);
  *                 its 2D tables within memory by recomputation too
  *                 (jax.checkpoint on its log-likelihood VJPs,
  *                 train/vjp.py:109-124).
+ *   count_chunk   anti-diagonal steps per item of the split E-step's count
+ *                 pass on the warp kernels (0: 64; 8..512): shorter items
+ *                 shorten the tail after the wavefronts, at a small fixed
+ *                 cost per item.
  * Results do not depend on the tuning (the same kernels and arithmetic on
- * the same work items).  Defaults {0, 0, -1, 0, 0}. */
+ * the same work items; the count sums' order may differ).  Defaults
+ * {0, 0, -1, 0, 0, 0}. */
 typedef struct phmm_tuning {
     int32_t variant;
     int32_t wave_per_sm;
     int32_t count_per_sm;
     int32_t priorities;
     int32_t checkpoint;
+    int32_t count_chunk;
 } phmm_tuning;
 int phmm_set_tuning(phmm_plan *plan, const phmm_tuning *tuning);
 int phmm_get_tuning(const phmm_plan *plan, phmm_tuning *tuning);

@@ -17,12 +17,13 @@ class FakePlan:
         self.families = families
         self.cfg = None
 
-    def set_tuning(self, variant=0, wave_per_sm=0, count_per_sm=-1, priorities=0, checkpoint=0):
+    def set_tuning(self, variant=0, wave_per_sm=0, count_per_sm=-1, priorities=0, checkpoint=0, count_chunk=0):
         from pairhmm import _lib
         if variant not in (0,) + tuple(self.families):
             raise _lib.PairHMMError('no kernels of this family')
         self.cfg = (variant, wave_per_sm, count_per_sm, priorities)
         self.ckpt = checkpoint
+        self.chunk = count_chunk
 
 
 class FakeBatch:
@@ -46,7 +47,8 @@ def test_cache_round_trip(tmp_path, monkeypatch):
     autotune._MEM.clear()
     plan, batch = FakePlan(), FakeBatch([50, 60], [55, 70])
     assert autotune.lookup(plan, batch) is None
-    entry = {'tuning': {'variant': 7, 'wave_per_sm': 4, 'count_per_sm': -1, 'priorities': 1, 'checkpoint': 0},
+    entry = {'tuning': {'variant': 7, 'wave_per_sm': 4, 'count_per_sm': -1, 'priorities': 1, 'checkpoint': 0,
+                        'count_chunk': 0},
              'ms': 2.2,
              'default_ms': 2.3, 'evaluated': 9}
     autotune._store(autotune._key(plan, batch), entry)
@@ -65,9 +67,30 @@ def test_coordinate_descent_finds_the_fast_configuration(monkeypatch, tmp_path):
     # time as a function of the configuration: best at family 7, 3 CTAs/SM, no overlap grid, priorities
     cost = lambda v, w, c, p: 2.0 + 0.3 * (v != 7) + 0.1 * abs((w or 2) - 3) + 0.05 * (c != 0) + 0.05 * (p != 1)
     monkeypatch.setattr(autotune, '_time', lambda pl, b, out, reps, flush, fo: (cost(*pl.cfg), None))
-    r = autotune.tune(plan, batch, flush_bytes=0)
-    assert r['tuning'] == {'variant': 7, 'wave_per_sm': 3, 'count_per_sm': 0, 'priorities': 1, 'checkpoint': 0}
+    r = autotune.tune(plan, batch, flush_bytes=0, warmup_s=0)
+    assert r['tuning'] == {'variant': 7, 'wave_per_sm': 3, 'count_per_sm': 0, 'priorities': 1, 'checkpoint': 0,
+                           'count_chunk': 0}
     assert plan.cfg == (7, 3, 0, 1)
     assert abs(r['ms'] - 2.0) < 1e-9 and r['default_ms'] > r['ms'] and r['evaluated'] == len(r['table'])
     autotune._MEM.clear()
     assert autotune.lookup(plan, batch)['tuning'] == r['tuning']
+
+
+def test_winner_confirmed_against_fresh_default_timing(monkeypatch, tmp_path):
+    """A default timed slow once (a clock ramp) must not hand the win to a
+    configuration that is no faster when both are timed again."""
+    from pairhmm import autotune
+    monkeypatch.setenv('PAIRHMM_TUNE_CACHE', str(tmp_path / 'tuning.json'))
+    autotune._MEM.clear()
+    plan, batch = FakePlan(), FakeBatch([100] * 8, [90] * 8)
+    calls = []
+
+    def fake_time(pl, b, out, reps, flush, fo):
+        calls.append(pl.cfg)
+        if len(calls) == 1:
+            return 3.0, None                          # the first timing runs at low clocks
+        return (1.99 if pl.cfg[1] == 4 else 2.0), None  # wave_per_sm=4 within noise of the rest
+    monkeypatch.setattr(autotune, '_time', fake_time)
+    r = autotune.tune(plan, batch, flush_bytes=0, warmup_s=0, store=False)
+    assert r['tuning'] == autotune.DEFAULT and plan.cfg == (0, 0, -1, 0)
+    assert abs(r['ms'] - 2.0) < 1e-9 and abs(r['default_ms'] - 2.0) < 1e-9

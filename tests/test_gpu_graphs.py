@@ -7,8 +7,11 @@
   inputs (log-likelihoods bit for bit: the forward recursion is the same
   arithmetic; counts to 1e-12, being sums in another order), and the results
   of a call must survive the next call.
-* The autotuner: a tuned plan gives bit-identical log-likelihoods, names its
-  configuration, and a later lookup returns it.
+* The autotuner: a tuned plan gives bit-identical log-likelihoods (the
+  forward recursion does not depend on the launch configuration), counts
+  equal to 1e-6 relative (the count pass's chunk length is a tuning axis and
+  changes the order of the float32 partial sums), names its configuration,
+  and a later lookup returns it.
 """
 import numpy as np
 import pytest
@@ -75,7 +78,7 @@ def test_autotuned_plan_same_results(cuda_lib, tmp_path, monkeypatch):
     got = _lib.estep(plan, b)
     torch.cuda.synchronize()
     assert torch.equal(got['ll'], want['ll']) and (got['status'] == 0).all()
-    torch.testing.assert_close(got['n_trans'], want['n_trans'], rtol=1e-12, atol=1e-12)
+    torch.testing.assert_close(got['n_trans'], want['n_trans'], rtol=1e-6, atol=1e-6)
     autotune._MEM.clear()
     plan2 = _lib.Plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), K * F)
     assert autotune.apply_cached(plan2, b) == r['tuning'] and plan2.get_tuning() == r['tuning']

@@ -130,17 +130,18 @@ def test_estep_matches_oracle(cuda_lib, model, K, F, C, variant):
         assert_counts(out['cnt_D'][b], cD)
 
 
-def test_two_warp_forward_only_matches_oracle(cuda_lib):
+@pytest.mark.parametrize('variant', [7])
+def test_two_warp_forward_only_matches_oracle(cuda_lib, variant):
     """phmm_forward on the two-warp stripe kernels (variant 7)."""
     from pairhmm import _lib
     rng = np.random.default_rng(11)
     chi, st, groups, EM, EI, ED = oracle_case('mixdom2', rng, 3, 1, 1)
     xs, ys = zip(*[related_pair(rng, a, b) for a, b in LENGTHS + [(200, 150)]])
     plan = _lib.Plan(st, groups, EM.shape[0])
-    plan.set_variant(7)
+    plan.set_variant(variant)
     b = _lib.make_batch(xs, ys, chi[None], EM[None], EI[None], ED[None])
     ll_f, st_f = _lib.forward(plan, b)
-    assert plan.last_variant == 7
+    assert plan.last_variant == variant
     assert (st_f.cpu().numpy() == 0).all()
     for k, (x, y) in enumerate(zip(xs, ys)):
         ll = oracle_estep(chi, st, groups, EM, EI, ED, x, y)[0]

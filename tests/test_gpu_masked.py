@@ -86,7 +86,7 @@ def test_match_aligned_batch_matches_oracle(cuda_lib, variant):
     try:
         r = api.estep_batch_match_aligned(lt, st, xs, ys, [a[0] for a in al], [a[1] for a in al], subs, pis, K, F)
         got = api.to_host(r)
-        assert plan.last_variant == (7 if variant == 0 else 1)
+        assert plan.last_variant == (7 if variant == 0 else variant)
     finally:
         plan.set_variant(0)
     EM, EI, ED = dp.group_tables_per_domain(subs, pis, K)
@@ -128,7 +128,7 @@ def test_band_mask_estep_matches_oracle(cuda_lib, variant):
     try:
         bt = _lib.make_batch(xs, ys, chi[None], EM, EI, ED, cell_masks=masks)
         got = api.to_host(_lib.estep(plan, bt))
-        assert plan.last_variant == (7 if variant == 0 else 1)
+        assert plan.last_variant == (7 if variant == 0 else variant)
         ll_fwd, _ = _lib.forward(plan, bt)   # forward only, same kernels' forward
         ll_fwd = ll_fwd.cpu().numpy()
     finally:
@@ -177,3 +177,67 @@ def test_mask_refused_by_other_families(cuda_lib):
             _lib.estep(plan, _lib.make_batch([x], [y], chi[None], EM, EI, ED, cell_masks=[mask]))
     finally:
         plan.set_variant(0)
+
+
+def test_band_layout_estep_multi_stripe_matches_oracle(cuda_lib):
+    """phmm_estep_band (estep_batch_banded) over a batch of multi-stripe pairs
+    (TKF91, up to 700 x 650, W = 16): the stripes skip the steps off their
+    band, and the log-likelihoods, expected transitions and band-layout
+    posteriors equal the oracle's banded model."""
+    from pairhmm import api, synth
+    from oracle import dp, masked, models as om
+    rng = np.random.default_rng(91)
+    Q, pi, _ = synth.rand_Q_pi(rng)
+    t = 0.5
+    chi = om.tkf91_trans(0.03, 0.035, t)
+    st = np.array([0, 1, 2, 3, 4], np.int8)
+    sub = om.transition_matrix(Q, t)
+    shapes = [(700, 650), (200, 230), (64, 64), (65, 90)]
+    xs = [rng.integers(0, 20, a) for a, _ in shapes]
+    ys = [rng.integers(0, 20, b) for _, b in shapes]
+    centers = [np.round(np.arange(a + 1) * b / a).astype(int) for a, b in shapes]
+    ll, posts, n = api.estep_batch_banded(om.safe_log(chi), st, xs, ys, sub, pi, centers, 16)
+    EM, EI, ED = dp.group_tables_tkf(sub, pi)
+    W = masked.pad_to_bin(16)
+    for b, (a, ly) in enumerate(shapes):
+        emit = dp.log_emission_table(st, np.zeros(5, int), xs[b], ys[b], EM, EI, ED)
+        emit[~masked.band_allowed(a, ly, centers[b], W)] = om.NEG_INF
+        want_ll, post, want_n, _, _ = dp.forward_backward(om.safe_log(chi), st, emit)
+        _close_ll(ll[b], want_ll)
+        np.testing.assert_allclose(n[b], want_n, rtol=1e-5, atol=1e-6 * max(1.0, np.abs(want_n).max()))
+        jj = centers[b][:, None] - W + np.arange(2 * W + 1)[None, :]
+        ok = (jj >= 0) & (jj <= ly)
+        want_pb = np.zeros((a + 1, 2 * W + 1, 5))
+        ii, bb = np.nonzero(ok)
+        want_pb[ii, bb] = post[ii, jj[ii, bb]]
+        assert posts[b].shape[0] == masked.pad_to_bin(a) + 1
+        np.testing.assert_allclose(posts[b][:a + 1], want_pb, rtol=1e-5, atol=1e-6)
+        assert not posts[b][a + 1:].any()
+
+
+def test_mask_with_an_empty_stripe(cuda_lib):
+    """A mask that leaves no cell live in one 64-row stripe: that stripe and
+    the ones below skip every step and wait on nothing; the pair has no
+    likelihood and no counts, and the other pairs of the batch are exact."""
+    from pairhmm import api, synth, _lib
+    from oracle import dp, models as om
+    rng = np.random.default_rng(5)
+    Q, pi, _ = synth.rand_Q_pi(rng)
+    chi = om.tkf91_trans(0.03, 0.035, 0.4)
+    st = np.array([0, 1, 2, 3, 4], np.int8)
+    EM, EI, ED = dp.group_tables_tkf(om.transition_matrix(Q, 0.4), pi)
+    shapes = [(200, 190), (150, 160)]
+    xs = [rng.integers(0, 20, a) for a, _ in shapes]
+    ys = [rng.integers(0, 20, b) for _, b in shapes]
+    masks = [api.band_mask(a, b, np.round(np.arange(a + 1) * b / a).astype(int), 12) for a, b in shapes]
+    masks[0][64:128] = 0
+    plan = api.get_plan(st, np.zeros(5, np.int32), 1)
+    got = api.to_host(_lib.estep(plan, _lib.make_batch(xs, ys, chi[None], EM, EI, ED, cell_masks=masks)))
+    assert plan.last_variant == 7
+    assert got['ll'][0] <= -1e29 and got['status'][0] != 0 and not got['n_trans'][0].any()
+    emit = dp.log_emission_table(st, np.zeros(5, int), xs[1], ys[1], EM, EI, ED)
+    emit[masks[1] == 0] = om.NEG_INF
+    ll, _, n, _, _ = dp.forward_backward(om.safe_log(chi), st, emit)
+    assert got['status'][1] == 0
+    _close_ll(got['ll'][1], ll)
+    np.testing.assert_allclose(got['n_trans'][1], n, rtol=1e-5, atol=1e-6)

@@ -63,6 +63,11 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
     float *bnd = sm + LT.bnd;
     int *bndE = reinterpret_cast<int *>(sm) + LT.bndE;
     volatile int *s_abort = reinterpret_cast<int *>(sm) + LT.flag;
+    // halo staging: thread 0 copies column t+1 of the edge row above into
+    // slot (t+1) & 1 with cp.async at the start of step t, so the copy runs
+    // during the step's contraction instead of on the step's critical path
+    float *hst = sm + L.halo;
+    int *hstE = reinterpret_cast<int *>(sm) + L.haloE;
 
     if (r < 32) load_model_w<SH>(P, p, m, L, sm, smb, CHI_FWD_PAIRS);
     if (r < 2 * SP) bnd[r] = 0.f;
@@ -94,6 +99,20 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
         prev[q] = make_float2(0.f, 0.f); d0[q] = make_float2(0.f, 0.f); m0[q] = make_float2(0.f, 0.f);
     }
     const int T_last = (nrows - 1) + Ly;
+    // under a cell mask: the steps that touch the stripe's live columns, and
+    // the live columns of the row above (off them every value is zero, so the
+    // other steps are skipped and the halo there reads as zero)
+    int t_beg = 0, t_end = T_last, hlo = 0, hhi = Ly;
+    if (MK) {
+        const int2 rg = P.srange[m.stripe_base + si];
+        t_beg = max(0, rg.x);
+        t_end = min(T_last, rg.y + nrows - 1);
+        if (si > 0) {
+            const int2 ra = P.srange[m.stripe_base + si - 1];
+            hlo = ra.x;
+            hhi = min(Ly, ra.y);
+        }
+    }
     // M- and I-type emission factors of the cell of the next step, loaded one
     // step ahead (the y character and the table lookup are two dependent loads)
     // (and the cell's type mask: bit 0 M, 1 I, 2 D may emit; 7 without a mask)
@@ -110,18 +129,46 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
         for (int k = 0; k < NI; ++k) eMI[NM + k] = sm[offI[k] + yj];
         if (MK) mbx = in ? (int)__ldg(mrow + j) : 7;
     };
-    load_emit(0);
+    load_emit(t_beg);
     bool aborted = false;
     float hx[SP];
 #pragma unroll
     for (int s = 0; s < SP; ++s) hx[s] = 0.f;
     int hxE = EXP_NONE, hx_col = -1, pv = 0;
     if (si > 0 && r == 0) pv = ld_acquire(prog_above);
+    // a stripe that starts past step 0: row 0's first M predecessor is column
+    // t_beg - 1 of the row above, which the skipped step t_beg - 1 would have
+    // read -- load it into the history here
+    if (MK && si > 0 && r == 0 && t_beg <= t_end && t_beg - 1 >= max(hlo, 0) && t_beg - 1 <= hhi) {
+        const int col = t_beg - 1;
+        if (!wait_geq(prog_above, col + 1, P.spin_limit)) {
+            s_abort[t_beg & 1] = 1;   // seen by all threads after the first step's barrier
+        } else {
+            const float *src = edge_above + (int64_t)col * SP;
+#pragma unroll
+            for (int q = 0; q < SQ; ++q) m0[q] = make_float2(__ldcg(src + 2 * q), __ldcg(src + 2 * q + 1));
+            Em0 = __ldcg(edgeE_above + col);
+        }
+    }
 
-    for (int t = 0; t <= T_last; ++t) {
-        // halo (row i0-1, column t) for thread 0: normally prefetched during step t-1
-        if (si > 0 && t <= Ly && r == 0 && hx_col != t) {
-            if (!wait_geq(prog_above, t + 1, P.spin_limit)) {
+    for (int t = t_beg; t <= t_end; ++t) {
+        // halo (row i0-1, column t) for thread 0: staged during step t-1, else
+        // waited for and loaded here
+        if (si > 0 && t <= Ly && r == 0) {
+            if (MK && (t < hlo || t > hhi)) {   // off the live columns above: zero
+#pragma unroll
+                for (int s = 0; s < SP; ++s) hx[s] = 0.f;
+                hxE = EXP_NONE;
+            } else if (hx_col == t) {
+                cp_wait0();
+                const float4 *st = reinterpret_cast<const float4 *>(hst + (t & 1) * SP);
+#pragma unroll
+                for (int q = 0; q < SP / 4; ++q) {
+                    const float4 v = st[q];
+                    hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
+                }
+                hxE = hstE[t & 1];
+            } else if (!wait_geq(prog_above, t + 1, P.spin_limit)) {
                 s_abort[t & 1] = 1;   // read by all threads after this step's barrier
             } else {
                 const float4 *src = reinterpret_cast<const float4 *>(edge_above + (int64_t)t * SP);
@@ -131,8 +178,21 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
                     hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
                 }
                 hxE = __ldcg(edgeE_above + t);
-                hx_col = t;
             }
+            // stage column t+1 when the progress read earlier covers it
+            if (t + 1 <= hhi && (!MK || t + 1 >= hlo) && pv > t + 1) {
+                const float *src = edge_above + (int64_t)(t + 1) * SP;
+                float *dst = hst + ((t + 1) & 1) * SP;
+#pragma unroll
+                for (int q = 0; q < SP / 4; ++q) cp_async16(dst + 4 * q, src + 4 * q);
+                cp_async4(hstE + ((t + 1) & 1), edgeE_above + t + 1);
+                cp_commit();
+                hx_col = t + 1;
+            }
+            // progress for the staging of column t+2 at the start of step t+1,
+            // polled now (only when the last value read does not cover it) so
+            // the load has the whole step to arrive
+            if (t + 2 <= hhi && pv <= t + 2) pv = ld_acquire(prog_above);
         }
         const int jc = t - r;
         const bool valid = r < nrows && jc >= 0 && jc <= Ly;
@@ -258,7 +318,7 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
                     dst[q] = make_float4(v[0], v[1], v[2], v[3]);
                 }
                 edgeE_mine[jc] = Enew;
-                if (((jc + 1) % PUB) == 0 || jc == Ly) st_release(prog_mine, jc + 1);
+                if (((jc + 1) % PUB) == 0 || jc == t_end - (ROWS - 1)) st_release(prog_mine, jc + 1);
             }
             if (rowi == Lx && jc == Ly && si + 1 == m.n_stripes) {
                 double a = 0.0;
@@ -289,25 +349,12 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
             bndE[t & 1] = Eprev;
         }
         load_emit(t + 1);
-        // prefetch halo column t+1 when the progress read last step covers it
-        if (si > 0 && r == 0 && t + 1 <= Ly) {
-            if (pv > t + 1) {
-                const float4 *src = reinterpret_cast<const float4 *>(edge_above + (int64_t)(t + 1) * SP);
-#pragma unroll
-                for (int q = 0; q < SP / 4; ++q) {
-                    const float4 v = __ldcg(src + q);
-                    hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
-                }
-                hxE = __ldcg(edgeE_above + t + 1);
-                hx_col = t + 1;
-            }
-            if (pv <= t + 2) pv = ld_acquire(prog_above);
-        }
         __syncthreads();
         // the flag of step t is written only before this barrier, and the
         // next write goes to the other parity: every thread sees the same value
         if (s_abort[t & 1]) { aborted = true; break; }
     }
+    if (r == 0) cp_wait0();   // no staged copy outlives the stripe
     if (aborted) {
         if (r == ROWS - 1 && has_below) st_release(prog_mine, Ly + 1);
         if (r == 0) {
@@ -343,6 +390,10 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
     float *bnd = sm + LT.bnd;
     int *bndE = reinterpret_cast<int *>(sm) + LT.bndE;
     volatile int *s_abort = reinterpret_cast<int *>(sm) + LT.flag;
+    // halo staging: thread 63 copies column jb-1 of the edge row below into
+    // slot (jb-1) & 1 with cp.async at the start of the step that reads jb
+    float *hst = sm + L.halo;
+    int *hstE = reinterpret_cast<int *>(sm) + L.haloE;
 
     if (r < 32) load_model_w<SH>(P, p, m, L, sm, smb, CHI_BWD_PAIRS);
     if (r < 2 * SP) bnd[r] = 0.f;
@@ -376,6 +427,19 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
     }
 
     const int T_last = (nrows - 1) + Ly;
+    // under a cell mask: the steps that touch the stripe's live columns, and
+    // the live columns of the row below (as in the forward)
+    int t_beg = 0, t_end = T_last, hlo = 0, hhi = Ly;
+    if (MK) {
+        const int2 rg = P.srange[m.stripe_base + si];
+        t_beg = max(0, rg.x);
+        t_end = min(T_last, rg.y + nrows - 1);
+        if (has_below) {
+            const int2 rb = P.srange[m.stripe_base + si + 1];
+            hlo = rb.x;
+            hhi = min(Ly, rb.y);
+        }
+    }
     // M- and I-type emission factors of the cell of the next step, loaded one step ahead
     // (and the cell's type mask, as in the forward, folded into the factors
     // here, off the step's dependency chain: eDc is eD with the D bit applied)
@@ -396,18 +460,50 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
 #pragma unroll
         for (int k = 0; k < SH::ND; ++k) eDc[k] = eD[k] * bD;
     };
-    load_emit(T_last);
+    load_emit(t_end);
     bool aborted = false;
     float hx[SP];
 #pragma unroll
     for (int s = 0; s < SP; ++s) hx[s] = 0.f;
     int hxE = EXP_NONE, hx_col = -1, pv = 0;
     if (has_below && r == ROWS - 1) pv = ld_acquire(prog_below);
+    // a stripe that ends before its last step: row 63's first M successor is
+    // column jb + 1 of the row below (jb = t_end - 63), which the skipped step
+    // t_end + 1 would have received -- load it into the history here
+    if (MK && has_below && r == ROWS - 1 && t_beg <= t_end) {
+        const int col = t_end - (ROWS - 1) + 1;
+        if (col >= max(hlo, 0) && col <= hhi) {
+            if (!wait_geq(prog_below, Ly + 1 - col, P.spin_limit)) {
+                s_abort[t_end & 1] = 1;   // seen by all threads after the first step's barrier
+            } else {
+                const float *src = edge_below + (int64_t)col * SP;
+#pragma unroll
+                for (int q = 0; q < KQ; ++q) {
+                    if (2 * q >= NE) continue;
+                    mR[q] = make_float2(__ldcg(src + 2 * q), __ldcg(src + 2 * q + 1));
+                }
+                EmR = __ldcg(edgeE_below + col);
+            }
+        }
+    }
 
-    for (int t = T_last; t >= 0; --t) {
+    for (int t = t_end; t >= t_beg; --t) {
         const int jb = t - (ROWS - 1);
-        if (has_below && jb >= 0 && jb <= Ly && r == ROWS - 1 && hx_col != jb) {
-            if (!wait_geq(prog_below, Ly + 1 - jb, P.spin_limit)) {
+        if (has_below && jb >= 0 && jb <= Ly && r == ROWS - 1) {
+            if (MK && (jb < hlo || jb > hhi)) {   // off the live columns below: zero
+#pragma unroll
+                for (int s = 0; s < SP; ++s) hx[s] = 0.f;
+                hxE = EXP_NONE;
+            } else if (hx_col == jb) {   // staged during the previous step
+                cp_wait0();
+                const float4 *st = reinterpret_cast<const float4 *>(hst + (jb & 1) * SP);
+#pragma unroll
+                for (int q = 0; q < SP / 4; ++q) {
+                    const float4 v = st[q];
+                    hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
+                }
+                hxE = hstE[jb & 1];
+            } else if (!wait_geq(prog_below, Ly + 1 - jb, P.spin_limit)) {
                 s_abort[t & 1] = 1;   // read by all threads after this step's barrier
             } else {
                 const float4 *src = reinterpret_cast<const float4 *>(edge_below + (int64_t)jb * SP);
@@ -417,8 +513,19 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
                     hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
                 }
                 hxE = __ldcg(edgeE_below + jb);
-                hx_col = jb;
             }
+            // stage column jb-1 when the progress read earlier covers it
+            if (jb - 1 >= hlo && (!MK || jb - 1 <= hhi) && pv >= Ly + 1 - (jb - 1)) {
+                const float *src = edge_below + (int64_t)(jb - 1) * SP;
+                float *dst = hst + ((jb - 1) & 1) * SP;
+#pragma unroll
+                for (int q = 0; q < SP / 4; ++q) cp_async16(dst + 4 * q, src + 4 * q);
+                cp_async4(hstE + ((jb - 1) & 1), edgeE_below + jb - 1);
+                cp_commit();
+                hx_col = jb - 1;
+            }
+            // progress for the staging of column jb-2 at the next step, polled now
+            if (jb - 2 >= hlo && pv < Ly + 1 - (jb - 2)) pv = ld_acquire(prog_below);
         }
         const int jc = t - r;
         const bool valid = r < nrows && jc >= 0 && jc <= Ly;
@@ -554,7 +661,7 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
                     e[q] = make_float4(v[0], v[1], v[2], v[3]);
                 }
                 edgeE_mine[jc] = Eb;
-                if ((jc % PUB) == 0) st_release(prog_mine, Ly + 1 - jc);
+                if ((jc % PUB) == 0 || jc == t_beg) st_release(prog_mine, Ly + 1 - jc);
             }
         }
 #pragma unroll
@@ -576,24 +683,12 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
             bndE[t & 1] = Ewn;
         }
         load_emit(t - 1);
-        if (has_below && r == ROWS - 1 && jb - 1 >= 0 && jb - 1 <= Ly) {
-            if (pv >= Ly + 1 - (jb - 1)) {
-                const float4 *src = reinterpret_cast<const float4 *>(edge_below + (int64_t)(jb - 1) * SP);
-#pragma unroll
-                for (int q = 0; q < SP / 4; ++q) {
-                    const float4 v = __ldcg(src + q);
-                    hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
-                }
-                hxE = __ldcg(edgeE_below + jb - 1);
-                hx_col = jb - 1;
-            }
-            if (pv < Ly + 3 - jb) pv = ld_acquire(prog_below);
-        }
         __syncthreads();
         // the flag of step t is written only before this barrier, and the
         // next write goes to the other parity: every thread sees the same value
         if (s_abort[t & 1]) { aborted = true; break; }
     }
+    if (r == ROWS - 1) cp_wait0();   // no staged copy outlives the stripe
     if (aborted && r == 0) {
         atomicOr(P.status + p, PHMM_ST_TIMEOUT);
         if (has_above) st_release(prog_mine, Ly + 1);
@@ -625,7 +720,7 @@ __global__ void __launch_bounds__(TWT) stripe_tw_kernel(const KParams P) {
 }  // namespace warp2
 
 // ---------------------------------------------------------------- two-warp count pass
-// count_chunk_w with one row per thread: a 64-thread CTA takes a chunk of CCH
+// count_chunk_w with one row per thread: a 64-thread CTA takes a chunk of P.cch
 // anti-diagonal steps of one stripe, both warps sharing the model tables and
 // the double-buffered lattice rows.  Row r's D- and M-successors come from row
 // r+1 by __shfl_down inside a warp, through a shared slot across the two warps
@@ -670,10 +765,25 @@ __device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const Sm
     const int64_t latc = m.lat_base + (int64_t)si * (ROWS + Ly) * ROWS;
     const int64_t latb = m.lat_base + (int64_t)(si + 1) * (ROWS + Ly) * ROWS;   // stripe below (row 0)
     const int T_last = (nrows - 1) + Ly;
-    const int t0 = ch * CCH;
-    const int t_hi = min(T_last, t0 + CCH - 1);
+    // under a cell mask the recursions visited only the steps [t_beg, t_last]
+    // of this stripe and columns [blo, bhi] of the first row below: the count
+    // covers those steps of the chunk and reads the rest as zero
+    int t_beg = 0, t_last = T_last, blo = 0, bhi = Ly;
+    if (P.srange) {
+        const int2 rg = P.srange[m.stripe_base + si];
+        t_beg = max(0, rg.x);
+        t_last = min(T_last, rg.y + nrows - 1);
+        if (has_below) {
+            const int2 rb = P.srange[m.stripe_base + si + 1];
+            blo = rb.x;
+            bhi = min(Ly, rb.y);
+        }
+    }
+    const int t0 = ch * P.cch;
+    const int t_hi = min(t_last, t0 + P.cch - 1);
+    const int t_lo = max(t0, t_beg);
     const int t_top = min(T_last, t_hi + 2);   // two steps of successor history first
-    if (t0 > T_last) return;                    // uniform over the CTA
+    if (t_lo > t_hi) return;                    // uniform over the CTA
     int *s_flag = reinterpret_cast<int *>(sm) + LT.slotE + 2;
     if (P.count_wait) {   // the wavefronts may still run: wait for the stripes read here
         if (r == 0) *s_flag = count_ready(P, m, si) ? 1 : 0;
@@ -697,18 +807,24 @@ __device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const Sm
     float *slot = sm + LT.slot;
     int *slotE = reinterpret_cast<int *>(sm) + LT.slotE;
     auto prefetch = [&](int t) {
-        if (t >= t0) {
+        if (t >= t_lo) {
             const int buf = t & 1;
-            const float *srcF = P.lat + (latc + (int64_t)t * ROWS) * SP;
-            const float *srcB = P.blat + (latc + (int64_t)t * ROWS) * SP;
-            for (int idx = r; idx < ROWS * SP / 4; idx += TWT) {
-                const int rr = idx / (SP / 4), q = idx % (SP / 4);
-                if (t <= t_hi) cp_async16(fbuf + buf * ROWS * SPP + rr * SPP + 4 * q, srcF + 4 * idx);
-                cp_async16(bbuf + buf * ROWS * SPP + rr * SPP + 4 * q, srcB + 4 * idx);
-            }
-            if (r < ROWS / 4) {
-                if (t <= t_hi) cp_async16(fEb + buf * ROWS + 4 * r, P.lat_exp + latc + (int64_t)t * ROWS + 4 * r);
-                cp_async16(bEb + buf * ROWS + 4 * r, P.blat_exp + latc + (int64_t)t * ROWS + 4 * r);
+            if (t > t_last) {   // successor history past the live steps: b~ = 0
+                for (int idx = r; idx < ROWS * SPP; idx += TWT) bbuf[buf * ROWS * SPP + idx] = 0.f;
+                bEb[buf * ROWS + r] = EXP_NONE;
+            } else {
+                const float *srcF = P.lat + (latc + (int64_t)t * ROWS) * SP;
+                const float *srcB = P.blat + (latc + (int64_t)t * ROWS) * SP;
+                for (int idx = r; idx < ROWS * SP / 4; idx += TWT) {
+                    const int rr = idx / (SP / 4), q = idx % (SP / 4);
+                    if (t <= t_hi) cp_async16(fbuf + buf * ROWS * SPP + rr * SPP + 4 * q, srcF + 4 * idx);
+                    cp_async16(bbuf + buf * ROWS * SPP + rr * SPP + 4 * q, srcB + 4 * idx);
+                }
+                if (r < ROWS / 4) {
+                    if (t <= t_hi)
+                        cp_async16(fEb + buf * ROWS + 4 * r, P.lat_exp + latc + (int64_t)t * ROWS + 4 * r);
+                    cp_async16(bEb + buf * ROWS + 4 * r, P.blat_exp + latc + (int64_t)t * ROWS + 4 * r);
+                }
             }
         }
         cp_commit();
@@ -784,7 +900,7 @@ __device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const Sm
     auto load_below = [&](int t) {
         const int jb = t - (ROWS - 1);
         bbE = EXP_NONE;
-        if (r == ROWS - 1 && has_below && t >= t0 && jb >= 0 && jb <= Ly) {
+        if (r == ROWS - 1 && has_below && t >= t_lo && jb >= blo && jb <= bhi) {
             const int64_t cell = latb + (int64_t)jb * ROWS;
             bbE = __ldcg(P.blat_exp + cell);
             const float4 *src = reinterpret_cast<const float4 *>(P.blat + cell * SP);
@@ -800,7 +916,7 @@ __device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const Sm
     };
     load_below(t_top);
 
-    for (int t = t_top; t >= t0; --t) {
+    for (int t = t_top; t >= t_lo; --t) {
         const bool count = t <= t_hi;
         const int buf = t & 1;
         // step t's rows have landed (this thread's copies, then everyone's),
@@ -1008,7 +1124,7 @@ __device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const Sm
         }
     }
     // I-type columns not completed inside the chunk (touched by rows below row 0)
-    for (int j = max(0, t0 - (ROWS - 1)) + r; j <= min(Ly, t0 - 1); j += TWT) {
+    for (int j = max(0, t_lo - (ROWS - 1)) + r; j <= min(Ly, t_lo - 1); j += TWT) {
         const int sl = j % ROWS;
         const int yt = ys[j];
 #pragma unroll

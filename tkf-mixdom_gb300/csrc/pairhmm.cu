@@ -63,6 +63,7 @@ struct PairMeta {
     int64_t lat_base;    // first cell of the pair's lattice (stripe-diagonal layout)
     int64_t edge_base;   // first cell of the pair's edge rows
     int64_t tab_base;    // first cell of the pair's optional row-major tables
+    int64_t row_base;    // rows 0..Lx of the pairs before this one (band-layout outputs)
     int32_t Lx, Ly;
     int32_t n_stripes;
     int32_t stripe_base;
@@ -94,6 +95,7 @@ struct KParams {
     float *bedge;
     int *bedge_exp;
     int count_wait;                     // count pass waits for the stripes it reads
+    int cch;                            // anti-diagonal steps per count chunk (warp count passes)
     float *edge;
     int *edge_exp;
     int *progress;
@@ -105,6 +107,9 @@ struct KParams {
     long long spin_limit;
     const int *wave_ctr;                // overlapped count pass: forward, backward claim counters
     const unsigned char *cmask;         // per-cell type mask (bit 0 M, 1 I, 2 D) at tab_base, or null
+    // two-warp stripes under a cell mask: columns [x, y] of the cells the mask
+    // leaves live in each stripe (global stripe index), or null (all columns)
+    const int2 *srange;
     float beam_scale;                   // > 0: forward states below max * beam_scale pruned (generic kernels)
     // wide kernels, stripe-edge checkpointing: lattice cell offset of each
     // stripe (global stripe index) in the current group's scratch, or null
@@ -228,6 +233,11 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     unsigned s = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
@@ -903,6 +913,66 @@ __global__ void fill_f64(double *p, int64_t n, double v) {
         p[idx] = v;
 }
 
+// Live column range of each stripe under a cell mask: one CTA per forward
+// stripe item (pair, stripe) scans the stripe's rows of the mask and writes
+// the smallest and largest column with a nonzero entry to range[stripe_base +
+// stripe], or (RANGE_EMPTY_LO, RANGE_EMPTY_HI) when the mask leaves nothing.
+// The terminal cell (Lx, Ly) always counts, so the stripe holding it visits
+// the cell the log-likelihood is read from.  Off its range a stripe's forward
+// and backward values are zero (no cell there may emit), which is what lets
+// the recursions skip those anti-diagonal steps.
+constexpr int RANGE_EMPTY_LO = 1 << 30, RANGE_EMPTY_HI = -(1 << 30);
+
+__global__ void stripe_range_kernel(const KParams P, int rows, int2 *range) {
+    const int2 w = P.items[blockIdx.x];
+    const PairMeta m = P.meta[w.x];
+    const int si = w.y, i0 = si * rows, nrows = min(rows, m.Lx + 1 - i0);
+    __shared__ int s_lo, s_hi;
+    if (threadIdx.x == 0) { s_lo = RANGE_EMPTY_LO; s_hi = RANGE_EMPTY_HI; }
+    __syncthreads();
+    int lo = RANGE_EMPTY_LO, hi = RANGE_EMPTY_HI;
+    for (int r = 0; r < nrows; ++r) {
+        const unsigned char *row = P.cmask + m.tab_base + (int64_t)(i0 + r) * (m.Ly + 1);
+        for (int j = threadIdx.x; j <= m.Ly; j += blockDim.x)
+            if (row[j]) { lo = min(lo, j); hi = max(hi, j); }
+    }
+    if (si + 1 == m.n_stripes && threadIdx.x == 0) { lo = min(lo, m.Ly); hi = max(hi, m.Ly); }
+    if (lo <= hi) { atomicMin(&s_lo, lo); atomicMax(&s_hi, hi); }
+    __syncthreads();
+    if (threadIdx.x == 0) range[m.stripe_base + si] = make_int2(s_lo, s_hi);
+}
+
+// Band-layout posteriors from the split E-step's two-warp lattices: one CTA
+// per forward stripe item; position (i, b) of a pair's rows takes
+// f~ b~ 2^(Ef + Eb) / P at cell (i, center[i] - W + b) for the emitting
+// states and the start (source slots 0..nsrc-1, start last); cells off the
+// stripe's live columns or off the lattice stay 0 (set by the caller).
+__global__ void band_post_kernel(const KParams P, int rows, int stride, int nsrc, const int32_t *center, int W,
+                                 double *out) {
+    const int2 w = P.items[blockIdx.x];
+    const int p = w.x, si = w.y;
+    const PairMeta m = P.meta[p];
+    const double llv = P.ll[p];
+    if (!(llv > -1e29)) return;
+    const double lam = llv / LN2;
+    const int i0 = si * rows, nrows = min(rows, m.Lx + 1 - i0), BW = 2 * W + 1;
+    const int2 rg = P.srange[m.stripe_base + si];
+    const int jlo = max(0, rg.x), jhi = min(m.Ly, rg.y);
+    const int64_t latc = m.lat_base + (int64_t)si * (rows + m.Ly) * rows;
+    for (int idx = threadIdx.x; idx < nrows * BW; idx += blockDim.x) {
+        const int r = idx / BW, b = idx - r * BW, i = i0 + r;
+        const int j = center[m.row_base + i] - W + b;
+        if (j < jlo || j > jhi) continue;
+        const int64_t cell = latc + (int64_t)(j + r) * rows + r;
+        const int Ef = P.lat_exp[cell], Eb = P.blat_exp[cell];
+        if (Ef <= EXP_NONE || Eb <= EXP_NONE) continue;
+        const double sc = exp2((double)(Ef + Eb) - lam);
+        double *o = out + ((m.row_base + i) * BW + b) * P.N;
+        for (int s = 0; s < nsrc; ++s)
+            o[P.w_orig[s]] = (double)P.lat[cell * stride + s] * (double)P.blat[cell * stride + s] * sc;
+    }
+}
+
 }  // namespace
 
 #include "estep_warp.cuh"
@@ -975,7 +1045,7 @@ struct phmm_plan {
     int w_nm = 0, w_ni = 0, w_nd = 0;
     int grid_div = 1;       // persistent grids use 1/grid_div of the resident slots
     int launch_per_sm = 0;  // > 0: the next launch takes this many resident CTAs per SM (at most occ)
-    phmm_tuning tuning = {0, 0, -1, 0, 0};   // phmm_set_tuning (variant is `variant` below)
+    phmm_tuning tuning = {0, 0, -1, 0, 0, 0};   // phmm_set_tuning (variant is `variant` below)
     int variant = 0;        // 0 automatic, 1 generic, 2 warp, 3 block, 4/5 split warp/block E-step, 6 wide,
                             // 7 split E-step on two-warp stripes
     bool two_warp = false;  // the last warp-family call ran the two-warp stripe kernels
@@ -1448,6 +1518,7 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     K.spin_limit = plan->spin_limit > 0 ? plan->spin_limit : kSpinLimit;
     K.wave_ctr = nullptr;
     K.cmask = nullptr;
+    K.srange = nullptr;
     K.beam_scale = 0.f;
     // ---- wavefronts, then the count pass (both on the caller's stream: a wide
     // wavefront CTA needs most of an SM's shared memory, so a count CTA waiting
@@ -1634,7 +1705,7 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
                (int64_t)(b->Lx_host[c] + 1) * (b->Ly_host[c] + 1);
     });
     plan->h_meta.resize(P_);
-    int64_t lat_cells = 0, edge_cells = 0, tab_cells = 0;
+    int64_t lat_cells = 0, edge_cells = 0, tab_cells = 0, row_cells = 0;
     int stripes = 0, max_ly = 0;
     for (int p = 0; p < P_; ++p) {
         PairMeta &m = plan->h_meta[p];
@@ -1647,6 +1718,8 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         m.lat_base = lat_cells;
         m.edge_base = edge_cells;
         m.tab_base = tab_cells;
+        m.row_base = row_cells;
+        row_cells += m.Lx + 1;
         stripes += m.n_stripes;
         if (estep) lat_cells += (int64_t)m.n_stripes * (rows + m.Ly) * rows;
         edge_cells += (int64_t)m.n_stripes * (m.Ly + 1);
@@ -1654,20 +1727,46 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         max_ly = std::max(max_ly, m.Ly);
     }
     plan->h_items.clear();
-    for (int p : order)
-        for (int s = 0; s < plan->h_meta[p].n_stripes; ++s) plan->h_items.push_back(make_int2(p, s));
+    // stripe items in pop order; a stripe only waits on stripes of its pair
+    // popped before it.  Unmasked: pair by pair, longest pairs first (a pair's
+    // stripes all run at once, one behind the other, and the longest pairs set
+    // the critical path).  Under a cell mask (two-warp kernels, which skip the
+    // steps off each stripe's live columns): a narrow band keeps only a couple
+    // of a pair's stripes busy at a time, so pair-by-pair order would park most
+    // CTAs on stripes that cannot start yet -- there the items go stripe by
+    // stripe (the first stripe of every pair, then the second, ...; the
+    // backward from the last stripe up).
+    const bool by_stripe = masked && two_warp;
+    int max_stripes = 0;
+    for (int p = 0; p < P_; ++p) max_stripes = std::max(max_stripes, plan->h_meta[p].n_stripes);
+    if (by_stripe) {
+        for (int s = 0; s < max_stripes; ++s)
+            for (int p : order)
+                if (s < plan->h_meta[p].n_stripes) plan->h_items.push_back(make_int2(p, s));
+    } else {
+        for (int p : order)
+            for (int s = 0; s < plan->h_meta[p].n_stripes; ++s) plan->h_items.push_back(make_int2(p, s));
+    }
     const int n_items = (int)plan->h_items.size();
-    if (estep)
+    if (estep && by_stripe) {
+        for (int k = 0; k < max_stripes; ++k)
+            for (int p : order)
+                if (k < plan->h_meta[p].n_stripes)
+                    plan->h_items.push_back(make_int2(p, plan->h_meta[p].n_stripes - 1 - k));
+    } else if (estep) {
         for (int p : order)
             for (int s = plan->h_meta[p].n_stripes - 1; s >= 0; --s) plan->h_items.push_back(make_int2(p, s));
+    }
     int n_citems = 0;
+    const int cch = plan->tuning.count_chunk > 0 ? plan->tuning.count_chunk : warp2::CCH;
+    K.cch = cch;
     if (split) {   // count chunks: (pair, stripe << 12 | chunk), shortest pairs first (ready first)
         for (auto it = order.rbegin(); it != order.rend(); ++it) {
             const int p = *it;
             const PairMeta &m = plan->h_meta[p];
             for (int s = 0; s < m.n_stripes; ++s) {
                 const int nrows = std::min(rows, m.Lx + 1 - s * rows);
-                const int nch = (nrows + m.Ly + warp2::CCH - 1) / warp2::CCH;
+                const int nch = (nrows + m.Ly + cch - 1) / cch;
                 if (nch > 4096 || s >= (1 << 19)) return fail(PHMM_E_ARG, "pair too long for the count chunk index");
                 for (int c = 0; c < nch; ++c) plan->h_items.push_back(make_int2(p, (s << 12) | c));
                 n_citems += nch;
@@ -1683,10 +1782,12 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         }
     }
     int rc;
+    // masked two-warp calls: the stripes' live column ranges follow the items
+    const size_t n_range = (masked && two_warp) ? (size_t)stripes : 0;
     // ---- scratch: plan-owned buffers, or carved from the caller's workspace
     const size_t o_meta = 0;
     const size_t o_items = align256(o_meta + sizeof(PairMeta) * P_);
-    const size_t o_cnt = align256(o_items + sizeof(int2) * plan->h_items.size());
+    const size_t o_cnt = align256(o_items + sizeof(int2) * (plan->h_items.size() + n_range));
     const size_t o_prog = align256(o_cnt + 4 * sizeof(int));
     const size_t o_edge = align256(o_prog + sizeof(int) * 2 * (size_t)stripes);
     const size_t o_edgeE = align256(o_edge + sizeof(float) * (size_t)edge_cells * stride);
@@ -1725,7 +1826,8 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         }
     } else {
         if ((rc = ensure((char **)&plan->meta, &plan->meta_cap, sizeof(PairMeta) * P_))) return rc;
-        if ((rc = ensure((char **)&plan->items, &plan->items_cap, sizeof(int2) * plan->h_items.size()))) return rc;
+        if ((rc = ensure((char **)&plan->items, &plan->items_cap, sizeof(int2) * (plan->h_items.size() + n_range))))
+            return rc;
         if ((rc = ensure(&plan->edge, &plan->edge_cap, (size_t)edge_cells * stride))) return rc;
         if ((rc = ensure(&plan->edge_exp, &plan->edgeE_cap, (size_t)edge_cells * estride))) return rc;
         if ((rc = ensure(&plan->progress, &plan->prog_cap, (size_t)2 * stripes))) return rc;
@@ -1802,6 +1904,15 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     K.wave_ctr = nullptr;
     K.cmask = b->cell_mask;
     K.beam_scale = b->beam_log_width > 0.0 ? (float)exp(-b->beam_log_width) : 0.f;
+    K.srange = nullptr;
+    if (n_range) {
+        int2 *range = (int2 *)d_items + plan->h_items.size();
+        K.items = (const int2 *)d_items;
+        stripe_range_kernel<<<n_items, 256, 0, stream>>>(K, rows, range);
+        CUDA_TRY(cudaGetLastError());
+        plan->launches++;
+        K.srange = range;
+    }
     if (split) return launch_split(plan, K, wl ? wl : bl, bl != nullptr, n_items, n_citems, stripes, max_ly, d_items,
                                    d_counters, d_progress, d_bedge, d_bedge_exp, stream);
     for (int pass = 0; pass < (estep ? 2 : 1); ++pass) {
@@ -2200,6 +2311,50 @@ int phmm_estep_tables(phmm_plan *plan, const phmm_batch *batch, double *ll_out, 
                stream);
 }
 
+int phmm_estep_band(phmm_plan *plan, const phmm_batch *batch, const int32_t *band_center, int32_t band_half_width,
+                    double *ll_out, double *n_trans, double *cnt_M, double *cnt_I, double *cnt_D,
+                    int32_t *status_out, double *post_band, void *stream) {
+    NvtxRange range("phmm_estep_band");
+    if (!plan || !batch) return fail(PHMM_E_ARG, "null plan or batch");
+    if (!batch->cell_mask) return fail(PHMM_E_ARG, "phmm_estep_band: the batch carries no band (cell mask)");
+    if (!band_center || !post_band || band_half_width < 0) return fail(PHMM_E_ARG, "phmm_estep_band: bad band output");
+    if (batch->beam_log_width > 0.0) return fail(PHMM_E_ARG, "phmm_estep_band: beam pruning is not banded");
+    if (plan->variant != 0 && plan->variant != 7)
+        return fail(PHMM_E_ARG, "phmm_estep_band runs on the two-warp kernels (variant 0 or 7)");
+    if (!find_warp_launcher(plan->w_nm, plan->w_ni, plan->w_nd))
+        return fail(PHMM_E_ARG, "phmm_estep_band: no two-warp kernels for this state space");
+    int rc = run(plan, batch, true, ll_out, n_trans, cnt_M, cnt_I, cnt_D, status_out, nullptr, nullptr, nullptr,
+                 stream);
+    if (rc) return rc;
+    if (!plan->two_warp || plan->last_variant != 7)
+        return fail(PHMM_E_ARG, "phmm_estep_band: the E-step did not run on the two-warp kernels");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int N = plan->base.N, BW = 2 * band_half_width + 1;
+    int64_t rows = 0;
+    for (int p = 0; p < batch->n_pairs; ++p) rows += batch->Lx_host[p] + 1;
+    CUDA_TRY(cudaMemsetAsync(post_band, 0, sizeof(double) * (size_t)rows * BW * N, st));
+    // the E-step's work description and lattices stay in the plan's buffers;
+    // the forward stripe items come first in the item list, the stripe
+    // ranges right after the whole list
+    KParams K = plan->base;
+    K.meta = (const PairMeta *)plan->meta;
+    K.items = (const int2 *)plan->items;
+    K.lat = plan->lat;
+    K.lat_exp = plan->lat_exp;
+    K.blat = plan->blat;
+    K.blat_exp = plan->blat_exp;
+    K.ll = ll_out;
+    K.srange = (const int2 *)plan->items + plan->h_items.size();
+    int n_items = 0;
+    for (int p = 0; p < batch->n_pairs; ++p) n_items += plan->h_meta[p].n_stripes;
+    const int nsrc = plan->w_nm + plan->w_ni + plan->w_nd + 1;
+    const int stride = (nsrc + 3) & ~3;
+    band_post_kernel<<<n_items, 256, 0, st>>>(K, warp2::ROWS, stride, nsrc, band_center, band_half_width, post_band);
+    CUDA_TRY(cudaGetLastError());
+    plan->launches++;
+    return 0;
+}
+
 int phmm_workspace_bytes(phmm_plan *plan, const phmm_batch *batch, int estep, size_t *bytes) {
     if (!bytes) return fail(PHMM_E_ARG, "null output");
     return run(plan, batch, estep != 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
@@ -2259,9 +2414,10 @@ int phmm_last_variant(const phmm_plan *plan) { return plan ? plan->last_variant 
 int phmm_set_tuning(phmm_plan *plan, const phmm_tuning *t) {
     if (!plan || !t) return fail(PHMM_E_ARG, "null plan or tuning");
     if (t->wave_per_sm < 0 || t->wave_per_sm > 64 || t->count_per_sm < -1 || t->count_per_sm > 64 ||
-        t->priorities < 0 || t->priorities > 1 || t->checkpoint < 0 || t->checkpoint > 2)
+        t->priorities < 0 || t->priorities > 1 || t->checkpoint < 0 || t->checkpoint > 2 ||
+        (t->count_chunk != 0 && (t->count_chunk < 8 || t->count_chunk > 512)))
         return fail(PHMM_E_ARG, "tuning out of range (wave_per_sm 0..64, count_per_sm -1..64, priorities 0/1, "
-                                "checkpoint 0..2)");
+                                "checkpoint 0..2, count_chunk 0 or 8..512)");
     int rc = phmm_set_variant(plan, t->variant);
     if (rc) return rc;
     plan->tuning = *t;
@@ -2514,6 +2670,7 @@ extern "C" int phmm_estep_static(const phmm_model_desc *md, const phmm_batch *b,
     K.spin_limit = kSpinLimit;
     K.wave_ctr = nullptr;
     K.cmask = nullptr;
+    K.srange = nullptr;
     K.beam_scale = 0.f;
     phmm_plan launch_ctx;   // carries the SM count for the shared launchers; owns no memory
     launch_ctx.sm_count = g_static_sms[dev];

@@ -18,7 +18,7 @@ from .build import LIB_PATH
 _LIB = None
 
 EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep',
-           'phmm_estep_tables', 'phmm_workspace_bytes', 'phmm_forward_ws', 'phmm_estep_ws',
+           'phmm_estep_tables', 'phmm_estep_band', 'phmm_workspace_bytes', 'phmm_forward_ws', 'phmm_estep_ws',
            'phmm_estep_static', 'phmm_set_timing', 'phmm_kernel_times', 'phmm_kernel_time',
            'phmm_set_variant', 'phmm_set_spin_limit', 'phmm_set_tuning', 'phmm_get_tuning',
            'phmm_last_variant', 'phmm_last_launch_count',
@@ -35,7 +35,8 @@ EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep'
 class Tuning(ctypes.Structure):
     """phmm_tuning: the launch configuration the autotuner searches."""
     _fields_ = [('variant', ctypes.c_int32), ('wave_per_sm', ctypes.c_int32),
-                ('count_per_sm', ctypes.c_int32), ('priorities', ctypes.c_int32), ('checkpoint', ctypes.c_int32)]
+                ('count_per_sm', ctypes.c_int32), ('priorities', ctypes.c_int32), ('checkpoint', ctypes.c_int32),
+                ('count_chunk', ctypes.c_int32)]
 
 
 class ModelDesc(ctypes.Structure):
@@ -111,6 +112,8 @@ def load(path=None):
     lib.phmm_estep_static.restype = ctypes.c_int
     lib.phmm_estep_tables.argtypes = [vp, ctypes.POINTER(Batch)] + [vp] * 10
     lib.phmm_estep_tables.restype = ctypes.c_int
+    lib.phmm_estep_band.argtypes = [vp, ctypes.POINTER(Batch), vp, i32] + [vp] * 8
+    lib.phmm_estep_band.restype = ctypes.c_int
     lib.phmm_workspace_bytes.argtypes = [vp, ctypes.POINTER(Batch), ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
     lib.phmm_workspace_bytes.restype = ctypes.c_int
     lib.phmm_forward_ws.argtypes = [vp, ctypes.POINTER(Batch), vp, ctypes.c_size_t, vp, vp, vp]
@@ -245,7 +248,7 @@ class Plan:
     def set_variant(self, variant):
         """0 automatic, 1 generic, 2 register-resident warp, 3 quad-per-warp block
         kernels, 4 split warp E-step (forward || backward recursion, then counts),
-        5 split block E-step."""
+        5 split block E-step, 6 wide kernels, 7 split E-step on two-warp stripes."""
         _check(self.lib.phmm_set_variant(self.handle, int(variant)), 'phmm_set_variant')
 
     @property
@@ -255,20 +258,21 @@ class Plan:
     def set_timing(self, enable=True):
         _check(self.lib.phmm_set_timing(self.handle, int(enable)), 'phmm_set_timing')
 
-    def set_tuning(self, variant=0, wave_per_sm=0, count_per_sm=-1, priorities=0, checkpoint=0):
+    def set_tuning(self, variant=0, wave_per_sm=0, count_per_sm=-1, priorities=0, checkpoint=0, count_chunk=0):
         """Launch configuration (phmm_set_tuning): kernel family, resident CTAs
         per SM of each wavefront grid (0 automatic), of the overlapped count
         grid (-1 automatic, 0 none), wavefront/count stream priorities, and
         stripe-edge checkpointing of the wide kernels' E-step (0 automatic,
-        1 on, 2 off)."""
-        t = Tuning(int(variant), int(wave_per_sm), int(count_per_sm), int(priorities), int(checkpoint))
+        1 on, 2 off), and the count-pass chunk length (0: 64 steps)."""
+        t = Tuning(int(variant), int(wave_per_sm), int(count_per_sm), int(priorities), int(checkpoint),
+                   int(count_chunk))
         _check(self.lib.phmm_set_tuning(self.handle, ctypes.byref(t)), 'phmm_set_tuning')
 
     def get_tuning(self):
         t = Tuning()
         _check(self.lib.phmm_get_tuning(self.handle, ctypes.byref(t)), 'phmm_get_tuning')
         return {'variant': t.variant, 'wave_per_sm': t.wave_per_sm, 'count_per_sm': t.count_per_sm,
-                'priorities': t.priorities, 'checkpoint': t.checkpoint}
+                'priorities': t.priorities, 'checkpoint': t.checkpoint, 'count_chunk': t.count_chunk}
 
     def set_spin_limit(self, iterations=0):
         """Bound of the kernels' inter-CTA waits in polling iterations (0: the
@@ -559,6 +563,37 @@ def estep_tables(plan, batch, want_F=True, want_B=True, want_post=True, stream=N
         ctypes.c_void_p(s.cuda_stream)), 'phmm_estep_tables')
     return out
 
+
+def estep_band(plan, batch, band_centers, band_half_width, stream=None):
+    """phmm_estep_band: E-step of a banded batch (its cell masks hold the
+    bands) with posteriors in band layout.  band_centers: per pair an int
+    array of Lx+1 centre columns.  Returns the phmm_estep outputs plus
+    'post_band' [sum(Lx+1), 2W+1, N] float64 (pairs' rows concatenated)."""
+    P = batch.n_pairs
+    N = plan.n_states
+    G = plan.n_groups
+    dev = batch.residues.device
+    W = int(band_half_width)
+    centers = np.concatenate([np.asarray(c, np.int32)[:int(a) + 1] for c, a in zip(band_centers, batch.Lx)])
+    if centers.size != int((batch.Lx.astype(np.int64) + 1).sum()):
+        raise ValueError('band_centers: Lx+1 centre columns per pair')
+    d_centers = torch.as_tensor(centers).to(dev)
+    out = {
+        'll': torch.empty(P, dtype=torch.float64, device=dev),
+        'n_trans': torch.empty(P, N, N, dtype=torch.float64, device=dev),
+        'cnt_M': torch.empty(P, G, 21, 21, dtype=torch.float64, device=dev),
+        'cnt_I': torch.empty(P, G, 21, dtype=torch.float64, device=dev),
+        'cnt_D': torch.empty(P, G, 21, dtype=torch.float64, device=dev),
+        'status': torch.empty(P, dtype=torch.int32, device=dev),
+        'post_band': torch.empty(centers.size, 2 * W + 1, N, dtype=torch.float64, device=dev),
+    }
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    _check(plan.lib.phmm_estep_band(
+        plan.handle, ctypes.byref(batch.struct()), _ptr(d_centers), W, _ptr(out['ll']), _ptr(out['n_trans']),
+        _ptr(out['cnt_M']), _ptr(out['cnt_I']), _ptr(out['cnt_D']), _ptr(out['status']), _ptr(out['post_band']),
+        ctypes.c_void_p(s.cuda_stream)), 'phmm_estep_band')
+    out['_centers'] = d_centers   # kept alive until the stream has read it
+    return out
 
 
 class MixDom2Prologue:

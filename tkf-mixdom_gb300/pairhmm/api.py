@@ -339,25 +339,82 @@ def _to_band_layout(dense, band_center, W):
     return out
 
 
+def has_two_warp(plan):
+    """Whether the plan's state space has two-warp stripe kernels (probed
+    once: phmm_set_tuning refuses family 7 without them)."""
+    v = getattr(plan, '_two_warp', None)
+    if v is None:
+        saved = plan.get_tuning()
+        try:
+            plan.set_tuning(**dict(saved, variant=7))
+            v = True
+        except _lib.PairHMMError:
+            v = False
+        finally:
+            plan.set_tuning(**saved)
+        plan._two_warp = v
+    return v
+
+
 def forward_backward_2d_banded(log_trans, state_types, x_seq, y_seq, sub_matrix, pi, band_center, band_width):
     """(log_prob, posteriors_bands, expected_trans) -- dp/hmm.py:2395-2491.
 
     The forward and backward recursions over the cells |j - c_i| <= W
     (W = pad_to_bin(band_width)); posteriors in the reference's band layout
     (pad_to_bin(Lx)+1, 2W+1, N), position (i, b) holding column c_i - W + b.
-    Runs the cell-masked E-step (cells off the band emit nothing).  For Lx
-    off a padding bin the reference's own backward starts from a terminal
-    band placed at row pad_to_bin(Lx) (dp/hmm.py:2337-2343) and its
-    posteriors and counts are not those of the banded model; these are."""
+    Runs the cell-masked E-step (cells off the band emit nothing) through
+    phmm_estep_band, whose stripes skip the anti-diagonal steps off their
+    rows' band and which writes the band-layout posteriors on the device
+    (O(L W) work); a state space without two-warp kernels takes the generic
+    kernels' full tables instead.  For Lx off a padding bin the reference's
+    own backward starts from a terminal band placed at row pad_to_bin(Lx)
+    (dp/hmm.py:2337-2343) and its posteriors and counts are not those of the
+    banded model; these are."""
     st = np.asarray(state_types)
     x, y = np.asarray(x_seq), np.asarray(y_seq)
     Lx, Ly = x.shape[0], y.shape[0]
     W = pad_to_bin(int(band_width))
     mask = band_mask(Lx, Ly, band_center, band_width)
     EM, EI, ED = _tkf_tables(sub_matrix, pi)
-    r = _run_single_tables(_chi_from_log(log_trans), st, np.zeros(st.size, np.int32), EM, EI, ED, x, y,
-                           cell_mask=mask)
-    return r['ll'], _to_band_layout(r['post'], band_center, W), r['n_trans']
+    chi = _chi_from_log(log_trans)
+    groups = np.zeros(st.size, np.int32)
+    plan = get_plan(st, groups, EM.shape[0])
+    if not has_two_warp(plan):
+        r = _run_single_tables(chi, st, groups, EM, EI, ED, x, y, cell_mask=mask)
+        return r['ll'], _to_band_layout(r['post'], band_center, W), r['n_trans']
+    b = _lib.make_batch([x], [y], np.asarray(chi)[None], np.asarray(EM)[None], np.asarray(EI)[None],
+                        np.asarray(ED)[None], device=_device(), cell_masks=[mask])
+    out = _lib.estep_band(plan, b, [np.asarray(band_center, int)[:Lx + 1]], W)
+    post = np.zeros((pad_to_bin(Lx) + 1, 2 * W + 1, st.size))
+    post[:Lx + 1] = out['post_band'].cpu().numpy()
+    return float(out['ll'][0].item()), post, out['n_trans'][0].cpu().numpy()
+
+
+def estep_batch_banded(log_trans, state_types, xs, ys, sub_matrix, pi, band_centers, band_width):
+    """Batched forward_backward_2d_banded (the reference vmaps the single-pair
+    call): one phmm_estep_band launch over every pair.  Returns (log_prob [P],
+    posteriors_bands list of (pad_to_bin(Lx)+1, 2W+1, N), expected_trans
+    [P, N, N]).  Needs a state space with two-warp kernels."""
+    st = np.asarray(state_types)
+    W = pad_to_bin(int(band_width))
+    EM, EI, ED = _tkf_tables(sub_matrix, pi)
+    plan = get_plan(st, np.zeros(st.size, np.int32), EM.shape[0])
+    if not has_two_warp(plan):
+        raise _lib.PairHMMError('estep_batch_banded: no two-warp kernels for this state space')
+    xs = [np.asarray(x) for x in xs]
+    ys = [np.asarray(y) for y in ys]
+    masks = [band_mask(x.size, y.size, c, band_width) for x, y, c in zip(xs, ys, band_centers)]
+    b = _lib.make_batch(xs, ys, np.asarray(_chi_from_log(log_trans))[None], np.asarray(EM)[None],
+                        np.asarray(EI)[None], np.asarray(ED)[None], device=_device(), cell_masks=masks)
+    out = _lib.estep_band(plan, b, [np.asarray(c, int)[:x.size + 1] for c, x in zip(band_centers, xs)], W)
+    pb = out['post_band'].cpu().numpy()
+    posts, r0 = [], 0
+    for x in xs:
+        p_ = np.zeros((pad_to_bin(x.size) + 1, 2 * W + 1, st.size))
+        p_[:x.size + 1] = pb[r0:r0 + x.size + 1]
+        posts.append(p_)
+        r0 += x.size + 1
+    return out['ll'].cpu().numpy(), posts, out['n_trans'].cpu().numpy()
 
 
 def msa_to_envelope(x_len, y_len, msa_x_row, msa_y_row, band_width, gap_token=-1):

@@ -9,7 +9,8 @@ and what varies is how they share the GPU:
   on two-warp or one-warp stripes; block kernels; wide kernels);
 * resident CTAs per SM of each persistent wavefront grid;
 * CTAs per SM of the count grid that runs beside the wavefronts (or none);
-* stream priorities (wavefronts first when SM slots free up).
+* stream priorities (wavefronts first when SM slots free up);
+* the length of the count pass's work items (the tail after the wavefronts).
 
 Stripe-edge checkpointing (phmm_tuning.checkpoint) is left at its automatic
 setting: it trades arithmetic for memory, and a batch that fits either way
@@ -31,6 +32,7 @@ import json
 import math
 import os
 import threading
+import time
 import zlib
 
 import numpy as np
@@ -38,7 +40,8 @@ import torch
 
 from . import _lib
 
-DEFAULT = {'variant': 0, 'wave_per_sm': 0, 'count_per_sm': -1, 'priorities': 0, 'checkpoint': 0}
+DEFAULT = {'variant': 0, 'wave_per_sm': 0, 'count_per_sm': -1, 'priorities': 0, 'checkpoint': 0, 'count_chunk': 0}
+AXES = ('variant', 'wave_per_sm', 'count_per_sm', 'priorities', 'count_chunk')
 _MEM = {}
 _LOCK = threading.Lock()
 
@@ -147,32 +150,50 @@ def _time(plan, batch, out, reps, flush, forward_only):
     return float(np.median(ts)), out
 
 
+def _warm(plan, batch, forward_only, seconds):
+    """Run the batch for `seconds` first: an idle GPU starts at low clocks, and
+    the first configuration timed would otherwise pay for the ramp."""
+    end = time.perf_counter() + seconds
+    out = None
+    while time.perf_counter() < end:
+        if forward_only:
+            _lib.forward(plan, batch)
+        else:
+            out = _lib.estep(plan, batch, out=out)
+        torch.cuda.synchronize()
+
+
 def _axes(plan):
     """Values of each axis that fit this state space (the families are probed:
     set_tuning refuses one without kernels for it)."""
     fams = []
     for v in (7, 4, 5, 6):
         try:
-            plan.set_tuning(v, 0, -1, 0, 0)
+            plan.set_tuning(v, 0, -1, 0, 0, 0)
             fams.append(v)
         except _lib.PairHMMError:
             pass
     plan.set_tuning(**DEFAULT)
     return {'variant': [0] + fams, 'wave_per_sm': [0, 1, 2, 3, 4], 'count_per_sm': [-1, 0, 1, 2],
-            'priorities': [0, 1]}
+            'priorities': [0, 1], 'count_chunk': [0, 32, 128]}
 
 
-def tune(plan, batch, reps=5, forward_only=False, flush_bytes=256 << 20, store=True):
+def tune(plan, batch, reps=5, forward_only=False, flush_bytes=256 << 20, store=True, warmup_s=0.5):
     """Search the launch configuration for this batch on this plan, apply the
     fastest and (store=True) cache it.  Returns {'tuning', 'ms', 'default_ms',
-    'evaluated', 'key', 'table'}; the table lists every configuration timed."""
+    'evaluated', 'key', 'table'}; the table lists every configuration timed.
+    The GPU is warmed on the batch for warmup_s seconds first, and the winner
+    is timed again against the defaults at the end (it must still be faster
+    by more than 1 %), so clock ramps and one-off noise do not pick it."""
     flush = torch.empty(flush_bytes, dtype=torch.uint8, device=batch.residues.device) if flush_bytes else None
     axes = _axes(plan)
+    if warmup_s > 0:
+        _warm(plan, batch, forward_only, warmup_s)
     table = []
     seen = {}
 
     def score(cfg):
-        k = tuple(cfg[a] for a in ('variant', 'wave_per_sm', 'count_per_sm', 'priorities', 'checkpoint'))
+        k = tuple(cfg[a] for a in AXES + ('checkpoint',))
         if k in seen:
             return seen[k]
         try:
@@ -188,7 +209,7 @@ def tune(plan, batch, reps=5, forward_only=False, flush_bytes=256 << 20, store=T
     best_ms = default_ms = score(best)
     for _ in range(2):   # two sweeps of coordinate descent
         improved = False
-        for axis in ('variant', 'wave_per_sm', 'count_per_sm', 'priorities'):
+        for axis in AXES:
             for v in axes[axis]:
                 if v == best[axis]:
                     continue
@@ -198,6 +219,13 @@ def tune(plan, batch, reps=5, forward_only=False, flush_bytes=256 << 20, store=T
                     best, best_ms, improved = cfg, ms, True
         if not improved:
             break
+    if best != DEFAULT:   # confirm against the defaults with fresh timings
+        plan.set_tuning(**DEFAULT)
+        default_ms, _ = _time(plan, batch, None, reps, flush, forward_only)
+        plan.set_tuning(**best)
+        best_ms, _ = _time(plan, batch, None, reps, flush, forward_only)
+        if not best_ms < default_ms * 0.99:
+            best, best_ms = dict(DEFAULT), default_ms
     plan.set_tuning(**best)
     entry = {'tuning': best, 'ms': round(best_ms, 4), 'default_ms': round(default_ms, 4), 'evaluated': len(table)}
     key = _key(plan, batch)

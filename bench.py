@@ -78,6 +78,8 @@ def parse_args():
     ap.add_argument('--serving-requests', type=int, default=2000,
                     help='requests in the serving-stream leg (0: skip it)')
     ap.add_argument('--serving-rate', type=float, default=5000.0)
+    ap.add_argument('--tensor', action='store_true',
+                    help='wide kernels: forward contraction on the tensor cores as 3xTF32 (phmm_tuning.tensor)')
     ap.add_argument('--banded-pairs', type=int, default=1024,
                     help='pairs of the banded-vs-full E-step leg (0: skip)')
     return ap.parse_args()
@@ -581,10 +583,12 @@ def main():
     batch = _lib.make_batch(w.xs, w.ys, chi, EM, EI, ED, device=dev)
     if args.variant:
         plan.set_variant(args.variant)
+    if args.tensor:   # the wide kernels' forward contraction on the tensor cores (3xTF32)
+        plan.set_tuning(**dict(plan.get_tuning(), tensor=1))
     # the project's autotuner (pairhmm.autotune) picks the launch configuration
     # for this batch before anything is timed; skipped when one call is long
     tuning = None
-    if not args.no_tune and not args.variant:
+    if not args.no_tune and not args.variant and not args.tensor:
         from pairhmm import autotune
         t0 = time.perf_counter()
         (_lib.forward(plan, batch) if fwd_only else _lib.estep(plan, batch))
@@ -762,6 +766,7 @@ def main():
                        'parallelism': (f'replicas x{ws}, one combined workload of {ws} configurations '
                                        'LPT-sharded by E-step cost' if ws > 1 else 'replicas x1'),
                        'tuning': tuning,
+                       'wide_contraction': '3xTF32 tensor cores' if args.tensor else 'float32 CUDA cores',
                        'status_nonzero': int((status != 0).sum())},
             'roofline': roofline, 'roofline_hbm': roofline_hbm, 'cpu_baseline': cpu, 'accuracy': acc,
             'e2e': {'value': e2e_value, 'unit': 'cell-state updates/s', 'h2d_bytes_per_step': h2d,

@@ -17,13 +17,13 @@ class FakePlan:
         self.families = families
         self.cfg = None
 
-    def set_tuning(self, variant=0, wave_per_sm=0, count_per_sm=-1, priorities=0, checkpoint=0, count_chunk=0):
+    def set_tuning(self, variant=0, wave_per_sm=0, count_per_sm=-1, priorities=0, checkpoint=0, tensor=0):
         from pairhmm import _lib
         if variant not in (0,) + tuple(self.families):
             raise _lib.PairHMMError('no kernels of this family')
         self.cfg = (variant, wave_per_sm, count_per_sm, priorities)
         self.ckpt = checkpoint
-        self.chunk = count_chunk
+        self.tensor = tensor
 
 
 class FakeBatch:
@@ -48,7 +48,7 @@ def test_cache_round_trip(tmp_path, monkeypatch):
     plan, batch = FakePlan(), FakeBatch([50, 60], [55, 70])
     assert autotune.lookup(plan, batch) is None
     entry = {'tuning': {'variant': 7, 'wave_per_sm': 4, 'count_per_sm': -1, 'priorities': 1, 'checkpoint': 0,
-                        'count_chunk': 0},
+                        'tensor': 0},
              'ms': 2.2,
              'default_ms': 2.3, 'evaluated': 9}
     autotune._store(autotune._key(plan, batch), entry)
@@ -69,7 +69,7 @@ def test_coordinate_descent_finds_the_fast_configuration(monkeypatch, tmp_path):
     monkeypatch.setattr(autotune, '_time', lambda pl, b, out, reps, flush, fo: (cost(*pl.cfg), None))
     r = autotune.tune(plan, batch, flush_bytes=0, warmup_s=0)
     assert r['tuning'] == {'variant': 7, 'wave_per_sm': 3, 'count_per_sm': 0, 'priorities': 1, 'checkpoint': 0,
-                           'count_chunk': 0}
+                           'tensor': 0}
     assert plan.cfg == (7, 3, 0, 1)
     assert abs(r['ms'] - 2.0) < 1e-9 and r['default_ms'] > r['ms'] and r['evaluated'] == len(r['table'])
     autotune._MEM.clear()

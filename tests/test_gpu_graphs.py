@@ -9,9 +9,9 @@
   of a call must survive the next call.
 * The autotuner: a tuned plan gives bit-identical log-likelihoods (the
   forward recursion does not depend on the launch configuration), counts
-  equal to 1e-6 relative (the count pass's chunk length is a tuning axis and
-  changes the order of the float32 partial sums), names its configuration,
-  and a later lookup returns it.
+  equal to 1e-6 relative (the float64 atomic sums of the count pass may add
+  up in another order), names its configuration, and a later lookup returns
+  it.
 """
 import numpy as np
 import pytest

@@ -19,7 +19,7 @@
 
 namespace warp2 {
 
-constexpr int CCH = 64;   // default anti-diagonal steps per count chunk (phmm_tuning.count_chunk)
+constexpr int CCH = 64;   // anti-diagonal steps per count chunk
 
 // ---------------------------------------------------------------- backward recursion only
 template <class SH>
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(32) backward_rec_warp_kernel(const KParams P) 
 }
 
 // ---------------------------------------------------------------- counts from both lattices
-// One warp per chunk of P.cch anti-diagonal steps of one stripe.  The forward
+// One warp per chunk of CCH anti-diagonal steps of one stripe.  The forward
 // and backward lattice rows of step t-1 are copied into shared memory with
 // cp.async while step t is processed (double buffer); lane 31's successor in
 // the first row of the stripe below is loaded one step ahead into registers.
@@ -307,8 +307,8 @@ __device__ void count_chunk_w(const KParams &P, int p, int si, int ch, const Sme
     const int64_t latc = m.lat_base + (int64_t)si * (ROWS + Ly) * ROWS;
     const int64_t latb = m.lat_base + (int64_t)(si + 1) * (ROWS + Ly) * ROWS;   // stripe below (row 0)
     const int T_last = (nrows - 1) + Ly;
-    const int t0 = ch * P.cch;
-    const int t_hi = min(T_last, t0 + P.cch - 1);
+    const int t0 = ch * CCH;
+    const int t_hi = min(T_last, t0 + CCH - 1);
     const int t_top = min(T_last, t_hi + 2);   // two steps of successor history first
     if (t0 > T_last) return;
     if (P.count_wait) {   // the wavefronts may still run: wait for the stripes read here

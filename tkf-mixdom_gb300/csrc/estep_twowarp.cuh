@@ -63,11 +63,6 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
     float *bnd = sm + LT.bnd;
     int *bndE = reinterpret_cast<int *>(sm) + LT.bndE;
     volatile int *s_abort = reinterpret_cast<int *>(sm) + LT.flag;
-    // halo staging: thread 0 copies column t+1 of the edge row above into
-    // slot (t+1) & 1 with cp.async at the start of step t, so the copy runs
-    // during the step's contraction instead of on the step's critical path
-    float *hst = sm + L.halo;
-    int *hstE = reinterpret_cast<int *>(sm) + L.haloE;
 
     if (r < 32) load_model_w<SH>(P, p, m, L, sm, smb, CHI_FWD_PAIRS);
     if (r < 2 * SP) bnd[r] = 0.f;
@@ -152,22 +147,14 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
     }
 
     for (int t = t_beg; t <= t_end; ++t) {
-        // halo (row i0-1, column t) for thread 0: staged during step t-1, else
-        // waited for and loaded here
-        if (si > 0 && t <= Ly && r == 0) {
-            if (MK && (t < hlo || t > hhi)) {   // off the live columns above: zero
+        // halo (row i0-1, column t) for thread 0: normally prefetched during
+        // step t-1; zero off the live columns above (a cell mask)
+        if (si > 0 && t <= Ly && r == 0 && hx_col != t) {
+            if (MK && (t < hlo || t > hhi)) {
 #pragma unroll
                 for (int s = 0; s < SP; ++s) hx[s] = 0.f;
                 hxE = EXP_NONE;
-            } else if (hx_col == t) {
-                cp_wait0();
-                const float4 *st = reinterpret_cast<const float4 *>(hst + (t & 1) * SP);
-#pragma unroll
-                for (int q = 0; q < SP / 4; ++q) {
-                    const float4 v = st[q];
-                    hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
-                }
-                hxE = hstE[t & 1];
+                hx_col = t;
             } else if (!wait_geq(prog_above, t + 1, P.spin_limit)) {
                 s_abort[t & 1] = 1;   // read by all threads after this step's barrier
             } else {
@@ -178,21 +165,8 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
                     hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
                 }
                 hxE = __ldcg(edgeE_above + t);
+                hx_col = t;
             }
-            // stage column t+1 when the progress read earlier covers it
-            if (t + 1 <= hhi && (!MK || t + 1 >= hlo) && pv > t + 1) {
-                const float *src = edge_above + (int64_t)(t + 1) * SP;
-                float *dst = hst + ((t + 1) & 1) * SP;
-#pragma unroll
-                for (int q = 0; q < SP / 4; ++q) cp_async16(dst + 4 * q, src + 4 * q);
-                cp_async4(hstE + ((t + 1) & 1), edgeE_above + t + 1);
-                cp_commit();
-                hx_col = t + 1;
-            }
-            // progress for the staging of column t+2 at the start of step t+1,
-            // polled now (only when the last value read does not cover it) so
-            // the load has the whole step to arrive
-            if (t + 2 <= hhi && pv <= t + 2) pv = ld_acquire(prog_above);
         }
         const int jc = t - r;
         const bool valid = r < nrows && jc >= 0 && jc <= Ly;
@@ -349,12 +323,31 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
             bndE[t & 1] = Eprev;
         }
         load_emit(t + 1);
+        // prefetch halo column t+1 when the progress read last step covers it
+        // (its loads then overlap the barrier), and poll for the column after
+        if (si > 0 && r == 0 && t + 1 <= Ly) {
+            if (MK && (t + 1 < hlo || t + 1 > hhi)) {
+#pragma unroll
+                for (int s = 0; s < SP; ++s) hx[s] = 0.f;
+                hxE = EXP_NONE;
+                hx_col = t + 1;
+            } else if (pv > t + 1) {
+                const float4 *src = reinterpret_cast<const float4 *>(edge_above + (int64_t)(t + 1) * SP);
+#pragma unroll
+                for (int q = 0; q < SP / 4; ++q) {
+                    const float4 v = __ldcg(src + q);
+                    hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
+                }
+                hxE = __ldcg(edgeE_above + t + 1);
+                hx_col = t + 1;
+            }
+            if (t + 2 <= hhi && pv <= t + 2) pv = ld_acquire(prog_above);
+        }
         __syncthreads();
         // the flag of step t is written only before this barrier, and the
         // next write goes to the other parity: every thread sees the same value
         if (s_abort[t & 1]) { aborted = true; break; }
     }
-    if (r == 0) cp_wait0();   // no staged copy outlives the stripe
     if (aborted) {
         if (r == ROWS - 1 && has_below) st_release(prog_mine, Ly + 1);
         if (r == 0) {
@@ -390,10 +383,6 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
     float *bnd = sm + LT.bnd;
     int *bndE = reinterpret_cast<int *>(sm) + LT.bndE;
     volatile int *s_abort = reinterpret_cast<int *>(sm) + LT.flag;
-    // halo staging: thread 63 copies column jb-1 of the edge row below into
-    // slot (jb-1) & 1 with cp.async at the start of the step that reads jb
-    float *hst = sm + L.halo;
-    int *hstE = reinterpret_cast<int *>(sm) + L.haloE;
 
     if (r < 32) load_model_w<SH>(P, p, m, L, sm, smb, CHI_BWD_PAIRS);
     if (r < 2 * SP) bnd[r] = 0.f;
@@ -489,20 +478,14 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
 
     for (int t = t_end; t >= t_beg; --t) {
         const int jb = t - (ROWS - 1);
-        if (has_below && jb >= 0 && jb <= Ly && r == ROWS - 1) {
-            if (MK && (jb < hlo || jb > hhi)) {   // off the live columns below: zero
+        // halo (row i0+64, column jb) for thread 63: normally prefetched during
+        // step t+1; zero off the live columns below (a cell mask)
+        if (has_below && jb >= 0 && jb <= Ly && r == ROWS - 1 && hx_col != jb) {
+            if (MK && (jb < hlo || jb > hhi)) {
 #pragma unroll
                 for (int s = 0; s < SP; ++s) hx[s] = 0.f;
                 hxE = EXP_NONE;
-            } else if (hx_col == jb) {   // staged during the previous step
-                cp_wait0();
-                const float4 *st = reinterpret_cast<const float4 *>(hst + (jb & 1) * SP);
-#pragma unroll
-                for (int q = 0; q < SP / 4; ++q) {
-                    const float4 v = st[q];
-                    hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
-                }
-                hxE = hstE[jb & 1];
+                hx_col = jb;
             } else if (!wait_geq(prog_below, Ly + 1 - jb, P.spin_limit)) {
                 s_abort[t & 1] = 1;   // read by all threads after this step's barrier
             } else {
@@ -513,19 +496,8 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
                     hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
                 }
                 hxE = __ldcg(edgeE_below + jb);
+                hx_col = jb;
             }
-            // stage column jb-1 when the progress read earlier covers it
-            if (jb - 1 >= hlo && (!MK || jb - 1 <= hhi) && pv >= Ly + 1 - (jb - 1)) {
-                const float *src = edge_below + (int64_t)(jb - 1) * SP;
-                float *dst = hst + ((jb - 1) & 1) * SP;
-#pragma unroll
-                for (int q = 0; q < SP / 4; ++q) cp_async16(dst + 4 * q, src + 4 * q);
-                cp_async4(hstE + ((jb - 1) & 1), edgeE_below + jb - 1);
-                cp_commit();
-                hx_col = jb - 1;
-            }
-            // progress for the staging of column jb-2 at the next step, polled now
-            if (jb - 2 >= hlo && pv < Ly + 1 - (jb - 2)) pv = ld_acquire(prog_below);
         }
         const int jc = t - r;
         const bool valid = r < nrows && jc >= 0 && jc <= Ly;
@@ -683,12 +655,31 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
             bndE[t & 1] = Ewn;
         }
         load_emit(t - 1);
+        // prefetch halo column jb-1 when the progress read last step covers it,
+        // and poll for the column after
+        if (has_below && r == ROWS - 1 && jb - 1 >= 0 && jb - 1 <= Ly) {
+            if (MK && (jb - 1 < hlo || jb - 1 > hhi)) {
+#pragma unroll
+                for (int s = 0; s < SP; ++s) hx[s] = 0.f;
+                hxE = EXP_NONE;
+                hx_col = jb - 1;
+            } else if (pv >= Ly + 1 - (jb - 1)) {
+                const float4 *src = reinterpret_cast<const float4 *>(edge_below + (int64_t)(jb - 1) * SP);
+#pragma unroll
+                for (int q = 0; q < SP / 4; ++q) {
+                    const float4 v = __ldcg(src + q);
+                    hx[4 * q] = v.x; hx[4 * q + 1] = v.y; hx[4 * q + 2] = v.z; hx[4 * q + 3] = v.w;
+                }
+                hxE = __ldcg(edgeE_below + jb - 1);
+                hx_col = jb - 1;
+            }
+            if (jb - 2 >= hlo && pv < Ly + 3 - jb) pv = ld_acquire(prog_below);
+        }
         __syncthreads();
         // the flag of step t is written only before this barrier, and the
         // next write goes to the other parity: every thread sees the same value
         if (s_abort[t & 1]) { aborted = true; break; }
     }
-    if (r == ROWS - 1) cp_wait0();   // no staged copy outlives the stripe
     if (aborted && r == 0) {
         atomicOr(P.status + p, PHMM_ST_TIMEOUT);
         if (has_above) st_release(prog_mine, Ly + 1);
@@ -720,7 +711,7 @@ __global__ void __launch_bounds__(TWT) stripe_tw_kernel(const KParams P) {
 }  // namespace warp2
 
 // ---------------------------------------------------------------- two-warp count pass
-// count_chunk_w with one row per thread: a 64-thread CTA takes a chunk of P.cch
+// count_chunk_w with one row per thread: a 64-thread CTA takes a chunk of CCH
 // anti-diagonal steps of one stripe, both warps sharing the model tables and
 // the double-buffered lattice rows.  Row r's D- and M-successors come from row
 // r+1 by __shfl_down inside a warp, through a shared slot across the two warps
@@ -748,7 +739,8 @@ __host__ __device__ inline SmemCT make_smem_ct(int SP, int KP, int NI, int G, in
     return L;
 }
 
-template <class SH>
+// MK: a cell-masked batch (the stripes' live step ranges in P.srange)
+template <class SH, bool MK>
 __device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const SmemCT &LT, float *sm,
                                unsigned char *smb) {
     constexpr int NE = SH::NE, NSRC = SH::NSRC, SP = SH::SP, KP = SH::KP, NM = SH::NM, NI = SH::NI;
@@ -769,7 +761,7 @@ __device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const Sm
     // of this stripe and columns [blo, bhi] of the first row below: the count
     // covers those steps of the chunk and reads the rest as zero
     int t_beg = 0, t_last = T_last, blo = 0, bhi = Ly;
-    if (P.srange) {
+    if (MK) {
         const int2 rg = P.srange[m.stripe_base + si];
         t_beg = max(0, rg.x);
         t_last = min(T_last, rg.y + nrows - 1);
@@ -779,8 +771,8 @@ __device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const Sm
             bhi = min(Ly, rb.y);
         }
     }
-    const int t0 = ch * P.cch;
-    const int t_hi = min(t_last, t0 + P.cch - 1);
+    const int t0 = ch * CCH;
+    const int t_hi = min(t_last, t0 + CCH - 1);
     const int t_lo = max(t0, t_beg);
     const int t_top = min(T_last, t_hi + 2);   // two steps of successor history first
     if (t_lo > t_hi) return;                    // uniform over the CTA
@@ -809,7 +801,7 @@ __device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const Sm
     auto prefetch = [&](int t) {
         if (t >= t_lo) {
             const int buf = t & 1;
-            if (t > t_last) {   // successor history past the live steps: b~ = 0
+            if (MK && t > t_last) {   // successor history past the live steps: b~ = 0
                 for (int idx = r; idx < ROWS * SPP; idx += TWT) bbuf[buf * ROWS * SPP + idx] = 0.f;
                 bEb[buf * ROWS + r] = EXP_NONE;
             } else {
@@ -1140,7 +1132,7 @@ __device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const Sm
     __syncthreads();
 }
 
-template <class SH>
+template <class SH, bool MK>
 __global__ void __launch_bounds__(TWT) count_tw_kernel(const KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *sm = reinterpret_cast<float *>(smem_raw);
@@ -1153,7 +1145,7 @@ __global__ void __launch_bounds__(TWT) count_tw_kernel(const KParams P) {
         __syncthreads();
         if (it >= P.n_items) break;
         const int2 w = P.items[it];
-        count_chunk_tw<SH>(P, w.x, w.y >> 12, w.y & 4095, L, sm, smem_raw);
+        count_chunk_tw<SH, MK>(P, w.x, w.y >> 12, w.y & 4095, L, sm, smem_raw);
     }
 }
 

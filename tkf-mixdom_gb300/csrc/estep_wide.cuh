@@ -83,7 +83,33 @@ __device__ __forceinline__ float emit_g(const KParams &P, const float *eM, const
     return 0.f;
 }
 
+// ---------------------------------------------------------------- 3xTF32 helpers
+// x = hi + lo with hi = x rounded to TF32 and lo the TF32-rounded remainder;
+// hi*hi + hi*lo + lo*hi then carries about 21 bits of each product.
+__device__ __forceinline__ void tf32_split(float x, uint32_t &hi, uint32_t &lo) {
+    uint32_t h, l;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+    const float rem = x - __uint_as_float(h);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(rem));
+    hi = h;
+    lo = l;
+}
+
+// c += a b on the tensor cores (one warp; m16 n8 k8, TF32 inputs, float32
+// accumulator).  Fragments: a0 (g, q), a1 (g+8, q), a2 (g, q+4), a3 (g+8, q+4);
+// b0 (k q, n g), b1 (k q+4, n g); c0/c1 (g, 2q / 2q+1), c2/c3 (g+8, ...), with
+// g = lane / 4, q = lane % 4.
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
 // ---------------------------------------------------------------- forward
+// TC: the step's contraction on the tensor cores (phmm_tuning.tensor; the host
+// sets it only where every warp's 16 destinations share one type)
+template <bool TC>
 __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, float *sm, unsigned char *smb) {
     const int NS = P.NS, KS = P.kend[2], NQd = KS / 4, N = P.N;
     const PairMeta m = P.meta[p];
@@ -289,9 +315,78 @@ __device__ void fwd_stripe_wd(const KParams &P, int p, int si, const SmemWd &L, 
                         }
                     }
             };
-            int s8 = 0;
-            for (; s8 + 8 <= NS; s8 += 8) block(s8, 8);
-            if (s8 < NS) block(s8, NS - s8);
+            if (TC) {
+                // the warp's 32 rows x 16 destinations (quads 4 warp .. 4 warp + 3)
+                // as 2 x 2 tiles of m16 n8 over k-steps of 8 sources, 3xTF32
+                const int g = lane >> 2, cq = lane & 3, n0 = 16 * warp;
+                const float *bw = base - r0;   // the warp's rows from 0
+                float c[2][2][4];
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                    for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) c[mt][nt][e] = 0.f;
+                for (int s0 = 0; s0 < NS; s0 += 8) {
+                    const int sa0 = s0 + cq, sa1 = s0 + cq + 4;
+                    const bool in0 = sa0 < NS, in1 = sa1 < NS;
+                    uint32_t ahi[2][4], alo[2][4], bhi[2][2], blo[2][2];
+#pragma unroll
+                    for (int mt = 0; mt < 2; ++mt) {
+                        const int m0 = 16 * mt + g;
+                        const float a0 = in0 ? bw[sa0 * stride + m0] : 0.f;
+                        const float a1 = in0 ? bw[sa0 * stride + m0 + 8] : 0.f;
+                        const float a2 = in1 ? bw[sa1 * stride + m0] : 0.f;
+                        const float a3 = in1 ? bw[sa1 * stride + m0 + 8] : 0.f;
+                        tf32_split(a0, ahi[mt][0], alo[mt][0]);
+                        tf32_split(a1, ahi[mt][1], alo[mt][1]);
+                        tf32_split(a2, ahi[mt][2], alo[mt][2]);
+                        tf32_split(a3, ahi[mt][3], alo[mt][3]);
+                    }
+#pragma unroll
+                    for (int nt = 0; nt < 2; ++nt) {
+                        const int n = n0 + 8 * nt + g;
+                        const float b0 = in0 ? chiS[sa0 * KS + n] : 0.f;
+                        const float b1 = in1 ? chiS[sa1 * KS + n] : 0.f;
+                        tf32_split(b0, bhi[nt][0], blo[nt][0]);
+                        tf32_split(b1, bhi[nt][1], blo[nt][1]);
+                    }
+#pragma unroll
+                    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                        for (int nt = 0; nt < 2; ++nt) {   // small terms first
+                            mma_tf32(c[mt][nt], alo[mt], bhi[nt]);
+                            mma_tf32(c[mt][nt], ahi[mt], blo[nt]);
+                            mma_tf32(c[mt][nt], ahi[mt], bhi[nt]);
+                        }
+                }
+                // back to this thread's 4 x 4 tile through the warp's own output
+                // rows of ring A's slot for this step (free until the outputs
+                // land there): [destination][row]
+                float *stg = A + ((t & 1) * NS + n0) * RW;
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                    for (int nt = 0; nt < 2; ++nt) {
+                        const int d = 8 * nt + 2 * cq, rw = 16 * mt + g;
+                        stg[d * RW + rw] = c[mt][nt][0];
+                        stg[(d + 1) * RW + rw] = c[mt][nt][1];
+                        stg[d * RW + rw + 8] = c[mt][nt][2];
+                        stg[(d + 1) * RW + rw + 8] = c[mt][nt][3];
+                    }
+                __syncwarp();
+                const int ql = qd - 4 * warp;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float4 v = *reinterpret_cast<const float4 *>(stg + (4 * ql + u) * RW + r0);
+                    acc[0][u] = v.x; acc[1][u] = v.y; acc[2][u] = v.z; acc[3][u] = v.w;
+                }
+                __syncwarp();
+            } else {
+                int s8 = 0;
+                for (; s8 + 8 <= NS; s8 += 8) block(s8, 8);
+                if (s8 < NS) block(s8, NS - s8);
+            }
             // emissions, scale, outputs
             float mxr[4];
 #pragma unroll
@@ -652,6 +747,7 @@ __device__ void bwd_rec_stripe_wd(const KParams &P, int p, int si, const SmemWd 
     if (tid == 0) st_release(prog_mine, Ly + 2);
 }
 
+template <bool TC>
 __global__ void __launch_bounds__(512) fwdbwd_wide_kernel(const KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
@@ -666,7 +762,7 @@ __global__ void __launch_bounds__(512) fwdbwd_wide_kernel(const KParams P) {
         if (it >= P.n_items) break;
         const int2 w = P.items[it];
         if (w.y & blk::BWD_ITEM) bwd_rec_stripe_wd(P, w.x, w.y & ~blk::BWD_ITEM, Lb, sm, smem_raw);
-        else fwd_stripe_wd(P, w.x, w.y, Lf, sm, smem_raw);
+        else fwd_stripe_wd<TC>(P, w.x, w.y, Lf, sm, smem_raw);
     }
 }
 
@@ -966,6 +1062,7 @@ __global__ void __launch_bounds__(CT, 1) count_wide_kernel(const KParams P) {
     }
 }
 
+template <bool TC>
 __global__ void __launch_bounds__(512) forward_wide_kernel(const KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
@@ -978,7 +1075,7 @@ __global__ void __launch_bounds__(512) forward_wide_kernel(const KParams P) {
         const int it = s_item;
         if (it >= P.n_items) break;
         const int2 w = P.items[it];
-        fwd_stripe_wd(P, w.x, w.y, L, sm, smem_raw);
+        fwd_stripe_wd<TC>(P, w.x, w.y, L, sm, smem_raw);
     }
 }
 

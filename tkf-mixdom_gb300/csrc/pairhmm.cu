@@ -95,7 +95,6 @@ struct KParams {
     float *bedge;
     int *bedge_exp;
     int count_wait;                     // count pass waits for the stripes it reads
-    int cch;                            // anti-diagonal steps per count chunk (warp count passes)
     float *edge;
     int *edge_exp;
     int *progress;
@@ -1294,6 +1293,17 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     if (NQd > 48 || ((NQ + wide::SPL - 1) / wide::SPL) * NQd > wide::CT * wide::CTPT)
         return fail(PHMM_E_ARG, "state space too large for the wide kernels");
     if (!ws_need) plan->last_variant = 6;
+    // forward contraction on the tensor cores (phmm_tuning.tensor), for
+    // forward-only calls: a warp's 16 destinations form its m16n8 tiles, so
+    // every warp needs four whole destination quads of one type.  (In an
+    // E-step the forward's 3xTF32 rounding no longer cancels against the
+    // float32 backward's: counts went 1e-3 off at 162 states.)
+    bool tc = !estep && plan->tuning.tensor != 0 && NQd % 4 == 0;
+    for (int w = 0; tc && w < NQd / 4; ++w)
+        for (int q = 1; q < 4; ++q)
+            if (K.quad_type[4 * w + q] != K.quad_type[4 * w]) tc = false;
+    auto fb_kernel = tc ? wide::fwdbwd_wide_kernel<true> : wide::fwdbwd_wide_kernel<false>;
+    auto f_kernel = tc ? wide::forward_wide_kernel<true> : wide::forward_wide_kernel<false>;
     std::vector<int> order(P_);
     for (int p = 0; p < P_; ++p) {
         if (b->Lx_host[p] < 0 || b->Ly_host[p] < 0) return fail(PHMM_E_ARG, "negative length");
@@ -1365,10 +1375,9 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
             const int threads = 32 * ((NQd + 3) / 4);
             const int rbytes = std::max(wide::make_smem_wd(NS, KS, max_ly, false).bytes,
                                         wide::make_smem_wd(NS, KS, max_ly, true).bytes);
-            CUDA_TRY(cudaFuncSetAttribute(wide::fwdbwd_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          rbytes));
+            CUDA_TRY(cudaFuncSetAttribute(fb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, rbytes));
             int rocc = 0;
-            CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rocc, wide::fwdbwd_wide_kernel, threads, rbytes));
+            CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rocc, fb_kernel, threads, rbytes));
             const int gmax = std::max(1, plan->sm_count * std::max(rocc, 1) / 2);
             std::vector<int2> members;
             auto close = [&]() {
@@ -1530,7 +1539,7 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         const int threads = 32 * ((NQd + 3) / 4);
         const int bytes = std::max(wide::make_smem_wd(NS, KS, max_ly, false).bytes,
                                    estep ? wide::make_smem_wd(NS, KS, max_ly, true).bytes : 0);
-        auto kern = estep ? wide::fwdbwd_wide_kernel : wide::forward_wide_kernel;
+        auto kern = estep ? fb_kernel : f_kernel;
         CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         int occ = 0;
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, bytes));
@@ -1568,7 +1577,7 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
             const int rbytes = std::max(wide::make_smem_wd(NS, KS, max_ly, false).bytes,
                                         wide::make_smem_wd(NS, KS, max_ly, true).bytes);
             int rocc = 0;
-            CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rocc, wide::fwdbwd_wide_kernel, threads, rbytes));
+            CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rocc, fb_kernel, threads, rbytes));
             if (rocc < 1) return fail(PHMM_E_ARG, "wide kernel does not fit on an SM (shared memory)");
             K.lat = d_lat;
             K.blat = d_blat;
@@ -1582,7 +1591,7 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
                 K.items = (const int2 *)d_items + g.rc_off;
                 K.n_items = (int)g.n_rc;
                 K.counter = d_counters;
-                wide::fwdbwd_wide_kernel<<<std::min((int)g.n_rc, plan->sm_count * rocc), threads, rbytes, stream>>>(K);
+                fb_kernel<<<std::min((int)g.n_rc, plan->sm_count * rocc), threads, rbytes, stream>>>(K);
                 CUDA_TRY(cudaGetLastError());
                 // counts of the group from its scratch lattices
                 K.recompute = 0;
@@ -1758,8 +1767,7 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
             for (int s = plan->h_meta[p].n_stripes - 1; s >= 0; --s) plan->h_items.push_back(make_int2(p, s));
     }
     int n_citems = 0;
-    const int cch = plan->tuning.count_chunk > 0 ? plan->tuning.count_chunk : warp2::CCH;
-    K.cch = cch;
+    const int cch = warp2::CCH;
     if (split) {   // count chunks: (pair, stripe << 12 | chunk), shortest pairs first (ready first)
         for (auto it = order.rbegin(); it != order.rend(); ++it) {
             const int p = *it;
@@ -2007,7 +2015,7 @@ int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, 
     int bytes = 0, threads = 32;
     if (kind == 3 && plan->two_warp) {   // count pass of the two-warp split E-step
         bytes = warp2::make_smem_ct(SH::SP, SH::KP, SH::NI, K.G, max_ly).bytes;
-        kern = warp2::count_tw_kernel<SH>;
+        kern = K.srange ? warp2::count_tw_kernel<SH, true> : warp2::count_tw_kernel<SH, false>;
         threads = warp2::TWT;
     } else if (kind == 3) {
         bytes = warp2::make_smem_c(SH::SP, SH::KP, SH::NI, K.G, max_ly).bytes;
@@ -2415,9 +2423,9 @@ int phmm_set_tuning(phmm_plan *plan, const phmm_tuning *t) {
     if (!plan || !t) return fail(PHMM_E_ARG, "null plan or tuning");
     if (t->wave_per_sm < 0 || t->wave_per_sm > 64 || t->count_per_sm < -1 || t->count_per_sm > 64 ||
         t->priorities < 0 || t->priorities > 1 || t->checkpoint < 0 || t->checkpoint > 2 ||
-        (t->count_chunk != 0 && (t->count_chunk < 8 || t->count_chunk > 512)))
+        t->tensor < 0 || t->tensor > 1)
         return fail(PHMM_E_ARG, "tuning out of range (wave_per_sm 0..64, count_per_sm -1..64, priorities 0/1, "
-                                "checkpoint 0..2, count_chunk 0 or 8..512)");
+                                "checkpoint 0..2, tensor 0/1)");
     int rc = phmm_set_variant(plan, t->variant);
     if (rc) return rc;
     plan->tuning = *t;

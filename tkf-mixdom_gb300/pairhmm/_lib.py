@@ -36,7 +36,7 @@ class Tuning(ctypes.Structure):
     """phmm_tuning: the launch configuration the autotuner searches."""
     _fields_ = [('variant', ctypes.c_int32), ('wave_per_sm', ctypes.c_int32),
                 ('count_per_sm', ctypes.c_int32), ('priorities', ctypes.c_int32), ('checkpoint', ctypes.c_int32),
-                ('count_chunk', ctypes.c_int32)]
+                ('tensor', ctypes.c_int32)]
 
 
 class ModelDesc(ctypes.Structure):
@@ -258,21 +258,22 @@ class Plan:
     def set_timing(self, enable=True):
         _check(self.lib.phmm_set_timing(self.handle, int(enable)), 'phmm_set_timing')
 
-    def set_tuning(self, variant=0, wave_per_sm=0, count_per_sm=-1, priorities=0, checkpoint=0, count_chunk=0):
+    def set_tuning(self, variant=0, wave_per_sm=0, count_per_sm=-1, priorities=0, checkpoint=0, tensor=0):
         """Launch configuration (phmm_set_tuning): kernel family, resident CTAs
         per SM of each wavefront grid (0 automatic), of the overlapped count
-        grid (-1 automatic, 0 none), wavefront/count stream priorities, and
+        grid (-1 automatic, 0 none), wavefront/count stream priorities,
         stripe-edge checkpointing of the wide kernels' E-step (0 automatic,
-        1 on, 2 off), and the count-pass chunk length (0: 64 steps)."""
+        1 on, 2 off), and the wide forward contraction on the tensor cores as
+        3xTF32 (tensor=1)."""
         t = Tuning(int(variant), int(wave_per_sm), int(count_per_sm), int(priorities), int(checkpoint),
-                   int(count_chunk))
+                   int(tensor))
         _check(self.lib.phmm_set_tuning(self.handle, ctypes.byref(t)), 'phmm_set_tuning')
 
     def get_tuning(self):
         t = Tuning()
         _check(self.lib.phmm_get_tuning(self.handle, ctypes.byref(t)), 'phmm_get_tuning')
         return {'variant': t.variant, 'wave_per_sm': t.wave_per_sm, 'count_per_sm': t.count_per_sm,
-                'priorities': t.priorities, 'checkpoint': t.checkpoint, 'count_chunk': t.count_chunk}
+                'priorities': t.priorities, 'checkpoint': t.checkpoint, 'tensor': t.tensor}
 
     def set_spin_limit(self, iterations=0):
         """Bound of the kernels' inter-CTA waits in polling iterations (0: the

@@ -9,12 +9,13 @@ and what varies is how they share the GPU:
   on two-warp or one-warp stripes; block kernels; wide kernels);
 * resident CTAs per SM of each persistent wavefront grid;
 * CTAs per SM of the count grid that runs beside the wavefronts (or none);
-* stream priorities (wavefronts first when SM slots free up);
-* the length of the count pass's work items (the tail after the wavefronts).
+* stream priorities (wavefronts first when SM slots free up).
 
 Stripe-edge checkpointing (phmm_tuning.checkpoint) is left at its automatic
 setting: it trades arithmetic for memory, and a batch that fits either way
-runs faster without it.
+runs faster without it.  The tensor-core contraction (phmm_tuning.tensor)
+is left off: it changes the results' rounding, which a launch setting must
+not.
 
 Results do not depend on the configuration (the same kernels on the same work
 items), only the time does.  The search is a coordinate descent over those
@@ -40,8 +41,8 @@ import torch
 
 from . import _lib
 
-DEFAULT = {'variant': 0, 'wave_per_sm': 0, 'count_per_sm': -1, 'priorities': 0, 'checkpoint': 0, 'count_chunk': 0}
-AXES = ('variant', 'wave_per_sm', 'count_per_sm', 'priorities', 'count_chunk')
+DEFAULT = {'variant': 0, 'wave_per_sm': 0, 'count_per_sm': -1, 'priorities': 0, 'checkpoint': 0, 'tensor': 0}
+AXES = ('variant', 'wave_per_sm', 'count_per_sm', 'priorities')
 _MEM = {}
 _LOCK = threading.Lock()
 
@@ -175,7 +176,7 @@ def _axes(plan):
             pass
     plan.set_tuning(**DEFAULT)
     return {'variant': [0] + fams, 'wave_per_sm': [0, 1, 2, 3, 4], 'count_per_sm': [-1, 0, 1, 2],
-            'priorities': [0, 1], 'count_chunk': [0, 32, 128]}
+            'priorities': [0, 1]}
 
 
 def tune(plan, batch, reps=5, forward_only=False, flush_bytes=256 << 20, store=True, warmup_s=0.5):
@@ -193,7 +194,7 @@ def tune(plan, batch, reps=5, forward_only=False, flush_bytes=256 << 20, store=T
     seen = {}
 
     def score(cfg):
-        k = tuple(cfg[a] for a in AXES + ('checkpoint',))
+        k = tuple(cfg[a] for a in AXES + ('checkpoint', 'tensor'))
         if k in seen:
             return seen[k]
         try:

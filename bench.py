@@ -73,6 +73,8 @@ def parse_args():
                     help='truncate every sequence to at most L residues (small case for ncu captures)')
     ap.add_argument('--cpu-seconds', type=float, default=12.0)
     ap.add_argument('--no-tune', action='store_true', help='skip the autotuner (library defaults)')
+    ap.add_argument('--dense', action='store_true',
+                    help='give the kernels only the dense chi (no factored MixDom transitions)')
     ap.add_argument('--no-accuracy', action='store_true',
                     help='skip the accuracy leg (every pair against the FP64 oracle)')
     ap.add_argument('--serving-requests', type=int, default=2000,
@@ -580,7 +582,10 @@ def main():
         chi = pm.tkf91_trans(w.params['ins_rate'], w.params['del_rate'], tt.cpu()).to(dev)
         EM, EI, ED = pm.tables_tkf(pm.transition_matrix(pm._t(w.params['Q'], dev), tt), pm._t(w.params['pi'], dev))
         plan = api.get_plan(np.array([pm.S, pm.M, pm.I, pm.D, pm.E]), np.zeros(5, np.int32), 1)
-    batch = _lib.make_batch(w.xs, w.ys, chi, EM, EI, ED, device=dev)
+    nest, nest_kf = None, None
+    if w.model == 'mixdom2' and not args.dense:   # the factored MixDom transitions (phmm_batch.nest)
+        nest, nest_kf = api._mixdom2_nest(w.params, w.ts, dev), (K, F)
+    batch = _lib.make_batch(w.xs, w.ys, chi, EM, EI, ED, device=dev, nest=nest, nest_kf=nest_kf)
     if args.variant:
         plan.set_variant(args.variant)
     if args.tensor:   # the wide kernels' forward contraction on the tensor cores (3xTF32)
@@ -767,6 +772,8 @@ def main():
                                        'LPT-sharded by E-step cost' if ws > 1 else 'replicas x1'),
                        'tuning': tuning,
                        'wide_contraction': '3xTF32 tensor cores' if args.tensor else 'float32 CUDA cores',
+                       'transitions': ('factored MixDom chi (phmm_batch.nest)' if nest is not None
+                                       else 'dense chi'),
                        'status_nonzero': int((status != 0).sum())},
             'roofline': roofline, 'roofline_hbm': roofline_hbm, 'cpu_baseline': cpu, 'accuracy': acc,
             'e2e': {'value': e2e_value, 'unit': 'cell-state updates/s', 'h2d_bytes_per_step': h2d,

@@ -92,6 +92,21 @@ typedef struct phmm_batch {
      * (variants 0 and 1; the automatic choice takes them for a pruned batch)
      * and by phmm_estep_tables. */
     double beam_log_width;
+    /* device, may be NULL: the MixDom transitions of chi in factored form
+     * (build_nested_trans, models/mixdom.py:343-394), one record per pair
+     * (or one shared, as chi), 20*K*F + 25*K*F*F floats, body state
+     * q = 0..5KF-1 being state 2 + q:
+     *   exit[q]; cin[a][q] for the top-level types a = M, I, D
+     *   (= dest[q] * T_exit_k[d_q][a][U(q)]); intra[d][5F][5F], the
+     *   same-domain block without its inter-domain part,
+     * so that chi[2+s][2+k] = exit[s] cin[U(s)][k] + [same domain] intra.
+     * The dense chi is still required (start row, end column, counts).
+     * With it the two-warp stripes of a compiled layout (K = 3, F = 1)
+     * contract each cell in about 6N + 11KF^2 multiply-adds instead of N^2;
+     * other layouts, masked and pruned batches use the dense chi.
+     * phmm_mixdom2_nest builds it.  nest_dom = K, nest_frag = F. */
+    const float *nest;
+    int32_t nest_dom, nest_frag;
 } phmm_batch;
 
 typedef struct phmm_plan phmm_plan;
@@ -285,6 +300,19 @@ int phmm_mixdom2_class_counts_dp(const void *param_block, int32_t n_dom, int32_t
                                  const double *cnt_I, const double *cnt_D, double *class_match,
                                  double *class_insert, double *class_delete, double *classdist_counts,
                                  void *stream);
+
+/* The factored form of the collapsed chi (phmm_batch.nest), float32
+ * [P][20KF + 25KF^2] on the device, for per-pair times t [P] (device float64):
+ * the exit factors, entry-weighted top-level transitions and same-domain
+ * blocks that build_nested_trans (models/mixdom.py:252-423) assembles chi
+ * from.  The _dp form reads the parameter block of phmm_mixdom2_param_block
+ * from device memory (capturable, as phmm_mixdom2_tables_dp). */
+int phmm_mixdom2_nest(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t, float *nest, void *stream);
+int phmm_mixdom2_nest_dp(const void *param_block, int32_t n_dom, int32_t n_frag, int32_t n_classes,
+                         int32_t n_pairs, const double *t, float *nest, void *stream);
+/* 1 when the E-step kernels have a factored instantiation for the MixDom
+ * layout (n_dom, n_frag) (otherwise a batch's nest record is ignored). */
+int phmm_nest_supported(int32_t n_dom, int32_t n_frag);
 
 /* The collapsed chi alone (float32 and, when chi64 is not null, float64
  * [P][N][N]) for the gradient path, and its vector-Jacobian product:

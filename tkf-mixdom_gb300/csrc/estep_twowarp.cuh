@@ -26,25 +26,111 @@ struct SmemTW {
     int bnd;        // float offset: boundary slots [2][SP]
     int bndE;       // int offset: boundary exponents [2]
     int flag;       // int offset: [0], [1] abort flags by step parity, [2] popped item
+    int nest;       // float offset: factored MixDom transition coefficients (NestSlots), or -1
     int bytes;
 };
 
-__host__ __device__ inline SmemTW make_smem_tw(int SP, int KP, int NI, int G, int max_ly, bool bwd) {
+__host__ __device__ inline SmemTW make_smem_tw(int SP, int KP, int NI, int G, int max_ly, bool bwd,
+                                               int nest_floats = 0) {
     SmemTW L;
     L.w = make_smem_w(SP, KP, NI, G, max_ly, bwd, false);
     int o = L.w.bytes / 4;   // L.w.bytes is a multiple of 16
     L.bnd = o; o += 2 * SP;
     L.bndE = o; o += 4;
     L.flag = o; o += 4;
+    L.nest = -1;
+    if (nest_floats > 0) { L.nest = o; o += al4(nest_floats); }   // o stays a multiple of 4
     L.bytes = o * 4;
     return L;
 }
 
+// ---------------------------------------------------------------- factored (nested) transitions
+// The collapsed MixDom chi (models/mixdom.py:252-423) is, between body
+// states, chi[s][k] = exit[s] T_exit_k[d_k][U(s)][U(k)] dest[k] plus a
+// same-domain block: the inter-domain part factors through the three
+// top-level types U in {M, I, D} (MM, MI, MD -> M; II -> I; DD -> D), and
+// within a domain the M-block couples MM, MI, MD (3F x 3F) while II and DD
+// couple only among their own fragments (F x F).  With cin[a][k] = dest[k]
+// T_exit_k[d_k][a][U(k)] a destination's sum over all sources becomes
+//   sum_s f[s] chi[s][k] = sum_a cin[a][k] G_a + sum_{s in block(k)} f[s] intra[s][k],
+//   G_a = sum_{s: U(s) = a} exit[s] f[s],
+// 3 + 3F (or 3 + F) multiply-adds instead of N, plus the three G sums per
+// cell; the backward recursion is the transpose.  NoNest keeps the dense
+// contraction (any chi); Nest<K, F> is the MixDom layout with K domains and
+// F fragments, in the two-warp slot order (M states, then I, then D, each in
+// state order: MM_df; MI_df, II_df per domain; MD_df, DD_df per domain).
+struct NoNest { static constexpr int K = 0, F = 0; };
+template <int K_, int F_> struct Nest { static constexpr int K = K_, F = F_; };
+
+template <class SH, class NT>
+struct NestSlots {
+    static constexpr int K = NT::K, F = NT::F, NM = SH::NM, NI = SH::NI, NE = SH::NE;
+    static_assert(NM == K * F && NI == 2 * K * F && SH::ND == 2 * K * F, "nested slots need the MixDom shape");
+    static constexpr int IS = (3 * F + 3) & ~3;   // intra row stride (floats)
+    __host__ __device__ static constexpr int dom(int s) {
+        return s < NM ? s / F : (s < NM + NI ? (s - NM) / (2 * F) : (s - NM - NI) / (2 * F));
+    }
+    __host__ __device__ static constexpr int uv(int s) {   // 0 MM, 1 MI, 2 MD, 3 II, 4 DD
+        return s < NM ? 0 : (s < NM + NI ? (((s - NM) % (2 * F)) < F ? 1 : 3) : (((s - NM - NI) % (2 * F)) < F ? 2 : 4));
+    }
+    __host__ __device__ static constexpr int frag(int s) {
+        return s < NM ? s % F : (s < NM + NI ? ((s - NM) % (2 * F)) % F : ((s - NM - NI) % (2 * F)) % F);
+    }
+    __host__ __device__ static constexpr int U(int s) { return uv(s) < 3 ? 0 : uv(s) - 2; }   // 0 M, 1 I, 2 D
+    __host__ __device__ static constexpr int slot(int d, int u, int f) {
+        return u == 0 ? d * F + f
+                      : (u == 1 ? NM + d * 2 * F + f
+                                : (u == 3 ? NM + d * 2 * F + F + f
+                                          : (u == 2 ? NM + NI + d * 2 * F + f : NM + NI + d * 2 * F + F + f)));
+    }
+    __host__ __device__ static constexpr int n_intra(int s) { return uv(s) < 3 ? 3 * F : F; }
+    // the j-th same-block partner of slot s (a source of destination s in the
+    // forward, a destination of source s in the backward)
+    __host__ __device__ static constexpr int partner(int s, int j) {
+        return uv(s) < 3 ? slot(dom(s), j / F, j % F) : slot(dom(s), uv(s), j);
+    }
+    __host__ __device__ static constexpr int local(int s) { return uv(s) * F + frag(s); }   // index in the domain block
+    __host__ __device__ static constexpr int body(int s) { return dom(s) * 5 * F + local(s); }   // state - 2
+    // shared-memory region (floats): exit[SP], cin[3][KP], chi0[KP] (start -> k), intra rows [NE][IS]
+    static constexpr int OX = 0, OC = SH::SP, O0 = OC + 3 * SH::KP, OI = O0 + SH::KP;
+    static constexpr int FLOATS = OI + NE * IS;
+};
+
+// Load the factored coefficients of pair p (record in state order, see
+// include/pairhmm.h phmm_batch.nest) into the slot-ordered shared region; one
+// warp.  BWD: intra rows by source (partners = destinations), else by destination.
+template <class SH, class NT, bool BWD>
+__device__ void load_nest_tw(const KParams &P, int p, float *nz) {
+    using NS = NestSlots<SH, NT>;
+    constexpr int K = NT::K, F = NT::F, nb = 5 * K * F, bs = 5 * F;
+    const int lane = threadIdx.x & 31;
+    const float *rec = P.nest + (int64_t)p * P.nest_stride;
+    const float *chi = P.chi + (int64_t)p * P.chi_stride;
+    for (int s = lane; s < SH::SP; s += 32) nz[NS::OX + s] = s < NS::NE ? __ldg(rec + NS::body(s)) : 0.f;
+    for (int idx = lane; idx < 3 * SH::KP; idx += 32) {
+        const int a = idx / SH::KP, k = idx % SH::KP;
+        nz[NS::OC + idx] = k < NS::NE ? __ldg(rec + nb + a * nb + NS::body(k)) : 0.f;
+    }
+    for (int k = lane; k < SH::KP; k += 32) nz[NS::O0 + k] = k < NS::NE ? __ldg(chi + P.w_orig[k]) : 0.f;
+    for (int idx = lane; idx < NS::NE * NS::IS; idx += 32) {
+        const int s = idx / NS::IS, j = idx % NS::IS;
+        float v = 0.f;
+        if (j < NS::n_intra(s)) {
+            const int q = NS::partner(s, j);
+            const int row = BWD ? NS::local(s) : NS::local(q), col = BWD ? NS::local(q) : NS::local(s);
+            v = __ldg(rec + 4 * nb + NS::dom(s) * bs * bs + row * bs + col);
+        }
+        nz[NS::OI + idx] = v;
+    }
+}
+
 // MK: the batch carries a cell mask (a separate instantiation, so the
 // unmasked recursion carries none of the mask's instructions)
-template <class SH, bool MK>
+// NT: NoNest (dense chi) or Nest<K, F> (factored MixDom transitions, unmasked batches)
+template <class SH, bool MK, class NT = NoNest>
 __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT, float *sm,
                               unsigned char *smb) {
+    static_assert(NT::K == 0 || !MK, "the factored contraction runs on unmasked batches");
     constexpr int NE = SH::NE, NSRC = SH::NSRC, SP = SH::SP, KP = SH::KP, NM = SH::NM, NI = SH::NI;
     const SmemW &L = LT.w;
     const PairMeta m = P.meta[p];
@@ -65,6 +151,9 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
     volatile int *s_abort = reinterpret_cast<int *>(sm) + LT.flag;
 
     if (r < 32) load_model_w<SH>(P, p, m, L, sm, smb, CHI_FWD_PAIRS);
+    if constexpr (NT::K > 0) {
+        if (r >= 32) load_nest_tw<SH, NT, false>(P, p, sm + LT.nest);
+    }
     if (r < 2 * SP) bnd[r] = 0.f;
     if (r < 2) bndE[r] = EXP_NONE;
     if (r < 2) s_abort[r] = 0;
@@ -89,6 +178,9 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
     constexpr int SQ = SP / 2;
     float2 prev[SQ], d0[SQ], m0[SQ];
     int Eprev = EXP_NONE, Em0 = EXP_NONE;
+    // factored contraction: the type sums G_a of the M- and I-predecessors
+    // (carried from earlier steps: G(m0) is the previous step's G(d0))
+    float Gm[3] = {0.f, 0.f, 0.f}, Gp[3] = {0.f, 0.f, 0.f}, Gd[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < SQ; ++q) {
         prev[q] = make_float2(0.f, 0.f); d0[q] = make_float2(0.f, 0.f); m0[q] = make_float2(0.f, 0.f);
@@ -203,31 +295,91 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
         const bool hasM = valid && jc >= 1 && rowi >= 1 && (mbx & 1);
         const int EI = hasI ? Eprev : EXP_NONE, ED = hasD ? EdA : EXP_NONE, EM = hasM ? Em0 : EXP_NONE;
         const int Eref = max(max(EI, ED), EM);
-        float2 acc2[NE];
+        float acc[NE];
+        if constexpr (NT::K > 0) {
+            using NS = NestSlots<SH, NT>;
+            const float *nz = sm + LT.nest;
+            const float4 *nx4 = reinterpret_cast<const float4 *>(nz + NS::OX);
+            const float4 *nc4 = reinterpret_cast<const float4 *>(nz + NS::OC);
+            const float4 *ni4 = reinterpret_cast<const float4 *>(nz + NS::OI);
+            auto comp = [](const float4 &v, int u) { return u == 0 ? v.x : (u == 1 ? v.y : (u == 2 ? v.z : v.w)); };
+            auto elem = [](const float2 (&v)[SQ], int s) { return (s & 1) ? v[s >> 1].y : v[s >> 1].x; };
+            // G of the D-predecessor just received
+            Gd[0] = Gd[1] = Gd[2] = 0.f;
 #pragma unroll
-        for (int k = 0; k < NE; ++k) acc2[k] = make_float2(0.f, 0.f);
+            for (int s4 = 0; s4 < SP / 4; ++s4) {
+                const float4 ex = nx4[s4];
 #pragma unroll
-        for (int q = 0; q < SQ; ++q) {
-            if (2 * q >= NSRC) continue;
-            const float4 *row = chi4 + q * (KP / 2);   // sources 2q, 2q+1 for all destinations
+                for (int u = 0; u < 4; ++u) {
+                    const int s = 4 * s4 + u;
+                    if (s < NE) Gd[NS::U(s)] = fmaf(comp(ex, u), elem(d0, s), Gd[NS::U(s)]);
+                }
+            }
 #pragma unroll
-            for (int kp = 0; kp < KP / 2; ++kp) {
-                const float4 cv = row[kp];             // (k, k+1) x (2q, 2q+1)
+            for (int k4 = 0; k4 < KP / 4; ++k4) {
+                const float4 c0 = nc4[k4], c1 = nc4[KP / 4 + k4], c2 = nc4[2 * (KP / 4) + k4];
 #pragma unroll
-                for (int u = 0; u < 2; ++u) {
-                    const int k = 2 * kp + u;
-                    if (k < NE) {
-                        const int ty = SH::type_of(k);
-                        const float2 pk = ty == T_M ? m0[q] : (ty == T_I ? prev[q] : d0[q]);
-                        acc2[k] = __ffma2_rn(pk, u == 0 ? make_float2(cv.x, cv.y) : make_float2(cv.z, cv.w),
-                                             acc2[k]);
+                for (int u = 0; u < 4; ++u) {
+                    const int k = 4 * k4 + u;
+                    if (k >= NE) continue;
+                    const int ty = SH::type_of(k);
+                    const float g0 = ty == T_M ? Gm[0] : (ty == T_I ? Gp[0] : Gd[0]);
+                    const float g1 = ty == T_M ? Gm[1] : (ty == T_I ? Gp[1] : Gd[1]);
+                    const float g2 = ty == T_M ? Gm[2] : (ty == T_I ? Gp[2] : Gd[2]);
+                    float a = comp(c0, u) * g0;
+                    a = fmaf(comp(c1, u), g1, a);
+                    a = fmaf(comp(c2, u), g2, a);
+#pragma unroll
+                    for (int j4 = 0; j4 < NS::IS / 4; ++j4) {
+                        const float4 cv = ni4[k * (NS::IS / 4) + j4];
+#pragma unroll
+                        for (int v = 0; v < 4; ++v) {
+                            const int j = 4 * j4 + v;
+                            if (j < NS::n_intra(k)) {
+                                const int sj = NS::partner(k, j);
+                                const float pv = ty == T_M ? elem(m0, sj) : (ty == T_I ? elem(prev, sj) : elem(d0, sj));
+                                a = fmaf(comp(cv, v), pv, a);
+                            }
+                        }
+                    }
+                    acc[k] = a;
+                }
+            }
+            // the start state is non-zero only at the origin: the cells next to it
+            const float stm = elem(m0, NE), stp = elem(prev, NE), std_ = elem(d0, NE);
+            if (__any_sync(0xffffffffu, stm != 0.f || stp != 0.f || std_ != 0.f)) {
+#pragma unroll
+                for (int k = 0; k < NE; ++k) {
+                    const int ty = SH::type_of(k);
+                    acc[k] = fmaf(nz[NS::O0 + k], ty == T_M ? stm : (ty == T_I ? stp : std_), acc[k]);
+                }
+            }
+        } else {
+            float2 acc2[NE];
+#pragma unroll
+            for (int k = 0; k < NE; ++k) acc2[k] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < SQ; ++q) {
+                if (2 * q >= NSRC) continue;
+                const float4 *row = chi4 + q * (KP / 2);   // sources 2q, 2q+1 for all destinations
+#pragma unroll
+                for (int kp = 0; kp < KP / 2; ++kp) {
+                    const float4 cv = row[kp];             // (k, k+1) x (2q, 2q+1)
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const int k = 2 * kp + u;
+                        if (k < NE) {
+                            const int ty = SH::type_of(k);
+                            const float2 pk = ty == T_M ? m0[q] : (ty == T_I ? prev[q] : d0[q]);
+                            acc2[k] = __ffma2_rn(pk, u == 0 ? make_float2(cv.x, cv.y) : make_float2(cv.z, cv.w),
+                                                 acc2[k]);
+                        }
                     }
                 }
             }
-        }
-        float acc[NE];
 #pragma unroll
-        for (int k = 0; k < NE; ++k) acc[k] = acc2[k].x + acc2[k].y;
+            for (int k = 0; k < NE; ++k) acc[k] = acc2[k].x + acc2[k].y;
+        }
         // emissions, type scales, per-cell renormalisation
         const float sM = hasM ? pow2f(EM - Eref) : 0.f, sI = hasI ? pow2f(EI - Eref) : 0.f;
         const float sD = hasD ? pow2f(ED - Eref) : 0.f;
@@ -313,6 +465,15 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
             prev[q].x = s0 < NE ? acc[s0] : (s0 == NE ? sNew : 0.f);
             prev[q].y = s1 < NE ? acc[s1] : (s1 == NE ? sNew : 0.f);
         }
+        if constexpr (NT::K > 0) {   // G of the new cell (the next step's I-predecessor)
+            using NS = NestSlots<SH, NT>;
+            const float *nz = sm + LT.nest;
+            float g[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int s = 0; s < NE; ++s) g[NS::U(s)] = fmaf(nz[NS::OX + s], acc[s], g[NS::U(s)]);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) { Gm[a] = Gd[a]; Gp[a] = g[a]; }
+        }
         Em0 = EdA;
         Eprev = Enew;
         // row 31 hands its new state to row 32 for step t+1
@@ -361,9 +522,10 @@ __device__ void fwd_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT,
     if (r == 0) st_release(prog_mine, Ly + 2);
 }
 
-template <class SH, bool MK>
+template <class SH, bool MK, class NT = NoNest>
 __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW &LT, float *sm,
                                   unsigned char *smb) {
+    static_assert(NT::K == 0 || !MK, "the factored contraction runs on unmasked batches");
     constexpr int NE = SH::NE, NSRC = SH::NSRC, SP = SH::SP, KP = SH::KP, NM = SH::NM, NI = SH::NI;
     const SmemW &L = LT.w;
     const PairMeta m = P.meta[p];
@@ -385,6 +547,9 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
     volatile int *s_abort = reinterpret_cast<int *>(sm) + LT.flag;
 
     if (r < 32) load_model_w<SH>(P, p, m, L, sm, smb, CHI_BWD_PAIRS);
+    if constexpr (NT::K > 0) {
+        if (r >= 32) load_nest_tw<SH, NT, true>(P, p, sm + LT.nest);
+    }
     if (r < 2 * SP) bnd[r] = 0.f;
     if (r < 2) bndE[r] = EXP_NONE;
     if (r < 2) s_abort[r] = 0;
@@ -549,24 +714,77 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
             }
             w2[q] = make_float2(wv[0], wv[1]);
         }
-        float2 acc2[NSRC];
-#pragma unroll
-        for (int s2 = 0; s2 < NSRC; ++s2) acc2[s2] = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int q = 0; q < KQ; ++q) {
-            if (2 * q >= NE) continue;
-            const float4 *row = chiB4 + q * (SP / 2);   // destinations 2q, 2q+1 for all sources
-#pragma unroll
-            for (int sp = 0; sp < SP / 2; ++sp) {
-                const float4 cv = row[sp];             // (2q, 2q+1) x (s, s+1)
-                if (2 * sp < NSRC) acc2[2 * sp] = __ffma2_rn(w2[q], make_float2(cv.x, cv.y), acc2[2 * sp]);
-                if (2 * sp + 1 < NSRC)
-                    acc2[2 * sp + 1] = __ffma2_rn(w2[q], make_float2(cv.z, cv.w), acc2[2 * sp + 1]);
-            }
-        }
         float acc[NSRC];
+        if constexpr (NT::K > 0) {
+            using NS = NestSlots<SH, NT>;
+            const float *nz = sm + LT.nest;
+            const float4 *nx4 = reinterpret_cast<const float4 *>(nz + NS::OX);
+            const float4 *nc4 = reinterpret_cast<const float4 *>(nz + NS::OC);
+            const float4 *ni4 = reinterpret_cast<const float4 *>(nz + NS::OI);
+            auto comp = [](const float4 &v, int u) { return u == 0 ? v.x : (u == 1 ? v.y : (u == 2 ? v.z : v.w)); };
+            auto wv = [&](int k) { return (k & 1) ? w2[k >> 1].y : w2[k >> 1].x; };
+            // the type sums over destinations, Gb_a = sum_k cin[a][k] w_k
+            float Gb[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-        for (int s2 = 0; s2 < NSRC; ++s2) acc[s2] = acc2[s2].x + acc2[s2].y;
+            for (int k4 = 0; k4 < KP / 4; ++k4) {
+                const float4 c0 = nc4[k4], c1 = nc4[KP / 4 + k4], c2 = nc4[2 * (KP / 4) + k4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int k = 4 * k4 + u;
+                    if (k >= NE) continue;
+                    Gb[0] = fmaf(comp(c0, u), wv(k), Gb[0]);
+                    Gb[1] = fmaf(comp(c1, u), wv(k), Gb[1]);
+                    Gb[2] = fmaf(comp(c2, u), wv(k), Gb[2]);
+                }
+            }
+#pragma unroll
+            for (int s4 = 0; s4 < SP / 4; ++s4) {
+                const float4 ex = nx4[s4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int sidx = 4 * s4 + u;
+                    if (sidx >= NE) continue;
+                    float a = comp(ex, u) * Gb[NS::U(sidx)];
+#pragma unroll
+                    for (int j4 = 0; j4 < NS::IS / 4; ++j4) {
+                        const float4 cv = ni4[sidx * (NS::IS / 4) + j4];
+#pragma unroll
+                        for (int v = 0; v < 4; ++v) {
+                            const int j = 4 * j4 + v;
+                            if (j < NS::n_intra(sidx)) a = fmaf(comp(cv, v), wv(NS::partner(sidx, j)), a);
+                        }
+                    }
+                    acc[sidx] = a;
+                }
+            }
+            // the start state's backward value matters only at the origin
+            acc[NE] = 0.f;
+            const bool origin = valid && rowi == 0 && jc == 0;
+            if (__any_sync(0xffffffffu, origin)) {
+                float a = 0.f;
+#pragma unroll
+                for (int k = 0; k < NE; ++k) a = fmaf(nz[NS::O0 + k], wv(k), a);
+                if (origin) acc[NE] = a;
+            }
+        } else {
+            float2 acc2[NSRC];
+#pragma unroll
+            for (int s2 = 0; s2 < NSRC; ++s2) acc2[s2] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < KQ; ++q) {
+                if (2 * q >= NE) continue;
+                const float4 *row = chiB4 + q * (SP / 2);   // destinations 2q, 2q+1 for all sources
+#pragma unroll
+                for (int sp = 0; sp < SP / 2; ++sp) {
+                    const float4 cv = row[sp];             // (2q, 2q+1) x (s, s+1)
+                    if (2 * sp < NSRC) acc2[2 * sp] = __ffma2_rn(w2[q], make_float2(cv.x, cv.y), acc2[2 * sp]);
+                    if (2 * sp + 1 < NSRC)
+                        acc2[2 * sp + 1] = __ffma2_rn(w2[q], make_float2(cv.z, cv.w), acc2[2 * sp + 1]);
+                }
+            }
+#pragma unroll
+            for (int s2 = 0; s2 < NSRC; ++s2) acc[s2] = acc2[s2].x + acc2[s2].y;
+        }
         if (term) {
 #pragma unroll
             for (int s = 0; s < NSRC; ++s) acc[s] = sm[L.chiE + s];
@@ -691,11 +909,13 @@ __device__ void bwd_rec_stripe_tw(const KParams &P, int p, int si, const SmemTW 
 
 // Persistent two-warp CTAs popping stripe items (forward: kind 5; backward
 // recursion: kind 6).
-template <class SH, bool BWD, bool MK>
+template <class SH, bool BWD, bool MK, class NT = NoNest>
 __global__ void __launch_bounds__(TWT) stripe_tw_kernel(const KParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *sm = reinterpret_cast<float *>(smem_raw);
-    const SmemTW L = make_smem_tw(SH::SP, SH::KP, SH::NI, P.G, P.max_ly, BWD);
+    int nest_floats = 0;
+    if constexpr (NT::K > 0) nest_floats = NestSlots<SH, NT>::FLOATS;
+    const SmemTW L = make_smem_tw(SH::SP, SH::KP, SH::NI, P.G, P.max_ly, BWD, nest_floats);
     int *s_item = reinterpret_cast<int *>(sm) + L.flag + 2;
     for (;;) {
         if (threadIdx.x == 0) *s_item = atomicAdd(P.counter, 1);
@@ -703,8 +923,8 @@ __global__ void __launch_bounds__(TWT) stripe_tw_kernel(const KParams P) {
         const int it = *s_item;
         if (it >= P.n_items) break;
         const int2 w = P.items[it];
-        if (BWD) bwd_rec_stripe_tw<SH, MK>(P, w.x, w.y, L, sm, smem_raw);
-        else fwd_stripe_tw<SH, MK>(P, w.x, w.y, L, sm, smem_raw);
+        if (BWD) bwd_rec_stripe_tw<SH, MK, NT>(P, w.x, w.y, L, sm, smem_raw);
+        else fwd_stripe_tw<SH, MK, NT>(P, w.x, w.y, L, sm, smem_raw);
     }
 }
 

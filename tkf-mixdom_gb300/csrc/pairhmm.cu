@@ -117,6 +117,11 @@ struct KParams {
     int recompute;                      // 1: stripes recomputed from complete edge rows (no waits, no
                                         // edge / progress / log-likelihood writes)
     int ckpt;                           // count pass: row 0 of the stripe below from its backward edge row
+    // factored MixDom transitions (phmm_batch.nest), or null: the two-warp
+    // stripes of a shape with a nested instantiation contract through them
+    const float *nest;
+    int64_t nest_stride;
+    int nest_K, nest_F;
 };
 
 struct SmemLayout {
@@ -1123,6 +1128,33 @@ WarpLauncher find_warp_launcher(int nm, int ni, int nd) {
     return nullptr;
 }
 
+// ---- factored MixDom transitions (phmm_batch.nest)
+int64_t nest_record_len(int K, int F) { return 20LL * K * F + 25LL * K * F * F; }
+
+// (K, F) layouts with a nested instantiation of the two-warp stripes
+bool has_nest_tw(int nm, int K, int F) { return nm == 3 && K == 3 && F == 1; }
+
+// the record must describe the plan's state space, and the plan's two-warp
+// slot order must be the canonical MixDom order the nested kernels assume
+// (M states, then I, then D, each in state order)
+int check_nest(const phmm_plan *plan, const phmm_batch *b) {
+    const int K = b->nest_dom, F = b->nest_frag;
+    if (K < 1 || F < 1 || plan->base.N != 2 + 5 * K * F || plan->w_nm != K * F || plan->w_ni != 2 * K * F ||
+        plan->w_nd != 2 * K * F)
+        return fail(PHMM_E_ARG, "phmm_batch.nest: nest_dom / nest_frag do not match the plan's MixDom state space");
+    const int NM = K * F, NI = 2 * K * F, NE = 5 * K * F;
+    for (int s = 0; s < NE; ++s) {
+        int d, u, f;
+        if (s < NM) { d = s / F; u = 0; f = s % F; }
+        else if (s < NM + NI) { const int w = (s - NM) % (2 * F); d = (s - NM) / (2 * F); u = w < F ? 1 : 3; f = w % F; }
+        else { const int w = (s - NM - NI) % (2 * F); d = (s - NM - NI) / (2 * F); u = w < F ? 2 : 4; f = w % F; }
+        if (plan->base.w_orig[s] != 2 + d * 5 * F + u * F + f)
+            return fail(PHMM_E_ARG, "phmm_batch.nest: the plan's state types are not the MixDom layout "
+                                    "(state 2 + d*5F + uv*F + f)");
+    }
+    return 0;
+}
+
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // The split E-step: forward on the caller's stream and backward recursion on
@@ -1703,6 +1735,13 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         plan->last_variant = two_warp ? 7 : (bl ? (split ? 5 : 3) : (split ? 4 : (wl ? 2 : 1)));
         plan->two_warp = two_warp;
     }
+    // factored transitions: checked against the plan's state space; used by
+    // the two-warp stripes (unmasked) where the shape has an instantiation
+    if (b->nest) {
+        const int rc = check_nest(plan, b);
+        if (rc) return rc;
+    }
+    const bool use_nest = b->nest && two_warp && !masked && !beam && has_nest_tw(plan->w_nm, b->nest_dom, b->nest_frag);
     // ---- plan: stripes, offsets, longest-first order
     std::vector<int> order(P_);
     for (int p = 0; p < P_; ++p) {
@@ -1887,6 +1926,12 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     K.n_items = n_items;
     K.chi = b->chi;
     K.chi_stride = b->chi_per_pair ? (int64_t)N * N : 0;
+    if (use_nest) {
+        K.nest = b->nest;
+        K.nest_stride = b->chi_per_pair ? nest_record_len(b->nest_dom, b->nest_frag) : 0;
+        K.nest_K = b->nest_dom;
+        K.nest_F = b->nest_frag;
+    }
     K.eM = b->emit_M;
     K.eI = b->emit_I;
     K.eD = b->emit_D;
@@ -2009,6 +2054,21 @@ int launch_block(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind,
     return 0;
 }
 
+// the nested two-warp stripe kernel of shape SH for the MixDom layout (K, F),
+// with its shared-memory coefficient floats, or null where none is compiled
+template <class SH>
+void (*nest_tw_kernel(bool bwd, int K, int F, int &floats))(const KParams) {
+    if constexpr (SH::NM == 3 && SH::NI == 6 && SH::ND == 6) {
+        if (K == 3 && F == 1) {
+            using NT = warp2::Nest<3, 1>;
+            floats = warp2::NestSlots<SH, NT>::FLOATS;
+            return bwd ? warp2::stripe_tw_kernel<SH, true, false, NT> : warp2::stripe_tw_kernel<SH, false, false, NT>;
+        }
+    }
+    floats = 0;
+    return nullptr;
+}
+
 template <class SH>
 int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, cudaStream_t stream) {
     void (*kern)(const KParams) = nullptr;
@@ -2021,9 +2081,15 @@ int launch_warp(phmm_plan *plan, KParams &K, int n_items, int max_ly, int kind, 
         bytes = warp2::make_smem_c(SH::SP, SH::KP, SH::NI, K.G, max_ly).bytes;
         kern = warp2::count_warp_kernel<SH>;
     } else if (kind == 5 || kind == 6) {   // two-warp stripes: forward / backward recursion
-        bytes = warp2::make_smem_tw(SH::SP, SH::KP, SH::NI, K.G, max_ly, kind == 6).bytes;
-        if (K.cmask) kern = kind == 5 ? warp2::stripe_tw_kernel<SH, false, true> : warp2::stripe_tw_kernel<SH, true, true>;
-        else kern = kind == 5 ? warp2::stripe_tw_kernel<SH, false, false> : warp2::stripe_tw_kernel<SH, true, false>;
+        int nest_floats = 0;
+        if (K.nest) kern = nest_tw_kernel<SH>(kind == 6, K.nest_K, K.nest_F, nest_floats);
+        bytes = warp2::make_smem_tw(SH::SP, SH::KP, SH::NI, K.G, max_ly, kind == 6, nest_floats).bytes;
+        if (kern) {
+        } else if (K.cmask) {
+            kern = kind == 5 ? warp2::stripe_tw_kernel<SH, false, true> : warp2::stripe_tw_kernel<SH, true, true>;
+        } else {
+            kern = kind == 5 ? warp2::stripe_tw_kernel<SH, false, false> : warp2::stripe_tw_kernel<SH, true, false>;
+        }
         threads = warp2::TWT;
     } else {
         bytes = warp2::make_smem_w(SH::SP, SH::KP, SH::NI, K.G, max_ly, kind != 0, kind == 1).bytes;
@@ -2081,6 +2147,7 @@ int run_groups(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, dou
             g.x_off_host = b->x_off_host + p0;
             g.y_off_host = b->y_off_host + p0;
             g.chi = b->chi + (b->chi_per_pair ? (int64_t)p0 * N * N : 0);
+            if (b->nest) g.nest = b->nest + (b->chi_per_pair ? (int64_t)p0 * nest_record_len(b->nest_dom, b->nest_frag) : 0);
             g.emit_M = b->emit_M + (b->emit_per_pair ? (int64_t)p0 * G * 441 : 0);
             g.emit_I = b->emit_I + (b->emit_per_pair ? (int64_t)p0 * G * 21 : 0);
             g.emit_D = b->emit_D + (b->emit_per_pair ? (int64_t)p0 * G * 21 : 0);
@@ -2138,6 +2205,10 @@ int phmm_last_error(char *buf, size_t len) {
         buf[n] = 0;
     }
     return (int)g_err.size();
+}
+
+int phmm_nest_supported(int32_t n_dom, int32_t n_frag) {
+    return has_nest_tw(n_dom * n_frag, n_dom, n_frag) ? 1 : 0;
 }
 
 int phmm_plan_create(const phmm_model_desc *md, phmm_plan **out) {

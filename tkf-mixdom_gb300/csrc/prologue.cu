@@ -316,8 +316,44 @@ __device__ void build_chi(const ChiParams<T> &cp, int K, int F, int N, ChiSmem<T
     }
 }
 
+// The factored form of chi (models/mixdom.py:343-394) from the builder's
+// intermediate results (after build_chi): per body state q = d*5F + j*F + f,
+// exit[q] = notext[d,f] exi[d,j]; cin[a][q] = T_exit_k[d][a][U(j)] dest[q]
+// for the top-level types a = M, I, D; and each domain's same-domain block
+// without its inter part, intra[d][j'F+f'][jF+f] (the M-block couples the
+// sub-states MM, MI, MD; II and DD couple within themselves).  Layout of
+// phmm_batch.nest: exit [nb], cin [3][nb], intra [K][5F][5F].
+template <class T>
+__device__ void write_nest(const ChiParams<T> &cp, int K, int F, const ChiSmem<T> &sm, float *rec) {
+    const int nb = 5 * K * F, bs = 5 * F;
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+        const int k = q / bs, j = (q % bs) / F, f = q % F;
+        T notext = cst<T>(1.0);
+        for (int g = 0; g < F; ++g) notext = notext - cp.ext[(k * F + f) * F + g];
+        rec[q] = (float)(notext * sm.exi[5 * k + j]);
+        const T dest = cp.fw[k * F + f] * sm.ent[5 * k + j];
+        for (int a = 0; a < 3; ++a) rec[nb + a * nb + q] = (float)(sm.Tex[25 * k + MID[a] * 5 + UV_U[j]] * dest);
+    }
+    for (int idx = threadIdx.x; idx < K * bs * bs; idx += blockDim.x) {
+        const int k = idx / (bs * bs), i = (idx / bs) % bs, c = idx % bs;
+        const int jp = i / F, fp = i % F, jq = c / F, fq = c % F;
+        T v = cst<T>(0.0);
+        if ((jp < 3 && jq < 3) || jp == jq) {
+            T notext = cst<T>(1.0);
+            for (int g = 0; g < F; ++g) notext = notext - cp.ext[(k * F + fp) * F + g];
+            const T e = cp.ext[(k * F + fp) * F + fq];
+            if (jp < 3 && jq < 3)
+                v = notext * sm.tauK[25 * k + MID[jp] * 5 + MID[jq]] * cp.fw[k * F + fq] + (jp == jq ? e : cst<T>(0.0));
+            else
+                v = notext * sm.kap[k] * cp.fw[k * F + fq] + e;
+        }
+        rec[4 * nb + idx] = (float)v;
+    }
+}
+
+// chi (nullable), its float64 copy (nullable) and the factored record (nullable) of pair blockIdx.x
 __device__ __forceinline__ void chi_kernel_body(const Packed &prm, const double *__restrict__ ts, int N, float *__restrict__ chi,
-           double *__restrict__ chi64) {
+           double *__restrict__ chi64, float *__restrict__ nest = nullptr) {
     extern __shared__ double smem_d[];
     __shared__ int piv_row;
     const int p = blockIdx.x;
@@ -325,12 +361,27 @@ __device__ __forceinline__ void chi_kernel_body(const Packed &prm, const double 
     sm.carve(smem_d, prm.K);
     const ChiParams<double> cp{prm.main_ins, prm.main_del, ts[p], prm.v + prm.o_dins, prm.v + prm.o_ddel,
                                prm.v + prm.o_dw, prm.v + prm.o_fw, prm.v + prm.o_ext};
-    float *out = chi + (size_t)p * N * N;
+    float *out = chi ? chi + (size_t)p * N * N : nullptr;
     double *out64 = chi64 ? chi64 + (size_t)p * N * N : nullptr;
     build_chi(cp, prm.K, prm.F, N, sm, &piv_row, [&](int idx, double v) {
-        out[idx] = (float)v;
+        if (out) out[idx] = (float)v;
         if (out64) out64[idx] = v;
     });
+    if (nest) {
+        __syncthreads();
+        const int K = prm.K, F = prm.F;
+        write_nest(cp, K, F, sm, nest + (size_t)p * (20 * K * F + 25 * K * F * F));
+    }
+}
+
+__global__ void __launch_bounds__(THREADS)
+nest_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, int N, float *__restrict__ nest) {
+    chi_kernel_body(prm, ts, N, nullptr, nullptr, nest);
+}
+
+__global__ void __launch_bounds__(THREADS)
+nest_kernel_dp(const Packed *__restrict__ prm, const double *__restrict__ ts, int N, float *__restrict__ nest) {
+    chi_kernel_body(*prm, ts, N, nullptr, nullptr, nest);
 }
 
 __global__ void __launch_bounds__(THREADS)
@@ -1134,6 +1185,48 @@ extern "C" int phmm_mixdom2_tables_dp(const void *param_block, int32_t n_dom, in
     chi_kernel_dp<<<n_pairs, THREADS, chi_smem, st>>>(pk, t, N, chi, nullptr);
     expm_kernel_dp<<<n_pairs * C, THREADS, 0, st>>>(pk, t, class_subs);
     tables_kernel_dp<<<n_pairs, THREADS, 0, st>>>(pk, class_subs, emit_M, emit_I, emit_D);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    return PHMM_OK;
+}
+
+extern "C" int phmm_mixdom2_nest(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t, float *nest,
+                                 void *stream) {
+    using namespace pro;
+    Packed pk;
+    int rc = pack_params(prm, pk, "phmm_mixdom2_nest");
+    if (rc) return rc;
+    if (n_pairs < 0) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_nest: negative n_pairs");
+    if (n_pairs == 0) return PHMM_OK;
+    if (!t || !nest) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_nest: null device buffer");
+    const int N = 2 + 5 * pk.K * pk.F;
+    const size_t chi_smem = sizeof(double) * ChiSmem<double>::elems(pk.K);
+    if (chi_smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(nest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chi_smem);
+        if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    }
+    nest_kernel<<<n_pairs, THREADS, chi_smem, (cudaStream_t)stream>>>(pk, t, N, nest);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    return PHMM_OK;
+}
+
+extern "C" int phmm_mixdom2_nest_dp(const void *param_block, int32_t n_dom, int32_t n_frag, int32_t n_classes,
+                                    int32_t n_pairs, const double *t, float *nest, void *stream) {
+    using namespace pro;
+    const int K = n_dom, F = n_frag, C = n_classes;
+    if (K < 1 || F < 1 || C < 1 || K * F > MAXK || n_pairs < 0)
+        return pro_fail(PHMM_E_ARG, "phmm_mixdom2_nest_dp: bad shape");
+    if (n_pairs == 0) return PHMM_OK;
+    if (!param_block || !t || !nest) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_nest_dp: null device buffer");
+    const Packed *pk = reinterpret_cast<const Packed *>(param_block);
+    const int N = 2 + 5 * K * F;
+    const size_t chi_smem = sizeof(double) * ChiSmem<double>::elems(K);
+    if (chi_smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(nest_kernel_dp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chi_smem);
+        if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
+    }
+    nest_kernel_dp<<<n_pairs, THREADS, chi_smem, (cudaStream_t)stream>>>(pk, t, N, nest);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
     return PHMM_OK;

@@ -29,7 +29,8 @@ EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep'
            'phmm_sample_workspace_bytes', 'phmm_sample_paths', 'phmm_pairs_count', 'phmm_pairs_decode',
            'phmm_estep_ws_prepare', 'phmm_estep_ws_launch', 'phmm_mixdom2_param_block_bytes',
            'phmm_mixdom2_param_block', 'phmm_mixdom2_tables_dp', 'phmm_mixdom2_class_counts_dp',
-           'phmm_holmes_rubin_block_bytes', 'phmm_holmes_rubin_block', 'phmm_holmes_rubin_dp')
+           'phmm_holmes_rubin_block_bytes', 'phmm_holmes_rubin_block', 'phmm_holmes_rubin_dp',
+           'phmm_mixdom2_nest', 'phmm_mixdom2_nest_dp', 'phmm_nest_supported')
 
 
 class Tuning(ctypes.Structure):
@@ -60,7 +61,10 @@ class Batch(ctypes.Structure):
                 ('emit_D', ctypes.c_void_p),
                 ('emit_per_pair', ctypes.c_int32),
                 ('cell_mask', ctypes.c_void_p),
-                ('beam_log_width', ctypes.c_double)]
+                ('beam_log_width', ctypes.c_double),
+                ('nest', ctypes.c_void_p),
+                ('nest_dom', ctypes.c_int32),
+                ('nest_frag', ctypes.c_int32)]
 
 
 class MixDom2Params(ctypes.Structure):
@@ -186,6 +190,12 @@ def load(path=None):
     lib.phmm_mixdom2_param_block.restype = ctypes.c_int
     lib.phmm_mixdom2_tables_dp.argtypes = [vp] + [ctypes.c_int32] * 4 + [vp] * 7
     lib.phmm_mixdom2_tables_dp.restype = ctypes.c_int
+    lib.phmm_mixdom2_nest.argtypes = [ctypes.POINTER(MixDom2Params), ctypes.c_int32, vp, vp, vp]
+    lib.phmm_mixdom2_nest.restype = ctypes.c_int
+    lib.phmm_mixdom2_nest_dp.argtypes = [vp] + [ctypes.c_int32] * 4 + [vp] * 3
+    lib.phmm_mixdom2_nest_dp.restype = ctypes.c_int
+    lib.phmm_nest_supported.argtypes = [ctypes.c_int32, ctypes.c_int32]
+    lib.phmm_nest_supported.restype = ctypes.c_int
     lib.phmm_mixdom2_class_counts_dp.argtypes = [vp] + [ctypes.c_int32] * 4 + [vp] * 9
     lib.phmm_mixdom2_class_counts_dp.restype = ctypes.c_int
     lib.phmm_holmes_rubin_block_bytes.argtypes = [ctypes.c_int32]
@@ -310,6 +320,8 @@ class DeviceBatch:
     emit_D: torch.Tensor        # float32 [P or 1, G, 21]
     cell_mask: torch.Tensor = None   # uint8 [sum (Lx+1)(Ly+1)]: bit 0 M, 1 I, 2 D may emit
     beam_log_width: float = 0.0      # > 0: beam pruning of the forward (generic kernels)
+    nest: torch.Tensor = None        # float32 [P or 1, R]: factored MixDom transitions (models.nested_record)
+    nest_kf: tuple = (0, 0)          # (K, F) of the nest records
     _struct: Batch = field(default=None, repr=False)
 
     @property
@@ -333,7 +345,10 @@ class DeviceBatch:
                 ctypes.c_void_p(self.emit_D.data_ptr()),
                 int(self.emit_M.shape[0] == P),
                 ctypes.c_void_p(self.cell_mask.data_ptr() if self.cell_mask is not None else 0),
-                float(self.beam_log_width))
+                float(self.beam_log_width),
+                ctypes.c_void_p(self.nest.data_ptr() if self.nest is not None else 0),
+                int(self.nest_kf[0]) if self.nest is not None else 0,
+                int(self.nest_kf[1]) if self.nest is not None else 0)
         return self._struct
 
 
@@ -428,12 +443,14 @@ class OutputArena:
         return self.t[name]
 
 
-def make_batch(xs, ys, chi, emit_M, emit_I, emit_D, device='cuda', cell_masks=None, beam_log_width=0.0):
+def make_batch(xs, ys, chi, emit_M, emit_I, emit_D, device='cuda', cell_masks=None, beam_log_width=0.0,
+               nest=None, nest_kf=None):
     """Build a DeviceBatch from host sequences and float tables.
 
     chi: [P or 1, N, N]; emit_*: [P or 1, G, ...] (numpy or torch, any float);
     cell_masks: optional list of per-pair uint8 arrays (Lx+1, Ly+1) (bit 0 M,
-    1 I, 2 D may emit at the cell)."""
+    1 I, 2 D may emit at the cell); nest: optional [P or 1, R] factored
+    MixDom transitions of chi (models.nested_record) with nest_kf = (K, F)."""
     buf, xo, yo, Lx, Ly = pack_residues(xs, ys)
 
     def dev(a, dt):
@@ -453,7 +470,9 @@ def make_batch(xs, ys, chi, emit_M, emit_I, emit_D, device='cuda', cell_masks=No
                        residues=dev(buf, torch.uint8), chi=dev(chi, torch.float32),
                        emit_M=dev(emit_M, torch.float32), emit_I=dev(emit_I, torch.float32),
                        emit_D=dev(emit_D, torch.float32), cell_mask=cm,
-                       beam_log_width=float(beam_log_width))
+                       beam_log_width=float(beam_log_width),
+                       nest=None if nest is None else dev(nest, torch.float32),
+                       nest_kf=(0, 0) if nest is None else tuple(int(v) for v in nest_kf))
 
 
 def forward(plan, batch, stream=None):
@@ -647,6 +666,22 @@ class MixDom2Prologue:
         _check(self.lib.phmm_mixdom2_tables(ctypes.byref(self.struct), P, _ptr(t), _ptr(chi), _ptr(EM), _ptr(EI),
                                             _ptr(ED), _ptr(csubs), ctypes.c_void_p(s.cuda_stream)),
                'phmm_mixdom2_tables')
+
+    def nest_supported(self):
+        """True when the E-step kernels contract this layout (K, F) through the factored record."""
+        return bool(self.lib.phmm_nest_supported(self.K, self.F))
+
+    def nest(self, t, stream=None, out=None):
+        """phmm_mixdom2_nest: the factored transitions (phmm_batch.nest), float32
+        [P, 20KF + 25KF^2] on t's device, for float64 device times t [P]."""
+        P = t.numel()
+        R = 20 * self.K * self.F + 25 * self.K * self.F * self.F
+        if out is None:
+            out = torch.empty(P, R, dtype=torch.float32, device=t.device)
+        s = stream if stream is not None else torch.cuda.current_stream(t.device)
+        _check(self.lib.phmm_mixdom2_nest(ctypes.byref(self.struct), P, _ptr(t), _ptr(out),
+                                          ctypes.c_void_p(s.cuda_stream)), 'phmm_mixdom2_nest')
+        return out
 
     def class_count_shapes(self, P):
         C, A = self.C, self.A

@@ -762,6 +762,14 @@ def _mixdom2_tables(params, ts, device):
     return K, F, chi, csubs, EM, EI, ED
 
 
+def _mixdom2_nest(params, ts, device):
+    """The factored transitions of _mixdom2_tables' chi, float32 [P, R] on
+    `device` (models.nested_record; phmm_batch.nest)."""
+    rec = pm.nested_record(params['main_ins'], params['main_del'], pm._t(ts), params['dom_ins'],
+                           params['dom_del'], params['dom_weights'], params['frag_weights'], params['ext_rates'])
+    return rec.to(device=device, dtype=torch.float32).contiguous()
+
+
 def to_host(result):
     """A result dict of device tensors as host numpy arrays, copied with one
     synchronisation (asynchronous copies into reused pinned memory)."""
@@ -1024,7 +1032,8 @@ def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True, exact_suffst
     t_dev = (ts if isinstance(ts, torch.Tensor) else torch.from_numpy(
         np.ascontiguousarray(np.asarray(ts, np.float64).reshape(-1)))).to(device=dev, dtype=torch.float64)
     chi, EM, EI, ED, csubs = pro(t_dev, device=dev)
-    b = _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev)
+    nest = pro.nest(t_dev) if pro.nest_supported() else None
+    b = _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev, nest=nest, nest_kf=(K, F))
     autotune.apply_cached(plan, b)
     # every output in one device buffer: one copy brings them all to the host
     P, N, G, C, A = b.n_pairs, 2 + 5 * K * F, K * F, pro.C, pro.A

@@ -12,6 +12,7 @@ once:
   pinned host blocks -> device   (parameter block, Holmes-Rubin class blocks,
                                   residues, per-pair times)
   phmm_mixdom2_tables_dp         (chi, P_c(t), emission tables)
+  phmm_mixdom2_nest_dp           (chi in factored form, where the kernels use it)
   phmm_estep_ws_launch           (the split E-step on a graph-owned workspace
                                   whose work description was written once)
   phmm_mixdom2_class_counts_dp   (per-class counts)
@@ -81,6 +82,9 @@ class MixDom2EStepGraph:
         self.EI = torch.empty(P, G, 21, dtype=f32, device=self.dev)
         self.ED = torch.empty(P, G, 21, dtype=f32, device=self.dev)
         self.csubs = torch.empty(P, C, A, A, dtype=f64, device=self.dev)
+        # the factored transitions, where the kernels have them for (K, F)
+        self.nest = (torch.empty(P, 20 * K * F + 25 * K * F * F, dtype=f32, device=self.dev)
+                     if pro.nest_supported() else None)
         # outputs in one arena
         self.specs = [('ll', (P,), f64), ('n_trans', (P, N, N), f64), ('cnt_M', (P, G, 21, 21), f64),
                       ('cnt_I', (P, G, 21), f64), ('cnt_D', (P, G, 21), f64), ('status', (P,), torch.int32)]
@@ -90,7 +94,8 @@ class MixDom2EStepGraph:
         # the plan (own: its side streams belong to the capture stream) and workspace
         self.plan = _lib.Plan(pm.mixdom_state_types(K, F), pm.mixdom_state_groups(K, F), G)
         self.batch = _lib.DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo, residues=self.d_res, chi=self.chi,
-                                      emit_M=self.EM, emit_I=self.EI, emit_D=self.ED)
+                                      emit_M=self.EM, emit_I=self.EI, emit_D=self.ED, nest=self.nest,
+                                      nest_kf=(K, F))
         need = ctypes.c_size_t()
         _lib._check(self.lib.phmm_workspace_bytes(self.plan.handle, ctypes.byref(self.batch.struct()), 1,
                                                   ctypes.byref(need)), 'phmm_workspace_bytes')
@@ -141,6 +146,9 @@ class MixDom2EStepGraph:
         _lib._check(lib.phmm_mixdom2_tables_dp(_ptr(self.d_par), self.K, self.F, self.C, P, _ptr(self.d_t),
                                                _ptr(self.chi), _ptr(self.EM), _ptr(self.EI), _ptr(self.ED),
                                                _ptr(self.csubs), s), 'phmm_mixdom2_tables_dp')
+        if self.nest is not None:
+            _lib._check(lib.phmm_mixdom2_nest_dp(_ptr(self.d_par), self.K, self.F, self.C, P, _ptr(self.d_t),
+                                                 _ptr(self.nest), s), 'phmm_mixdom2_nest_dp')
         ar = self.arena
         _lib._check(lib.phmm_estep_ws_launch(self.plan.handle, ctypes.byref(self.batch.struct()), _ptr(self.ws),
                                              self.ws.numel(), _ptr(ar['ll']), _ptr(ar['n_trans']), _ptr(ar['cnt_M']),

@@ -243,9 +243,11 @@ def effective_trans_per_type(main_ins, main_del, t, dom_ins, dom_del, dom_w):
     return T_exit_k, T_NN + T_exit_k.sum(dim=-3)
 
 
-def build_nested_trans(main_ins, main_del, t, dom_ins, dom_del, dom_w, frag_w, ext_rates):
-    """Collapsed MixDom chi [..., N, N] (models/mixdom.py:252-423); t may be
-    a [B] tensor of per-pair times."""
+def _nested_parts(main_ins, main_del, t, dom_ins, dom_del, dom_w, frag_w, ext_rates):
+    """The factors of the collapsed MixDom chi (models/mixdom.py:252-423):
+    exit_flat [..., nb] (exit_full), dest_flat [..., nb] (frag weight x
+    entry factor), T_exit_k [..., K, 5, 5], the per-domain intra blocks
+    [..., K, 5F, 5F], the SS row and EE column of the body, and the 5x5 T."""
     t = _t(t)
     dom_ins, dom_del, dom_w, frag_w = _t(dom_ins), _t(dom_del), _t(dom_w), _t(frag_w)
     ext = _t(ext_rates)
@@ -253,7 +255,6 @@ def build_nested_trans(main_ins, main_del, t, dom_ins, dom_del, dom_w, frag_w, e
         ext = torch.diag_embed(ext)
     K, F = frag_w.shape
     nb = K * 5 * F
-    N = 2 + nb
     lead = t.shape
     T_exit_k, T = effective_trans_per_type(main_ins, main_del, t, dom_ins, dom_del, dom_w)
     tau_all = tkf91_trans(dom_ins, dom_del, t[..., None])                  # [...,K,5,5]
@@ -269,12 +270,6 @@ def build_nested_trans(main_ins, main_del, t, dom_ins, dom_del, dom_w, frag_w, e
     exit_full = notext[:, None, :] * exit_inner[..., :, :, None]            # [...,K,5,F]
     exit_flat = exit_full.reshape(*lead, nb)
     dest_flat = (frag_w[:, None, :] * entry[..., :, :, None]).reshape(*lead, nb)
-    T_kc = T_exit_k[..., :, _UV_U, :][..., _UV_U]                            # [...,K,5,5]
-    bs = 5 * F
-    d_idx = torch.arange(nb) // bs
-    suv = torch.tensor(np.tile(np.repeat(np.arange(5), F), K))
-    T_exp = T_kc[..., d_idx[None, :], suv[:, None], suv[None, :]]
-    chi_inter = exit_flat[..., :, None] * T_exp * dest_flat[..., None, :]
     tau_MID_all = tau_all[..., _MID, :][..., _MID]                          # [...,K,3,3]
     nonext_M = torch.einsum('df,...dxy,dg->...dxfyg', notext, tau_MID_all, frag_w).reshape(*lead, K, 3 * F, 3 * F)
     ext_M = _block_diag_batched([ext, ext, ext])                            # [K,3F,3F]
@@ -282,19 +277,60 @@ def build_nested_trans(main_ins, main_del, t, dom_ins, dom_del, dom_w, frag_w, e
     nonext_I = (notext[:, :, None] * kap[:, None, None] * frag_w[:, None, :]).expand(*lead, K, F, F)
     intra_I = nonext_I + ext
     blocks = _block_diag_batched([intra_M, intra_I, intra_I])              # [...,K,bs,bs]
+    ss_T = T_exit_k[..., :, S, :][..., _UV_U]                              # [...,K,5]
+    ss_body = (ss_T[..., :, :, None] * frag_w[:, None, :] * entry[..., :, :, None]).reshape(*lead, nb)
+    ee_body = (exit_full * T[..., _UV_U, E][..., None, :, None]).reshape(*lead, nb)
+    return K, F, exit_flat, dest_flat, T_exit_k, blocks, ss_body, ee_body, T
+
+
+def build_nested_trans(main_ins, main_del, t, dom_ins, dom_del, dom_w, frag_w, ext_rates):
+    """Collapsed MixDom chi [..., N, N] (models/mixdom.py:252-423); t may be
+    a [B] tensor of per-pair times."""
+    K, F, exit_flat, dest_flat, T_exit_k, blocks, ss_body, ee_body, T = _nested_parts(
+        main_ins, main_del, t, dom_ins, dom_del, dom_w, frag_w, ext_rates)
+    lead = exit_flat.shape[:-1]
+    nb = K * 5 * F
+    N = 2 + nb
+    bs = 5 * F
+    T_kc = T_exit_k[..., :, _UV_U, :][..., _UV_U]                            # [...,K,5,5]
+    d_idx = torch.arange(nb) // bs
+    suv = torch.tensor(np.tile(np.repeat(np.arange(5), F), K))
+    T_exp = T_kc[..., d_idx[None, :], suv[:, None], suv[None, :]]
+    chi_inter = exit_flat[..., :, None] * T_exp * dest_flat[..., None, :]
     chi_intra = torch.zeros(*lead, nb, nb, dtype=F64, device=blocks.device)
     for k in range(K):
         chi_intra[..., k * bs:(k + 1) * bs, k * bs:(k + 1) * bs] = blocks[..., k, :, :]
     chi_body = chi_inter + chi_intra
-    ss_T = T_exit_k[..., :, S, :][..., _UV_U]                              # [...,K,5]
-    ss_body = (ss_T[..., :, :, None] * frag_w[:, None, :] * entry[..., :, :, None]).reshape(*lead, nb)
-    ee_body = (exit_full * T[..., _UV_U, E][..., None, :, None]).reshape(*lead, nb)
     chi = torch.zeros(*lead, N, N, dtype=F64, device=chi_body.device)
     chi[..., 0, 1] = T[..., S, E]
     chi[..., 0, 2:] = ss_body
     chi[..., 2:, 1] = ee_body
     chi[..., 2:, 2:] = chi_body
     return chi
+
+
+def nest_record_len(K, F):
+    """Floats per pair of the nested chi record: exit [nb], cin [3][nb], intra [K][5F][5F]."""
+    return 20 * K * F + 25 * K * F * F
+
+
+def nested_record(main_ins, main_del, t, dom_ins, dom_del, dom_w, frag_w, ext_rates):
+    """The collapsed MixDom chi in factored form, [..., R] float64 with
+    R = nest_record_len(K, F), body states q = 0..nb-1 (state 2 + q, i.e.
+    domain q // 5F, sub-state (q % 5F) // F, fragment q % F):
+      exit[q]                      exit factor of source q (exit_full);
+      cin[a][q], a = M, I, D       dest[q] * T_exit_k[d_q, a, U(q)];
+      intra[d][i][j]               same-domain block without the inter part.
+    For body states chi[2+s, 2+k] = exit[s] cin[U(s)][k] + [d_s = d_k] intra[d][s', k']
+    (models/mixdom.py:343-394); the SS row and EE column stay in the dense chi."""
+    K, F, exit_flat, dest_flat, T_exit_k, blocks, _, _, _ = _nested_parts(
+        main_ins, main_del, t, dom_ins, dom_del, dom_w, frag_w, ext_rates)
+    lead = exit_flat.shape[:-1]
+    nb = K * 5 * F
+    d_idx = torch.arange(nb) // (5 * F)
+    u_of = torch.tensor(np.tile(np.repeat(np.asarray(_UV_U), F), K))       # main type of each body state
+    cin = torch.stack([T_exit_k[..., d_idx, a, u_of] * dest_flat for a in (M, I, D)], dim=-2)   # [...,3,nb]
+    return torch.cat([exit_flat, cin.reshape(*lead, 3 * nb), blocks.reshape(*lead, K * 25 * F * F)], dim=-1)
 
 
 # ---------------------------------------------------------------- CTMC and emissions

@@ -310,6 +310,14 @@ int phmm_mixdom2_class_counts_dp(const void *param_block, int32_t n_dom, int32_t
 int phmm_mixdom2_nest(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t, float *nest, void *stream);
 int phmm_mixdom2_nest_dp(const void *param_block, int32_t n_dom, int32_t n_frag, int32_t n_classes,
                          int32_t n_pairs, const double *t, float *nest, void *stream);
+/* phmm_mixdom2_tables / _dp that also write the factored record (one build
+ * of chi serves both). */
+int phmm_mixdom2_tables_nest(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t, float *chi,
+                             float *emit_M, float *emit_I, float *emit_D, double *class_subs, float *nest,
+                             void *stream);
+int phmm_mixdom2_tables_nest_dp(const void *param_block, int32_t n_dom, int32_t n_frag, int32_t n_classes,
+                                int32_t n_pairs, const double *t, float *chi, float *emit_M, float *emit_I,
+                                float *emit_D, double *class_subs, float *nest, void *stream);
 /* 1 when the E-step kernels have a factored instantiation for the MixDom
  * layout (n_dom, n_frag) (otherwise a batch's nest record is ignored). */
 int phmm_nest_supported(int32_t n_dom, int32_t n_frag);

@@ -940,9 +940,6 @@ __global__ void __launch_bounds__(TWT) stripe_tw_kernel(const KParams P) {
 // destination) for ROWS / groups rows.
 namespace warp2 {
 
-constexpr int CCH_SHORT = 16;        // steps of a short count chunk
-constexpr int CCH_LONG_MAX = 2048;   // chunk indices from here on are short chunks
-
 struct SmemCT {
     SmemC c;
     int slot;    // float offset: [2][SP] w~ of row 32 at the previous step
@@ -994,12 +991,8 @@ __device__ void count_chunk_tw(const KParams &P, int p, int si, int ch, const Sm
             bhi = min(Ly, rb.y);
         }
     }
-    // chunk ch < CCH_LONG_MAX: steps [ch CCH, ch CCH + CCH); else a short
-    // chunk of CCH_SHORT steps (the end stripes of a batch's longest pairs)
-    const bool shortc = ch >= CCH_LONG_MAX;
-    const int clen = shortc ? CCH_SHORT : CCH;
-    const int t0 = (shortc ? ch - CCH_LONG_MAX : ch) * clen;
-    const int t_hi = min(t_last, t0 + clen - 1);
+    const int t0 = ch * CCH;
+    const int t_hi = min(t_last, t0 + CCH - 1);
     const int t_lo = max(t0, t_beg);
     const int t_top = min(T_last, t_hi + 2);   // two steps of successor history first
     if (t_lo > t_hi) return;                    // uniform over the CTA

@@ -1808,28 +1808,14 @@ int run_core(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
     int n_citems = 0;
     const int cch = warp2::CCH;
     if (split) {   // count chunks: (pair, stripe << 12 | chunk), shortest pairs first (ready first)
-        // two-warp stripes: the stripes of the batch's longest pairs -- ready
-        // last (a chunk also waits for its pair's log-likelihood, known when
-        // the pair's forward ends), the count pass's tail -- in short chunks
-        // of CCH_SHORT steps (chunk index CCH_LONG_MAX + c), so that their
-        // counting spreads over more CTAs
-        int max_steps = 0;
-        for (int p = 0; p < P_; ++p) max_steps = std::max(max_steps, plan->h_meta[p].Lx + plan->h_meta[p].Ly);
         for (auto it = order.rbegin(); it != order.rend(); ++it) {
             const int p = *it;
             const PairMeta &m = plan->h_meta[p];
-            const int ns = m.n_stripes;
-            const bool long_pair = two_warp && 20 * (m.Lx + m.Ly) >= 17 * max_steps;
-            for (int s = 0; s < ns; ++s) {
+            for (int s = 0; s < m.n_stripes; ++s) {
                 const int nrows = std::min(rows, m.Lx + 1 - s * rows);
-                const bool shortc = long_pair &&
-                                    (nrows + m.Ly + warp2::CCH_SHORT - 1) / warp2::CCH_SHORT <= warp2::CCH_LONG_MAX;
-                const int len = shortc ? warp2::CCH_SHORT : cch;
-                const int nch = (nrows + m.Ly + len - 1) / len;
-                if ((two_warp ? nch > warp2::CCH_LONG_MAX : nch > 4096) || s >= (1 << 19))
-                    return fail(PHMM_E_ARG, "pair too long for the count chunk index");
-                for (int c = 0; c < nch; ++c)
-                    plan->h_items.push_back(make_int2(p, (s << 12) | (shortc ? warp2::CCH_LONG_MAX + c : c)));
+                const int nch = (nrows + m.Ly + cch - 1) / cch;
+                if (nch > 4096 || s >= (1 << 19)) return fail(PHMM_E_ARG, "pair too long for the count chunk index");
+                for (int c = 0; c < nch; ++c) plan->h_items.push_back(make_int2(p, (s << 12) | c));
                 n_citems += nch;
             }
         }

@@ -385,15 +385,17 @@ nest_kernel_dp(const Packed *__restrict__ prm, const double *__restrict__ ts, in
 }
 
 __global__ void __launch_bounds__(THREADS)
-chi_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, int N, float *__restrict__ chi, double *__restrict__ chi64) {
-    chi_kernel_body(prm, ts, N, chi, chi64);
+chi_kernel(const __grid_constant__ Packed prm, const double *__restrict__ ts, int N, float *__restrict__ chi, double *__restrict__ chi64,
+           float *__restrict__ nest = nullptr) {
+    chi_kernel_body(prm, ts, N, chi, chi64, nest);
 }
 
 // the same with the parameter block in device memory (a captured graph
 // refreshes it by a copy before each replay)
 __global__ void __launch_bounds__(THREADS)
-chi_kernel_dp(const Packed *__restrict__ prm, const double *__restrict__ ts, int N, float *__restrict__ chi, double *__restrict__ chi64) {
-    chi_kernel_body(*prm, ts, N, chi, chi64);
+chi_kernel_dp(const Packed *__restrict__ prm, const double *__restrict__ ts, int N, float *__restrict__ chi, double *__restrict__ chi64,
+              float *__restrict__ nest = nullptr) {
+    chi_kernel_body(*prm, ts, N, chi, chi64, nest);
 }
 
 // Vector-Jacobian product of chi: for pair p = blockIdx.x and parameter
@@ -805,8 +807,23 @@ extern "C" size_t phmm_mixdom2_class_subs_count(const phmm_mixdom2_params *prm, 
     return (size_t)n_pairs * prm->n_classes * pro::NA * pro::NA;
 }
 
+static int mixdom2_tables(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t, float *chi,
+                          float *emit_M, float *emit_I, float *emit_D, double *class_subs, float *nest, void *stream);
+
 extern "C" int phmm_mixdom2_tables(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t, float *chi,
                                    float *emit_M, float *emit_I, float *emit_D, double *class_subs, void *stream) {
+    return mixdom2_tables(prm, n_pairs, t, chi, emit_M, emit_I, emit_D, class_subs, nullptr, stream);
+}
+
+extern "C" int phmm_mixdom2_tables_nest(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t, float *chi,
+                                        float *emit_M, float *emit_I, float *emit_D, double *class_subs, float *nest,
+                                        void *stream) {
+    if (!nest && n_pairs > 0) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_tables_nest: null nest buffer");
+    return mixdom2_tables(prm, n_pairs, t, chi, emit_M, emit_I, emit_D, class_subs, nest, stream);
+}
+
+static int mixdom2_tables(const phmm_mixdom2_params *prm, int32_t n_pairs, const double *t, float *chi,
+                          float *emit_M, float *emit_I, float *emit_D, double *class_subs, float *nest, void *stream) {
     using namespace pro;
     Packed pk;
     int rc = pack_params(prm, pk, "phmm_mixdom2_tables");
@@ -823,7 +840,7 @@ extern "C" int phmm_mixdom2_tables(const phmm_mixdom2_params *prm, int32_t n_pai
         cudaError_t e = cudaFuncSetAttribute(chi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chi_smem);
         if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
     }
-    chi_kernel<<<n_pairs, THREADS, chi_smem, st>>>(pk, t, N, chi, nullptr);
+    chi_kernel<<<n_pairs, THREADS, chi_smem, st>>>(pk, t, N, chi, nullptr, nest);
     expm_kernel<<<n_pairs * C, THREADS, 0, st>>>(pk, t, class_subs);
     tables_kernel<<<n_pairs, THREADS, 0, st>>>(pk, class_subs, emit_M, emit_I, emit_D);
     cudaError_t e = cudaGetLastError();
@@ -1164,9 +1181,29 @@ extern "C" int phmm_mixdom2_param_block(const phmm_mixdom2_params *prm, void *ho
     return pack_params(prm, *reinterpret_cast<Packed *>(host_block), "phmm_mixdom2_param_block");
 }
 
+static int mixdom2_tables_dp(const void *param_block, int32_t n_dom, int32_t n_frag, int32_t n_classes,
+                             int32_t n_pairs, const double *t, float *chi, float *emit_M, float *emit_I,
+                             float *emit_D, double *class_subs, float *nest, void *stream);
+
 extern "C" int phmm_mixdom2_tables_dp(const void *param_block, int32_t n_dom, int32_t n_frag, int32_t n_classes,
                                       int32_t n_pairs, const double *t, float *chi, float *emit_M, float *emit_I,
                                       float *emit_D, double *class_subs, void *stream) {
+    return mixdom2_tables_dp(param_block, n_dom, n_frag, n_classes, n_pairs, t, chi, emit_M, emit_I, emit_D,
+                             class_subs, nullptr, stream);
+}
+
+extern "C" int phmm_mixdom2_tables_nest_dp(const void *param_block, int32_t n_dom, int32_t n_frag,
+                                           int32_t n_classes, int32_t n_pairs, const double *t, float *chi,
+                                           float *emit_M, float *emit_I, float *emit_D, double *class_subs,
+                                           float *nest, void *stream) {
+    if (!nest && n_pairs > 0) return pro_fail(PHMM_E_ARG, "phmm_mixdom2_tables_nest_dp: null nest buffer");
+    return mixdom2_tables_dp(param_block, n_dom, n_frag, n_classes, n_pairs, t, chi, emit_M, emit_I, emit_D,
+                             class_subs, nest, stream);
+}
+
+static int mixdom2_tables_dp(const void *param_block, int32_t n_dom, int32_t n_frag, int32_t n_classes,
+                             int32_t n_pairs, const double *t, float *chi, float *emit_M, float *emit_I,
+                             float *emit_D, double *class_subs, float *nest, void *stream) {
     using namespace pro;
     const int K = n_dom, F = n_frag, C = n_classes;
     if (K < 1 || F < 1 || C < 1 || K * F > MAXK || n_pairs < 0)
@@ -1182,7 +1219,7 @@ extern "C" int phmm_mixdom2_tables_dp(const void *param_block, int32_t n_dom, in
         cudaError_t e = cudaFuncSetAttribute(chi_kernel_dp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chi_smem);
         if (e != cudaSuccess) return pro_fail(PHMM_E_CUDA, cudaGetErrorString(e));
     }
-    chi_kernel_dp<<<n_pairs, THREADS, chi_smem, st>>>(pk, t, N, chi, nullptr);
+    chi_kernel_dp<<<n_pairs, THREADS, chi_smem, st>>>(pk, t, N, chi, nullptr, nest);
     expm_kernel_dp<<<n_pairs * C, THREADS, 0, st>>>(pk, t, class_subs);
     tables_kernel_dp<<<n_pairs, THREADS, 0, st>>>(pk, class_subs, emit_M, emit_I, emit_D);
     cudaError_t e = cudaGetLastError();

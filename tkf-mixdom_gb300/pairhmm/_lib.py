@@ -30,7 +30,8 @@ EXPORTS = ('phmm_plan_create', 'phmm_plan_destroy', 'phmm_forward', 'phmm_estep'
            'phmm_estep_ws_prepare', 'phmm_estep_ws_launch', 'phmm_mixdom2_param_block_bytes',
            'phmm_mixdom2_param_block', 'phmm_mixdom2_tables_dp', 'phmm_mixdom2_class_counts_dp',
            'phmm_holmes_rubin_block_bytes', 'phmm_holmes_rubin_block', 'phmm_holmes_rubin_dp',
-           'phmm_mixdom2_nest', 'phmm_mixdom2_nest_dp', 'phmm_nest_supported')
+           'phmm_mixdom2_nest', 'phmm_mixdom2_nest_dp', 'phmm_nest_supported', 'phmm_mixdom2_tables_nest',
+           'phmm_mixdom2_tables_nest_dp')
 
 
 class Tuning(ctypes.Structure):
@@ -194,6 +195,10 @@ def load(path=None):
     lib.phmm_mixdom2_nest.restype = ctypes.c_int
     lib.phmm_mixdom2_nest_dp.argtypes = [vp] + [ctypes.c_int32] * 4 + [vp] * 3
     lib.phmm_mixdom2_nest_dp.restype = ctypes.c_int
+    lib.phmm_mixdom2_tables_nest.argtypes = [ctypes.POINTER(MixDom2Params), ctypes.c_int32] + [vp] * 8
+    lib.phmm_mixdom2_tables_nest.restype = ctypes.c_int
+    lib.phmm_mixdom2_tables_nest_dp.argtypes = [vp] + [ctypes.c_int32] * 4 + [vp] * 8
+    lib.phmm_mixdom2_tables_nest_dp.restype = ctypes.c_int
     lib.phmm_nest_supported.argtypes = [ctypes.c_int32, ctypes.c_int32]
     lib.phmm_nest_supported.restype = ctypes.c_int
     lib.phmm_mixdom2_class_counts_dp.argtypes = [vp] + [ctypes.c_int32] * 4 + [vp] * 9
@@ -659,10 +664,16 @@ class MixDom2Prologue:
         N, G = self.N, self.G
         return (P, N, N), (P, G, 21, 21), (P, G, 21), (P, G, 21), (P, self.C, self.A, self.A)
 
-    def run(self, t, chi, EM, EI, ED, csubs, stream=None):
-        """Write into caller tensors: t float64 [P] and the five outputs of shapes(P)."""
+    def run(self, t, chi, EM, EI, ED, csubs, stream=None, nest=None):
+        """Write into caller tensors: t float64 [P] and the five outputs of
+        shapes(P) (and the factored record into `nest`, when given)."""
         P = t.numel()
         s = stream if stream is not None else torch.cuda.current_stream(t.device)
+        if nest is not None:
+            _check(self.lib.phmm_mixdom2_tables_nest(ctypes.byref(self.struct), P, _ptr(t), _ptr(chi), _ptr(EM),
+                                                     _ptr(EI), _ptr(ED), _ptr(csubs), _ptr(nest),
+                                                     ctypes.c_void_p(s.cuda_stream)), 'phmm_mixdom2_tables_nest')
+            return
         _check(self.lib.phmm_mixdom2_tables(ctypes.byref(self.struct), P, _ptr(t), _ptr(chi), _ptr(EM), _ptr(EI),
                                             _ptr(ED), _ptr(csubs), ctypes.c_void_p(s.cuda_stream)),
                'phmm_mixdom2_tables')
@@ -726,7 +737,10 @@ class MixDom2Prologue:
                                              ctypes.c_void_p(s.cuda_stream)), 'phmm_mixdom2_chi_vjp')
         return out
 
-    def __call__(self, ts, device='cuda', stream=None):
+    def __call__(self, ts, device='cuda', stream=None, with_nest=False):
+        """(chi, EM, EI, ED, csubs) on the device for per-pair times ts; with
+        with_nest, the factored record (phmm_batch.nest) appended, built by
+        the same launch."""
         if isinstance(ts, torch.Tensor):
             t = ts.to(device=device, dtype=torch.float64).reshape(-1).contiguous()
         else:
@@ -734,8 +748,12 @@ class MixDom2Prologue:
         shp = self.shapes(t.numel())
         f32, f64 = torch.float32, torch.float64
         outs = [torch.empty(sh, dtype=f64 if i == 4 else f32, device=t.device) for i, sh in enumerate(shp)]
-        self.run(t, *outs, stream=stream)
-        return tuple(outs)
+        nest = None
+        if with_nest:
+            R = 20 * self.K * self.F + 25 * self.K * self.F * self.F
+            nest = torch.empty(t.numel(), R, dtype=f32, device=t.device)
+        self.run(t, *outs, stream=stream, nest=nest)
+        return tuple(outs) + ((nest,) if with_nest else ())
 
 
 def mixdom2_tables(params, ts, device='cuda', stream=None):

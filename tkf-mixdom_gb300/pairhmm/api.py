@@ -1031,8 +1031,10 @@ def estep_batch_mixdom2(params, xs, ys, ts, with_class_counts=True, exact_suffst
             return res
     t_dev = (ts if isinstance(ts, torch.Tensor) else torch.from_numpy(
         np.ascontiguousarray(np.asarray(ts, np.float64).reshape(-1)))).to(device=dev, dtype=torch.float64)
-    chi, EM, EI, ED, csubs = pro(t_dev, device=dev)
-    nest = pro.nest(t_dev) if pro.nest_supported() else None
+    if pro.nest_supported():   # the kernels contract this layout through the factored record
+        chi, EM, EI, ED, csubs, nest = pro(t_dev, device=dev, with_nest=True)
+    else:
+        (chi, EM, EI, ED, csubs), nest = pro(t_dev, device=dev), None
     b = _lib.make_batch(xs, ys, chi, EM, EI, ED, device=dev, nest=nest, nest_kf=(K, F))
     autotune.apply_cached(plan, b)
     # every output in one device buffer: one copy brings them all to the host

@@ -11,8 +11,8 @@ once:
 
   pinned host blocks -> device   (parameter block, Holmes-Rubin class blocks,
                                   residues, per-pair times)
-  phmm_mixdom2_tables_dp         (chi, P_c(t), emission tables)
-  phmm_mixdom2_nest_dp           (chi in factored form, where the kernels use it)
+  phmm_mixdom2_tables[_nest]_dp  (chi, P_c(t), emission tables; chi's factored
+                                  form where the kernels use it)
   phmm_estep_ws_launch           (the split E-step on a graph-owned workspace
                                   whose work description was written once)
   phmm_mixdom2_class_counts_dp   (per-class counts)
@@ -143,12 +143,15 @@ class MixDom2EStepGraph:
             self.d_hr.copy_(self.h_hr, non_blocking=True)
             self.d_res.copy_(self.h_res, non_blocking=True)
             self.d_t.copy_(self.h_t, non_blocking=True)
-        _lib._check(lib.phmm_mixdom2_tables_dp(_ptr(self.d_par), self.K, self.F, self.C, P, _ptr(self.d_t),
-                                               _ptr(self.chi), _ptr(self.EM), _ptr(self.EI), _ptr(self.ED),
-                                               _ptr(self.csubs), s), 'phmm_mixdom2_tables_dp')
-        if self.nest is not None:
-            _lib._check(lib.phmm_mixdom2_nest_dp(_ptr(self.d_par), self.K, self.F, self.C, P, _ptr(self.d_t),
-                                                 _ptr(self.nest), s), 'phmm_mixdom2_nest_dp')
+        if self.nest is not None:   # the tables and the factored record from one build of chi
+            _lib._check(lib.phmm_mixdom2_tables_nest_dp(_ptr(self.d_par), self.K, self.F, self.C, P, _ptr(self.d_t),
+                                                        _ptr(self.chi), _ptr(self.EM), _ptr(self.EI), _ptr(self.ED),
+                                                        _ptr(self.csubs), _ptr(self.nest), s),
+                        'phmm_mixdom2_tables_nest_dp')
+        else:
+            _lib._check(lib.phmm_mixdom2_tables_dp(_ptr(self.d_par), self.K, self.F, self.C, P, _ptr(self.d_t),
+                                                   _ptr(self.chi), _ptr(self.EM), _ptr(self.EI), _ptr(self.ED),
+                                                   _ptr(self.csubs), s), 'phmm_mixdom2_tables_dp')
         ar = self.arena
         _lib._check(lib.phmm_estep_ws_launch(self.plan.handle, ctypes.byref(self.batch.struct()), _ptr(self.ws),
                                              self.ws.numel(), _ptr(ar['ll']), _ptr(ar['n_trans']), _ptr(ar['cnt_M']),

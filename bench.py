@@ -733,6 +733,11 @@ def main():
                                f'({peaks.get("sm_max_mhz")} MHz, {src} MEASURED_PEAKS.json); '
                                'the DP is a dense FP32 CUDA-core contraction: no tensor-core or HBM bound',
                 'flop_per_cell': fpc * N * N,
+                'flop_accounting': ('dense 2N^2 per cell per pass; with the factored MixDom transitions '
+                                    '(config.transitions) this is effective FLOP: the two-warp recursions '
+                                    'execute 5 (5KF) + 11 K F^2 (forward) and 4 (5KF) + 11 K F^2 (backward) '
+                                    'multiply-adds per cell, 108 and 93 at K=3 F=1 against 240' if nest is not None
+                                    else 'dense 2N^2 per cell per pass'),
                 'fwd_kernel_ms': fwd_avg, 'bwd_kernel_ms': bwd_avg, 'count_kernel_ms': cnt_avg,
                 'count_overlaps_wavefronts': overlapped,
                 'kernels': [f[0] for f in fam if f[0]],

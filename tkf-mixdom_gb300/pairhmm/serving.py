@@ -279,7 +279,9 @@ class CudaExecutor:
             st = pm.mixdom_state_types(K, F)
             gr = pm.mixdom_state_groups(K, F)
             G = K * F
-            m.extra = {'K': K, 'F': F, 'prologue': _lib.MixDom2Prologue(p)}
+            pro = _lib.MixDom2Prologue(p)
+            # the factored transitions (phmm_batch.nest) where the kernels have them
+            m.extra = {'K': K, 'F': F, 'prologue': pro, 'nest': pro.nest_supported()}
         else:
             raise ValueError(f'unknown model kind {m.kind!r}')
         m.plan = get_plan(st, gr, G)
@@ -297,6 +299,8 @@ class CudaExecutor:
         pro = m.extra['prologue']
         if m.kind == 'mixdom2':
             sizes += [('t', 8 * P), ('csubs', 8 * P * pro.C * pro.A * pro.A)]
+            if m.extra.get('nest'):
+                sizes += [('nest', 4 * P * (20 * pro.K * pro.F + 25 * pro.K * pro.F * pro.F))]
         else:
             sizes += [('t', 8 * P), ('csubs', 8 * P * pro.A * pro.A)]
         return sizes
@@ -350,10 +354,14 @@ class CudaExecutor:
                 csubs = views['csubs'].view(torch.float64).view(P, pro.C, pro.A, pro.A)
             else:
                 csubs = views['csubs'].view(torch.float64).view(P, pro.A, pro.A)
-            pro.run(t_v, chi_v, eM, eI, eD, csubs, stream=s)
+            nest = None
+            if m.kind == 'mixdom2' and m.extra.get('nest'):
+                nest = f32(views['nest'], 20 * pro.K * pro.F + 25 * pro.K * pro.F * pro.F)
+            pro.run(t_v, chi_v, eM, eI, eD, csubs, stream=s, **({'nest': nest} if nest is not None else {}))
             chi = EM = EI = ED = None
             batch = _lib.DeviceBatch(Lx=Lx, Ly=Ly, x_off=xo, y_off=yo, residues=res, chi=chi_v,
-                                     emit_M=eM, emit_I=eI, emit_D=eD)
+                                     emit_M=eM, emit_I=eI, emit_D=eD, nest=nest,
+                                     nest_kf=(m.extra.get('K', 0), m.extra.get('F', 0)))
             _lib.estep_ws(m.plan, batch, (self.arena.data_ptr() + off, ws_n), stream=s, out=out)
             dev_out = dict(out)
             if m.kind == 'mixdom2' and m.class_counts:

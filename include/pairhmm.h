@@ -102,8 +102,10 @@ typedef struct phmm_batch {
      * so that chi[2+s][2+k] = exit[s] cin[U(s)][k] + [same domain] intra.
      * The dense chi is still required (start row, end column, counts).
      * With it the two-warp stripes of a compiled layout (K = 3, F = 1)
-     * contract each cell in about 6N + 11KF^2 multiply-adds instead of N^2;
-     * other layouts, masked and pruned batches use the dense chi.
+     * contract each cell in about 6N + 11KF^2 multiply-adds instead of N^2,
+     * and the wide kernels at F = 4 (K = 4..8; not with checkpointing or the
+     * tensor-core forward) in about 3N + 11KF^2 per pass; other layouts,
+     * masked and pruned batches use the dense chi.
      * phmm_mixdom2_nest builds it.  nest_dom = K, nest_frag = F. */
     const float *nest;
     int32_t nest_dom, nest_frag;
@@ -319,7 +321,9 @@ int phmm_mixdom2_tables_nest_dp(const void *param_block, int32_t n_dom, int32_t 
                                 int32_t n_pairs, const double *t, float *chi, float *emit_M, float *emit_I,
                                 float *emit_D, double *class_subs, float *nest, void *stream);
 /* 1 when the E-step kernels have a factored instantiation for the MixDom
- * layout (n_dom, n_frag) (otherwise a batch's nest record is ignored). */
+ * layout (n_dom, n_frag): the 17-state two-warp stripes (3, 1) and the wide
+ * kernels at n_frag = 4, n_dom = 4..8 (otherwise a batch's nest record is
+ * ignored). */
 int phmm_nest_supported(int32_t n_dom, int32_t n_frag);
 
 /* The collapsed chi alone (float32 and, when chi64 is not null, float64

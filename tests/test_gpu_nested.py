@@ -109,4 +109,36 @@ def test_device_record_equals_float64_builder(cuda_lib, K, F, C):
     want = pm.nested_record(p['main_ins'], p['main_del'], torch.as_tensor(ts), p['dom_ins'], p['dom_del'],
                             p['dom_weights'], p['frag_weights'], p['ext_rates']).numpy()
     np.testing.assert_allclose(got, want, rtol=2e-7, atol=1e-30)
-    assert pro.nest_supported() == (K == 3 and F == 1)
+    assert pro.nest_supported() == ((K, F) == (3, 1) or (F == 4 and 4 <= K <= 8))
+
+
+WIDE_LENGTHS = [(0, 0), (1, 1), (2, 1), (0, 7), (31, 33), (33, 31), (70, 66), (130, 121)]
+
+
+def test_wide_nested_estep_matches_oracle_and_dense(cuda_lib):
+    """162 states (K=8, F=4) on the wide kernels with the factored record:
+    the C oracle and the dense wide kernels on the same batch."""
+    from oracle import pool
+    rng = np.random.default_rng(77)
+    K, F = 8, 4
+    cases, nest = nested_case(rng, K, F, 2, len(WIDE_LENGTHS))
+    xs, ys = [], []
+    for Lx, Ly in WIDE_LENGTHS:
+        x, y = related_pair(rng, Lx, Ly)
+        xs.append(x)
+        ys.append(y)
+    got, plan = run(cases, xs, ys, nest, (K, F))
+    assert plan.last_variant == 6
+    dense, _ = run(cases, xs, ys)
+    assert (got['status'] == 0).all(), got['status']
+    oracle = pool.estep_pairs([tuple(c) + (x, y) for c, x, y in zip(cases, xs, ys)])
+    for b, (ll, n, (cM, cI, cD)) in enumerate(oracle):
+        assert abs(got['ll'][b] - ll) <= LL_RTOL * abs(ll) + 1e-9, (b, got['ll'][b], ll)
+        assert abs(got['ll'][b] - dense['ll'][b]) <= LL_RTOL * abs(ll) + 1e-9
+        assert_counts(got['n_trans'][b], n)
+        assert_counts(got['cnt_M'][b], cM)
+        assert_counts(got['cnt_I'][b], cI)
+        assert_counts(got['cnt_D'][b], cD)
+    fwd, _ = run(cases, xs, ys, nest, (K, F), forward_only=True)
+    for b, (ll, _, _) in enumerate(oracle):
+        assert abs(fwd['ll'][b] - ll) <= LL_RTOL * abs(ll) + 1e-9, (b, fwd['ll'][b], ll)

@@ -985,6 +985,7 @@ __global__ void band_post_kernel(const KParams P, int rows, int stride, int nsrc
 #include "estep_block.cuh"
 #include "estep_block_split.cuh"
 #include "estep_wide.cuh"
+#include "estep_wide_nest.cuh"
 
 namespace {
 
@@ -1130,6 +1131,25 @@ WarpLauncher find_warp_launcher(int nm, int ni, int nd) {
 
 // ---- factored MixDom transitions (phmm_batch.nest)
 int64_t nest_record_len(int K, int F) { return 20LL * K * F + 25LL * K * F * F; }
+
+// the wide kernels contract through the record where one quad of slots is one
+// (domain, sub-state) block: F = 4, the type groups in state order (MM_d; MI_d,
+// II_d per domain; MD_d, DD_d per domain), the start state after them
+bool wide_nest_layout(const KParams &K, int nK, int nF) {
+    if (nF != 4 || nK < 1 || K.N != 2 + 20 * nK) return false;
+    if (K.kbeg[0] != 0 || K.kend[0] != 4 * nK || K.kbeg[1] != 4 * nK || K.kend[1] != 12 * nK ||
+        K.kbeg[2] != 12 * nK || K.kend[2] != 20 * nK || K.s_slot < 20 * nK)
+        return false;
+    for (int q = 0; q < 5 * nK; ++q) {
+        int d, uv;
+        if (q < nK) { d = q; uv = 0; }
+        else if (q < 3 * nK) { const int i = q - nK; d = i / 2; uv = (i & 1) ? 3 : 1; }
+        else { const int i = q - 3 * nK; d = i / 2; uv = (i & 1) ? 4 : 2; }
+        for (int u = 0; u < 4; ++u)
+            if (K.slot_orig[4 * q + u] != 2 + d * 20 + uv * 4 + u) return false;
+    }
+    return true;
+}
 
 // (K, F) layouts with a nested instantiation of the two-warp stripes
 bool has_nest_tw(int nm, int K, int F) { return nm == 3 && K == 3 && F == 1; }
@@ -1336,6 +1356,14 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
             if (K.quad_type[4 * w + q] != K.quad_type[4 * w]) tc = false;
     auto fb_kernel = tc ? wide::fwdbwd_wide_kernel<true> : wide::fwdbwd_wide_kernel<false>;
     auto f_kernel = tc ? wide::forward_wide_kernel<true> : wide::forward_wide_kernel<false>;
+    // factored MixDom transitions (phmm_batch.nest): the wide_nest kernels where
+    // the slot layout allows (checked per plan) and neither the tensor-core
+    // forward nor stripe-edge checkpointing is asked for (decided below)
+    if (b->nest) {
+        const int rc = check_nest(plan, b);
+        if (rc) return rc;
+    }
+    bool wnest = b->nest && !tc && wide_nest_layout(K, b->nest_dom, b->nest_frag);
     std::vector<int> order(P_);
     for (int p = 0; p < P_; ++p) {
         if (b->Lx_host[p] < 0 || b->Ly_host[p] < 0) return fail(PHMM_E_ARG, "negative length");
@@ -1391,6 +1419,7 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         ckpt = plan->tuning.checkpoint == 1 ||
                (plan->tuning.checkpoint == 0 && pair_bytes > 0.4 * (double)plan->total_mem);
     }
+    if (ckpt) wnest = false;   // the recompute passes run the dense kernels
     struct CkGroup { size_t rc_off, n_rc, c_off, n_c; };
     std::vector<CkGroup> groups;
     int64_t grp_cells = 0;   // scratch cells of the largest group (each lattice)
@@ -1569,9 +1598,18 @@ int run_wide(phmm_plan *plan, const phmm_batch *b, bool estep, double *ll, doubl
         K.n_items = n_fb;
         K.counter = d_counters;
         const int threads = 32 * ((NQd + 3) / 4);
-        const int bytes = std::max(wide::make_smem_wd(NS, KS, max_ly, false).bytes,
-                                   estep ? wide::make_smem_wd(NS, KS, max_ly, true).bytes : 0);
+        int bytes = std::max(wide::make_smem_wd(NS, KS, max_ly, false).bytes,
+                             estep ? wide::make_smem_wd(NS, KS, max_ly, true).bytes : 0);
         auto kern = estep ? fb_kernel : f_kernel;
+        if (wnest) {   // the factored contraction: no dense chi in shared memory
+            K.nest = b->nest;
+            K.nest_stride = b->chi_per_pair ? nest_record_len(b->nest_dom, b->nest_frag) : 0;
+            K.nest_K = b->nest_dom;
+            K.nest_F = b->nest_frag;
+            kern = estep ? wide::wide_nest_kernel<false> : wide::wide_nest_kernel<true>;
+            bytes = std::max(wide::make_smem_wn(NS, KS, max_ly, false).bytes,
+                             estep ? wide::make_smem_wn(NS, KS, max_ly, true).bytes : 0);
+        }
         CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
         int occ = 0;
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, bytes));
@@ -2208,7 +2246,10 @@ int phmm_last_error(char *buf, size_t len) {
 }
 
 int phmm_nest_supported(int32_t n_dom, int32_t n_frag) {
-    return has_nest_tw(n_dom * n_frag, n_dom, n_frag) ? 1 : 0;
+    // the two-warp stripes of 17 states; the wide kernels at F = 4 (K = 4..8:
+    // more than 64 slots, one quad of slots per (domain, sub-state) block)
+    const bool wide_ok = n_frag == 4 && n_dom >= 4 && 20 * n_dom <= 160;
+    return (has_nest_tw(n_dom * n_frag, n_dom, n_frag) || wide_ok) ? 1 : 0;
 }
 
 int phmm_plan_create(const phmm_model_desc *md, phmm_plan **out) {

@@ -30,6 +30,7 @@ constexpr int NIA = 52;   // floats per quad of intra coefficients (12 partners 
 struct SmemWn {
     int A, B, E, MX, G, llp, misc;   // rings as the dense kernels; G: type-sum ring
     int ex, cin, c0, chiE, ia, pq;   // coefficients (pq: ints, partner quads [NQd][3])
+    int us;                          // int offset: top-level type U of each slot (3 = none) [NS]
     int ys;                          // byte offset
     int bytes;
 };
@@ -50,6 +51,7 @@ __host__ __device__ inline SmemWn make_smem_wn(int NS, int KS, int max_ly, bool 
     L.chiE = o; o += (NS + 3) & ~3;
     L.ia = o; o += NQd * NIA;
     L.pq = o; o += (3 * NQd + 3) & ~3;
+    L.us = o; o += (NS + 3) & ~3;
     o = (o + 1) & ~1;
     L.llp = o / 2; o += 2 * (KS / 4 + 4);
     L.misc = o; o += 8;
@@ -73,6 +75,12 @@ __device__ __forceinline__ int nest_quad_of(const KParams &P, int d, int uv) {
 }
 __device__ __forceinline__ int nest_U(int uv) { return uv < 3 ? 0 : uv - 2; }
 
+// exponent of a stored maximum (positive float bits): e with m 2^-e in [0.5, 1)
+// for normal m; a subnormal maximum counts as 2^-126 (the predicted output
+// exponent then keeps the cell's values a little below 0.5, which every
+// consumer takes with its exponent)
+__device__ __forceinline__ int exp_of_max_n(int mbits) { return max((mbits >> 23) & 0xff, 1) - 126; }
+
 // Coefficients of pair p into shared memory (all threads).  bwd: intra rows by
 // source quad (partners = destination slots), else by destination quad.
 __device__ void load_nest_wide(const KParams &P, int p, const SmemWn &L, float *sm, bool bwd) {
@@ -82,14 +90,18 @@ __device__ void load_nest_wide(const KParams &P, int p, const SmemWn &L, float *
     const int tid = threadIdx.x, nt = blockDim.x;
     const float *rec = P.nest + (int64_t)p * P.nest_stride;
     const float *chi = P.chi + (int64_t)p * P.chi_stride;
+    int *us = reinterpret_cast<int *>(sm) + L.us;
     for (int s = tid; s < NS; s += nt) {
         float v = 0.f;
+        int u = 3;
         if (s < KS) {
             int d, uv;
             nest_quad_du(P, s >> 2, d, uv);
             v = __ldg(rec + d * bs + uv * F + (s & 3));
+            u = nest_U(uv);
         }
         sm[L.ex + s] = v;
+        us[s] = u;
         const int os = P.slot_orig[s];
         sm[L.chiE + s] = os >= 0 ? __ldg(chi + os * N + P.e_idx) : 0.f;
     }
@@ -121,6 +133,27 @@ __device__ void load_nest_wide(const KParams &P, int p, const SmemWn &L, float *
         sm[L.ia + q * NIA + j * 4 + u] = v;
     }
 }
+
+// Emission factors of a thread's 4 destination slots (one quad, one type) at
+// its 4 rows, looked up per step by the y character only: offsets into the
+// M / I tables built once per stripe, D factors (fixed by the row's x) read
+// once.  (The dense kernels decode slot type and group per lookup.)
+struct QuadEmit {
+    const float *tab;   // eM (by x and y), eI (by y) or eD (by x)
+    int gb[4];          // [u] group offset
+    int xo[4];          // [row] x offset (M: 21 x, D: x, I: 0)
+    int ym;             // 1: add y (M, I), 0 (D)
+    __device__ void init(const KParams &P, const float *eMg, const float *eIg, const float *eDg, int q, const int (&xr)[4]) {
+        const int qt = P.quad_type[q];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) gb[u] = P.slot_group[4 * q + u] * (qt == T_M ? 441 : 21);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) xo[i] = qt == T_M ? xr[i] * 21 : (qt == T_D ? xr[i] : 0);
+        tab = qt == T_M ? eMg : (qt == T_I ? eIg : eDg);
+        ym = qt == T_D ? 0 : 1;
+    }
+    __device__ __forceinline__ float at(int i, int u, int y) const { return __ldg(tab + gb[u] + xo[i] + ym * y); }
+};
 
 // ---------------------------------------------------------------- forward
 __device__ void fwd_stripe_wn(const KParams &P, int p, int si, const SmemWn &L, float *sm, unsigned char *smb) {
@@ -176,6 +209,9 @@ __device__ void fwd_stripe_wn(const KParams &P, int p, int si, const SmemWn &L, 
     if (active) nest_quad_du(P, qd, myd, myuv);
     const int myU = nest_U(myuv);
     const int T_last = (nrows - 1) + Ly;
+    QuadEmit qe;
+    qe.init(P, eMg, eIg, eDg, active ? qd : 0, xr);
+    const int *usl = reinterpret_cast<const int *>(sm) + L.us;
     __syncthreads();   // coefficients in place
     float cinr[3][4], exr[4];
     int pqr[3] = {-1, -1, -1};
@@ -212,11 +248,11 @@ __device__ void fwd_stripe_wn(const KParams &P, int p, int si, const SmemWn &L, 
         for (int s = lane; s < NS; s += 32) {
             const float v = __ldcg(src + s);
             B[(bs * NS + s) * BW] = v;
-            if (s < KS) {
-                int d, uv;
-                nest_quad_du(P, s >> 2, d, uv);
-                g[nest_U(uv)] = fmaf(sm[L.ex + s], v, g[nest_U(uv)]);
-            }
+            const int u = usl[s];
+            const float c = sm[L.ex + s] * v;
+            g[0] += u == 0 ? c : 0.f;
+            g[1] += u == 1 ? c : 0.f;
+            g[2] += u == 2 ? c : 0.f;
         }
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -259,9 +295,11 @@ __device__ void fwd_stripe_wn(const KParams &P, int p, int si, const SmemWn &L, 
                     reinterpret_cast<int *>(dst)[NS] = E[((t - 1) & 3) * BW + RW];
                     reinterpret_cast<int *>(dst)[NS + 1] = MX[((t - 1) & 3) * BW + RW];
                 }
-                __threadfence();
-                __syncwarp();
-                if (lane == 0 && (((jb + 1) % WPUB) == 0 || jb == Ly)) st_release(prog_mine, jb + 1);
+                if (((jb + 1) % WPUB) == 0 || jb == Ly) {   // publish: this and the earlier columns' rows
+                    __threadfence();
+                    __syncwarp();
+                    if (lane == 0) st_release(prog_mine, jb + 1);
+                }
             }
         }
         if (active) {
@@ -277,17 +315,17 @@ __device__ void fwd_stripe_wn(const KParams &P, int p, int si, const SmemWn &L, 
                     if (j >= 1) {
                         const int mb = MX[((t - 1) & 3) * BW + r + 1];
                         const int e = E[((t - 1) & 3) * BW + r + 1];
-                        if (mb > 0 && e > EXP_NONE) EI = e + exp_of_max(mb);
+                        if (mb > 0 && e > EXP_NONE) EI = e + exp_of_max_n(mb);
                     }
                     if (row >= 1) {
                         const int mb = MX[((t - 1) & 3) * BW + r];
                         const int e = E[((t - 1) & 3) * BW + r];
-                        if (mb > 0 && e > EXP_NONE) ED = e + exp_of_max(mb);
+                        if (mb > 0 && e > EXP_NONE) ED = e + exp_of_max_n(mb);
                     }
                     if (row >= 1 && j >= 1) {
                         const int mb = MX[((t - 2) & 3) * BW + r];
                         const int e = E[((t - 2) & 3) * BW + r];
-                        if (mb > 0 && e > EXP_NONE) EM = e + exp_of_max(mb);
+                        if (mb > 0 && e > EXP_NONE) EM = e + exp_of_max_n(mb);
                     }
                 }
                 const int Eout = max(max(EI, ED), EM);
@@ -346,7 +384,7 @@ __device__ void fwd_stripe_wn(const KParams &P, int p, int si, const SmemWn &L, 
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     float v = 0.f;
-                    if (valid[i] && sc[i] > 0.f) v = acc[i][u] * sc[i] * emit_g(P, eMg, eIg, eDg, 4 * qd + u, xr[i], yj);
+                    if (valid[i] && sc[i] > 0.f) v = acc[i][u] * sc[i] * qe.at(i, u, yj);
                     if (4 * qd + u == P.s_slot) v = origin ? 1.f : 0.f;
                     acc[i][u] = v;
                     mxr[i] = fmaxf(mxr[i], v);
@@ -489,6 +527,8 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
     if (active) nest_quad_du(P, qs, myd, myuv);
     const int myU = nest_U(myuv);
     const int myT = active ? P.quad_type[qs] - T_M : 0;   // my quad as destinations: 0 M, 1 I, 2 D
+    QuadEmit qe;
+    qe.init(P, eMg, eIg, eDg, active ? qs : 0, xr);
     __syncthreads();
     float cinr[3][4], exr[4];
     int pqr[3] = {-1, -1, -1};
@@ -503,6 +543,7 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
 #pragma unroll
         for (int j = 0; j < 3; ++j) pqr[j] = pq[3 * qs + j];
     } else {
+        // (inactive: no partners)
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             exr[u] = 0.f;
@@ -511,6 +552,9 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
         }
     }
     const float *iaq = sm + L.ia + (active ? qs : 0) * NIA;
+    int tqr[3];   // the partner quads' destination types
+#pragma unroll
+    for (int j = 0; j < 3; ++j) tqr[j] = pqr[j] >= 0 ? P.quad_type[pqr[j]] : T_NONE;
     // halo: row i0+RW at column c: B slot (c + RW) % 3 index RW + 3, E / MX slot
     // (c + RW) & 3 index RW, its nine P sums in P slot (c + RW) & 3 index RW + 3
     auto fetch_halo = [&](int col) -> bool {
@@ -527,7 +571,8 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
         for (int kk = lane; kk < KS; kk += 32) {
             const float w = __ldcg(src + kk);
             B[(bs * KS + kk) * BW + RW + 3] = w;
-            const int tk = P.quad_type[kk >> 2] - T_M;
+            const int qk = kk >> 2, qi = P.kbeg[1] / 4, qd0 = P.kbeg[2] / 4;
+            const int tk = qk < qi ? 0 : (qk < qd0 ? 1 : 2);
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 const float c = sm[L.cin + a * KS + kk] * w;
@@ -556,9 +601,11 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
             reinterpret_cast<int *>(dst)[NS] = E[(t & 3) * BW + 0];
             reinterpret_cast<int *>(dst)[NS + 1] = MX[(t & 3) * BW + 0];
         }
-        __threadfence();
-        __syncwarp();
-        if (lane == 0 && ((t % WPUB) == 0)) st_release(prog_mine, Ly + 1 - t);
+        if ((t % WPUB) == 0) {   // publish: this and the earlier (higher) columns' rows
+            __threadfence();
+            __syncwarp();
+            if (lane == 0) st_release(prog_mine, Ly + 1 - t);
+        }
     };
     __syncthreads();
     if (warp == 0 && !fetch_halo(T_last - (RW - 1))) misc[0] = 1;
@@ -588,15 +635,15 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
                 if (valid[i] && !term[i]) {
                     if (j + 1 <= Ly) {
                         const int mb = MX[((t + 1) & 3) * BW + r], e = E[((t + 1) & 3) * BW + r];
-                        if (mb > 0 && e > EXP_NONE) { EsI[i] = e; vI = e + exp_of_max(mb); }
+                        if (mb > 0 && e > EXP_NONE) { EsI[i] = e; vI = e + exp_of_max_n(mb); }
                     }
                     if (row + 1 <= Lx) {
                         const int mb = MX[((t + 1) & 3) * BW + r + 1], e = E[((t + 1) & 3) * BW + r + 1];
-                        if (mb > 0 && e > EXP_NONE) { EsD[i] = e; vD = e + exp_of_max(mb); }
+                        if (mb > 0 && e > EXP_NONE) { EsD[i] = e; vD = e + exp_of_max_n(mb); }
                     }
                     if (row + 1 <= Lx && j + 1 <= Ly) {
                         const int mb = MX[((t + 2) & 3) * BW + r + 1], e = E[((t + 2) & 3) * BW + r + 1];
-                        if (mb > 0 && e > EXP_NONE) { EsM[i] = e; vM = e + exp_of_max(mb); }
+                        if (mb > 0 && e > EXP_NONE) { EsM[i] = e; vM = e + exp_of_max_n(mb); }
                     }
                 }
                 Eo[i] = term[i] ? 0 : max(max(vI, vD), vM);
@@ -623,7 +670,7 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
 #pragma unroll
             for (int pj = 0; pj < 3; ++pj) {
                 if (pqr[pj] < 0) continue;
-                const int tq = P.quad_type[pqr[pj]];
+                const int tq = tqr[pj];
                 const float *wb = tq == T_M ? B + ((t + 2) % 3) * KS * BW + r0 + 4
                                             : (tq == T_I ? A + ((t + 1) & 1) * KS * RW + r0 : B + ((t + 1) % 3) * KS * BW + r0 + 4);
                 const int wst = tq == T_I ? RW : BW;
@@ -654,7 +701,7 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
                     float b = 0.f;
                     if (valid[i]) {
                         b = term[i] ? sm[L.chiE + 4 * qs + u] : acc[i][u];
-                        mxr[i] = fmaxf(mxr[i], b * emit_g(P, eMg, eIg, eDg, 4 * qs + u, xr[i], yj));
+                        mxr[i] = fmaxf(mxr[i], b * qe.at(i, u, yj));
                     }
                     bv[i][u] = b;
                 }
@@ -667,7 +714,7 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
                 float wv[4];
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
-                    wv[u] = valid[i] ? bv[i][u] * emit_g(P, eMg, eIg, eDg, 4 * qs + u, xr[i], yj) : 0.f;
+                    wv[u] = valid[i] ? bv[i][u] * qe.at(i, u, yj) : 0.f;
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     A[(sa * KS + 4 * qs + u) * RW + r] = wv[u];
@@ -706,7 +753,7 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
 // Persistent CTAs over interleaved forward and backward stripe items (E-step),
 // or forward items only.
 template <bool FWD_ONLY>
-__global__ void __launch_bounds__(512) wide_nest_kernel(const KParams P) {
+__global__ void __launch_bounds__(384) wide_nest_kernel(const KParams P) {   // 32 x 12 warps at most (48 quads)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
     float *sm = reinterpret_cast<float *>(smem_raw);

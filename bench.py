@@ -712,7 +712,8 @@ def main():
            4: (('warp2::forward_warp_kernel', 2), ('warp2::backward_rec_warp_kernel', 2),
                ('warp2::count_warp_kernel', 2)),
            5: (('blk::fwdbwd_block_kernel', 4), (None, 0), ('blk::count_block_kernel', 2)),
-           6: ((('wide::forward_wide_kernel', 2) if fwd_only else ('wide::fwdbwd_wide_kernel', 4)), (None, 0),
+           6: ((('wide::wide_nest_kernel', 2 if fwd_only else 4) if nest is not None else
+                (('wide::forward_wide_kernel', 2) if fwd_only else ('wide::fwdbwd_wide_kernel', 4))), (None, 0),
                ('wide::count_wide_kernel', 2)),
            7: (('warp2::stripe_tw_kernel<...,0>', 2), ('warp2::stripe_tw_kernel<...,1>', 2),
                ('warp2::count_tw_kernel', 2))}[plan.last_variant]
@@ -734,9 +735,11 @@ def main():
                                'the DP is a dense FP32 CUDA-core contraction: no tensor-core or HBM bound',
                 'flop_per_cell': fpc * N * N,
                 'flop_accounting': ('dense 2N^2 per cell per pass; with the factored MixDom transitions '
-                                    '(config.transitions) this is effective FLOP: the two-warp recursions '
-                                    'execute 5 (5KF) + 11 K F^2 (forward) and 4 (5KF) + 11 K F^2 (backward) '
-                                    'multiply-adds per cell, 108 and 93 at K=3 F=1 against 240' if nest is not None
+                                    '(config.transitions) this is effective FLOP: the factored recursions '
+                                    'execute about 5 (5KF) + 11 K F^2 (forward) and 4 (5KF) + 11 K F^2 '
+                                    '(backward) multiply-adds per cell (two-warp, K=3 F=1: 108 and 93 against '
+                                    '240; wide, K=8 F=4: about 3 (5KF) + 11 K F^2 = 1,888 against 26,880)'
+                                    if nest is not None
                                     else 'dense 2N^2 per cell per pass'),
                 'fwd_kernel_ms': fwd_avg, 'bwd_kernel_ms': bwd_avg, 'count_kernel_ms': cnt_avg,
                 'count_overlaps_wavefronts': overlapped,

@@ -39,3 +39,15 @@ def test_record_rebuilds_oracle_chi(K, F, C, mixdom1_ext):
         sub = np.repeat(np.array([0, 0, 0, 1, 2]), F)
         assert np.all(intra[:, sub[:, None] != sub[None, :]] == 0.0)
         assert np.all(rec[i] >= 0.0)
+
+
+def test_library_reports_the_factored_layouts():
+    """phmm_nest_supported (a host query, no GPU): the 17-state two-warp layout
+    and the wide kernels' F = 4 layouts with 4..8 domains."""
+    from pairhmm import _lib
+    lib = _lib.load()
+    assert lib.phmm_nest_supported(3, 1) == 1
+    for K in range(4, 9):
+        assert lib.phmm_nest_supported(K, 4) == 1
+    for K, F in [(1, 1), (2, 1), (4, 1), (2, 2), (4, 2), (3, 4), (9, 4), (8, 2)]:
+        assert lib.phmm_nest_supported(K, F) == 0, (K, F)

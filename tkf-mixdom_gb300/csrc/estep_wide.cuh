@@ -782,6 +782,7 @@ constexpr int CTPT = 2;          // outer-product tiles per thread (ceil(NQ/2) *
 
 struct SmemWc {
     int fst, ust, tM, tI, tD;   // float offsets
+    int sg;                     // int offset: emission group of each destination slot [KS]
     int bytes;
 };
 
@@ -794,6 +795,7 @@ __host__ __device__ inline SmemWc make_smem_wc(int NS, int KS, int wM, int wI, i
     L.tM = o; o += (wM * 441 + 3) & ~3;
     L.tI = o; o += (wI * 21 + 3) & ~3;
     L.tD = o; o += (wD * 21 + 3) & ~3;
+    L.sg = o; o += (KS + 3) & ~3;
     L.bytes = o * 4;
     return L;
 }
@@ -859,6 +861,18 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
         for (int u = 0; u < 16; ++u) { csum[a][u] = 0.f; ccomp[a][u] = 0.f; }
     constexpr int KQ = 3;   // destination quads per phase-A thread: ceil(NQd / 16) <= KQ
     constexpr int FQ = 2;   // source quads per phase-A thread: ceil(SQ / 16) <= FQ
+    // per item, my destination quads' types and emission-table offsets (the
+    // successor's characters: x of row + 1 for M and D, y of column + 1 for M
+    // and I), so no step indexes the parameter block with a per-thread index
+    int qtr[KQ];
+#pragma unroll
+    for (int a = 0; a < KQ; ++a) {
+        const int q = sub + 16 * a;
+        qtr[a] = q < NQd ? P.quad_type[q] : T_NONE;
+    }
+    int *sg = reinterpret_cast<int *>(sm) + L.sg;   // slot groups, read from shared memory per lookup
+    for (int k = tid; k < KS; k += CT) sg[k] = P.slot_group[k];
+    __syncthreads();
     // prefetched lattice data of one step
     int Ef = EXP_NONE, Eb = EXP_NONE;
     int Es[KQ];
@@ -890,7 +904,7 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
             const int q = sub + 16 * a;
             if (q >= NQd) continue;
             if (emis) bo[a] = __ldcg(reinterpret_cast<const float4 *>(P.blat + cell * ES) + q);
-            const int qt = P.quad_type[q];
+            const int qt = qtr[a];
             const float *rec = nullptr;
             if (qt == T_I && hI) rec = P.blat + (latc + (int64_t)(t + 1) * RW + c) * ES;
             else if (qt == T_D && hD && below_ok)
@@ -930,15 +944,19 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
                 const int q = sub + 16 * a;
                 if (q >= NQd) continue;
                 float4 uu = make_float4(0.f, 0.f, 0.f, 0.f);
-                const int qt = P.quad_type[q];
+                const int qt = qtr[a];
                 if (live && Es[a] > EXP_NONE && !term) {
                     int du = Es[a] + Ef - Ep;
                     if (du > 126) { du = 126; atomicOr(P.status + p, PHMM_ST_SCALE_CLAMP); }
                     const float us = fminf(warp2::scale_pow2(rfrac, max(du, -200)), 3e38f);
-                    const int xi = qt == T_I ? xc : xn, yy = qt == T_D ? yj : yn;
+                    // I: x of my row, y of column + 1; D: x of row + 1; M: both of the successor
+                    // the successor's characters: M (x of row + 1, y of column + 1), I (y), D (x)
+                    const float *et = qt == T_M ? eMg : (qt == T_I ? eIg : eDg);
+                    const int add = qt == T_M ? xn * 21 + yn : (qt == T_I ? yn : xn);
+                    const int gm = qt == T_M ? 441 : 21;
                     float e[4];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) e[u] = sw[a] ? 1.f : emit_g(P, eMg, eIg, eDg, 4 * q + u, xi, yy);
+                    for (int u = 0; u < 4; ++u) e[u] = sw[a] ? 1.f : __ldg(et + sg[4 * q + u] * gm + add);
                     uu = make_float4(sv[a].x * e[0] * us, sv[a].y * e[1] * us, sv[a].z * e[2] * us, sv[a].w * e[3] * us);
                 }
                 *reinterpret_cast<float4 *>(ust + c * UW + 4 * q) = uu;
@@ -952,7 +970,7 @@ __device__ void count_stripe_wd(const KParams &P, int p, int si, int sp, const S
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         const int s = 4 * q + u;
-                        const int st = P.slot_type[s];
+                        const int st = qt;
                         if (pk[u] == 0.f) continue;
                         if (st == T_M) atomicAdd(tM + (s - mb) * 441 + xc * 21 + yj, pk[u]);
                         else if (st == T_I) atomicAdd(tI + (s - ib) * 21 + yj, pk[u]);

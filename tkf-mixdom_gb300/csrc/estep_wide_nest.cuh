@@ -236,38 +236,64 @@ __device__ void fwd_stripe_wn(const KParams &P, int p, int si, const SmemWn &L, 
     const float *iaq = sm + L.ia + (active ? qd : 0) * NIA;
     // halo column col of row i0-1: B slot (col - 1) % 3 index 0, E / MX slot
     // (col - 1) & 3, and its type sums in G slot (col - 1) & 3 index 0 (warp 0)
-    auto fetch_halo = [&](int col) -> bool {
+    // The halo column is loaded into registers one step before it is staged
+    // (its L2 latency then overlaps a whole step instead of holding warp 0
+    // -- and with it the step's barrier -- at the end of each step).
+    constexpr int HQ = (WMAXS + 31) / 32;
+    float hv[HQ];
+    int hE = EXP_NONE, hMX = 0;
+    auto load_halo = [&](int col) -> bool {   // warp 0
         if (!has_above || col > Ly) return true;
         int ok = 1;
         if (lane == 0) ok = wait_geq(prog_above, col + 1, P.spin_limit) ? 1 : 0;
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (!ok) return false;
-        const int bs = (col + 2) % 3, es = (col + 3) & 3;
         const float *src = edge_above + (int64_t)col * ES;
+#pragma unroll
+        for (int j = 0; j < HQ; ++j) {
+            const int s2 = lane + 32 * j;
+            hv[j] = s2 < NS ? __ldcg(src + s2) : 0.f;
+        }
+        if (lane == 0) {
+            hE = __ldcg(reinterpret_cast<const int *>(src) + NS);
+            hMX = __ldcg(reinterpret_cast<const int *>(src) + NS + 1);
+        }
+        return true;
+    };
+    auto stage_halo = [&](int col) {   // warp 0: the loaded column into B, E / MX and its type sums
+        if (!has_above || col > Ly) return;
+        const int bs = (col + 2) % 3, es = (col + 3) & 3;
         float g[3] = {0.f, 0.f, 0.f};
-        for (int s = lane; s < NS; s += 32) {
-            const float v = __ldcg(src + s);
-            B[(bs * NS + s) * BW] = v;
-            const int u = usl[s];
-            const float c = sm[L.ex + s] * v;
-            g[0] += u == 0 ? c : 0.f;
-            g[1] += u == 1 ? c : 0.f;
-            g[2] += u == 2 ? c : 0.f;
+#pragma unroll
+        for (int j = 0; j < HQ; ++j) {
+            const int s2 = lane + 32 * j;
+            if (s2 < NS) {
+                B[(bs * NS + s2) * BW] = hv[j];
+                const int u = usl[s2];
+                const float c = sm[L.ex + s2] * hv[j];
+                g[0] += u == 0 ? c : 0.f;
+                g[1] += u == 1 ? c : 0.f;
+                g[2] += u == 2 ? c : 0.f;
+            }
         }
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) g[a] += __shfl_xor_sync(0xffffffffu, g[a], o);
         if (lane == 0) {
-            E[es * BW] = __ldcg(reinterpret_cast<const int *>(src) + NS);
-            MX[es * BW] = __ldcg(reinterpret_cast<const int *>(src) + NS + 1);
+            E[es * BW] = hE;
+            MX[es * BW] = hMX;
 #pragma unroll
             for (int a = 0; a < 3; ++a) GB[es * GS + a * BW] = g[a];
         }
-        return true;
     };
     __syncthreads();
-    if (warp == 0 && !fetch_halo(0)) misc[0] = 1;
+    if (warp == 0) {
+        bool ok = load_halo(0);
+        if (ok) stage_halo(0);
+        if (ok) ok = load_halo(1);
+        if (!ok && lane == 0) misc[0] = 1;
+    }
     int llE = EXP_NONE;
     bool aborted = false;
     int k = 0;
@@ -431,7 +457,10 @@ __device__ void fwd_stripe_wn(const KParams &P, int p, int si, const SmemWn &L, 
                 atomicMax(MX + 0 * BW + 1, __float_as_int(1.f));
             }
         }
-        if (warp == 0 && t + 1 <= T_last && !fetch_halo(t + 1)) misc[(k + 1) & 1] = 1;
+        if (warp == 0 && t + 1 <= T_last) {   // column t+1 (loaded last step) staged; t+2 loaded
+            stage_halo(t + 1);
+            if (t + 2 <= T_last && !load_halo(t + 2) && lane == 0) misc[(k + 1) & 1] = 1;
+        }
     }
     __syncthreads();
     if (!aborted && has_below) {
@@ -557,28 +586,49 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
     for (int j = 0; j < 3; ++j) tqr[j] = pqr[j] >= 0 ? P.quad_type[pqr[j]] : T_NONE;
     // halo: row i0+RW at column c: B slot (c + RW) % 3 index RW + 3, E / MX slot
     // (c + RW) & 3 index RW, its nine P sums in P slot (c + RW) & 3 index RW + 3
-    auto fetch_halo = [&](int col) -> bool {
+    constexpr int HQ = (WMAXS + 31) / 32;
+    float hv[HQ];
+    int hE = EXP_NONE, hMX = 0;
+    auto load_halo = [&](int col) -> bool {   // warp 0 (loaded a step before staged, as in the forward)
         if (!has_below || col < 0 || col > Ly) return true;
         int ok = 1;
         if (lane == 0) ok = wait_geq(prog_below, Ly + 1 - col, P.spin_limit) ? 1 : 0;
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (!ok) return false;
-        const int bs = (col + RW) % 3, es = (col + RW) & 3;
         const float *src = edge_below + (int64_t)col * ES;
+#pragma unroll
+        for (int jj = 0; jj < HQ; ++jj) {
+            const int kk = lane + 32 * jj;
+            hv[jj] = kk < KS ? __ldcg(src + kk) : 0.f;
+        }
+        if (lane == 0) {
+            hE = __ldcg(reinterpret_cast<const int *>(src) + NS);
+            hMX = __ldcg(reinterpret_cast<const int *>(src) + NS + 1);
+        }
+        return true;
+    };
+    auto stage_halo = [&](int col) {
+        if (!has_below || col < 0 || col > Ly) return;
+        const int bs = (col + RW) % 3, es = (col + RW) & 3;
         float pv[9];
 #pragma unroll
         for (int v = 0; v < 9; ++v) pv[v] = 0.f;
-        for (int kk = lane; kk < KS; kk += 32) {
-            const float w = __ldcg(src + kk);
-            B[(bs * KS + kk) * BW + RW + 3] = w;
-            const int qk = kk >> 2, qi = P.kbeg[1] / 4, qd0 = P.kbeg[2] / 4;
-            const int tk = qk < qi ? 0 : (qk < qd0 ? 1 : 2);
+        const int qi = P.kbeg[1] / 4, qd0 = P.kbeg[2] / 4;
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                const float c = sm[L.cin + a * KS + kk] * w;
-                pv[0 + a] += tk == 0 ? c : 0.f;
-                pv[3 + a] += tk == 1 ? c : 0.f;
-                pv[6 + a] += tk == 2 ? c : 0.f;
+        for (int jj = 0; jj < HQ; ++jj) {
+            const int kk = lane + 32 * jj;
+            if (kk < KS) {
+                const float w = hv[jj];
+                B[(bs * KS + kk) * BW + RW + 3] = w;
+                const int qk = kk >> 2;
+                const int tk = qk < qi ? 0 : (qk < qd0 ? 1 : 2);
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const float c = sm[L.cin + a * KS + kk] * w;
+                    pv[0 + a] += tk == 0 ? c : 0.f;
+                    pv[3 + a] += tk == 1 ? c : 0.f;
+                    pv[6 + a] += tk == 2 ? c : 0.f;
+                }
             }
         }
 #pragma unroll
@@ -586,12 +636,11 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) pv[v] += __shfl_xor_sync(0xffffffffu, pv[v], o);
         if (lane == 0) {
-            E[es * BW + RW] = __ldcg(reinterpret_cast<const int *>(src) + NS);
-            MX[es * BW + RW] = __ldcg(reinterpret_cast<const int *>(src) + NS + 1);
+            E[es * BW + RW] = hE;
+            MX[es * BW + RW] = hMX;
 #pragma unroll
             for (int v = 0; v < 9; ++v) PR[es * PS + v * BW + RW + 3] = pv[v];
         }
-        return true;
     };
     auto publish_top = [&](int t) {
         if (!has_above || t < 0 || t > Ly) return;
@@ -608,7 +657,12 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
         }
     };
     __syncthreads();
-    if (warp == 0 && !fetch_halo(T_last - (RW - 1))) misc[0] = 1;
+    if (warp == 0) {
+        bool ok = load_halo(T_last - (RW - 1));
+        if (ok) stage_halo(T_last - (RW - 1));
+        if (ok) ok = load_halo(T_last - RW);
+        if (!ok && lane == 0) misc[0] = 1;
+    }
     bool aborted = false;
     int k = 0;
     for (int t = T_last; t >= 0; --t, ++k) {
@@ -736,7 +790,10 @@ __device__ void bwd_rec_stripe_wn(const KParams &P, int p, int si, const SmemWn 
                 }
             }
         }
-        if (warp == 0 && !fetch_halo(t - RW)) misc[(k + 1) & 1] = 1;
+        if (warp == 0) {   // column t - RW (loaded last step) staged; the next one loaded
+            stage_halo(t - RW);
+            if (!load_halo(t - RW - 1) && lane == 0) misc[(k + 1) & 1] = 1;
+        }
     }
     __syncthreads();
     if (!aborted && warp == (nt > 32 ? 1 : 0)) publish_top(0);

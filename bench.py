@@ -705,6 +705,9 @@ def main():
     peaks, src = measured_peaks()
     fwd_avg, bwd_avg, cnt_avg = float(np.mean(fwd_ms)), float(np.mean(bwd_ms)), float(np.mean(cnt_ms))
     total_cells = float(cells.sum())
+    # the kernels contract through the factored record only for the layouts the library has
+    nest_used = (nest is not None and bool(_lib.load().phmm_nest_supported(*nest_kf))
+                 and plan.last_variant in (6, 7))
     # (kernel name, algorithmic FLOP per cell) of forward, backward, count pass
     fam = {1: (('forward_kernel', 2), ('backward_kernel', 4), (None, 0)),
            2: (('warp2::forward_warp_kernel', 2), ('warp2::backward_warp_kernel', 4), (None, 0)),
@@ -712,7 +715,7 @@ def main():
            4: (('warp2::forward_warp_kernel', 2), ('warp2::backward_rec_warp_kernel', 2),
                ('warp2::count_warp_kernel', 2)),
            5: (('blk::fwdbwd_block_kernel', 4), (None, 0), ('blk::count_block_kernel', 2)),
-           6: ((('wide::wide_nest_kernel', 2 if fwd_only else 4) if nest is not None else
+           6: ((('wide::wide_nest_kernel', 2 if fwd_only else 4) if nest_used else
                 (('wide::forward_wide_kernel', 2) if fwd_only else ('wide::fwdbwd_wide_kernel', 4))), (None, 0),
                ('wide::count_wide_kernel', 2)),
            7: (('warp2::stripe_tw_kernel<...,0>', 2), ('warp2::stripe_tw_kernel<...,1>', 2),
@@ -739,7 +742,7 @@ def main():
                                     'execute about 5 (5KF) + 11 K F^2 (forward) and 4 (5KF) + 11 K F^2 '
                                     '(backward) multiply-adds per cell (two-warp, K=3 F=1: 108 and 93 against '
                                     '240; wide, K=8 F=4: about 3 (5KF) + 11 K F^2 = 1,888 against 26,880)'
-                                    if nest is not None
+                                    if nest_used
                                     else 'dense 2N^2 per cell per pass'),
                 'fwd_kernel_ms': fwd_avg, 'bwd_kernel_ms': bwd_avg, 'count_kernel_ms': cnt_avg,
                 'count_overlaps_wavefronts': overlapped,
@@ -780,7 +783,7 @@ def main():
                                        'LPT-sharded by E-step cost' if ws > 1 else 'replicas x1'),
                        'tuning': tuning,
                        'wide_contraction': '3xTF32 tensor cores' if args.tensor else 'float32 CUDA cores',
-                       'transitions': ('factored MixDom chi (phmm_batch.nest)' if nest is not None
+                       'transitions': ('factored MixDom chi (phmm_batch.nest)' if nest_used
                                        else 'dense chi'),
                        'status_nonzero': int((status != 0).sum())},
             'roofline': roofline, 'roofline_hbm': roofline_hbm, 'cpu_baseline': cpu, 'accuracy': acc,

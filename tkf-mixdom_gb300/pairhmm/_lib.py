@@ -398,31 +398,72 @@ def to_host(tensors):
         return {k: (v.numpy() if isinstance(v, torch.Tensor) else v) for k, v in tensors.items()}
     stream = torch.cuda.current_stream(dev)
     stor = items[0][1].untyped_storage()
-    shared = all(v.device == dev and v.is_contiguous() and v.untyped_storage().data_ptr() == stor.data_ptr()
+    base, nb = stor.data_ptr(), stor.nbytes()
+    # one device buffer holds them all (an output arena): its bytes come back in
+    # one copy and the arrays are numpy views of the pinned block
+    shared = all(v.device == dev and v.dtype in _NP_DTYPE and v.is_contiguous()
+                 and base <= v.data_ptr() and v.data_ptr() + v.numel() * v.element_size() <= base + nb
                  for _, v in items)
     views = {}
     if shared:
-        nb = stor.nbytes()
         host = torch.empty(nb, dtype=torch.uint8, pin_memory=True)
         src = torch.empty(0, dtype=torch.uint8, device=dev).set_(stor, 0, (nb,))
         host.copy_(src, non_blocking=True)
+        hn = host.numpy()
         for k, v in items:
-            o = v.storage_offset() * v.element_size()
-            views[k] = host[o:o + v.numel() * v.element_size()].view(v.dtype).view(v.shape)
-    else:
-        sizes = [(v.numel() * v.element_size() + 255) // 256 * 256 for _, v in items]
-        host = torch.empty(max(sum(sizes), 1), dtype=torch.uint8, pin_memory=True)
-        o = 0
-        for (k, v), n in zip(items, sizes):
-            hv = host[o:o + v.numel() * v.element_size()].view(v.dtype).view(v.shape)
-            hv.copy_(v if v.is_contiguous() else v.contiguous(), non_blocking=True)
-            views[k] = hv
-            o += n
+            o = v.data_ptr() - base
+            views[k] = hn[o:o + v.numel() * v.element_size()].view(_NP_DTYPE[v.dtype]).reshape(v.shape)
+        stream.synchronize()
+        out = dict(tensors)
+        out.update(views)
+        return out
+    sizes = [(v.numel() * v.element_size() + 255) // 256 * 256 for _, v in items]
+    host = torch.empty(max(sum(sizes), 1), dtype=torch.uint8, pin_memory=True)
+    o = 0
+    for (k, v), n in zip(items, sizes):
+        hv = host[o:o + v.numel() * v.element_size()].view(v.dtype).view(v.shape)
+        hv.copy_(v if v.is_contiguous() else v.contiguous(), non_blocking=True)
+        views[k] = hv
+        o += n
     stream.synchronize()
     out = {k: v.numpy() for k, v in views.items()}
     for k, v in tensors.items():
         if k not in out:
             out[k] = v
+    return out
+
+
+_ESIZE = {torch.float64: 8, torch.float32: 4, torch.int64: 8, torch.int32: 4, torch.uint8: 1}
+_NP_DTYPE = {torch.float64: np.float64, torch.float32: np.float32, torch.int64: np.int64, torch.int32: np.int32,
+             torch.uint8: np.uint8}
+
+
+def arena_layout(specs):
+    """Layout of an output arena: specs is a list of (name, shape, dtype), each
+    slice 256-byte aligned.  Returns ([(name, dtype, shape, strides, element
+    offset)], bytes)."""
+    lay, o = [], 0
+    for name, shape, dt in specs:
+        shape = tuple(int(s) for s in shape)
+        esz = _ESIZE[dt]
+        st, n = [], 1
+        for s in reversed(shape):
+            st.append(n)
+            n *= s
+        lay.append((name, dt, shape, tuple(reversed(st)), o // esz))
+        o += (n * esz + 255) // 256 * 256
+    return lay, max(o, 256)
+
+
+def arena_views(buf, layout):
+    """The named tensors of an arena layout over the uint8 buffer buf (one
+    strided view each: a call returning many outputs pays one view per output)."""
+    typed, out = {}, {}
+    for name, dt, shape, st, off in layout:
+        v = typed.get(dt)
+        if v is None:
+            v = typed[dt] = buf.view(dt)
+        out[name] = v.as_strided(shape, st, off)
     return out
 
 
@@ -432,17 +473,9 @@ class OutputArena:
 
     def __init__(self, device, specs):
         # specs: list of (name, shape, dtype); each slice 256-byte aligned
-        sizes = []
-        for _, shape, dt in specs:
-            n = int(np.prod(shape)) * torch.empty(0, dtype=dt).element_size()
-            sizes.append((n + 255) // 256 * 256)
-        self.buf = torch.empty(max(sum(sizes), 256), dtype=torch.uint8, device=device)
-        self.t, o = {}, 0
-        for (name, shape, dt), n in zip(specs, sizes):
-            cnt = int(np.prod(shape))
-            esz = torch.empty(0, dtype=dt).element_size()
-            self.t[name] = self.buf[o:o + cnt * esz].view(dt).view(*shape)
-            o += n
+        self.layout, nb = arena_layout(specs)
+        self.buf = torch.empty(nb, dtype=torch.uint8, device=device)
+        self.t = arena_views(self.buf, self.layout)
 
     def __getitem__(self, name):
         return self.t[name]

@@ -768,7 +768,7 @@ def main():
         if not args.no_accuracy:
             try:
                 acc = accuracy_of_workload(args, w, plan, out, chi, EM, EI, ED, fwd_only, dev)
-            except Exception as e:   # never lose the bench line to the checker
+            except Exception as e:   # never lose the bench line to the oracle leg
                 acc = {'error': repr(e)}
         line = {
             'metric': spec['metric'], 'value': value,

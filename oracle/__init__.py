@@ -1,8 +1,8 @@
 """CPU FP64 oracle for the 2D pair-HMM hot path -- TEST INFRASTRUCTURE ONLY.
 
 A NumPy float64 restatement of the reference's (evoldoers/tkf-mixdom)
-pair-HMM forward/backward, E-step and emission-count code.  It is the checker
-for the CUDA path: only ``tests/``, ``__graft_entry__.smoke()`` and the
+pair-HMM forward/backward, E-step and emission-count code, against which the
+CUDA path is compared: only ``tests/``, ``__graft_entry__.smoke()`` and the
 ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it.
 The product package never does, and the product fails loudly when its CUDA
 library is missing instead of falling back to this code.

@@ -2,8 +2,8 @@
 
 Log-space NumPy float64 restatement of the reference's 2D DP
 (``python/tkfmixdom/jax/dp/hmm.py``).  Used only by tests, ``smoke()`` and
-the CPU-baseline leg of ``bench.py`` as the checker; the product never
-imports it.
+the CPU-baseline leg of ``bench.py``, as the FP64 comparison for the CUDA
+path; the product never imports it.
 
 The recursion is evaluated one anti-diagonal at a time, vectorised over the
 cells of the diagonal, exactly as ``_forward_2d_core_diag``

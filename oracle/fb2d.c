@@ -1,6 +1,6 @@
 /* FP64 oracle in C: 2D pair-HMM forward-backward (TEST INFRASTRUCTURE ONLY).
  *
- * The checker's fast twin of oracle/dp.py, used by the test-suite (against
+ * The oracle's fast twin of oracle/dp.py, used by the test-suite (against
  * the NumPy oracle) and by bench.py's CPU legs; the product never links it.
  * It restates the same log-space recursions of the reference
  * (python/tkfmixdom/jax/dp/hmm.py):

@@ -6,7 +6,7 @@ oracle (oracle/fb2d.c through oracle/pool.py, all host cores).
   through the public batched call estep_batch_mixdom2;
 * MixDom2 n_dom=4 n_frag=2 n_classes=2 (42 states): one pair of about
   1450 x 1450 (the long end of LogUniform(200, 1500)), E-step outputs and the
-  gradient of mixdom2_log_prob; the gradient's checker is the score identity
+  gradient of mixdom2_log_prob; the gradient's reference is the score identity
   evaluated on the ORACLE's counts, differentiated by central differences of
   the oracle's own builders (oracle/models.py), so nothing of the product is
   on the checking side;

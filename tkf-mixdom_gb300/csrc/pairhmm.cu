@@ -2291,7 +2291,7 @@ int phmm_plan_create(const phmm_model_desc *md, phmm_plan **out) {
         while (slot_orig.size() % 4) { slot_orig.push_back(-1); slot_type.push_back(T_NONE); }
     }
     const int NS = (int)slot_orig.size();
-    if (NS > MAXS) return fail(PHMM_E_ARG, "too many emitting states for this build (max 164)");
+    if (NS > MAXS) return fail(PHMM_E_ARG, "too many emitting states for the generic kernels (max 164)");
     K.N = N;
     K.NS = NS;
     K.NQ = NS / 4;

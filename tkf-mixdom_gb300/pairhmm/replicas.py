@@ -3,7 +3,7 @@
 Pairs are independent (the reference vmaps over them with shared
 parameters, train/tkf92_svi_bw.py:214-217), so a multi-GPU E-step is one
 batch per rank and a host-side reduction afterwards, as the reference's own
-driver sums per-pair results on the host (train_pfam.py:2858-2876):
+training script sums per-pair results on the host (train_pfam.py:2858-2876):
 
 * ``lpt_partition`` splits pairs over ranks by longest-processing-time bin
   packing of the E-step cost (Lx+1)(Ly+1)N^2 (the per-rank step time is the
